@@ -1,0 +1,147 @@
+/* yune_cuda.h -- C-ABI of the GB300 path-tracing core (libyune_gb300.so).
+ *
+ * This replaces Yune's OpenCL dispatch: CLManager (include/CLManager.h:43-170) and the
+ * OpenCL calls of RendererCore::setup / enqueueKernels / updateRenderKernelArgs /
+ * updatePostProcessingKernelArgs (src/RendererCore.cpp:155-606). The caller keeps its
+ * own Scene, BVH and Camera and hands over the same buffers it used to upload with
+ * clCreateBuffer(COPY_HOST_PTR): TriangleGPU, Material and BVHNodeGPU arrays, the Cam
+ * block, plus the per-pass arguments of the `pathtracer` kernel (GI_CHECK, reset, rand;
+ * kernels/legacy/udpt.cl:158-160).
+ *
+ * Conventions: every function returns 0 (YC_OK) or a negative YC_E* code and never
+ * throws; yc_last_error() gives the message of the most recent failure on the calling
+ * thread. A context owns one CUDA stream and every device buffer it allocates; it is
+ * not thread-safe (one host thread per context, as RendererCore drives CLManager from
+ * the GUI thread). Pointers named *_host are host memory; the core copies them.
+ */
+#ifndef YUNE_CUDA_H
+#define YUNE_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "yune_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error codes, mirroring the classes CLManager::checkError maps cl_int codes to
+ * (src/CLManager.cpp:755-855). */
+enum {
+  YC_OK = 0,
+  YC_E_INVALID = -1,        /* bad argument (CL_INVALID_VALUE and friends) */
+  YC_E_NOMEM = -2,          /* device or host allocation failed (CL_OUT_OF_*_MEMORY) */
+  YC_E_LAUNCH = -3,         /* kernel launch or CUDA runtime failure */
+  YC_E_TIMEOUT = -4,        /* a bounded device wait gave up */
+  YC_E_NODEVICE = -5,       /* no CUDA device */
+  YC_E_OVERFLOW = -6,       /* a device bound (traversal stack, queue) was exceeded */
+  YC_E_BUDGET = -7,         /* admission refused: the request exceeds the HBM budget */
+  YC_E_NOTFOUND = -8        /* unknown scene / accumulator / job id */
+};
+
+/* integrators */
+enum { YC_UDPT = 0, YC_BDPT = 1 };
+/* diffuse BRDF: Lambert (udpt.cl:621-622) or the Oren-Nayar rule of
+ * kernels/legacy/udpt-primitives.cl:673-686 */
+enum { YC_BRDF_LAMBERT = 0, YC_BRDF_OREN_NAYAR = 1 };
+
+/* Per-pass options. The reference fixes these with #defines in the kernel text
+ * (udpt.cl:3-9, bdpt.cl:1-8) or with kernel arguments (udpt.cl:158-160). */
+typedef struct yc_pass_cfg {
+  int32_t integrator;      /* YC_UDPT or YC_BDPT */
+  int32_t mis;             /* 1 = the MIS branch of evaluateDirectLighting (udpt.cl:570-608) */
+  int32_t rr_threshold;    /* RR_THRESHOLD: roulette when bounce index > this (6 in udpt.cl) */
+  int32_t max_depth;       /* bound of the GI loop (100000 in udpt.cl:463) */
+  int32_t brdf_model;      /* YC_BRDF_* */
+  int32_t mis_lobe_fix;    /* 0 = reference behaviour; 1 = draw the lobe when the shadow
+                              ray is blocked, so a MIS BRDF hit never divides by zero */
+  int32_t bdpt_bounces;    /* BDPT_BOUNCES (20 in bdpt.cl:7) */
+  int32_t block, block_x, block_y;   /* image tile of this launch (udpt.cl:166-167);
+                                        block_x = block_y = 1 renders the whole frame */
+} yc_pass_cfg;
+
+/* Ray counters since the last yc_reset_stats: every traceRay-equivalent query of the
+ * reference algorithm (primary, extension, NEE shadow, MIS BRDF, BDPT connection), and
+ * how many of them needed a BVH traversal (a MIS ray whose closest light is not the
+ * sampled one is settled analytically, as its outcome does not depend on the BVH). */
+typedef struct yc_stats {
+  uint64_t rays;            /* all queries */
+  uint64_t primary, extension, shadow, mis, connection;
+  uint64_t traversed;       /* queries that walked the BVH */
+  uint64_t samples;         /* pixel paths completed */
+  uint64_t stack_overflow;  /* traversals that hit the stack bound (must be 0) */
+} yc_stats;
+
+typedef struct yc_ctx yc_ctx;
+
+/* ---- context (CLManager::setup, src/CLManager.cpp:118-156) ---- */
+int yc_create(int device, yc_ctx** out);
+int yc_destroy(yc_ctx* ctx);
+const char* yc_last_error(void);
+int yc_synchronize(yc_ctx* ctx);
+
+/* ---- scene buffers (CLManager::setupVertexBuffer / setupMatBuffer / setupBVHBuffer,
+ *      src/CLManager.cpp:420-484) ---- */
+/* Copies and repacks one scene: triangles into a 48-byte (v1, e1, e2) stream in leaf
+ * order, the BVH into 64-byte two-child nodes, normals into per-triangle shading
+ * records. n_node = 0 means brute force over all triangles (traceRay, udpt.cl:280-284).
+ * lights: the quad lights of the scene (1..16). */
+int yc_upload_scene(yc_ctx* ctx, const yc_triangle* tris_host, int n_tri, const yc_material* mats_host,
+                    int n_mat, const yc_bvh_node* nodes_host, int n_node, const yc_quad_light* lights_host,
+                    int n_light, int* scene_id);
+int yc_set_lights(yc_ctx* ctx, int scene_id, const yc_quad_light* lights_host, int n_light);
+int yc_release_scene(yc_ctx* ctx, int scene_id);
+/* bytes the scene holds on the device */
+int yc_scene_bytes(yc_ctx* ctx, int scene_id, uint64_t* bytes);
+
+/* ---- camera (CLManager::setupCameraBuffer + the map/unmap of
+ *      RendererCore::updateRenderKernelArgs, src/RendererCore.cpp:532-555) ---- */
+int yc_set_camera(yc_ctx* ctx, const yc_cam* cam_host);
+
+/* ---- accumulators (the RGBA32F images of CLManager::setupImageBuffers,
+ *      src/CLManager.cpp:381-411; one device buffer, updated in place) ---- */
+int yc_alloc_accum(yc_ctx* ctx, int width, int height, int* accum_id);
+int yc_free_accum(yc_ctx* ctx, int accum_id);
+int yc_read_accum(yc_ctx* ctx, int accum_id, float* rgba_host);
+int yc_write_accum(yc_ctx* ctx, int accum_id, const float* rgba_host);
+/* device address of the accumulator (width*height float4) for zero-copy consumers */
+int yc_accum_device_ptr(yc_ctx* ctx, int accum_id, void** dptr);
+
+/* ---- one render pass: the `pathtracer` launch of RendererCore::enqueueKernels
+ *      (src/RendererCore.cpp:284-299), one sample per pixel of the tile, running mean
+ *      into the accumulator (udpt.cl:196-210). Asynchronous on the context stream. ---- */
+int yc_render_pass(yc_ctx* ctx, int scene_id, int accum_id, uint32_t rand_seed, int reset, int gi_check,
+                   const yc_pass_cfg* cfg);
+/* n_pass passes back to back (pass k uses rand_seeds[k]; reset applies to the first). */
+int yc_render_passes(yc_ctx* ctx, int scene_id, int accum_id, const uint32_t* rand_seeds_host, int n_pass,
+                     int reset_first, int gi_check, const yc_pass_cfg* cfg);
+
+/* ---- post pass: the `tonemap` launch (kernels/post-proc/tonemap.cl:14-35,
+ *      src/RendererCore.cpp:340-371). out_host receives width*height float4. ---- */
+int yc_tonemap(yc_ctx* ctx, int accum_id, float* rgba_out_host);
+
+/* ---- direct ray queries (traceRay of udpt.cl:240-286 on explicit rays) ----
+ * rays_host: n records of 9 floats (origin xyzw, dir xyzw, length). Closest query:
+ * tri_out = closest triangle (original index, -1 none), light_out = light hit (-1
+ * none), t_out = final ray length. Shadow query (any_hit = 1): tri_out = 1 if any
+ * triangle or light closes the segment, else 0; light_out and t_out may be NULL. */
+int yc_trace(yc_ctx* ctx, int scene_id, const float* rays_host, int n, int any_hit, int* tri_out,
+             int* light_out, float* t_out);
+/* Same query on device buffers: rays_dev as above, results written to device arrays.
+ * Asynchronous on the context stream. */
+int yc_trace_device(yc_ctx* ctx, int scene_id, const float* rays_dev, int n, int any_hit, int* tri_dev,
+                    float* t_dev);
+
+/* ---- statistics and tuning ---- */
+int yc_get_stats(yc_ctx* ctx, yc_stats* out);
+int yc_reset_stats(yc_ctx* ctx);
+/* Wall time of the device work of the last yc_render_pass(es) call, in ms (CUDA
+ * events on the context stream). */
+int yc_last_pass_ms(yc_ctx* ctx, float* ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* YUNE_CUDA_H */

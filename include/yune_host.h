@@ -1,0 +1,81 @@
+/* yune_host.h -- host-side producers of the buffers the CUDA core consumes.
+ *
+ * In Yune these buffers come from Scene/BVH/Camera, which stay on the caller's side
+ * of the boundary. This library restates those producers so that a headless caller
+ * (tests, the benchmark, a batch or serving front end) can build the same
+ * TriangleGPU / BVHNodeGPU / Cam arrays without the GUI application:
+ *   yh_bvh_build      <- BVH::createBVH          src/BVH.cpp:56-173 (node array
+ *                        identical to the reference builder's for the same input)
+ *   yh_triangle_aabb  <- TriangleCPU::computeAABB src/TriangleCPU.cpp:51-71
+ *   yh_camera_look    <- Camera::setViewMatrix + Camera::setBuffer
+ *                        src/Camera.cpp:66-82,105-117
+ *   yh_scene_*        procedural scenes (Cornell box, seeded boxes, subdivided and
+ *                     displaced icospheres, sphere grids) in place of OBJ files.
+ * Every function returns 0 on success and a negative YH_E* code on failure.
+ */
+#ifndef YUNE_HOST_H
+#define YUNE_HOST_H
+
+#include "yune_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  YH_OK = 0,
+  YH_E_INVALID = -1,      /* bad argument */
+  YH_E_NOMEM = -2,        /* host allocation failed */
+  YH_E_RANGE = -3         /* index or size out of range */
+};
+
+/* ---- BVH (src/BVH.cpp) ---- */
+typedef struct yh_bvh yh_bvh;
+/* Builds the breadth-first binned BVH of BVH::createBVH over tris[0..n_tri).
+ * bins: BVH::bins (20 by default; <= 2 selects median splits only).
+ * leaf_max: BVH::leaf_primitives (10 in the reference; 1..10).
+ * The root box is the union of the padded triangle boxes, as Scene::loadModel
+ * computes it (src/Scene.cpp:350-356). */
+int yh_bvh_build(const yc_triangle* tris, int n_tri, int bins, int leaf_max, yh_bvh** out);
+int yh_bvh_node_count(const yh_bvh* b);
+int yh_bvh_copy_nodes(const yh_bvh* b, yc_bvh_node* out, int capacity);
+/* Longest root-to-leaf path (edges); the traversal stack needs depth + 1 slots. */
+int yh_bvh_depth(const yh_bvh* b);
+void yh_bvh_free(yh_bvh* b);
+
+/* TriangleCPU::computeCentroid / computeAABB for one triangle. */
+int yh_triangle_aabb(const yc_triangle* t, yc_aabb* aabb, yc_float4* centroid);
+
+/* ---- camera (src/Camera.cpp) ---- */
+/* Writes the Cam rows of mat4(side, up, -look, eye) with y_fov in degrees. The
+ * vectors are normalised as Camera::setViewMatrix does. */
+int yh_camera_look(const float eye[3], const float side[3], const float up[3],
+                   const float look[3], float y_fov_deg, yc_cam* out);
+
+/* ---- procedural scenes ---- */
+typedef struct yh_scene yh_scene;
+int yh_scene_new(yh_scene** out);
+void yh_scene_free(yh_scene* s);
+/* Appends a material, returns its index in *mat_id. */
+int yh_scene_add_material(yh_scene* s, const yc_material* m, int* mat_id);
+/* Unit-cube Cornell box: 5 walls (10 triangles, x,y,z in [-0.5,0.5], open at +z),
+ * a quad light under the ceiling and two boxes with seeded yaw (24 triangles).
+ * Materials: walls Oren-Nayar sigma^2 = on_sigma2 (white, red, green), box 0 modified
+ * Phong with exponent phong_exp, box 1 Oren-Nayar white. light_emission sets the
+ * quad's ke. */
+int yh_scene_add_cornell(yh_scene* s, uint64_t seed, float on_sigma2, float phong_exp,
+                         float light_emission, int with_boxes);
+/* Icosphere subdivided `level` times (20*4^level triangles), radius r, centre c,
+ * each vertex moved radially by r*U(-disp, disp) from a seeded stream; vertex
+ * normals are the area-weighted face normals (the unit position when disp == 0). */
+int yh_scene_add_icosphere(yh_scene* s, const float c[3], float r, int level,
+                           float disp, uint64_t seed, int mat_id);
+int yh_scene_add_light(yh_scene* s, const yc_quad_light* l);
+int yh_scene_counts(const yh_scene* s, int* n_tri, int* n_mat, int* n_light);
+int yh_scene_copy(const yh_scene* s, yc_triangle* tris, yc_material* mats, yc_quad_light* lights);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* YUNE_HOST_H */

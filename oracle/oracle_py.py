@@ -1,0 +1,197 @@
+"""ctypes front end of the CPU oracle (liboracle.so) and of the compiled reference
+(_ref/libyune_ref.so).
+
+TEST INFRASTRUCTURE: used by tests, the smoke check and the benchmark's CPU-baseline
+leg only.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+vp = C.c_void_p
+i32 = C.c_int
+u32 = C.c_uint32
+
+
+class OrCfg(C.Structure):
+    _fields_ = [("mis", i32), ("rr_threshold", i32), ("max_depth", i32), ("brdf_model", i32),
+                ("mis_lobe_fix", i32), ("heap_size", i32), ("gi_check", i32)]
+
+
+class OrCounters(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("rays", "primary", "extension", "shadow", "mis", "heap_overflow")]
+
+
+_orc = None
+_ref = None
+_ref_tried = False
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def orc():
+    global _orc
+    if _orc is None:
+        path = build_oracle.build_oracle()
+        L = C.CDLL(path)
+        L.or_trace.argtypes = [vp, i32, vp, i32, vp, i32, vp, i32, i32, i32, vp, vp, vp, vp]
+        L.or_render.argtypes = [vp, i32, vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, u32, i32, C.POINTER(OrCfg), i32,
+                                i32, i32, C.POINTER(OrCounters)]
+        L.or_render_f64.argtypes = L.or_render.argtypes
+        L.or_tonemap.argtypes = [vp, i32, i32, vp]
+        L.or_ym_eval.argtypes = [i32, vp, vp, vp, i32]
+        L.or_wang_hash.argtypes = [u32]
+        L.or_wang_hash.restype = u32
+        L.or_xor_shift.argtypes = [u32]
+        L.or_xor_shift.restype = u32
+        L.or_brdf.argtypes = [vp, i32, vp, i32, i32, vp, vp, vp, vp, i32, C.c_float, i32, vp]
+        _orc = L
+    return _orc
+
+
+def ref():
+    """The compiled reference, or None when no reference text is available."""
+    global _ref, _ref_tried
+    if not _ref_tried:
+        _ref_tried = True
+        try:
+            path = build_oracle.build_ref()
+        except RuntimeError:
+            path = None
+        if path and os.path.exists(path):
+            L = C.CDLL(path)
+            L.ref_render.argtypes = [i32, vp, i32, vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, u32, i32, i32, i32, i32,
+                                     i32]
+            L.ref_trace.argtypes = [vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, vp, vp]
+            L.ref_tonemap.argtypes = [vp, i32, i32, vp]
+            L.ref_oren_nayar.argtypes = [vp, vp, vp, vp, vp, vp]
+            if hasattr(L, "ref_bvh_build"):
+                L.ref_bvh_build.argtypes = [vp, i32, i32, i32, vp, i32, C.POINTER(i32)]
+            _ref = L
+    return _ref
+
+
+def cfg_of(cfg, heap_size=1500):
+    c = OrCfg()
+    c.mis = int(cfg.get("mis", 0))
+    c.rr_threshold = int(cfg.get("rr_threshold", 6))
+    c.max_depth = int(cfg.get("max_depth", 100000))
+    c.brdf_model = int(cfg.get("brdf_model", 0))
+    c.mis_lobe_fix = int(cfg.get("mis_lobe_fix", 0))
+    c.heap_size = heap_size
+    c.gi_check = int(cfg.get("gi_check", 1))
+    return c
+
+
+def render(scene, accum, rand_seed, reset, cfg, threads=0, rows=None, f64=False, heap_size=1500):
+    """One oracle pass into accum (H x W x 4, float32 or float64 for f64)."""
+    L = orc()
+    H, W = accum.shape[:2]
+    cnt = OrCounters()
+    c = cfg_of(cfg, heap_size)
+    r0, r1 = rows if rows else (0, 0)
+    fn = L.or_render_f64 if f64 else L.or_render
+    rc = fn(_p(scene.tris), len(scene.tris), _p(scene.mats), len(scene.mats), _p(scene.nodes), len(scene.nodes),
+            _p(scene.lights), len(scene.lights), _p(scene.cam), W, H, _p(accum), int(rand_seed) & 0xFFFFFFFF, reset,
+            C.byref(c), threads, r0, r1, C.byref(cnt))
+    if rc != 0:
+        raise RuntimeError("or_render failed: %d" % rc)
+    return {k: getattr(cnt, k) for k, _ in OrCounters._fields_}
+
+
+def trace(scene, rays9, any_hit=False, heap_size=1500):
+    L = orc()
+    rays9 = np.ascontiguousarray(rays9, np.float32)
+    n = rays9.shape[0]
+    tri = np.zeros(n, np.int32)
+    light = np.zeros(n, np.int32)
+    t = np.zeros(n, np.float32)
+    ov = np.zeros(n, np.int32)
+    rc = L.or_trace(_p(scene.tris), len(scene.tris), _p(scene.nodes), len(scene.nodes), _p(scene.lights),
+                    len(scene.lights), _p(rays9), n, int(any_hit), heap_size, _p(tri), _p(light), _p(t), _p(ov))
+    if rc != 0:
+        raise RuntimeError("or_trace failed")
+    return tri, light, t, ov
+
+
+def tonemap(accum):
+    L = orc()
+    H, W = accum.shape[:2]
+    out = np.zeros((H, W, 4), np.float32)
+    a = np.ascontiguousarray(accum, np.float32)
+    L.or_tonemap(_p(a), W, H, _p(out))
+    return out
+
+
+# ---- the compiled reference ----
+VARIANT = {"udpt_a": 0, "udpt_mis": 1, "udpt_mis4": 2, "bdpt20": 10, "bdpt8": 11, "bdpt8_l4": 12}
+
+
+def ref_render(scene, accum, rand_seed, reset, variant, rr_threshold, max_depth, gi_check=1, threads=0):
+    L = ref()
+    H, W = accum.shape[:2]
+    rc = L.ref_render(VARIANT[variant], _p(scene.tris), len(scene.tris), _p(scene.mats), len(scene.mats),
+                      _p(scene.nodes), len(scene.nodes), _p(scene.lights), len(scene.lights), _p(scene.cam), W, H,
+                      _p(accum), int(rand_seed) & 0xFFFFFFFF, reset, gi_check, rr_threshold, max_depth, threads)
+    if rc != 0:
+        raise RuntimeError("ref_render failed: %d" % rc)
+
+
+def ref_trace(scene, rays9, any_hit=False):
+    L = ref()
+    rays9 = np.ascontiguousarray(rays9, np.float32)
+    n = rays9.shape[0]
+    tri = np.zeros(n, np.int32)
+    light = np.zeros(n, np.int32)
+    t = np.zeros(n, np.float32)
+    rc = L.ref_trace(_p(scene.tris), len(scene.tris), _p(scene.nodes), len(scene.nodes), _p(scene.lights),
+                     len(scene.lights), _p(rays9), n, int(any_hit), _p(tri), _p(light), _p(t))
+    if rc != 0:
+        raise RuntimeError("ref_trace failed: %d" % rc)
+    return tri, light, t
+
+
+def ref_tonemap(accum):
+    L = ref()
+    H, W = accum.shape[:2]
+    out = np.zeros((H, W, 4), np.float32)
+    a = np.ascontiguousarray(accum, np.float32)
+    L.ref_tonemap(_p(a), W, H, _p(out))
+    return out
+
+
+def ref_bvh(tris, bins=20, leaf=10):
+    from yune_gb300.layouts import BVH_NODE
+    L = ref()
+    cap = max(64, 8 * len(tris))
+    out = np.zeros(cap, BVH_NODE)
+    n = C.c_int()
+    rc = L.ref_bvh_build(_p(tris), len(tris), bins, leaf, _p(out), cap, C.byref(n))
+    if rc != 0:
+        raise RuntimeError("ref_bvh_build failed: %d" % rc)
+    return out[: n.value].copy()
+
+
+def seeded_rays(scene, n, seed=0, inside=True):
+    """n rays (origin xyzw, dir xyzw, length) with origins inside the scene box and
+    directions uniform on the sphere, as 9 float32 per ray; w = 1 for origins and 0 for
+    directions, as the reference's rays carry."""
+    rng = np.random.default_rng(seed)
+    lo = np.array([-0.49, -0.49, -0.49])
+    hi = np.array([0.49, 0.49, 0.49])
+    o = rng.uniform(lo, hi, size=(n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d = d.astype(np.float32)
+    r = np.zeros((n, 9), np.float32)
+    r[:, 0:3] = o
+    r[:, 3] = 1.0
+    r[:, 4:7] = d
+    r[:, 7] = 0.0
+    r[:, 8] = np.inf
+    return r

@@ -1,0 +1,105 @@
+"""ctypes bindings of libyune_gb300.so (include/yune_cuda.h and include/yune_host.h).
+
+The library is loaded from the package directory only; when it is missing the import
+fails with the build command to run, so nothing falls back to another implementation.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libyune_gb300.so")
+
+vp = C.c_void_p
+i32 = C.c_int
+u32 = C.c_uint32
+f32 = C.c_float
+
+
+class PassCfg(C.Structure):
+    """yc_pass_cfg"""
+    _fields_ = [("integrator", i32), ("mis", i32), ("rr_threshold", i32), ("max_depth", i32),
+                ("brdf_model", i32), ("mis_lobe_fix", i32), ("bdpt_bounces", i32), ("block", i32),
+                ("block_x", i32), ("block_y", i32)]
+
+
+class Stats(C.Structure):
+    """yc_stats"""
+    _fields_ = [(n, C.c_uint64) for n in ("rays", "primary", "extension", "shadow", "mis", "connection",
+                                          "traversed", "samples", "stack_overflow")]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    # core
+    "yc_create": (i32, [i32, C.POINTER(vp)]),
+    "yc_destroy": (i32, [vp]),
+    "yc_last_error": (C.c_char_p, []),
+    "yc_synchronize": (i32, [vp]),
+    "yc_upload_scene": (i32, [vp, vp, i32, vp, i32, vp, i32, vp, i32, C.POINTER(i32)]),
+    "yc_set_lights": (i32, [vp, i32, vp, i32]),
+    "yc_release_scene": (i32, [vp, i32]),
+    "yc_scene_bytes": (i32, [vp, i32, C.POINTER(C.c_uint64)]),
+    "yc_set_camera": (i32, [vp, vp]),
+    "yc_alloc_accum": (i32, [vp, i32, i32, C.POINTER(i32)]),
+    "yc_free_accum": (i32, [vp, i32]),
+    "yc_read_accum": (i32, [vp, i32, vp]),
+    "yc_write_accum": (i32, [vp, i32, vp]),
+    "yc_accum_device_ptr": (i32, [vp, i32, C.POINTER(vp)]),
+    "yc_render_pass": (i32, [vp, i32, i32, u32, i32, i32, C.POINTER(PassCfg)]),
+    "yc_render_passes": (i32, [vp, i32, i32, vp, i32, i32, i32, C.POINTER(PassCfg)]),
+    "yc_tonemap": (i32, [vp, i32, vp]),
+    "yc_trace": (i32, [vp, i32, vp, i32, i32, vp, vp, vp]),
+    "yc_trace_device": (i32, [vp, i32, vp, i32, i32, vp, vp]),
+    "yc_get_stats": (i32, [vp, C.POINTER(Stats)]),
+    "yc_reset_stats": (i32, [vp]),
+    "yc_last_pass_ms": (i32, [vp, C.POINTER(f32)]),
+    # host producers
+    "yh_bvh_build": (i32, [vp, i32, i32, i32, C.POINTER(vp)]),
+    "yh_bvh_node_count": (i32, [vp]),
+    "yh_bvh_copy_nodes": (i32, [vp, vp, i32]),
+    "yh_bvh_depth": (i32, [vp]),
+    "yh_bvh_free": (None, [vp]),
+    "yh_triangle_aabb": (i32, [vp, vp, vp]),
+    "yh_camera_look": (i32, [vp, vp, vp, vp, f32, vp]),
+    "yh_scene_new": (i32, [C.POINTER(vp)]),
+    "yh_scene_free": (None, [vp]),
+    "yh_scene_add_material": (i32, [vp, vp, C.POINTER(i32)]),
+    "yh_scene_add_cornell": (i32, [vp, C.c_uint64, f32, f32, f32, i32]),
+    "yh_scene_add_icosphere": (i32, [vp, vp, f32, i32, f32, C.c_uint64, i32]),
+    "yh_scene_add_light": (i32, [vp, vp]),
+    "yh_scene_counts": (i32, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
+    "yh_scene_copy": (i32, [vp, vp, vp, vp]),
+}
+
+_lib = None
+
+
+class YuneError(RuntimeError):
+    """A C-ABI call returned a negative status."""
+
+    def __init__(self, code, msg):
+        super().__init__("%s (code %d)" % (msg, code))
+        self.code = code
+
+
+def lib():
+    """The loaded library; raises ImportError when it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libyune_gb300.so is not built; run: python -c 'import __graft_entry__ as g; g.build()'")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc, what=""):
+    if rc != 0:
+        msg = lib().yc_last_error()
+        msg = msg.decode() if msg else ""
+        raise YuneError(rc, (what + ": " if what else "") + msg)
+    return rc

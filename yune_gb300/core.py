@@ -1,0 +1,124 @@
+"""RendererCore-style driver over the C-ABI (the calls src/RendererCore.cpp makes).
+
+    r = Renderer()                       # CLManager::setup
+    sid = r.upload(scene)                # setupVertexBuffer / setupMatBuffer / setupBVHBuffer
+    r.set_camera(scene.cam)              # setupCameraBuffer, Camera::setBuffer
+    aid = r.alloc_accum(w, h)            # setupImageBuffers
+    r.render(sid, aid, rand, reset=1)    # enqueueKernels: one `pathtracer` pass
+    img = r.tonemap(aid)                 # the `tonemap` pass
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .layouts import ptr
+
+
+def cfg_struct(cfg):
+    s = N.PassCfg()
+    for k, _ in N.PassCfg._fields_:
+        setattr(s, k, int(cfg.get(k, 0)))
+    if s.block_x == 0:
+        s.block_x = 1
+    if s.block_y == 0:
+        s.block_y = 1
+    return s
+
+
+class Renderer:
+    def __init__(self, device=0):
+        self.L = N.lib()
+        h = C.c_void_p()
+        N.check(self.L.yc_create(device, C.byref(h)), "yc_create")
+        self.h = h
+        self._accum_shape = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.yc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, scene):
+        sid = C.c_int()
+        N.check(self.L.yc_upload_scene(self.h, ptr(scene.tris), len(scene.tris), ptr(scene.mats), len(scene.mats),
+                                       ptr(scene.nodes), len(scene.nodes), ptr(scene.lights), len(scene.lights),
+                                       C.byref(sid)), "yc_upload_scene")
+        return sid.value
+
+    def release(self, sid):
+        N.check(self.L.yc_release_scene(self.h, sid), "yc_release_scene")
+
+    def set_camera(self, cam):
+        N.check(self.L.yc_set_camera(self.h, ptr(cam)), "yc_set_camera")
+
+    def alloc_accum(self, w, h):
+        aid = C.c_int()
+        N.check(self.L.yc_alloc_accum(self.h, w, h, C.byref(aid)), "yc_alloc_accum")
+        self._accum_shape[aid.value] = (h, w)
+        return aid.value
+
+    def free_accum(self, aid):
+        N.check(self.L.yc_free_accum(self.h, aid), "yc_free_accum")
+        self._accum_shape.pop(aid, None)
+
+    def render(self, sid, aid, rand_seed, reset=0, gi_check=1, cfg=None):
+        c = cfg_struct(cfg or {})
+        N.check(self.L.yc_render_pass(self.h, sid, aid, int(rand_seed) & 0xFFFFFFFF, reset, gi_check, C.byref(c)),
+                "yc_render_pass")
+
+    def render_passes(self, sid, aid, seeds, reset_first=1, gi_check=1, cfg=None):
+        c = cfg_struct(cfg or {})
+        s = np.ascontiguousarray(seeds, dtype=np.uint32)
+        N.check(self.L.yc_render_passes(self.h, sid, aid, ptr(s), len(s), reset_first, gi_check, C.byref(c)),
+                "yc_render_passes")
+
+    def read_accum(self, aid):
+        h, w = self._accum_shape[aid]
+        out = np.zeros((h, w, 4), np.float32)
+        N.check(self.L.yc_read_accum(self.h, aid, ptr(out)), "yc_read_accum")
+        return out
+
+    def write_accum(self, aid, img):
+        img = np.ascontiguousarray(img, np.float32)
+        N.check(self.L.yc_write_accum(self.h, aid, ptr(img)), "yc_write_accum")
+
+    def tonemap(self, aid):
+        h, w = self._accum_shape[aid]
+        out = np.zeros((h, w, 4), np.float32)
+        N.check(self.L.yc_tonemap(self.h, aid, ptr(out)), "yc_tonemap")
+        return out
+
+    def trace(self, sid, rays9, any_hit=False):
+        rays9 = np.ascontiguousarray(rays9, np.float32)
+        n = rays9.shape[0]
+        tri = np.zeros(n, np.int32)
+        light = np.zeros(n, np.int32)
+        t = np.zeros(n, np.float32)
+        N.check(self.L.yc_trace(self.h, sid, ptr(rays9), n, int(any_hit), ptr(tri), ptr(light), ptr(t)), "yc_trace")
+        return tri, light, t
+
+    def stats(self):
+        s = N.Stats()
+        N.check(self.L.yc_get_stats(self.h, C.byref(s)), "yc_get_stats")
+        return {k: getattr(s, k) for k, _ in N.Stats._fields_}
+
+    def reset_stats(self):
+        N.check(self.L.yc_reset_stats(self.h), "yc_reset_stats")
+
+    def last_pass_ms(self):
+        ms = C.c_float()
+        N.check(self.L.yc_last_pass_ms(self.h, C.byref(ms)), "yc_last_pass_ms")
+        return ms.value
+
+    def synchronize(self):
+        N.check(self.L.yc_synchronize(self.h), "yc_synchronize")

@@ -1,0 +1,510 @@
+// api.cu -- the C-ABI of include/yune_cuda.h: context, scene and accumulator buffers,
+// and the render-pass driver that replaces CLManager + RendererCore's OpenCL calls.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "yc_internal.h"
+#include "yc_repack.h"
+#include "yune_cuda.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define YC_CUDA(call)                                                                        \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      return fail(e_ == cudaErrorMemoryAllocation ? YC_E_NOMEM : YC_E_LAUNCH,                \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                       \
+  } while (0)
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    release();
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    else p = nullptr;
+    return e;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+struct Scene {
+  DevBuf<float4> nodes, tris, shade;
+  DevBuf<yc_material> mats;
+  DevBuf<yc_quad_light> lights;
+  yc::DevScene dev{};
+  uint64_t bytes = 0;
+};
+
+struct Accum {
+  DevBuf<float4> buf;
+  int w = 0, h = 0;
+};
+
+}  // namespace
+
+struct yc_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::map<int, std::unique_ptr<Scene>> scenes;
+  std::map<int, std::unique_ptr<Accum>> accums;
+  int next_scene = 1, next_accum = 1;
+  yc_cam cam{};
+  bool have_cam = false;
+  // wavefront buffers, sized for the largest image seen
+  size_t cap_paths = 0;
+  DevBuf<int4> misc;
+  DevBuf<float4> f4bufs[12];
+  DevBuf<int> q[4];                  // closest/any for two rounds
+  DevBuf<yc::RoundCounters> rc;      // two round-counter blocks
+  DevBuf<yc::DevStats> stats;
+  yc::RoundCounters* rc_host = nullptr;   // pinned
+  int logic_grid = 0;
+  int sm_count = 0;
+  float last_ms = 0.0f;
+  // direct queries
+  DevBuf<float> q_rays;
+  DevBuf<int> q_tri;
+  DevBuf<float> q_t;
+  DevBuf<int> q_work;
+};
+
+namespace {
+
+int ensure_paths(yc_ctx* c, size_t n) {
+  if (n <= c->cap_paths) return 0;
+  YC_CUDA(c->misc.alloc(n));
+  for (auto& b : c->f4bufs) YC_CUDA(b.alloc(n));
+  for (auto& b : c->q) YC_CUDA(b.alloc(n));
+  c->cap_paths = n;
+  return 0;
+}
+
+yc::PathState path_state(yc_ctx* c) {
+  yc::PathState ps;
+  ps.misc = c->misc.p;
+  ps.thr = c->f4bufs[0].p;
+  ps.thr_next = c->f4bufs[1].p;
+  ps.direct = c->f4bufs[2].p;
+  ps.indirect = c->f4bufs[3].p;
+  ps.ls = c->f4bufs[4].p;
+  ps.hp = c->f4bufs[5].p;
+  ps.nrm = c->f4bufs[6].p;
+  ps.wo = c->f4bufs[7].p;
+  ps.wi = c->f4bufs[8].p;
+  ps.ro = c->f4bufs[9].p;
+  ps.rd = c->f4bufs[10].p;
+  ps.hit = c->f4bufs[11].p;
+  return ps;
+}
+
+Scene* find_scene(yc_ctx* c, int id) {
+  auto it = c->scenes.find(id);
+  return it == c->scenes.end() ? nullptr : it->second.get();
+}
+Accum* find_accum(yc_ctx* c, int id) {
+  auto it = c->accums.find(id);
+  return it == c->accums.end() ? nullptr : it->second.get();
+}
+
+int validate_cfg(const yc_pass_cfg* cfg) {
+  if (!cfg) return fail(YC_E_INVALID, "cfg is NULL");
+  if (cfg->integrator != YC_UDPT && cfg->integrator != YC_BDPT) return fail(YC_E_INVALID, "unknown integrator");
+  if (cfg->max_depth < 0) return fail(YC_E_INVALID, "max_depth < 0");
+  if (cfg->block_x < 1 || cfg->block_y < 1 || cfg->block < 0 || cfg->block >= cfg->block_x * cfg->block_y)
+    return fail(YC_E_INVALID, "bad block tiling");
+  return 0;
+}
+
+// Runs one pass (all rounds) on the context stream; the host polls the queue sizes
+// every few rounds.
+int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int gi_check, const yc_pass_cfg* cfg) {
+  if (cfg->integrator != YC_UDPT) return fail(YC_E_INVALID, "integrator not available in this build");
+  const int W = ac->w, H = ac->h;
+  int rc_ = ensure_paths(c, (size_t)W * H);
+  if (rc_) return rc_;
+  yc::PassParams pp{};
+  pp.sc = sc->dev;
+  pp.cam = c->cam;
+  pp.accum = ac->buf.p;
+  pp.width = W;
+  pp.height = H;
+  // tile of this launch (udpt.cl:166-167, src/RendererCore.cpp:146-150)
+  pp.tile_w = (int)std::ceil((float)W / cfg->block_x);
+  pp.tile_h = (int)std::ceil((float)H / cfg->block_y);
+  pp.off_x = (int)(std::ceil((float)W / cfg->block_x) * (float)(cfg->block % cfg->block_x));
+  pp.off_y = (int)(std::ceil((float)H / cfg->block_y) * (float)(cfg->block / cfg->block_x));
+  pp.rand_seed = rand_seed;
+  pp.reset = reset;
+  pp.gi_check = gi_check;
+  pp.mis = cfg->mis;
+  pp.rr_threshold = cfg->rr_threshold;
+  pp.max_depth = cfg->max_depth;
+  pp.brdf_model = cfg->brdf_model;
+  pp.mis_lobe_fix = cfg->mis_lobe_fix;
+  const yc::PathState ps = path_state(c);
+  yc::RoundCounters* rc = c->rc.p;
+  YC_CUDA(cudaMemsetAsync(rc, 0, 2 * sizeof(yc::RoundCounters), c->stream));
+  yc::launch_raygen(pp, ps, c->q[0].p, rc + 0, c->stats.p, c->stream);
+  YC_CUDA(cudaPeekAtLastError());
+  const int grid_c = yc::trace_grid_blocks(false, sc->dev.depth);
+  const int grid_a = yc::trace_grid_blocks(true, sc->dev.depth);
+  if (grid_c <= 0 || grid_a <= 0) return fail(YC_E_LAUNCH, "trace kernel cannot be resident (stack too deep)");
+  int cur = 0;
+  const int check_every = 6;
+  for (int round = 0; round < 1000000; ++round) {
+    int* in_c = c->q[2 * cur].p;
+    int* in_a = c->q[2 * cur + 1].p;
+    int* out_c = c->q[2 * (1 - cur)].p;
+    int* out_a = c->q[2 * (1 - cur) + 1].p;
+    yc::RoundCounters* rin = rc + cur;
+    yc::RoundCounters* rout = rc + (1 - cur);
+    if (yc::launch_trace(sc->dev, false, in_c, &rin->n_closest, &rin->work_closest, ps.ro, ps.rd, ps.hit, c->stats.p,
+                         grid_c, c->stream))
+      return fail(YC_E_LAUNCH, std::string("extend kernel: ") + cudaGetErrorString(cudaGetLastError()));
+    if (yc::launch_trace(sc->dev, true, in_a, &rin->n_any, &rin->work_any, ps.ro, ps.rd, ps.hit, c->stats.p, grid_a,
+                         c->stream))
+      return fail(YC_E_LAUNCH, std::string("occlusion kernel: ") + cudaGetErrorString(cudaGetLastError()));
+    YC_CUDA(cudaMemsetAsync(rout, 0, sizeof(yc::RoundCounters), c->stream));
+    yc::launch_logic(pp, ps, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid, c->stream);
+    YC_CUDA(cudaPeekAtLastError());
+    cur = 1 - cur;
+    if ((round + 1) % check_every == 0) {
+      YC_CUDA(cudaMemcpyAsync(c->rc_host, rc + cur, sizeof(yc::RoundCounters), cudaMemcpyDeviceToHost, c->stream));
+      YC_CUDA(cudaStreamSynchronize(c->stream));
+      if (c->rc_host->n_closest == 0 && c->rc_host->n_any == 0) break;
+    }
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* yc_last_error(void) { return g_last_error.c_str(); }
+
+int yc_create(int device, yc_ctx** out) {
+  if (!out) return fail(YC_E_INVALID, "out is NULL");
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return fail(YC_E_NODEVICE, "no CUDA device");
+  if (device < 0 || device >= n) return fail(YC_E_INVALID, "device index out of range");
+  YC_CUDA(cudaSetDevice(device));
+  yc_ctx* c = new (std::nothrow) yc_ctx;
+  if (!c) return fail(YC_E_NOMEM, "host allocation failed");
+  c->device = device;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  if (e == cudaSuccess) e = c->rc.alloc(2);
+  if (e == cudaSuccess) e = c->stats.alloc(1);
+  if (e == cudaSuccess) e = cudaMallocHost(&c->rc_host, sizeof(yc::RoundCounters));
+  if (e == cudaSuccess) e = c->q_work.alloc(1);
+  if (e == cudaSuccess) e = cudaMemset(c->stats.p, 0, sizeof(yc::DevStats));
+  if (e != cudaSuccess) {
+    yc_destroy(c);
+    return fail(YC_E_LAUNCH, std::string("context setup: ") + cudaGetErrorString(e));
+  }
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  c->logic_grid = std::max(1, c->sm_count) * 4;
+  *out = c;
+  return YC_OK;
+}
+
+int yc_destroy(yc_ctx* c) {
+  if (!c) return YC_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->scenes.clear();
+  c->accums.clear();
+  if (c->rc_host) cudaFreeHost(c->rc_host);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return YC_OK;
+}
+
+int yc_synchronize(yc_ctx* c) {
+  if (!c) return fail(YC_E_INVALID, "ctx is NULL");
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  return YC_OK;
+}
+
+int yc_upload_scene(yc_ctx* c, const yc_triangle* tris, int n_tri, const yc_material* mats, int n_mat,
+                    const yc_bvh_node* nodes, int n_node, const yc_quad_light* lights, int n_light, int* scene_id) {
+  if (!c || !scene_id) return fail(YC_E_INVALID, "ctx or scene_id is NULL");
+  if (n_tri < 0 || n_mat < 0 || n_node < 0) return fail(YC_E_INVALID, "negative count");
+  if ((n_tri > 0 && !tris) || (n_mat > 0 && !mats) || (n_node > 0 && !nodes))
+    return fail(YC_E_INVALID, "NULL array with non-zero count");
+  if (n_light < 1 || n_light > yc::MAX_LIGHTS || !lights) return fail(YC_E_INVALID, "need 1..16 lights");
+  for (int i = 0; i < n_tri; ++i)
+    if (tris[i].matID < 0 || tris[i].matID >= n_mat)
+      return fail(YC_E_INVALID, "triangle " + std::to_string(i) + " has matID out of range");
+  yc::Repacked rp;
+  std::string err;
+  if (yc::repack_scene(tris, n_tri, nodes, n_node, rp, err)) return fail(YC_E_INVALID, err);
+  std::unique_ptr<Scene> s(new (std::nothrow) Scene);
+  if (!s) return fail(YC_E_NOMEM, "host allocation failed");
+  YC_CUDA(cudaSetDevice(c->device));
+  YC_CUDA(s->nodes.alloc(std::max<size_t>(rp.nodes.size(), 4)));
+  YC_CUDA(s->tris.alloc(std::max<size_t>(rp.tris.size(), 3)));
+  YC_CUDA(s->shade.alloc(std::max<size_t>(rp.shade.size(), 4)));
+  YC_CUDA(s->mats.alloc(std::max(n_mat, 1)));
+  YC_CUDA(s->lights.alloc(yc::MAX_LIGHTS));
+  if (!rp.nodes.empty())
+    YC_CUDA(cudaMemcpyAsync(s->nodes.p, rp.nodes.data(), rp.nodes.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+  if (!rp.tris.empty())
+    YC_CUDA(cudaMemcpyAsync(s->tris.p, rp.tris.data(), rp.tris.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+  if (!rp.shade.empty())
+    YC_CUDA(cudaMemcpyAsync(s->shade.p, rp.shade.data(), rp.shade.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+  if (n_mat > 0)
+    YC_CUDA(cudaMemcpyAsync(s->mats.p, mats, n_mat * sizeof(yc_material), cudaMemcpyHostToDevice, c->stream));
+  YC_CUDA(cudaMemcpyAsync(s->lights.p, lights, n_light * sizeof(yc_quad_light), cudaMemcpyHostToDevice, c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  yc::DevScene& d = s->dev;
+  d.nodes = s->nodes.p;
+  d.tris = s->tris.p;
+  d.shade = s->shade.p;
+  d.mats = s->mats.p;
+  d.lights = s->lights.p;
+  d.n_lights = n_light;
+  d.n_tri = n_tri;
+  d.n_mat = n_mat;
+  d.root_link = rp.root_link;
+  d.root_test = rp.root_test;
+  d.depth = rp.depth;
+  d.root_lo = rp.root_lo;
+  d.root_hi = rp.root_hi;
+  s->bytes = s->nodes.bytes() + s->tris.bytes() + s->shade.bytes() + s->mats.bytes() + s->lights.bytes();
+  const int id = c->next_scene++;
+  c->scenes[id] = std::move(s);
+  *scene_id = id;
+  return YC_OK;
+}
+
+int yc_set_lights(yc_ctx* c, int scene_id, const yc_quad_light* lights, int n_light) {
+  if (!c) return fail(YC_E_INVALID, "ctx is NULL");
+  Scene* s = find_scene(c, scene_id);
+  if (!s) return fail(YC_E_NOTFOUND, "unknown scene");
+  if (n_light < 1 || n_light > yc::MAX_LIGHTS || !lights) return fail(YC_E_INVALID, "need 1..16 lights");
+  YC_CUDA(cudaMemcpyAsync(s->lights.p, lights, n_light * sizeof(yc_quad_light), cudaMemcpyHostToDevice, c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  s->dev.n_lights = n_light;
+  return YC_OK;
+}
+
+int yc_release_scene(yc_ctx* c, int scene_id) {
+  if (!c) return fail(YC_E_INVALID, "ctx is NULL");
+  auto it = c->scenes.find(scene_id);
+  if (it == c->scenes.end()) return fail(YC_E_NOTFOUND, "unknown scene");
+  cudaStreamSynchronize(c->stream);
+  c->scenes.erase(it);
+  return YC_OK;
+}
+
+int yc_scene_bytes(yc_ctx* c, int scene_id, uint64_t* bytes) {
+  if (!c || !bytes) return fail(YC_E_INVALID, "NULL argument");
+  Scene* s = find_scene(c, scene_id);
+  if (!s) return fail(YC_E_NOTFOUND, "unknown scene");
+  *bytes = s->bytes;
+  return YC_OK;
+}
+
+int yc_set_camera(yc_ctx* c, const yc_cam* cam) {
+  if (!c || !cam) return fail(YC_E_INVALID, "NULL argument");
+  c->cam = *cam;
+  c->have_cam = true;
+  return YC_OK;
+}
+
+int yc_alloc_accum(yc_ctx* c, int w, int h, int* accum_id) {
+  if (!c || !accum_id || w <= 0 || h <= 0) return fail(YC_E_INVALID, "bad accumulator size");
+  if ((size_t)w * h > (size_t)1 << 28) return fail(YC_E_INVALID, "accumulator too large");
+  std::unique_ptr<Accum> a(new (std::nothrow) Accum);
+  if (!a) return fail(YC_E_NOMEM, "host allocation failed");
+  YC_CUDA(a->buf.alloc((size_t)w * h));
+  YC_CUDA(cudaMemsetAsync(a->buf.p, 0, a->buf.bytes(), c->stream));
+  a->w = w;
+  a->h = h;
+  const int id = c->next_accum++;
+  c->accums[id] = std::move(a);
+  *accum_id = id;
+  return YC_OK;
+}
+
+int yc_free_accum(yc_ctx* c, int accum_id) {
+  if (!c) return fail(YC_E_INVALID, "ctx is NULL");
+  auto it = c->accums.find(accum_id);
+  if (it == c->accums.end()) return fail(YC_E_NOTFOUND, "unknown accumulator");
+  cudaStreamSynchronize(c->stream);
+  c->accums.erase(it);
+  return YC_OK;
+}
+
+int yc_read_accum(yc_ctx* c, int accum_id, float* out) {
+  if (!c || !out) return fail(YC_E_INVALID, "NULL argument");
+  Accum* a = find_accum(c, accum_id);
+  if (!a) return fail(YC_E_NOTFOUND, "unknown accumulator");
+  YC_CUDA(cudaMemcpyAsync(out, a->buf.p, a->buf.bytes(), cudaMemcpyDeviceToHost, c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  return YC_OK;
+}
+
+int yc_write_accum(yc_ctx* c, int accum_id, const float* in) {
+  if (!c || !in) return fail(YC_E_INVALID, "NULL argument");
+  Accum* a = find_accum(c, accum_id);
+  if (!a) return fail(YC_E_NOTFOUND, "unknown accumulator");
+  YC_CUDA(cudaMemcpyAsync(a->buf.p, in, a->buf.bytes(), cudaMemcpyHostToDevice, c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  return YC_OK;
+}
+
+int yc_accum_device_ptr(yc_ctx* c, int accum_id, void** dptr) {
+  if (!c || !dptr) return fail(YC_E_INVALID, "NULL argument");
+  Accum* a = find_accum(c, accum_id);
+  if (!a) return fail(YC_E_NOTFOUND, "unknown accumulator");
+  *dptr = a->buf.p;
+  return YC_OK;
+}
+
+int yc_render_passes(yc_ctx* c, int scene_id, int accum_id, const uint32_t* rands, int n_pass, int reset_first,
+                     int gi_check, const yc_pass_cfg* cfg) {
+  if (!c || !rands || n_pass < 0) return fail(YC_E_INVALID, "NULL argument");
+  if (int r = validate_cfg(cfg)) return r;
+  Scene* s = find_scene(c, scene_id);
+  if (!s) return fail(YC_E_NOTFOUND, "unknown scene");
+  Accum* a = find_accum(c, accum_id);
+  if (!a) return fail(YC_E_NOTFOUND, "unknown accumulator");
+  if (!c->have_cam) return fail(YC_E_INVALID, "no camera set");
+  YC_CUDA(cudaSetDevice(c->device));
+  YC_CUDA(cudaEventRecord(c->ev0, c->stream));
+  for (int k = 0; k < n_pass; ++k) {
+    const int r = run_pass(c, s, a, rands[k], (k == 0) ? reset_first : 0, gi_check, cfg);
+    if (r) return r;
+  }
+  YC_CUDA(cudaEventRecord(c->ev1, c->stream));
+  YC_CUDA(cudaEventSynchronize(c->ev1));
+  YC_CUDA(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
+  return YC_OK;
+}
+
+int yc_render_pass(yc_ctx* c, int scene_id, int accum_id, uint32_t rand_seed, int reset, int gi_check,
+                   const yc_pass_cfg* cfg) {
+  return yc_render_passes(c, scene_id, accum_id, &rand_seed, 1, reset, gi_check, cfg);
+}
+
+int yc_tonemap(yc_ctx* c, int accum_id, float* out) {
+  if (!c || !out) return fail(YC_E_INVALID, "NULL argument");
+  Accum* a = find_accum(c, accum_id);
+  if (!a) return fail(YC_E_NOTFOUND, "unknown accumulator");
+  DevBuf<float4> tmp;
+  YC_CUDA(tmp.alloc(a->buf.n));
+  yc::launch_tonemap(a->buf.p, tmp.p, (int)a->buf.n, c->stream);
+  YC_CUDA(cudaPeekAtLastError());
+  YC_CUDA(cudaMemcpyAsync(out, tmp.p, tmp.bytes(), cudaMemcpyDeviceToHost, c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  return YC_OK;
+}
+
+int yc_trace_device(yc_ctx* c, int scene_id, const float* rays_dev, int n, int any_hit, int* tri_dev, float* t_dev) {
+  if (!c || n < 0 || (n > 0 && (!rays_dev || !tri_dev))) return fail(YC_E_INVALID, "NULL argument");
+  Scene* s = find_scene(c, scene_id);
+  if (!s) return fail(YC_E_NOTFOUND, "unknown scene");
+  if (n == 0) return YC_OK;
+  YC_CUDA(cudaMemsetAsync(c->q_work.p, 0, sizeof(int), c->stream));
+  if (yc::launch_trace_rays(s->dev, any_hit != 0, rays_dev, n, tri_dev, t_dev, c->q_work.p, c->stats.p, c->stream))
+    return fail(YC_E_LAUNCH, std::string("trace kernel: ") + cudaGetErrorString(cudaGetLastError()));
+  return YC_OK;
+}
+
+int yc_trace(yc_ctx* c, int scene_id, const float* rays, int n, int any_hit, int* tri_out, int* light_out,
+             float* t_out) {
+  if (!c || n < 0 || (n > 0 && (!rays || !tri_out))) return fail(YC_E_INVALID, "NULL argument");
+  if (n == 0) return YC_OK;
+  YC_CUDA(c->q_rays.alloc((size_t)n * 9));
+  YC_CUDA(c->q_tri.alloc(n));
+  YC_CUDA(c->q_t.alloc(n));
+  YC_CUDA(cudaMemcpyAsync(c->q_rays.p, rays, (size_t)n * 9 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  int r = yc_trace_device(c, scene_id, c->q_rays.p, n, any_hit, c->q_tri.p, c->q_t.p);
+  if (r) return r;
+  std::vector<int> tri(n);
+  YC_CUDA(cudaMemcpyAsync(tri.data(), c->q_tri.p, n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  if (t_out) YC_CUDA(cudaMemcpyAsync(t_out, c->q_t.p, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < n; ++i) {
+    if (any_hit) {
+      tri_out[i] = tri[i];
+      if (light_out) light_out[i] = -1;
+    } else if (tri[i] <= -2) {
+      tri_out[i] = -1;
+      if (light_out) light_out[i] = -2 - tri[i];
+    } else {
+      tri_out[i] = tri[i];
+      if (light_out) light_out[i] = -1;
+    }
+  }
+  return YC_OK;
+}
+
+int yc_get_stats(yc_ctx* c, yc_stats* out) {
+  if (!c || !out) return fail(YC_E_INVALID, "NULL argument");
+  yc::DevStats d;
+  YC_CUDA(cudaMemcpyAsync(&d, c->stats.p, sizeof(d), cudaMemcpyDeviceToHost, c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  out->rays = d.rays;
+  out->primary = d.primary;
+  out->extension = d.extension;
+  out->shadow = d.shadow;
+  out->mis = d.mis;
+  out->connection = d.connection;
+  out->traversed = d.traversed;
+  out->samples = d.samples;
+  out->stack_overflow = d.stack_overflow;
+  return YC_OK;
+}
+
+int yc_reset_stats(yc_ctx* c) {
+  if (!c) return fail(YC_E_INVALID, "ctx is NULL");
+  YC_CUDA(cudaMemsetAsync(c->stats.p, 0, sizeof(yc::DevStats), c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  return YC_OK;
+}
+
+int yc_last_pass_ms(yc_ctx* c, float* ms) {
+  if (!c || !ms) return fail(YC_E_INVALID, "NULL argument");
+  *ms = c->last_ms;
+  return YC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,203 @@
+// repack.cpp -- turns the caller's TriangleGPU / BVHNodeGPU arrays into the device
+// layout described in yc_scene.h (host side, once per upload).
+//
+// The reference walks BVHNodeGPU directly: a node is processed as a leaf when
+// child_idx == -1 and vert_len > 0, otherwise its children child_idx and child_idx + 1
+// are box-tested, each only when vert_len > 0 || child_idx > 0 (traverseBVH,
+// kernels/legacy/udpt.cl:298-321). The repack keeps exactly that structure: each
+// reference interior node becomes one 64-byte node carrying its children's boxes, each
+// reference leaf becomes a contiguous run of its vert_list triangles (in vert_list
+// order) in the 48-byte stream, and a child the reference never queues becomes
+// LINK_NONE. With no BVH (bvh_size == 0) the reference tests every triangle in index
+// order (udpt.cl:280-284); that case becomes a chain of nodes with unbounded boxes whose
+// leaves hold the triangles in index order.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../ym_math.h"
+#include "yc_repack.h"
+
+namespace yc {
+
+namespace {
+
+struct Builder {
+  const yc_triangle* tris;
+  int n_tri;
+  const yc_bvh_node* nodes;
+  int n_node;
+  std::vector<float4> out_nodes;
+  std::vector<float4> out_tris;
+  int depth = 0;
+
+  int emit_leaf(const int* list, int count) {
+    const int first = (int)(out_tris.size() / 3);
+    for (int k = 0; k < count; ++k) {
+      const yc_triangle& t = tris[list[k]];
+      float4 a, b, c;
+      a.x = t.v1.x; a.y = t.v1.y; a.z = t.v1.z;
+      int id = list[k];
+      std::memcpy(&a.w, &id, 4);
+      b.x = t.v2.x - t.v1.x; b.y = t.v2.y - t.v1.y; b.z = t.v2.z - t.v1.z; b.w = 0.0f;
+      c.x = t.v3.x - t.v1.x; c.y = t.v3.y - t.v1.y; c.z = t.v3.z - t.v1.z; c.w = 0.0f;
+      out_tris.push_back(a);
+      out_tris.push_back(b);
+      out_tris.push_back(c);
+    }
+    return ~((first << 4) | count);
+  }
+};
+
+bool is_leaf(const yc_bvh_node& n) { return (float)n.child_idx == -1.0f && n.vert_len > 0; }
+bool is_queued(const yc_bvh_node& n) { return n.vert_len > 0 || n.child_idx > 0; }
+
+}  // namespace
+
+int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, int n_node, Repacked& out,
+                 std::string& err) {
+  Builder b{tris, n_tri, nodes, n_node, {}, {}, 0};
+  out = Repacked();
+  const float INF = INFINITY;
+  // shading records: normalize(vn1..vn3) and the material index
+  out.shade.resize((size_t)n_tri * 4);
+  for (int i = 0; i < n_tri; ++i) {
+    const yc_triangle& t = tris[i];
+    const yc_float4* vn[3] = {&t.vn1, &t.vn2, &t.vn3};
+    for (int k = 0; k < 3; ++k) {
+      const ym::f4 n = ym::normalize(ym::mk(vn[k]->x, vn[k]->y, vn[k]->z, vn[k]->w));
+      out.shade[4 * (size_t)i + k] = float4{n.x, n.y, n.z, n.w};
+    }
+    float mid;
+    int m = t.matID;
+    std::memcpy(&mid, &m, 4);
+    out.shade[4 * (size_t)i + 3] = float4{mid, 0.0f, 0.0f, 0.0f};
+  }
+
+  if (n_tri == 0) {
+    out.root_link = LINK_NONE;
+    out.root_test = 0;
+    out.depth = 0;
+    return 0;
+  }
+  if (n_node == 0) {
+    // brute force: chain of unbounded nodes, leaves of up to 15 triangles in index order
+    const int per = 15;
+    const int n_leaf = (n_tri + per - 1) / per;
+    std::vector<int> ids(n_tri);
+    for (int i = 0; i < n_tri; ++i) ids[i] = i;
+    if (n_leaf == 1) {
+      out.root_link = b.emit_leaf(ids.data(), n_tri);
+    } else {
+      for (int l = 0; l < n_leaf - 1; ++l) {
+        const int leaf = b.emit_leaf(ids.data() + l * per, per);
+        int next;
+        if (l == n_leaf - 2) {
+          const int rest = n_tri - (l + 1) * per;
+          next = b.emit_leaf(ids.data() + (l + 1) * per, rest);
+        } else {
+          next = (int)(b.out_nodes.size() / 4) + 1;
+        }
+        int l0 = leaf, l1 = next;
+        float4 n0{-INF, INF, -INF, INF}, n1{-INF, INF, -INF, INF}, n2{-INF, INF, -INF, INF}, n3;
+        std::memcpy(&n3.x, &l0, 4);
+        std::memcpy(&n3.y, &l1, 4);
+        n3.z = n3.w = 0.0f;
+        b.out_nodes.push_back(n0);
+        b.out_nodes.push_back(n1);
+        b.out_nodes.push_back(n2);
+        b.out_nodes.push_back(n3);
+      }
+      out.root_link = 0;
+    }
+    out.root_test = 0;
+    out.depth = 2;
+    out.nodes.swap(b.out_nodes);
+    out.tris.swap(b.out_tris);
+    return 0;
+  }
+
+  // validate the reference node array
+  for (int i = 0; i < n_node; ++i) {
+    const yc_bvh_node& n = nodes[i];
+    if (n.vert_len > 10) { err = "BVH node " + std::to_string(i) + " has vert_len > 10"; return -1; }
+    if (is_leaf(n)) {
+      for (int k = 0; k < n.vert_len; ++k)
+        if (n.vert_list[k] < 0 || n.vert_list[k] >= n_tri) {
+          err = "BVH leaf " + std::to_string(i) + " references triangle " + std::to_string(n.vert_list[k]);
+          return -1;
+        }
+    } else if (is_queued(n) || i == 0) {
+      if (n.child_idx <= 0 || n.child_idx + 1 >= n_node) {
+        err = "BVH node " + std::to_string(i) + " has child_idx " + std::to_string(n.child_idx) + " out of range";
+        return -1;
+      }
+    }
+  }
+  const yc_bvh_node& root = nodes[0];
+  out.root_test = 1;
+  out.root_lo = float4{root.aabb.p_min.x, root.aabb.p_min.y, root.aabb.p_min.z, 0.0f};
+  out.root_hi = float4{root.aabb.p_max.x, root.aabb.p_max.y, root.aabb.p_max.z, 0.0f};
+  if (is_leaf(root)) {
+    out.root_link = b.emit_leaf(root.vert_list, root.vert_len);
+    out.depth = 0;
+    out.tris.swap(b.out_tris);
+    return 0;
+  }
+  // breadth-first over interior nodes; packed index assigned on first visit
+  std::vector<int> packed_of(n_node, -1);
+  std::vector<int> level(n_node, 0);
+  std::vector<int> order;
+  order.reserve(n_node);
+  order.push_back(0);
+  packed_of[0] = 0;
+  for (size_t q = 0; q < order.size(); ++q) {
+    const int ni = order[q];
+    const yc_bvh_node& n = nodes[ni];
+    for (int c = 0; c < 2; ++c) {
+      const int ci = n.child_idx + c;
+      const yc_bvh_node& ch = nodes[ci];
+      if (is_queued(ch) && !is_leaf(ch)) {
+        if (packed_of[ci] >= 0) { err = "BVH is not a tree (node reached twice)"; return -1; }
+        packed_of[ci] = (int)order.size();
+        level[ci] = level[ni] + 1;
+        order.push_back(ci);
+        if ((int)order.size() > n_node) { err = "BVH has a cycle"; return -1; }
+      }
+    }
+  }
+  b.out_nodes.resize(order.size() * 4);
+  int depth = 0;
+  for (size_t q = 0; q < order.size(); ++q) {
+    const yc_bvh_node& n = nodes[order[q]];
+    depth = std::max(depth, level[order[q]] + 1);
+    int link[2];
+    const yc_aabb* box[2];
+    for (int c = 0; c < 2; ++c) {
+      const int ci = n.child_idx + c;
+      const yc_bvh_node& ch = nodes[ci];
+      box[c] = &ch.aabb;
+      if (!is_queued(ch)) link[c] = LINK_NONE;
+      else if (is_leaf(ch)) link[c] = b.emit_leaf(ch.vert_list, ch.vert_len);
+      else link[c] = packed_of[ci];
+    }
+    float4* o = &b.out_nodes[4 * q];
+    o[0] = float4{box[0]->p_min.x, box[0]->p_max.x, box[0]->p_min.y, box[0]->p_max.y};
+    o[1] = float4{box[1]->p_min.x, box[1]->p_max.x, box[1]->p_min.y, box[1]->p_max.y};
+    o[2] = float4{box[0]->p_min.z, box[0]->p_max.z, box[1]->p_min.z, box[1]->p_max.z};
+    float4 l;
+    std::memcpy(&l.x, &link[0], 4);
+    std::memcpy(&l.y, &link[1], 4);
+    l.z = l.w = 0.0f;
+    o[3] = l;
+    if ((b.out_tris.size() / 3) >= (size_t)(1 << 27)) { err = "scene too large for the 27-bit stream index"; return -1; }
+  }
+  out.root_link = 0;
+  out.depth = depth;
+  out.nodes.swap(b.out_nodes);
+  out.tris.swap(b.out_tris);
+  return 0;
+}
+
+}  // namespace yc

@@ -1,0 +1,80 @@
+// yc_internal.h -- host-side declarations shared by the core's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "yc_scene.h"
+#include "yune_cuda.h"
+
+namespace yc {
+
+// ---- wavefront path state: one slot per path, structure of arrays ----
+// misc.x seed, misc.y pixel index, misc.z packed (state | flags << 4 | (j+1) << 12 |
+// (k+1) << 20), misc.w bounce index.
+struct PathState {
+  int4* misc;
+  float4* thr;        // throughput
+  float4* thr_next;   // throughput after the pending bounce (udpt.cl:504-507)
+  float4* direct;     // direct_color (udpt.cl:455)
+  float4* indirect;   // indirect_color
+  float4* ls;         // light_sample of the pending NEE (udpt.cl:562-563)
+  float4* hp;         // xyz hit point, w light_pdf
+  float4* nrm;        // xyz shading normal, w brdf_prob of the NEE lobe
+  float4* wo;         // xyz w_o, w brdf_pdf of the MIS sample
+  float4* wi;         // xyz NEE direction, w material index (int bits)
+  float4* ro;         // emitted ray: origin xyz, length
+  float4* rd;         // emitted ray: direction xyz
+  float4* hit;        // trace result: (t, u, v, tri) or (occluded, -, -, -)
+};
+
+// queues of one round: path indices for the closest-hit and the any-hit kernels
+struct Queues {
+  int* closest;
+  int* any;
+};
+
+// per-round device counters (cleared by one memset per round)
+struct RoundCounters {
+  int n_closest;      // entries appended to the closest queue
+  int n_any;          // entries appended to the any-hit queue
+  int work_closest;   // persistent-kernel work cursors
+  int work_any;
+  int work_logic;
+  int pad[3];
+};
+
+// device-wide statistics (yc_stats layout, 64-bit counters)
+struct DevStats {
+  unsigned long long rays, primary, extension, shadow, mis, connection, traversed, samples, stack_overflow;
+};
+
+struct PassParams {
+  DevScene sc;
+  yc_cam cam;
+  float4* accum;
+  int width, height;
+  int tile_w, tile_h;      // work-item grid of one block launch
+  int off_x, off_y;        // pixel offset of the block (udpt.cl:166-167)
+  uint32_t rand_seed;
+  int reset;
+  int gi_check;
+  int mis, rr_threshold, max_depth, brdf_model, mis_lobe_fix;
+};
+
+// launchers (udpt.cu / trace.cu)
+void launch_raygen(const PassParams& pp, const PathState& ps, int* q_closest, RoundCounters* rc, DevStats* st,
+                   cudaStream_t s);
+void launch_logic(const PassParams& pp, const PathState& ps, const int* in_closest, const int* in_any,
+                  const RoundCounters* rc_in, int* out_closest, int* out_any, RoundCounters* rc_out,
+                  DevStats* st, int grid, cudaStream_t s);
+int launch_trace(const DevScene& sc, bool any_hit, const int* queue, const int* count, int* work,
+                 const float4* ro, const float4* rd, float4* hit, DevStats* st, int grid_blocks,
+                 cudaStream_t s);
+void launch_tonemap(const float4* in, float4* out, int n, cudaStream_t s);
+// direct query: rays as 9 floats each
+int launch_trace_rays(const DevScene& sc, bool any_hit, const float* rays9, int n, int* tri_out, float* t_out,
+                      int* work, DevStats* st, cudaStream_t s);
+int trace_grid_blocks(bool any_hit, int depth);
+
+}  // namespace yc

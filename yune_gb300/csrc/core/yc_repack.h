@@ -1,0 +1,28 @@
+// yc_repack.h -- host-side repack of a scene into the device layout of yc_scene.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "yc_scene.h"
+
+namespace yc {
+
+struct Repacked {
+  std::vector<float4> nodes;   // 4 per interior node
+  std::vector<float4> tris;    // 3 per stream slot
+  std::vector<float4> shade;   // 4 per original triangle
+  int root_link = LINK_NONE;
+  int root_test = 0;
+  int depth = 0;
+  float4 root_lo{0, 0, 0, 0}, root_hi{0, 0, 0, 0};
+};
+
+// Returns 0, or -1 with a message when the node array is not a tree the reference
+// traversal could walk (child indices out of range, vert_len > 10, ...).
+int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, int n_node, Repacked& out,
+                 std::string& err);
+
+}  // namespace yc

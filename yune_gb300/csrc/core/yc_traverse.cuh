@@ -1,0 +1,217 @@
+// yc_traverse.cuh -- BVH traversal for sm_103a: while-while depth-first walk over the
+// repacked two-child nodes with a per-thread stack in shared memory.
+//
+// The tests themselves are the reference's, operation for operation, so the accepted
+// triangles and their t are bit-identical to traverseBVH + rayTriangleIntersection
+// (kernels/legacy/udpt.cl:288-390). What changes is the order of the walk: the
+// reference visits, breadth first, every box the ray's half-line crosses and keeps the
+// first triangle with the smallest t; here the nearer child is visited first and a
+// child is skipped once its entry distance lies beyond the closest hit found so far (by
+// a margin of 2^-10 relative, so rounding of the entry distance can never hide a
+// triangle the reference would accept). The closest t and its triangle are therefore
+// the reference's, except between triangles at exactly the same t, where the first one
+// visited wins in both walks and the walks differ in order.
+//
+// The translation unit is compiled with -fmad=false: no multiply-add is fused, as in
+// the reference arithmetic.
+#pragma once
+
+#include <stdint.h>
+
+#include "yc_scene.h"
+
+namespace yc {
+
+struct RayIn {
+  float ox, oy, oz, tmax;
+  float dx, dy, dz;
+};
+
+struct HitOut {
+  float t, u, v;
+  int tri;   // original triangle index, -1 when nothing closer than tmax
+};
+
+// OpenCL `min` (y if y < x, otherwise x); NaN-sensitive like the reference.
+__device__ __forceinline__ float ocl_min(float x, float y) { return (y < x) ? y : x; }
+// OpenCL `fmax` (NaN operand ignored; ties keep x).
+__device__ __forceinline__ float ocl_fmax(float x, float y) {
+  if (x != x) return y;
+  if (y != y) return x;
+  return (x < y) ? y : x;
+}
+
+// rayAabbIntersection (udpt.cl:392-431) exactly, for rays with a zero or subnormal
+// direction component (1/d = inf can make (p - o) * inv NaN, and the reference then
+// skips that axis). Returns hit and the entry distance.
+__device__ __forceinline__ bool box_ref(float ox, float oy, float oz, float ix, float iy, float iz,
+                                        float lx, float hx, float ly, float hy, float lz, float hz,
+                                        float& tentry) {
+  float t_max = __int_as_float(0x7f800000), t_min = -__int_as_float(0x7f800000);
+  float mn = __fmul_rn(__fsub_rn(lx, ox), ix), mx = __fmul_rn(__fsub_rn(hx, ox), ix);
+  if (!(mn != mn)) { t_min = ocl_fmax(ocl_min(mn, mx), t_min); t_max = ocl_min(ocl_fmax(mn, mx), t_max); }
+  mn = __fmul_rn(__fsub_rn(ly, oy), iy); mx = __fmul_rn(__fsub_rn(hy, oy), iy);
+  if (!(mn != mn)) { t_min = ocl_fmax(ocl_min(mn, mx), t_min); t_max = ocl_min(ocl_fmax(mn, mx), t_max); }
+  if (t_max < t_min) { tentry = t_min; return false; }
+  mn = __fmul_rn(__fsub_rn(lz, oz), iz); mx = __fmul_rn(__fsub_rn(hz, oz), iz);
+  if (!(mn != mn)) { t_min = ocl_fmax(ocl_min(mn, mx), t_min); t_max = ocl_min(ocl_fmax(mn, mx), t_max); }
+  tentry = t_min;
+  return t_max > ocl_fmax(t_min, 0.0f);
+}
+
+// The same test when every 1/d is finite: no operand can be NaN, so min/max are the
+// hardware FMNMX and the result (hit or not) equals the reference's.
+__device__ __forceinline__ bool box_fast(float ox, float oy, float oz, float ix, float iy, float iz,
+                                         float lx, float hx, float ly, float hy, float lz, float hz,
+                                         float& tentry) {
+  const float ax = __fmul_rn(__fsub_rn(lx, ox), ix), bx = __fmul_rn(__fsub_rn(hx, ox), ix);
+  const float ay = __fmul_rn(__fsub_rn(ly, oy), iy), by = __fmul_rn(__fsub_rn(hy, oy), iy);
+  const float az = __fmul_rn(__fsub_rn(lz, oz), iz), bz = __fmul_rn(__fsub_rn(hz, oz), iz);
+  const float t0 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fminf(az, bz));
+  const float t1 = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz));
+  tentry = t0;
+  return t1 > fmaxf(t0, 0.0f);
+}
+
+struct TriHit {
+  float t, u, v;
+};
+
+// rayTriangleIntersection (udpt.cl:326-390): Moller-Trumbore with the reference's
+// operation order; the `+ 0.0f` is the w-lane product of the float4 dot (0 * 0), which
+// only turns a -0 sum into +0, as the reference's four-lane dot does.
+__device__ __forceinline__ bool tri_test(float ox, float oy, float oz, float dx, float dy, float dz,
+                                         const float4& a, const float4& b, const float4& c, float best,
+                                         TriHit& out) {
+  // e1 = b.xyz, e2 = c.xyz, v1 = a.xyz
+  const float px = __fsub_rn(__fmul_rn(dy, c.z), __fmul_rn(dz, c.y));
+  const float py = __fsub_rn(__fmul_rn(dz, c.x), __fmul_rn(dx, c.z));
+  const float pz = __fsub_rn(__fmul_rn(dx, c.y), __fmul_rn(dy, c.x));
+  const float det = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(b.x, px), __fmul_rn(b.y, py)), __fmul_rn(b.z, pz)), 0.0f);
+  const float inv_det = __frcp_rn(det);
+  const float sx = __fsub_rn(ox, a.x), sy = __fsub_rn(oy, a.y), sz = __fsub_rn(oz, a.z);
+  const float u = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(px, sx), __fmul_rn(py, sy)), __fmul_rn(pz, sz)), 0.0f), inv_det);
+  if (u < 0.0f || u > 1.0f) return false;
+  const float qx = __fsub_rn(__fmul_rn(sy, b.z), __fmul_rn(sz, b.y));
+  const float qy = __fsub_rn(__fmul_rn(sz, b.x), __fmul_rn(sx, b.z));
+  const float qz = __fsub_rn(__fmul_rn(sx, b.y), __fmul_rn(sy, b.x));
+  const float v = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(qx, dx), __fmul_rn(qy, dy)), __fmul_rn(qz, dz)), 0.0f), inv_det);
+  if (v < 0.0f || __fadd_rn(u, v) > 1.0f) return false;
+  const float t = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(c.x, qx), __fmul_rn(c.y, qy)), __fmul_rn(c.z, qz)), 0.0f), inv_det);
+  if (t > 0.0f && t < best) {
+    out.t = t; out.u = u; out.v = v;
+    return true;
+  }
+  return false;
+}
+
+// Cull factor for the distance test: a child is skipped when its entry distance exceeds
+// the best t by more than 2^-10 relative.
+__device__ __forceinline__ float cull_bound(float best) { return best * 1.0009765625f; }
+
+// Walks the scene for one ray. ANY = true stops at the first accepted triangle (shadow
+// rays, udpt.cl:306-308). stack: this thread's column, stride `stride` ints. Returns
+// false when the stack bound was exceeded (the result is then incomplete).
+template <bool ANY>
+__device__ __forceinline__ bool traverse(const DevScene& sc, const RayIn& r, int* stack, int stride, int stack_cap,
+                                         HitOut& out) {
+  const float ox = r.ox, oy = r.oy, oz = r.oz;
+  const float dx = r.dx, dy = r.dy, dz = r.dz;
+  const float ix = __frcp_rn(dx), iy = __frcp_rn(dy), iz = __frcp_rn(dz);
+  const bool exact = isinf(ix) || isinf(iy) || isinf(iz);
+  float best = r.tmax;
+  int best_tri = -1;
+  float bu = 0.0f, bv = 0.0f;
+  out.tri = -1;
+  out.t = best;
+  out.u = out.v = 0.0f;
+
+  int link = sc.root_link;
+  if (link == LINK_NONE) return true;
+  if (sc.root_test) {
+    float te;
+    const bool h = exact ? box_ref(ox, oy, oz, ix, iy, iz, sc.root_lo.x, sc.root_hi.x, sc.root_lo.y, sc.root_hi.y,
+                                   sc.root_lo.z, sc.root_hi.z, te)
+                         : box_fast(ox, oy, oz, ix, iy, iz, sc.root_lo.x, sc.root_hi.x, sc.root_lo.y,
+                                    sc.root_hi.y, sc.root_lo.z, sc.root_hi.z, te);
+    if (!h) return true;
+  }
+  int sp = 0;
+  bool ok = true;
+  for (;;) {
+    // descend through interior nodes
+    while (link >= 0) {
+      const float4* nd = sc.nodes + 4 * (size_t)link;
+      const float4 n0 = __ldg(nd + 0);
+      const float4 n1 = __ldg(nd + 1);
+      const float4 n2 = __ldg(nd + 2);
+      const int2 n3 = __ldg(reinterpret_cast<const int2*>(nd + 3));
+      float t0, t1;
+      bool h0, h1;
+      if (!exact) {
+        h0 = box_fast(ox, oy, oz, ix, iy, iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, t0);
+        h1 = box_fast(ox, oy, oz, ix, iy, iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, t1);
+      } else {
+        h0 = box_ref(ox, oy, oz, ix, iy, iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, t0);
+        h1 = box_ref(ox, oy, oz, ix, iy, iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, t1);
+      }
+      const float cb = cull_bound(best);
+      h0 = h0 && n3.x != LINK_NONE && !(t0 > cb);
+      h1 = h1 && n3.y != LINK_NONE && !(t1 > cb);
+      if (h0 && h1) {
+        const bool swap = t1 < t0;
+        const int near_l = swap ? n3.y : n3.x, far_l = swap ? n3.x : n3.y;
+        const float far_t = swap ? t0 : t1;
+        if (sp >= stack_cap) { ok = false; link = LINK_NONE; break; }
+        stack[(2 * sp + 0) * stride] = far_l;
+        stack[(2 * sp + 1) * stride] = __float_as_int(far_t);
+        ++sp;
+        link = near_l;
+      } else if (h0) {
+        link = n3.x;
+      } else if (h1) {
+        link = n3.y;
+      } else {
+        link = LINK_NONE;
+        break;
+      }
+    }
+    // leaf: ~link = (first slot << 4) | count
+    if (link != LINK_NONE) {
+      const int enc = ~link;
+      const int count = enc & 15;
+      const float4* tp = sc.tris + 3 * (size_t)(enc >> 4);
+      for (int k = 0; k < count; ++k) {
+        const float4 a = __ldg(tp + 3 * k + 0);
+        const float4 b = __ldg(tp + 3 * k + 1);
+        const float4 c = __ldg(tp + 3 * k + 2);
+        TriHit th;
+        if (tri_test(ox, oy, oz, dx, dy, dz, a, b, c, best, th)) {
+          best = th.t;
+          bu = th.u;
+          bv = th.v;
+          best_tri = __float_as_int(a.w);
+          if (ANY) {
+            out.t = best; out.u = bu; out.v = bv; out.tri = best_tri;
+            return ok;
+          }
+        }
+      }
+    }
+    // pop the next subtree whose entry is still within reach
+    link = LINK_NONE;
+    while (sp > 0) {
+      --sp;
+      const float te = __int_as_float(stack[(2 * sp + 1) * stride]);
+      if (!(te > cull_bound(best))) { link = stack[(2 * sp) * stride]; break; }
+    }
+    if (link == LINK_NONE) break;
+  }
+  out.t = best;
+  out.u = bu;
+  out.v = bv;
+  out.tri = best_tri;
+  return ok;
+}
+
+}  // namespace yc

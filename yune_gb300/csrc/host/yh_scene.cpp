@@ -1,0 +1,243 @@
+// yh_scene.cpp -- seeded procedural scenes that stand in for Yune's OBJ/MTL input.
+//
+// The output is what Scene::loadModel produces (src/Scene.cpp:133-383): TriangleGPU
+// records with points at w = 1, normals at w = 0 and a material index, plus Material
+// records whose colours carry w = 1 (src/Scene.cpp:173-200). Lights are quads, the
+// form the reference kernels intersect analytically (kernels/legacy/udpt.cl:97-106).
+// Every random draw comes from std::mt19937_64 mapped to [0,1) by the top 53 bits, so
+// the same seed gives the same scene on every host.
+#include "yune_host.h"
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <new>
+#include <random>
+#include <utility>
+#include <vector>
+
+struct yh_scene {
+  std::vector<yc_triangle> tris;
+  std::vector<yc_material> mats;
+  std::vector<yc_quad_light> lights;
+};
+
+namespace {
+
+struct D3 { double x, y, z; };
+inline D3 operator+(D3 a, D3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline D3 operator-(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline D3 operator*(D3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+inline double dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline D3 cross(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline D3 unit(D3 a) { const double l = std::sqrt(dot(a, a)); return l > 0 ? a * (1.0 / l) : a; }
+
+inline double u01(std::mt19937_64& g) { return (double)(g() >> 11) * (1.0 / 9007199254740992.0); }
+
+yc_float4 pt(D3 p) { return yc_float4{(float)p.x, (float)p.y, (float)p.z, 1.0f}; }
+yc_float4 vec(D3 v) { return yc_float4{(float)v.x, (float)v.y, (float)v.z, 0.0f}; }
+
+yc_material base_material() {
+  yc_material m;
+  std::memset(&m, 0, sizeof(m));
+  m.ke = yc_float4{0, 0, 0, 1};
+  m.kd = yc_float4{0.3f, 0.3f, 0.3f, 1};
+  m.ks = yc_float4{0, 0, 0, 1};
+  m.n = 1; m.k = 1; m.px = 1; m.py = 1; m.alpha_x = 100; m.alpha_y = 100;   // newMaterial()
+  return m;
+}
+
+void push_tri(yh_scene* s, D3 a, D3 b, D3 c, D3 na, D3 nb, D3 nc, int mat) {
+  yc_triangle t;
+  std::memset(&t, 0, sizeof(t));
+  t.v1 = pt(a); t.v2 = pt(b); t.v3 = pt(c);
+  t.vn1 = vec(na); t.vn2 = vec(nb); t.vn3 = vec(nc);
+  t.matID = mat;
+  s->tris.push_back(t);
+}
+
+// quad a-b-c-d (counter-clockwise seen from the side the normal points to)
+void push_quad(yh_scene* s, D3 a, D3 b, D3 c, D3 d, D3 n, int mat) {
+  push_tri(s, a, b, c, n, n, n, mat);
+  push_tri(s, a, c, d, n, n, n, mat);
+}
+
+void push_box(yh_scene* s, D3 center, D3 half, double yaw, int mat) {
+  const double cy = std::cos(yaw), sy = std::sin(yaw);
+  auto xf = [&](D3 p) {   // rotate about +y then translate
+    return D3{cy * p.x + sy * p.z + center.x, p.y + center.y, -sy * p.x + cy * p.z + center.z};
+  };
+  auto xn = [&](D3 n) { return D3{cy * n.x + sy * n.z, n.y, -sy * n.x + cy * n.z}; };
+  const double hx = half.x, hy = half.y, hz = half.z;
+  D3 p[8] = {{-hx, -hy, -hz}, {hx, -hy, -hz}, {hx, hy, -hz}, {-hx, hy, -hz},
+             {-hx, -hy, hz},  {hx, -hy, hz},  {hx, hy, hz},  {-hx, hy, hz}};
+  for (auto& q : p) q = xf(q);
+  push_quad(s, p[4], p[5], p[6], p[7], xn({0, 0, 1}), mat);    // +z
+  push_quad(s, p[1], p[0], p[3], p[2], xn({0, 0, -1}), mat);   // -z
+  push_quad(s, p[5], p[1], p[2], p[6], xn({1, 0, 0}), mat);    // +x
+  push_quad(s, p[0], p[4], p[7], p[3], xn({-1, 0, 0}), mat);   // -x
+  push_quad(s, p[7], p[6], p[2], p[3], xn({0, 1, 0}), mat);    // +y
+  push_quad(s, p[0], p[1], p[5], p[4], xn({0, -1, 0}), mat);   // -y
+}
+
+// Unit icosphere: the 12 icosahedron vertices, faces found as the triples at the
+// edge length, then `level` midpoint subdivisions projected back to the sphere.
+void icosphere(int level, std::vector<D3>& v, std::vector<int>& f) {
+  const double phi = (1.0 + std::sqrt(5.0)) / 2.0;
+  v.clear(); f.clear();
+  for (int s1 = -1; s1 <= 1; s1 += 2)
+    for (int s2 = -1; s2 <= 1; s2 += 2) {
+      v.push_back(unit({(double)s1, s2 * phi, 0}));
+      v.push_back(unit({0, (double)s1, s2 * phi}));
+      v.push_back(unit({s2 * phi, 0, (double)s1}));
+    }
+  double min_d = 1e9;
+  for (size_t i = 0; i < v.size(); ++i)
+    for (size_t j = i + 1; j < v.size(); ++j) min_d = std::min(min_d, dot(v[i] - v[j], v[i] - v[j]));
+  auto adj = [&](int i, int j) { return std::fabs(dot(v[i] - v[j], v[i] - v[j]) - min_d) < 1e-9; };
+  for (int i = 0; i < 12; ++i)
+    for (int j = i + 1; j < 12; ++j)
+      for (int k = j + 1; k < 12; ++k)
+        if (adj(i, j) && adj(j, k) && adj(i, k)) {
+          D3 n = cross(v[j] - v[i], v[k] - v[i]);
+          if (dot(n, v[i] + v[j] + v[k]) > 0) { f.push_back(i); f.push_back(j); f.push_back(k); }
+          else { f.push_back(i); f.push_back(k); f.push_back(j); }
+        }
+  for (int l = 0; l < level; ++l) {
+    std::map<std::pair<int, int>, int> mid;
+    auto midpoint = [&](int i, int j) {
+      std::pair<int, int> key(std::min(i, j), std::max(i, j));
+      auto it = mid.find(key);
+      if (it != mid.end()) return it->second;
+      v.push_back(unit(v[i] + v[j]));
+      const int idx = (int)v.size() - 1;
+      mid.emplace(key, idx);
+      return idx;
+    };
+    std::vector<int> nf;
+    nf.reserve(f.size() * 4);
+    for (size_t t = 0; t < f.size(); t += 3) {
+      const int i = f[t], j = f[t + 1], k = f[t + 2];
+      const int ij = midpoint(i, j), jk = midpoint(j, k), ki = midpoint(k, i);
+      const int quad[12] = {i, ij, ki, ij, j, jk, ki, jk, k, ij, jk, ki};
+      nf.insert(nf.end(), quad, quad + 12);
+    }
+    f.swap(nf);
+  }
+}
+
+}  // namespace
+
+extern "C" int yh_scene_new(yh_scene** out) {
+  if (!out) return YH_E_INVALID;
+  *out = new (std::nothrow) yh_scene;
+  return *out ? YH_OK : YH_E_NOMEM;
+}
+extern "C" void yh_scene_free(yh_scene* s) { delete s; }
+
+extern "C" int yh_scene_add_material(yh_scene* s, const yc_material* m, int* mat_id) {
+  if (!s || !m) return YH_E_INVALID;
+  s->mats.push_back(*m);
+  if (mat_id) *mat_id = (int)s->mats.size() - 1;
+  return YH_OK;
+}
+
+extern "C" int yh_scene_add_light(yh_scene* s, const yc_quad_light* l) {
+  if (!s || !l) return YH_E_INVALID;
+  s->lights.push_back(*l);
+  return YH_OK;
+}
+
+extern "C" int yh_scene_add_cornell(yh_scene* s, uint64_t seed, float on_sigma2, float phong_exp,
+                                    float light_emission, int with_boxes) {
+  if (!s) return YH_E_INVALID;
+  std::mt19937_64 g(seed);
+  const int m0 = (int)s->mats.size();
+  yc_material white = base_material();
+  white.kd = yc_float4{0.73f, 0.73f, 0.73f, 1};
+  white.alpha_x = white.alpha_y = on_sigma2;
+  yc_material red = white;
+  red.kd = yc_float4{0.63f, 0.065f, 0.05f, 1};
+  yc_material green = white;
+  green.kd = yc_float4{0.14f, 0.45f, 0.091f, 1};
+  yc_material phong = base_material();
+  phong.kd = yc_float4{0.35f, 0.35f, 0.35f, 1};
+  phong.ks = yc_float4{0.45f, 0.45f, 0.45f, 1};
+  phong.px = phong_exp * 0.5f;
+  phong.py = phong_exp * 0.5f;
+  phong.alpha_x = phong.alpha_y = 0.0f;
+  s->mats.push_back(white);
+  s->mats.push_back(red);
+  s->mats.push_back(green);
+  s->mats.push_back(phong);
+  const int W = m0, R = m0 + 1, G = m0 + 2, P = m0 + 3;
+  const double h = 0.5;
+  push_quad(s, {-h, -h, -h}, {-h, -h, h}, {h, -h, h}, {h, -h, -h}, {0, 1, 0}, W);    // floor
+  push_quad(s, {-h, h, -h}, {h, h, -h}, {h, h, h}, {-h, h, h}, {0, -1, 0}, W);       // ceiling
+  push_quad(s, {-h, -h, -h}, {h, -h, -h}, {h, h, -h}, {-h, h, -h}, {0, 0, 1}, W);    // back
+  push_quad(s, {-h, -h, -h}, {-h, h, -h}, {-h, h, h}, {-h, -h, h}, {1, 0, 0}, R);    // left
+  push_quad(s, {h, -h, -h}, {h, -h, h}, {h, h, h}, {h, h, -h}, {-1, 0, 0}, G);       // right
+  const double yaw0 = (10.0 + 15.0 * u01(g)) * M_PI / 180.0;
+  const double yaw1 = -(10.0 + 15.0 * u01(g)) * M_PI / 180.0;
+  if (with_boxes) {
+    push_box(s, {-0.18, -0.2, -0.15}, {0.14, 0.3, 0.14}, yaw0, P);
+    push_box(s, {0.18, -0.36, 0.14}, {0.14, 0.14, 0.14}, yaw1, W);
+  }
+  yc_quad_light l;
+  std::memset(&l, 0, sizeof(l));
+  l.pos = yc_float4{-0.125f, 0.499f, -0.125f, 1.0f};
+  l.normal = yc_float4{0, -1, 0, 0};
+  l.ke = yc_float4{light_emission, light_emission, light_emission, 0};
+  l.edge_l = yc_float4{0.25f, 0, 0, 0};
+  l.edge_w = yc_float4{0, 0, 0.25f, 0};
+  s->lights.push_back(l);
+  return YH_OK;
+}
+
+extern "C" int yh_scene_add_icosphere(yh_scene* s, const float c[3], float r, int level, float disp,
+                                      uint64_t seed, int mat_id) {
+  if (!s || !c || level < 0 || level > 9 || !(r > 0)) return YH_E_INVALID;
+  try {
+    std::vector<D3> v;
+    std::vector<int> f;
+    icosphere(level, v, f);
+    std::mt19937_64 g(seed);
+    std::vector<D3> p(v.size()), n(v.size(), D3{0, 0, 0});
+    const D3 cc{c[0], c[1], c[2]};
+    for (size_t i = 0; i < v.size(); ++i) {
+      const double k = disp > 0 ? 1.0 + disp * (2.0 * u01(g) - 1.0) : 1.0;
+      p[i] = cc + v[i] * (r * k);
+    }
+    if (disp > 0) {
+      for (size_t t = 0; t < f.size(); t += 3) {
+        const D3 fn = cross(p[f[t + 1]] - p[f[t]], p[f[t + 2]] - p[f[t]]);   // area weighted
+        for (int q = 0; q < 3; ++q) n[f[t + q]] = n[f[t + q]] + fn;
+      }
+      for (auto& x : n) x = unit(x);
+    } else {
+      n = v;
+    }
+    s->tris.reserve(s->tris.size() + f.size() / 3);
+    for (size_t t = 0; t < f.size(); t += 3)
+      push_tri(s, p[f[t]], p[f[t + 1]], p[f[t + 2]], n[f[t]], n[f[t + 1]], n[f[t + 2]], mat_id);
+  } catch (const std::bad_alloc&) {
+    return YH_E_NOMEM;
+  }
+  return YH_OK;
+}
+
+extern "C" int yh_scene_counts(const yh_scene* s, int* n_tri, int* n_mat, int* n_light) {
+  if (!s) return YH_E_INVALID;
+  if (n_tri) *n_tri = (int)s->tris.size();
+  if (n_mat) *n_mat = (int)s->mats.size();
+  if (n_light) *n_light = (int)s->lights.size();
+  return YH_OK;
+}
+
+extern "C" int yh_scene_copy(const yh_scene* s, yc_triangle* tris, yc_material* mats, yc_quad_light* lights) {
+  if (!s) return YH_E_INVALID;
+  if (tris && !s->tris.empty()) std::memcpy(tris, s->tris.data(), s->tris.size() * sizeof(yc_triangle));
+  if (mats && !s->mats.empty()) std::memcpy(mats, s->mats.data(), s->mats.size() * sizeof(yc_material));
+  if (lights && !s->lights.empty()) std::memcpy(lights, s->lights.data(), s->lights.size() * sizeof(yc_quad_light));
+  return YH_OK;
+}

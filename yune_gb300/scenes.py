@@ -1,0 +1,185 @@
+"""Seeded procedural scenes and the render configurations built from them.
+
+These replace Yune's OBJ/MTL input (src/Scene.cpp:133-383) for headless runs. The
+geometry comes from the host producers in libyune_gb300.so (yh_scene_*), the BVH from
+yh_bvh_build (the node array of src/BVH.cpp:56-173) and the camera from yh_camera_look
+(src/Camera.cpp:66-117).
+
+Configurations (sizes and spp of the benchmark workloads):
+  c0  Cornell box: 5 walls (10 tris), two seeded-yaw boxes (24 tris), quad light
+      (emission 15) under the ceiling; walls Oren-Nayar sigma^2 = 0.09 (sigma 0.3), one
+      box modified Phong exponent 50; 512x512, 64 spp; NEE + MIS, roulette after
+      bounce 3; leaf <= 10, 20 bins.
+  c1  c0 plus a level-6 icosphere (81,920 tris, radius 0.35) of dielectric IOR 1.5;
+      leaf <= 4; 1024x1024, 256 spp, at most 16 bounces, roulette after bounce 3.
+"""
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as N
+from .layouts import BVH_NODE, CAM, MATERIAL, QUAD_LIGHT, TRIANGLE, ptr
+
+
+@dataclass
+class SceneData:
+    tris: np.ndarray
+    mats: np.ndarray
+    lights: np.ndarray
+    nodes: np.ndarray
+    depth: int
+    cam: np.ndarray
+    width: int
+    height: int
+    spp: int
+    cfg: dict = field(default_factory=dict)
+    name: str = ""
+
+    @property
+    def n_tri(self):
+        return len(self.tris)
+
+
+def default_cfg(**kw):
+    cfg = dict(integrator=0, mis=1, rr_threshold=3, max_depth=100000, brdf_model=1, mis_lobe_fix=1,
+               bdpt_bounces=20, block=0, block_x=1, block_y=1)
+    cfg.update(kw)
+    return cfg
+
+
+def material(kd=(0.3, 0.3, 0.3), ks=(0, 0, 0), ke=(0, 0, 0), n=1.0, px=1.0, py=1.0, alpha=100.0,
+             specular=0, transmissive=0):
+    m = np.zeros(1, MATERIAL)
+    m["ke"] = (*ke, 1.0)
+    m["kd"] = (*kd, 1.0)
+    m["ks"] = (*ks, 1.0)
+    m["n"] = n
+    m["k"] = 1.0
+    m["px"] = px
+    m["py"] = py
+    m["alpha_x"] = alpha
+    m["alpha_y"] = alpha
+    m["is_specular"] = specular
+    m["is_transmissive"] = transmissive
+    return m
+
+
+class Builder:
+    """Thin owner of a yh_scene handle."""
+
+    def __init__(self):
+        L = N.lib()
+        h = C.c_void_p()
+        N.check(L.yh_scene_new(C.byref(h)), "yh_scene_new")
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            N.lib().yh_scene_free(self.h)
+            self.h = None
+
+    def cornell(self, seed=0, sigma2=0.09, phong_exp=50.0, emission=15.0, boxes=True):
+        N.check(N.lib().yh_scene_add_cornell(self.h, seed, sigma2, phong_exp, emission, int(boxes)), "cornell")
+        return self
+
+    def add_material(self, m):
+        mid = C.c_int()
+        N.check(N.lib().yh_scene_add_material(self.h, ptr(m), C.byref(mid)), "material")
+        return mid.value
+
+    def icosphere(self, center, radius, level, mat_id, disp=0.0, seed=0):
+        c = np.asarray(center, np.float32)
+        N.check(N.lib().yh_scene_add_icosphere(self.h, ptr(c), radius, level, disp, seed, mat_id), "icosphere")
+        return self
+
+    def add_light(self, l):
+        N.check(N.lib().yh_scene_add_light(self.h, ptr(l)), "light")
+        return self
+
+    def arrays(self):
+        nt, nm, nl = C.c_int(), C.c_int(), C.c_int()
+        L = N.lib()
+        N.check(L.yh_scene_counts(self.h, C.byref(nt), C.byref(nm), C.byref(nl)), "counts")
+        tris = np.zeros(nt.value, TRIANGLE)
+        mats = np.zeros(nm.value, MATERIAL)
+        lights = np.zeros(nl.value, QUAD_LIGHT)
+        N.check(L.yh_scene_copy(self.h, ptr(tris), ptr(mats), ptr(lights)), "copy")
+        return tris, mats, lights
+
+
+def build_bvh(tris, bins=20, leaf=10):
+    """Node array of BVH::createBVH for these triangles, and the tree depth."""
+    L = N.lib()
+    h = C.c_void_p()
+    N.check(L.yh_bvh_build(ptr(tris), len(tris), bins, leaf, C.byref(h)), "yh_bvh_build")
+    try:
+        n = L.yh_bvh_node_count(h)
+        nodes = np.zeros(n, BVH_NODE)
+        N.check(L.yh_bvh_copy_nodes(h, ptr(nodes), n), "copy nodes")
+        depth = L.yh_bvh_depth(h)
+    finally:
+        L.yh_bvh_free(h)
+    return nodes, depth
+
+
+def camera(eye=(0.0, 0.0, 1.4), side=(1.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), look=(0.0, 0.0, -1.0), fov=60.0):
+    cam = np.zeros(1, CAM)
+    a = [np.asarray(v, np.float32) for v in (eye, side, up, look)]
+    N.check(N.lib().yh_camera_look(ptr(a[0]), ptr(a[1]), ptr(a[2]), ptr(a[3]), fov, ptr(cam)), "camera")
+    return cam
+
+
+def dielectric(ior=1.5, r0=0.04):
+    return material(kd=(0, 0, 0), ks=(r0, r0, r0), n=ior, specular=1, transmissive=1, alpha=0.0)
+
+
+def c0(width=512, height=512, spp=64, seed=0):
+    b = Builder().cornell(seed=seed)
+    tris, mats, lights = b.arrays()
+    nodes, depth = build_bvh(tris, 20, 10)
+    return SceneData(tris, mats, lights, nodes, depth, camera(), width, height, spp,
+                     default_cfg(max_depth=100000), "c0")
+
+
+def c1(width=1024, height=1024, spp=256, seed=0, level=6):
+    b = Builder().cornell(seed=seed)
+    glass = b.add_material(dielectric(1.5))
+    b.icosphere((0.0, 0.0, 0.0), 0.35, level, glass)
+    tris, mats, lights = b.arrays()
+    nodes, depth = build_bvh(tris, 20, 4)
+    return SceneData(tris, mats, lights, nodes, depth, camera(), width, height, spp, default_cfg(max_depth=16), "c1")
+
+
+CONFIGS = {"c0": c0, "c1": c1}
+
+
+def pass_seeds(seed, n):
+    """Per-pass `rand` values: the first n outputs of std::mt19937(seed), which is what
+    uniform_int_distribution<unsigned>(0, UINT_MAX) over mt19937 returns
+    (src/RendererCore.cpp:61-63, 268)."""
+    return mt19937(seed, n)
+
+
+def mt19937(seed, n):
+    """First n outputs of the 32-bit Mersenne Twister (Matsumoto and Nishimura 1998)."""
+    mt = [0] * 624
+    mt[0] = seed & 0xFFFFFFFF
+    for i in range(1, 624):
+        mt[i] = (1812433253 * (mt[i - 1] ^ (mt[i - 1] >> 30)) + i) & 0xFFFFFFFF
+    idx = 624
+    out = []
+    for _ in range(n):
+        if idx >= 624:
+            for i in range(624):
+                y = (mt[i] & 0x80000000) | (mt[(i + 1) % 624] & 0x7FFFFFFF)
+                mt[i] = mt[(i + 397) % 624] ^ (y >> 1) ^ (0x9908B0DF if y & 1 else 0)
+            idx = 0
+        y = mt[idx]
+        idx += 1
+        y ^= y >> 11
+        y ^= (y << 7) & 0x9D2C5680
+        y ^= (y << 15) & 0xEFC60000
+        y ^= y >> 18
+        out.append(y & 0xFFFFFFFF)
+    return np.array(out, dtype=np.uint32)
