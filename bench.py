@@ -1,0 +1,306 @@
+"""Benchmark of the path-tracing core on the plain per-frame path.
+
+Workload (one step = one render pass = one sample per pixel over the frame, the
+per-pass contract of src/RendererCore.cpp:248-469): the glass-icosphere Cornell box
+(81,954 triangles, SAH BVH with leaf <= 4), 1024x1024, NEE + MIS, roulette after bounce
+3, at most 16 bounces; synthetic seeded scene, per-pass seeds from mt19937(0).
+
+Printed (one JSON line on rank 0):
+  value        Mrays/s over the timed passes: every traceRay-equivalent query (primary,
+               extension, NEE shadow, MIS) / device time of the passes (CUDA events on the
+               context stream), inputs resident in HBM, L2 flushed between passes
+  e2e          the same metric through the C-ABI with host buffers: per pass the camera
+               block goes host -> device and the tonemapped frame comes back
+  roofline     the extend (closest-hit) kernel: algorithmic bytes (32 B per box test,
+               48 B per triangle test, 52 B of ray/hit records per ray) / its event time,
+               against the measured L2 read bandwidth (the node + triangle set, ~9 MB,
+               stays in L2); hbm_frac against MEASURED_PEAKS.json's HBM copy bandwidth
+  cpu_baseline the reference kernel source compiled as C++ (oracle/_ref), all host
+               threads, on a band of rows of the same frame
+`--impl reference` times that CPU reference alone on the same workload.
+With torchrun (N > 1) every rank renders its own replica (the work does not exchange
+data; multi-GPU is replicas only) and the value is the sum of the ranks' rays over the
+slowest rank's time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=64)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c1")
+    ap.add_argument("--e2e-steps", type=int, default=8)
+    ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return rank, local, ws, dist
+    return rank, local, ws, None
+
+
+def peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def scene_for(name):
+    from yune_gb300 import scenes
+    return scenes.CONFIGS[name]()
+
+
+def cpu_reference(scene, seeds, seconds, want_rays=True):
+    """Times the reference kernel source (compiled as C++) on bands of rows of the frame
+    with all host threads; rays counted by the oracle on the same band (same algorithm,
+    bit-identical results). Falls back to the oracle port when the compiled reference is
+    not available."""
+    from oracle import oracle_py as O
+    W, H = scene.width, scene.height
+    cfg = scene.cfg
+    threads = os.cpu_count() or 1
+    use_ref = O.ref() is not None and cfg.get("brdf_model", 0) == 0 and not cfg.get("mis_lobe_fix", 0)
+    kind = "reference" if use_ref else "port"
+    acc = np.zeros((H, W, 4), np.float32)
+    band = max(1, H // 64)
+    rows_done, t_total, rays = 0, 0.0, 0
+    y = 0
+    k = 0
+    while t_total < seconds and y < H:
+        r = (y, min(H, y + band))
+        t0 = time.perf_counter()
+        if use_ref:
+            O.ref_render(scene, acc, seeds[k % len(seeds)], 1, "udpt_mis" if cfg["mis"] else "udpt_a",
+                         cfg["rr_threshold"], cfg["max_depth"], threads=threads, rows=r)
+        else:
+            c = O.render(scene, acc, seeds[k % len(seeds)], 1, cfg, threads=threads, rows=r)
+        dt = time.perf_counter() - t0
+        t_total += dt
+        if use_ref and want_rays:
+            acc2 = np.zeros_like(acc)
+            c = O.render(scene, acc2, seeds[k % len(seeds)], 1, cfg, threads=threads, rows=r)
+        rays += c["rays"]
+        rows_done += r[1] - r[0]
+        y = r[1]
+    value = rays / t_total / 1e6 if t_total > 0 else 0.0
+    return {"value": value, "unit": METRIC, "cores": threads, "kind": kind,
+            "sample": "%d of %d rows x %d px, 1 pass, %.1f s" % (rows_done, H, W, t_total),
+            "samples_per_s": rows_done * W / t_total if t_total > 0 else 0.0}
+
+
+def run_reference(args, rank, ws, dist):
+    scene = scene_for(args.config)
+    from yune_gb300 import scenes
+    seeds = scenes.pass_seeds(0, args.steps + args.warmup)
+    if rank != 0:
+        return
+    cb = cpu_reference(scene, seeds, args.cpu_seconds)
+    cfg = {"workload": "%s: %d tris, %dx%d, cfg %s" % (args.config, scene.n_tri, scene.width, scene.height,
+                                                      json.dumps(scene.cfg, sort_keys=True)),
+           "spp_total": scene.spp}
+    line = {"metric": METRIC, "value": cb["value"], "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32", "data": "synthetic", "config": cfg,
+            "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": METRIC, "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args, rank, local, ws, dist):
+    from yune_gb300 import scenes
+    from yune_gb300.core import Renderer
+    scene = scene_for(args.config)
+    seeds = scenes.pass_seeds(0, args.warmup + args.steps + args.e2e_steps)
+    W, H = scene.width, scene.height
+    r = Renderer(local)
+    sid = r.upload(scene)
+    r.set_camera(scene.cam)
+    aid = r.alloc_accum(W, H)
+    l2 = r.measure_l2_gbs(48 << 20, 20)
+    # warm-up
+    for k in range(args.warmup):
+        r.render(sid, aid, seeds[k], reset=1 if k == 0 else 0, cfg=scene.cfg)
+    r.synchronize()
+    r.reset_stats()
+    r.set_profiling(True)
+    if dist:
+        dist.barrier()
+    ms_total = 0.0
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            r.flush_l2(256 << 20)
+            r.render(sid, aid, seeds[args.warmup + k], reset=0, cfg=scene.cfg)
+            ms_total += r.last_pass_ms()
+    r.synchronize()
+    st = r.stats()
+    kt = r.kernel_times()
+    r.set_profiling(False)
+    # e2e through the C-ABI with host buffers: camera in, tonemapped frame out
+    ldr = None
+    t0 = time.perf_counter()
+    for k in range(args.e2e_steps):
+        r.set_camera(scene.cam)
+        r.render(sid, aid, seeds[args.warmup + args.steps + k], reset=0, cfg=scene.cfg)
+        ldr = r.tonemap(aid)
+    e2e_s = time.perf_counter() - t0
+    e2e_stats = r.stats()
+    e2e_rays = e2e_stats["rays"] - st["rays"]
+    img = r.read_accum(aid)
+    rays = st["rays"]
+    t_s = ms_total / 1e3
+    if dist:
+        import torch
+        tt = torch.tensor([t_s, float(rays), e2e_s, float(e2e_rays)], dtype=torch.float64)
+        mx = tt.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = tt.clone()
+        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        t_s, e2e_s = mx[0].item(), mx[2].item()
+        rays, e2e_rays = sm[1].item(), sm[3].item()
+    if rank != 0:
+        r.close()
+        return
+    pk, pk_kind = peaks()
+    ext_bytes = 64.0 * st["ext_nodes"] + 48.0 * st["ext_tris"] + 32.0 * st["ext_rays"] + 52.0 * st["ext_rays"]
+    ext_ms = kt["extend_ms"]
+    achieved = ext_bytes / (ext_ms / 1e3) / 1e9 if ext_ms > 0 else 0.0
+    launches = int(kt["raygen_launches"] + kt["extend_launches"] + kt["occlusion_launches"] + kt["logic_launches"])
+    traffic = None
+    prof_file = os.path.join(ROOT, "profiles", "extend_traffic.json")
+    if os.path.exists(prof_file):
+        with open(prof_file) as f:
+            tr = json.load(f)
+        if tr.get("config") == args.config and kt["extend_launches"]:
+            traffic = tr.get("dram_bytes_per_launch")
+    samples = st["samples"]
+    line = {
+        "metric": METRIC, "value": rays / t_s / 1e6, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": "%s: glass icosphere Cornell box, %d tris, %dx%d, 1 spp per step, NEE+MIS, RR after "
+                               "bounce 3, max depth %d" % (args.config, scene.n_tri, W, H, scene.cfg["max_depth"]),
+                   "spp_total": scene.spp, "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "samples_per_s": samples / t_s * (ws if dist else 1),
+        "rays_per_sample": st["rays"] / max(1, samples),
+        "traversed_rays": st["traversed"],
+        "gpu_launches": launches,
+        "kernel_ms": {"raygen": kt["raygen_ms"], "extend": kt["extend_ms"], "occlusion": kt["occlusion_ms"],
+                      "logic": kt["logic_ms"], "rounds": kt["rounds"]},
+        "roofline": {"kernel": "k_trace_paths<false> (extend)", "bound": "l2", "achieved": achieved,
+                     "peak": l2, "unit": "GB/s", "frac": achieved / l2 if l2 else None, "traffic": traffic,
+                     "peak_source": "measured L2 read bandwidth (yc_measure_l2_gbs, 48 MB x 20 sweeps)",
+                     "hbm_peak": pk.get("hbm_gbs"), "hbm_frac": achieved / pk.get("hbm_gbs", 1.0),
+                     "hbm_peak_source": pk_kind,
+                     "bytes_per_ray": ext_bytes / max(1, st["ext_rays"]),
+                     "box_tests_per_ray": 2.0 * st["ext_nodes"] / max(1, st["ext_rays"]),
+                     "tri_tests_per_ray": st["ext_tris"] / max(1, st["ext_rays"])},
+        "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else 0.0, "unit": METRIC,
+                "h2d_bytes_per_step": 80 + 4, "d2h_bytes_per_step": W * H * 16,
+                "steps": args.e2e_steps},
+        "clocks": clk.summary(),
+        "stack_overflow": st["stack_overflow"],
+        "image_mean": float(np.nanmean(img[..., :3])),
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_reference(scene, seeds, args.cpu_seconds)
+    r.close()
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    rank, local, ws, dist = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, rank, ws, dist)
+    else:
+        run_ours(args, rank, local, ws, dist)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -71,7 +71,20 @@ typedef struct yc_stats {
   uint64_t traversed;       /* queries that walked the BVH */
   uint64_t samples;         /* pixel paths completed */
   uint64_t stack_overflow;  /* traversals that hit the stack bound (must be 0) */
+  /* work of the traversal kernels: rays walked, two-child nodes fetched (2 box tests,
+   * 64 B each) and triangles tested (48 B each), for the closest-hit (extend) and the
+   * any-hit (occlusion) kernel */
+  uint64_t ext_rays, ext_nodes, ext_tris;
+  uint64_t any_rays, any_nodes, any_tris;
 } yc_stats;
+
+/* Device time per kernel kind, summed over launches since the last reset, when
+ * profiling is on (CUDA events around each launch on the context stream). */
+typedef struct yc_kernel_times {
+  double raygen_ms, extend_ms, occlusion_ms, logic_ms;
+  uint64_t raygen_launches, extend_launches, occlusion_launches, logic_launches;
+  uint64_t rounds;
+} yc_kernel_times;
 
 typedef struct yc_ctx yc_ctx;
 
@@ -139,6 +152,15 @@ int yc_reset_stats(yc_ctx* ctx);
 /* Wall time of the device work of the last yc_render_pass(es) call, in ms (CUDA
  * events on the context stream). */
 int yc_last_pass_ms(yc_ctx* ctx, float* ms);
+/* Per-kernel event timing of yc_render_pass(es) (off by default). */
+int yc_set_profiling(yc_ctx* ctx, int on);
+int yc_get_kernel_times(yc_ctx* ctx, yc_kernel_times* out);
+/* Writes `bytes` of scratch memory on the context stream (evicts L2 between timed
+ * passes; benchmark hygiene). */
+int yc_flush_l2(yc_ctx* ctx, size_t bytes);
+/* Measured L2 read bandwidth in GB/s: `iters` sweeps of a `bytes` buffer (below the L2
+ * size) with 128-bit loads; the roofline denominator of the traversal kernels. */
+int yc_measure_l2_gbs(yc_ctx* ctx, size_t bytes, int iters, double* gbs);
 
 #ifdef __cplusplus
 }

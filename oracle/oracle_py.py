@@ -66,7 +66,7 @@ def ref():
         if path and os.path.exists(path):
             L = C.CDLL(path)
             L.ref_render.argtypes = [i32, vp, i32, vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, u32, i32, i32, i32, i32,
-                                     i32]
+                                     i32, i32, i32]
             L.ref_trace.argtypes = [vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, vp, vp]
             L.ref_tonemap.argtypes = [vp, i32, i32, vp]
             L.ref_oren_nayar.argtypes = [vp, vp, vp, vp, vp, vp]
@@ -132,12 +132,14 @@ def tonemap(accum):
 VARIANT = {"udpt_a": 0, "udpt_mis": 1, "udpt_mis4": 2, "bdpt20": 10, "bdpt8": 11, "bdpt8_l4": 12}
 
 
-def ref_render(scene, accum, rand_seed, reset, variant, rr_threshold, max_depth, gi_check=1, threads=0):
+def ref_render(scene, accum, rand_seed, reset, variant, rr_threshold, max_depth, gi_check=1, threads=0, rows=None):
     L = ref()
     H, W = accum.shape[:2]
+    r0, r1 = rows if rows else (0, 0)
     rc = L.ref_render(VARIANT[variant], _p(scene.tris), len(scene.tris), _p(scene.mats), len(scene.mats),
                       _p(scene.nodes), len(scene.nodes), _p(scene.lights), len(scene.lights), _p(scene.cam), W, H,
-                      _p(accum), int(rand_seed) & 0xFFFFFFFF, reset, gi_check, rr_threshold, max_depth, threads)
+                      _p(accum), int(rand_seed) & 0xFFFFFFFF, reset, gi_check, rr_threshold, max_depth, threads, r0,
+                      r1)
     if rc != 0:
         raise RuntimeError("ref_render failed: %d" % rc)
 

@@ -139,9 +139,9 @@ template <class K> void set_normal_bdpt(K* dst, int cap, const yc_quad_light* l,
 }
 
 template <class Fn>
-void parallel_rows(int H, int threads, Fn fn) {
+void parallel_rows(int row0, int H, int threads, Fn fn) {
   if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
-  std::atomic<int> next(0);
+  std::atomic<int> next(row0);
   auto work = [&]() {
     for (;;) {
       const int y = next.fetch_add(1);
@@ -169,7 +169,7 @@ static_assert(sizeof(yref::udpt_a::Camera) == sizeof(yc_cam), "Camera");
     set_lights(light_sources, kLights, l, nl);                                                        \
     SETN(light_sources, kLights, l, nl);                                                              \
     yref::image2d_t img{reinterpret_cast<yref::float4*>(accum), W, H};                                \
-    parallel_rows(H, threads, [&](int y) {                                                            \
+    parallel_rows(row0, row1, threads, [&](int y) {                                                            \
       for (int x = 0; x < W; ++x) {                                                                   \
         yref::tl_gid[0] = (size_t)x;                                                                  \
         yref::tl_gid[1] = (size_t)y;                                                                  \
@@ -181,14 +181,16 @@ static_assert(sizeof(yref::udpt_a::Camera) == sizeof(yc_cam), "Camera");
 
 extern "C" {
 
-// One pass of the reference `pathtracer` kernel over a W x H RGBA32F accumulator,
-// updated in place. variant: 0 udpt_a, 1 udpt_mis, 2 udpt_mis4, 10 bdpt20, 11 bdpt8,
+// One pass of the reference `pathtracer` kernel over rows [row0, row1) of a W x H
+// RGBA32F accumulator, updated in place (row1 <= row0: the whole image). variant: 0 udpt_a, 1 udpt_mis, 2 udpt_mis4, 10 bdpt20, 11 bdpt8,
 // 12 bdpt8_l4.
 int ref_render(int variant, const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_bvh_node* b,
                int nb, const yc_quad_light* l, int nl, const yc_cam* cam, int W, int H, float* accum,
-               uint32_t rand_, int reset, int gi_check, int rr_threshold, int max_depth, int threads) {
+               uint32_t rand_, int reset, int gi_check, int rr_threshold, int max_depth, int threads, int row0,
+               int row1) {
   (void)nm;
   if (!cam || !accum || W <= 0 || H <= 0 || !l) return -1;
+  if (row1 <= row0) { row0 = 0; row1 = H; }
   yref::yref_rr_threshold = rr_threshold;
   yref::yref_max_depth = max_depth;
   switch (variant) {

@@ -1,0 +1,103 @@
+"""Generates the golden fixtures in this directory from Yune's own code, compiled as C++
+by oracle/build_oracle.py (needs the reference tree; run where it is present):
+
+    python tests/golden/make_golden.py
+
+The fixtures pin the CPU oracle and the host producers on machines without the
+reference tree:
+  bvh_<scene>.npz      BVH::createBVH node arrays (src/BVH.cpp) for the scene's triangles
+  trace_<scene>.npz    traceRay (kernels/legacy/udpt.cl:240-286) on seeded rays
+                       (oracle_py.seeded_rays(scene, 4096, seed=5)) and on the segments
+                       ending just past each closest hit (shadow rays)
+  render_c0.npz        3 passes of `pathtracer` (udpt.cl as shipped, and with -DMIS
+                       RR_THRESHOLD 3) on a 32x24 Cornell box, plus `tonemap`
+                       (kernels/post-proc/tonemap.cl) of the MIS accumulator
+  oren_nayar.npz       OrenNayarBRDF (kernels/legacy/udpt-primitives.cl:696-725)
+Each file records a SHA-256 of the scene arrays it was made from.
+"""
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle_py as O  # noqa: E402
+from yune_gb300 import scenes  # noqa: E402
+from yune_gb300.layouts import MATERIAL  # noqa: E402
+
+
+def scene_hash(s):
+    h = hashlib.sha256()
+    for a in (s.tris, s.mats, s.lights, s.cam):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def golden_scenes():
+    return {"c0": scenes.c0(32, 24), "c1l3": scenes.c1(32, 24, level=3)}
+
+
+def node_fields(nodes):
+    return dict(p_min=nodes["p_min"][:, :3].copy(), p_max=nodes["p_max"][:, :3].copy(),
+                child_idx=nodes["child_idx"].copy(), vert_len=nodes["vert_len"].copy(),
+                vert_list=np.where(np.arange(10)[None, :] < np.maximum(nodes["vert_len"], 0)[:, None],
+                                   nodes["vert_list"], -1).astype(np.int32))
+
+
+def main():
+    if O.ref() is None:
+        raise SystemExit("the compiled reference is not available here")
+    for name, s in golden_scenes().items():
+        leaf = 10 if name == "c0" else 4
+        nodes = O.ref_bvh(s.tris, 20, leaf)
+        np.savez_compressed(os.path.join(HERE, "bvh_%s.npz" % name), scene_sha256=scene_hash(s), bins=20, leaf=leaf,
+                            **node_fields(nodes))
+        rays = O.seeded_rays(s, 4096, seed=5)
+        tri, light, t = O.ref_trace(s, rays)
+        seg = rays.copy()
+        seg[:, 8] = np.where(np.isfinite(t), t * np.float32(1.001), np.float32(0.6))
+        occ_tri, occ_light, _ = O.ref_trace(s, seg, any_hit=True)
+        np.savez_compressed(os.path.join(HERE, "trace_%s.npz" % name), scene_sha256=scene_hash(s), ray_seed=5,
+                            n_rays=4096, tri=tri, light=light, t=t, occluded=((occ_tri >= 0) | (occ_light >= 0)))
+    s = golden_scenes()["c0"]
+    seeds = scenes.pass_seeds(2024, 3)
+    out = {}
+    for variant, rr in (("udpt_a", 6), ("udpt_mis", 3)):
+        acc = np.zeros((24, 32, 4), np.float32)
+        for k, sd in enumerate(seeds):
+            O.ref_render(s, acc, sd, 1 if k == 0 else 0, variant, rr, 100000)
+        out[variant] = acc
+    out["tonemap_mis"] = O.ref_tonemap(out["udpt_mis"])
+    np.savez_compressed(os.path.join(HERE, "render_c0.npz"), scene_sha256=scene_hash(s), seeds=seeds, **out)
+    # Oren-Nayar on random frames
+    rng = np.random.default_rng(9)
+    n = 256
+    nrm = rng.normal(size=(n, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    wi = rng.normal(size=(n, 3))
+    wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+    wo = rng.normal(size=(n, 3))
+    wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+    hp = rng.uniform(-0.5, 0.5, size=(n, 3))
+    m = np.zeros(1, MATERIAL)
+    m["kd"] = (0.63, 0.065, 0.05, 1.0)
+    m["alpha_x"] = 0.09
+    f4 = lambda v, w: np.concatenate([v, np.full((n, 1), w)], axis=1).astype(np.float32)  # noqa: E731
+    NRM, WI, WO, HP = f4(nrm, 0.0), f4(wi, 0.0), f4(wo, 0.0), f4(hp, 1.0)
+    res = np.zeros((n, 4), np.float32)
+    for i in range(n):
+        o = np.zeros(4, np.float32)
+        O.ref().ref_oren_nayar(m.ctypes.data, HP[i].ctypes.data, NRM[i].ctypes.data, WI[i].ctypes.data,
+                               WO[i].ctypes.data, o.ctypes.data)
+        res[i] = o
+    np.savez_compressed(os.path.join(HERE, "oren_nayar.npz"), material=m, normal=NRM, w_i=WI, w_o=WO, hit_point=HP,
+                        value=res)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -25,7 +25,15 @@ class PassCfg(C.Structure):
 class Stats(C.Structure):
     """yc_stats"""
     _fields_ = [(n, C.c_uint64) for n in ("rays", "primary", "extension", "shadow", "mis", "connection",
-                                          "traversed", "samples", "stack_overflow")]
+                                          "traversed", "samples", "stack_overflow", "ext_rays", "ext_nodes",
+                                          "ext_tris", "any_rays", "any_nodes", "any_tris")]
+
+
+class KernelTimes(C.Structure):
+    """yc_kernel_times"""
+    _fields_ = [("raygen_ms", C.c_double), ("extend_ms", C.c_double), ("occlusion_ms", C.c_double),
+                ("logic_ms", C.c_double), ("raygen_launches", C.c_uint64), ("extend_launches", C.c_uint64),
+                ("occlusion_launches", C.c_uint64), ("logic_launches", C.c_uint64), ("rounds", C.c_uint64)]
 
 
 # name -> (restype, argtypes)
@@ -53,6 +61,10 @@ SIGNATURES = {
     "yc_get_stats": (i32, [vp, C.POINTER(Stats)]),
     "yc_reset_stats": (i32, [vp]),
     "yc_last_pass_ms": (i32, [vp, C.POINTER(f32)]),
+    "yc_set_profiling": (i32, [vp, i32]),
+    "yc_get_kernel_times": (i32, [vp, C.POINTER(KernelTimes)]),
+    "yc_flush_l2": (i32, [vp, C.c_size_t]),
+    "yc_measure_l2_gbs": (i32, [vp, C.c_size_t, i32, C.POINTER(C.c_double)]),
     # host producers
     "yh_bvh_build": (i32, [vp, i32, i32, i32, C.POINTER(vp)]),
     "yh_bvh_node_count": (i32, [vp]),

@@ -120,5 +120,21 @@ class Renderer:
         N.check(self.L.yc_last_pass_ms(self.h, C.byref(ms)), "yc_last_pass_ms")
         return ms.value
 
+    def set_profiling(self, on=True):
+        N.check(self.L.yc_set_profiling(self.h, int(on)), "yc_set_profiling")
+
+    def kernel_times(self):
+        k = N.KernelTimes()
+        N.check(self.L.yc_get_kernel_times(self.h, C.byref(k)), "yc_get_kernel_times")
+        return {n: getattr(k, n) for n, _ in N.KernelTimes._fields_}
+
+    def flush_l2(self, nbytes=256 << 20):
+        N.check(self.L.yc_flush_l2(self.h, nbytes), "yc_flush_l2")
+
+    def measure_l2_gbs(self, nbytes=48 << 20, iters=20):
+        g = C.c_double()
+        N.check(self.L.yc_measure_l2_gbs(self.h, nbytes, iters, C.byref(g)), "yc_measure_l2_gbs")
+        return g.value
+
     def synchronize(self):
         N.check(self.L.yc_synchronize(self.h), "yc_synchronize")

@@ -66,6 +66,7 @@ struct Scene {
 
 struct Accum {
   DevBuf<float4> buf;
+  DevBuf<float4> ldr;   // tonemapped image
   int w = 0, h = 0;
 };
 
@@ -91,6 +92,13 @@ struct yc_ctx {
   int logic_grid = 0;
   int sm_count = 0;
   float last_ms = 0.0f;
+  // per-kernel event timing
+  bool profile = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<std::pair<int, size_t>> ev_marks;   // kind, index of the start event
+  yc_kernel_times ktimes{};
+  DevBuf<char> flush_buf;
   // direct queries
   DevBuf<float> q_rays;
   DevBuf<int> q_tri;
@@ -107,6 +115,53 @@ int ensure_paths(yc_ctx* c, size_t n) {
   for (auto& b : c->q) YC_CUDA(b.alloc(n));
   c->cap_paths = n;
   return 0;
+}
+
+// event pairs around kernel launches (profiling only)
+enum { K_RAYGEN = 0, K_EXTEND = 1, K_OCCL = 2, K_LOGIC = 3 };
+cudaEvent_t next_event(yc_ctx* c) {
+  if (c->ev_used == c->ev_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    c->ev_pool.push_back(e);
+  }
+  return c->ev_pool[c->ev_used++];
+}
+struct KTimer {
+  yc_ctx* c;
+  int kind;
+  size_t idx = 0;
+  bool on;
+  KTimer(yc_ctx* c_, int k) : c(c_), kind(k), on(c_->profile) {
+    if (!on) return;
+    idx = c->ev_used;
+    cudaEvent_t e = next_event(c);
+    if (!e) { on = false; return; }
+    cudaEventRecord(e, c->stream);
+  }
+  ~KTimer() {
+    if (!on) return;
+    cudaEvent_t e = next_event(c);
+    if (!e) return;
+    cudaEventRecord(e, c->stream);
+    c->ev_marks.emplace_back(kind, idx);
+  }
+};
+void collect_events(yc_ctx* c) {
+  if (c->ev_marks.empty()) { c->ev_used = 0; return; }
+  cudaStreamSynchronize(c->stream);
+  for (auto& m : c->ev_marks) {
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, c->ev_pool[m.second], c->ev_pool[m.second + 1]);
+    switch (m.first) {
+      case K_RAYGEN: c->ktimes.raygen_ms += ms; c->ktimes.raygen_launches++; break;
+      case K_EXTEND: c->ktimes.extend_ms += ms; c->ktimes.extend_launches++; break;
+      case K_OCCL: c->ktimes.occlusion_ms += ms; c->ktimes.occlusion_launches++; break;
+      default: c->ktimes.logic_ms += ms; c->ktimes.logic_launches++; break;
+    }
+  }
+  c->ev_marks.clear();
+  c->ev_used = 0;
 }
 
 yc::PathState path_state(yc_ctx* c) {
@@ -174,7 +229,10 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
   const yc::PathState ps = path_state(c);
   yc::RoundCounters* rc = c->rc.p;
   YC_CUDA(cudaMemsetAsync(rc, 0, 2 * sizeof(yc::RoundCounters), c->stream));
-  yc::launch_raygen(pp, ps, c->q[0].p, rc + 0, c->stats.p, c->stream);
+  {
+    KTimer kt(c, K_RAYGEN);
+    yc::launch_raygen(pp, ps, c->q[0].p, rc + 0, c->stats.p, c->stream);
+  }
   YC_CUDA(cudaPeekAtLastError());
   const int grid_c = yc::trace_grid_blocks(false, sc->dev.depth);
   const int grid_a = yc::trace_grid_blocks(true, sc->dev.depth);
@@ -188,15 +246,26 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     int* out_a = c->q[2 * (1 - cur) + 1].p;
     yc::RoundCounters* rin = rc + cur;
     yc::RoundCounters* rout = rc + (1 - cur);
-    if (yc::launch_trace(sc->dev, false, in_c, &rin->n_closest, &rin->work_closest, ps.ro, ps.rd, ps.hit, c->stats.p,
-                         grid_c, c->stream))
-      return fail(YC_E_LAUNCH, std::string("extend kernel: ") + cudaGetErrorString(cudaGetLastError()));
-    if (yc::launch_trace(sc->dev, true, in_a, &rin->n_any, &rin->work_any, ps.ro, ps.rd, ps.hit, c->stats.p, grid_a,
-                         c->stream))
-      return fail(YC_E_LAUNCH, std::string("occlusion kernel: ") + cudaGetErrorString(cudaGetLastError()));
+    int e1, e2;
+    {
+      KTimer kt(c, K_EXTEND);
+      e1 = yc::launch_trace(sc->dev, false, in_c, &rin->n_closest, &rin->work_closest, ps.ro, ps.rd, ps.hit,
+                            c->stats.p, grid_c, c->stream);
+    }
+    if (e1) return fail(YC_E_LAUNCH, std::string("extend kernel: ") + cudaGetErrorString(cudaGetLastError()));
+    {
+      KTimer kt(c, K_OCCL);
+      e2 = yc::launch_trace(sc->dev, true, in_a, &rin->n_any, &rin->work_any, ps.ro, ps.rd, ps.hit, c->stats.p,
+                            grid_a, c->stream);
+    }
+    if (e2) return fail(YC_E_LAUNCH, std::string("occlusion kernel: ") + cudaGetErrorString(cudaGetLastError()));
     YC_CUDA(cudaMemsetAsync(rout, 0, sizeof(yc::RoundCounters), c->stream));
-    yc::launch_logic(pp, ps, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid, c->stream);
+    {
+      KTimer kt(c, K_LOGIC);
+      yc::launch_logic(pp, ps, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid, c->stream);
+    }
     YC_CUDA(cudaPeekAtLastError());
+    c->ktimes.rounds++;
     cur = 1 - cur;
     if ((round + 1) % check_every == 0) {
       YC_CUDA(cudaMemcpyAsync(c->rc_host, rc + cur, sizeof(yc::RoundCounters), cudaMemcpyDeviceToHost, c->stream));
@@ -247,6 +316,8 @@ int yc_destroy(yc_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   c->scenes.clear();
   c->accums.clear();
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  c->ev_pool.clear();
   if (c->rc_host) cudaFreeHost(c->rc_host);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -416,6 +487,7 @@ int yc_render_passes(yc_ctx* c, int scene_id, int accum_id, const uint32_t* rand
   YC_CUDA(cudaEventRecord(c->ev1, c->stream));
   YC_CUDA(cudaEventSynchronize(c->ev1));
   YC_CUDA(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
+  collect_events(c);
   return YC_OK;
 }
 
@@ -428,11 +500,10 @@ int yc_tonemap(yc_ctx* c, int accum_id, float* out) {
   if (!c || !out) return fail(YC_E_INVALID, "NULL argument");
   Accum* a = find_accum(c, accum_id);
   if (!a) return fail(YC_E_NOTFOUND, "unknown accumulator");
-  DevBuf<float4> tmp;
-  YC_CUDA(tmp.alloc(a->buf.n));
-  yc::launch_tonemap(a->buf.p, tmp.p, (int)a->buf.n, c->stream);
+  if (a->ldr.n != a->buf.n) YC_CUDA(a->ldr.alloc(a->buf.n));
+  yc::launch_tonemap(a->buf.p, a->ldr.p, (int)a->buf.n, c->stream);
   YC_CUDA(cudaPeekAtLastError());
-  YC_CUDA(cudaMemcpyAsync(out, tmp.p, tmp.bytes(), cudaMemcpyDeviceToHost, c->stream));
+  YC_CUDA(cudaMemcpyAsync(out, a->ldr.p, a->ldr.bytes(), cudaMemcpyDeviceToHost, c->stream));
   YC_CUDA(cudaStreamSynchronize(c->stream));
   return YC_OK;
 }
@@ -491,6 +562,12 @@ int yc_get_stats(yc_ctx* c, yc_stats* out) {
   out->traversed = d.traversed;
   out->samples = d.samples;
   out->stack_overflow = d.stack_overflow;
+  out->ext_rays = d.ext_rays;
+  out->ext_nodes = d.ext_nodes;
+  out->ext_tris = d.ext_tris;
+  out->any_rays = d.any_rays;
+  out->any_nodes = d.any_nodes;
+  out->any_tris = d.any_tris;
   return YC_OK;
 }
 
@@ -498,6 +575,33 @@ int yc_reset_stats(yc_ctx* c) {
   if (!c) return fail(YC_E_INVALID, "ctx is NULL");
   YC_CUDA(cudaMemsetAsync(c->stats.p, 0, sizeof(yc::DevStats), c->stream));
   YC_CUDA(cudaStreamSynchronize(c->stream));
+  return YC_OK;
+}
+
+int yc_set_profiling(yc_ctx* c, int on) {
+  if (!c) return fail(YC_E_INVALID, "ctx is NULL");
+  c->profile = on != 0;
+  c->ktimes = yc_kernel_times{};
+  return YC_OK;
+}
+
+int yc_get_kernel_times(yc_ctx* c, yc_kernel_times* out) {
+  if (!c || !out) return fail(YC_E_INVALID, "NULL argument");
+  collect_events(c);
+  *out = c->ktimes;
+  return YC_OK;
+}
+
+int yc_flush_l2(yc_ctx* c, size_t bytes) {
+  if (!c) return fail(YC_E_INVALID, "ctx is NULL");
+  if (c->flush_buf.n < bytes) YC_CUDA(c->flush_buf.alloc(bytes));
+  YC_CUDA(cudaMemsetAsync(c->flush_buf.p, (int)(c->ktimes.rounds & 0xff), bytes, c->stream));
+  return YC_OK;
+}
+
+int yc_measure_l2_gbs(yc_ctx* c, size_t bytes, int iters, double* gbs) {
+  if (!c || !gbs || bytes < 4096 || iters < 1) return fail(YC_E_INVALID, "bad argument");
+  if (yc::l2_read_gbs(bytes, iters, c->stream, gbs)) return fail(YC_E_LAUNCH, "L2 probe failed");
   return YC_OK;
 }
 

@@ -8,7 +8,14 @@
 // reference interior node becomes one 64-byte node carrying its children's boxes, each
 // reference leaf becomes a contiguous run of its vert_list triangles (in vert_list
 // order) in the 48-byte stream, and a child the reference never queues becomes
-// LINK_NONE. With no BVH (bvh_size == 0) the reference tests every triangle in index
+// LINK_NONE.
+// Equal-t ties: the reference accepts a triangle only when its t is strictly smaller
+// than the current length, so among triangles at the same t the first one it visits
+// wins. Its node array is built breadth first (src/BVH.cpp:65-165) and its queue is
+// processed in index order, so that first one lies in the leaf with the smallest node
+// index, at the smallest vert_list slot. Each stream slot carries that rank
+// (node index * 16 + slot) as a tie-break key, so the depth-first walk picks the same
+// triangle. With no BVH (bvh_size == 0) the reference tests every triangle in index
 // order (udpt.cl:280-284); that case becomes a chain of nodes with unbounded boxes whose
 // leaves hold the triangles in index order.
 #include <cmath>
@@ -32,7 +39,9 @@ struct Builder {
   std::vector<float4> out_tris;
   int depth = 0;
 
-  int emit_leaf(const int* list, int count) {
+  // order_base: visiting rank of the leaf in the reference traversal; the triangle's
+  // tie-break key is order_base + its slot.
+  int emit_leaf(const int* list, int count, int order_base) {
     const int first = (int)(out_tris.size() / 3);
     for (int k = 0; k < count; ++k) {
       const yc_triangle& t = tris[list[k]];
@@ -40,7 +49,9 @@ struct Builder {
       a.x = t.v1.x; a.y = t.v1.y; a.z = t.v1.z;
       int id = list[k];
       std::memcpy(&a.w, &id, 4);
-      b.x = t.v2.x - t.v1.x; b.y = t.v2.y - t.v1.y; b.z = t.v2.z - t.v1.z; b.w = 0.0f;
+      const int key = order_base + k;
+      b.x = t.v2.x - t.v1.x; b.y = t.v2.y - t.v1.y; b.z = t.v2.z - t.v1.z;
+      std::memcpy(&b.w, &key, 4);
       c.x = t.v3.x - t.v1.x; c.y = t.v3.y - t.v1.y; c.z = t.v3.z - t.v1.z; c.w = 0.0f;
       out_tris.push_back(a);
       out_tris.push_back(b);
@@ -88,14 +99,14 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
     std::vector<int> ids(n_tri);
     for (int i = 0; i < n_tri; ++i) ids[i] = i;
     if (n_leaf == 1) {
-      out.root_link = b.emit_leaf(ids.data(), n_tri);
+      out.root_link = b.emit_leaf(ids.data(), n_tri, 0);
     } else {
       for (int l = 0; l < n_leaf - 1; ++l) {
-        const int leaf = b.emit_leaf(ids.data() + l * per, per);
+        const int leaf = b.emit_leaf(ids.data() + l * per, per, l * per);
         int next;
         if (l == n_leaf - 2) {
           const int rest = n_tri - (l + 1) * per;
-          next = b.emit_leaf(ids.data() + (l + 1) * per, rest);
+          next = b.emit_leaf(ids.data() + (l + 1) * per, rest, (l + 1) * per);
         } else {
           next = (int)(b.out_nodes.size() / 4) + 1;
         }
@@ -139,8 +150,9 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
   out.root_test = 1;
   out.root_lo = float4{root.aabb.p_min.x, root.aabb.p_min.y, root.aabb.p_min.z, 0.0f};
   out.root_hi = float4{root.aabb.p_max.x, root.aabb.p_max.y, root.aabb.p_max.z, 0.0f};
+  if (n_node >= (1 << 27)) { err = "BVH too large for the 27-bit tie-break rank"; return -1; }
   if (is_leaf(root)) {
-    out.root_link = b.emit_leaf(root.vert_list, root.vert_len);
+    out.root_link = b.emit_leaf(root.vert_list, root.vert_len, 0);
     out.depth = 0;
     out.tris.swap(b.out_tris);
     return 0;
@@ -179,7 +191,7 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
       const yc_bvh_node& ch = nodes[ci];
       box[c] = &ch.aabb;
       if (!is_queued(ch)) link[c] = LINK_NONE;
-      else if (is_leaf(ch)) link[c] = b.emit_leaf(ch.vert_list, ch.vert_len);
+      else if (is_leaf(ch)) link[c] = b.emit_leaf(ch.vert_list, ch.vert_len, ci * 16);
       else link[c] = packed_of[ci];
     }
     float4* o = &b.out_nodes[4 * q];

@@ -22,6 +22,32 @@ __device__ __forceinline__ int warp_fetch(int* work, int n) {
   return __shfl_sync(0xffffffffu, base, 0);
 }
 
+// warp-reduced traversal counters, one atomic per warp and counter
+template <bool ANY>
+__device__ __forceinline__ void flush_counts(DevStats* st, unsigned rays, const WalkCount& wc,
+                                             unsigned long long overflow) {
+  unsigned long long r = rays, nn = wc.nodes, tt = wc.tris;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    r += __shfl_xor_sync(0xffffffffu, r, off);
+    nn += __shfl_xor_sync(0xffffffffu, nn, off);
+    tt += __shfl_xor_sync(0xffffffffu, tt, off);
+    overflow += __shfl_xor_sync(0xffffffffu, overflow, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (ANY) {
+      if (r) atomicAdd(&st->any_rays, r);
+      if (nn) atomicAdd(&st->any_nodes, nn);
+      if (tt) atomicAdd(&st->any_tris, tt);
+    } else {
+      if (r) atomicAdd(&st->ext_rays, r);
+      if (nn) atomicAdd(&st->ext_nodes, nn);
+      if (tt) atomicAdd(&st->ext_tris, tt);
+    }
+    if (overflow) atomicAdd(&st->stack_overflow, overflow);
+  }
+}
+
 template <bool ANY>
 __global__ void __launch_bounds__(TRACE_TB) k_trace_paths(DevScene sc, const int* __restrict__ queue,
                                                           const int* __restrict__ count, int* work,
@@ -32,6 +58,8 @@ __global__ void __launch_bounds__(TRACE_TB) k_trace_paths(DevScene sc, const int
   int* stack = smem + threadIdx.x;
   const int n = *count;
   unsigned long long overflow = 0;
+  WalkCount wc;
+  unsigned rays = 0;
   for (;;) {
     const int base = warp_fetch(work, n);
     if (base >= n) break;
@@ -42,12 +70,13 @@ __global__ void __launch_bounds__(TRACE_TB) k_trace_paths(DevScene sc, const int
       const float4 d = rd[p];
       RayIn r{o.x, o.y, o.z, o.w, d.x, d.y, d.z};
       HitOut h;
-      if (!traverse<ANY>(sc, r, stack, TRACE_TB, stack_cap, h)) ++overflow;
+      if (!traverse<ANY>(sc, r, stack, TRACE_TB, stack_cap, h, wc)) ++overflow;
+      ++rays;
       if (ANY) hit[p] = make_float4(h.tri >= 0 ? 1.0f : 0.0f, 0.0f, 0.0f, 0.0f);
       else hit[p] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
     }
   }
-  if (overflow) atomicAdd(&st->stack_overflow, overflow);
+  flush_counts<ANY>(st, rays, wc, overflow);
 }
 
 // traceRay (udpt.cl:240-286) on explicit rays of 9 floats: light loop, then the BVH.
@@ -58,11 +87,14 @@ __global__ void __launch_bounds__(TRACE_TB) k_trace_rays(DevScene sc, const floa
   extern __shared__ int smem[];
   int* stack = smem + threadIdx.x;
   unsigned long long overflow = 0;
+  WalkCount wc;
+  unsigned nrays = 0;
   for (;;) {
     const int base = warp_fetch(work, n);
     if (base >= n) break;
     const int e = base + (threadIdx.x & 31);
     if (e < n) {
+      ++nrays;
       const float* q = rays + 9 * (size_t)e;
       const f4 o = ym::mk(q[0], q[1], q[2], q[3]);
       const f4 d = ym::mk(q[4], q[5], q[6], q[7]);
@@ -71,7 +103,7 @@ __global__ void __launch_bounds__(TRACE_TB) k_trace_rays(DevScene sc, const floa
       light_test(sc, o, d, len, light);
       RayIn r{o.x, o.y, o.z, len, d.x, d.y, d.z};
       HitOut h;
-      if (!traverse<ANY>(sc, r, stack, TRACE_TB, stack_cap, h)) ++overflow;
+      if (!traverse<ANY>(sc, r, stack, TRACE_TB, stack_cap, h, wc)) ++overflow;
       if (ANY) {
         tri_out[e] = (h.tri >= 0 || light >= 0) ? 1 : 0;
         if (t_out) t_out[e] = h.tri >= 0 ? h.t : len;
@@ -83,7 +115,7 @@ __global__ void __launch_bounds__(TRACE_TB) k_trace_rays(DevScene sc, const floa
       }
     }
   }
-  if (overflow) atomicAdd(&st->stack_overflow, overflow);
+  flush_counts<ANY>(st, nrays, wc, overflow);
 }
 
 static int stack_cap_for(int depth) { return depth + 2; }

@@ -47,6 +47,7 @@ struct RoundCounters {
 // device-wide statistics (yc_stats layout, 64-bit counters)
 struct DevStats {
   unsigned long long rays, primary, extension, shadow, mis, connection, traversed, samples, stack_overflow;
+  unsigned long long ext_rays, ext_nodes, ext_tris, any_rays, any_nodes, any_tris;
 };
 
 struct PassParams {
@@ -76,5 +77,6 @@ void launch_tonemap(const float4* in, float4* out, int n, cudaStream_t s);
 int launch_trace_rays(const DevScene& sc, bool any_hit, const float* rays9, int n, int* tri_out, float* t_out,
                       int* work, DevStats* st, cudaStream_t s);
 int trace_grid_blocks(bool any_hit, int depth);
+int l2_read_gbs(size_t bytes, int iters, cudaStream_t s, double* gbs);
 
 }  // namespace yc

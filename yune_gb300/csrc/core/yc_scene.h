@@ -13,7 +13,9 @@
 //           child the reference never queues (vert_len <= 0 and child_idx <= 0,
 //           udpt.cl:316).
 //   tris    3 x float4 (48 B) per stream slot, leaves' triangles contiguous:
-//             (v1.xyz, original index as int bits), (e1 = v2 - v1, 0), (e2 = v3 - v1, 0)
+//             (v1.xyz, original index), (e1 = v2 - v1, tie-break rank), (e2 = v3 - v1, 0)
+//           with the index and rank as int bits; the rank orders triangles at equal t
+//           the way the reference's breadth-first walk meets them (see repack.cpp)
 //           e1/e2 are the subtractions rayTriangleIntersection does (udpt.cl:328-329),
 //           done once on the host in FP32, which gives the same bits.
 //   shade   4 x float4 (64 B) per original triangle: normalize(vn1..vn3) (udpt.cl:377-379,

@@ -8,9 +8,10 @@
 // first triangle with the smallest t; here the nearer child is visited first and a
 // child is skipped once its entry distance lies beyond the closest hit found so far (by
 // a margin of 2^-10 relative, so rounding of the entry distance can never hide a
-// triangle the reference would accept). The closest t and its triangle are therefore
-// the reference's, except between triangles at exactly the same t, where the first one
-// visited wins in both walks and the walks differ in order.
+// triangle the reference would accept). Between triangles at exactly the same t the
+// reference keeps the first it visits; every stream slot carries that visiting rank and
+// an equal-t candidate replaces the current one only when its rank is lower, so the
+// closest triangle and its t are the reference's bit for bit.
 //
 // The translation unit is compiled with -fmad=false: no multiply-add is fused, as in
 // the reference arithmetic.
@@ -30,6 +31,11 @@ struct RayIn {
 struct HitOut {
   float t, u, v;
   int tri;   // original triangle index, -1 when nothing closer than tmax
+};
+
+// work done by one walk: two-child nodes fetched and triangles tested
+struct WalkCount {
+  unsigned nodes = 0, tris = 0;
 };
 
 // OpenCL `min` (y if y < x, otherwise x); NaN-sensitive like the reference.
@@ -82,7 +88,7 @@ struct TriHit {
 // only turns a -0 sum into +0, as the reference's four-lane dot does.
 __device__ __forceinline__ bool tri_test(float ox, float oy, float oz, float dx, float dy, float dz,
                                          const float4& a, const float4& b, const float4& c, float best,
-                                         TriHit& out) {
+                                         int best_rank, TriHit& out) {
   // e1 = b.xyz, e2 = c.xyz, v1 = a.xyz
   const float px = __fsub_rn(__fmul_rn(dy, c.z), __fmul_rn(dz, c.y));
   const float py = __fsub_rn(__fmul_rn(dz, c.x), __fmul_rn(dx, c.z));
@@ -98,7 +104,7 @@ __device__ __forceinline__ bool tri_test(float ox, float oy, float oz, float dx,
   const float v = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(qx, dx), __fmul_rn(qy, dy)), __fmul_rn(qz, dz)), 0.0f), inv_det);
   if (v < 0.0f || __fadd_rn(u, v) > 1.0f) return false;
   const float t = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(c.x, qx), __fmul_rn(c.y, qy)), __fmul_rn(c.z, qz)), 0.0f), inv_det);
-  if (t > 0.0f && t < best) {
+  if (t > 0.0f && (t < best || (t == best && __float_as_int(b.w) < best_rank))) {
     out.t = t; out.u = u; out.v = v;
     return true;
   }
@@ -114,13 +120,14 @@ __device__ __forceinline__ float cull_bound(float best) { return best * 1.000976
 // false when the stack bound was exceeded (the result is then incomplete).
 template <bool ANY>
 __device__ __forceinline__ bool traverse(const DevScene& sc, const RayIn& r, int* stack, int stride, int stack_cap,
-                                         HitOut& out) {
+                                         HitOut& out, WalkCount& wc) {
   const float ox = r.ox, oy = r.oy, oz = r.oz;
   const float dx = r.dx, dy = r.dy, dz = r.dz;
   const float ix = __frcp_rn(dx), iy = __frcp_rn(dy), iz = __frcp_rn(dz);
   const bool exact = isinf(ix) || isinf(iy) || isinf(iz);
   float best = r.tmax;
   int best_tri = -1;
+  int best_rank = -1;   // the initial length (a light or the segment end) is never tied
   float bu = 0.0f, bv = 0.0f;
   out.tri = -1;
   out.t = best;
@@ -146,6 +153,7 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayIn& r, int
       const float4 n1 = __ldg(nd + 1);
       const float4 n2 = __ldg(nd + 2);
       const int2 n3 = __ldg(reinterpret_cast<const int2*>(nd + 3));
+      ++wc.nodes;
       float t0, t1;
       bool h0, h1;
       if (!exact) {
@@ -182,15 +190,17 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayIn& r, int
       const int count = enc & 15;
       const float4* tp = sc.tris + 3 * (size_t)(enc >> 4);
       for (int k = 0; k < count; ++k) {
+        ++wc.tris;
         const float4 a = __ldg(tp + 3 * k + 0);
         const float4 b = __ldg(tp + 3 * k + 1);
         const float4 c = __ldg(tp + 3 * k + 2);
         TriHit th;
-        if (tri_test(ox, oy, oz, dx, dy, dz, a, b, c, best, th)) {
+        if (tri_test(ox, oy, oz, dx, dy, dz, a, b, c, best, best_rank, th)) {
           best = th.t;
           bu = th.u;
           bv = th.v;
           best_tri = __float_as_int(a.w);
+          best_rank = __float_as_int(b.w);
           if (ANY) {
             out.t = best; out.u = bu; out.v = bv; out.tri = best_tri;
             return ok;

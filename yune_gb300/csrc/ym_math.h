@@ -12,8 +12,9 @@
 //
 // Accuracy (checked against double-precision libm in tests/test_ym_math.py):
 //   sin/cos : <= 2 ulp for |x| <= 65536, double-precision reduction above that
-//   log2    : <= 2 ulp ; exp2 : <= 2 ulp ; pow : relative error <= 2^-20 for
-//             |y*log2(x)| <= 128, which covers every call site in the renderer.
+//   log2    : relative error < 3e-7 ; exp2 : <= 2 ulp ;
+//   pow     : relative error <= 3e-7 * (1 + |y * log2(x)|) (the FP32 log2 error scaled
+//             by the exponent), exactly x for y == 1 and 1 for y == 0.
 #pragma once
 
 #include <stdint.h>
