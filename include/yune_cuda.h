@@ -130,6 +130,23 @@ int yc_render_pass(yc_ctx* ctx, int scene_id, int accum_id, uint32_t rand_seed, 
 int yc_render_passes(yc_ctx* ctx, int scene_id, int accum_id, const uint32_t* rand_seeds_host, int n_pass,
                      int reset_first, int gi_check, const yc_pass_cfg* cfg);
 
+/* ---- allocation-free render pass over one tile ----
+ * No counterpart in the reference. For callers that cannot allocate device memory when
+ * they render: a real-time loop where cudaMalloc's implicit device synchronisation would
+ * stall the frame, or a host whose device memory belongs to its own allocator and that
+ * forbids driver allocations after start-up. yc_render_pass sizes its wavefront state
+ * to the image on first use; this call keeps that state in a static device array of the
+ * library (about 3.7 MB, held by every GPU that loads the library until exit) and so
+ * renders one tile of at most 16384 pixels (cfg->block / block_x / block_y select it,
+ * as for yc_render_pass) with no allocation. The scene and accumulator come from
+ * yc_upload_scene / yc_alloc_accum, made beforehand. A larger tile is rejected with
+ * YC_E_INVALID. The first call on a device looks up the array's device address; make
+ * that first call before any stream capture. All calls share the array: calls whose
+ * work overlaps on the GPU (two contexts on one device) race and must be serialised.
+ * Results equal yc_render_pass with the same arguments. */
+int yc_render_pass_noalloc(yc_ctx* ctx, int scene_id, int accum_id, uint32_t rand_seed, int reset, int gi_check,
+                           const yc_pass_cfg* cfg);
+
 /* ---- post pass: the `tonemap` launch (kernels/post-proc/tonemap.cl:14-35,
  *      src/RendererCore.cpp:340-371). out_host receives width*height float4. ---- */
 int yc_tonemap(yc_ctx* ctx, int accum_id, float* rgba_out_host);

@@ -55,6 +55,7 @@ SIGNATURES = {
     "yc_accum_device_ptr": (i32, [vp, i32, C.POINTER(vp)]),
     "yc_render_pass": (i32, [vp, i32, i32, u32, i32, i32, C.POINTER(PassCfg)]),
     "yc_render_passes": (i32, [vp, i32, i32, vp, i32, i32, i32, C.POINTER(PassCfg)]),
+    "yc_render_pass_noalloc": (i32, [vp, i32, i32, u32, i32, i32, C.POINTER(PassCfg)]),
     "yc_tonemap": (i32, [vp, i32, vp]),
     "yc_trace": (i32, [vp, i32, vp, i32, i32, vp, vp, vp]),
     "yc_trace_device": (i32, [vp, i32, vp, i32, i32, vp, vp]),

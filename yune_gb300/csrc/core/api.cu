@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "yc_internal.h"
+#include "yc_noalloc.h"
 #include "yc_repack.h"
 #include "yune_cuda.h"
 
@@ -494,6 +495,49 @@ int yc_render_passes(yc_ctx* c, int scene_id, int accum_id, const uint32_t* rand
 int yc_render_pass(yc_ctx* c, int scene_id, int accum_id, uint32_t rand_seed, int reset, int gi_check,
                    const yc_pass_cfg* cfg) {
   return yc_render_passes(c, scene_id, accum_id, &rand_seed, 1, reset, gi_check, cfg);
+}
+
+int yc_render_pass_noalloc(yc_ctx* c, int scene_id, int accum_id, uint32_t rand_seed, int reset, int gi_check,
+                           const yc_pass_cfg* cfg) {
+  if (!c) return fail(YC_E_INVALID, "ctx is NULL");
+  if (int r = validate_cfg(cfg)) return r;
+  if (cfg->integrator != YC_UDPT) return fail(YC_E_INVALID, "integrator not available in this build");
+  Scene* sc = find_scene(c, scene_id);
+  if (!sc) return fail(YC_E_NOTFOUND, "unknown scene");
+  Accum* ac = find_accum(c, accum_id);
+  if (!ac) return fail(YC_E_NOTFOUND, "unknown accumulator");
+  if (!c->have_cam) return fail(YC_E_INVALID, "no camera set");
+  YC_CUDA(cudaSetDevice(c->device));
+  yc::NoallocPass a{};
+  yc::PassParams& pp = a.pp;
+  const int W = ac->w, H = ac->h;
+  pp.sc = sc->dev;
+  pp.cam = c->cam;
+  pp.accum = ac->buf.p;
+  pp.width = W;
+  pp.height = H;
+  pp.tile_w = (int)std::ceil((float)W / cfg->block_x);
+  pp.tile_h = (int)std::ceil((float)H / cfg->block_y);
+  pp.off_x = (int)(std::ceil((float)W / cfg->block_x) * (float)(cfg->block % cfg->block_x));
+  pp.off_y = (int)(std::ceil((float)H / cfg->block_y) * (float)(cfg->block / cfg->block_x));
+  pp.rand_seed = rand_seed;
+  pp.reset = reset;
+  pp.gi_check = gi_check;
+  pp.mis = cfg->mis;
+  pp.rr_threshold = cfg->rr_threshold;
+  pp.max_depth = cfg->max_depth;
+  pp.brdf_model = cfg->brdf_model;
+  pp.mis_lobe_fix = cfg->mis_lobe_fix;
+  a.device = c->device;
+  a.stream = c->stream;
+  a.stats = c->stats.p;
+  a.rc_host = c->rc_host;
+  a.logic_grid = c->logic_grid;
+  std::string err;
+  const int r = yc::noalloc_render(a, err);
+  if (r) return fail(r, err);
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  return YC_OK;
 }
 
 int yc_tonemap(yc_ctx* c, int accum_id, float* out) {
