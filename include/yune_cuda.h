@@ -163,6 +163,18 @@ int yc_trace(yc_ctx* ctx, int scene_id, const float* rays_host, int n, int any_h
 int yc_trace_device(yc_ctx* ctx, int scene_id, const float* rays_dev, int n, int any_hit, int* tri_dev,
                     float* t_dev);
 
+/* ---- options ---- */
+enum {
+  /* Interior hierarchy of uploaded scenes (applies to later yc_upload_scene calls):
+   * 0 = the reference node tree as given; 1 (default) = the reference's leaves, each with
+   * its triangles in vert_list order, under interior nodes rebuilt by a binned SAH over
+   * the leaf boxes. Both give the reference's closest hit bit for bit; 1 tests fewer
+   * boxes (the reference tree keeps the spatial boxes of empty children in its parents'
+   * bounds and falls back to spatial-median splits below a node area of about 1). */
+  YC_OPT_TREE = 1
+};
+int yc_set_option(yc_ctx* ctx, int option, int value);
+
 /* ---- statistics and tuning ---- */
 int yc_get_stats(yc_ctx* ctx, yc_stats* out);
 int yc_reset_stats(yc_ctx* ctx);

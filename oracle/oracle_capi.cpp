@@ -10,6 +10,7 @@
 #include <thread>
 #include <vector>
 
+#include "bdpt_oracle.hpp"
 #include "udpt_oracle.hpp"
 
 extern "C" {
@@ -57,7 +58,7 @@ void add(or_counters* o, const orc::Counters& c) {
 template <class R, class Acc>
 int render(const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_bvh_node* b, int nb,
            const yc_quad_light* l, int nl, const yc_cam* cam, int W, int H, Acc* accum, uint32_t rand_,
-           int reset, const or_cfg* cfg, int threads, int row0, int row1, or_counters* out) {
+           int reset, const or_cfg* cfg, int threads, int row0, int row1, or_counters* out, int bdpt_bounces = 0) {
   if (!cam || !accum || W <= 0 || H <= 0 || nl < 0 || nl > 16) return -1;
   if (row1 <= row0) { row0 = 0; row1 = H; }
   const orc::Scene<R> sc = mk_scene<R>(t, nt, m, nm, b, nb, l, nl);
@@ -66,12 +67,13 @@ int render(const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_
   std::atomic<int> next(row0);
   std::vector<orc::Counters> cnts(threads);
   auto work = [&](int tid) {
-    orc::Tracer<R> tr(sc, k, cnts[tid]);
+    orc::BdptTracer<R> tr(sc, k, cnts[tid], bdpt_bounces > 0 ? bdpt_bounces : 20);
     for (;;) {
       const int y = next.fetch_add(1);
       if (y >= row1) break;
       for (int x = 0; x < W; ++x) {
-        const orc::V4<R> c = orc::pixel_sample<R>(tr, *cam, x, y, W, H, rand_);
+        const orc::V4<R> c = bdpt_bounces > 0 ? orc::pixel_sample_bdpt<R>(tr, *cam, x, y, W, H, rand_)
+                                              : orc::pixel_sample<R>(tr, *cam, x, y, W, H, rand_);
         Acc* p = accum + 4 * ((size_t)y * W + x);
         const orc::V4<R> prev{(R)p[0], (R)p[1], (R)p[2], (R)p[3]};
         const orc::V4<R> o = orc::accumulate<R>(c, prev, reset);
@@ -124,6 +126,25 @@ int or_render(const yc_triangle* t, int nt, const yc_material* m, int nm, const 
               int reset, const or_cfg* cfg, int threads, int row0, int row1, or_counters* out) {
   return render<float, float>(t, nt, m, nm, b, nb, l, nl, cam, W, H, accum, rand_, reset, cfg, threads, row0,
                               row1, out);
+}
+
+// One pass of the BDPT `pathtracer` (kernels/legacy/bdpt.cl:158-210) with
+// BDPT_BOUNCES = bounces (<= 32).
+int or_render_bdpt(const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_bvh_node* b, int nb,
+                   const yc_quad_light* l, int nl, const yc_cam* cam, int W, int H, float* accum, uint32_t rand_,
+                   int reset, const or_cfg* cfg, int bounces, int threads, int row0, int row1, or_counters* out) {
+  if (bounces < 2 || bounces > 32) return -1;
+  return render<float, float>(t, nt, m, nm, b, nb, l, nl, cam, W, H, accum, rand_, reset, cfg, threads, row0, row1,
+                              out, bounces);
+}
+
+int or_render_bdpt_f64(const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_bvh_node* b, int nb,
+                       const yc_quad_light* l, int nl, const yc_cam* cam, int W, int H, double* accum,
+                       uint32_t rand_, int reset, const or_cfg* cfg, int bounces, int threads, int row0, int row1,
+                       or_counters* out) {
+  if (bounces < 2 || bounces > 32) return -1;
+  return render<double, double>(t, nt, m, nm, b, nb, l, nl, cam, W, H, accum, rand_, reset, cfg, threads, row0,
+                                row1, out, bounces);
 }
 
 // The same pass evaluated in double precision into a double accumulator.

@@ -43,6 +43,9 @@ def orc():
         L.or_render.argtypes = [vp, i32, vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, u32, i32, C.POINTER(OrCfg), i32,
                                 i32, i32, C.POINTER(OrCounters)]
         L.or_render_f64.argtypes = L.or_render.argtypes
+        L.or_render_bdpt.argtypes = [vp, i32, vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, u32, i32,
+                                     C.POINTER(OrCfg), i32, i32, i32, i32, C.POINTER(OrCounters)]
+        L.or_render_bdpt_f64.argtypes = L.or_render_bdpt.argtypes
         L.or_tonemap.argtypes = [vp, i32, i32, vp]
         L.or_ym_eval.argtypes = [i32, vp, vp, vp, i32]
         L.or_wang_hash.argtypes = [u32]
@@ -101,6 +104,22 @@ def render(scene, accum, rand_seed, reset, cfg, threads=0, rows=None, f64=False,
             C.byref(c), threads, r0, r1, C.byref(cnt))
     if rc != 0:
         raise RuntimeError("or_render failed: %d" % rc)
+    return {k: getattr(cnt, k) for k, _ in OrCounters._fields_}
+
+
+def render_bdpt(scene, accum, rand_seed, reset, bounces, threads=0, rows=None, f64=False, heap_size=1500):
+    """One oracle BDPT pass (bdpt.cl) into accum."""
+    L = orc()
+    H, W = accum.shape[:2]
+    cnt = OrCounters()
+    c = cfg_of({}, heap_size)
+    r0, r1 = rows if rows else (0, 0)
+    fn = L.or_render_bdpt_f64 if f64 else L.or_render_bdpt
+    rc = fn(_p(scene.tris), len(scene.tris), _p(scene.mats), len(scene.mats), _p(scene.nodes), len(scene.nodes),
+            _p(scene.lights), len(scene.lights), _p(scene.cam), W, H, _p(accum), int(rand_seed) & 0xFFFFFFFF, reset,
+            C.byref(c), bounces, threads, r0, r1, C.byref(cnt))
+    if rc != 0:
+        raise RuntimeError("or_render_bdpt failed: %d" % rc)
     return {k: getattr(cnt, k) for k, _ in OrCounters._fields_}
 
 

@@ -191,6 +191,16 @@ int ref_render(int variant, const yc_triangle* t, int nt, const yc_material* m, 
   (void)nm;
   if (!cam || !accum || W <= 0 || H <= 0 || !l) return -1;
   if (row1 <= row0) { row0 = 0; row1 = H; }
+  // bdpt.cl keeps extending the eye path after the camera ray hits the light, from a
+  // vertex whose triangle_ID is -1, so it reads scene_data[-1]; give it a valid record
+  // there (material 0). The pixel colour does not depend on it.
+  std::vector<yc_triangle> padded;
+  if (variant >= 10) {
+    padded.resize((size_t)nt + 1);
+    std::memset(padded.data(), 0, sizeof(yc_triangle));
+    if (nt > 0) std::memcpy(padded.data() + 1, t, (size_t)nt * sizeof(yc_triangle));
+    t = padded.data() + 1;
+  }
   yref::yref_rr_threshold = rr_threshold;
   yref::yref_max_depth = max_depth;
   switch (variant) {

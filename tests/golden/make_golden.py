@@ -13,6 +13,8 @@ reference tree:
                        RR_THRESHOLD 3) on a 32x24 Cornell box, plus `tonemap`
                        (kernels/post-proc/tonemap.cl) of the MIS accumulator
   oren_nayar.npz       OrenNayarBRDF (kernels/legacy/udpt-primitives.cl:696-725)
+  render_bdpt.npz      2 passes of the BDPT `pathtracer` (kernels/legacy/bdpt.cl with
+                       BDPT_BOUNCES 8) on a 32x24 Cornell box with 1 and with 4 lights
 Each file records a SHA-256 of the scene arrays it was made from.
 """
 import hashlib
@@ -96,6 +98,17 @@ def main():
         res[i] = o
     np.savez_compressed(os.path.join(HERE, "oren_nayar.npz"), material=m, normal=NRM, w_i=WI, w_o=WO, hit_point=HP,
                         value=res)
+    # BDPT
+    out = {}
+    seeds = scenes.pass_seeds(606, 2)
+    for lights, variant in ((1, "bdpt8"), (4, "bdpt8_l4")):
+        sb = scenes.c0_bdpt(32, 24, bounces=8, lights=lights)
+        acc = np.zeros((24, 32, 4), np.float32)
+        for k, sd in enumerate(seeds):
+            O.ref_render(sb, acc, sd, 1 if k == 0 else 0, variant, 4, 100000)
+        out["lights%d" % lights] = acc
+        out["sha_lights%d" % lights] = scene_hash(sb)
+    np.savez_compressed(os.path.join(HERE, "render_bdpt.npz"), seeds=seeds, **out)
     print("golden fixtures written to", HERE)
 
 

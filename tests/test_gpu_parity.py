@@ -37,10 +37,13 @@ def _cmp_closest(gpu, orc):
     return int(diff.sum()), int(tie.sum())
 
 
+@pytest.mark.parametrize("tree", [0, 1])
 @pytest.mark.parametrize("cfg_name,level", [("c0", None), ("c1", 6)])
-def test_trace_closest_and_any(renderer, cfg_name, level):
+def test_trace_closest_and_any(renderer, cfg_name, level, tree):
     s = scenes.c0(64, 64) if cfg_name == "c0" else scenes.c1(64, 64, level=level)
+    renderer.set_tree_mode(tree)
     sid = renderer.upload(s)
+    renderer.set_tree_mode(1)
     rays = O.seeded_rays(s, 50000 if cfg_name == "c0" else 20000, seed=11)
     g = renderer.trace(sid, rays, any_hit=False)
     o = O.trace(s, rays, any_hit=False)
@@ -56,10 +59,13 @@ def test_trace_closest_and_any(renderer, cfg_name, level):
     renderer.release(sid)
 
 
-def test_trace_axis_aligned_rays(renderer):
+@pytest.mark.parametrize("tree", [0, 1])
+def test_trace_axis_aligned_rays(renderer, tree):
     """Rays with zero direction components take the reference's NaN-skipping slab path."""
     s = scenes.c0(64, 64)
+    renderer.set_tree_mode(tree)
     sid = renderer.upload(s)
+    renderer.set_tree_mode(1)
     rng = np.random.default_rng(3)
     n = 6000
     r = np.zeros((n, 9), np.float32)
@@ -172,3 +178,26 @@ def test_block_tiling_covers_frame(renderer):
     for b in range(4):
         renderer.render(sid, a_tile, 4242, reset=1, cfg=dict(s.cfg, block=b, block_x=2, block_y=2))
     assert np.array_equal(renderer.read_accum(a_full), renderer.read_accum(a_tile))
+
+
+@pytest.mark.parametrize("bounces,lights", [(8, 1), (20, 1), (8, 4)])
+def test_render_parity_bdpt(renderer, bounces, lights):
+    """Naive BDPT (kernels/legacy/bdpt.cl) on the GPU against the oracle."""
+    s = scenes.c0_bdpt(40, 32, bounces=bounces, lights=lights)
+    seeds = scenes.pass_seeds(8, 2)
+    sid = renderer.upload(s)
+    renderer.set_camera(s.cam)
+    aid = renderer.alloc_accum(40, 32)
+    renderer.reset_stats()
+    renderer.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+    gpu = renderer.read_accum(aid)
+    st = renderer.stats()
+    renderer.free_accum(aid)
+    renderer.release(sid)
+    ref = np.zeros((32, 40, 4), np.float32)
+    for k, sd in enumerate(seeds):
+        O.render_bdpt(s, ref, sd, 1 if k == 0 else 0, bounces)
+    assert st["stack_overflow"] == 0
+    assert _rel_bad(gpu, ref) == 0
+    assert np.array_equal(gpu[..., 3], ref[..., 3])
+    assert st["samples"] == 40 * 32 * 2

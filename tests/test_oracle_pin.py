@@ -97,6 +97,17 @@ def test_oracle_oren_nayar_matches_reference():
     assert np.array_equal(out.view(np.int32), g["value"].view(np.int32))
 
 
+@pytest.mark.parametrize("lights", [1, 4])
+def test_oracle_bdpt_matches_reference(lights):
+    g = _load("render_bdpt.npz")
+    s = scenes.c0_bdpt(32, 24, bounces=8, lights=lights)
+    assert MG.scene_hash(s) == str(g["sha_lights%d" % lights])
+    acc = np.zeros((24, 32, 4), np.float32)
+    for k, sd in enumerate(g["seeds"]):
+        O.render_bdpt(s, acc, sd, 1 if k == 0 else 0, 8, threads=2)
+    assert np.array_equal(acc.view(np.int32), g["lights%d" % lights].view(np.int32))
+
+
 # ---- live comparisons against the compiled reference (where the reference tree is) ----
 needs_ref = pytest.mark.skipif(O.ref() is None, reason="compiled reference not available")
 
@@ -164,3 +175,18 @@ def test_oracle_render_live_brute_force_and_gi_off():
             O.render(s, a, sd, 1 if k == 0 else 0, dict(mis=0, rr_threshold=6, max_depth=100000, gi_check=gi))
             O.ref_render(s, b, sd, 1 if k == 0 else 0, "udpt_a", 6, 100000, gi_check=gi)
         assert np.array_equal(a.view(np.int32), b.view(np.int32))
+
+
+@needs_ref
+@pytest.mark.parametrize("variant,bounces", [("bdpt20", 20), ("bdpt8", 8)])
+def test_oracle_bdpt_live_glass_scene(variant, bounces):
+    """BDPT on the icosphere scene (no specular materials in bdpt.cl: the dielectric is
+    shaded as its kd/ks say)."""
+    s = scenes.c1(24, 20, level=3)
+    seeds = scenes.pass_seeds(12, 2)
+    a = np.zeros((20, 24, 4), np.float32)
+    b = np.zeros((20, 24, 4), np.float32)
+    for k, sd in enumerate(seeds):
+        O.render_bdpt(s, a, sd, 1 if k == 0 else 0, bounces, threads=4)
+        O.ref_render(s, b, sd, 1 if k == 0 else 0, variant, 4, 100000, threads=4)
+    assert np.array_equal(a.view(np.int32), b.view(np.int32))

@@ -63,6 +63,7 @@ SIGNATURES = {
     "yc_reset_stats": (i32, [vp]),
     "yc_last_pass_ms": (i32, [vp, C.POINTER(f32)]),
     "yc_set_profiling": (i32, [vp, i32]),
+    "yc_set_option": (i32, [vp, i32, i32]),
     "yc_get_kernel_times": (i32, [vp, C.POINTER(KernelTimes)]),
     "yc_flush_l2": (i32, [vp, C.c_size_t]),
     "yc_measure_l2_gbs": (i32, [vp, C.c_size_t, i32, C.POINTER(C.c_double)]),

@@ -120,6 +120,10 @@ class Renderer:
         N.check(self.L.yc_last_pass_ms(self.h, C.byref(ms)), "yc_last_pass_ms")
         return ms.value
 
+    def set_tree_mode(self, mode):
+        """0: reference node tree; 1: SAH hierarchy over the reference leaves (default)."""
+        N.check(self.L.yc_set_option(self.h, 1, int(mode)), "yc_set_option")
+
     def set_profiling(self, on=True):
         N.check(self.L.yc_set_profiling(self.h, int(on)), "yc_set_profiling")
 

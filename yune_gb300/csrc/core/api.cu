@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "yc_bdpt.h"
 #include "yc_internal.h"
 #include "yc_noalloc.h"
 #include "yc_repack.h"
@@ -82,6 +83,7 @@ struct yc_ctx {
   int next_scene = 1, next_accum = 1;
   yc_cam cam{};
   bool have_cam = false;
+  int tree_mode = yc::TREE_SAH_OVER_LEAVES;
   // wavefront buffers, sized for the largest image seen
   size_t cap_paths = 0;
   DevBuf<int4> misc;
@@ -100,6 +102,9 @@ struct yc_ctx {
   std::vector<std::pair<int, size_t>> ev_marks;   // kind, index of the start event
   yc_kernel_times ktimes{};
   DevBuf<char> flush_buf;
+  // BDPT subpath vertices
+  DevBuf<float4> bd_lv, bd_ev;
+  size_t bd_cap = 0;
   // direct queries
   DevBuf<float> q_rays;
   DevBuf<int> q_tri;
@@ -204,7 +209,8 @@ int validate_cfg(const yc_pass_cfg* cfg) {
 // Runs one pass (all rounds) on the context stream; the host polls the queue sizes
 // every few rounds.
 int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int gi_check, const yc_pass_cfg* cfg) {
-  if (cfg->integrator != YC_UDPT) return fail(YC_E_INVALID, "integrator not available in this build");
+  const bool bdpt = cfg->integrator == YC_BDPT;
+  if (bdpt && (cfg->bdpt_bounces < 2 || cfg->bdpt_bounces > 32)) return fail(YC_E_INVALID, "bdpt_bounces must be 2..32");
   const int W = ac->w, H = ac->h;
   int rc_ = ensure_paths(c, (size_t)W * H);
   if (rc_) return rc_;
@@ -228,11 +234,25 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
   pp.brdf_model = cfg->brdf_model;
   pp.mis_lobe_fix = cfg->mis_lobe_fix;
   const yc::PathState ps = path_state(c);
+  yc::BdptBuffers bb{};
+  if (bdpt) {
+    const size_t need = (size_t)W * H * 4 * cfg->bdpt_bounces;
+    if (c->bd_cap < need) {
+      YC_CUDA(c->bd_lv.alloc(need));
+      YC_CUDA(c->bd_ev.alloc(need));
+      c->bd_cap = need;
+    }
+    bb.lv = c->bd_lv.p;
+    bb.ev = c->bd_ev.p;
+    bb.N = (size_t)W * H;
+    bb.bounces = cfg->bdpt_bounces;
+  }
   yc::RoundCounters* rc = c->rc.p;
   YC_CUDA(cudaMemsetAsync(rc, 0, 2 * sizeof(yc::RoundCounters), c->stream));
   {
     KTimer kt(c, K_RAYGEN);
-    yc::launch_raygen(pp, ps, c->q[0].p, rc + 0, c->stats.p, c->stream);
+    if (bdpt) yc::launch_raygen_bdpt(pp, ps, bb, c->q[0].p, rc + 0, c->stats.p, c->stream);
+    else yc::launch_raygen(pp, ps, c->q[0].p, rc + 0, c->stats.p, c->stream);
   }
   YC_CUDA(cudaPeekAtLastError());
   const int grid_c = yc::trace_grid_blocks(false, sc->dev.depth);
@@ -263,7 +283,9 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     YC_CUDA(cudaMemsetAsync(rout, 0, sizeof(yc::RoundCounters), c->stream));
     {
       KTimer kt(c, K_LOGIC);
-      yc::launch_logic(pp, ps, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid, c->stream);
+      if (bdpt) yc::launch_logic_bdpt(pp, ps, bb, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid,
+                                      c->stream);
+      else yc::launch_logic(pp, ps, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid, c->stream);
     }
     YC_CUDA(cudaPeekAtLastError());
     c->ktimes.rounds++;
@@ -345,7 +367,7 @@ int yc_upload_scene(yc_ctx* c, const yc_triangle* tris, int n_tri, const yc_mate
       return fail(YC_E_INVALID, "triangle " + std::to_string(i) + " has matID out of range");
   yc::Repacked rp;
   std::string err;
-  if (yc::repack_scene(tris, n_tri, nodes, n_node, rp, err)) return fail(YC_E_INVALID, err);
+  if (yc::repack_scene(tris, n_tri, nodes, n_node, c->tree_mode, rp, err)) return fail(YC_E_INVALID, err);
   std::unique_ptr<Scene> s(new (std::nothrow) Scene);
   if (!s) return fail(YC_E_NOMEM, "host allocation failed");
   YC_CUDA(cudaSetDevice(c->device));
@@ -620,6 +642,18 @@ int yc_reset_stats(yc_ctx* c) {
   YC_CUDA(cudaMemsetAsync(c->stats.p, 0, sizeof(yc::DevStats), c->stream));
   YC_CUDA(cudaStreamSynchronize(c->stream));
   return YC_OK;
+}
+
+int yc_set_option(yc_ctx* c, int option, int value) {
+  if (!c) return fail(YC_E_INVALID, "ctx is NULL");
+  switch (option) {
+    case YC_OPT_TREE:
+      if (value != yc::TREE_REFERENCE && value != yc::TREE_SAH_OVER_LEAVES) return fail(YC_E_INVALID, "bad tree mode");
+      c->tree_mode = value;
+      return YC_OK;
+    default:
+      return fail(YC_E_INVALID, "unknown option");
+  }
 }
 
 int yc_set_profiling(yc_ctx* c, int on) {

@@ -18,6 +18,7 @@
 // triangle. With no BVH (bvh_size == 0) the reference tests every triangle in index
 // order (udpt.cl:280-284); that case becomes a chain of nodes with unbounded boxes whose
 // leaves hold the triangles in index order.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -64,10 +65,120 @@ struct Builder {
 bool is_leaf(const yc_bvh_node& n) { return (float)n.child_idx == -1.0f && n.vert_len > 0; }
 bool is_queued(const yc_bvh_node& n) { return n.vert_len > 0 || n.child_idx > 0; }
 
+// ---- SAH hierarchy over the reference leaves ----
+// Each reference leaf keeps its triangles, their order and its tie-break rank; only the
+// interior nodes above the leaves are rebuilt, by a binned surface-area-heuristic split
+// of the leaves' box centroids (32 bins per axis). A node's box is the union of the
+// leaf boxes below it, so it contains every box the reference tree places below it and
+// a ray that reaches a leaf in the reference passes every box on the way down here too.
+struct LeafItem {
+  float lo[3], hi[3];
+  float c[3];
+  int link;
+};
+
+struct SahBuilder {
+  std::vector<LeafItem>& items;
+  std::vector<float4>& out_nodes;
+  int max_depth = 0;
+
+  static float area(const float lo[3], const float hi[3]) {
+    const float d0 = hi[0] - lo[0], d1 = hi[1] - lo[1], d2 = hi[2] - lo[2];
+    return 2.0f * (d0 * d1 + d0 * d2 + d1 * d2);
+  }
+
+  // returns the link of the subtree over items [b, e)
+  int build(int b, int e, int depth, float lo_out[3], float hi_out[3]) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int i = b; i < e; ++i)
+      for (int k = 0; k < 3; ++k) {
+        lo[k] = std::min(lo[k], items[i].lo[k]);
+        hi[k] = std::max(hi[k], items[i].hi[k]);
+        clo[k] = std::min(clo[k], items[i].c[k]);
+        chi[k] = std::max(chi[k], items[i].c[k]);
+      }
+    for (int k = 0; k < 3; ++k) { lo_out[k] = lo[k]; hi_out[k] = hi[k]; }
+    max_depth = std::max(max_depth, depth);
+    if (e - b == 1) return items[b].link;
+    // binned SAH
+    constexpr int NB = 32;
+    int best_axis = -1, best_split = -1;
+    float best_cost = INFINITY;
+    for (int k = 0; k < 3; ++k) {
+      const float ext = chi[k] - clo[k];
+      if (!(ext > 0.0f)) continue;
+      int cnt[NB] = {0};
+      float blo[NB][3], bhi[NB][3];
+      for (int q = 0; q < NB; ++q)
+        for (int a = 0; a < 3; ++a) { blo[q][a] = INFINITY; bhi[q][a] = -INFINITY; }
+      const float scale = NB / ext;
+      for (int i = b; i < e; ++i) {
+        int q = (int)((items[i].c[k] - clo[k]) * scale);
+        q = std::min(NB - 1, std::max(0, q));
+        cnt[q]++;
+        for (int a = 0; a < 3; ++a) {
+          blo[q][a] = std::min(blo[q][a], items[i].lo[a]);
+          bhi[q][a] = std::max(bhi[q][a], items[i].hi[a]);
+        }
+      }
+      float rlo[NB][3], rhi[NB][3];
+      int rcnt[NB];
+      float alo[3] = {INFINITY, INFINITY, INFINITY}, ahi[3] = {-INFINITY, -INFINITY, -INFINITY};
+      int ac = 0;
+      for (int q = NB - 1; q >= 0; --q) {
+        for (int a = 0; a < 3; ++a) { alo[a] = std::min(alo[a], blo[q][a]); ahi[a] = std::max(ahi[a], bhi[q][a]); }
+        ac += cnt[q];
+        for (int a = 0; a < 3; ++a) { rlo[q][a] = alo[a]; rhi[q][a] = ahi[a]; }
+        rcnt[q] = ac;
+      }
+      float llo[3] = {INFINITY, INFINITY, INFINITY}, lhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+      int lc = 0;
+      for (int q = 0; q < NB - 1; ++q) {
+        for (int a = 0; a < 3; ++a) { llo[a] = std::min(llo[a], blo[q][a]); lhi[a] = std::max(lhi[a], bhi[q][a]); }
+        lc += cnt[q];
+        const int rc = rcnt[q + 1];
+        if (lc == 0 || rc == 0) continue;
+        const float cost = area(llo, lhi) * lc + area(rlo[q + 1], rhi[q + 1]) * rc;
+        if (cost < best_cost) { best_cost = cost; best_axis = k; best_split = q; }
+      }
+    }
+    int mid;
+    if (best_axis < 0) {
+      mid = (b + e) / 2;   // coincident centroids: split the list in half
+    } else {
+      const float ext = chi[best_axis] - clo[best_axis];
+      const float scale = NB / ext;
+      auto left = [&](const LeafItem& it) {
+        int q = (int)((it.c[best_axis] - clo[best_axis]) * scale);
+        q = std::min(NB - 1, std::max(0, q));
+        return q <= best_split;
+      };
+      mid = (int)(std::partition(items.begin() + b, items.begin() + e, left) - items.begin());
+      if (mid == b || mid == e) mid = (b + e) / 2;
+    }
+    const int node = (int)(out_nodes.size() / 4);
+    out_nodes.resize(out_nodes.size() + 4);
+    float l0[3], h0[3], l1[3], h1[3];
+    const int c0 = build(b, mid, depth + 1, l0, h0);
+    const int c1 = build(mid, e, depth + 1, l1, h1);
+    float4* o = &out_nodes[4 * (size_t)node];
+    o[0] = float4{l0[0], h0[0], l0[1], h0[1]};
+    o[1] = float4{l1[0], h1[0], l1[1], h1[1]};
+    o[2] = float4{l0[2], h0[2], l1[2], h1[2]};
+    float4 l;
+    std::memcpy(&l.x, &c0, 4);
+    std::memcpy(&l.y, &c1, 4);
+    l.z = l.w = 0.0f;
+    o[3] = l;
+    return node;
+  }
+};
+
 }  // namespace
 
-int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, int n_node, Repacked& out,
-                 std::string& err) {
+int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, int n_node, int tree_mode,
+                 Repacked& out, std::string& err) {
   Builder b{tris, n_tri, nodes, n_node, {}, {}, 0};
   out = Repacked();
   const float INF = INFINITY;
@@ -154,6 +265,39 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
   if (is_leaf(root)) {
     out.root_link = b.emit_leaf(root.vert_list, root.vert_len, 0);
     out.depth = 0;
+    out.tris.swap(b.out_tris);
+    return 0;
+  }
+  if (tree_mode == TREE_SAH_OVER_LEAVES) {
+    // the leaves the reference traversal can reach, in node-index order
+    std::vector<LeafItem> items;
+    std::vector<char> reach(n_node, 0);
+    reach[0] = 1;
+    for (int i = 0; i < n_node; ++i) {
+      if (!reach[i]) continue;
+      const yc_bvh_node& n = nodes[i];
+      if (is_leaf(n)) {
+        LeafItem it;
+        const float* plo = &n.aabb.p_min.x;
+        const float* phi = &n.aabb.p_max.x;
+        for (int k = 0; k < 3; ++k) {
+          it.lo[k] = plo[k];
+          it.hi[k] = phi[k];
+          it.c[k] = 0.5f * (plo[k] + phi[k]);
+        }
+        it.link = b.emit_leaf(n.vert_list, n.vert_len, i * 16);
+        items.push_back(it);
+      } else if (is_queued(n) || i == 0) {
+        for (int c = 0; c < 2; ++c)
+          if (is_queued(nodes[n.child_idx + c])) reach[n.child_idx + c] = 1;
+      }
+    }
+    if (items.empty()) { out.root_link = LINK_NONE; out.depth = 0; return 0; }
+    SahBuilder sb{items, b.out_nodes};
+    float lo[3], hi[3];
+    out.root_link = sb.build(0, (int)items.size(), 0, lo, hi);
+    out.depth = sb.max_depth + 1;
+    out.nodes.swap(b.out_nodes);
     out.tris.swap(b.out_tris);
     return 0;
   }

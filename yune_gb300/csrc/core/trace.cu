@@ -1,8 +1,10 @@
 // trace.cu -- the extend (closest-hit) and occlusion (any-hit) kernels.
 //
-// Persistent kernels: one grid of (SM count x resident blocks) CTAs; each warp takes 32
-// queue entries at a time from a device cursor and every lane walks its ray to the end
-// (yc_traverse.cuh). Each thread keeps its traversal stack in a column of dynamic shared
+// Persistent kernels: one grid of (SM count x resident blocks) CTAs. A warp takes rays
+// from a device cursor for its idle lanes (one atomic per refill) whenever at least
+// REFILL_AT lanes are idle, and advances every busy lane's walk by one leaf per step
+// (yc_traverse.cuh), so lanes whose rays end early do not wait for the warp's longest
+// ray. Each thread keeps its traversal stack in a column of dynamic shared
 // memory (stride = block size, so the 32 lanes of a warp hit 32 different banks); the
 // column holds depth + 1 entries of (link, entry distance). A walk that would overflow
 // the stack is counted in DevStats::stack_overflow instead of writing out of bounds.
@@ -15,12 +17,6 @@
 namespace yc {
 
 constexpr int TRACE_TB = 128;
-
-__device__ __forceinline__ int warp_fetch(int* work, int n) {
-  int base = 0;
-  if ((threadIdx.x & 31) == 0) base = atomicAdd(work, 32);
-  return __shfl_sync(0xffffffffu, base, 0);
-}
 
 // warp-reduced traversal counters, one atomic per warp and counter
 template <bool ANY>
@@ -48,74 +44,128 @@ __device__ __forceinline__ void flush_counts(DevStats* st, unsigned rays, const 
   }
 }
 
+// Lanes refill when at least this many of a warp's 32 lanes are idle.
+constexpr int REFILL_AT = 8;
+
+// The persistent loop shared by both kernels. Src supplies ray e of the work list
+// (begin) and stores its result (end).
+template <bool ANY, class Src>
+__device__ __forceinline__ void trace_loop(const DevScene& sc, Src& src, int n, int* work, int stack_cap,
+                                           DevStats* st) {
+  extern __shared__ int smem[];
+  int* stack = smem + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  unsigned long long overflow = 0;
+  WalkCount wc;
+  unsigned rays = 0;
+  Walk w;
+  int e_cur = -1;            // work-list entry of this lane's ray, -1 when idle
+  bool more = true;          // the work list may still hold rays (warp-uniform)
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xffffffffu, e_cur < 0);
+    if (more && (__popc(idle) >= REFILL_AT || idle == 0xffffffffu)) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(work, __popc(idle));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + __popc(idle) >= n) more = false;
+      if (e_cur < 0) {
+        const int e = base + __popc(idle & ((1u << lane) - 1));
+        if (e < n) {
+          e_cur = e;
+          RayIn r;
+          src.begin(e, r);
+          walk_begin(sc, r, w);
+          ++rays;
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, e_cur >= 0) == 0) {
+      if (!more) break;
+      continue;
+    }
+    if (e_cur >= 0) {
+      bool of = false;
+      bool done = (w.link == LINK_NONE) || walk_step<ANY>(sc, w, stack, TRACE_TB, stack_cap, wc, of);
+      if (of) ++overflow;
+      if (done) {
+        HitOut h;
+        h.t = w.best; h.u = w.bu; h.v = w.bv; h.tri = w.best_tri;
+        src.end(e_cur, h);
+        e_cur = -1;
+      }
+    }
+  }
+  flush_counts<ANY>(st, rays, wc, overflow);
+}
+
+// rays of the path state, addressed through the queue
+template <bool ANY>
+struct PathSrc {
+  const int* __restrict__ queue;
+  const float4* __restrict__ ro;
+  const float4* __restrict__ rd;
+  float4* hit;
+  int p;
+  __device__ __forceinline__ void begin(int e, RayIn& r) {
+    const int q = queue[e];
+    const float4 o = ro[q];
+    const float4 d = rd[q];
+    r = RayIn{o.x, o.y, o.z, o.w, d.x, d.y, d.z};
+  }
+  __device__ __forceinline__ void end(int e, const HitOut& h) {
+    const int q = queue[e];
+    if (ANY) hit[q] = make_float4(h.tri >= 0 ? 1.0f : 0.0f, 0.0f, 0.0f, 0.0f);
+    else hit[q] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+  }
+};
+
 template <bool ANY>
 __global__ void __launch_bounds__(TRACE_TB) k_trace_paths(DevScene sc, const int* __restrict__ queue,
                                                           const int* __restrict__ count, int* work,
                                                           const float4* __restrict__ ro,
                                                           const float4* __restrict__ rd, float4* hit, int stack_cap,
                                                           DevStats* st) {
-  extern __shared__ int smem[];
-  int* stack = smem + threadIdx.x;
-  const int n = *count;
-  unsigned long long overflow = 0;
-  WalkCount wc;
-  unsigned rays = 0;
-  for (;;) {
-    const int base = warp_fetch(work, n);
-    if (base >= n) break;
-    const int e = base + (threadIdx.x & 31);
-    if (e < n) {
-      const int p = queue[e];
-      const float4 o = ro[p];
-      const float4 d = rd[p];
-      RayIn r{o.x, o.y, o.z, o.w, d.x, d.y, d.z};
-      HitOut h;
-      if (!traverse<ANY>(sc, r, stack, TRACE_TB, stack_cap, h, wc)) ++overflow;
-      ++rays;
-      if (ANY) hit[p] = make_float4(h.tri >= 0 ? 1.0f : 0.0f, 0.0f, 0.0f, 0.0f);
-      else hit[p] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
-    }
-  }
-  flush_counts<ANY>(st, rays, wc, overflow);
+  PathSrc<ANY> src{queue, ro, rd, hit, 0};
+  trace_loop<ANY>(sc, src, *count, work, stack_cap, st);
 }
 
 // traceRay (udpt.cl:240-286) on explicit rays of 9 floats: light loop, then the BVH.
 template <bool ANY>
+struct RaySrc {
+  const DevScene* sc;
+  const float* __restrict__ rays;
+  int* tri_out;
+  float* t_out;
+  int light;
+  float len;
+  __device__ __forceinline__ void begin(int e, RayIn& r) {
+    const float* q = rays + 9 * (size_t)e;
+    const f4 o = ym::mk(q[0], q[1], q[2], q[3]);
+    const f4 d = ym::mk(q[4], q[5], q[6], q[7]);
+    len = q[8];
+    light = -1;
+    light_test(*sc, o, d, len, light);
+    r = RayIn{o.x, o.y, o.z, len, d.x, d.y, d.z};
+  }
+  __device__ __forceinline__ void end(int e, const HitOut& h) {
+    if (ANY) {
+      tri_out[e] = (h.tri >= 0 || light >= 0) ? 1 : 0;
+      if (t_out) t_out[e] = h.tri >= 0 ? h.t : len;
+    } else {
+      tri_out[e] = h.tri;
+      if (t_out) t_out[e] = h.tri >= 0 ? h.t : len;
+      // a light hit is reported as -2 - light (unpacked by the host entry point)
+      if (h.tri < 0 && light >= 0) tri_out[e] = -2 - light;
+    }
+  }
+};
+
+template <bool ANY>
 __global__ void __launch_bounds__(TRACE_TB) k_trace_rays(DevScene sc, const float* __restrict__ rays, int n,
                                                          int* work, int* tri_out, float* t_out, int stack_cap,
                                                          DevStats* st) {
-  extern __shared__ int smem[];
-  int* stack = smem + threadIdx.x;
-  unsigned long long overflow = 0;
-  WalkCount wc;
-  unsigned nrays = 0;
-  for (;;) {
-    const int base = warp_fetch(work, n);
-    if (base >= n) break;
-    const int e = base + (threadIdx.x & 31);
-    if (e < n) {
-      ++nrays;
-      const float* q = rays + 9 * (size_t)e;
-      const f4 o = ym::mk(q[0], q[1], q[2], q[3]);
-      const f4 d = ym::mk(q[4], q[5], q[6], q[7]);
-      float len = q[8];
-      int light = -1;
-      light_test(sc, o, d, len, light);
-      RayIn r{o.x, o.y, o.z, len, d.x, d.y, d.z};
-      HitOut h;
-      if (!traverse<ANY>(sc, r, stack, TRACE_TB, stack_cap, h, wc)) ++overflow;
-      if (ANY) {
-        tri_out[e] = (h.tri >= 0 || light >= 0) ? 1 : 0;
-        if (t_out) t_out[e] = h.tri >= 0 ? h.t : len;
-      } else {
-        tri_out[e] = h.tri;
-        if (t_out) t_out[e] = h.tri >= 0 ? h.t : len;
-        // light index for a light hit is packed after the triangle array by the caller
-        if (h.tri < 0 && light >= 0) tri_out[e] = -2 - light;
-      }
-    }
-  }
-  flush_counts<ANY>(st, nrays, wc, overflow);
+  RaySrc<ANY> src{&sc, rays, tri_out, t_out, -1, 0.0f};
+  trace_loop<ANY>(sc, src, n, work, stack_cap, st);
 }
 
 static int stack_cap_for(int depth) { return depth + 2; }

@@ -20,9 +20,12 @@ struct Repacked {
   float4 root_lo{0, 0, 0, 0}, root_hi{0, 0, 0, 0};
 };
 
+// tree_mode: how the interior nodes above the reference leaves are laid out
+enum { TREE_REFERENCE = 0, TREE_SAH_OVER_LEAVES = 1 };
+
 // Returns 0, or -1 with a message when the node array is not a tree the reference
 // traversal could walk (child indices out of range, vert_len > 10, ...).
-int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, int n_node, Repacked& out,
-                 std::string& err);
+int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, int n_node, int tree_mode,
+                 Repacked& out, std::string& err);
 
 }  // namespace yc

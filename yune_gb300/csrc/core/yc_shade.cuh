@@ -271,6 +271,59 @@ __device__ __forceinline__ int sample_lights(const DevScene& sc, const Vtx& v, u
   return -1;
 }
 
+// ---- the BDPT variants (kernels/legacy/bdpt.cl) ----
+// evaluateBRDF, bdpt.cl:718-737: reflection vector without the normal flip
+__device__ __forceinline__ f4 brdf_b(f4 w_i, f4 w_o, f4 n, const yc_material& m, bool glossy, float rr_prob) {
+  f4 refl = ym::mul(2.0f, ym::dot(w_i, n)) * n - w_i;
+  refl = ym::normalize(refl);
+  if (!glossy) return (ld4(m.kd) * INV_PI_F) / rr_prob;
+  const float ca = ym::pow(ym::fmax(ym::dot(w_o, refl), 0.0f), ym::add(m.px, m.py));
+  const int pe = (int)ym::add(m.px, m.py);
+  return ((((ld4(m.ks) * ca) * (float)(pe + 2)) * INV_PI_F) * 0.5f) / rr_prob;
+}
+
+// phongSampleHemisphere, bdpt.cl:807-870: lobe axis without the normal flip
+__device__ __forceinline__ f4 sample_phong_b(const Vtx& v, const yc_material& m, f4 w_i, uint32_t& seed, float& pdf) {
+  f4 Nz = ym::mul(2.0f, ym::dot(w_i, v.n)) * v.n - w_i;
+  Nz = ym::normalize(Nz);
+  f4 Nx, Ny;
+  frame(Nz, Nx, Ny);
+  const float r1 = draw(seed);
+  const float r2 = draw(seed);
+  const int pe = (int)ym::add(m.px, m.py);
+  const float phi = ym::mul(ym::mul(2.0f, PI_F), r2);
+  const float ct = ym::pow(r1, ym::div(1.0f, (float)(pe + 1)));
+  float st = ym::sub(1.0f, ym::pow(r1, ym::div(2.0f, (float)(pe + 1))));
+  st = ym::sqrt(st);
+  const f4 d = ym::mk(ym::mul(st, ym::cos(phi)), ym::mul(st, ym::sin(phi)), ct, 0.0f);
+  const f4 dir = to_world(Nx, Ny, Nz, v.hp, d);
+  if (ym::dot(dir, v.n) < 0.0f) pdf = 0.0f;
+  else pdf = (float)((double)(pe + 1) * 0.5 * (double)INV_PI_F * (double)ym::pow(ct, (float)pe));
+  return dir;
+}
+
+// sampleGlossyPdf, bdpt.cl:1048-1105: probabilities raised by (1 - max)/2, no absorption
+__device__ __forceinline__ bool sample_glossy_b(const yc_material& m, uint32_t& seed, float& prob) {
+  const float r = draw(seed);
+  const f4 ks = ld4(m.ks), kd = ld4(m.kd);
+  if (ym::length3(ks) == 0.0f) { prob = 1.0f; return false; }
+  if (ym::length3(kd) == 0.0f || ym::add(ym::add(kd.x, kd.y), kd.z) == 0.0f) { prob = 1.0f; return true; }
+  const f4 sum = ks + kd;
+  const float mx = ym::max(sum.x, ym::max(sum.y, sum.z));
+  float pd, ps;
+  if (mx == sum.x) { pd = kd.x; ps = ks.x; }
+  else if (mx == sum.y) { pd = kd.y; ps = ks.y; }
+  else { pd = kd.z; ps = ks.z; }
+  if (mx < 1.0f) {
+    const float half = ym::div(ym::sub(1.0f, mx), 2.0f);
+    pd = ym::add(pd, half);
+    ps = ym::add(ps, half);
+  }
+  if (r < pd) { prob = pd; return false; }
+  prob = ps;
+  return true;
+}
+
 // getYluminance, udpt.cl:1121-1124
 __device__ __forceinline__ float luminance(f4 c) {
   return ym::add(ym::add(ym::mul(0.212671f, c.x), ym::mul(0.715160f, c.y)), ym::mul(0.072169f, c.z));

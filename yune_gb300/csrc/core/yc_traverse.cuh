@@ -147,7 +147,7 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayIn& r, int
   bool ok = true;
   for (;;) {
     // descend through interior nodes
-    while (link >= 0) {
+    while (link >= 0 && link != LINK_NONE) {
       const float4* nd = sc.nodes + 4 * (size_t)link;
       const float4 n0 = __ldg(nd + 0);
       const float4 n1 = __ldg(nd + 1);
@@ -222,6 +222,111 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayIn& r, int
   out.v = bv;
   out.tri = best_tri;
   return ok;
+}
+
+// ---- resumable walk for the persistent kernels ----
+// The state of one ray's walk, so a warp can run its lanes' walks step by step and hand
+// a lane a new ray as soon as its walk ends (the replenishing persistent warps of Aila
+// and Laine, "Understanding the Efficiency of Ray Traversal on GPUs", HPG 2009).
+struct Walk {
+  float ox, oy, oz, dx, dy, dz, ix, iy, iz;
+  float best, bu, bv;
+  int best_tri, best_rank;
+  int link, sp;
+  bool exact;
+};
+
+__device__ __forceinline__ void walk_begin(const DevScene& sc, const RayIn& r, Walk& w) {
+  w.ox = r.ox; w.oy = r.oy; w.oz = r.oz;
+  w.dx = r.dx; w.dy = r.dy; w.dz = r.dz;
+  w.ix = __frcp_rn(r.dx); w.iy = __frcp_rn(r.dy); w.iz = __frcp_rn(r.dz);
+  w.exact = isinf(w.ix) || isinf(w.iy) || isinf(w.iz);
+  w.best = r.tmax; w.bu = 0.0f; w.bv = 0.0f;
+  w.best_tri = -1; w.best_rank = -1;
+  w.sp = 0;
+  w.link = sc.root_link;
+  if (w.link != LINK_NONE && sc.root_test) {
+    float te;
+    const bool h = w.exact ? box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, sc.root_lo.x, sc.root_hi.x, sc.root_lo.y,
+                                     sc.root_hi.y, sc.root_lo.z, sc.root_hi.z, te)
+                           : box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, sc.root_lo.x, sc.root_hi.x, sc.root_lo.y,
+                                      sc.root_hi.y, sc.root_lo.z, sc.root_hi.z, te);
+    if (!h) w.link = LINK_NONE;
+  }
+}
+
+// One trip of the walk: descend to a leaf, test its triangles, pop the next subtree.
+// Returns true when the walk has ended (w.link == LINK_NONE); `overflow` is set when
+// the stack bound was reached (the walk then ends early).
+template <bool ANY>
+__device__ __forceinline__ bool walk_step(const DevScene& sc, Walk& w, int* stack, int stride, int stack_cap,
+                                          WalkCount& wc, bool& overflow) {
+  int link = w.link;
+  while (link >= 0 && link != LINK_NONE) {
+    const float4* nd = sc.nodes + 4 * (size_t)link;
+    const float4 n0 = __ldg(nd + 0);
+    const float4 n1 = __ldg(nd + 1);
+    const float4 n2 = __ldg(nd + 2);
+    const int2 n3 = __ldg(reinterpret_cast<const int2*>(nd + 3));
+    ++wc.nodes;
+    float t0, t1;
+    bool h0, h1;
+    if (!w.exact) {
+      h0 = box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, t0);
+      h1 = box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, t1);
+    } else {
+      h0 = box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, t0);
+      h1 = box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, t1);
+    }
+    const float cb = cull_bound(w.best);
+    h0 = h0 && n3.x != LINK_NONE && !(t0 > cb);
+    h1 = h1 && n3.y != LINK_NONE && !(t1 > cb);
+    if (h0 && h1) {
+      const bool swap = t1 < t0;
+      const int near_l = swap ? n3.y : n3.x, far_l = swap ? n3.x : n3.y;
+      const float far_t = swap ? t0 : t1;
+      if (w.sp >= stack_cap) { overflow = true; w.sp = 0; link = LINK_NONE; break; }
+      stack[(2 * w.sp + 0) * stride] = far_l;
+      stack[(2 * w.sp + 1) * stride] = __float_as_int(far_t);
+      ++w.sp;
+      link = near_l;
+    } else if (h0) {
+      link = n3.x;
+    } else if (h1) {
+      link = n3.y;
+    } else {
+      link = LINK_NONE;
+      break;
+    }
+  }
+  if (link != LINK_NONE) {
+    const int enc = ~link;
+    const int count = enc & 15;
+    const float4* tp = sc.tris + 3 * (size_t)(enc >> 4);
+    for (int k = 0; k < count; ++k) {
+      ++wc.tris;
+      const float4 a = __ldg(tp + 3 * k + 0);
+      const float4 b = __ldg(tp + 3 * k + 1);
+      const float4 c = __ldg(tp + 3 * k + 2);
+      TriHit th;
+      if (tri_test(w.ox, w.oy, w.oz, w.dx, w.dy, w.dz, a, b, c, w.best, w.best_rank, th)) {
+        w.best = th.t;
+        w.bu = th.u;
+        w.bv = th.v;
+        w.best_tri = __float_as_int(a.w);
+        w.best_rank = __float_as_int(b.w);
+        if (ANY) { w.sp = 0; w.link = LINK_NONE; return true; }
+      }
+    }
+  }
+  link = LINK_NONE;
+  while (w.sp > 0) {
+    --w.sp;
+    const float te = __int_as_float(stack[(2 * w.sp + 1) * stride]);
+    if (!(te > cull_bound(w.best))) { link = stack[(2 * w.sp) * stride]; break; }
+  }
+  w.link = link;
+  return link == LINK_NONE;
 }
 
 }  // namespace yc

@@ -151,7 +151,32 @@ def c1(width=1024, height=1024, spp=256, seed=0, level=6):
     return SceneData(tris, mats, lights, nodes, depth, camera(), width, height, spp, default_cfg(max_depth=16), "c1")
 
 
-CONFIGS = {"c0": c0, "c1": c1}
+def four_lights(lights, emission=(4.0, 7.0, 10.0, 13.0)):
+    """Four quad lights under the ceiling, spread across the box (the stress
+    configuration's multi-light set, picked per sample by the multiple-light CDF of
+    sampleLights, kernels/legacy/udpt.cl:632-698)."""
+    out = np.zeros(4, QUAD_LIGHT)
+    for i in range(4):
+        out[i] = lights[0]
+        out[i]["pos"][0] = -0.4 + 0.22 * i
+        out[i]["pos"][2] = -0.3 + 0.1 * i
+        out[i]["ke"][:3] = emission[i]
+    return out
+
+
+def c0_bdpt(width=512, height=512, spp=64, seed=0, bounces=8, lights=4):
+    """Cornell box with `lights` quad lights, naive BDPT with `bounces` vertices per
+    subpath (the stress configuration's integrator on the small scene)."""
+    b = Builder().cornell(seed=seed)
+    tris, mats, ls = b.arrays()
+    if lights == 4:
+        ls = four_lights(ls)
+    nodes, depth = build_bvh(tris, 20, 10)
+    return SceneData(tris, mats, ls, nodes, depth, camera(), width, height, spp,
+                     default_cfg(integrator=1, mis=0, bdpt_bounces=bounces), "c0_bdpt")
+
+
+CONFIGS = {"c0": c0, "c1": c1, "c0_bdpt": c0_bdpt}
 
 
 def pass_seeds(seed, n):
