@@ -49,6 +49,15 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu", action="store_true")
+    # batched (c2) and served (c3) comparisons against the plain per-pass loop
+    ap.add_argument("--jobs", type=int, default=64)
+    ap.add_argument("--spp", type=int, default=4, help="c2: passes per job")
+    ap.add_argument("--pool", type=int, default=0, help="batch path slots (0: 2M)")
+    ap.add_argument("--requests", type=int, default=40)
+    ap.add_argument("--rate", type=float, default=20.0, help="c3: Poisson arrival rate (req/s)")
+    ap.add_argument("--res-max", type=int, default=1024)
+    ap.add_argument("--spp-max", type=int, default=128)
+    ap.add_argument("--max-tris", type=int, default=500_000)
     return ap.parse_args()
 
 
@@ -139,10 +148,17 @@ def cpu_reference(scene, seeds, seconds, want_rays=True):
     not available."""
     from oracle import oracle_py as O
     W, H = scene.width, scene.height
-    cfg = scene.cfg
+    cfg = dict(scene.cfg)
     threads = os.cpu_count() or 1
-    use_ref = O.ref() is not None and cfg.get("brdf_model", 0) == 0 and not cfg.get("mis_lobe_fix", 0)
+    use_ref = O.ref() is not None
     kind = "reference" if use_ref else "port"
+    note = ""
+    if use_ref and (cfg.get("brdf_model", 0) or cfg.get("mis_lobe_fix", 0)):
+        # udpt.cl has neither the Oren-Nayar term nor the lobe fix: it runs its nearest
+        # variant (Lambert, reference MIS), and the oracle counts the rays of that variant
+        cfg["brdf_model"] = 0
+        cfg["mis_lobe_fix"] = 0
+        note = "; udpt.cl with -DMIS (Lambert diffuse, no lobe fix)"
     acc = np.zeros((H, W, 4), np.float32)
     band = max(1, H // 64)
     rows_done, t_total, rays = 0, 0.0, 0
@@ -166,7 +182,7 @@ def cpu_reference(scene, seeds, seconds, want_rays=True):
         y = r[1]
     value = rays / t_total / 1e6 if t_total > 0 else 0.0
     return {"value": value, "unit": METRIC, "cores": threads, "kind": kind,
-            "sample": "%d of %d rows x %d px, 1 pass, %.1f s" % (rows_done, H, W, t_total),
+            "sample": "%d of %d rows x %d px, 1 pass, %.1f s%s" % (rows_done, H, W, t_total, note),
             "samples_per_s": rows_done * W / t_total if t_total > 0 else 0.0}
 
 
@@ -290,8 +306,95 @@ def run_ours(args, rank, local, ws, dist):
     print(json.dumps(line))
 
 
+def run_c2(args):
+    """Mixed batch: every job rendered pass by pass (plain) and all jobs in one batch."""
+    from yune_gb300 import scenes, workloads
+    from yune_gb300.batch import Batch
+    from yune_gb300.core import Renderer
+    jobs = workloads.c2_jobs(n_jobs=args.jobs, spp=args.spp, max_tris=args.max_tris)
+    r = Renderer(0)
+    sids = [r.upload(s) for s in jobs]
+    seeds = [scenes.pass_seeds(1000 + i, s.spp) for i, s in enumerate(jobs)]
+    px = sum(s.width * s.height for s in jobs)
+    out = {}
+    # plain
+    accs = [r.alloc_accum(s.width, s.height) for s in jobs]
+    r.reset_stats()
+    r.synchronize()
+    t0 = time.perf_counter()
+    for s, sid, a, sd in zip(jobs, sids, accs, seeds):
+        r.set_camera(s.cam)
+        r.render_passes(sid, a, sd, reset_first=1, cfg=s.cfg)
+    r.synchronize()
+    tp = time.perf_counter() - t0
+    stp = r.stats()
+    plain_imgs = [r.read_accum(a) for a in accs[:4]]
+    for a in accs:
+        r.free_accum(a)
+    # batched
+    accs = [r.alloc_accum(s.width, s.height) for s in jobs]
+    b = Batch(r, pool_paths=args.pool)
+    for s, sid, a, sd in zip(jobs, sids, accs, seeds):
+        b.add_job(sid, a, s.cam, sd, s.cfg)
+    r.reset_stats()
+    r.synchronize()
+    t0 = time.perf_counter()
+    left = b.run()
+    r.synchronize()
+    tb = time.perf_counter() - t0
+    stb = r.stats()
+    same = all(np.array_equal(r.read_accum(a).view(np.int32), w.view(np.int32)) for a, w in zip(accs[:4], plain_imgs))
+    b.close()
+    out = {"metric": METRIC, "unit": METRIC, "config": {"workload": "c2 mixed batch", "jobs": len(jobs), "spp": args.spp,
+                                                         "pixels_per_pass": px,
+                                                         "triangles": int(sum(s.n_tri for s in jobs))},
+           "plain": {"value": stp["rays"] / tp / 1e6, "seconds": tp, "samples_per_s": stp["samples"] / tp},
+           "batched": {"value": stb["rays"] / tb / 1e6, "seconds": tb, "samples_per_s": stb["samples"] / tb,
+                       "unfinished": left},
+           "speedup": tp / tb, "equal_results": bool(same), "rays_equal": stp["rays"] == stb["rays"]}
+    r.close()
+    print(json.dumps(out))
+
+
+def run_c3(args):
+    """Served requests (continuous batching) against the plain first-come loop."""
+    from yune_gb300 import serve, workloads
+    from yune_gb300.core import Renderer
+    resident = workloads.c3_scenes(8, max_tris=args.max_tris)
+    reqs = workloads.c3_requests(args.requests, args.rate, len(resident), res_range=(256, args.res_max),
+                                 spp_range=(16, args.spp_max))
+    mk = lambda: [serve.Request(a, sc, w, h, spp, seed=i) for i, (a, sc, w, h, spp) in enumerate(reqs)]  # noqa: E731
+    r = Renderer(0)
+    r.reset_stats()
+    srv = serve.Server(r, resident, hbm_budget=40 << 30, pool_paths=args.pool or (1 << 21))
+    t0 = time.perf_counter()
+    served = srv.run(mk())
+    ts = time.perf_counter() - t0
+    sts = r.stats()
+    srv.close()
+    r.reset_stats()
+    t0 = time.perf_counter()
+    plain = serve.serve_plain(r, resident, mk())
+    tpl = time.perf_counter() - t0
+    stp = r.stats()
+    p50s, p99s = serve.percentiles(served)
+    p50p, p99p = serve.percentiles(plain)
+    out = {"metric": "p50/p99 time to target spp (s)", "unit": "s",
+           "config": {"workload": "c3 serving", "requests": len(reqs), "rate_per_s": args.rate,
+                      "resolution": [256, args.res_max], "spp": [16, args.spp_max],
+                      "scene_triangles": [int(s.n_tri) for s in resident]},
+           "served": {"p50": p50s, "p99": p99s, "Mrays_s": sts["rays"] / ts / 1e6, "seconds": ts},
+           "plain": {"p50": p50p, "p99": p99p, "Mrays_s": stp["rays"] / tpl / 1e6, "seconds": tpl}}
+    r.close()
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
+    if args.impl == "ours" and args.config == "c2":
+        return run_c2(args)
+    if args.impl == "ours" and args.config == "c3":
+        return run_c3(args)
     rank, local, ws, dist = dist_init(args)
     if args.impl == "reference":
         run_reference(args, rank, ws, dist)

@@ -107,6 +107,8 @@ int yc_set_lights(yc_ctx* ctx, int scene_id, const yc_quad_light* lights_host, i
 int yc_release_scene(yc_ctx* ctx, int scene_id);
 /* bytes the scene holds on the device */
 int yc_scene_bytes(yc_ctx* ctx, int scene_id, uint64_t* bytes);
+/* interior levels of the uploaded hierarchy (a traversal stack needs depth + 2 slots) */
+int yc_scene_depth(yc_ctx* ctx, int scene_id, int* depth);
 
 /* ---- camera (CLManager::setupCameraBuffer + the map/unmap of
  *      RendererCore::updateRenderKernelArgs, src/RendererCore.cpp:532-555) ---- */
@@ -162,6 +164,38 @@ int yc_trace(yc_ctx* ctx, int scene_id, const float* rays_host, int n, int any_h
  * Asynchronous on the context stream. */
 int yc_trace_device(yc_ctx* ctx, int scene_id, const float* rays_dev, int n, int any_hit, int* tri_dev,
                     float* t_dev);
+
+/* ---- batch and serving engine ----
+ * No single counterpart in the reference, which renders one frame per launch. A batch
+ * renders many jobs (scene, camera, accumulator, pass seeds) in one persistent
+ * wavefront: a fixed pool of path slots takes pixel tasks from all jobs, renders each
+ * pixel's passes in order (bit-identical per pixel to yc_render_pass with the same
+ * seeds) and takes the next task, so jobs of any size and resolution keep the GPU full.
+ * Rounds are captured in a CUDA graph. Jobs may be added while the batch runs
+ * (serving). */
+typedef struct yc_batch yc_batch;
+typedef struct yc_batch_cfg {
+  int32_t pool_paths;          /* path slots (wavefront size); 0 = 2,097,152 */
+  int32_t rounds_per_launch;   /* rounds per graph launch (even); 0 = 8 */
+  int32_t logic_blocks_per_sm; /* logic kernel CTAs per SM; 0 = 4 */
+  int32_t use_graph;           /* 1 = capture the rounds in a CUDA graph */
+  int32_t max_jobs;            /* capacity of the job table; 0 = 1024 */
+  int32_t stack_cap;           /* traversal stack entries; 0 = from the first jobs' scenes */
+} yc_batch_cfg;
+int yc_batch_create(yc_ctx* ctx, const yc_batch_cfg* cfg, yc_batch** out);
+/* Adds a job: n_pass passes of scene_id into accum_id seen from *cam, pass k with
+ * pass_seeds_host[k]; reset_first = 1 restarts the accumulator (udpt.cl:196-199).
+ * cfg: integrator must be YC_UDPT. */
+int yc_batch_add_job(yc_batch* b, int scene_id, int accum_id, const yc_cam* cam, const uint32_t* pass_seeds_host,
+                     int n_pass, int reset_first, const yc_pass_cfg* cfg, int* job_id);
+/* Runs up to max_launches graph launches (0 = until every job is done) and reports how
+ * many jobs are still unfinished. */
+int yc_batch_run(yc_batch* b, int max_launches, int* unfinished_jobs);
+/* pixels whose passes are all done, and the job's pixel count */
+int yc_batch_job_progress(yc_batch* b, int job_id, int64_t* pixels_done, int64_t* pixels_total);
+/* A batch belongs to its context: yc_destroy releases the context's remaining batches,
+ * after which their handles must not be used. */
+int yc_batch_destroy(yc_batch* b);
 
 /* ---- options ---- */
 enum {

@@ -156,6 +156,43 @@ int or_render_f64(const yc_triangle* t, int nt, const yc_material* m, int nm, co
                                 row0, row1, out);
 }
 
+// Converged-image reference: n_pass passes (seeds[k]) of the FP64 restatement over an
+// explicit pixel list, accumulated as a running mean into out (n x 4 doubles). Used for
+// the RMSE of a configuration against a high-spp double-precision image.
+int or_render_pixels_f64(const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_bvh_node* b, int nb,
+                         const yc_quad_light* l, int nl, const yc_cam* cam, int W, int H, const int* xs,
+                         const int* ys, int n, const uint32_t* seeds, int n_pass, const or_cfg* cfg, int bdpt_bounces,
+                         int threads, double* out) {
+  if (!cam || !xs || !ys || !seeds || !out || n < 0 || n_pass <= 0) return -1;
+  const orc::Scene<double> sc = mk_scene<double>(t, nt, m, nm, b, nb, l, nl);
+  const orc::Config k = to_cfg(cfg);
+  if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+  std::atomic<int> next(0);
+  auto work = [&]() {
+    orc::Counters cnt;
+    orc::BdptTracer<double> tr(sc, k, cnt, bdpt_bounces > 0 ? bdpt_bounces : 20);
+    for (;;) {
+      const int i = next.fetch_add(1);
+      if (i >= n) break;
+      orc::V4<double> acc{0, 0, 0, 0};
+      for (int p = 0; p < n_pass; ++p) {
+        const orc::V4<double> c = bdpt_bounces > 0 ? orc::pixel_sample_bdpt<double>(tr, *cam, xs[i], ys[i], W, H, seeds[p])
+                                                   : orc::pixel_sample<double>(tr, *cam, xs[i], ys[i], W, H, seeds[p]);
+        acc = orc::accumulate<double>(c, acc, p == 0 ? 1 : 0);
+      }
+      out[4 * (size_t)i + 0] = acc.x;
+      out[4 * (size_t)i + 1] = acc.y;
+      out[4 * (size_t)i + 2] = acc.z;
+      out[4 * (size_t)i + 3] = acc.w;
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int i = 1; i < threads; ++i) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
+  return 0;
+}
+
 // tonemap, kernels/post-proc/tonemap.cl:14-47: Reinhard with L_white = 1 on Y + 0.001,
 // then pow(., 1/2.2); the clamp result is discarded as in tonemap.cl:32.
 int or_tonemap(const float* in, int W, int H, float* out) {

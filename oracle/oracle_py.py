@@ -52,6 +52,8 @@ def orc():
         L.or_wang_hash.restype = u32
         L.or_xor_shift.argtypes = [u32]
         L.or_xor_shift.restype = u32
+        L.or_render_pixels_f64.argtypes = [vp, i32, vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, vp, i32, vp, i32,
+                                           C.POINTER(OrCfg), i32, i32, vp]
         L.or_brdf.argtypes = [vp, i32, vp, i32, i32, vp, vp, vp, vp, i32, C.c_float, i32, vp]
         _orc = L
     return _orc
@@ -121,6 +123,23 @@ def render_bdpt(scene, accum, rand_seed, reset, bounces, threads=0, rows=None, f
     if rc != 0:
         raise RuntimeError("or_render_bdpt failed: %d" % rc)
     return {k: getattr(cnt, k) for k, _ in OrCounters._fields_}
+
+
+def reference_pixels_f64(scene, xs, ys, seeds, cfg, bdpt_bounces=0, threads=0):
+    """FP64 running mean over len(seeds) passes at the given pixels (n x 4 doubles)."""
+    L = orc()
+    xs = np.ascontiguousarray(xs, np.int32)
+    ys = np.ascontiguousarray(ys, np.int32)
+    sd = np.ascontiguousarray(seeds, np.uint32)
+    out = np.zeros((len(xs), 4), np.float64)
+    c = cfg_of(cfg)
+    rc = L.or_render_pixels_f64(_p(scene.tris), len(scene.tris), _p(scene.mats), len(scene.mats), _p(scene.nodes),
+                                len(scene.nodes), _p(scene.lights), len(scene.lights), _p(scene.cam), scene.width,
+                                scene.height, _p(xs), _p(ys), len(xs), _p(sd), len(sd), C.byref(c), bdpt_bounces,
+                                threads, _p(out))
+    if rc != 0:
+        raise RuntimeError("or_render_pixels_f64 failed")
+    return out
 
 
 def trace(scene, rays9, any_hit=False, heap_size=1500):

@@ -1,0 +1,48 @@
+"""Converged FP64 references for the RMSE of each configuration.
+
+65,536 passes of the double-precision restatement of the reference kernels
+(oracle/udpt_oracle.hpp, oracle/bdpt_oracle.hpp) on a 32 x 32 grid of pixels of each
+configuration's frame, with pass seeds from mt19937(7777) (independent of the seeds the
+benchmark renders with). Writes tests/golden/fp64_<config>.npz. Runs on the CPU:
+
+    python tests/golden/make_fp64_refs.py [config ...]
+"""
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle_py as O  # noqa: E402
+from yune_gb300 import scenes  # noqa: E402
+
+N_PASS = 65536
+GRID = 32
+
+
+def grid(s):
+    xs = (np.arange(GRID) * s.width) // GRID + s.width // (2 * GRID)
+    ys = (np.arange(GRID) * s.height) // GRID + s.height // (2 * GRID)
+    X, Y = np.meshgrid(xs, ys)
+    return X.ravel().astype(np.int32), Y.ravel().astype(np.int32)
+
+
+def make(name):
+    s = scenes.CONFIGS[name]()
+    X, Y = grid(s)
+    seeds = scenes.mt19937(7777, N_PASS)
+    bounces = s.cfg["bdpt_bounces"] if s.cfg.get("integrator", 0) == 1 else 0
+    t0 = time.time()
+    ref = O.reference_pixels_f64(s, X, Y, seeds, s.cfg, bdpt_bounces=bounces)
+    np.savez_compressed(os.path.join(HERE, "fp64_%s.npz" % name), xs=X, ys=Y, ref=ref, n_pass=N_PASS,
+                        seconds=time.time() - t0)
+    print(name, "done in %.0f s" % (time.time() - t0))
+
+
+if __name__ == "__main__":
+    for name in (sys.argv[1:] or ["c0", "c1", "c0_bdpt"]):
+        make(name)

@@ -36,6 +36,12 @@ class KernelTimes(C.Structure):
                 ("occlusion_launches", C.c_uint64), ("logic_launches", C.c_uint64), ("rounds", C.c_uint64)]
 
 
+class BatchCfg(C.Structure):
+    """yc_batch_cfg"""
+    _fields_ = [("pool_paths", i32), ("rounds_per_launch", i32), ("logic_blocks_per_sm", i32), ("use_graph", i32),
+                ("max_jobs", i32), ("stack_cap", i32)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     # core
@@ -47,6 +53,7 @@ SIGNATURES = {
     "yc_set_lights": (i32, [vp, i32, vp, i32]),
     "yc_release_scene": (i32, [vp, i32]),
     "yc_scene_bytes": (i32, [vp, i32, C.POINTER(C.c_uint64)]),
+    "yc_scene_depth": (i32, [vp, i32, C.POINTER(i32)]),
     "yc_set_camera": (i32, [vp, vp]),
     "yc_alloc_accum": (i32, [vp, i32, i32, C.POINTER(i32)]),
     "yc_free_accum": (i32, [vp, i32]),
@@ -67,6 +74,11 @@ SIGNATURES = {
     "yc_get_kernel_times": (i32, [vp, C.POINTER(KernelTimes)]),
     "yc_flush_l2": (i32, [vp, C.c_size_t]),
     "yc_measure_l2_gbs": (i32, [vp, C.c_size_t, i32, C.POINTER(C.c_double)]),
+    "yc_batch_create": (i32, [vp, C.POINTER(BatchCfg), C.POINTER(vp)]),
+    "yc_batch_add_job": (i32, [vp, i32, i32, vp, vp, i32, i32, C.POINTER(PassCfg), C.POINTER(i32)]),
+    "yc_batch_run": (i32, [vp, i32, C.POINTER(i32)]),
+    "yc_batch_job_progress": (i32, [vp, i32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "yc_batch_destroy": (i32, [vp]),
     # host producers
     "yh_bvh_build": (i32, [vp, i32, i32, i32, C.POINTER(vp)]),
     "yh_bvh_node_count": (i32, [vp]),

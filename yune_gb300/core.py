@@ -8,6 +8,7 @@
     img = r.tonemap(aid)                 # the `tonemap` pass
 """
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -33,9 +34,12 @@ class Renderer:
         N.check(self.L.yc_create(device, C.byref(h)), "yc_create")
         self.h = h
         self._accum_shape = {}
+        self._children = weakref.WeakSet()   # batches: the context releases them
 
     def close(self):
         if getattr(self, "h", None):
+            for ch in list(self._children):
+                ch._detach()
             self.L.yc_destroy(self.h)
             self.h = None
 
@@ -54,6 +58,11 @@ class Renderer:
                                        ptr(scene.nodes), len(scene.nodes), ptr(scene.lights), len(scene.lights),
                                        C.byref(sid)), "yc_upload_scene")
         return sid.value
+
+    def scene_depth(self, sid):
+        d = C.c_int()
+        N.check(self.L.yc_scene_depth(self.h, sid, C.byref(d)), "yc_scene_depth")
+        return d.value
 
     def release(self, sid):
         N.check(self.L.yc_release_scene(self.h, sid), "yc_release_scene")

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "yc_bdpt.h"
+#include "yc_engine.h"
 #include "yc_internal.h"
 #include "yc_noalloc.h"
 #include "yc_repack.h"
@@ -74,8 +75,14 @@ struct Accum {
 
 }  // namespace
 
+struct yc_batch;
+namespace {
+void free_batch(yc_batch* b);
+}
+
 struct yc_ctx {
   int device = 0;
+  std::vector<yc_batch*> batches;   // owned: destroyed with the context
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::map<int, std::unique_ptr<Scene>> scenes;
@@ -337,6 +344,8 @@ int yc_destroy(yc_ctx* c) {
   if (!c) return YC_OK;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  for (yc_batch* b : c->batches) free_batch(b);   // batches never outlive their context
+  c->batches.clear();
   c->scenes.clear();
   c->accums.clear();
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
@@ -432,6 +441,14 @@ int yc_scene_bytes(yc_ctx* c, int scene_id, uint64_t* bytes) {
   Scene* s = find_scene(c, scene_id);
   if (!s) return fail(YC_E_NOTFOUND, "unknown scene");
   *bytes = s->bytes;
+  return YC_OK;
+}
+
+int yc_scene_depth(yc_ctx* c, int scene_id, int* depth) {
+  if (!c || !depth) return fail(YC_E_INVALID, "NULL argument");
+  Scene* s = find_scene(c, scene_id);
+  if (!s) return fail(YC_E_NOTFOUND, "unknown scene");
+  *depth = s->dev.depth;
   return YC_OK;
 }
 
@@ -686,6 +703,259 @@ int yc_measure_l2_gbs(yc_ctx* c, size_t bytes, int iters, double* gbs) {
 int yc_last_pass_ms(yc_ctx* c, float* ms) {
   if (!c || !ms) return fail(YC_E_INVALID, "NULL argument");
   *ms = c->last_ms;
+  return YC_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// batch and serving engine (engine.cu)
+struct yc_batch {
+  yc_ctx* ctx = nullptr;
+  yc_batch_cfg cfg{};
+  int pool = 0;
+  DevBuf<int4> misc;
+  DevBuf<float4> f4bufs[12];
+  DevBuf<int2> job_pass;
+  DevBuf<int> free_stack;
+  DevBuf<int> q[4];
+  DevBuf<yc::RoundCounters> rc;
+  DevBuf<yc::BatchCtl> ctl;
+  DevBuf<yc::BatchJob> jobs;
+  DevBuf<unsigned long long> job_done;
+  std::vector<std::unique_ptr<DevBuf<uint32_t>>> seeds;
+  std::vector<yc::BatchJob> host_jobs;
+  long long task_total = 0;
+  int stack_cap = 0;
+  int grid_c = 0, grid_a = 0, logic_grid = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool started = false;
+  // pinned readback
+  yc::BatchCtl* ctl_host = nullptr;
+  yc::RoundCounters* rc_host = nullptr;
+  unsigned long long* done_host = nullptr;
+};
+
+namespace {
+
+// releases a batch; the owning context must still be alive
+void free_batch(yc_batch* b) {
+  if (b->ctx && b->ctx->stream) cudaStreamSynchronize(b->ctx->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->ctl_host) cudaFreeHost(b->ctl_host);
+  if (b->rc_host) cudaFreeHost(b->rc_host);
+  if (b->done_host) cudaFreeHost(b->done_host);
+  delete b;
+}
+
+yc::PathState batch_state(yc_batch* b) {
+  yc::PathState ps;
+  ps.misc = b->misc.p;
+  float4** f[12] = {&ps.thr, &ps.thr_next, &ps.direct, &ps.indirect, &ps.ls, &ps.hp,
+                    &ps.nrm, &ps.wo, &ps.wi, &ps.ro, &ps.rd, &ps.hit};
+  for (int i = 0; i < 12; ++i) *f[i] = b->f4bufs[i].p;
+  return ps;
+}
+
+// one round: fill idle slots, trace both queues, step every path (A -> B)
+int batch_round(yc_batch* b, int cur) {
+  yc_ctx* c = b->ctx;
+  const yc::PathState ps = batch_state(b);
+  int* in_c = b->q[2 * cur].p;
+  int* in_a = b->q[2 * cur + 1].p;
+  int* out_c = b->q[2 * (1 - cur)].p;
+  int* out_a = b->q[2 * (1 - cur) + 1].p;
+  yc::RoundCounters* rin = b->rc.p + cur;
+  yc::RoundCounters* rout = b->rc.p + (1 - cur);
+  yc::launch_batch_fill(b->jobs.p, b->ctl.p, ps, b->job_pass.p, b->free_stack.p, in_c, rin, c->stats.p, b->job_done.p,
+                        1, c->stream);
+  yc::launch_batch_trace(false, b->jobs.p, b->job_pass.p, in_c, &rin->n_closest, &rin->work_closest, ps.ro, ps.rd,
+                         ps.hit, c->stats.p, b->stack_cap, b->grid_c, c->stream);
+  yc::launch_batch_trace(true, b->jobs.p, b->job_pass.p, in_a, &rin->n_any, &rin->work_any, ps.ro, ps.rd, ps.hit,
+                         c->stats.p, b->stack_cap, b->grid_a, c->stream);
+  YC_CUDA(cudaMemsetAsync(rout, 0, sizeof(yc::RoundCounters), c->stream));
+  yc::launch_batch_logic(b->jobs.p, b->ctl.p, ps, b->job_pass.p, b->free_stack.p, in_c, in_a, rin, out_c, out_a, rout,
+                         c->stats.p, b->job_done.p, b->logic_grid, c->stream);
+  YC_CUDA(cudaPeekAtLastError());
+  return 0;
+}
+
+int batch_launch(yc_batch* b) {
+  yc_ctx* c = b->ctx;
+  const int rounds = b->cfg.rounds_per_launch;
+  if (b->cfg.use_graph) {
+    if (!b->exec) {
+      YC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      int r = 0;
+      for (int k = 0; k < rounds && !r; ++k) r = batch_round(b, k & 1);
+      cudaGraph_t g = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+      if (r) { if (g) cudaGraphDestroy(g); return r; }
+      if (e != cudaSuccess) return fail(YC_E_LAUNCH, std::string("graph capture: ") + cudaGetErrorString(e));
+      b->graph = g;
+      YC_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    }
+    YC_CUDA(cudaGraphLaunch(b->exec, c->stream));
+  } else {
+    for (int k = 0; k < rounds; ++k)
+      if (int r = batch_round(b, k & 1)) return r;
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
+  if (!c || !out) return fail(YC_E_INVALID, "NULL argument");
+  *out = nullptr;
+  std::unique_ptr<yc_batch> b(new (std::nothrow) yc_batch);
+  if (!b) return fail(YC_E_NOMEM, "host allocation failed");
+  b->ctx = c;
+  if (cfg) b->cfg = *cfg;
+  if (b->cfg.pool_paths <= 0) b->cfg.pool_paths = 1 << 21;
+  if (b->cfg.rounds_per_launch <= 0) b->cfg.rounds_per_launch = 8;
+  if (b->cfg.rounds_per_launch & 1) b->cfg.rounds_per_launch += 1;
+  if (b->cfg.logic_blocks_per_sm <= 0) b->cfg.logic_blocks_per_sm = 4;
+  if (b->cfg.max_jobs <= 0) b->cfg.max_jobs = 1024;
+  const size_t n = (size_t)b->cfg.pool_paths;
+  YC_CUDA(cudaSetDevice(c->device));
+  YC_CUDA(b->misc.alloc(n));
+  for (auto& f : b->f4bufs) YC_CUDA(f.alloc(n));
+  YC_CUDA(b->job_pass.alloc(n));
+  YC_CUDA(b->free_stack.alloc(n));
+  for (auto& q : b->q) YC_CUDA(q.alloc(n));
+  YC_CUDA(b->rc.alloc(2));
+  YC_CUDA(b->ctl.alloc(1));
+  YC_CUDA(b->jobs.alloc(b->cfg.max_jobs));
+  YC_CUDA(b->job_done.alloc(b->cfg.max_jobs));
+  YC_CUDA(cudaMallocHost(&b->ctl_host, sizeof(yc::BatchCtl)));
+  YC_CUDA(cudaMallocHost(&b->rc_host, 2 * sizeof(yc::RoundCounters)));
+  YC_CUDA(cudaMallocHost(&b->done_host, b->cfg.max_jobs * sizeof(unsigned long long)));
+  // every slot starts on the free stack
+  std::vector<int> fs(n);
+  for (size_t i = 0; i < n; ++i) fs[i] = (int)(n - 1 - i);
+  YC_CUDA(cudaMemcpyAsync(b->free_stack.p, fs.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  yc::BatchCtl ctl{};
+  ctl.free_top = (int)n;
+  YC_CUDA(cudaMemcpyAsync(b->ctl.p, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, c->stream));
+  YC_CUDA(cudaMemsetAsync(b->rc.p, 0, 2 * sizeof(yc::RoundCounters), c->stream));
+  YC_CUDA(cudaMemsetAsync(b->job_done.p, 0, b->cfg.max_jobs * sizeof(unsigned long long), c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  b->logic_grid = std::max(1, c->sm_count) * b->cfg.logic_blocks_per_sm;
+  *out = b.release();
+  c->batches.push_back(*out);
+  return YC_OK;
+}
+
+int yc_batch_add_job(yc_batch* b, int scene_id, int accum_id, const yc_cam* cam, const uint32_t* seeds, int n_pass,
+                     int reset_first, const yc_pass_cfg* cfg, int* job_id) {
+  if (!b || !cam || !seeds || n_pass <= 0 || !job_id) return fail(YC_E_INVALID, "bad argument");
+  if (int r = validate_cfg(cfg)) return r;
+  if (cfg->integrator != YC_UDPT) return fail(YC_E_INVALID, "the batch engine runs the unidirectional integrator");
+  yc_ctx* c = b->ctx;
+  Scene* sc = find_scene(c, scene_id);
+  if (!sc) return fail(YC_E_NOTFOUND, "unknown scene");
+  Accum* ac = find_accum(c, accum_id);
+  if (!ac) return fail(YC_E_NOTFOUND, "unknown accumulator");
+  if ((int)b->host_jobs.size() >= b->cfg.max_jobs) return fail(YC_E_BUDGET, "job table full");
+  const int need_cap = sc->dev.depth + 2;
+  if (!b->started) b->stack_cap = std::max(b->stack_cap, b->cfg.stack_cap > 0 ? b->cfg.stack_cap : need_cap);
+  else if (need_cap > b->stack_cap)
+    return fail(YC_E_INVALID, "scene BVH deeper than the running batch's traversal stack");
+  std::unique_ptr<DevBuf<uint32_t>> sd(new DevBuf<uint32_t>);
+  YC_CUDA(sd->alloc(n_pass));
+  YC_CUDA(cudaMemcpyAsync(sd->p, seeds, n_pass * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+  yc::BatchJob j{};
+  j.pp.sc = sc->dev;
+  j.pp.cam = *cam;
+  j.pp.accum = ac->buf.p;
+  j.pp.width = ac->w;
+  j.pp.height = ac->h;
+  j.pp.tile_w = ac->w;
+  j.pp.tile_h = ac->h;
+  j.pp.gi_check = 1;
+  j.pp.mis = cfg->mis;
+  j.pp.rr_threshold = cfg->rr_threshold;
+  j.pp.max_depth = cfg->max_depth;
+  j.pp.brdf_model = cfg->brdf_model;
+  j.pp.mis_lobe_fix = cfg->mis_lobe_fix;
+  j.seeds = sd->p;
+  j.n_pass = n_pass;
+  j.reset_first = reset_first;
+  j.task_base = b->task_total;
+  j.n_pix = ac->w * ac->h;
+  const int id = (int)b->host_jobs.size();
+  YC_CUDA(cudaMemcpyAsync(b->jobs.p + id, &j, sizeof(j), cudaMemcpyHostToDevice, c->stream));
+  b->task_total += j.n_pix;
+  // publish: job count and task total (read by the kernels between launches)
+  const int nj = id + 1;
+  YC_CUDA(cudaMemcpyAsync(&b->ctl.p->n_jobs, &nj, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  const unsigned long long tt = (unsigned long long)b->task_total;
+  YC_CUDA(cudaMemcpyAsync(&b->ctl.p->task_total, &tt, sizeof(tt), cudaMemcpyHostToDevice, c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  b->host_jobs.push_back(j);
+  b->seeds.push_back(std::move(sd));
+  *job_id = id;
+  return YC_OK;
+}
+
+int yc_batch_run(yc_batch* b, int max_launches, int* unfinished) {
+  if (!b) return fail(YC_E_INVALID, "batch is NULL");
+  yc_ctx* c = b->ctx;
+  YC_CUDA(cudaSetDevice(c->device));
+  if (!b->started) {
+    if (b->stack_cap <= 0) b->stack_cap = b->cfg.stack_cap > 0 ? b->cfg.stack_cap : 32;
+    b->grid_c = yc::batch_trace_grid(false, b->stack_cap);
+    b->grid_a = yc::batch_trace_grid(true, b->stack_cap);
+    if (b->grid_c <= 0 || b->grid_a <= 0) return fail(YC_E_LAUNCH, "batch trace kernel cannot be resident");
+    b->started = true;
+  }
+  YC_CUDA(cudaEventRecord(c->ev0, c->stream));
+  int launches = 0;
+  for (;;) {
+    if (int r = batch_launch(b)) return r;
+    ++launches;
+    YC_CUDA(cudaMemcpyAsync(b->ctl_host, b->ctl.p, sizeof(yc::BatchCtl), cudaMemcpyDeviceToHost, c->stream));
+    YC_CUDA(cudaMemcpyAsync(b->rc_host, b->rc.p, 2 * sizeof(yc::RoundCounters), cudaMemcpyDeviceToHost, c->stream));
+    YC_CUDA(cudaMemcpyAsync(b->done_host, b->job_done.p, b->host_jobs.size() * sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, c->stream));
+    YC_CUDA(cudaStreamSynchronize(c->stream));
+    int left = 0;
+    for (size_t i = 0; i < b->host_jobs.size(); ++i)
+      if (b->done_host[i] < (unsigned long long)b->host_jobs[i].n_pix) ++left;
+    if (unfinished) *unfinished = left;
+    const bool idle = b->rc_host[0].n_closest == 0 && b->rc_host[0].n_any == 0 &&
+                      b->ctl_host->free_top == b->cfg.pool_paths;
+    if (left == 0 || (idle && b->ctl_host->task_next >= b->ctl_host->task_total)) break;
+    if (max_launches > 0 && launches >= max_launches) break;
+  }
+  YC_CUDA(cudaEventRecord(c->ev1, c->stream));
+  YC_CUDA(cudaEventSynchronize(c->ev1));
+  YC_CUDA(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
+  return YC_OK;
+}
+
+int yc_batch_job_progress(yc_batch* b, int job_id, int64_t* done, int64_t* total) {
+  if (!b || job_id < 0 || job_id >= (int)b->host_jobs.size()) return fail(YC_E_NOTFOUND, "unknown job");
+  unsigned long long d = 0;
+  YC_CUDA(cudaMemcpyAsync(&d, b->job_done.p + job_id, sizeof(d), cudaMemcpyDeviceToHost, b->ctx->stream));
+  YC_CUDA(cudaStreamSynchronize(b->ctx->stream));
+  if (done) *done = (int64_t)d;
+  if (total) *total = b->host_jobs[job_id].n_pix;
+  return YC_OK;
+}
+
+int yc_batch_destroy(yc_batch* b) {
+  if (!b) return YC_OK;
+  if (b->ctx) {
+    auto& v = b->ctx->batches;
+    v.erase(std::remove(v.begin(), v.end(), b), v.end());
+  }
+  free_batch(b);
   return YC_OK;
 }
 

@@ -1,0 +1,278 @@
+// engine.cu -- batch and serving engine: many render jobs in one persistent wavefront.
+//
+// A batch owns a fixed pool of path slots. Every job (scene, camera, accumulator, pass
+// seeds) contributes one pixel task per pixel; a slot takes a task, renders that pixel's
+// passes one after the other (each pass is a full `pathtracer` sample, udpt.cl:158-211,
+// accumulated in pass order, so every pixel's result is bit-identical to the per-pass
+// path), then takes the next task. Slots regenerate in place inside the logic kernel
+// (path regeneration), so the wavefront stays full while jobs of any size and
+// resolution start and finish; the extend and occlusion kernels read each ray's scene
+// from the job table, so one launch walks many BVHs. Jobs can be added between launches
+// (serving); task claims go through a compare-and-swap on the task cursor so tasks
+// admitted later are never skipped.
+#include <cuda_runtime.h>
+
+#include "yc_engine.h"
+#include "yc_trace_loop.cuh"
+#include "yc_udpt.cuh"
+
+namespace yc {
+
+constexpr int ENGINE_TB = 256;
+
+__device__ __forceinline__ int job_of_task(const BatchJob* jobs, int n_jobs, unsigned long long t) {
+  int lo = 0, hi = n_jobs - 1;
+  while (lo < hi) {   // last job with task_base <= t
+    const int mid = (lo + hi + 1) >> 1;
+    if ((unsigned long long)jobs[mid].task_base <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// first pass (or the next pass) of pixel `pix` of job `job` in slot p
+__device__ __forceinline__ void start_pass(const BatchJob& J, int job, int pix, int pass, int p, const PathState& ps,
+                                           int2* job_pass) {
+  const int W = J.pp.width;
+  uint32_t seed;
+  f4 o, d;
+  float len;
+  int k;
+  camera_ray(J.pp, pix % W, pix / W, J.seeds[pass], seed, o, d, len, k);
+  ps.misc[p] = make_int4((int)seed, pix, pack_misc(S_PRIMARY, 0, -1, k), 0);
+  ps.ro[p] = make_float4(o.x, o.y, o.z, len);
+  ps.rd[p] = make_float4(d.x, d.y, d.z, d.w);
+  job_pass[p] = make_int2(job, pass);
+}
+
+// Claims up to `want` consecutive tasks below task_total; returns the first and sets got.
+__device__ __forceinline__ unsigned long long claim_tasks(BatchCtl* ctl, int want, int& got) {
+  unsigned long long t = atomicAdd(&ctl->task_next, 0ull);
+  const unsigned long long total = ctl->task_total;
+  for (int tries = 0; tries < 1024; ++tries) {
+    if (t >= total) { got = 0; return t; }
+    const unsigned long long n = (total - t) < (unsigned long long)want ? (total - t) : (unsigned long long)want;
+    const unsigned long long old = atomicCAS(&ctl->task_next, t, t + n);
+    if (old == t) { got = (int)n; return t; }
+    t = old;
+  }
+  got = 0;   // heavy contention: leave the tasks to the next fill
+  return t;
+}
+
+// ---- fill: idle slots (on the free stack) take new tasks ----
+__global__ void __launch_bounds__(ENGINE_TB) k_batch_fill(const BatchJob* __restrict__ jobs, BatchCtl* ctl,
+                                                          PathState ps, int2* job_pass, int* free_stack,
+                                                          int* q_closest, RoundCounters* rc, DevStats* st) {
+  __shared__ unsigned long long s_t0;
+  __shared__ int s_n, s_top;
+  // one block claims for the whole grid: grid is launched with a single block
+  if (threadIdx.x == 0) {
+    const int free_n = ctl->free_top;
+    int got = 0;
+    const unsigned long long t0 = free_n > 0 ? claim_tasks(ctl, free_n, got) : 0ull;
+    s_t0 = t0;
+    s_n = got;
+    s_top = free_n - got;
+    ctl->free_top = free_n - got;
+  }
+  __syncthreads();
+  const int n = s_n;
+  const int n_jobs = ctl->n_jobs;
+  const int lane = threadIdx.x & 31;
+  for (int base = 0; base < n; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const bool active = i < n;
+    int p = -1;
+    if (active) {
+      p = free_stack[s_top + i];
+      const unsigned long long t = s_t0 + (unsigned long long)i;
+      const int job = job_of_task(jobs, n_jobs, t);
+      start_pass(jobs[job], job, (int)(t - (unsigned long long)jobs[job].task_base), 0, p, ps, job_pass);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, active);
+    int b = 0;
+    if (lane == 0 && m) b = atomicAdd(&rc->n_closest, __popc(m));
+    b = __shfl_sync(0xffffffffu, b, 0);
+    if (active) q_closest[b + __popc(m & ((1u << lane) - 1))] = p;
+    if (lane == 0 && m) {
+      atomicAdd(&st->primary, (unsigned long long)__popc(m));
+      atomicAdd(&st->rays, (unsigned long long)__popc(m));
+      atomicAdd(&st->traversed, (unsigned long long)__popc(m));
+    }
+  }
+}
+
+void launch_batch_fill(const BatchJob* jobs, BatchCtl* ctl, const PathState& ps, int2* job_pass, int* free_stack,
+                       int* q_closest, RoundCounters* rc, DevStats* st, unsigned long long* job_done, int grid,
+                       cudaStream_t s) {
+  (void)job_done;
+  (void)grid;
+  k_batch_fill<<<1, ENGINE_TB, 0, s>>>(jobs, ctl, ps, job_pass, free_stack, q_closest, rc, st);
+}
+
+// ---- logic with regeneration ----
+__global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __restrict__ jobs, BatchCtl* ctl,
+                                                           PathState ps, int2* job_pass, int* free_stack,
+                                                           const int* __restrict__ in_closest,
+                                                           const int* __restrict__ in_any, const RoundCounters* rc_in,
+                                                           int* out_closest, int* out_any, RoundCounters* rc_out,
+                                                           DevStats* st, unsigned long long* job_done) {
+  __shared__ unsigned long long s_cnt[8];
+  if (threadIdx.x < 8) s_cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const int nc = rc_in->n_closest, na = rc_in->n_any;
+  const int n = nc + na;
+  const int lane = threadIdx.x & 31;
+  const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int warps_total = (gridDim.x * blockDim.x) >> 5;
+  const int n_jobs = ctl->n_jobs;
+  for (int wbase = warp_global * 32; wbase < n; wbase += warps_total * 32) {
+    const int e = wbase + lane;
+    int emit = 0;
+    int p = -1;
+    bool need_task = false;
+    LogicCounts lc;
+    if (e < n) {
+      p = e < nc ? in_closest[e] : in_any[e - nc];
+      const int2 jp = job_pass[p];
+      const BatchJob& J = jobs[jp.x];
+      const int reset = (jp.y == 0) ? J.reset_first : 0;
+      emit = logic_path(J.pp, reset, ps, p, lc);
+      if (emit == 0) {
+        if (jp.y + 1 < J.n_pass) {   // next pass of the same pixel
+          start_pass(J, jp.x, ps.misc[p].y, jp.y + 1, p, ps, job_pass);
+          emit = 1;
+          lc.rays++; lc.trav++; lc.prim++;
+        } else {
+          atomicAdd(&job_done[jp.x], 1ull);
+          need_task = true;
+        }
+      }
+    }
+    // slots whose pixel is done take the next tasks, one claim per warp
+    const unsigned mt = __ballot_sync(0xffffffffu, need_task);
+    if (mt) {
+      unsigned long long t0 = 0;
+      int got = 0;
+      if (lane == 0) t0 = claim_tasks(ctl, __popc(mt), got);
+      t0 = __shfl_sync(0xffffffffu, t0, 0);
+      got = __shfl_sync(0xffffffffu, got, 0);
+      if (need_task) {
+        const int rank = __popc(mt & ((1u << lane) - 1));
+        if (rank < got) {
+          const unsigned long long t = t0 + (unsigned long long)rank;
+          const int job = job_of_task(jobs, n_jobs, t);
+          start_pass(jobs[job], job, (int)(t - (unsigned long long)jobs[job].task_base), 0, p, ps, job_pass);
+          emit = 1;
+          lc.rays++; lc.trav++; lc.prim++;
+        } else {
+          free_stack[atomicAdd(&ctl->free_top, 1)] = p;
+        }
+      }
+    }
+    const unsigned mc = __ballot_sync(0xffffffffu, emit == 1);
+    const unsigned ma = __ballot_sync(0xffffffffu, emit == 2);
+    int bc = 0, ba = 0;
+    if (lane == 0) {
+      if (mc) bc = atomicAdd(&rc_out->n_closest, __popc(mc));
+      if (ma) ba = atomicAdd(&rc_out->n_any, __popc(ma));
+    }
+    bc = __shfl_sync(0xffffffffu, bc, 0);
+    ba = __shfl_sync(0xffffffffu, ba, 0);
+    const unsigned below = (1u << lane) - 1;
+    if (emit == 1) out_closest[bc + __popc(mc & below)] = p;
+    if (emit == 2) out_any[ba + __popc(ma & below)] = p;
+    unsigned v[7] = {lc.rays, lc.ext, lc.shadow, lc.mis, lc.trav, lc.samples, lc.prim};
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+      unsigned x = v[q];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+      if (lane == 0 && x) atomicAdd(&s_cnt[q], (unsigned long long)x);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (s_cnt[0]) atomicAdd(&st->rays, s_cnt[0]);
+    if (s_cnt[1]) atomicAdd(&st->extension, s_cnt[1]);
+    if (s_cnt[2]) atomicAdd(&st->shadow, s_cnt[2]);
+    if (s_cnt[3]) atomicAdd(&st->mis, s_cnt[3]);
+    if (s_cnt[4]) atomicAdd(&st->traversed, s_cnt[4]);
+    if (s_cnt[5]) atomicAdd(&st->samples, s_cnt[5]);
+    if (s_cnt[6]) atomicAdd(&st->primary, s_cnt[6]);
+  }
+}
+
+void launch_batch_logic(const BatchJob* jobs, BatchCtl* ctl, const PathState& ps, int2* job_pass, int* free_stack,
+                        const int* in_closest, const int* in_any, const RoundCounters* rc_in, int* out_closest,
+                        int* out_any, RoundCounters* rc_out, DevStats* st, unsigned long long* job_done, int grid,
+                        cudaStream_t s) {
+  k_batch_logic<<<grid, ENGINE_TB, 0, s>>>(jobs, ctl, ps, job_pass, free_stack, in_closest, in_any, rc_in,
+                                           out_closest, out_any, rc_out, st, job_done);
+}
+
+// ---- traversal with a scene per ray ----
+template <bool ANY>
+struct BatchSrc {
+  const BatchJob* jobs;
+  const int2* job_pass;
+  const int* __restrict__ queue;
+  const float4* __restrict__ ro;
+  const float4* __restrict__ rd;
+  float4* hit;
+  __device__ __forceinline__ const DevScene& begin(int e, RayIn& r) {
+    const int q = queue[e];
+    const float4 o = ro[q];
+    const float4 d = rd[q];
+    r = RayIn{o.x, o.y, o.z, o.w, d.x, d.y, d.z};
+    return jobs[job_pass[q].x].pp.sc;
+  }
+  __device__ __forceinline__ void end(int e, const HitOut& h) {
+    const int q = queue[e];
+    if (ANY) hit[q] = make_float4(h.tri >= 0 ? 1.0f : 0.0f, 0.0f, 0.0f, 0.0f);
+    else hit[q] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+  }
+};
+
+template <bool ANY>
+__global__ void __launch_bounds__(TRACE_TB) k_batch_trace(const BatchJob* jobs, const int2* job_pass,
+                                                          const int* __restrict__ queue, const int* __restrict__ count,
+                                                          int* work, const float4* __restrict__ ro,
+                                                          const float4* __restrict__ rd, float4* hit, int stack_cap,
+                                                          DevStats* st) {
+  BatchSrc<ANY> src{jobs, job_pass, queue, ro, rd, hit};
+  trace_loop<ANY>(src, *count, work, stack_cap, st);
+}
+
+static size_t batch_smem(int cap) { return (size_t)TRACE_TB * 2 * cap * sizeof(int); }
+
+int batch_trace_grid(bool any_hit, int stack_cap) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = batch_smem(stack_cap);
+  if (any_hit) {
+    cudaFuncSetAttribute(k_batch_trace<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_trace<true>, TRACE_TB, smem);
+  } else {
+    cudaFuncSetAttribute(k_batch_trace<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_trace<false>, TRACE_TB, smem);
+  }
+  return per_sm > 0 ? per_sm * sms : -1;
+}
+
+int launch_batch_trace(bool any_hit, const BatchJob* jobs, const int2* job_pass, const int* queue, const int* count,
+                       int* work, const float4* ro, const float4* rd, float4* hit, DevStats* st, int stack_cap,
+                       int grid_blocks, cudaStream_t s) {
+  const size_t smem = batch_smem(stack_cap);
+  if (any_hit)
+    k_batch_trace<true><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
+                                                            stack_cap, st);
+  else
+    k_batch_trace<false><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
+                                                             stack_cap, st);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace yc

@@ -1,0 +1,44 @@
+// yc_engine.h -- device structures of the batch/serving engine (engine.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "yc_internal.h"
+
+namespace yc {
+
+// One render job: a scene, camera, accumulator and pass list. pp.rand_seed and pp.reset
+// are unused (the pass seed comes from `seeds`, the reset flag from reset_first).
+struct BatchJob {
+  PassParams pp;
+  const uint32_t* seeds;   // n_pass per-pass seeds (device)
+  int n_pass;
+  int reset_first;
+  long long task_base;     // first global pixel-task index of this job
+  int n_pix;
+  int pad_;
+};
+
+// Device-side control block of a batch.
+struct BatchCtl {
+  unsigned long long task_next;    // next unassigned pixel task
+  unsigned long long task_total;   // tasks admitted so far
+  int n_jobs;
+  int free_top;                    // slots on the free stack
+  int pad_[2];
+};
+
+void launch_batch_fill(const BatchJob* jobs, BatchCtl* ctl, const PathState& ps, int2* job_pass, int* free_stack,
+                       int* q_closest, RoundCounters* rc, DevStats* st, unsigned long long* job_done,
+                       int grid, cudaStream_t s);
+void launch_batch_logic(const BatchJob* jobs, BatchCtl* ctl, const PathState& ps, int2* job_pass,
+                        int* free_stack, const int* in_closest, const int* in_any, const RoundCounters* rc_in,
+                        int* out_closest, int* out_any, RoundCounters* rc_out, DevStats* st,
+                        unsigned long long* job_done, int grid, cudaStream_t s);
+int launch_batch_trace(bool any_hit, const BatchJob* jobs, const int2* job_pass, const int* queue,
+                       const int* count, int* work, const float4* ro, const float4* rd, float4* hit, DevStats* st,
+                       int stack_cap, int grid_blocks, cudaStream_t s);
+int batch_trace_grid(bool any_hit, int stack_cap);
+
+}  // namespace yc

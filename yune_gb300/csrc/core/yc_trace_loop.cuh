@@ -1,0 +1,91 @@
+// yc_trace_loop.cuh -- the replenishing persistent traversal loop, shared by the per-pass
+// trace kernels (trace.cu) and the batch engine (engine.cu).
+#pragma once
+
+#include "yc_internal.h"
+#include "yc_traverse.cuh"
+
+namespace yc {
+
+constexpr int TRACE_TB = 128;
+
+// warp-reduced traversal counters, one atomic per warp and counter
+template <bool ANY>
+__device__ __forceinline__ void flush_counts(DevStats* st, unsigned rays, const WalkCount& wc,
+                                             unsigned long long overflow) {
+  unsigned long long r = rays, nn = wc.nodes, tt = wc.tris;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    r += __shfl_xor_sync(0xffffffffu, r, off);
+    nn += __shfl_xor_sync(0xffffffffu, nn, off);
+    tt += __shfl_xor_sync(0xffffffffu, tt, off);
+    overflow += __shfl_xor_sync(0xffffffffu, overflow, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (ANY) {
+      if (r) atomicAdd(&st->any_rays, r);
+      if (nn) atomicAdd(&st->any_nodes, nn);
+      if (tt) atomicAdd(&st->any_tris, tt);
+    } else {
+      if (r) atomicAdd(&st->ext_rays, r);
+      if (nn) atomicAdd(&st->ext_nodes, nn);
+      if (tt) atomicAdd(&st->ext_tris, tt);
+    }
+    if (overflow) atomicAdd(&st->stack_overflow, overflow);
+  }
+}
+
+// Lanes refill when at least this many of a warp's 32 lanes are idle.
+constexpr int REFILL_AT = 8;
+
+// The persistent loop shared by the kernels. Src supplies ray e of the work list and the
+// scene it walks (begin) and stores its result (end).
+template <bool ANY, class Src>
+__device__ __forceinline__ void trace_loop(Src& src, int n, int* work, int stack_cap, DevStats* st) {
+  extern __shared__ int smem[];
+  int* stack = smem + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  unsigned long long overflow = 0;
+  WalkCount wc;
+  unsigned rays = 0;
+  Walk w;
+  int e_cur = -1;            // work-list entry of this lane's ray, -1 when idle
+  bool more = true;          // the work list may still hold rays (warp-uniform)
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xffffffffu, e_cur < 0);
+    if (more && (__popc(idle) >= REFILL_AT || idle == 0xffffffffu)) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(work, __popc(idle));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + __popc(idle) >= n) more = false;
+      if (e_cur < 0) {
+        const int e = base + __popc(idle & ((1u << lane) - 1));
+        if (e < n) {
+          e_cur = e;
+          RayIn r;
+          const DevScene& sc = src.begin(e, r);
+          walk_begin(sc, r, w);
+          ++rays;
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, e_cur >= 0) == 0) {
+      if (!more) break;
+      continue;
+    }
+    if (e_cur >= 0) {
+      bool of = false;
+      bool done = (w.link == LINK_NONE) || walk_step<ANY>(w, stack, TRACE_TB, stack_cap, wc, of);
+      if (of) ++overflow;
+      if (done) {
+        HitOut h;
+        h.t = w.best; h.u = w.bu; h.v = w.bv; h.tri = w.best_tri;
+        src.end(e_cur, h);
+        e_cur = -1;
+      }
+    }
+  }
+  flush_counts<ANY>(st, rays, wc, overflow);
+}
+
+}  // namespace yc

@@ -229,6 +229,8 @@ __device__ __forceinline__ bool traverse(const DevScene& sc, const RayIn& r, int
 // a lane a new ray as soon as its walk ends (the replenishing persistent warps of Aila
 // and Laine, "Understanding the Efficiency of Ray Traversal on GPUs", HPG 2009).
 struct Walk {
+  const float4* nodes;   // the scene of this ray (lanes of one warp may walk different scenes)
+  const float4* tris;
   float ox, oy, oz, dx, dy, dz, ix, iy, iz;
   float best, bu, bv;
   int best_tri, best_rank;
@@ -237,6 +239,8 @@ struct Walk {
 };
 
 __device__ __forceinline__ void walk_begin(const DevScene& sc, const RayIn& r, Walk& w) {
+  w.nodes = sc.nodes;
+  w.tris = sc.tris;
   w.ox = r.ox; w.oy = r.oy; w.oz = r.oz;
   w.dx = r.dx; w.dy = r.dy; w.dz = r.dz;
   w.ix = __frcp_rn(r.dx); w.iy = __frcp_rn(r.dy); w.iz = __frcp_rn(r.dz);
@@ -259,11 +263,11 @@ __device__ __forceinline__ void walk_begin(const DevScene& sc, const RayIn& r, W
 // Returns true when the walk has ended (w.link == LINK_NONE); `overflow` is set when
 // the stack bound was reached (the walk then ends early).
 template <bool ANY>
-__device__ __forceinline__ bool walk_step(const DevScene& sc, Walk& w, int* stack, int stride, int stack_cap,
-                                          WalkCount& wc, bool& overflow) {
+__device__ __forceinline__ bool walk_step(Walk& w, int* stack, int stride, int stack_cap, WalkCount& wc,
+                                          bool& overflow) {
   int link = w.link;
   while (link >= 0 && link != LINK_NONE) {
-    const float4* nd = sc.nodes + 4 * (size_t)link;
+    const float4* nd = w.nodes + 4 * (size_t)link;
     const float4 n0 = __ldg(nd + 0);
     const float4 n1 = __ldg(nd + 1);
     const float4 n2 = __ldg(nd + 2);
@@ -302,7 +306,7 @@ __device__ __forceinline__ bool walk_step(const DevScene& sc, Walk& w, int* stac
   if (link != LINK_NONE) {
     const int enc = ~link;
     const int count = enc & 15;
-    const float4* tp = sc.tris + 3 * (size_t)(enc >> 4);
+    const float4* tp = w.tris + 3 * (size_t)(enc >> 4);
     for (int k = 0; k < count; ++k) {
       ++wc.tris;
       const float4 a = __ldg(tp + 3 * k + 0);

@@ -1,0 +1,132 @@
+"""Render server: continuous batching of render requests over resident scenes.
+
+Requests (scene, resolution, target spp) arrive over time. A request is admitted when
+its accumulator fits the HBM budget left by the requests in flight; it then becomes a
+job of one long-lived batch (yune_gb300.batch), whose slots interleave the wavefronts of
+every admitted request and take new work as pixels finish, so requests that arrive
+while others run start as soon as memory frees up. Scenes stay resident; accumulators
+are freed when their request completes. Latency is arrival to completion of the target
+spp (the spp is the RMSE target: the estimate is the same at equal spp in any mix).
+"""
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import scenes
+from .batch import Batch
+
+
+@dataclass
+class Request:
+    arrival: float
+    scene: int
+    width: int
+    height: int
+    spp: int
+    seed: int = 0
+    # filled in by the server
+    admitted: float = -1.0
+    done: float = -1.0
+    job: int = -1
+    accum: int = -1
+    result: np.ndarray = field(default=None, repr=False)
+
+    @property
+    def bytes(self):
+        return self.width * self.height * 16 + self.spp * 4
+
+    @property
+    def latency(self):
+        return self.done - self.arrival
+
+
+class Server:
+    def __init__(self, renderer, resident, hbm_budget, pool_paths=1 << 21, rounds_per_launch=8, keep_results=False,
+                 cfg=None):
+        self.r = renderer
+        self.scenes = resident
+        self.sids = [renderer.upload(s) for s in resident]
+        self.budget = int(hbm_budget)
+        self.in_use = 0
+        self.keep = keep_results
+        self.cfg = cfg or scenes.default_cfg(max_depth=16)
+        cap = max(renderer.scene_depth(sid) for sid in self.sids) + 2
+        self.batch = Batch(renderer, pool_paths=pool_paths, rounds_per_launch=rounds_per_launch, max_jobs=4096,
+                           stack_cap=cap)
+
+    def _admit(self, q, now):
+        if q.bytes > self.budget:
+            raise ValueError("request larger than the whole HBM budget")
+        if self.in_use + q.bytes > self.budget:
+            return False
+        s = self.scenes[q.scene]
+        q.accum = self.r.alloc_accum(q.width, q.height)
+        q.job = self.batch.add_job(self.sids[q.scene], q.accum, s.cam, scenes.pass_seeds(q.seed, q.spp), self.cfg)
+        q.admitted = now
+        self.in_use += q.bytes
+        return True
+
+    def run(self, requests, clock=time.perf_counter):
+        """Serves the requests (sorted by arrival) in real time; returns them completed."""
+        pending = sorted(requests, key=lambda q: q.arrival)
+        live = []
+        t0 = clock()
+        i = 0
+        while i < len(pending) or live:
+            now = clock() - t0
+            # admission in arrival order while memory allows
+            while i < len(pending) and pending[i].arrival <= now and self._admit(pending[i], now):
+                live.append(pending[i])
+                i += 1
+            if not live:
+                if i < len(pending):
+                    time.sleep(max(0.0, pending[i].arrival - (clock() - t0)))
+                continue
+            self.batch.run(max_launches=1)
+            now = clock() - t0
+            still = []
+            for q in live:
+                d, tot = self.batch.progress(q.job)
+                if d >= tot:
+                    q.done = now
+                    if self.keep:
+                        q.result = self.r.read_accum(q.accum)
+                    self.r.free_accum(q.accum)
+                    self.in_use -= q.bytes
+                else:
+                    still.append(q)
+            live = still
+        return pending
+
+    def close(self):
+        self.batch.close()
+
+
+def serve_plain(renderer, resident, requests, cfg=None, clock=time.perf_counter, keep_results=False):
+    """The plain loop: requests one at a time, first come first served, each rendered
+    pass by pass with yc_render_pass (the reference's per-frame dispatch)."""
+    cfg = cfg or scenes.default_cfg(max_depth=16)
+    sids = [renderer.upload(s) for s in resident]
+    pending = sorted(requests, key=lambda q: q.arrival)
+    t0 = clock()
+    for q in pending:
+        now = clock() - t0
+        if q.arrival > now:
+            time.sleep(q.arrival - now)
+        q.admitted = clock() - t0
+        s = resident[q.scene]
+        renderer.set_camera(s.cam)
+        aid = renderer.alloc_accum(q.width, q.height)
+        renderer.render_passes(sids[q.scene], aid, scenes.pass_seeds(q.seed, q.spp), reset_first=1, cfg=cfg)
+        renderer.synchronize()
+        q.done = clock() - t0
+        if keep_results:
+            q.result = renderer.read_accum(aid)
+        renderer.free_accum(aid)
+    return pending
+
+
+def percentiles(reqs):
+    lat = np.array([q.latency for q in reqs])
+    return float(np.percentile(lat, 50)), float(np.percentile(lat, 99))
