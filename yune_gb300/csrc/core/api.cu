@@ -886,6 +886,12 @@ int yc_batch_add_job(yc_batch* b, int scene_id, int accum_id, const yc_cam* cam,
   j.seeds = sd->p;
   j.n_pass = n_pass;
   j.reset_first = reset_first;
+  if (b->started) {   // claims may have run the cursor past the last total: start after it
+    unsigned long long next = 0;
+    YC_CUDA(cudaMemcpyAsync(&next, &b->ctl.p->task_next, sizeof(next), cudaMemcpyDeviceToHost, c->stream));
+    YC_CUDA(cudaStreamSynchronize(c->stream));
+    if ((long long)next > b->task_total) b->task_total = (long long)next;
+  }
   j.task_base = b->task_total;
   j.n_pix = ac->w * ac->h;
   const int id = (int)b->host_jobs.size();

@@ -8,8 +8,8 @@
 // (path regeneration), so the wavefront stays full while jobs of any size and
 // resolution start and finish; the extend and occlusion kernels read each ray's scene
 // from the job table, so one launch walks many BVHs. Jobs can be added between launches
-// (serving); task claims go through a compare-and-swap on the task cursor so tasks
-// admitted later are never skipped.
+// (serving); a task claim is one atomicAdd on the task cursor, and a job added later
+// starts at or after the cursor, so its tasks are never skipped.
 #include <cuda_runtime.h>
 
 #include "yc_engine.h"
@@ -46,17 +46,14 @@ __device__ __forceinline__ void start_pass(const BatchJob& J, int job, int pix, 
 }
 
 // Claims up to `want` consecutive tasks below task_total; returns the first and sets got.
+// One atomicAdd per claim: the cursor may run past task_total (those tasks do not exist
+// and are dropped); yc_batch_add_job starts a new job at or after the cursor, so no task
+// admitted later falls into the overshoot.
 __device__ __forceinline__ unsigned long long claim_tasks(BatchCtl* ctl, int want, int& got) {
-  unsigned long long t = atomicAdd(&ctl->task_next, 0ull);
-  const unsigned long long total = ctl->task_total;
-  for (int tries = 0; tries < 1024; ++tries) {
-    if (t >= total) { got = 0; return t; }
-    const unsigned long long n = (total - t) < (unsigned long long)want ? (total - t) : (unsigned long long)want;
-    const unsigned long long old = atomicCAS(&ctl->task_next, t, t + n);
-    if (old == t) { got = (int)n; return t; }
-    t = old;
-  }
-  got = 0;   // heavy contention: leave the tasks to the next fill
+  const unsigned long long total = *(volatile unsigned long long*)&ctl->task_total;
+  if (*(volatile unsigned long long*)&ctl->task_next >= total) { got = 0; return total; }
+  const unsigned long long t = atomicAdd(&ctl->task_next, (unsigned long long)want);
+  got = t >= total ? 0 : (int)((total - t) < (unsigned long long)want ? (total - t) : (unsigned long long)want);
   return t;
 }
 
