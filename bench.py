@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--res-max", type=int, default=1024)
     ap.add_argument("--spp-max", type=int, default=128)
     ap.add_argument("--max-tris", type=int, default=500_000)
+    ap.add_argument("--profile", action="store_true", help="c2: per-kernel split of the batched run")
     return ap.parse_args()
 
 
@@ -308,7 +309,7 @@ def run_ours(args, rank, local, ws, dist):
 
 def run_c2(args):
     """Mixed batch: every job rendered pass by pass (plain) and all jobs in one batch."""
-    from yune_gb300 import scenes, workloads
+    from yune_gb300 import autotune, scenes, workloads
     from yune_gb300.batch import Batch
     from yune_gb300.core import Renderer
     jobs = workloads.c2_jobs(n_jobs=args.jobs, spp=args.spp, max_tris=args.max_tris)
@@ -331,9 +332,26 @@ def run_c2(args):
     plain_imgs = [r.read_accum(a) for a in accs[:4]]
     for a in accs:
         r.free_accum(a)
-    # batched
+    # batched: launch shape from the autotuner (untimed), unless --pool fixes the pool
+    cap = max(r.scene_depth(sid) for sid in sids) + 2
+    if args.pool:
+        shape, trials, tune_s = autotune.BatchShape(pool_paths=args.pool), [], 0.0
+    else:
+        shape, trials, tune_s = autotune.tune_scenes(r, jobs, sids, stack_cap=cap)
+    if args.profile:   # per-kernel split of the batched run (graph off, CUDA events per launch)
+        accs = [r.alloc_accum(s.width, s.height) for s in jobs]
+        b = Batch(r, use_graph=False, stack_cap=cap, **shape.kwargs())
+        for s, sid, a, sd in zip(jobs, sids, accs, seeds):
+            b.add_job(sid, a, s.cam, sd, s.cfg)
+        r.set_profiling(True)
+        b.run()
+        kt_batch = r.kernel_times()
+        r.set_profiling(False)
+        b.close()
+        for a in accs:
+            r.free_accum(a)
     accs = [r.alloc_accum(s.width, s.height) for s in jobs]
-    b = Batch(r, pool_paths=args.pool)
+    b = Batch(r, stack_cap=cap, **shape.kwargs())
     for s, sid, a, sd in zip(jobs, sids, accs, seeds):
         b.add_job(sid, a, s.cam, sd, s.cfg)
     r.reset_stats()
@@ -351,7 +369,11 @@ def run_c2(args):
            "plain": {"value": stp["rays"] / tp / 1e6, "seconds": tp, "samples_per_s": stp["samples"] / tp},
            "batched": {"value": stb["rays"] / tb / 1e6, "seconds": tb, "samples_per_s": stb["samples"] / tb,
                        "unfinished": left},
-           "speedup": tp / tb, "equal_results": bool(same), "rays_equal": stp["rays"] == stb["rays"]}
+           "speedup": tp / tb, "equal_results": bool(same), "rays_equal": stp["rays"] == stb["rays"],
+           "autotune": {"shape": shape.kwargs(), "seconds": tune_s,
+                        "trials": [[t.kwargs(), ms] for t, ms in trials]}}
+    if args.profile:
+        out["batched"]["kernel_ms"] = kt_batch
     r.close()
     print(json.dumps(out))
 

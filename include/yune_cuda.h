@@ -84,6 +84,8 @@ typedef struct yc_kernel_times {
   double raygen_ms, extend_ms, occlusion_ms, logic_ms;
   uint64_t raygen_launches, extend_launches, occlusion_launches, logic_launches;
   uint64_t rounds;
+  double sort_ms;              /* batch engine: shade-queue sort (histogram, scan, scatter) */
+  uint64_t sort_launches;
 } yc_kernel_times;
 
 typedef struct yc_ctx yc_ctx;
@@ -181,6 +183,8 @@ typedef struct yc_batch_cfg {
   int32_t use_graph;           /* 1 = capture the rounds in a CUDA graph */
   int32_t max_jobs;            /* capacity of the job table; 0 = 1024 */
   int32_t stack_cap;           /* traversal stack entries; 0 = from the first jobs' scenes */
+  int32_t sort_threshold;      /* shade queues of at least this many paths are sorted by path
+                                  phase and material class before the logic kernel; 0 = never */
 } yc_batch_cfg;
 int yc_batch_create(yc_ctx* ctx, const yc_batch_cfg* cfg, yc_batch** out);
 /* Adds a job: n_pass passes of scene_id into accum_id seen from *cam, pass k with

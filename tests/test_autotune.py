@@ -1,0 +1,36 @@
+"""The batch autotuner's search on the CPU, with a fake calibration clock."""
+from yune_gb300 import autotune
+
+
+class _FakeRenderer:
+    def __init__(self):
+        self.live = 0
+
+    def alloc_accum(self, w, h):
+        self.live += 1
+        return self.live
+
+    def free_accum(self, a):
+        self.live -= 1
+
+
+def test_coordinate_search_finds_the_separable_optimum(monkeypatch):
+    seen = []
+
+    def clock(renderer, jobs, shape, cap, accs):
+        seen.append(shape.kwargs())
+        return (abs(shape.pool_paths - (1 << 20)) / 1e5 + abs(shape.rounds_per_launch - 16)
+                + abs(shape.logic_blocks_per_sm - 2))
+
+    monkeypatch.setattr(autotune, "_calibrate", clock)
+    r = _FakeRenderer()
+    best, trials = autotune.tune(r, [(0, None, [1], None)] * 3, [(1920, 1080)] * 3)
+    assert best == autotune.BatchShape(1 << 20, 16, 2, 0)
+    assert len(trials) == len(seen) and r.live == 0   # scratch accumulators released
+
+
+def test_pool_never_exceeds_the_pixels_in_the_mix(monkeypatch):
+    monkeypatch.setattr(autotune, "_calibrate", lambda r, j, shape, c, a: 1.0 / shape.pool_paths)
+    best, trials = autotune.tune(_FakeRenderer(), [(0, None, [1], None)], [(256, 256)])
+    assert best.pool_paths == 1 << 16
+    assert all(t.pool_paths <= 1 << 16 for t, _ in trials)

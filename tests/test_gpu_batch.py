@@ -18,8 +18,9 @@ def _jobs():
     return [(a, scenes.pass_seeds(1, 3)), (b, scenes.pass_seeds(2, 2)), (c, scenes.pass_seeds(3, 5))]
 
 
-@pytest.mark.parametrize("use_graph,pool", [(True, 4096), (False, 1000), (True, 1 << 16)])
-def test_batch_matches_per_pass(use_graph, pool):
+@pytest.mark.parametrize("use_graph,pool,sort", [(True, 4096, 0), (False, 1000, 0), (True, 1 << 16, 0),
+                                                (True, 4096, 1), (False, 1000, 64)])
+def test_batch_matches_per_pass(use_graph, pool, sort):
     jobs = _jobs()
     with Renderer(0) as r:
         ids = []
@@ -32,7 +33,7 @@ def test_batch_matches_per_pass(use_graph, pool):
             aid = r.alloc_accum(s.width, s.height)
             r.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
             want.append(r.read_accum(aid))
-        b = Batch(r, pool_paths=pool, rounds_per_launch=4, use_graph=use_graph)
+        b = Batch(r, pool_paths=pool, rounds_per_launch=4, use_graph=use_graph, sort_threshold=sort)
         accs = []
         for (s, seeds), sid in zip(jobs, ids):
             aid = r.alloc_accum(s.width, s.height)
@@ -64,4 +65,28 @@ def test_batch_jobs_added_while_running():
         a_ref = r.alloc_accum(jobs[1][0].width, jobs[1][0].height)
         r.render_passes(sids[1], a_ref, jobs[1][1], reset_first=1, cfg=jobs[1][0].cfg)
         assert np.array_equal(got1.view(np.int32), r.read_accum(a_ref).view(np.int32))
+        b.close()
+
+
+def test_autotuned_shape_gives_identical_results():
+    """The tuner only picks a launch shape: the tuned batch renders the same bits."""
+    from yune_gb300 import autotune
+    jobs = _jobs()
+    with Renderer(0) as r:
+        sids = [r.upload(s) for s, _ in jobs]
+        cap = max(r.scene_depth(sid) for sid in sids) + 2
+        shape, trials, _ = autotune.tune_scenes(r, [s for s, _ in jobs], sids, stack_cap=cap)
+        assert trials and all(ms > 0 for _, ms in trials)
+        assert shape.pool_paths >= 1 << 16
+        b = Batch(r, stack_cap=cap, **shape.kwargs())
+        accs = []
+        for (s, seeds), sid in zip(jobs, sids):
+            accs.append(r.alloc_accum(s.width, s.height))
+            b.add_job(sid, accs[-1], s.cam, seeds, s.cfg)
+        assert b.run() == 0
+        for (s, seeds), sid, aid in zip(jobs, sids, accs):
+            r.set_camera(s.cam)
+            ref = r.alloc_accum(s.width, s.height)
+            r.render_passes(sid, ref, seeds, reset_first=1, cfg=s.cfg)
+            assert np.array_equal(r.read_accum(aid).view(np.int32), r.read_accum(ref).view(np.int32))
         b.close()

@@ -33,13 +33,14 @@ class KernelTimes(C.Structure):
     """yc_kernel_times"""
     _fields_ = [("raygen_ms", C.c_double), ("extend_ms", C.c_double), ("occlusion_ms", C.c_double),
                 ("logic_ms", C.c_double), ("raygen_launches", C.c_uint64), ("extend_launches", C.c_uint64),
-                ("occlusion_launches", C.c_uint64), ("logic_launches", C.c_uint64), ("rounds", C.c_uint64)]
+                ("occlusion_launches", C.c_uint64), ("logic_launches", C.c_uint64), ("rounds", C.c_uint64),
+                ("sort_ms", C.c_double), ("sort_launches", C.c_uint64)]
 
 
 class BatchCfg(C.Structure):
     """yc_batch_cfg"""
     _fields_ = [("pool_paths", i32), ("rounds_per_launch", i32), ("logic_blocks_per_sm", i32), ("use_graph", i32),
-                ("max_jobs", i32), ("stack_cap", i32)]
+                ("max_jobs", i32), ("stack_cap", i32), ("sort_threshold", i32)]
 
 
 # name -> (restype, argtypes)

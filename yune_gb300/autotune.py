@@ -1,0 +1,96 @@
+"""Autotuner for the batch engine's launch shape.
+
+The batch engine (yc_batch_*) has four free parameters that change speed but never
+results: the number of path slots in flight (the wavefront size), the rounds captured
+in one CUDA graph launch, the logic kernel's blocks per SM, and the queue size from which
+the shade queue is sorted by path phase and material class (0: never). The best values depend
+on the job mix (total pixels, scene sizes, path lengths), so the tuner times candidate
+shapes on a calibration run of the mix itself: every job's first pass, into scratch
+accumulators, with the engine's own CUDA-event clock (yc_last_pass_ms). It searches one
+parameter at a time (pool size, rounds per launch, logic blocks, sort threshold) from
+the engine defaults, keeping the best value of each before moving on.
+"""
+import time
+from dataclasses import dataclass
+
+from . import scenes
+from .batch import Batch
+
+POOLS = (1 << 19, 1 << 20, 1 << 21, 1 << 22)
+ROUNDS = (4, 8, 16)
+LOGIC_BLOCKS = (2, 4, 8)
+SORT = (1 << 16, 1 << 18)
+
+
+@dataclass
+class BatchShape:
+    pool_paths: int = 1 << 21
+    rounds_per_launch: int = 8
+    logic_blocks_per_sm: int = 4
+    sort_threshold: int = 0
+
+    def kwargs(self):
+        return dict(pool_paths=self.pool_paths, rounds_per_launch=self.rounds_per_launch,
+                    logic_blocks_per_sm=self.logic_blocks_per_sm, sort_threshold=self.sort_threshold)
+
+
+def _calibrate(renderer, jobs, shape, stack_cap, accs):
+    """Milliseconds of one pass of every job under `shape` (device time of yc_batch_run)."""
+    b = Batch(renderer, stack_cap=stack_cap, **shape.kwargs())
+    try:
+        for (sid, cam, seeds, cfg), a in zip(jobs, accs):
+            b.add_job(sid, a, cam, seeds[:1], cfg)
+        b.run()
+        return renderer.last_pass_ms()
+    finally:
+        b.close()
+
+
+def tune(renderer, jobs, sizes, stack_cap=0, log=None):
+    """Picks a BatchShape for `jobs`, a list of (scene_id, cam, seeds, cfg) tuples, whose
+    frames have the (width, height) of `sizes`. Returns (shape, trials) where trials lists
+    (shape, ms) in the order they were timed."""
+    accs = [renderer.alloc_accum(w, h) for (w, h) in sizes]
+    total_px = sum(w * h for (w, h) in sizes)
+    trials = []
+    try:
+        best = BatchShape()
+        best.pool_paths = min(best.pool_paths, _round_pool(total_px))
+        best_ms = _calibrate(renderer, jobs, best, stack_cap, accs)
+        trials.append((BatchShape(**best.kwargs()), best_ms))
+        for field, values in (("pool_paths", POOLS), ("rounds_per_launch", ROUNDS),
+                              ("logic_blocks_per_sm", LOGIC_BLOCKS), ("sort_threshold", SORT)):
+            for v in values:
+                if v == getattr(best, field):
+                    continue
+                if field == "pool_paths" and v > _round_pool(total_px):
+                    continue   # more slots than pixels stay idle
+                cand = BatchShape(**best.kwargs())
+                setattr(cand, field, v)
+                ms = _calibrate(renderer, jobs, cand, stack_cap, accs)
+                trials.append((cand, ms))
+                if log:
+                    log("autotune %s -> %.2f ms" % (cand, ms))
+                if ms < best_ms:
+                    best, best_ms = cand, ms
+    finally:
+        for a in accs:
+            renderer.free_accum(a)
+    return best, trials
+
+
+def _round_pool(total_px):
+    p = 1 << 16
+    while p < total_px and p < POOLS[-1]:
+        p <<= 1
+    return p
+
+
+def tune_scenes(renderer, scene_list, sids, seed=4242, stack_cap=0, log=None):
+    """tune() for SceneData records already uploaded as `sids` (calibration seeds are
+    drawn independently of the seeds the jobs render with)."""
+    jobs = [(sid, s.cam, scenes.pass_seeds(seed + i, 1), s.cfg) for i, (s, sid) in enumerate(zip(scene_list, sids))]
+    sizes = [(s.width, s.height) for s in scene_list]
+    t0 = time.perf_counter()
+    shape, trials = tune(renderer, jobs, sizes, stack_cap=stack_cap, log=log)
+    return shape, trials, time.perf_counter() - t0

@@ -131,7 +131,7 @@ int ensure_paths(yc_ctx* c, size_t n) {
 }
 
 // event pairs around kernel launches (profiling only)
-enum { K_RAYGEN = 0, K_EXTEND = 1, K_OCCL = 2, K_LOGIC = 3 };
+enum { K_RAYGEN = 0, K_EXTEND = 1, K_OCCL = 2, K_LOGIC = 3, K_SORT = 4 };
 cudaEvent_t next_event(yc_ctx* c) {
   if (c->ev_used == c->ev_pool.size()) {
     cudaEvent_t e;
@@ -145,7 +145,7 @@ struct KTimer {
   int kind;
   size_t idx = 0;
   bool on;
-  KTimer(yc_ctx* c_, int k) : c(c_), kind(k), on(c_->profile) {
+  KTimer(yc_ctx* c_, int k, bool allowed = true) : c(c_), kind(k), on(c_->profile && allowed) {
     if (!on) return;
     idx = c->ev_used;
     cudaEvent_t e = next_event(c);
@@ -170,6 +170,7 @@ void collect_events(yc_ctx* c) {
       case K_RAYGEN: c->ktimes.raygen_ms += ms; c->ktimes.raygen_launches++; break;
       case K_EXTEND: c->ktimes.extend_ms += ms; c->ktimes.extend_launches++; break;
       case K_OCCL: c->ktimes.occlusion_ms += ms; c->ktimes.occlusion_launches++; break;
+      case K_SORT: c->ktimes.sort_ms += ms; c->ktimes.sort_launches++; break;
       default: c->ktimes.logic_ms += ms; c->ktimes.logic_launches++; break;
     }
   }
@@ -719,6 +720,8 @@ struct yc_batch {
   DevBuf<int2> job_pass;
   DevBuf<int> free_stack;
   DevBuf<int> q[4];
+  DevBuf<int> sort_keys, sorted;
+  DevBuf<yc::SortCtl> sctl;
   DevBuf<yc::RoundCounters> rc;
   DevBuf<yc::BatchCtl> ctl;
   DevBuf<yc::BatchJob> jobs;
@@ -759,8 +762,8 @@ yc::PathState batch_state(yc_batch* b) {
   return ps;
 }
 
-// one round: fill idle slots, trace both queues, step every path (A -> B)
-int batch_round(yc_batch* b, int cur) {
+// one round: trace both queues, step every path (A -> B)
+int batch_round(yc_batch* b, int cur, bool timed) {
   yc_ctx* c = b->ctx;
   const yc::PathState ps = batch_state(b);
   int* in_c = b->q[2 * cur].p;
@@ -769,27 +772,53 @@ int batch_round(yc_batch* b, int cur) {
   int* out_a = b->q[2 * (1 - cur) + 1].p;
   yc::RoundCounters* rin = b->rc.p + cur;
   yc::RoundCounters* rout = b->rc.p + (1 - cur);
-  yc::launch_batch_fill(b->jobs.p, b->ctl.p, ps, b->job_pass.p, b->free_stack.p, in_c, rin, c->stats.p, b->job_done.p,
-                        1, c->stream);
-  yc::launch_batch_trace(false, b->jobs.p, b->job_pass.p, in_c, &rin->n_closest, &rin->work_closest, ps.ro, ps.rd,
-                         ps.hit, c->stats.p, b->stack_cap, b->grid_c, c->stream);
-  yc::launch_batch_trace(true, b->jobs.p, b->job_pass.p, in_a, &rin->n_any, &rin->work_any, ps.ro, ps.rd, ps.hit,
-                         c->stats.p, b->stack_cap, b->grid_a, c->stream);
+  {
+    KTimer kt(c, K_EXTEND, timed);
+    yc::launch_batch_trace(false, b->jobs.p, b->job_pass.p, in_c, &rin->n_closest, &rin->work_closest, ps.ro, ps.rd,
+                           ps.hit, c->stats.p, b->stack_cap, b->grid_c, c->stream);
+  }
+  {
+    KTimer kt(c, K_OCCL, timed);
+    yc::launch_batch_trace(true, b->jobs.p, b->job_pass.p, in_a, &rin->n_any, &rin->work_any, ps.ro, ps.rd, ps.hit,
+                           c->stats.p, b->stack_cap, b->grid_a, c->stream);
+  }
   YC_CUDA(cudaMemsetAsync(rout, 0, sizeof(yc::RoundCounters), c->stream));
-  yc::launch_batch_logic(b->jobs.p, b->ctl.p, ps, b->job_pass.p, b->free_stack.p, in_c, in_a, rin, out_c, out_a, rout,
-                         c->stats.p, b->job_done.p, b->logic_grid, c->stream);
+  YC_CUDA(cudaMemsetAsync(b->sctl.p, 0, sizeof(yc::SortCtl), c->stream));
+  if (b->cfg.sort_threshold > 0) {
+    KTimer kt(c, K_SORT, timed);
+    yc::launch_batch_sort(b->jobs.p, b->job_pass.p, ps, in_c, in_a, rin, b->sort_keys.p, b->sorted.p, b->sctl.p,
+                          b->cfg.sort_threshold, b->logic_grid, c->stream);
+  }
+  {
+    KTimer kt(c, K_LOGIC, timed);
+    yc::launch_batch_logic(b->jobs.p, b->ctl.p, ps, b->job_pass.p, b->free_stack.p, in_c, in_a, rin, out_c, out_a,
+                           rout, c->stats.p, b->job_done.p, b->sorted.p, b->sctl.p, b->logic_grid, c->stream);
+  }
+  c->ktimes.rounds++;
   YC_CUDA(cudaPeekAtLastError());
   return 0;
 }
 
+// one launch: free slots take new tasks (appended to round 0's closest-hit queue), then
+// an even number of rounds, so every launch starts on queue pair 0
+int batch_body(yc_batch* b, bool timed) {
+  yc_ctx* c = b->ctx;
+  {
+    KTimer kt(c, K_RAYGEN, timed);
+    yc::launch_batch_fill(b->jobs.p, b->ctl.p, batch_state(b), b->job_pass.p, b->free_stack.p, b->q[0].p, b->rc.p,
+                          c->stats.p, b->logic_grid, c->stream);
+  }
+  int r = 0;
+  for (int k = 0; k < b->cfg.rounds_per_launch && !r; ++k) r = batch_round(b, k & 1, timed);
+  return r;
+}
+
 int batch_launch(yc_batch* b) {
   yc_ctx* c = b->ctx;
-  const int rounds = b->cfg.rounds_per_launch;
   if (b->cfg.use_graph) {
     if (!b->exec) {
       YC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-      int r = 0;
-      for (int k = 0; k < rounds && !r; ++k) r = batch_round(b, k & 1);
+      const int r = batch_body(b, false);
       cudaGraph_t g = nullptr;
       const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
       if (r) { if (g) cudaGraphDestroy(g); return r; }
@@ -798,11 +827,10 @@ int batch_launch(yc_batch* b) {
       YC_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
     }
     YC_CUDA(cudaGraphLaunch(b->exec, c->stream));
-  } else {
-    for (int k = 0; k < rounds; ++k)
-      if (int r = batch_round(b, k & 1)) return r;
+    c->ktimes.rounds += b->cfg.rounds_per_launch;
+    return 0;
   }
-  return 0;
+  return batch_body(b, true);
 }
 
 }  // namespace
@@ -828,6 +856,11 @@ int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
   YC_CUDA(b->job_pass.alloc(n));
   YC_CUDA(b->free_stack.alloc(n));
   for (auto& q : b->q) YC_CUDA(q.alloc(n));
+  YC_CUDA(b->sctl.alloc(1));
+  if (b->cfg.sort_threshold > 0) {
+    YC_CUDA(b->sort_keys.alloc(n));
+    YC_CUDA(b->sorted.alloc(n));
+  }
   YC_CUDA(b->rc.alloc(2));
   YC_CUDA(b->ctl.alloc(1));
   YC_CUDA(b->jobs.alloc(b->cfg.max_jobs));
@@ -930,6 +963,7 @@ int yc_batch_run(yc_batch* b, int max_launches, int* unfinished) {
     YC_CUDA(cudaMemcpyAsync(b->done_host, b->job_done.p, b->host_jobs.size() * sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, c->stream));
     YC_CUDA(cudaStreamSynchronize(c->stream));
+    collect_events(c);
     int left = 0;
     for (size_t i = 0; i < b->host_jobs.size(); ++i)
       if (b->done_host[i] < (unsigned long long)b->host_jobs[i].n_pix) ++left;

@@ -58,54 +58,58 @@ __device__ __forceinline__ unsigned long long claim_tasks(BatchCtl* ctl, int wan
 }
 
 // ---- fill: idle slots (on the free stack) take new tasks ----
-__global__ void __launch_bounds__(ENGINE_TB) k_batch_fill(const BatchJob* __restrict__ jobs, BatchCtl* ctl,
-                                                          PathState ps, int2* job_pass, int* free_stack,
+// k_batch_plan claims, in one thread, as many tasks as there are free slots; k_batch_fill
+// then starts them across the grid.
+__global__ void k_batch_plan(BatchCtl* ctl) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int free_n = ctl->free_top;
+  int got = 0;
+  const unsigned long long t0 = free_n > 0 ? claim_tasks(ctl, free_n, got) : 0ull;
+  ctl->fill_t0 = t0;
+  ctl->fill_n = got;
+  ctl->fill_top = free_n - got;
+  ctl->free_top = free_n - got;
+}
+
+__global__ void __launch_bounds__(ENGINE_TB) k_batch_fill(const BatchJob* __restrict__ jobs, const BatchCtl* ctl,
+                                                          PathState ps, int2* job_pass, const int* free_stack,
                                                           int* q_closest, RoundCounters* rc, DevStats* st) {
-  __shared__ unsigned long long s_t0;
-  __shared__ int s_n, s_top;
-  // one block claims for the whole grid: grid is launched with a single block
-  if (threadIdx.x == 0) {
-    const int free_n = ctl->free_top;
-    int got = 0;
-    const unsigned long long t0 = free_n > 0 ? claim_tasks(ctl, free_n, got) : 0ull;
-    s_t0 = t0;
-    s_n = got;
-    s_top = free_n - got;
-    ctl->free_top = free_n - got;
-  }
-  __syncthreads();
-  const int n = s_n;
+  const int n = ctl->fill_n;
+  const int top = ctl->fill_top;
+  const unsigned long long t0 = ctl->fill_t0;
   const int n_jobs = ctl->n_jobs;
   const int lane = threadIdx.x & 31;
-  for (int base = 0; base < n; base += blockDim.x) {
-    const int i = base + threadIdx.x;
+  const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int warps_total = (gridDim.x * blockDim.x) >> 5;
+  unsigned long long started = 0;
+  for (int wbase = warp_global * 32; wbase < n; wbase += warps_total * 32) {
+    const int i = wbase + lane;
     const bool active = i < n;
     int p = -1;
     if (active) {
-      p = free_stack[s_top + i];
-      const unsigned long long t = s_t0 + (unsigned long long)i;
+      p = free_stack[top + i];
+      const unsigned long long t = t0 + (unsigned long long)i;
       const int job = job_of_task(jobs, n_jobs, t);
       start_pass(jobs[job], job, (int)(t - (unsigned long long)jobs[job].task_base), 0, p, ps, job_pass);
     }
     const unsigned m = __ballot_sync(0xffffffffu, active);
     int b = 0;
-    if (lane == 0 && m) b = atomicAdd(&rc->n_closest, __popc(m));
+    if (lane == 0) b = atomicAdd(&rc->n_closest, __popc(m));
     b = __shfl_sync(0xffffffffu, b, 0);
     if (active) q_closest[b + __popc(m & ((1u << lane) - 1))] = p;
-    if (lane == 0 && m) {
-      atomicAdd(&st->primary, (unsigned long long)__popc(m));
-      atomicAdd(&st->rays, (unsigned long long)__popc(m));
-      atomicAdd(&st->traversed, (unsigned long long)__popc(m));
-    }
+    started += __popc(m);
+  }
+  if (lane == 0 && started) {
+    atomicAdd(&st->primary, started);
+    atomicAdd(&st->rays, started);
+    atomicAdd(&st->traversed, started);
   }
 }
 
 void launch_batch_fill(const BatchJob* jobs, BatchCtl* ctl, const PathState& ps, int2* job_pass, int* free_stack,
-                       int* q_closest, RoundCounters* rc, DevStats* st, unsigned long long* job_done, int grid,
-                       cudaStream_t s) {
-  (void)job_done;
-  (void)grid;
-  k_batch_fill<<<1, ENGINE_TB, 0, s>>>(jobs, ctl, ps, job_pass, free_stack, q_closest, rc, st);
+                       int* q_closest, RoundCounters* rc, DevStats* st, int grid, cudaStream_t s) {
+  k_batch_plan<<<1, 32, 0, s>>>(ctl);
+  k_batch_fill<<<grid, ENGINE_TB, 0, s>>>(jobs, ctl, ps, job_pass, free_stack, q_closest, rc, st);
 }
 
 // ---- logic with regeneration ----
@@ -114,7 +118,8 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __res
                                                            const int* __restrict__ in_closest,
                                                            const int* __restrict__ in_any, const RoundCounters* rc_in,
                                                            int* out_closest, int* out_any, RoundCounters* rc_out,
-                                                           DevStats* st, unsigned long long* job_done) {
+                                                           DevStats* st, unsigned long long* job_done,
+                                                           const int* __restrict__ sorted, const SortCtl* sctl) {
   __shared__ unsigned long long s_cnt[8];
   if (threadIdx.x < 8) s_cnt[threadIdx.x] = 0;
   __syncthreads();
@@ -124,6 +129,7 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __res
   const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int warps_total = (gridDim.x * blockDim.x) >> 5;
   const int n_jobs = ctl->n_jobs;
+  const bool use_sorted = sctl->use != 0;
   for (int wbase = warp_global * 32; wbase < n; wbase += warps_total * 32) {
     const int e = wbase + lane;
     int emit = 0;
@@ -131,7 +137,7 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __res
     bool need_task = false;
     LogicCounts lc;
     if (e < n) {
-      p = e < nc ? in_closest[e] : in_any[e - nc];
+      p = use_sorted ? sorted[e] : (e < nc ? in_closest[e] : in_any[e - nc]);
       const int2 jp = job_pass[p];
       const BatchJob& J = jobs[jp.x];
       const int reset = (jp.y == 0) ? J.reset_first : 0;
@@ -203,10 +209,96 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __res
 
 void launch_batch_logic(const BatchJob* jobs, BatchCtl* ctl, const PathState& ps, int2* job_pass, int* free_stack,
                         const int* in_closest, const int* in_any, const RoundCounters* rc_in, int* out_closest,
-                        int* out_any, RoundCounters* rc_out, DevStats* st, unsigned long long* job_done, int grid,
-                        cudaStream_t s) {
+                        int* out_any, RoundCounters* rc_out, DevStats* st, unsigned long long* job_done,
+                        const int* sorted, const SortCtl* sctl, int grid, cudaStream_t s) {
   k_batch_logic<<<grid, ENGINE_TB, 0, s>>>(jobs, ctl, ps, job_pass, free_stack, in_closest, in_any, rc_in,
-                                           out_closest, out_any, rc_out, st, job_done);
+                                           out_closest, out_any, rc_out, st, job_done, sorted, sctl);
+}
+
+// ---- shade-queue sort (counting sort over SORT_KEYS keys) ----
+__device__ __forceinline__ int material_class(const yc_material& m) {
+  if (m.is_specular) return m.is_transmissive ? 3 : 2;
+  return (m.ks.x > 0.0f || m.ks.y > 0.0f || m.ks.z > 0.0f) ? 1 : 0;   // a glossy lobe can be drawn
+}
+
+__device__ __forceinline__ int logic_key(const BatchJob* jobs, const int2* job_pass, const PathState& ps, int p) {
+  const DevScene& sc = jobs[job_pass[p].x].pp.sc;
+  const int st = ps.misc[p].z & 15;   // the phase a path waits in: S_PRIMARY..S_EXT
+  int mat;
+  if (st == S_PRIMARY || st == S_EXT) {
+    const int tri = __float_as_int(ps.hit[p].w);
+    if (tri < 0) return st * 5 + 4;
+    mat = __float_as_int(__ldg(sc.shade + 4 * (size_t)tri + 3).x);
+  } else {
+    mat = __float_as_int(ps.wi[p].w);
+  }
+  return st * 5 + material_class(sc.mats[mat]);
+}
+
+__global__ void __launch_bounds__(ENGINE_TB) k_sort_hist(const BatchJob* __restrict__ jobs,
+                                                         const int2* __restrict__ job_pass, PathState ps,
+                                                         const int* __restrict__ in_closest,
+                                                         const int* __restrict__ in_any, const RoundCounters* rc_in,
+                                                         int* keys, SortCtl* sctl, int threshold) {
+  __shared__ int h[SORT_KEYS];
+  if (threadIdx.x < SORT_KEYS) h[threadIdx.x] = 0;
+  __syncthreads();
+  const int nc = rc_in->n_closest, n = nc + rc_in->n_any;
+  if (n < threshold) return;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int p = e < nc ? in_closest[e] : in_any[e - nc];
+    const int key = logic_key(jobs, job_pass, ps, p);
+    keys[e] = key;
+    atomicAdd(&h[key], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x < SORT_KEYS && h[threadIdx.x]) atomicAdd(&sctl->count[threadIdx.x], h[threadIdx.x]);
+}
+
+__global__ void k_sort_scan(const RoundCounters* rc_in, SortCtl* sctl, int threshold) {
+  if (threadIdx.x != 0) return;
+  const int n = rc_in->n_closest + rc_in->n_any;
+  const int use = (threshold > 0 && n >= threshold) ? 1 : 0;
+  if (use) {
+    int run = 0;
+    for (int k = 0; k < SORT_KEYS; ++k) {
+      sctl->cursor[k] = run;
+      run += sctl->count[k];
+    }
+  }
+  sctl->use = use;
+}
+
+__global__ void __launch_bounds__(ENGINE_TB) k_sort_scatter(const int* __restrict__ in_closest,
+                                                            const int* __restrict__ in_any, const RoundCounters* rc_in,
+                                                            const int* __restrict__ keys, int* sorted, SortCtl* sctl) {
+  if (!sctl->use) return;
+  const int nc = rc_in->n_closest, n = nc + rc_in->n_any;
+  const int lane = threadIdx.x & 31;
+  const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int warps_total = (gridDim.x * blockDim.x) >> 5;
+  for (int wbase = warp_global * 32; wbase < n; wbase += warps_total * 32) {
+    const int e = wbase + lane;
+    const bool active = e < n;
+    const int key = active ? keys[e] : -1 - lane;   // idle lanes match nobody
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (active && lane == leader) base = atomicAdd(&sctl->cursor[key], __popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (active) {
+      const int p = e < nc ? in_closest[e] : in_any[e - nc];
+      sorted[base + __popc(peers & ((1u << lane) - 1))] = p;
+    }
+  }
+}
+
+void launch_batch_sort(const BatchJob* jobs, const int2* job_pass, const PathState& ps, const int* in_closest,
+                       const int* in_any, const RoundCounters* rc_in, int* keys, int* sorted, SortCtl* sctl,
+                       int threshold, int grid, cudaStream_t s) {
+  k_sort_hist<<<grid, ENGINE_TB, 0, s>>>(jobs, job_pass, ps, in_closest, in_any, rc_in, keys, sctl, threshold);
+  k_sort_scan<<<1, 32, 0, s>>>(rc_in, sctl, threshold);
+  k_sort_scatter<<<grid, ENGINE_TB, 0, s>>>(in_closest, in_any, rc_in, keys, sorted, sctl);
 }
 
 // ---- traversal with a scene per ray ----

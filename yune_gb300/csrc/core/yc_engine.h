@@ -26,16 +26,32 @@ struct BatchCtl {
   unsigned long long task_total;   // tasks admitted so far
   int n_jobs;
   int free_top;                    // slots on the free stack
-  int pad_[2];
+  int fill_n;                      // the current fill: tasks claimed for free slots,
+  int fill_top;                    //   the free-stack position they are taken from,
+  unsigned long long fill_t0;      //   and the first of them
 };
 
+// Sorting of the shade queue by path phase (S_PRIMARY..S_EXT) and material class
+// (diffuse, glossy, mirror, dielectric, no surface): key = phase * 5 + class.
+constexpr int SORT_KEYS = 20;
+struct SortCtl {
+  int use;                  // 1: this round's shade queue is the sorted one
+  int pad_;
+  int count[SORT_KEYS];     // paths per key
+  int cursor[SORT_KEYS];    // scatter cursors (exclusive prefix of count)
+};
+
+void launch_batch_sort(const BatchJob* jobs, const int2* job_pass, const PathState& ps, const int* in_closest,
+                       const int* in_any, const RoundCounters* rc_in, int* keys, int* sorted, SortCtl* sctl,
+                       int threshold, int grid, cudaStream_t s);
+
 void launch_batch_fill(const BatchJob* jobs, BatchCtl* ctl, const PathState& ps, int2* job_pass, int* free_stack,
-                       int* q_closest, RoundCounters* rc, DevStats* st, unsigned long long* job_done,
-                       int grid, cudaStream_t s);
+                       int* q_closest, RoundCounters* rc, DevStats* st, int grid, cudaStream_t s);
 void launch_batch_logic(const BatchJob* jobs, BatchCtl* ctl, const PathState& ps, int2* job_pass,
                         int* free_stack, const int* in_closest, const int* in_any, const RoundCounters* rc_in,
                         int* out_closest, int* out_any, RoundCounters* rc_out, DevStats* st,
-                        unsigned long long* job_done, int grid, cudaStream_t s);
+                        unsigned long long* job_done, const int* sorted, const SortCtl* sctl, int grid,
+                        cudaStream_t s);
 int launch_batch_trace(bool any_hit, const BatchJob* jobs, const int2* job_pass, const int* queue,
                        const int* count, int* work, const float4* ro, const float4* rd, float4* hit, DevStats* st,
                        int stack_cap, int grid_blocks, cudaStream_t s);

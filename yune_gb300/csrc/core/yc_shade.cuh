@@ -228,42 +228,54 @@ __device__ __forceinline__ f4 brdf(f4 w_i, f4 w_o, const Vtx& v, const yc_materi
 // sampleLights, udpt.cl:632-698; -1 when no light is picked
 __device__ __forceinline__ int sample_lights(const DevScene& sc, const Vtx& v, uint32_t& seed, float& light_pdf,
                                              f4& w_i) {
+  // The reference keeps each light's sample and weight in arrays; here the weights are
+  // summed in a first sweep and the chosen light's sample is drawn again in a second
+  // sweep that replays the same xorshift stream, so nothing is spilled to local memory
+  // and every value is computed by the same operations in the same order.
   const int n = sc.n_lights;
+  const uint32_t seed0 = seed;
   float sum = 0.0f;
-  float weights[MAX_LIGHTS];
-  f4 w_is[MAX_LIGHTS];
   for (int i = 0; i < n; ++i) {
     const yc_quad_light& L = sc.lights[i];
     const float r1 = draw(seed);
     const float r2 = draw(seed);
     f4 t = ((ld4(L.pos) + r1 * ld4(L.edge_l)) + r2 * ld4(L.edge_w)) - v.hp;
     const float distance = ym::dot(t, t);
-    w_is[i] = t;
+    const f4 ti = t;
     t = ym::normalize(t);
     const f4 ln = ld4(L.normal);
     const float cf = ym::mul(ym::max(ym::dot(t, v.n), 0.0f), ym::max(ym::dot(-t, ln), 0.0f));
-    if (cf <= 0.0f) { weights[i] = 0.0f; continue; }
+    if (cf <= 0.0f) continue;
     const float area = ym::mul(ym::length(ld4(L.edge_l)), ym::length(ld4(L.edge_w)));
     if (n == 1) {
-      w_i = w_is[i];
+      w_i = ti;
       light_pdf = ym::div(1.0f, area);
       light_pdf = ym::mul(light_pdf, ym::div(distance, ym::fmax(ym::dot(-t, ln), 0.0f)));
       return i;
     }
-    weights[i] = ym::div(ym::mul(ym::mul(ym::length(ld4(L.ke)), cf), area), distance);
-    sum = ym::add(sum, weights[i]);
+    sum = ym::add(sum, ym::div(ym::mul(ym::mul(ym::length(ld4(L.ke)), cf), area), distance));
   }
   if (sum == 0.0f) return -1;
   const float r1 = draw(seed);
   float cum = 0.0f;
+  uint32_t replay = seed0;
   for (int i = 0; i < n; ++i) {
-    const float wgt = ym::div(weights[i], sum);
+    const yc_quad_light& L = sc.lights[i];
+    const float q1 = draw(replay);
+    const float q2 = draw(replay);
+    f4 t = ((ld4(L.pos) + q1 * ld4(L.edge_l)) + q2 * ld4(L.edge_w)) - v.hp;
+    const float distance = ym::dot(t, t);
+    const f4 ti = t;
+    t = ym::normalize(t);
+    const f4 ln = ld4(L.normal);
+    const float cf = ym::mul(ym::max(ym::dot(t, v.n), 0.0f), ym::max(ym::dot(-t, ln), 0.0f));
+    const float area = ym::mul(ym::length(ld4(L.edge_l)), ym::length(ld4(L.edge_w)));
+    const float weight = cf <= 0.0f ? 0.0f : ym::div(ym::mul(ym::mul(ym::length(ld4(L.ke)), cf), area), distance);
+    const float wgt = ym::div(weight, sum);
     if (r1 >= cum && r1 < ym::add(cum, wgt)) {
-      const yc_quad_light& L = sc.lights[i];
-      const float area = ym::mul(ym::length(ld4(L.edge_l)), ym::length(ld4(L.edge_w)));
-      w_i = w_is[i];
+      w_i = ti;
       light_pdf = ym::div(wgt, area);
-      light_pdf = ym::mul(light_pdf, ym::div(ym::dot(w_i, w_i), ym::fmax(ym::dot(-ym::normalize(w_i), ld4(L.normal)), 0.0f)));
+      light_pdf = ym::mul(light_pdf, ym::div(ym::dot(w_i, w_i), ym::fmax(ym::dot(-ym::normalize(w_i), ln), 0.0f)));
       return i;
     }
     cum = ym::add(cum, wgt);
