@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--spp-max", type=int, default=128)
     ap.add_argument("--max-tris", type=int, default=500_000)
     ap.add_argument("--profile", action="store_true", help="c2: per-kernel split of the batched run")
+    ap.add_argument("--quality", default="", help="comma list of configs: RMSE against the FP64 references")
     return ap.parse_args()
 
 
@@ -206,7 +207,7 @@ def run_reference(args, rank, ws, dist):
 
 
 def run_ours(args, rank, local, ws, dist):
-    from yune_gb300 import scenes
+    from yune_gb300 import quality, scenes
     from yune_gb300.core import Renderer
     scene = scene_for(args.config)
     seeds = scenes.pass_seeds(0, args.warmup + args.steps + args.e2e_steps)
@@ -298,6 +299,7 @@ def run_ours(args, rank, local, ws, dist):
                 "h2d_bytes_per_step": 80 + 4, "d2h_bytes_per_step": W * H * 16,
                 "steps": args.e2e_steps},
         "clocks": clk.summary(),
+        "image_error": quality.report(img, args.config, int(img[0, 0, 3])),
         "stack_overflow": st["stack_overflow"],
         "image_mean": float(np.nanmean(img[..., :3])),
     }
@@ -411,8 +413,42 @@ def run_c3(args):
     print(json.dumps(out))
 
 
+def run_quality(args):
+    """Relative RMSE of each configuration against its FP64 reference, at the
+    configuration's passes and at four times as many (an unbiased estimator halves it)."""
+    from yune_gb300 import quality, scenes
+    from yune_gb300.core import Renderer
+    r = Renderer(0)
+    out = {"metric": "relative RMSE vs the 65,536-pass FP64 reference", "configs": {}}
+    for name in args.quality.split(","):
+        s = scenes.CONFIGS[name]()
+        sid = r.upload(s)
+        r.set_camera(s.cam)
+        aid = r.alloc_accum(s.width, s.height)
+        res = {}
+        seeds = scenes.pass_seeds(11, 4 * s.spp)
+        t0 = time.perf_counter()
+        done = 0
+        for n in (s.spp, 4 * s.spp):
+            r.render_passes(sid, aid, seeds[done:n], reset_first=1 if done == 0 else 0, cfg=s.cfg)
+            done = n
+            res[str(n)] = quality.report(r.read_accum(aid), name, n)
+        res["seconds"] = time.perf_counter() - t0
+        a, b = res[str(s.spp)]["rel_rmse"], res[str(4 * s.spp)]["rel_rmse"]
+        res["decay_ratio_4x"] = a / b if b > 0 else None
+        a, b = res[str(s.spp)]["rmse_trimmed_1pct"], res[str(4 * s.spp)]["rmse_trimmed_1pct"]
+        res["decay_ratio_4x_trimmed"] = a / b if b > 0 else None
+        out["configs"][name] = res
+        r.free_accum(aid)
+        r.release(sid)
+    r.close()
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
+    if args.quality:
+        return run_quality(args)
     if args.impl == "ours" and args.config == "c2":
         return run_c2(args)
     if args.impl == "ours" and args.config == "c3":

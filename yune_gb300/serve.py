@@ -43,7 +43,7 @@ class Request:
 
 class Server:
     def __init__(self, renderer, resident, hbm_budget, pool_paths=1 << 21, rounds_per_launch=8, keep_results=False,
-                 cfg=None):
+                 cfg=None, logic_blocks_per_sm=2, sort_threshold=1 << 16):
         self.r = renderer
         self.scenes = resident
         self.sids = [renderer.upload(s) for s in resident]
@@ -53,7 +53,7 @@ class Server:
         self.cfg = cfg or scenes.default_cfg(max_depth=16)
         cap = max(renderer.scene_depth(sid) for sid in self.sids) + 2
         self.batch = Batch(renderer, pool_paths=pool_paths, rounds_per_launch=rounds_per_launch, max_jobs=4096,
-                           stack_cap=cap)
+                           stack_cap=cap, logic_blocks_per_sm=logic_blocks_per_sm, sort_threshold=sort_threshold)
 
     def _admit(self, q, now):
         if q.bytes > self.budget:
