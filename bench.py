@@ -60,6 +60,11 @@ def parse():
     ap.add_argument("--max-tris", type=int, default=500_000)
     ap.add_argument("--profile", action="store_true", help="c2: per-kernel split of the batched run")
     ap.add_argument("--quality", default="", help="comma list of configs: RMSE against the FP64 references")
+    ap.add_argument("--trace-bench", type=int, default=0, help="traversal alone on this many seeded rays")
+    ap.add_argument("--tail", type=int, default=-1, help="paths left at which a pass ends in the tail kernel "
+                                                         "(-1 auto, 0 off)")
+    ap.add_argument("--tree", type=int, default=1,
+                    help="interior hierarchy: 0 reference nodes, 1 binary SAH over the reference leaves, 2 four-wide")
     return ap.parse_args()
 
 
@@ -213,6 +218,8 @@ def run_ours(args, rank, local, ws, dist):
     seeds = scenes.pass_seeds(0, args.warmup + args.steps + args.e2e_steps)
     W, H = scene.width, scene.height
     r = Renderer(local)
+    r.set_tree_mode(args.tree)
+    r.set_tail_paths(args.tail)
     sid = r.upload(scene)
     r.set_camera(scene.cam)
     aid = r.alloc_accum(W, H)
@@ -261,10 +268,11 @@ def run_ours(args, rank, local, ws, dist):
         r.close()
         return
     pk, pk_kind = peaks()
-    ext_bytes = 64.0 * st["ext_nodes"] + 48.0 * st["ext_tris"] + 32.0 * st["ext_rays"] + 52.0 * st["ext_rays"]
+    ext_bytes = 32.0 * st["ext_boxes"] + 48.0 * st["ext_tris"] + 32.0 * st["ext_rays"] + 52.0 * st["ext_rays"]
     ext_ms = kt["extend_ms"]
     achieved = ext_bytes / (ext_ms / 1e3) / 1e9 if ext_ms > 0 else 0.0
-    launches = int(kt["raygen_launches"] + kt["extend_launches"] + kt["occlusion_launches"] + kt["logic_launches"])
+    launches = int(kt["raygen_launches"] + kt["extend_launches"] + kt["occlusion_launches"] + kt["logic_launches"]
+                   + kt["tail_launches"])
     traffic = None
     prof_file = os.path.join(ROOT, "profiles", "extend_traffic.json")
     if os.path.exists(prof_file):
@@ -286,14 +294,14 @@ def run_ours(args, rank, local, ws, dist):
         "traversed_rays": st["traversed"],
         "gpu_launches": launches,
         "kernel_ms": {"raygen": kt["raygen_ms"], "extend": kt["extend_ms"], "occlusion": kt["occlusion_ms"],
-                      "logic": kt["logic_ms"], "rounds": kt["rounds"]},
+                      "logic": kt["logic_ms"], "tail": kt["tail_ms"], "rounds": kt["rounds"]},
         "roofline": {"kernel": "k_trace_paths<false> (extend)", "bound": "l2", "achieved": achieved,
                      "peak": l2, "unit": "GB/s", "frac": achieved / l2 if l2 else None, "traffic": traffic,
                      "peak_source": "measured L2 read bandwidth (yc_measure_l2_gbs, 48 MB x 20 sweeps)",
                      "hbm_peak": pk.get("hbm_gbs"), "hbm_frac": achieved / pk.get("hbm_gbs", 1.0),
                      "hbm_peak_source": pk_kind,
                      "bytes_per_ray": ext_bytes / max(1, st["ext_rays"]),
-                     "box_tests_per_ray": 2.0 * st["ext_nodes"] / max(1, st["ext_rays"]),
+                     "box_tests_per_ray": st["ext_boxes"] / max(1, st["ext_rays"]),
                      "tri_tests_per_ray": st["ext_tris"] / max(1, st["ext_rays"])},
         "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else 0.0, "unit": METRIC,
                 "h2d_bytes_per_step": 80 + 4, "d2h_bytes_per_step": W * H * 16,
@@ -316,6 +324,7 @@ def run_c2(args):
     from yune_gb300.core import Renderer
     jobs = workloads.c2_jobs(n_jobs=args.jobs, spp=args.spp, max_tris=args.max_tris)
     r = Renderer(0)
+    r.set_tree_mode(args.tree)
     sids = [r.upload(s) for s in jobs]
     seeds = [scenes.pass_seeds(1000 + i, s.spp) for i, s in enumerate(jobs)]
     px = sum(s.width * s.height for s in jobs)
@@ -445,10 +454,53 @@ def run_quality(args):
     print(json.dumps(out))
 
 
+def run_trace_bench(args):
+    """Traversal alone: seeded incoherent rays (origins uniform in the Cornell box,
+    directions uniform on the sphere) through yc_trace_device, closest hit and any hit,
+    inputs resident on the device, CUDA-event time of the trace kernel."""
+    import torch
+    from yune_gb300 import scenes
+    from yune_gb300.core import Renderer
+    scene = scene_for(args.config)
+    n = args.trace_bench
+    rays = torch.from_numpy(scenes.box_rays(n, seed=3)).cuda()
+    tri = torch.empty(n, dtype=torch.int32, device="cuda")
+    t = torch.empty(n, dtype=torch.float32, device="cuda")
+    r = Renderer(0)
+    r.set_tree_mode(args.tree)
+    sid = r.upload(scene)
+    out = {"metric": "traversal Mrays/s", "config": {"workload": "%s, %d seeded incoherent rays" % (args.config, n),
+                                                     "tree_mode": args.tree}}
+    for any_hit in (False, True):
+        for _ in range(args.warmup):
+            r.trace_device(sid, rays.data_ptr(), n, any_hit, tri.data_ptr(), t.data_ptr())
+        r.synchronize()
+        r.reset_stats()
+        r.set_profiling(True)
+        for _ in range(args.steps):
+            r.flush_l2(256 << 20)
+            r.trace_device(sid, rays.data_ptr(), n, any_hit, tri.data_ptr(), t.data_ptr())
+        kt = r.kernel_times()
+        r.set_profiling(False)
+        st = r.stats()
+        ms = kt["occlusion_ms"] if any_hit else kt["extend_ms"]
+        pre = "any" if any_hit else "ext"
+        nr = st[pre + "_rays"]
+        nb = 32.0 * st[pre + "_boxes"] + 48.0 * st[pre + "_tris"] + (52.0 if not any_hit else 36.0) * nr
+        out["any_hit" if any_hit else "closest"] = {
+            "Mrays_s": nr / (ms / 1e3) / 1e6, "ms_per_launch": ms / args.steps,
+            "box_tests_per_ray": st[pre + "_boxes"] / max(1, nr), "tri_tests_per_ray": st[pre + "_tris"] / max(1, nr),
+            "algorithmic_GBs": nb / (ms / 1e3) / 1e9}
+    r.close()
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.quality:
         return run_quality(args)
+    if args.trace_bench:
+        return run_trace_bench(args)
     if args.impl == "ours" and args.config == "c2":
         return run_c2(args)
     if args.impl == "ours" and args.config == "c3":

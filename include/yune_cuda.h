@@ -71,11 +71,11 @@ typedef struct yc_stats {
   uint64_t traversed;       /* queries that walked the BVH */
   uint64_t samples;         /* pixel paths completed */
   uint64_t stack_overflow;  /* traversals that hit the stack bound (must be 0) */
-  /* work of the traversal kernels: rays walked, two-child nodes fetched (2 box tests,
-   * 64 B each) and triangles tested (48 B each), for the closest-hit (extend) and the
-   * any-hit (occlusion) kernel */
-  uint64_t ext_rays, ext_nodes, ext_tris;
-  uint64_t any_rays, any_nodes, any_tris;
+  /* work of the traversal kernels: rays walked, child boxes tested (32 B each; two per
+   * two-child node, four per four-child node) and triangles tested (48 B each), for the
+   * closest-hit (extend) and the any-hit (occlusion) kernel */
+  uint64_t ext_rays, ext_boxes, ext_tris;
+  uint64_t any_rays, any_boxes, any_tris;
 } yc_stats;
 
 /* Device time per kernel kind, summed over launches since the last reset, when
@@ -86,6 +86,8 @@ typedef struct yc_kernel_times {
   uint64_t rounds;
   double sort_ms;              /* batch engine: shade-queue sort (histogram, scan, scatter) */
   uint64_t sort_launches;
+  double tail_ms;              /* tail kernel (YC_OPT_TAIL) */
+  uint64_t tail_launches;
 } yc_kernel_times;
 
 typedef struct yc_ctx yc_ctx;
@@ -206,10 +208,17 @@ enum {
   /* Interior hierarchy of uploaded scenes (applies to later yc_upload_scene calls):
    * 0 = the reference node tree as given; 1 (default) = the reference's leaves, each with
    * its triangles in vert_list order, under interior nodes rebuilt by a binned SAH over
-   * the leaf boxes. Both give the reference's closest hit bit for bit; 1 tests fewer
-   * boxes (the reference tree keeps the spatial boxes of empty children in its parents'
-   * bounds and falls back to spatial-median splits below a node area of about 1). */
-  YC_OPT_TREE = 1
+   * the leaf boxes; 2 = the same hierarchy collapsed to four-child nodes (128 B, four
+   * boxes tested per node visit). All give the reference's closest hit bit for bit; 1
+   * and 2 test fewer boxes (the reference tree keeps the spatial boxes of empty children
+   * in its parents' bounds and falls back to spatial-median splits below a node area of
+   * about 1). */
+  YC_OPT_TREE = 1,
+  /* End of a unidirectional pass: once at most this many paths are left, one kernel
+   * finishes them a thread per path (trace and shading in turn) instead of round by
+   * round; the result is the same bits. -1 (default) = as many paths as one resident
+   * launch of that kernel holds; 0 = off. */
+  YC_OPT_TAIL = 2
 };
 int yc_set_option(yc_ctx* ctx, int option, int value);
 

@@ -37,7 +37,7 @@ def _cmp_closest(gpu, orc):
     return int(diff.sum()), int(tie.sum())
 
 
-@pytest.mark.parametrize("tree", [0, 1])
+@pytest.mark.parametrize("tree", [0, 1, 2])
 @pytest.mark.parametrize("cfg_name,level", [("c0", None), ("c1", 6)])
 def test_trace_closest_and_any(renderer, cfg_name, level, tree):
     s = scenes.c0(64, 64) if cfg_name == "c0" else scenes.c1(64, 64, level=level)
@@ -59,7 +59,7 @@ def test_trace_closest_and_any(renderer, cfg_name, level, tree):
     renderer.release(sid)
 
 
-@pytest.mark.parametrize("tree", [0, 1])
+@pytest.mark.parametrize("tree", [0, 1, 2])
 def test_trace_axis_aligned_rays(renderer, tree):
     """Rays with zero direction components take the reference's NaN-skipping slab path."""
     s = scenes.c0(64, 64)
@@ -201,3 +201,52 @@ def test_render_parity_bdpt(renderer, bounces, lights):
     assert _rel_bad(gpu, ref) == 0
     assert np.array_equal(gpu[..., 3], ref[..., 3])
     assert st["samples"] == 40 * 32 * 2
+
+
+@pytest.mark.parametrize("tree", [0, 2])
+def test_render_identical_across_tree_modes(renderer, tree):
+    """Every interior hierarchy gives the reference's hits, so whole renders are the same
+    bits as with the default one."""
+    s = scenes.c1(40, 32, level=5)
+    seeds = scenes.pass_seeds(21, 2)
+    out = []
+    for mode in (1, tree):
+        renderer.set_tree_mode(mode)
+        sid = renderer.upload(s)
+        renderer.set_tree_mode(1)
+        renderer.set_camera(s.cam)
+        aid = renderer.alloc_accum(40, 32)
+        renderer.reset_stats()
+        renderer.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+        out.append((renderer.read_accum(aid), renderer.stats()))
+        renderer.free_accum(aid)
+        renderer.release(sid)
+    assert out[1][1]["stack_overflow"] == 0
+    assert np.array_equal(out[0][0].view(np.int32), out[1][0].view(np.int32))
+    assert out[0][1]["rays"] == out[1][1]["rays"]
+
+
+@pytest.mark.parametrize("tree", [1, 2])
+def test_tail_kernel_gives_the_same_pass(renderer, tree):
+    """Finishing the last paths a thread each (YC_OPT_TAIL) changes no bit of the pass and
+    no ray count: off, from 64 paths, and from one resident launch (the default)."""
+    s = scenes.c1(48, 40, level=5)
+    seeds = scenes.pass_seeds(8, 3)
+    renderer.set_tree_mode(tree)
+    sid = renderer.upload(s)
+    renderer.set_tree_mode(1)
+    renderer.set_camera(s.cam)
+    out = []
+    for tail in (0, 64, -1):
+        renderer.set_tail_paths(tail)
+        aid = renderer.alloc_accum(48, 40)
+        renderer.reset_stats()
+        renderer.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+        out.append((renderer.read_accum(aid), renderer.stats()))
+        renderer.free_accum(aid)
+    renderer.set_tail_paths(-1)
+    renderer.release(sid)
+    for img, st in out[1:]:
+        assert np.array_equal(img.view(np.int32), out[0][0].view(np.int32))
+        for k in ("rays", "extension", "shadow", "mis", "samples", "ext_rays", "any_rays", "stack_overflow"):
+            assert st[k] == out[0][1][k], k

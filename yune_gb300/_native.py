@@ -25,8 +25,8 @@ class PassCfg(C.Structure):
 class Stats(C.Structure):
     """yc_stats"""
     _fields_ = [(n, C.c_uint64) for n in ("rays", "primary", "extension", "shadow", "mis", "connection",
-                                          "traversed", "samples", "stack_overflow", "ext_rays", "ext_nodes",
-                                          "ext_tris", "any_rays", "any_nodes", "any_tris")]
+                                          "traversed", "samples", "stack_overflow", "ext_rays", "ext_boxes",
+                                          "ext_tris", "any_rays", "any_boxes", "any_tris")]
 
 
 class KernelTimes(C.Structure):
@@ -34,7 +34,8 @@ class KernelTimes(C.Structure):
     _fields_ = [("raygen_ms", C.c_double), ("extend_ms", C.c_double), ("occlusion_ms", C.c_double),
                 ("logic_ms", C.c_double), ("raygen_launches", C.c_uint64), ("extend_launches", C.c_uint64),
                 ("occlusion_launches", C.c_uint64), ("logic_launches", C.c_uint64), ("rounds", C.c_uint64),
-                ("sort_ms", C.c_double), ("sort_launches", C.c_uint64)]
+                ("sort_ms", C.c_double), ("sort_launches", C.c_uint64), ("tail_ms", C.c_double),
+                ("tail_launches", C.c_uint64)]
 
 
 class BatchCfg(C.Structure):

@@ -116,6 +116,11 @@ class Renderer:
         N.check(self.L.yc_trace(self.h, sid, ptr(rays9), n, int(any_hit), ptr(tri), ptr(light), ptr(t)), "yc_trace")
         return tri, light, t
 
+    def trace_device(self, sid, rays_ptr, n, any_hit, tri_ptr, t_ptr):
+        """yc_trace_device on caller-owned device buffers (9 floats per ray in)."""
+        N.check(self.L.yc_trace_device(self.h, sid, C.c_void_p(rays_ptr), n, int(any_hit), C.c_void_p(tri_ptr),
+                                       C.c_void_p(t_ptr)), "yc_trace_device")
+
     def stats(self):
         s = N.Stats()
         N.check(self.L.yc_get_stats(self.h, C.byref(s)), "yc_get_stats")
@@ -132,6 +137,10 @@ class Renderer:
     def set_tree_mode(self, mode):
         """0: reference node tree; 1: SAH hierarchy over the reference leaves (default)."""
         N.check(self.L.yc_set_option(self.h, 1, int(mode)), "yc_set_option")
+
+    def set_tail_paths(self, n):
+        """Paths left at which a pass finishes in the tail kernel (-1 auto, 0 off)."""
+        N.check(self.L.yc_set_option(self.h, 2, int(n)), "yc_set_option")
 
     def set_profiling(self, on=True):
         N.check(self.L.yc_set_profiling(self.h, int(on)), "yc_set_profiling")

@@ -91,6 +91,7 @@ struct yc_ctx {
   yc_cam cam{};
   bool have_cam = false;
   int tree_mode = yc::TREE_SAH_OVER_LEAVES;
+  int tail_paths = -1;   // YC_OPT_TAIL: -1 = one resident launch of the tail kernel, 0 = off
   // wavefront buffers, sized for the largest image seen
   size_t cap_paths = 0;
   DevBuf<int4> misc;
@@ -131,7 +132,7 @@ int ensure_paths(yc_ctx* c, size_t n) {
 }
 
 // event pairs around kernel launches (profiling only)
-enum { K_RAYGEN = 0, K_EXTEND = 1, K_OCCL = 2, K_LOGIC = 3, K_SORT = 4 };
+enum { K_RAYGEN = 0, K_EXTEND = 1, K_OCCL = 2, K_LOGIC = 3, K_SORT = 4, K_TAIL = 5 };
 cudaEvent_t next_event(yc_ctx* c) {
   if (c->ev_used == c->ev_pool.size()) {
     cudaEvent_t e;
@@ -171,6 +172,7 @@ void collect_events(yc_ctx* c) {
       case K_EXTEND: c->ktimes.extend_ms += ms; c->ktimes.extend_launches++; break;
       case K_OCCL: c->ktimes.occlusion_ms += ms; c->ktimes.occlusion_launches++; break;
       case K_SORT: c->ktimes.sort_ms += ms; c->ktimes.sort_launches++; break;
+      case K_TAIL: c->ktimes.tail_ms += ms; c->ktimes.tail_launches++; break;
       default: c->ktimes.logic_ms += ms; c->ktimes.logic_launches++; break;
     }
   }
@@ -263,9 +265,14 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     else yc::launch_raygen(pp, ps, c->q[0].p, rc + 0, c->stats.p, c->stream);
   }
   YC_CUDA(cudaPeekAtLastError());
-  const int grid_c = yc::trace_grid_blocks(false, sc->dev.depth);
-  const int grid_a = yc::trace_grid_blocks(true, sc->dev.depth);
+  const int grid_c = yc::trace_grid_blocks(false, sc->dev.depth, sc->dev.wide != 0);
+  const int grid_a = yc::trace_grid_blocks(true, sc->dev.depth, sc->dev.wide != 0);
   if (grid_c <= 0 || grid_a <= 0) return fail(YC_E_LAUNCH, "trace kernel cannot be resident (stack too deep)");
+  int tail_grid = 0, tail_at = 0;
+  if (!bdpt && c->tail_paths != 0) {
+    const int capacity = yc::tail_capacity(sc->dev, &tail_grid);
+    tail_at = c->tail_paths < 0 ? capacity : std::min(c->tail_paths, capacity);
+  }
   int cur = 0;
   const int check_every = 6;
   for (int round = 0; round < 1000000; ++round) {
@@ -294,6 +301,11 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
       if (bdpt) yc::launch_logic_bdpt(pp, ps, bb, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid,
                                       c->stream);
       else yc::launch_logic(pp, ps, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid, c->stream);
+    }
+    if (tail_at > 0) {
+      KTimer kt(c, K_TAIL);
+      if (yc::launch_tail(pp, ps, out_c, out_a, rout, tail_at, c->stats.p, tail_grid, c->stream))
+        return fail(YC_E_LAUNCH, std::string("tail kernel: ") + cudaGetErrorString(cudaGetLastError()));
     }
     YC_CUDA(cudaPeekAtLastError());
     c->ktimes.rounds++;
@@ -408,6 +420,7 @@ int yc_upload_scene(yc_ctx* c, const yc_triangle* tris, int n_tri, const yc_mate
   d.root_link = rp.root_link;
   d.root_test = rp.root_test;
   d.depth = rp.depth;
+  d.wide = rp.wide;
   d.root_lo = rp.root_lo;
   d.root_hi = rp.root_hi;
   s->bytes = s->nodes.bytes() + s->tris.bytes() + s->shade.bytes() + s->mats.bytes() + s->lights.bytes();
@@ -598,8 +611,12 @@ int yc_trace_device(yc_ctx* c, int scene_id, const float* rays_dev, int n, int a
   if (!s) return fail(YC_E_NOTFOUND, "unknown scene");
   if (n == 0) return YC_OK;
   YC_CUDA(cudaMemsetAsync(c->q_work.p, 0, sizeof(int), c->stream));
-  if (yc::launch_trace_rays(s->dev, any_hit != 0, rays_dev, n, tri_dev, t_dev, c->q_work.p, c->stats.p, c->stream))
-    return fail(YC_E_LAUNCH, std::string("trace kernel: ") + cudaGetErrorString(cudaGetLastError()));
+  int e;
+  {
+    KTimer kt(c, any_hit ? K_OCCL : K_EXTEND);
+    e = yc::launch_trace_rays(s->dev, any_hit != 0, rays_dev, n, tri_dev, t_dev, c->q_work.p, c->stats.p, c->stream);
+  }
+  if (e) return fail(YC_E_LAUNCH, std::string("trace kernel: ") + cudaGetErrorString(cudaGetLastError()));
   return YC_OK;
 }
 
@@ -647,10 +664,10 @@ int yc_get_stats(yc_ctx* c, yc_stats* out) {
   out->samples = d.samples;
   out->stack_overflow = d.stack_overflow;
   out->ext_rays = d.ext_rays;
-  out->ext_nodes = d.ext_nodes;
+  out->ext_boxes = d.ext_boxes;
   out->ext_tris = d.ext_tris;
   out->any_rays = d.any_rays;
-  out->any_nodes = d.any_nodes;
+  out->any_boxes = d.any_boxes;
   out->any_tris = d.any_tris;
   return YC_OK;
 }
@@ -666,8 +683,13 @@ int yc_set_option(yc_ctx* c, int option, int value) {
   if (!c) return fail(YC_E_INVALID, "ctx is NULL");
   switch (option) {
     case YC_OPT_TREE:
-      if (value != yc::TREE_REFERENCE && value != yc::TREE_SAH_OVER_LEAVES) return fail(YC_E_INVALID, "bad tree mode");
+      if (value != yc::TREE_REFERENCE && value != yc::TREE_SAH_OVER_LEAVES && value != yc::TREE_WIDE4)
+        return fail(YC_E_INVALID, "bad tree mode");
       c->tree_mode = value;
+      return YC_OK;
+    case YC_OPT_TAIL:
+      if (value < -1) return fail(YC_E_INVALID, "bad tail threshold");
+      c->tail_paths = value;
       return YC_OK;
     default:
       return fail(YC_E_INVALID, "unknown option");
@@ -730,6 +752,7 @@ struct yc_batch {
   std::vector<yc::BatchJob> host_jobs;
   long long task_total = 0;
   int stack_cap = 0;
+  int wide = -1;   // node layout of the batch's scenes (-1: no job yet)
   int grid_c = 0, grid_a = 0, logic_grid = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -774,13 +797,13 @@ int batch_round(yc_batch* b, int cur, bool timed) {
   yc::RoundCounters* rout = b->rc.p + (1 - cur);
   {
     KTimer kt(c, K_EXTEND, timed);
-    yc::launch_batch_trace(false, b->jobs.p, b->job_pass.p, in_c, &rin->n_closest, &rin->work_closest, ps.ro, ps.rd,
-                           ps.hit, c->stats.p, b->stack_cap, b->grid_c, c->stream);
+    yc::launch_batch_trace(false, b->wide == 1, b->jobs.p, b->job_pass.p, in_c, &rin->n_closest, &rin->work_closest,
+                           ps.ro, ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_c, c->stream);
   }
   {
     KTimer kt(c, K_OCCL, timed);
-    yc::launch_batch_trace(true, b->jobs.p, b->job_pass.p, in_a, &rin->n_any, &rin->work_any, ps.ro, ps.rd, ps.hit,
-                           c->stats.p, b->stack_cap, b->grid_a, c->stream);
+    yc::launch_batch_trace(true, b->wide == 1, b->jobs.p, b->job_pass.p, in_a, &rin->n_any, &rin->work_any, ps.ro,
+                           ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_a, c->stream);
   }
   YC_CUDA(cudaMemsetAsync(rout, 0, sizeof(yc::RoundCounters), c->stream));
   YC_CUDA(cudaMemsetAsync(b->sctl.p, 0, sizeof(yc::SortCtl), c->stream));
@@ -895,6 +918,8 @@ int yc_batch_add_job(yc_batch* b, int scene_id, int accum_id, const yc_cam* cam,
   Accum* ac = find_accum(c, accum_id);
   if (!ac) return fail(YC_E_NOTFOUND, "unknown accumulator");
   if ((int)b->host_jobs.size() >= b->cfg.max_jobs) return fail(YC_E_BUDGET, "job table full");
+  if (b->wide >= 0 && sc->dev.wide != b->wide)
+    return fail(YC_E_INVALID, "scene node layout differs from the batch's other scenes (tree mode changed)");
   const int need_cap = sc->dev.depth + 2;
   if (!b->started) b->stack_cap = std::max(b->stack_cap, b->cfg.stack_cap > 0 ? b->cfg.stack_cap : need_cap);
   else if (need_cap > b->stack_cap)
@@ -938,6 +963,7 @@ int yc_batch_add_job(yc_batch* b, int scene_id, int accum_id, const yc_cam* cam,
   YC_CUDA(cudaStreamSynchronize(c->stream));
   b->host_jobs.push_back(j);
   b->seeds.push_back(std::move(sd));
+  b->wide = sc->dev.wide;
   *job_id = id;
   return YC_OK;
 }
@@ -948,8 +974,8 @@ int yc_batch_run(yc_batch* b, int max_launches, int* unfinished) {
   YC_CUDA(cudaSetDevice(c->device));
   if (!b->started) {
     if (b->stack_cap <= 0) b->stack_cap = b->cfg.stack_cap > 0 ? b->cfg.stack_cap : 32;
-    b->grid_c = yc::batch_trace_grid(false, b->stack_cap);
-    b->grid_a = yc::batch_trace_grid(true, b->stack_cap);
+    b->grid_c = yc::batch_trace_grid(false, b->stack_cap, b->wide == 1);
+    b->grid_a = yc::batch_trace_grid(true, b->stack_cap, b->wide == 1);
     if (b->grid_c <= 0 || b->grid_a <= 0) return fail(YC_E_LAUNCH, "batch trace kernel cannot be resident");
     b->started = true;
   }

@@ -324,43 +324,50 @@ struct BatchSrc {
   }
 };
 
-template <bool ANY>
+template <bool ANY, bool WIDE>
 __global__ void __launch_bounds__(TRACE_TB) k_batch_trace(const BatchJob* jobs, const int2* job_pass,
                                                           const int* __restrict__ queue, const int* __restrict__ count,
                                                           int* work, const float4* __restrict__ ro,
                                                           const float4* __restrict__ rd, float4* hit, int stack_cap,
                                                           DevStats* st) {
   BatchSrc<ANY> src{jobs, job_pass, queue, ro, rd, hit};
-  trace_loop<ANY>(src, *count, work, stack_cap, st);
+  trace_loop<ANY, WIDE>(src, *count, work, stack_cap, st);
 }
 
 static size_t batch_smem(int cap) { return (size_t)TRACE_TB * 2 * cap * sizeof(int); }
 
-int batch_trace_grid(bool any_hit, int stack_cap) {
+template <class K>
+static int batch_grid_of(K kernel, size_t smem) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t smem = batch_smem(stack_cap);
-  if (any_hit) {
-    cudaFuncSetAttribute(k_batch_trace<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_trace<true>, TRACE_TB, smem);
-  } else {
-    cudaFuncSetAttribute(k_batch_trace<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_trace<false>, TRACE_TB, smem);
-  }
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TRACE_TB, smem);
   return per_sm > 0 ? per_sm * sms : -1;
 }
 
-int launch_batch_trace(bool any_hit, const BatchJob* jobs, const int2* job_pass, const int* queue, const int* count,
-                       int* work, const float4* ro, const float4* rd, float4* hit, DevStats* st, int stack_cap,
-                       int grid_blocks, cudaStream_t s) {
+int batch_trace_grid(bool any_hit, int stack_cap, bool wide) {
   const size_t smem = batch_smem(stack_cap);
-  if (any_hit)
-    k_batch_trace<true><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
-                                                            stack_cap, st);
+  if (wide) return any_hit ? batch_grid_of(k_batch_trace<true, true>, smem) : batch_grid_of(k_batch_trace<false, true>, smem);
+  return any_hit ? batch_grid_of(k_batch_trace<true, false>, smem) : batch_grid_of(k_batch_trace<false, false>, smem);
+}
+
+int launch_batch_trace(bool any_hit, bool wide, const BatchJob* jobs, const int2* job_pass, const int* queue,
+                       const int* count, int* work, const float4* ro, const float4* rd, float4* hit, DevStats* st,
+                       int stack_cap, int grid_blocks, cudaStream_t s) {
+  const size_t smem = batch_smem(stack_cap);
+  if (any_hit && wide)
+    k_batch_trace<true, true><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
+                                                                  stack_cap, st);
+  else if (any_hit)
+    k_batch_trace<true, false><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
+                                                                   stack_cap, st);
+  else if (wide)
+    k_batch_trace<false, true><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
+                                                                   stack_cap, st);
   else
-    k_batch_trace<false><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
-                                                             stack_cap, st);
+    k_batch_trace<false, false><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
+                                                                    stack_cap, st);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -139,8 +139,8 @@ int noalloc_render(const NoallocPass& a, std::string& err) {
     return YC_E_LAUNCH;
   }
   k_raygen_tile<<<(n_paths + 255) / 256, 256, 0, s>>>(a.pp, ps, qs[0], rc, a.stats);
-  const int grid_c = trace_grid_blocks(false, a.pp.sc.depth);
-  const int grid_a = trace_grid_blocks(true, a.pp.sc.depth);
+  const int grid_c = trace_grid_blocks(false, a.pp.sc.depth, a.pp.sc.wide != 0);
+  const int grid_a = trace_grid_blocks(true, a.pp.sc.depth, a.pp.sc.wide != 0);
   if (grid_c <= 0 || grid_a <= 0) {
     err = "trace kernel cannot be resident (stack too deep)";
     return YC_E_LAUNCH;

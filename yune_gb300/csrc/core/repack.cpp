@@ -77,9 +77,20 @@ struct LeafItem {
   int link;
 };
 
+// A child reference of the in-memory binary tree: a leaf (node < 0, link = its leaf
+// link) or an interior node (index into SahBuilder::bins), with its box.
+struct BinRef {
+  int node;
+  int link;
+  float lo[3], hi[3];
+};
+struct BinNode {
+  BinRef c[2];
+};
+
 struct SahBuilder {
   std::vector<LeafItem>& items;
-  std::vector<float4>& out_nodes;
+  std::vector<BinNode> bins;
   int max_depth = 0;
 
   static float area(const float lo[3], const float hi[3]) {
@@ -87,20 +98,24 @@ struct SahBuilder {
     return 2.0f * (d0 * d1 + d0 * d2 + d1 * d2);
   }
 
-  // returns the link of the subtree over items [b, e)
-  int build(int b, int e, int depth, float lo_out[3], float hi_out[3]) {
-    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  // the subtree over items [b, e)
+  BinRef build(int b, int e, int depth) {
+    BinRef r;
     float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int k = 0; k < 3; ++k) { r.lo[k] = INFINITY; r.hi[k] = -INFINITY; }
     for (int i = b; i < e; ++i)
       for (int k = 0; k < 3; ++k) {
-        lo[k] = std::min(lo[k], items[i].lo[k]);
-        hi[k] = std::max(hi[k], items[i].hi[k]);
+        r.lo[k] = std::min(r.lo[k], items[i].lo[k]);
+        r.hi[k] = std::max(r.hi[k], items[i].hi[k]);
         clo[k] = std::min(clo[k], items[i].c[k]);
         chi[k] = std::max(chi[k], items[i].c[k]);
       }
-    for (int k = 0; k < 3; ++k) { lo_out[k] = lo[k]; hi_out[k] = hi[k]; }
     max_depth = std::max(max_depth, depth);
-    if (e - b == 1) return items[b].link;
+    if (e - b == 1) {
+      r.node = -1;
+      r.link = items[b].link;
+      return r;
+    }
     // binned SAH
     constexpr int NB = 32;
     int best_axis = -1, best_split = -1;
@@ -157,20 +172,82 @@ struct SahBuilder {
       mid = (int)(std::partition(items.begin() + b, items.begin() + e, left) - items.begin());
       if (mid == b || mid == e) mid = (b + e) / 2;
     }
-    const int node = (int)(out_nodes.size() / 4);
-    out_nodes.resize(out_nodes.size() + 4);
-    float l0[3], h0[3], l1[3], h1[3];
-    const int c0 = build(b, mid, depth + 1, l0, h0);
-    const int c1 = build(mid, e, depth + 1, l1, h1);
-    float4* o = &out_nodes[4 * (size_t)node];
-    o[0] = float4{l0[0], h0[0], l0[1], h0[1]};
-    o[1] = float4{l1[0], h1[0], l1[1], h1[1]};
-    o[2] = float4{l0[2], h0[2], l1[2], h1[2]};
+    const int node = (int)bins.size();
+    bins.emplace_back();
+    const BinRef c0 = build(b, mid, depth + 1);
+    const BinRef c1 = build(mid, e, depth + 1);
+    bins[node].c[0] = c0;
+    bins[node].c[1] = c1;
+    r.node = node;
+    r.link = 0;
+    return r;
+  }
+
+  // two-child layout of yc_scene.h, nodes in pre-order; returns the link of r
+  int emit_binary(const BinRef& r, std::vector<float4>& out) const {
+    if (r.node < 0) return r.link;
+    const int node = (int)(out.size() / 4);
+    out.resize(out.size() + 4);
+    const BinNode& bn = bins[r.node];
+    const int c0 = emit_binary(bn.c[0], out);
+    const int c1 = emit_binary(bn.c[1], out);
+    const BinRef& a = bn.c[0];
+    const BinRef& b = bn.c[1];
+    float4* o = &out[4 * (size_t)node];
+    o[0] = float4{a.lo[0], a.hi[0], a.lo[1], a.hi[1]};
+    o[1] = float4{b.lo[0], b.hi[0], b.lo[1], b.hi[1]};
+    o[2] = float4{a.lo[2], a.hi[2], b.lo[2], b.hi[2]};
     float4 l;
     std::memcpy(&l.x, &c0, 4);
     std::memcpy(&l.y, &c1, 4);
     l.z = l.w = 0.0f;
     o[3] = l;
+    return node;
+  }
+
+  // four-child layout (yc_scene.h, wide nodes): the children of a binary node are
+  // replaced, largest surface area first, by their own children until four remain.
+  // depth_out: wide levels below r.
+  int emit_wide(const BinRef& r, std::vector<float4>& out, int& depth_out) const {
+    depth_out = 0;
+    if (r.node < 0) return r.link;
+    BinRef kids[4];
+    int nk = 2;
+    kids[0] = bins[r.node].c[0];
+    kids[1] = bins[r.node].c[1];
+    while (nk < 4) {
+      int pick = -1;
+      float best = -1.0f;
+      for (int i = 0; i < nk; ++i)
+        if (kids[i].node >= 0 && area(kids[i].lo, kids[i].hi) > best) { best = area(kids[i].lo, kids[i].hi); pick = i; }
+      if (pick < 0) break;
+      const BinNode& bn = bins[kids[pick].node];
+      kids[pick] = bn.c[0];
+      kids[nk++] = bn.c[1];
+    }
+    const int node = (int)(out.size() / 8);
+    out.resize(out.size() + 8);
+    int links[4] = {LINK_NONE, LINK_NONE, LINK_NONE, LINK_NONE};
+    for (int i = 0; i < nk; ++i) {
+      int d = 0;
+      links[i] = emit_wide(kids[i], out, d);
+      depth_out = std::max(depth_out, d + 1);
+    }
+    float4* o = &out[8 * (size_t)node];
+    float v[6][4];
+    for (int i = 0; i < 4; ++i)
+      for (int k = 0; k < 3; ++k) {
+        v[2 * k][i] = i < nk ? kids[i].lo[k] : 0.0f;
+        v[2 * k + 1][i] = i < nk ? kids[i].hi[k] : 0.0f;
+      }
+    for (int f = 0; f < 6; ++f) o[f] = float4{v[f][0], v[f][1], v[f][2], v[f][3]};
+    float4 l;
+    std::memcpy(&l.x, &links[0], 4);
+    std::memcpy(&l.y, &links[1], 4);
+    std::memcpy(&l.z, &links[2], 4);
+    std::memcpy(&l.w, &links[3], 4);
+    o[6] = l;
+    o[7] = float4{0.0f, 0.0f, 0.0f, 0.0f};
     return node;
   }
 };
@@ -268,7 +345,7 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
     out.tris.swap(b.out_tris);
     return 0;
   }
-  if (tree_mode == TREE_SAH_OVER_LEAVES) {
+  if (tree_mode == TREE_SAH_OVER_LEAVES || tree_mode == TREE_WIDE4) {
     // the leaves the reference traversal can reach, in node-index order
     std::vector<LeafItem> items;
     std::vector<char> reach(n_node, 0);
@@ -293,10 +370,17 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
       }
     }
     if (items.empty()) { out.root_link = LINK_NONE; out.depth = 0; return 0; }
-    SahBuilder sb{items, b.out_nodes};
-    float lo[3], hi[3];
-    out.root_link = sb.build(0, (int)items.size(), 0, lo, hi);
-    out.depth = sb.max_depth + 1;
+    SahBuilder sb{items, {}};
+    const BinRef root_ref = sb.build(0, (int)items.size(), 0);
+    if (tree_mode == TREE_WIDE4) {
+      int d = 0;
+      out.root_link = sb.emit_wide(root_ref, b.out_nodes, d);
+      out.wide = 1;
+      out.depth = 3 * d;   // up to three entries pushed per wide level
+    } else {
+      out.root_link = sb.emit_binary(root_ref, b.out_nodes);
+      out.depth = sb.max_depth + 1;
+    }
     out.nodes.swap(b.out_nodes);
     out.tris.swap(b.out_tris);
     return 0;

@@ -38,14 +38,14 @@ struct PathSrc {
   }
 };
 
-template <bool ANY>
+template <bool ANY, bool WIDE>
 __global__ void __launch_bounds__(TRACE_TB) k_trace_paths(DevScene sc, const int* __restrict__ queue,
                                                           const int* __restrict__ count, int* work,
                                                           const float4* __restrict__ ro,
                                                           const float4* __restrict__ rd, float4* hit, int stack_cap,
                                                           DevStats* st) {
   PathSrc<ANY> src{&sc, queue, ro, rd, hit};
-  trace_loop<ANY>(src, *count, work, stack_cap, st);
+  trace_loop<ANY, WIDE>(src, *count, work, stack_cap, st);
 }
 
 // traceRay (udpt.cl:240-286) on explicit rays of 9 floats: light loop, then the BVH.
@@ -80,12 +80,12 @@ struct RaySrc {
   }
 };
 
-template <bool ANY>
+template <bool ANY, bool WIDE>
 __global__ void __launch_bounds__(TRACE_TB) k_trace_rays(DevScene sc, const float* __restrict__ rays, int n,
                                                          int* work, int* tri_out, float* t_out, int stack_cap,
                                                          DevStats* st) {
   RaySrc<ANY> src{&sc, rays, tri_out, t_out, -1, 0.0f};
-  trace_loop<ANY>(src, n, work, stack_cap, st);
+  trace_loop<ANY, WIDE>(src, n, work, stack_cap, st);
 }
 
 static int stack_cap_for(int depth) { return depth + 2; }
@@ -93,35 +93,40 @@ static size_t smem_for(int cap) { return (size_t)TRACE_TB * 2 * cap * sizeof(int
 
 static int g_sm_count = 0;
 
-int trace_grid_blocks(bool any_hit, int depth) {
+template <class K>
+static int resident_grid(K kernel, size_t smem) {
   if (g_sm_count == 0) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
     if (g_sm_count <= 0) g_sm_count = 1;
   }
-  const int cap = stack_cap_for(depth);
-  const size_t smem = smem_for(cap);
   int per_sm = 0;
-  if (any_hit) {
-    cudaFuncSetAttribute(k_trace_paths<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_paths<true>, TRACE_TB, smem);
-  } else {
-    cudaFuncSetAttribute(k_trace_paths<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_paths<false>, TRACE_TB, smem);
-  }
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TRACE_TB, smem);
   if (per_sm <= 0) return -1;
   return g_sm_count * per_sm;
+}
+
+int trace_grid_blocks(bool any_hit, int depth, bool wide) {
+  const size_t smem = smem_for(stack_cap_for(depth));
+  if (wide) return any_hit ? resident_grid(k_trace_paths<true, true>, smem) : resident_grid(k_trace_paths<false, true>, smem);
+  return any_hit ? resident_grid(k_trace_paths<true, false>, smem) : resident_grid(k_trace_paths<false, false>, smem);
 }
 
 int launch_trace(const DevScene& sc, bool any_hit, const int* queue, const int* count, int* work, const float4* ro,
                  const float4* rd, float4* hit, DevStats* st, int grid_blocks, cudaStream_t s) {
   const int cap = stack_cap_for(sc.depth);
   const size_t smem = smem_for(cap);
-  if (any_hit)
-    k_trace_paths<true><<<grid_blocks, TRACE_TB, smem, s>>>(sc, queue, count, work, ro, rd, hit, cap, st);
+  const bool wide = sc.wide != 0;
+  if (any_hit && wide)
+    k_trace_paths<true, true><<<grid_blocks, TRACE_TB, smem, s>>>(sc, queue, count, work, ro, rd, hit, cap, st);
+  else if (any_hit)
+    k_trace_paths<true, false><<<grid_blocks, TRACE_TB, smem, s>>>(sc, queue, count, work, ro, rd, hit, cap, st);
+  else if (wide)
+    k_trace_paths<false, true><<<grid_blocks, TRACE_TB, smem, s>>>(sc, queue, count, work, ro, rd, hit, cap, st);
   else
-    k_trace_paths<false><<<grid_blocks, TRACE_TB, smem, s>>>(sc, queue, count, work, ro, rd, hit, cap, st);
+    k_trace_paths<false, false><<<grid_blocks, TRACE_TB, smem, s>>>(sc, queue, count, work, ro, rd, hit, cap, st);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -129,15 +134,22 @@ int launch_trace_rays(const DevScene& sc, bool any_hit, const float* rays9, int 
                       int* work, DevStats* st, cudaStream_t s) {
   const int cap = stack_cap_for(sc.depth);
   const size_t smem = smem_for(cap);
-  const int grid = trace_grid_blocks(any_hit, sc.depth);
-  if (grid <= 0) return -1;
-  if (any_hit) {
-    cudaFuncSetAttribute(k_trace_rays<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_trace_rays<true><<<grid, TRACE_TB, smem, s>>>(sc, rays9, n, work, tri_out, t_out, cap, st);
+  const bool wide = sc.wide != 0;
+  int grid;
+  if (any_hit && wide) {
+    grid = resident_grid(k_trace_rays<true, true>, smem);
+    if (grid > 0) k_trace_rays<true, true><<<grid, TRACE_TB, smem, s>>>(sc, rays9, n, work, tri_out, t_out, cap, st);
+  } else if (any_hit) {
+    grid = resident_grid(k_trace_rays<true, false>, smem);
+    if (grid > 0) k_trace_rays<true, false><<<grid, TRACE_TB, smem, s>>>(sc, rays9, n, work, tri_out, t_out, cap, st);
+  } else if (wide) {
+    grid = resident_grid(k_trace_rays<false, true>, smem);
+    if (grid > 0) k_trace_rays<false, true><<<grid, TRACE_TB, smem, s>>>(sc, rays9, n, work, tri_out, t_out, cap, st);
   } else {
-    cudaFuncSetAttribute(k_trace_rays<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_trace_rays<false><<<grid, TRACE_TB, smem, s>>>(sc, rays9, n, work, tri_out, t_out, cap, st);
+    grid = resident_grid(k_trace_rays<false, false>, smem);
+    if (grid > 0) k_trace_rays<false, false><<<grid, TRACE_TB, smem, s>>>(sc, rays9, n, work, tri_out, t_out, cap, st);
   }
+  if (grid <= 0) return -1;
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -52,9 +52,9 @@ void launch_batch_logic(const BatchJob* jobs, BatchCtl* ctl, const PathState& ps
                         int* out_closest, int* out_any, RoundCounters* rc_out, DevStats* st,
                         unsigned long long* job_done, const int* sorted, const SortCtl* sctl, int grid,
                         cudaStream_t s);
-int launch_batch_trace(bool any_hit, const BatchJob* jobs, const int2* job_pass, const int* queue,
+int launch_batch_trace(bool any_hit, bool wide, const BatchJob* jobs, const int2* job_pass, const int* queue,
                        const int* count, int* work, const float4* ro, const float4* rd, float4* hit, DevStats* st,
                        int stack_cap, int grid_blocks, cudaStream_t s);
-int batch_trace_grid(bool any_hit, int stack_cap);
+int batch_trace_grid(bool any_hit, int stack_cap, bool wide);
 
 }  // namespace yc

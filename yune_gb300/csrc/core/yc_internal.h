@@ -47,7 +47,7 @@ struct RoundCounters {
 // device-wide statistics (yc_stats layout, 64-bit counters)
 struct DevStats {
   unsigned long long rays, primary, extension, shadow, mis, connection, traversed, samples, stack_overflow;
-  unsigned long long ext_rays, ext_nodes, ext_tris, any_rays, any_nodes, any_tris;
+  unsigned long long ext_rays, ext_boxes, ext_tris, any_rays, any_boxes, any_tris;
 };
 
 struct PassParams {
@@ -73,10 +73,14 @@ int launch_trace(const DevScene& sc, bool any_hit, const int* queue, const int* 
                  const float4* ro, const float4* rd, float4* hit, DevStats* st, int grid_blocks,
                  cudaStream_t s);
 void launch_tonemap(const float4* in, float4* out, int n, cudaStream_t s);
+// tail.cu: finish a pass's paths one thread each once at most `threshold` are left
+int tail_capacity(const DevScene& sc, int* grid_out);
+int launch_tail(const PassParams& pp, const PathState& ps, const int* in_closest, const int* in_any,
+                RoundCounters* rc_in, int threshold, DevStats* st, int grid, cudaStream_t s);
 // direct query: rays as 9 floats each
 int launch_trace_rays(const DevScene& sc, bool any_hit, const float* rays9, int n, int* tri_out, float* t_out,
                       int* work, DevStats* st, cudaStream_t s);
-int trace_grid_blocks(bool any_hit, int depth);
+int trace_grid_blocks(bool any_hit, int depth, bool wide);
 int l2_read_gbs(size_t bytes, int iters, cudaStream_t s, double* gbs);
 
 }  // namespace yc

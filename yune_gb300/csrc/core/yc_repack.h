@@ -11,17 +11,18 @@
 namespace yc {
 
 struct Repacked {
-  std::vector<float4> nodes;   // 4 per interior node
+  std::vector<float4> nodes;   // 4 per two-child node, 8 per four-child node
   std::vector<float4> tris;    // 3 per stream slot
   std::vector<float4> shade;   // 4 per original triangle
   int root_link = LINK_NONE;
   int root_test = 0;
-  int depth = 0;
+  int depth = 0;               // stack entries a walk can need
+  int wide = 0;                // 1: four-child nodes
   float4 root_lo{0, 0, 0, 0}, root_hi{0, 0, 0, 0};
 };
 
 // tree_mode: how the interior nodes above the reference leaves are laid out
-enum { TREE_REFERENCE = 0, TREE_SAH_OVER_LEAVES = 1 };
+enum { TREE_REFERENCE = 0, TREE_SAH_OVER_LEAVES = 1, TREE_WIDE4 = 2 };
 
 // Returns 0, or -1 with a message when the node array is not a tree the reference
 // traversal could walk (child indices out of range, vert_len > 10, ...).

@@ -2,7 +2,7 @@
 //
 // One scene in HBM is five read-only arrays, all 16-byte aligned and fetched with
 // 128-bit loads:
-//   nodes   4 x float4 (64 B) per interior node of the reference BVH, holding the boxes
+//   nodes   two-child layout: 4 x float4 (64 B) per interior node, holding the boxes
 //           of its two children (the 32 B a box test reads) and their links:
 //             n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
 //             n1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
@@ -12,6 +12,9 @@
 //           << 4) | triangle count (a reference leaf holds at most 10); LINK_NONE: a
 //           child the reference never queues (vert_len <= 0 and child_idx <= 0,
 //           udpt.cl:316).
+//           four-child layout (wide = 1): 8 x float4 (128 B) per node, the boxes of
+//           its four children as lo.x[4], hi.x[4], lo.y[4], hi.y[4], lo.z[4], hi.z[4],
+//           then the four links (LINK_NONE for an empty slot) and 16 unused bytes.
 //   tris    3 x float4 (48 B) per stream slot, leaves' triangles contiguous:
 //             (v1.xyz, original index), (e1 = v2 - v1, tie-break rank), (e2 = v3 - v1, 0)
 //           with the index and rank as int bits; the rank orders triangles at equal t
@@ -43,7 +46,7 @@ struct DevScene {
   int n_tri;
   int n_mat;
   int root_link;       // link of the reference root node 0
-  int root_pad_;
+  int wide;            // 1: four-child nodes (8 x float4 each), 0: two-child nodes
   int root_test;       // 1: test the root box first (traverseBVH, udpt.cl:295); 0: brute force
   int depth;           // interior levels below the root (stack slots needed)
   int pad_;

@@ -24,11 +24,11 @@ __device__ __forceinline__ void flush_counts(DevStats* st, unsigned rays, const 
   if ((threadIdx.x & 31) == 0) {
     if (ANY) {
       if (r) atomicAdd(&st->any_rays, r);
-      if (nn) atomicAdd(&st->any_nodes, nn);
+      if (nn) atomicAdd(&st->any_boxes, nn);
       if (tt) atomicAdd(&st->any_tris, tt);
     } else {
       if (r) atomicAdd(&st->ext_rays, r);
-      if (nn) atomicAdd(&st->ext_nodes, nn);
+      if (nn) atomicAdd(&st->ext_boxes, nn);
       if (tt) atomicAdd(&st->ext_tris, tt);
     }
     if (overflow) atomicAdd(&st->stack_overflow, overflow);
@@ -40,7 +40,7 @@ constexpr int REFILL_AT = 8;
 
 // The persistent loop shared by the kernels. Src supplies ray e of the work list and the
 // scene it walks (begin) and stores its result (end).
-template <bool ANY, class Src>
+template <bool ANY, bool WIDE, class Src>
 __device__ __forceinline__ void trace_loop(Src& src, int n, int* work, int stack_cap, DevStats* st) {
   extern __shared__ int smem[];
   int* stack = smem + threadIdx.x;
@@ -75,7 +75,7 @@ __device__ __forceinline__ void trace_loop(Src& src, int n, int* work, int stack
     }
     if (e_cur >= 0) {
       bool of = false;
-      bool done = (w.link == LINK_NONE) || walk_step<ANY>(w, stack, TRACE_TB, stack_cap, wc, of);
+      bool done = (w.link == LINK_NONE) || walk_step<ANY, WIDE>(w, stack, TRACE_TB, stack_cap, wc, of);
       if (of) ++overflow;
       if (done) {
         HitOut h;

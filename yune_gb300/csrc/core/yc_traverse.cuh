@@ -1,5 +1,5 @@
 // yc_traverse.cuh -- BVH traversal for sm_103a: while-while depth-first walk over the
-// repacked two-child nodes with a per-thread stack in shared memory.
+// repacked two-child or four-child nodes with a per-thread stack in shared memory.
 //
 // The tests themselves are the reference's, operation for operation, so the accepted
 // triangles and their t are bit-identical to traverseBVH + rayTriangleIntersection
@@ -33,7 +33,8 @@ struct HitOut {
   int tri;   // original triangle index, -1 when nothing closer than tmax
 };
 
-// work done by one walk: two-child nodes fetched and triangles tested
+// work done by walks: child boxes tested (two per two-child node, four per four-child
+// node) and triangles tested
 struct WalkCount {
   unsigned nodes = 0, tris = 0;
 };
@@ -115,115 +116,6 @@ __device__ __forceinline__ bool tri_test(float ox, float oy, float oz, float dx,
 // the best t by more than 2^-10 relative.
 __device__ __forceinline__ float cull_bound(float best) { return best * 1.0009765625f; }
 
-// Walks the scene for one ray. ANY = true stops at the first accepted triangle (shadow
-// rays, udpt.cl:306-308). stack: this thread's column, stride `stride` ints. Returns
-// false when the stack bound was exceeded (the result is then incomplete).
-template <bool ANY>
-__device__ __forceinline__ bool traverse(const DevScene& sc, const RayIn& r, int* stack, int stride, int stack_cap,
-                                         HitOut& out, WalkCount& wc) {
-  const float ox = r.ox, oy = r.oy, oz = r.oz;
-  const float dx = r.dx, dy = r.dy, dz = r.dz;
-  const float ix = __frcp_rn(dx), iy = __frcp_rn(dy), iz = __frcp_rn(dz);
-  const bool exact = isinf(ix) || isinf(iy) || isinf(iz);
-  float best = r.tmax;
-  int best_tri = -1;
-  int best_rank = -1;   // the initial length (a light or the segment end) is never tied
-  float bu = 0.0f, bv = 0.0f;
-  out.tri = -1;
-  out.t = best;
-  out.u = out.v = 0.0f;
-
-  int link = sc.root_link;
-  if (link == LINK_NONE) return true;
-  if (sc.root_test) {
-    float te;
-    const bool h = exact ? box_ref(ox, oy, oz, ix, iy, iz, sc.root_lo.x, sc.root_hi.x, sc.root_lo.y, sc.root_hi.y,
-                                   sc.root_lo.z, sc.root_hi.z, te)
-                         : box_fast(ox, oy, oz, ix, iy, iz, sc.root_lo.x, sc.root_hi.x, sc.root_lo.y,
-                                    sc.root_hi.y, sc.root_lo.z, sc.root_hi.z, te);
-    if (!h) return true;
-  }
-  int sp = 0;
-  bool ok = true;
-  for (;;) {
-    // descend through interior nodes
-    while (link >= 0 && link != LINK_NONE) {
-      const float4* nd = sc.nodes + 4 * (size_t)link;
-      const float4 n0 = __ldg(nd + 0);
-      const float4 n1 = __ldg(nd + 1);
-      const float4 n2 = __ldg(nd + 2);
-      const int2 n3 = __ldg(reinterpret_cast<const int2*>(nd + 3));
-      ++wc.nodes;
-      float t0, t1;
-      bool h0, h1;
-      if (!exact) {
-        h0 = box_fast(ox, oy, oz, ix, iy, iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, t0);
-        h1 = box_fast(ox, oy, oz, ix, iy, iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, t1);
-      } else {
-        h0 = box_ref(ox, oy, oz, ix, iy, iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, t0);
-        h1 = box_ref(ox, oy, oz, ix, iy, iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, t1);
-      }
-      const float cb = cull_bound(best);
-      h0 = h0 && n3.x != LINK_NONE && !(t0 > cb);
-      h1 = h1 && n3.y != LINK_NONE && !(t1 > cb);
-      if (h0 && h1) {
-        const bool swap = t1 < t0;
-        const int near_l = swap ? n3.y : n3.x, far_l = swap ? n3.x : n3.y;
-        const float far_t = swap ? t0 : t1;
-        if (sp >= stack_cap) { ok = false; link = LINK_NONE; break; }
-        stack[(2 * sp + 0) * stride] = far_l;
-        stack[(2 * sp + 1) * stride] = __float_as_int(far_t);
-        ++sp;
-        link = near_l;
-      } else if (h0) {
-        link = n3.x;
-      } else if (h1) {
-        link = n3.y;
-      } else {
-        link = LINK_NONE;
-        break;
-      }
-    }
-    // leaf: ~link = (first slot << 4) | count
-    if (link != LINK_NONE) {
-      const int enc = ~link;
-      const int count = enc & 15;
-      const float4* tp = sc.tris + 3 * (size_t)(enc >> 4);
-      for (int k = 0; k < count; ++k) {
-        ++wc.tris;
-        const float4 a = __ldg(tp + 3 * k + 0);
-        const float4 b = __ldg(tp + 3 * k + 1);
-        const float4 c = __ldg(tp + 3 * k + 2);
-        TriHit th;
-        if (tri_test(ox, oy, oz, dx, dy, dz, a, b, c, best, best_rank, th)) {
-          best = th.t;
-          bu = th.u;
-          bv = th.v;
-          best_tri = __float_as_int(a.w);
-          best_rank = __float_as_int(b.w);
-          if (ANY) {
-            out.t = best; out.u = bu; out.v = bv; out.tri = best_tri;
-            return ok;
-          }
-        }
-      }
-    }
-    // pop the next subtree whose entry is still within reach
-    link = LINK_NONE;
-    while (sp > 0) {
-      --sp;
-      const float te = __int_as_float(stack[(2 * sp + 1) * stride]);
-      if (!(te > cull_bound(best))) { link = stack[(2 * sp) * stride]; break; }
-    }
-    if (link == LINK_NONE) break;
-  }
-  out.t = best;
-  out.u = bu;
-  out.v = bv;
-  out.tri = best_tri;
-  return ok;
-}
-
 // ---- resumable walk for the persistent kernels ----
 // The state of one ray's walk, so a warp can run its lanes' walks step by step and hand
 // a lane a new ray as soon as its walk ends (the replenishing persistent warps of Aila
@@ -259,12 +151,47 @@ __device__ __forceinline__ void walk_begin(const DevScene& sc, const RayIn& r, W
   }
 }
 
-// One trip of the walk: descend to a leaf, test its triangles, pop the next subtree.
-// Returns true when the walk has ended (w.link == LINK_NONE); `overflow` is set when
-// the stack bound was reached (the walk then ends early).
+// Triangles of one leaf (the reference's vert_list run, yc_scene.h); returns true when
+// an any-hit walk has found its hit.
 template <bool ANY>
-__device__ __forceinline__ bool walk_step(Walk& w, int* stack, int stride, int stack_cap, WalkCount& wc,
-                                          bool& overflow) {
+__device__ __forceinline__ bool walk_leaf(Walk& w, int link, WalkCount& wc) {
+  const int enc = ~link;
+  const int count = enc & 15;
+  const float4* tp = w.tris + 3 * (size_t)(enc >> 4);
+  for (int k = 0; k < count; ++k) {
+    ++wc.tris;
+    const float4 a = __ldg(tp + 3 * k + 0);
+    const float4 b = __ldg(tp + 3 * k + 1);
+    const float4 c = __ldg(tp + 3 * k + 2);
+    TriHit th;
+    if (tri_test(w.ox, w.oy, w.oz, w.dx, w.dy, w.dz, a, b, c, w.best, w.best_rank, th)) {
+      w.best = th.t;
+      w.bu = th.u;
+      w.bv = th.v;
+      w.best_tri = __float_as_int(a.w);
+      w.best_rank = __float_as_int(b.w);
+      if (ANY) return true;
+    }
+  }
+  return false;
+}
+
+// pops the next subtree whose entry is still within reach (LINK_NONE: the walk ends)
+__device__ __forceinline__ int walk_pop(Walk& w, const int* stack, int stride) {
+  while (w.sp > 0) {
+    --w.sp;
+    const float te = __int_as_float(stack[(2 * w.sp + 1) * stride]);
+    if (!(te > cull_bound(w.best))) return stack[(2 * w.sp) * stride];
+  }
+  return LINK_NONE;
+}
+
+// One trip of the walk over two-child nodes: descend to a leaf, test its triangles,
+// pop the next subtree. Returns true when the walk has ended (w.link == LINK_NONE);
+// `overflow` is set when the stack bound was reached (the walk then ends early).
+template <bool ANY>
+__device__ __forceinline__ bool walk_step2(Walk& w, int* stack, int stride, int stack_cap, WalkCount& wc,
+                                           bool& overflow) {
   int link = w.link;
   while (link >= 0 && link != LINK_NONE) {
     const float4* nd = w.nodes + 4 * (size_t)link;
@@ -272,7 +199,7 @@ __device__ __forceinline__ bool walk_step(Walk& w, int* stack, int stride, int s
     const float4 n1 = __ldg(nd + 1);
     const float4 n2 = __ldg(nd + 2);
     const int2 n3 = __ldg(reinterpret_cast<const int2*>(nd + 3));
-    ++wc.nodes;
+    wc.nodes += 2;
     float t0, t1;
     bool h0, h1;
     if (!w.exact) {
@@ -303,34 +230,79 @@ __device__ __forceinline__ bool walk_step(Walk& w, int* stack, int stride, int s
       break;
     }
   }
-  if (link != LINK_NONE) {
-    const int enc = ~link;
-    const int count = enc & 15;
-    const float4* tp = w.tris + 3 * (size_t)(enc >> 4);
-    for (int k = 0; k < count; ++k) {
-      ++wc.tris;
-      const float4 a = __ldg(tp + 3 * k + 0);
-      const float4 b = __ldg(tp + 3 * k + 1);
-      const float4 c = __ldg(tp + 3 * k + 2);
-      TriHit th;
-      if (tri_test(w.ox, w.oy, w.oz, w.dx, w.dy, w.dz, a, b, c, w.best, w.best_rank, th)) {
-        w.best = th.t;
-        w.bu = th.u;
-        w.bv = th.v;
-        w.best_tri = __float_as_int(a.w);
-        w.best_rank = __float_as_int(b.w);
-        if (ANY) { w.sp = 0; w.link = LINK_NONE; return true; }
+  if (link != LINK_NONE && walk_leaf<ANY>(w, link, wc)) { w.sp = 0; w.link = LINK_NONE; return true; }
+  w.link = walk_pop(w, stack, stride);
+  return w.link == LINK_NONE;
+}
+
+// (t, link) compare-exchange: the smaller entry distance first
+__device__ __forceinline__ void cx(float& ta, int& la, float& tb, int& lb) {
+  if (tb < ta) {
+    const float t = ta; ta = tb; tb = t;
+    const int l = la; la = lb; lb = l;
+  }
+}
+
+// The same trip over four-child nodes (yc_scene.h, wide layout): the four child boxes
+// are tested with the reference's slab arithmetic, the hits sorted by entry distance,
+// the nearest visited next and the others pushed farthest first.
+template <bool ANY>
+__device__ __forceinline__ bool walk_step4(Walk& w, int* stack, int stride, int stack_cap, WalkCount& wc,
+                                           bool& overflow) {
+  const float INF = __int_as_float(0x7f800000);
+  int link = w.link;
+  while (link >= 0 && link != LINK_NONE) {
+    const float4* nd = w.nodes + 8 * (size_t)link;
+    const float4 lx = __ldg(nd + 0), hx = __ldg(nd + 1);
+    const float4 ly = __ldg(nd + 2), hy = __ldg(nd + 3);
+    const float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5);
+    const int4 ln = __ldg(reinterpret_cast<const int4*>(nd + 6));
+    wc.nodes += 4;
+    const float cb = cull_bound(w.best);
+    float t[4];
+    int l[4];
+    const float clx[4] = {lx.x, lx.y, lx.z, lx.w}, chx[4] = {hx.x, hx.y, hx.z, hx.w};
+    const float cly[4] = {ly.x, ly.y, ly.z, ly.w}, chy[4] = {hy.x, hy.y, hy.z, hy.w};
+    const float clz[4] = {lz.x, lz.y, lz.z, lz.w}, chz[4] = {hz.x, hz.y, hz.z, hz.w};
+    const int cl[4] = {ln.x, ln.y, ln.z, ln.w};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      float te;
+      bool h = !w.exact ? box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, clx[c], chx[c], cly[c], chy[c], clz[c], chz[c], te)
+                        : box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, clx[c], chx[c], cly[c], chy[c], clz[c], chz[c], te);
+      h = h && cl[c] != LINK_NONE && !(te > cb);
+      t[c] = h ? te : INF;
+      l[c] = h ? cl[c] : LINK_NONE;
+    }
+    // sorting network for four entries; misses (t = inf, LINK_NONE) end up last
+    cx(t[0], l[0], t[1], l[1]);
+    cx(t[2], l[2], t[3], l[3]);
+    cx(t[0], l[0], t[2], l[2]);
+    cx(t[1], l[1], t[3], l[3]);
+    cx(t[1], l[1], t[2], l[2]);
+    if (l[0] == LINK_NONE) { link = LINK_NONE; break; }
+    const int extra = (l[1] != LINK_NONE) + (l[2] != LINK_NONE) + (l[3] != LINK_NONE);
+    if (w.sp + extra > stack_cap) { overflow = true; w.sp = 0; link = LINK_NONE; break; }
+#pragma unroll
+    for (int c = 3; c >= 1; --c) {
+      if (l[c] != LINK_NONE) {
+        stack[(2 * w.sp + 0) * stride] = l[c];
+        stack[(2 * w.sp + 1) * stride] = __float_as_int(t[c]);
+        ++w.sp;
       }
     }
+    link = l[0];
   }
-  link = LINK_NONE;
-  while (w.sp > 0) {
-    --w.sp;
-    const float te = __int_as_float(stack[(2 * w.sp + 1) * stride]);
-    if (!(te > cull_bound(w.best))) { link = stack[(2 * w.sp) * stride]; break; }
-  }
-  w.link = link;
-  return link == LINK_NONE;
+  if (link != LINK_NONE && walk_leaf<ANY>(w, link, wc)) { w.sp = 0; w.link = LINK_NONE; return true; }
+  w.link = walk_pop(w, stack, stride);
+  return w.link == LINK_NONE;
+}
+
+template <bool ANY, bool WIDE>
+__device__ __forceinline__ bool walk_step(Walk& w, int* stack, int stride, int stack_cap, WalkCount& wc,
+                                          bool& overflow) {
+  if (WIDE) return walk_step4<ANY>(w, stack, stride, stack_cap, wc, overflow);
+  return walk_step2<ANY>(w, stack, stride, stack_cap, wc, overflow);
 }
 
 }  // namespace yc

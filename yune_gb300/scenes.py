@@ -208,3 +208,19 @@ def mt19937(seed, n):
         y ^= y >> 18
         out.append(y & 0xFFFFFFFF)
     return np.array(out, dtype=np.uint32)
+
+
+def box_rays(n, seed=0):
+    """n incoherent rays as 9 float32 each (origin xyz 1, direction xyz 0, length inf):
+    origins uniform inside the Cornell box, directions uniform on the sphere (numpy's
+    PCG64 stream of `seed`)."""
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(-0.49, 0.49, size=(n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    r = np.zeros((n, 9), np.float32)
+    r[:, 0:3] = o
+    r[:, 3] = 1.0
+    r[:, 4:7] = d
+    r[:, 8] = np.inf
+    return r
