@@ -1,4 +1,4 @@
-"""Benchmark of the path-tracing core on the plain per-frame path.
+"""Benchmark of the path-tracing core.
 
 Workload (one step = one render pass = one sample per pixel over the frame, the
 per-pass contract of src/RendererCore.cpp:248-469): the glass-icosphere Cornell box
@@ -6,21 +6,28 @@ per-pass contract of src/RendererCore.cpp:248-469): the glass-icosphere Cornell 
 3, at most 16 bounces; synthetic seeded scene, per-pass seeds from mt19937(0).
 
 Printed (one JSON line on rank 0):
-  value        Mrays/s over the timed passes: every traceRay-equivalent query (primary,
-               extension, NEE shadow, MIS) / device time of the passes (CUDA events on the
-               context stream), inputs resident in HBM, L2 flushed between passes
-  e2e          the same metric through the C-ABI with host buffers: per pass the camera
-               block goes host -> device and the tonemapped frame comes back
+  value        Mrays/s of the whole job: the K timed passes rendered as one job of the
+               batch engine (every pixel's passes in order in one path slot, so the image
+               is bit-identical to K yc_render_pass calls, checked in the line): every
+               traceRay-equivalent query (primary, extension, NEE shadow, MIS) / device
+               time (CUDA events on the context stream), inputs resident in HBM
+  per_pass     the same passes through yc_render_pass, one call per pass, L2 flushed
+               before each (the drop-in call of RendererCore)
+  e2e          the metric through the C-ABI with host buffers: per step the camera and
+               the pass seeds go host -> device and the tonemapped frame comes back
+               (engine, E passes per step); e2e_per_pass does it one pass per step
   roofline     the extend (closest-hit) kernel: algorithmic bytes (32 B per box test,
-               48 B per triangle test, 52 B of ray/hit records per ray) / its event time,
-               against the measured L2 read bandwidth (the node + triangle set, ~9 MB,
-               stays in L2); hbm_frac against MEASURED_PEAKS.json's HBM copy bandwidth
+               48 B per triangle test, 84 B of ray/hit records per ray) / its event time,
+               against the measured L2 read bandwidth (the node + triangle set stays in
+               L2); hbm_frac against MEASURED_PEAKS.json's HBM copy bandwidth
   cpu_baseline the reference kernel source compiled as C++ (oracle/_ref), all host
                threads, on a band of rows of the same frame
 `--impl reference` times that CPU reference alone on the same workload.
 With torchrun (N > 1) every rank renders its own replica (the work does not exchange
 data; multi-GPU is replicas only) and the value is the sum of the ranks' rays over the
 slowest rank's time.
+Other modes: --config c2 (mixed batch vs the plain loop), --config c3 (serving),
+--quality (RMSE against the FP64 references), --trace-bench N (traversal alone).
 """
 import argparse
 import json
@@ -47,6 +54,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c1")
     ap.add_argument("--e2e-steps", type=int, default=8)
+    ap.add_argument("--e2e-passes", type=int, default=8, help="passes per e2e step through the engine")
+    ap.add_argument("--groups", type=int, default=2, help="slot groups of the engine (c1 whole-job run)")
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu", action="store_true")
     # batched (c2) and served (c3) comparisons against the plain per-pass loop
@@ -211,105 +220,183 @@ def run_reference(args, rank, ws, dist):
     print(json.dumps(line))
 
 
+def _reduce(dist, t_s, rays):
+    """max of the ranks' times, sum of their rays (replicas)"""
+    if not dist:
+        return t_s, rays
+    import torch
+    mx = torch.tensor([t_s], dtype=torch.float64)
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    sm = torch.tensor([float(rays)], dtype=torch.float64)
+    dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+    return mx.item(), sm.item()
+
+
+def _extend_roofline(st, boxes_key, tris_key, rays_key, ms, l2, pk, pk_kind, kernel):
+    nbytes = 32.0 * st[boxes_key] + 48.0 * st[tris_key] + 84.0 * st[rays_key]
+    achieved = nbytes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+    return {"kernel": kernel, "bound": "l2", "achieved": achieved, "peak": l2, "unit": "GB/s",
+            "frac": achieved / l2 if l2 else None, "traffic": None,
+            "peak_source": "measured L2 read bandwidth (yc_measure_l2_gbs, 48 MB x 20 sweeps)",
+            "hbm_peak": pk.get("hbm_gbs"), "hbm_frac": achieved / pk.get("hbm_gbs", 1.0), "hbm_peak_source": pk_kind,
+            "bytes_per_ray": nbytes / max(1, st[rays_key]),
+            "box_tests_per_ray": st[boxes_key] / max(1, st[rays_key]),
+            "tri_tests_per_ray": st[tris_key] / max(1, st[rays_key])}
+
+
 def run_ours(args, rank, local, ws, dist):
+    """C1 on one GPU (a replica per rank under torchrun).
+
+    A. per-pass drop-in path: W warm-up passes, then K timed passes, one yc_render_pass
+       each (L2 flushed before each), per-kernel CUDA events;
+    B. the whole job through the batch engine: the same frame, W warm-up passes as one
+       job, then the K timed passes as one job (the value; path state of the pool is far
+       larger than L2), and its image compared bit for bit with A's;
+    C. a profiled copy of B without the graph (per-kernel events: split and roofline);
+    D. e2e through the C-ABI with host buffers: per step the camera and the pass seeds go
+       host -> device, the step's passes render, and the tonemapped frame comes back;
+       once through the engine (E passes per step) and once per pass (yc_render_pass).
+    """
     from yune_gb300 import quality, scenes
+    from yune_gb300.batch import Batch
     from yune_gb300.core import Renderer
     scene = scene_for(args.config)
-    seeds = scenes.pass_seeds(0, args.warmup + args.steps + args.e2e_steps)
+    K, Wm, E = args.steps, args.warmup, args.e2e_passes
+    seeds = scenes.pass_seeds(0, Wm + 2 * K + args.e2e_steps * (E + 1))
     W, H = scene.width, scene.height
     r = Renderer(local)
     r.set_tree_mode(args.tree)
     r.set_tail_paths(args.tail)
     sid = r.upload(scene)
     r.set_camera(scene.cam)
-    aid = r.alloc_accum(W, H)
     l2 = r.measure_l2_gbs(48 << 20, 20)
-    # warm-up
-    for k in range(args.warmup):
+    pk, pk_kind = peaks()
+
+    # A. per pass
+    aid = r.alloc_accum(W, H)
+    for k in range(Wm):
         r.render(sid, aid, seeds[k], reset=1 if k == 0 else 0, cfg=scene.cfg)
     r.synchronize()
     r.reset_stats()
     r.set_profiling(True)
+    pp_ms = 0.0
+    for k in range(K):
+        r.flush_l2(256 << 20)
+        r.render(sid, aid, seeds[Wm + k], reset=0, cfg=scene.cfg)
+        pp_ms += r.last_pass_ms()
+    r.synchronize()
+    st_pp = r.stats()
+    kt_pp = r.kernel_times()
+    r.set_profiling(False)
+    img_pp = r.read_accum(aid)
+
+    # B. the whole job through the engine
+    cap = r.scene_depth(sid) + 2
+    pool = 1 << 16
+    while pool < W * H and pool < (1 << 22):
+        pool <<= 1
+    shape = dict(pool_paths=pool, rounds_per_launch=8, logic_blocks_per_sm=2, sort_threshold=1 << 16,
+                 groups=args.groups)
+    aid_e = r.alloc_accum(W, H)
+    b = Batch(r, stack_cap=cap, **shape)
+    b.add_job(sid, aid_e, scene.cam, seeds[:Wm], scene.cfg, reset_first=1)
+    b.run()
+    b.add_job(sid, aid_e, scene.cam, seeds[Wm:Wm + K], scene.cfg, reset_first=0)
+    r.flush_l2(256 << 20)
+    r.synchronize()
+    r.reset_stats()
     if dist:
         dist.barrier()
-    ms_total = 0.0
     with Clocks(local) as clk:
-        for k in range(args.steps):
-            r.flush_l2(256 << 20)
-            r.render(sid, aid, seeds[args.warmup + k], reset=0, cfg=scene.cfg)
-            ms_total += r.last_pass_ms()
-    r.synchronize()
-    st = r.stats()
-    kt = r.kernel_times()
+        b.run()
+    en_ms = r.last_pass_ms()
+    st_en = r.stats()
+    img_en = r.read_accum(aid_e)
+    same = bool(np.array_equal(img_en.view(np.int32), img_pp.view(np.int32)))
+    b.close()
+
+    # C. profiled copy of B (no graph): kernel split and the extend kernel's roofline
+    aid_p = r.alloc_accum(W, H)
+    bp = Batch(r, stack_cap=cap, use_graph=False, **shape)
+    bp.add_job(sid, aid_p, scene.cam, seeds[Wm + K:Wm + 2 * K], scene.cfg, reset_first=1)
+    r.flush_l2(256 << 20)
+    r.reset_stats()
+    r.set_profiling(True)
+    bp.run()
+    kt_en = r.kernel_times()
+    st_enp = r.stats()
     r.set_profiling(False)
-    # e2e through the C-ABI with host buffers: camera in, tonemapped frame out
+    bp.close()
+    r.free_accum(aid_p)
+
+    # D. e2e with host buffers
+    base = Wm + 2 * K
     ldr = None
+    be = Batch(r, stack_cap=cap, **shape)
+    r.reset_stats()
+    t0 = time.perf_counter()
+    for k in range(args.e2e_steps):
+        be.add_job(sid, aid_e, scene.cam, seeds[base + k * E:base + (k + 1) * E], scene.cfg, reset_first=0)
+        be.run()
+        ldr = r.tonemap(aid_e)
+    e2e_s = time.perf_counter() - t0
+    e2e_rays = r.stats()["rays"]
+    be.close()
+    base += args.e2e_steps * E
+    r.reset_stats()
     t0 = time.perf_counter()
     for k in range(args.e2e_steps):
         r.set_camera(scene.cam)
-        r.render(sid, aid, seeds[args.warmup + args.steps + k], reset=0, cfg=scene.cfg)
+        r.render(sid, aid, seeds[base + k], reset=0, cfg=scene.cfg)
         ldr = r.tonemap(aid)
-    e2e_s = time.perf_counter() - t0
-    e2e_stats = r.stats()
-    e2e_rays = e2e_stats["rays"] - st["rays"]
-    img = r.read_accum(aid)
-    rays = st["rays"]
-    t_s = ms_total / 1e3
-    if dist:
-        import torch
-        tt = torch.tensor([t_s, float(rays), e2e_s, float(e2e_rays)], dtype=torch.float64)
-        mx = tt.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        sm = tt.clone()
-        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
-        t_s, e2e_s = mx[0].item(), mx[2].item()
-        rays, e2e_rays = sm[1].item(), sm[3].item()
+    e2e_pp_s = time.perf_counter() - t0
+    e2e_pp_rays = r.stats()["rays"]
+
+    t_s, rays = _reduce(dist, en_ms / 1e3, st_en["rays"])
+    pp_s, pp_rays = _reduce(dist, pp_ms / 1e3, st_pp["rays"])
+    e2e_s, e2e_rays = _reduce(dist, e2e_s, e2e_rays)
+    e2e_pp_s, e2e_pp_rays = _reduce(dist, e2e_pp_s, e2e_pp_rays)
     if rank != 0:
         r.close()
         return
-    pk, pk_kind = peaks()
-    ext_bytes = 32.0 * st["ext_boxes"] + 48.0 * st["ext_tris"] + 32.0 * st["ext_rays"] + 52.0 * st["ext_rays"]
-    ext_ms = kt["extend_ms"]
-    achieved = ext_bytes / (ext_ms / 1e3) / 1e9 if ext_ms > 0 else 0.0
-    launches = int(kt["raygen_launches"] + kt["extend_launches"] + kt["occlusion_launches"] + kt["logic_launches"]
-                   + kt["tail_launches"])
-    traffic = None
-    prof_file = os.path.join(ROOT, "profiles", "extend_traffic.json")
-    if os.path.exists(prof_file):
-        with open(prof_file) as f:
-            tr = json.load(f)
-        if tr.get("config") == args.config and kt["extend_launches"]:
-            traffic = tr.get("dram_bytes_per_launch")
-    samples = st["samples"]
+    launches = int(kt_en["raygen_launches"] + kt_en["extend_launches"] + kt_en["occlusion_launches"]
+                   + kt_en["logic_launches"] + kt_en["sort_launches"])
     line = {
-        "metric": METRIC, "value": rays / t_s / 1e6, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": rays / t_s / 1e6, "unit": METRIC, "n_gpus": ws, "steps": K,
+        "warmup": Wm, "ms_per_step": en_ms / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded procedural scene)",
         "config": {"workload": "%s: glass icosphere Cornell box, %d tris, %dx%d, 1 spp per step, NEE+MIS, RR after "
-                               "bounce 3, max depth %d" % (args.config, scene.n_tri, W, H, scene.cfg["max_depth"]),
-                   "spp_total": scene.spp, "l2": "flushed between timed steps (256 MB write)",
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
-        "samples_per_s": samples / t_s * (ws if dist else 1),
-        "rays_per_sample": st["rays"] / max(1, samples),
-        "traversed_rays": st["traversed"],
+                               "bounce 3, max depth %d; the K steps rendered as one job of K passes through the "
+                               "batch engine" % (args.config, scene.n_tri, W, H, scene.cfg["max_depth"]),
+                   "spp_total": scene.spp, "tree_mode": args.tree,
+                   "l2": "L2 flushed before the timed job; path state of %d slots (%d MB) is larger than L2"
+                         % (pool, pool * 224 >> 20),
+                   "engine_shape": shape, "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "samples_per_s": st_en["samples"] * (ws if dist else 1) / t_s,
+        "rays_per_sample": st_en["rays"] / max(1, st_en["samples"]),
         "gpu_launches": launches,
-        "kernel_ms": {"raygen": kt["raygen_ms"], "extend": kt["extend_ms"], "occlusion": kt["occlusion_ms"],
-                      "logic": kt["logic_ms"], "tail": kt["tail_ms"], "rounds": kt["rounds"]},
-        "roofline": {"kernel": "k_trace_paths<false> (extend)", "bound": "l2", "achieved": achieved,
-                     "peak": l2, "unit": "GB/s", "frac": achieved / l2 if l2 else None, "traffic": traffic,
-                     "peak_source": "measured L2 read bandwidth (yc_measure_l2_gbs, 48 MB x 20 sweeps)",
-                     "hbm_peak": pk.get("hbm_gbs"), "hbm_frac": achieved / pk.get("hbm_gbs", 1.0),
-                     "hbm_peak_source": pk_kind,
-                     "bytes_per_ray": ext_bytes / max(1, st["ext_rays"]),
-                     "box_tests_per_ray": st["ext_boxes"] / max(1, st["ext_rays"]),
-                     "tri_tests_per_ray": st["ext_tris"] / max(1, st["ext_rays"])},
-        "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else 0.0, "unit": METRIC,
-                "h2d_bytes_per_step": 80 + 4, "d2h_bytes_per_step": W * H * 16,
-                "steps": args.e2e_steps},
+        "engine_equal_to_per_pass": same,
+        "kernel_ms": {"fill": kt_en["raygen_ms"], "extend": kt_en["extend_ms"], "occlusion": kt_en["occlusion_ms"],
+                      "sort": kt_en["sort_ms"], "logic": kt_en["logic_ms"], "rounds": kt_en["rounds"]},
+        "roofline": _extend_roofline(st_enp, "ext_boxes", "ext_tris", "ext_rays", kt_en["extend_ms"], l2, pk, pk_kind,
+                                     "k_batch_trace<closest> (extend)"),
+        "per_pass": {"value": pp_rays / pp_s / 1e6, "ms_per_step": pp_ms / K, "unit": METRIC,
+                     "note": "yc_render_pass per pass (the drop-in call), L2 flushed before each pass",
+                     "kernel_ms": {"raygen": kt_pp["raygen_ms"], "extend": kt_pp["extend_ms"],
+                                   "occlusion": kt_pp["occlusion_ms"], "logic": kt_pp["logic_ms"],
+                                   "tail": kt_pp["tail_ms"], "rounds": kt_pp["rounds"]},
+                     "roofline": _extend_roofline(st_pp, "ext_boxes", "ext_tris", "ext_rays", kt_pp["extend_ms"], l2,
+                                                  pk, pk_kind, "k_trace_paths<closest> (extend)")},
+        "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else 0.0, "unit": METRIC, "passes_per_step": E,
+                "h2d_bytes_per_step": 80 + 4 * E, "d2h_bytes_per_step": W * H * 16, "steps": args.e2e_steps,
+                "path": "yc_batch_add_job + yc_batch_run + yc_tonemap to host"},
+        "e2e_per_pass": {"value": e2e_pp_rays / e2e_pp_s / 1e6 if e2e_pp_s > 0 else 0.0, "unit": METRIC,
+                         "h2d_bytes_per_step": 80 + 4, "d2h_bytes_per_step": W * H * 16, "steps": args.e2e_steps,
+                         "path": "yc_set_camera + yc_render_pass + yc_tonemap to host"},
         "clocks": clk.summary(),
-        "image_error": quality.report(img, args.config, int(img[0, 0, 3])),
-        "stack_overflow": st["stack_overflow"],
-        "image_mean": float(np.nanmean(img[..., :3])),
+        "image_error": quality.report(img_en, args.config, int(img_en[0, 0, 3])),
+        "stack_overflow": int(st_en["stack_overflow"] + st_pp["stack_overflow"]),
+        "image_mean": float(np.nanmean(img_en[..., :3])),
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_reference(scene, seeds, args.cpu_seconds)

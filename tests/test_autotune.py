@@ -25,7 +25,7 @@ def test_coordinate_search_finds_the_separable_optimum(monkeypatch):
     monkeypatch.setattr(autotune, "_calibrate", clock)
     r = _FakeRenderer()
     best, trials = autotune.tune(r, [(0, None, [1], None)] * 3, [(1920, 1080)] * 3)
-    assert best == autotune.BatchShape(1 << 20, 16, 2, 0)
+    assert best == autotune.BatchShape(1 << 20, 16, 2, 0, 2)
     assert len(trials) == len(seen) and r.live == 0   # scratch accumulators released
 
 

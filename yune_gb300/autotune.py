@@ -1,14 +1,15 @@
 """Autotuner for the batch engine's launch shape.
 
-The batch engine (yc_batch_*) has four free parameters that change speed but never
+The batch engine (yc_batch_*) has five free parameters that change speed but never
 results: the number of path slots in flight (the wavefront size), the rounds captured
-in one CUDA graph launch, the logic kernel's blocks per SM, and the queue size from which
-the shade queue is sorted by path phase and material class (0: never). The best values depend
+in one CUDA graph launch, the logic kernel's blocks per SM, the queue size from which
+the shade queue is sorted by path phase and material class (0: never), and the number
+of slot groups whose rounds run concurrently. The best values depend
 on the job mix (total pixels, scene sizes, path lengths), so the tuner times candidate
 shapes on a calibration run of the mix itself: every job's first pass, into scratch
 accumulators, with the engine's own CUDA-event clock (yc_last_pass_ms). It searches one
-parameter at a time (pool size, rounds per launch, logic blocks, sort threshold) from
-the engine defaults, keeping the best value of each before moving on.
+parameter at a time (pool size, rounds per launch, logic blocks, sort threshold,
+groups) from the engine defaults, keeping the best value of each before moving on.
 """
 import time
 from dataclasses import dataclass
@@ -20,6 +21,7 @@ POOLS = (1 << 19, 1 << 20, 1 << 21, 1 << 22)
 ROUNDS = (4, 8, 16)
 LOGIC_BLOCKS = (2, 4, 8)
 SORT = (1 << 16, 1 << 18)
+GROUPS = (1, 2, 4)
 
 
 @dataclass
@@ -28,10 +30,12 @@ class BatchShape:
     rounds_per_launch: int = 8
     logic_blocks_per_sm: int = 4
     sort_threshold: int = 0
+    groups: int = 2
 
     def kwargs(self):
         return dict(pool_paths=self.pool_paths, rounds_per_launch=self.rounds_per_launch,
-                    logic_blocks_per_sm=self.logic_blocks_per_sm, sort_threshold=self.sort_threshold)
+                    logic_blocks_per_sm=self.logic_blocks_per_sm, sort_threshold=self.sort_threshold,
+                    groups=self.groups)
 
 
 def _calibrate(renderer, jobs, shape, stack_cap, accs):
@@ -59,7 +63,8 @@ def tune(renderer, jobs, sizes, stack_cap=0, log=None):
         best_ms = _calibrate(renderer, jobs, best, stack_cap, accs)
         trials.append((BatchShape(**best.kwargs()), best_ms))
         for field, values in (("pool_paths", POOLS), ("rounds_per_launch", ROUNDS),
-                              ("logic_blocks_per_sm", LOGIC_BLOCKS), ("sort_threshold", SORT)):
+                              ("logic_blocks_per_sm", LOGIC_BLOCKS), ("sort_threshold", SORT),
+                              ("groups", GROUPS)):
             for v in values:
                 if v == getattr(best, field):
                     continue

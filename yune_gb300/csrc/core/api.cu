@@ -85,6 +85,9 @@ struct yc_ctx {
   std::vector<yc_batch*> batches;   // owned: destroyed with the context
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // the any-hit trace of a round runs on side_stream beside the closest-hit trace
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::map<int, std::unique_ptr<Scene>> scenes;
   std::map<int, std::unique_ptr<Accum>> accums;
   int next_scene = 1, next_accum = 1;
@@ -283,6 +286,15 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     yc::RoundCounters* rin = rc + cur;
     yc::RoundCounters* rout = rc + (1 - cur);
     int e1, e2;
+    // the two traces of a round are independent: the any-hit one runs on the side stream
+    // so that each fills the SMs the other's last rays leave idle (sequential when
+    // profiling, so each kernel's events time it alone)
+    const bool overlap = !c->profile;
+    cudaStream_t s_any = overlap ? c->side_stream : c->stream;
+    if (overlap) {
+      YC_CUDA(cudaEventRecord(c->ev_fork, c->stream));
+      YC_CUDA(cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
+    }
     {
       KTimer kt(c, K_EXTEND);
       e1 = yc::launch_trace(sc->dev, false, in_c, &rin->n_closest, &rin->work_closest, ps.ro, ps.rd, ps.hit,
@@ -292,9 +304,13 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     {
       KTimer kt(c, K_OCCL);
       e2 = yc::launch_trace(sc->dev, true, in_a, &rin->n_any, &rin->work_any, ps.ro, ps.rd, ps.hit, c->stats.p,
-                            grid_a, c->stream);
+                            grid_a, s_any);
     }
     if (e2) return fail(YC_E_LAUNCH, std::string("occlusion kernel: ") + cudaGetErrorString(cudaGetLastError()));
+    if (overlap) {
+      YC_CUDA(cudaEventRecord(c->ev_join, c->side_stream));
+      YC_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+    }
     YC_CUDA(cudaMemsetAsync(rout, 0, sizeof(yc::RoundCounters), c->stream));
     {
       KTimer kt(c, K_LOGIC);
@@ -338,6 +354,9 @@ int yc_create(int device, yc_ctx** out) {
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = c->rc.alloc(2);
   if (e == cudaSuccess) e = c->stats.alloc(1);
   if (e == cudaSuccess) e = cudaMallocHost(&c->rc_host, sizeof(yc::RoundCounters));
@@ -366,6 +385,12 @@ int yc_destroy(yc_ctx* c) {
   if (c->rc_host) cudaFreeHost(c->rc_host);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->side_stream) {
+    cudaStreamSynchronize(c->side_stream);
+    cudaStreamDestroy(c->side_stream);
+  }
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return YC_OK;
@@ -733,21 +758,42 @@ int yc_last_pass_ms(yc_ctx* c, float* ms) {
 
 // ---------------------------------------------------------------------------------------
 // batch and serving engine (engine.cu)
-struct yc_batch {
-  yc_ctx* ctx = nullptr;
-  yc_batch_cfg cfg{};
-  int pool = 0;
-  DevBuf<int4> misc;
-  DevBuf<float4> f4bufs[12];
-  DevBuf<int2> job_pass;
+// One slot group: a contiguous range of the pool's slots with its own free stack,
+// queues, counters and streams (the any-hit trace of a round runs on `side`).
+struct BatchGroup {
+  int first = 0, count = 0;
   DevBuf<int> free_stack;
   DevBuf<int> q[4];
   DevBuf<int> sort_keys, sorted;
   DevBuf<yc::SortCtl> sctl;
   DevBuf<yc::RoundCounters> rc;
   DevBuf<yc::BatchCtl> ctl;
+  cudaStream_t main = nullptr, side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_done = nullptr;
+  yc::BatchCtl* ctl_host = nullptr;         // pinned readback
+  yc::RoundCounters* rc_host = nullptr;
+  ~BatchGroup() {
+    if (main) { cudaStreamSynchronize(main); cudaStreamDestroy(main); }
+    if (side) { cudaStreamSynchronize(side); cudaStreamDestroy(side); }
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (ev_done) cudaEventDestroy(ev_done);
+    if (ctl_host) cudaFreeHost(ctl_host);
+    if (rc_host) cudaFreeHost(rc_host);
+  }
+};
+
+struct yc_batch {
+  yc_ctx* ctx = nullptr;
+  yc_batch_cfg cfg{};
+  DevBuf<int4> misc;
+  DevBuf<float4> f4bufs[12];
+  DevBuf<int2> job_pass;
+  DevBuf<yc::BatchTasks> tasks;
   DevBuf<yc::BatchJob> jobs;
   DevBuf<unsigned long long> job_done;
+  std::vector<std::unique_ptr<BatchGroup>> groups;
+  cudaEvent_t ev_start = nullptr;
   std::vector<std::unique_ptr<DevBuf<uint32_t>>> seeds;
   std::vector<yc::BatchJob> host_jobs;
   long long task_total = 0;
@@ -757,9 +803,7 @@ struct yc_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool started = false;
-  // pinned readback
-  yc::BatchCtl* ctl_host = nullptr;
-  yc::RoundCounters* rc_host = nullptr;
+  yc::BatchTasks* tasks_host = nullptr;     // pinned readback
   unsigned long long* done_host = nullptr;
 };
 
@@ -770,8 +814,9 @@ void free_batch(yc_batch* b) {
   if (b->ctx && b->ctx->stream) cudaStreamSynchronize(b->ctx->stream);
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
-  if (b->ctl_host) cudaFreeHost(b->ctl_host);
-  if (b->rc_host) cudaFreeHost(b->rc_host);
+  b->groups.clear();
+  if (b->ev_start) cudaEventDestroy(b->ev_start);
+  if (b->tasks_host) cudaFreeHost(b->tasks_host);
   if (b->done_host) cudaFreeHost(b->done_host);
   delete b;
 }
@@ -785,55 +830,79 @@ yc::PathState batch_state(yc_batch* b) {
   return ps;
 }
 
-// one round: trace both queues, step every path (A -> B)
-int batch_round(yc_batch* b, int cur, bool timed) {
+// one round of group g: trace both queues, step every path (A -> B). `serial`: every
+// launch on the context stream (per-kernel timing), else on the group's streams.
+int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
   yc_ctx* c = b->ctx;
   const yc::PathState ps = batch_state(b);
-  int* in_c = b->q[2 * cur].p;
-  int* in_a = b->q[2 * cur + 1].p;
-  int* out_c = b->q[2 * (1 - cur)].p;
-  int* out_a = b->q[2 * (1 - cur) + 1].p;
-  yc::RoundCounters* rin = b->rc.p + cur;
-  yc::RoundCounters* rout = b->rc.p + (1 - cur);
+  int* in_c = g.q[2 * cur].p;
+  int* in_a = g.q[2 * cur + 1].p;
+  int* out_c = g.q[2 * (1 - cur)].p;
+  int* out_a = g.q[2 * (1 - cur) + 1].p;
+  yc::RoundCounters* rin = g.rc.p + cur;
+  yc::RoundCounters* rout = g.rc.p + (1 - cur);
+  cudaStream_t sm = serial ? c->stream : g.main;
+  cudaStream_t sa = serial ? c->stream : g.side;
+  // the two traces of a round are independent and overlap
+  if (!serial) {
+    YC_CUDA(cudaEventRecord(g.ev_fork, sm));
+    YC_CUDA(cudaStreamWaitEvent(sa, g.ev_fork, 0));
+  }
   {
     KTimer kt(c, K_EXTEND, timed);
     yc::launch_batch_trace(false, b->wide == 1, b->jobs.p, b->job_pass.p, in_c, &rin->n_closest, &rin->work_closest,
-                           ps.ro, ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_c, c->stream);
+                           ps.ro, ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_c, sm);
   }
   {
     KTimer kt(c, K_OCCL, timed);
     yc::launch_batch_trace(true, b->wide == 1, b->jobs.p, b->job_pass.p, in_a, &rin->n_any, &rin->work_any, ps.ro,
-                           ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_a, c->stream);
+                           ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_a, sa);
   }
-  YC_CUDA(cudaMemsetAsync(rout, 0, sizeof(yc::RoundCounters), c->stream));
-  YC_CUDA(cudaMemsetAsync(b->sctl.p, 0, sizeof(yc::SortCtl), c->stream));
+  if (!serial) {
+    YC_CUDA(cudaEventRecord(g.ev_join, sa));
+    YC_CUDA(cudaStreamWaitEvent(sm, g.ev_join, 0));
+  }
+  YC_CUDA(cudaMemsetAsync(rout, 0, sizeof(yc::RoundCounters), sm));
+  YC_CUDA(cudaMemsetAsync(g.sctl.p, 0, sizeof(yc::SortCtl), sm));
   if (b->cfg.sort_threshold > 0) {
     KTimer kt(c, K_SORT, timed);
-    yc::launch_batch_sort(b->jobs.p, b->job_pass.p, ps, in_c, in_a, rin, b->sort_keys.p, b->sorted.p, b->sctl.p,
-                          b->cfg.sort_threshold, b->logic_grid, c->stream);
+    yc::launch_batch_sort(b->jobs.p, b->job_pass.p, ps, in_c, in_a, rin, g.sort_keys.p, g.sorted.p, g.sctl.p,
+                          b->cfg.sort_threshold, b->logic_grid, sm);
   }
   {
     KTimer kt(c, K_LOGIC, timed);
-    yc::launch_batch_logic(b->jobs.p, b->ctl.p, ps, b->job_pass.p, b->free_stack.p, in_c, in_a, rin, out_c, out_a,
-                           rout, c->stats.p, b->job_done.p, b->sorted.p, b->sctl.p, b->logic_grid, c->stream);
+    yc::launch_batch_logic(b->jobs.p, b->tasks.p, g.ctl.p, ps, b->job_pass.p, g.free_stack.p, in_c, in_a, rin, out_c,
+                           out_a, rout, c->stats.p, b->job_done.p, g.sorted.p, g.sctl.p, b->logic_grid, sm);
   }
   c->ktimes.rounds++;
   YC_CUDA(cudaPeekAtLastError());
   return 0;
 }
 
-// one launch: free slots take new tasks (appended to round 0's closest-hit queue), then
-// an even number of rounds, so every launch starts on queue pair 0
+// one launch: in every group, free slots take new tasks (appended to round 0's
+// closest-hit queue), then an even number of rounds, so every launch starts on queue
+// pair 0. The groups run concurrently on their streams, forked from and joined back to
+// the context stream (serially on it when kernels are timed one by one).
 int batch_body(yc_batch* b, bool timed) {
   yc_ctx* c = b->ctx;
-  {
-    KTimer kt(c, K_RAYGEN, timed);
-    yc::launch_batch_fill(b->jobs.p, b->ctl.p, batch_state(b), b->job_pass.p, b->free_stack.p, b->q[0].p, b->rc.p,
-                          c->stats.p, b->logic_grid, c->stream);
+  const bool serial = timed && c->profile;
+  if (!serial) YC_CUDA(cudaEventRecord(b->ev_start, c->stream));
+  for (auto& gp : b->groups) {
+    BatchGroup& g = *gp;
+    cudaStream_t sm = serial ? c->stream : g.main;
+    if (!serial) YC_CUDA(cudaStreamWaitEvent(sm, b->ev_start, 0));
+    {
+      KTimer kt(c, K_RAYGEN, timed);
+      yc::launch_batch_fill(b->jobs.p, b->tasks.p, g.ctl.p, batch_state(b), b->job_pass.p, g.free_stack.p, g.q[0].p,
+                            g.rc.p, c->stats.p, b->logic_grid, sm);
+    }
+    for (int k = 0; k < b->cfg.rounds_per_launch; ++k)
+      if (int r = batch_round(b, g, k & 1, timed, serial)) return r;
+    if (!serial) YC_CUDA(cudaEventRecord(g.ev_done, sm));
   }
-  int r = 0;
-  for (int k = 0; k < b->cfg.rounds_per_launch && !r; ++k) r = batch_round(b, k & 1, timed);
-  return r;
+  if (!serial)
+    for (auto& gp : b->groups) YC_CUDA(cudaStreamWaitEvent(c->stream, gp->ev_done, 0));
+  return 0;
 }
 
 int batch_launch(yc_batch* b) {
@@ -850,7 +919,7 @@ int batch_launch(yc_batch* b) {
       YC_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
     }
     YC_CUDA(cudaGraphLaunch(b->exec, c->stream));
-    c->ktimes.rounds += b->cfg.rounds_per_launch;
+    c->ktimes.rounds += (uint64_t)b->cfg.rounds_per_launch * b->groups.size();
     return 0;
   }
   return batch_body(b, true);
@@ -872,34 +941,55 @@ int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
   if (b->cfg.rounds_per_launch & 1) b->cfg.rounds_per_launch += 1;
   if (b->cfg.logic_blocks_per_sm <= 0) b->cfg.logic_blocks_per_sm = 4;
   if (b->cfg.max_jobs <= 0) b->cfg.max_jobs = 1024;
+  if (b->cfg.groups <= 0) b->cfg.groups = 2;
+  if (b->cfg.groups > 8 || b->cfg.groups > b->cfg.pool_paths) return fail(YC_E_INVALID, "groups must be 1..8");
   const size_t n = (size_t)b->cfg.pool_paths;
   YC_CUDA(cudaSetDevice(c->device));
   YC_CUDA(b->misc.alloc(n));
   for (auto& f : b->f4bufs) YC_CUDA(f.alloc(n));
   YC_CUDA(b->job_pass.alloc(n));
-  YC_CUDA(b->free_stack.alloc(n));
-  for (auto& q : b->q) YC_CUDA(q.alloc(n));
-  YC_CUDA(b->sctl.alloc(1));
-  if (b->cfg.sort_threshold > 0) {
-    YC_CUDA(b->sort_keys.alloc(n));
-    YC_CUDA(b->sorted.alloc(n));
-  }
-  YC_CUDA(b->rc.alloc(2));
-  YC_CUDA(b->ctl.alloc(1));
+  YC_CUDA(b->tasks.alloc(1));
   YC_CUDA(b->jobs.alloc(b->cfg.max_jobs));
   YC_CUDA(b->job_done.alloc(b->cfg.max_jobs));
-  YC_CUDA(cudaMallocHost(&b->ctl_host, sizeof(yc::BatchCtl)));
-  YC_CUDA(cudaMallocHost(&b->rc_host, 2 * sizeof(yc::RoundCounters)));
+  YC_CUDA(cudaEventCreateWithFlags(&b->ev_start, cudaEventDisableTiming));
+  YC_CUDA(cudaMallocHost(&b->tasks_host, sizeof(yc::BatchTasks)));
   YC_CUDA(cudaMallocHost(&b->done_host, b->cfg.max_jobs * sizeof(unsigned long long)));
-  // every slot starts on the free stack
-  std::vector<int> fs(n);
-  for (size_t i = 0; i < n; ++i) fs[i] = (int)(n - 1 - i);
-  YC_CUDA(cudaMemcpyAsync(b->free_stack.p, fs.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-  yc::BatchCtl ctl{};
-  ctl.free_top = (int)n;
-  YC_CUDA(cudaMemcpyAsync(b->ctl.p, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, c->stream));
-  YC_CUDA(cudaMemsetAsync(b->rc.p, 0, 2 * sizeof(yc::RoundCounters), c->stream));
+  YC_CUDA(cudaMemsetAsync(b->tasks.p, 0, sizeof(yc::BatchTasks), c->stream));
   YC_CUDA(cudaMemsetAsync(b->job_done.p, 0, b->cfg.max_jobs * sizeof(unsigned long long), c->stream));
+  const int G = b->cfg.groups;
+  for (int gi = 0; gi < G; ++gi) {
+    std::unique_ptr<BatchGroup> g(new (std::nothrow) BatchGroup);
+    if (!g) return fail(YC_E_NOMEM, "host allocation failed");
+    g->first = (int)((n * gi) / G);
+    g->count = (int)((n * (gi + 1)) / G) - g->first;
+    const size_t m = (size_t)g->count;
+    YC_CUDA(g->free_stack.alloc(m));
+    for (auto& q : g->q) YC_CUDA(q.alloc(m));
+    YC_CUDA(g->sctl.alloc(1));
+    if (b->cfg.sort_threshold > 0) {
+      YC_CUDA(g->sort_keys.alloc(m));
+      YC_CUDA(g->sorted.alloc(m));
+    }
+    YC_CUDA(g->rc.alloc(2));
+    YC_CUDA(g->ctl.alloc(1));
+    YC_CUDA(cudaStreamCreateWithFlags(&g->main, cudaStreamNonBlocking));
+    YC_CUDA(cudaStreamCreateWithFlags(&g->side, cudaStreamNonBlocking));
+    YC_CUDA(cudaEventCreateWithFlags(&g->ev_fork, cudaEventDisableTiming));
+    YC_CUDA(cudaEventCreateWithFlags(&g->ev_join, cudaEventDisableTiming));
+    YC_CUDA(cudaEventCreateWithFlags(&g->ev_done, cudaEventDisableTiming));
+    YC_CUDA(cudaMallocHost(&g->ctl_host, sizeof(yc::BatchCtl)));
+    YC_CUDA(cudaMallocHost(&g->rc_host, 2 * sizeof(yc::RoundCounters)));
+    // every slot of the group starts on its free stack
+    std::vector<int> fs(m);
+    for (size_t i = 0; i < m; ++i) fs[i] = g->first + (int)(m - 1 - i);
+    YC_CUDA(cudaMemcpyAsync(g->free_stack.p, fs.data(), m * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    yc::BatchCtl ctl{};
+    ctl.free_top = (int)m;
+    YC_CUDA(cudaMemcpyAsync(g->ctl.p, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, c->stream));
+    YC_CUDA(cudaMemsetAsync(g->rc.p, 0, 2 * sizeof(yc::RoundCounters), c->stream));
+    YC_CUDA(cudaStreamSynchronize(c->stream));   // fs leaves scope
+    b->groups.push_back(std::move(g));
+  }
   YC_CUDA(cudaStreamSynchronize(c->stream));
   b->logic_grid = std::max(1, c->sm_count) * b->cfg.logic_blocks_per_sm;
   *out = b.release();
@@ -946,7 +1036,7 @@ int yc_batch_add_job(yc_batch* b, int scene_id, int accum_id, const yc_cam* cam,
   j.reset_first = reset_first;
   if (b->started) {   // claims may have run the cursor past the last total: start after it
     unsigned long long next = 0;
-    YC_CUDA(cudaMemcpyAsync(&next, &b->ctl.p->task_next, sizeof(next), cudaMemcpyDeviceToHost, c->stream));
+    YC_CUDA(cudaMemcpyAsync(&next, &b->tasks.p->task_next, sizeof(next), cudaMemcpyDeviceToHost, c->stream));
     YC_CUDA(cudaStreamSynchronize(c->stream));
     if ((long long)next > b->task_total) b->task_total = (long long)next;
   }
@@ -957,9 +1047,9 @@ int yc_batch_add_job(yc_batch* b, int scene_id, int accum_id, const yc_cam* cam,
   b->task_total += j.n_pix;
   // publish: job count and task total (read by the kernels between launches)
   const int nj = id + 1;
-  YC_CUDA(cudaMemcpyAsync(&b->ctl.p->n_jobs, &nj, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  YC_CUDA(cudaMemcpyAsync(&b->tasks.p->n_jobs, &nj, sizeof(int), cudaMemcpyHostToDevice, c->stream));
   const unsigned long long tt = (unsigned long long)b->task_total;
-  YC_CUDA(cudaMemcpyAsync(&b->ctl.p->task_total, &tt, sizeof(tt), cudaMemcpyHostToDevice, c->stream));
+  YC_CUDA(cudaMemcpyAsync(&b->tasks.p->task_total, &tt, sizeof(tt), cudaMemcpyHostToDevice, c->stream));
   YC_CUDA(cudaStreamSynchronize(c->stream));
   b->host_jobs.push_back(j);
   b->seeds.push_back(std::move(sd));
@@ -984,8 +1074,12 @@ int yc_batch_run(yc_batch* b, int max_launches, int* unfinished) {
   for (;;) {
     if (int r = batch_launch(b)) return r;
     ++launches;
-    YC_CUDA(cudaMemcpyAsync(b->ctl_host, b->ctl.p, sizeof(yc::BatchCtl), cudaMemcpyDeviceToHost, c->stream));
-    YC_CUDA(cudaMemcpyAsync(b->rc_host, b->rc.p, 2 * sizeof(yc::RoundCounters), cudaMemcpyDeviceToHost, c->stream));
+    YC_CUDA(cudaMemcpyAsync(b->tasks_host, b->tasks.p, sizeof(yc::BatchTasks), cudaMemcpyDeviceToHost, c->stream));
+    for (auto& g : b->groups) {
+      YC_CUDA(cudaMemcpyAsync(g->ctl_host, g->ctl.p, sizeof(yc::BatchCtl), cudaMemcpyDeviceToHost, c->stream));
+      YC_CUDA(cudaMemcpyAsync(g->rc_host, g->rc.p, 2 * sizeof(yc::RoundCounters), cudaMemcpyDeviceToHost,
+                              c->stream));
+    }
     YC_CUDA(cudaMemcpyAsync(b->done_host, b->job_done.p, b->host_jobs.size() * sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, c->stream));
     YC_CUDA(cudaStreamSynchronize(c->stream));
@@ -994,9 +1088,10 @@ int yc_batch_run(yc_batch* b, int max_launches, int* unfinished) {
     for (size_t i = 0; i < b->host_jobs.size(); ++i)
       if (b->done_host[i] < (unsigned long long)b->host_jobs[i].n_pix) ++left;
     if (unfinished) *unfinished = left;
-    const bool idle = b->rc_host[0].n_closest == 0 && b->rc_host[0].n_any == 0 &&
-                      b->ctl_host->free_top == b->cfg.pool_paths;
-    if (left == 0 || (idle && b->ctl_host->task_next >= b->ctl_host->task_total)) break;
+    bool idle = true;
+    for (auto& g : b->groups)
+      idle = idle && g->rc_host[0].n_closest == 0 && g->rc_host[0].n_any == 0 && g->ctl_host->free_top == g->count;
+    if (left == 0 || (idle && b->tasks_host->task_next >= b->tasks_host->task_total)) break;
     if (max_launches > 0 && launches >= max_launches) break;
   }
   YC_CUDA(cudaEventRecord(c->ev1, c->stream));

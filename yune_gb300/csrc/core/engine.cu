@@ -9,7 +9,10 @@
 // resolution start and finish; the extend and occlusion kernels read each ray's scene
 // from the job table, so one launch walks many BVHs. Jobs can be added between launches
 // (serving); a task claim is one atomicAdd on the task cursor, and a job added later
-// starts at or after the cursor, so its tasks are never skipped.
+// starts at or after the cursor, so its tasks are never skipped. The pool is split into
+// slot groups, each with its own free stack and queues, whose rounds run concurrently
+// on their own streams and take tasks from the one shared cursor: while one group's
+// round waits on its last rays, the other groups' kernels use the idle SMs.
 #include <cuda_runtime.h>
 
 #include "yc_engine.h"
@@ -49,10 +52,10 @@ __device__ __forceinline__ void start_pass(const BatchJob& J, int job, int pix, 
 // One atomicAdd per claim: the cursor may run past task_total (those tasks do not exist
 // and are dropped); yc_batch_add_job starts a new job at or after the cursor, so no task
 // admitted later falls into the overshoot.
-__device__ __forceinline__ unsigned long long claim_tasks(BatchCtl* ctl, int want, int& got) {
-  const unsigned long long total = *(volatile unsigned long long*)&ctl->task_total;
-  if (*(volatile unsigned long long*)&ctl->task_next >= total) { got = 0; return total; }
-  const unsigned long long t = atomicAdd(&ctl->task_next, (unsigned long long)want);
+__device__ __forceinline__ unsigned long long claim_tasks(BatchTasks* tasks, int want, int& got) {
+  const unsigned long long total = *(volatile unsigned long long*)&tasks->task_total;
+  if (*(volatile unsigned long long*)&tasks->task_next >= total) { got = 0; return total; }
+  const unsigned long long t = atomicAdd(&tasks->task_next, (unsigned long long)want);
   got = t >= total ? 0 : (int)((total - t) < (unsigned long long)want ? (total - t) : (unsigned long long)want);
   return t;
 }
@@ -60,24 +63,25 @@ __device__ __forceinline__ unsigned long long claim_tasks(BatchCtl* ctl, int wan
 // ---- fill: idle slots (on the free stack) take new tasks ----
 // k_batch_plan claims, in one thread, as many tasks as there are free slots; k_batch_fill
 // then starts them across the grid.
-__global__ void k_batch_plan(BatchCtl* ctl) {
+__global__ void k_batch_plan(BatchTasks* tasks, BatchCtl* ctl) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int free_n = ctl->free_top;
   int got = 0;
-  const unsigned long long t0 = free_n > 0 ? claim_tasks(ctl, free_n, got) : 0ull;
+  const unsigned long long t0 = free_n > 0 ? claim_tasks(tasks, free_n, got) : 0ull;
   ctl->fill_t0 = t0;
   ctl->fill_n = got;
   ctl->fill_top = free_n - got;
   ctl->free_top = free_n - got;
 }
 
-__global__ void __launch_bounds__(ENGINE_TB) k_batch_fill(const BatchJob* __restrict__ jobs, const BatchCtl* ctl,
+__global__ void __launch_bounds__(ENGINE_TB) k_batch_fill(const BatchJob* __restrict__ jobs,
+                                                          const BatchTasks* tasks, const BatchCtl* ctl,
                                                           PathState ps, int2* job_pass, const int* free_stack,
                                                           int* q_closest, RoundCounters* rc, DevStats* st) {
   const int n = ctl->fill_n;
   const int top = ctl->fill_top;
   const unsigned long long t0 = ctl->fill_t0;
-  const int n_jobs = ctl->n_jobs;
+  const int n_jobs = tasks->n_jobs;
   const int lane = threadIdx.x & 31;
   const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int warps_total = (gridDim.x * blockDim.x) >> 5;
@@ -106,14 +110,15 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_fill(const BatchJob* __rest
   }
 }
 
-void launch_batch_fill(const BatchJob* jobs, BatchCtl* ctl, const PathState& ps, int2* job_pass, int* free_stack,
-                       int* q_closest, RoundCounters* rc, DevStats* st, int grid, cudaStream_t s) {
-  k_batch_plan<<<1, 32, 0, s>>>(ctl);
-  k_batch_fill<<<grid, ENGINE_TB, 0, s>>>(jobs, ctl, ps, job_pass, free_stack, q_closest, rc, st);
+void launch_batch_fill(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, int2* job_pass,
+                       int* free_stack, int* q_closest, RoundCounters* rc, DevStats* st, int grid, cudaStream_t s) {
+  k_batch_plan<<<1, 32, 0, s>>>(tasks, ctl);
+  k_batch_fill<<<grid, ENGINE_TB, 0, s>>>(jobs, tasks, ctl, ps, job_pass, free_stack, q_closest, rc, st);
 }
 
 // ---- logic with regeneration ----
-__global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __restrict__ jobs, BatchCtl* ctl,
+__global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __restrict__ jobs, BatchTasks* tasks,
+                                                           BatchCtl* ctl,
                                                            PathState ps, int2* job_pass, int* free_stack,
                                                            const int* __restrict__ in_closest,
                                                            const int* __restrict__ in_any, const RoundCounters* rc_in,
@@ -128,7 +133,7 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __res
   const int lane = threadIdx.x & 31;
   const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int warps_total = (gridDim.x * blockDim.x) >> 5;
-  const int n_jobs = ctl->n_jobs;
+  const int n_jobs = tasks->n_jobs;
   const bool use_sorted = sctl->use != 0;
   for (int wbase = warp_global * 32; wbase < n; wbase += warps_total * 32) {
     const int e = wbase + lane;
@@ -158,7 +163,7 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __res
     if (mt) {
       unsigned long long t0 = 0;
       int got = 0;
-      if (lane == 0) t0 = claim_tasks(ctl, __popc(mt), got);
+      if (lane == 0) t0 = claim_tasks(tasks, __popc(mt), got);
       t0 = __shfl_sync(0xffffffffu, t0, 0);
       got = __shfl_sync(0xffffffffu, got, 0);
       if (need_task) {
@@ -207,11 +212,12 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __res
   }
 }
 
-void launch_batch_logic(const BatchJob* jobs, BatchCtl* ctl, const PathState& ps, int2* job_pass, int* free_stack,
+void launch_batch_logic(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, int2* job_pass,
+                        int* free_stack,
                         const int* in_closest, const int* in_any, const RoundCounters* rc_in, int* out_closest,
                         int* out_any, RoundCounters* rc_out, DevStats* st, unsigned long long* job_done,
                         const int* sorted, const SortCtl* sctl, int grid, cudaStream_t s) {
-  k_batch_logic<<<grid, ENGINE_TB, 0, s>>>(jobs, ctl, ps, job_pass, free_stack, in_closest, in_any, rc_in,
+  k_batch_logic<<<grid, ENGINE_TB, 0, s>>>(jobs, tasks, ctl, ps, job_pass, free_stack, in_closest, in_any, rc_in,
                                            out_closest, out_any, rc_out, st, job_done, sorted, sctl);
 }
 

@@ -20,14 +20,20 @@ struct BatchJob {
   int pad_;
 };
 
-// Device-side control block of a batch.
-struct BatchCtl {
+// The task cursor and job count, shared by every slot group of a batch.
+struct BatchTasks {
   unsigned long long task_next;    // next unassigned pixel task
   unsigned long long task_total;   // tasks admitted so far
   int n_jobs;
-  int free_top;                    // slots on the free stack
+  int pad_;
+};
+
+// Control block of one slot group: its free stack and its current fill.
+struct BatchCtl {
+  int free_top;                    // slots on the group's free stack
   int fill_n;                      // the current fill: tasks claimed for free slots,
   int fill_top;                    //   the free-stack position they are taken from,
+  int pad_;
   unsigned long long fill_t0;      //   and the first of them
 };
 
@@ -45,9 +51,9 @@ void launch_batch_sort(const BatchJob* jobs, const int2* job_pass, const PathSta
                        const int* in_any, const RoundCounters* rc_in, int* keys, int* sorted, SortCtl* sctl,
                        int threshold, int grid, cudaStream_t s);
 
-void launch_batch_fill(const BatchJob* jobs, BatchCtl* ctl, const PathState& ps, int2* job_pass, int* free_stack,
-                       int* q_closest, RoundCounters* rc, DevStats* st, int grid, cudaStream_t s);
-void launch_batch_logic(const BatchJob* jobs, BatchCtl* ctl, const PathState& ps, int2* job_pass,
+void launch_batch_fill(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, int2* job_pass,
+                       int* free_stack, int* q_closest, RoundCounters* rc, DevStats* st, int grid, cudaStream_t s);
+void launch_batch_logic(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, int2* job_pass,
                         int* free_stack, const int* in_closest, const int* in_any, const RoundCounters* rc_in,
                         int* out_closest, int* out_any, RoundCounters* rc_out, DevStats* st,
                         unsigned long long* job_done, const int* sorted, const SortCtl* sctl, int grid,
