@@ -186,53 +186,40 @@ __device__ __forceinline__ int walk_pop(Walk& w, const int* stack, int stride) {
   return LINK_NONE;
 }
 
-// One trip of the walk over two-child nodes: descend to a leaf, test its triangles,
-// pop the next subtree. Returns true when the walk has ended (w.link == LINK_NONE);
-// `overflow` is set when the stack bound was reached (the walk then ends early).
-template <bool ANY>
-__device__ __forceinline__ bool walk_step2(Walk& w, int* stack, int stride, int stack_cap, WalkCount& wc,
-                                           bool& overflow) {
-  int link = w.link;
-  while (link >= 0 && link != LINK_NONE) {
-    const float4* nd = w.nodes + 4 * (size_t)link;
-    const float4 n0 = __ldg(nd + 0);
-    const float4 n1 = __ldg(nd + 1);
-    const float4 n2 = __ldg(nd + 2);
-    const int2 n3 = __ldg(reinterpret_cast<const int2*>(nd + 3));
-    wc.nodes += 2;
-    float t0, t1;
-    bool h0, h1;
-    if (!w.exact) {
-      h0 = box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, t0);
-      h1 = box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, t1);
-    } else {
-      h0 = box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, t0);
-      h1 = box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, t1);
-    }
-    const float cb = cull_bound(w.best);
-    h0 = h0 && n3.x != LINK_NONE && !(t0 > cb);
-    h1 = h1 && n3.y != LINK_NONE && !(t1 > cb);
-    if (h0 && h1) {
-      const bool swap = t1 < t0;
-      const int near_l = swap ? n3.y : n3.x, far_l = swap ? n3.x : n3.y;
-      const float far_t = swap ? t0 : t1;
-      if (w.sp >= stack_cap) { overflow = true; w.sp = 0; link = LINK_NONE; break; }
-      stack[(2 * w.sp + 0) * stride] = far_l;
-      stack[(2 * w.sp + 1) * stride] = __float_as_int(far_t);
-      ++w.sp;
-      link = near_l;
-    } else if (h0) {
-      link = n3.x;
-    } else if (h1) {
-      link = n3.y;
-    } else {
-      link = LINK_NONE;
-      break;
-    }
+// One interior node of the two-child layout: returns the next node (the nearer child
+// hit, the other one pushed), or the next subtree popped from the stack when neither
+// child is hit. LINK_NONE: the walk is over (or the stack bound was reached).
+__device__ __forceinline__ int visit2(Walk& w, int link, int* stack, int stride, int stack_cap, WalkCount& wc,
+                                      bool& overflow) {
+  const float4* nd = w.nodes + 4 * (size_t)link;
+  const float4 n0 = __ldg(nd + 0);
+  const float4 n1 = __ldg(nd + 1);
+  const float4 n2 = __ldg(nd + 2);
+  const int2 n3 = __ldg(reinterpret_cast<const int2*>(nd + 3));
+  wc.nodes += 2;
+  float t0, t1;
+  bool h0, h1;
+  if (!w.exact) {
+    h0 = box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, t0);
+    h1 = box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, t1);
+  } else {
+    h0 = box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, t0);
+    h1 = box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, t1);
   }
-  if (link != LINK_NONE && walk_leaf<ANY>(w, link, wc)) { w.sp = 0; w.link = LINK_NONE; return true; }
-  w.link = walk_pop(w, stack, stride);
-  return w.link == LINK_NONE;
+  const float cb = cull_bound(w.best);
+  h0 = h0 && n3.x != LINK_NONE && !(t0 > cb);
+  h1 = h1 && n3.y != LINK_NONE && !(t1 > cb);
+  if (h0 && h1) {
+    const bool swap = t1 < t0;
+    if (w.sp >= stack_cap) { overflow = true; w.sp = 0; return LINK_NONE; }
+    stack[(2 * w.sp + 0) * stride] = swap ? n3.x : n3.y;
+    stack[(2 * w.sp + 1) * stride] = __float_as_int(swap ? t0 : t1);
+    ++w.sp;
+    return swap ? n3.y : n3.x;
+  }
+  if (h0) return n3.x;
+  if (h1) return n3.y;
+  return walk_pop(w, stack, stride);
 }
 
 // (t, link) compare-exchange: the smaller entry distance first
@@ -243,66 +230,91 @@ __device__ __forceinline__ void cx(float& ta, int& la, float& tb, int& lb) {
   }
 }
 
-// The same trip over four-child nodes (yc_scene.h, wide layout): the four child boxes
-// are tested with the reference's slab arithmetic, the hits sorted by entry distance,
-// the nearest visited next and the others pushed farthest first.
-template <bool ANY>
-__device__ __forceinline__ bool walk_step4(Walk& w, int* stack, int stride, int stack_cap, WalkCount& wc,
-                                           bool& overflow) {
+// One interior node of the four-child layout (yc_scene.h, wide nodes): the four child
+// boxes are tested with the reference's slab arithmetic, the hits sorted by entry
+// distance, the nearest returned and the others pushed farthest first.
+__device__ __forceinline__ int visit4(Walk& w, int link, int* stack, int stride, int stack_cap, WalkCount& wc,
+                                      bool& overflow) {
   const float INF = __int_as_float(0x7f800000);
-  int link = w.link;
-  while (link >= 0 && link != LINK_NONE) {
-    const float4* nd = w.nodes + 8 * (size_t)link;
-    const float4 lx = __ldg(nd + 0), hx = __ldg(nd + 1);
-    const float4 ly = __ldg(nd + 2), hy = __ldg(nd + 3);
-    const float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5);
-    const int4 ln = __ldg(reinterpret_cast<const int4*>(nd + 6));
-    wc.nodes += 4;
-    const float cb = cull_bound(w.best);
-    float t[4];
-    int l[4];
-    const float clx[4] = {lx.x, lx.y, lx.z, lx.w}, chx[4] = {hx.x, hx.y, hx.z, hx.w};
-    const float cly[4] = {ly.x, ly.y, ly.z, ly.w}, chy[4] = {hy.x, hy.y, hy.z, hy.w};
-    const float clz[4] = {lz.x, lz.y, lz.z, lz.w}, chz[4] = {hz.x, hz.y, hz.z, hz.w};
-    const int cl[4] = {ln.x, ln.y, ln.z, ln.w};
+  const float4* nd = w.nodes + 8 * (size_t)link;
+  const float4 lx = __ldg(nd + 0), hx = __ldg(nd + 1);
+  const float4 ly = __ldg(nd + 2), hy = __ldg(nd + 3);
+  const float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5);
+  const int4 ln = __ldg(reinterpret_cast<const int4*>(nd + 6));
+  wc.nodes += 4;
+  const float cb = cull_bound(w.best);
+  float t[4];
+  int l[4];
+  const float clx[4] = {lx.x, lx.y, lx.z, lx.w}, chx[4] = {hx.x, hx.y, hx.z, hx.w};
+  const float cly[4] = {ly.x, ly.y, ly.z, ly.w}, chy[4] = {hy.x, hy.y, hy.z, hy.w};
+  const float clz[4] = {lz.x, lz.y, lz.z, lz.w}, chz[4] = {hz.x, hz.y, hz.z, hz.w};
+  const int cl[4] = {ln.x, ln.y, ln.z, ln.w};
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      float te;
-      bool h = !w.exact ? box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, clx[c], chx[c], cly[c], chy[c], clz[c], chz[c], te)
-                        : box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, clx[c], chx[c], cly[c], chy[c], clz[c], chz[c], te);
-      h = h && cl[c] != LINK_NONE && !(te > cb);
-      t[c] = h ? te : INF;
-      l[c] = h ? cl[c] : LINK_NONE;
-    }
-    // sorting network for four entries; misses (t = inf, LINK_NONE) end up last
-    cx(t[0], l[0], t[1], l[1]);
-    cx(t[2], l[2], t[3], l[3]);
-    cx(t[0], l[0], t[2], l[2]);
-    cx(t[1], l[1], t[3], l[3]);
-    cx(t[1], l[1], t[2], l[2]);
-    if (l[0] == LINK_NONE) { link = LINK_NONE; break; }
-    const int extra = (l[1] != LINK_NONE) + (l[2] != LINK_NONE) + (l[3] != LINK_NONE);
-    if (w.sp + extra > stack_cap) { overflow = true; w.sp = 0; link = LINK_NONE; break; }
-#pragma unroll
-    for (int c = 3; c >= 1; --c) {
-      if (l[c] != LINK_NONE) {
-        stack[(2 * w.sp + 0) * stride] = l[c];
-        stack[(2 * w.sp + 1) * stride] = __float_as_int(t[c]);
-        ++w.sp;
-      }
-    }
-    link = l[0];
+  for (int c = 0; c < 4; ++c) {
+    float te;
+    bool h = !w.exact ? box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, clx[c], chx[c], cly[c], chy[c], clz[c], chz[c], te)
+                      : box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, clx[c], chx[c], cly[c], chy[c], clz[c], chz[c], te);
+    h = h && cl[c] != LINK_NONE && !(te > cb);
+    t[c] = h ? te : INF;
+    l[c] = h ? cl[c] : LINK_NONE;
   }
-  if (link != LINK_NONE && walk_leaf<ANY>(w, link, wc)) { w.sp = 0; w.link = LINK_NONE; return true; }
-  w.link = walk_pop(w, stack, stride);
-  return w.link == LINK_NONE;
+  // sorting network for four entries; misses (t = inf, LINK_NONE) end up last
+  cx(t[0], l[0], t[1], l[1]);
+  cx(t[2], l[2], t[3], l[3]);
+  cx(t[0], l[0], t[2], l[2]);
+  cx(t[1], l[1], t[3], l[3]);
+  cx(t[1], l[1], t[2], l[2]);
+  if (l[0] == LINK_NONE) return walk_pop(w, stack, stride);
+  const int extra = (l[1] != LINK_NONE) + (l[2] != LINK_NONE) + (l[3] != LINK_NONE);
+  if (w.sp + extra > stack_cap) { overflow = true; w.sp = 0; return LINK_NONE; }
+#pragma unroll
+  for (int c = 3; c >= 1; --c) {
+    if (l[c] != LINK_NONE) {
+      stack[(2 * w.sp + 0) * stride] = l[c];
+      stack[(2 * w.sp + 1) * stride] = __float_as_int(t[c]);
+      ++w.sp;
+    }
+  }
+  return l[0];
 }
 
+// One step of the walk, the while-while loop with postponed leaves of Aila and Laine
+// ("Understanding the Efficiency of Ray Traversal on GPUs", 2009, and its 2012
+// addendum): interior nodes are visited until every lane of the warp still walking has
+// reached a leaf; a lane that meets its first leaf keeps it aside and goes on with the
+// next subtree, so the lanes test triangles together instead of one after another.
+// Returns true when the walk has ended (w.link == LINK_NONE); `overflow` is set when the
+// stack bound was reached (the walk then ends early). Leaves are kept aside before the
+// hits inside them lower the culling distance, so the walk may open a few more boxes
+// than a leaf-first order would; it never skips one that can hold a closer hit.
 template <bool ANY, bool WIDE>
 __device__ __forceinline__ bool walk_step(Walk& w, int* stack, int stride, int stack_cap, WalkCount& wc,
                                           bool& overflow) {
-  if (WIDE) return walk_step4<ANY>(w, stack, stride, stack_cap, wc, overflow);
-  return walk_step2<ANY>(w, stack, stride, stack_cap, wc, overflow);
+  int link = w.link;
+  int leaf = LINK_NONE;
+  while (link >= 0 && link != LINK_NONE) {
+    link = WIDE ? visit4(w, link, stack, stride, stack_cap, wc, overflow)
+                : visit2(w, link, stack, stride, stack_cap, wc, overflow);
+    if (link < 0 && link != LINK_NONE && leaf == LINK_NONE) {
+      leaf = link;
+      link = walk_pop(w, stack, stride);
+    }
+    if (!__any_sync(__activemask(), leaf == LINK_NONE)) break;
+  }
+  if (leaf == LINK_NONE && link < 0 && link != LINK_NONE) {
+    leaf = link;
+    link = walk_pop(w, stack, stride);
+  }
+  while (leaf != LINK_NONE) {
+    if (walk_leaf<ANY>(w, leaf, wc)) { w.sp = 0; w.link = LINK_NONE; return true; }
+    leaf = LINK_NONE;
+    if (link < 0 && link != LINK_NONE) {   // a second leaf met by the speculative walk
+      leaf = link;
+      link = walk_pop(w, stack, stride);
+    }
+  }
+  w.link = link;
+  return link == LINK_NONE;
 }
 
 }  // namespace yc
