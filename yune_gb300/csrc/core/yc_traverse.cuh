@@ -127,6 +127,7 @@ struct Walk {
   float best, bu, bv;
   int best_tri, best_rank;
   int link, sp;
+  float link_t;          // entry distance of the subtree `link` (checked again before it is opened)
   bool exact;
 };
 
@@ -141,6 +142,7 @@ __device__ __forceinline__ void walk_begin(const DevScene& sc, const RayIn& r, W
   w.best_tri = -1; w.best_rank = -1;
   w.sp = 0;
   w.link = sc.root_link;
+  w.link_t = -__int_as_float(0x7f800000);
   if (w.link != LINK_NONE && sc.root_test) {
     float te;
     const bool h = w.exact ? box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, sc.root_lo.x, sc.root_hi.x, sc.root_lo.y,
@@ -181,9 +183,18 @@ __device__ __forceinline__ int walk_pop(Walk& w, const int* stack, int stride) {
   while (w.sp > 0) {
     --w.sp;
     const float te = __int_as_float(stack[(2 * w.sp + 1) * stride]);
-    if (!(te > cull_bound(w.best))) return stack[(2 * w.sp) * stride];
+    if (!(te > cull_bound(w.best))) {
+      w.link_t = te;
+      return stack[(2 * w.sp) * stride];
+    }
   }
   return LINK_NONE;
+}
+
+// the pending subtree, unless a hit found since it was chosen puts it out of reach
+__device__ __forceinline__ int walk_recheck(Walk& w, int link, const int* stack, int stride) {
+  if (link != LINK_NONE && w.link_t > cull_bound(w.best)) return walk_pop(w, stack, stride);
+  return link;
 }
 
 // One interior node of the two-child layout: returns the next node (the nearer child
@@ -215,10 +226,11 @@ __device__ __forceinline__ int visit2(Walk& w, int link, int* stack, int stride,
     stack[(2 * w.sp + 0) * stride] = swap ? n3.x : n3.y;
     stack[(2 * w.sp + 1) * stride] = __float_as_int(swap ? t0 : t1);
     ++w.sp;
+    w.link_t = swap ? t1 : t0;
     return swap ? n3.y : n3.x;
   }
-  if (h0) return n3.x;
-  if (h1) return n3.y;
+  if (h0) { w.link_t = t0; return n3.x; }
+  if (h1) { w.link_t = t1; return n3.y; }
   return walk_pop(w, stack, stride);
 }
 
@@ -275,6 +287,7 @@ __device__ __forceinline__ int visit4(Walk& w, int link, int* stack, int stride,
       ++w.sp;
     }
   }
+  w.link_t = t[0];
   return l[0];
 }
 
@@ -290,7 +303,8 @@ __device__ __forceinline__ int visit4(Walk& w, int link, int* stack, int stride,
 template <bool ANY, bool WIDE>
 __device__ __forceinline__ bool walk_step(Walk& w, int* stack, int stride, int stack_cap, WalkCount& wc,
                                           bool& overflow) {
-  int link = w.link;
+  // (an any-hit walk keeps its segment length until it stops: nothing to check again)
+  int link = ANY ? w.link : walk_recheck(w, w.link, stack, stride);
   int leaf = LINK_NONE;
   while (link >= 0 && link != LINK_NONE) {
     link = WIDE ? visit4(w, link, stack, stride, stack_cap, wc, overflow)
@@ -308,6 +322,7 @@ __device__ __forceinline__ bool walk_step(Walk& w, int* stack, int stride, int s
   while (leaf != LINK_NONE) {
     if (walk_leaf<ANY>(w, leaf, wc)) { w.sp = 0; w.link = LINK_NONE; return true; }
     leaf = LINK_NONE;
+    if (!ANY) link = walk_recheck(w, link, stack, stride);
     if (link < 0 && link != LINK_NONE) {   // a second leaf met by the speculative walk
       leaf = link;
       link = walk_pop(w, stack, stride);
