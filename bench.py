@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--trace-bench", type=int, default=0, help="traversal alone on this many seeded rays")
     ap.add_argument("--tail", type=int, default=-1, help="paths left at which a pass ends in the tail kernel "
                                                          "(-1 auto, 0 off)")
+    ap.add_argument("--mixed", type=int, default=1,
+                    help="1: a round's closest-hit and any-hit rays share one traversal launch; 0: one launch each")
     ap.add_argument("--tree", type=int, default=1,
                     help="interior hierarchy: 0 reference nodes, 1 binary SAH over the reference leaves, 2 four-wide")
     return ap.parse_args()
@@ -232,16 +234,30 @@ def _reduce(dist, t_s, rays):
     return mx.item(), sm.item()
 
 
-def _extend_roofline(st, boxes_key, tris_key, rays_key, ms, l2, pk, pk_kind, kernel):
-    nbytes = 32.0 * st[boxes_key] + 48.0 * st[tris_key] + 84.0 * st[rays_key]
+def _trace_roofline(st, kt, l2, pk, pk_kind, kernel_mixed, kernel_extend):
+    """Roofline of the traversal kernel: algorithmic bytes (32 B per child box tested,
+    48 B per triangle tested, 84 B of ray and hit records per ray) over its event time.
+    With the mixed kernel (both ray kinds in one launch) the bytes of both kinds count;
+    otherwise the closest-hit (extend) kernel alone."""
+    mixed = kt.get("trace_launches", 0) > 0
+    kinds = ("ext", "any") if mixed else ("ext",)
+    boxes = sum(st[k + "_boxes"] for k in kinds)
+    tris = sum(st[k + "_tris"] for k in kinds)
+    rays = sum(st[k + "_rays"] for k in kinds)
+    ms = kt["trace_ms"] if mixed else kt["extend_ms"]
+    nbytes = 32.0 * boxes + 48.0 * tris + 84.0 * rays
     achieved = nbytes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
-    return {"kernel": kernel, "bound": "l2", "achieved": achieved, "peak": l2, "unit": "GB/s",
-            "frac": achieved / l2 if l2 else None, "traffic": None,
-            "peak_source": "measured L2 read bandwidth (yc_measure_l2_gbs, 48 MB x 20 sweeps)",
-            "hbm_peak": pk.get("hbm_gbs"), "hbm_frac": achieved / pk.get("hbm_gbs", 1.0), "hbm_peak_source": pk_kind,
-            "bytes_per_ray": nbytes / max(1, st[rays_key]),
-            "box_tests_per_ray": st[boxes_key] / max(1, st[rays_key]),
-            "tri_tests_per_ray": st[tris_key] / max(1, st[rays_key])}
+    out = {"kernel": kernel_mixed if mixed else kernel_extend, "bound": "l2", "achieved": achieved, "peak": l2,
+           "unit": "GB/s", "frac": achieved / l2 if l2 else None, "traffic": None,
+           "peak_source": "measured L2 read bandwidth (yc_measure_l2_gbs, 48 MB x 20 sweeps)",
+           "hbm_peak": pk.get("hbm_gbs"), "hbm_frac": achieved / pk.get("hbm_gbs", 1.0), "hbm_peak_source": pk_kind,
+           "rays": int(rays), "bytes_per_ray": nbytes / max(1, rays),
+           "box_tests_per_ray": boxes / max(1, rays), "tri_tests_per_ray": tris / max(1, rays),
+           "grays_per_s": rays / (ms / 1e3) / 1e9 if ms > 0 else 0.0}
+    if mixed:
+        out["closest_rays"] = int(st["ext_rays"])
+        out["any_rays"] = int(st["any_rays"])
+    return out
 
 
 def run_ours(args, rank, local, ws, dist):
@@ -267,6 +283,7 @@ def run_ours(args, rank, local, ws, dist):
     r = Renderer(local)
     r.set_tree_mode(args.tree)
     r.set_tail_paths(args.tail)
+    r.set_mixed_trace(args.mixed)
     sid = r.upload(scene)
     r.set_camera(scene.cam)
     l2 = r.measure_l2_gbs(48 << 20, 20)
@@ -360,7 +377,7 @@ def run_ours(args, rank, local, ws, dist):
         r.close()
         return
     launches = int(kt_en["raygen_launches"] + kt_en["extend_launches"] + kt_en["occlusion_launches"]
-                   + kt_en["logic_launches"] + kt_en["sort_launches"])
+                   + kt_en["trace_launches"] + kt_en["logic_launches"] + kt_en["sort_launches"])
     line = {
         "metric": METRIC, "value": rays / t_s / 1e6, "unit": METRIC, "n_gpus": ws, "steps": K,
         "warmup": Wm, "ms_per_step": en_ms / K, "higher_is_better": True, "scaling": "weak",
@@ -376,17 +393,19 @@ def run_ours(args, rank, local, ws, dist):
         "rays_per_sample": st_en["rays"] / max(1, st_en["samples"]),
         "gpu_launches": launches,
         "engine_equal_to_per_pass": same,
-        "kernel_ms": {"fill": kt_en["raygen_ms"], "extend": kt_en["extend_ms"], "occlusion": kt_en["occlusion_ms"],
-                      "sort": kt_en["sort_ms"], "logic": kt_en["logic_ms"], "rounds": kt_en["rounds"]},
-        "roofline": _extend_roofline(st_enp, "ext_boxes", "ext_tris", "ext_rays", kt_en["extend_ms"], l2, pk, pk_kind,
-                                     "k_batch_trace<closest> (extend)"),
+        "kernel_ms": {"fill": kt_en["raygen_ms"], "trace": kt_en["trace_ms"], "extend": kt_en["extend_ms"],
+                      "occlusion": kt_en["occlusion_ms"], "sort": kt_en["sort_ms"], "logic": kt_en["logic_ms"],
+                      "rounds": kt_en["rounds"]},
+        "roofline": _trace_roofline(st_enp, kt_en, l2, pk, pk_kind, "k_batch_trace_mixed (closest + any-hit rays)",
+                                    "k_batch_trace<closest> (extend)"),
         "per_pass": {"value": pp_rays / pp_s / 1e6, "ms_per_step": pp_ms / K, "unit": METRIC,
                      "note": "yc_render_pass per pass (the drop-in call), L2 flushed before each pass",
-                     "kernel_ms": {"raygen": kt_pp["raygen_ms"], "extend": kt_pp["extend_ms"],
-                                   "occlusion": kt_pp["occlusion_ms"], "logic": kt_pp["logic_ms"],
-                                   "tail": kt_pp["tail_ms"], "rounds": kt_pp["rounds"]},
-                     "roofline": _extend_roofline(st_pp, "ext_boxes", "ext_tris", "ext_rays", kt_pp["extend_ms"], l2,
-                                                  pk, pk_kind, "k_trace_paths<closest> (extend)")},
+                     "kernel_ms": {"raygen": kt_pp["raygen_ms"], "trace": kt_pp["trace_ms"],
+                                   "extend": kt_pp["extend_ms"], "occlusion": kt_pp["occlusion_ms"],
+                                   "logic": kt_pp["logic_ms"], "tail": kt_pp["tail_ms"], "rounds": kt_pp["rounds"]},
+                     "roofline": _trace_roofline(st_pp, kt_pp, l2, pk, pk_kind,
+                                                 "k_trace_paths_mixed (closest + any-hit rays)",
+                                                 "k_trace_paths<closest> (extend)")},
         "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else 0.0, "unit": METRIC, "passes_per_step": E,
                 "h2d_bytes_per_step": 80 + 4 * E, "d2h_bytes_per_step": W * H * 16, "steps": args.e2e_steps,
                 "path": "yc_batch_add_job + yc_batch_run + yc_tonemap to host"},
@@ -412,6 +431,7 @@ def run_c2(args):
     jobs = workloads.c2_jobs(n_jobs=args.jobs, spp=args.spp, max_tris=args.max_tris)
     r = Renderer(0)
     r.set_tree_mode(args.tree)
+    r.set_mixed_trace(args.mixed)
     sids = [r.upload(s) for s in jobs]
     seeds = [scenes.pass_seeds(1000 + i, s.spp) for i, s in enumerate(jobs)]
     px = sum(s.width * s.height for s in jobs)

@@ -88,6 +88,9 @@ typedef struct yc_kernel_times {
   uint64_t sort_launches;
   double tail_ms;              /* tail kernel (YC_OPT_TAIL) */
   uint64_t tail_launches;
+  double trace_ms;             /* one launch over a round's closest-hit and any-hit rays
+                                  (YC_OPT_MIXED_TRACE); extend_ms and occlusion_ms then stay 0 */
+  uint64_t trace_launches;
 } yc_kernel_times;
 
 typedef struct yc_ctx yc_ctx;
@@ -219,7 +222,12 @@ enum {
    * finishes them a thread per path (trace and shading in turn) instead of round by
    * round; the result is the same bits. -1 (default) = as many paths as one resident
    * launch of that kernel holds; 0 = off. */
-  YC_OPT_TAIL = 2
+  YC_OPT_TAIL = 2,
+  /* Traversal launches of a round: 1 (default) = the closest-hit (extension) and the
+   * any-hit (shadow, MIS) rays of a round share one launch; 0 = one launch each, the two
+   * overlapping on two streams. Same results either way. Applies to later
+   * yc_render_pass(es) calls and to batches created afterwards. */
+  YC_OPT_MIXED_TRACE = 3
 };
 int yc_set_option(yc_ctx* ctx, int option, int value);
 

@@ -47,6 +47,32 @@ def test_batch_matches_per_pass(use_graph, pool, sort, groups):
         b.close()
 
 
+@pytest.mark.parametrize("groups", [1, 2])
+def test_batch_separate_trace_launches_match(groups):
+    """With one traversal launch per ray kind (YC_OPT_MIXED_TRACE = 0) the batch gives the
+    same accumulators as the per-pass path, as with the mixed launch."""
+    jobs = _jobs()
+    with Renderer(0) as r:
+        r.set_mixed_trace(0)
+        ids = [r.upload(s) for s, _ in jobs]
+        want = []
+        for (s, seeds), sid in zip(jobs, ids):
+            r.set_camera(s.cam)
+            aid = r.alloc_accum(s.width, s.height)
+            r.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+            want.append(r.read_accum(aid))
+        b = Batch(r, pool_paths=4096, rounds_per_launch=4, use_graph=True, groups=groups)
+        accs = []
+        for (s, seeds), sid in zip(jobs, ids):
+            aid = r.alloc_accum(s.width, s.height)
+            accs.append(aid)
+            b.add_job(sid, aid, s.cam, seeds, s.cfg)
+        assert b.run() == 0
+        for aid, w in zip(accs, want):
+            assert np.array_equal(r.read_accum(aid).view(np.int32), w.view(np.int32))
+        b.close()
+
+
 def test_batch_jobs_added_while_running():
     """Serving: a job admitted after the batch started still renders exactly."""
     jobs = _jobs()

@@ -227,6 +227,39 @@ def test_render_identical_across_tree_modes(renderer, tree):
 
 
 @pytest.mark.parametrize("tree", [1, 2])
+def test_render_identical_with_and_without_mixed_trace(renderer, tree):
+    """One traversal launch over a round's closest-hit and any-hit rays (the default)
+    gives the same bits and the same ray counts as one launch per kind, and both equal
+    the oracle."""
+    s = scenes.c1(40, 32, level=5)
+    seeds = scenes.pass_seeds(31, 2)
+    renderer.set_tree_mode(tree)
+    sid = renderer.upload(s)
+    renderer.set_tree_mode(1)
+    renderer.set_camera(s.cam)
+    out = []
+    for mixed in (1, 0):
+        renderer.set_mixed_trace(mixed)
+        aid = renderer.alloc_accum(40, 32)
+        renderer.reset_stats()
+        renderer.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+        out.append((renderer.read_accum(aid), renderer.stats()))
+        renderer.free_accum(aid)
+    renderer.set_mixed_trace(1)
+    renderer.release(sid)
+    ref = np.zeros((32, 40, 4), np.float32)
+    for k, sd in enumerate(seeds):
+        O.render(s, ref, sd, 1 if k == 0 else 0, s.cfg)
+    for img, st in out:
+        assert st["stack_overflow"] == 0
+        assert np.array_equal(img.view(np.int32), ref.view(np.int32))
+    # (boxes and triangles tested may differ: the speculative walk of a lane depends on
+    # which rays share its warp)
+    for key in ("rays", "ext_rays", "any_rays", "traversed"):
+        assert out[0][1][key] == out[1][1][key], key
+
+
+@pytest.mark.parametrize("tree", [1, 2])
 def test_tail_kernel_gives_the_same_pass(renderer, tree):
     """Finishing the last paths a thread each (YC_OPT_TAIL) changes no bit of the pass and
     no ray count: off, from 64 paths, and from one resident launch (the default)."""

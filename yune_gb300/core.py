@@ -142,6 +142,11 @@ class Renderer:
         """Paths left at which a pass finishes in the tail kernel (-1 auto, 0 off)."""
         N.check(self.L.yc_set_option(self.h, 2, int(n)), "yc_set_option")
 
+    def set_mixed_trace(self, on):
+        """1: a round's closest-hit and any-hit rays share one traversal launch (default);
+        0: one launch each."""
+        N.check(self.L.yc_set_option(self.h, 3, int(on)), "yc_set_option")
+
     def set_profiling(self, on=True):
         N.check(self.L.yc_set_profiling(self.h, int(on)), "yc_set_profiling")
 

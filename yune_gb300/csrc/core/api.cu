@@ -95,6 +95,7 @@ struct yc_ctx {
   bool have_cam = false;
   int tree_mode = yc::TREE_SAH_OVER_LEAVES;
   int tail_paths = -1;   // YC_OPT_TAIL: -1 = one resident launch of the tail kernel, 0 = off
+  int mixed_trace = 1;   // YC_OPT_MIXED_TRACE: one traversal launch per round for both ray kinds
   // wavefront buffers, sized for the largest image seen
   size_t cap_paths = 0;
   DevBuf<int4> misc;
@@ -135,7 +136,7 @@ int ensure_paths(yc_ctx* c, size_t n) {
 }
 
 // event pairs around kernel launches (profiling only)
-enum { K_RAYGEN = 0, K_EXTEND = 1, K_OCCL = 2, K_LOGIC = 3, K_SORT = 4, K_TAIL = 5 };
+enum { K_RAYGEN = 0, K_EXTEND = 1, K_OCCL = 2, K_LOGIC = 3, K_SORT = 4, K_TAIL = 5, K_TRACE = 6 };
 cudaEvent_t next_event(yc_ctx* c) {
   if (c->ev_used == c->ev_pool.size()) {
     cudaEvent_t e;
@@ -176,6 +177,7 @@ void collect_events(yc_ctx* c) {
       case K_OCCL: c->ktimes.occlusion_ms += ms; c->ktimes.occlusion_launches++; break;
       case K_SORT: c->ktimes.sort_ms += ms; c->ktimes.sort_launches++; break;
       case K_TAIL: c->ktimes.tail_ms += ms; c->ktimes.tail_launches++; break;
+      case K_TRACE: c->ktimes.trace_ms += ms; c->ktimes.trace_launches++; break;
       default: c->ktimes.logic_ms += ms; c->ktimes.logic_launches++; break;
     }
   }
@@ -268,9 +270,12 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     else yc::launch_raygen(pp, ps, c->q[0].p, rc + 0, c->stats.p, c->stream);
   }
   YC_CUDA(cudaPeekAtLastError());
+  const bool mixed = c->mixed_trace != 0;
   const int grid_c = yc::trace_grid_blocks(false, sc->dev.depth, sc->dev.wide != 0);
   const int grid_a = yc::trace_grid_blocks(true, sc->dev.depth, sc->dev.wide != 0);
-  if (grid_c <= 0 || grid_a <= 0) return fail(YC_E_LAUNCH, "trace kernel cannot be resident (stack too deep)");
+  const int grid_m = mixed ? yc::trace_mixed_grid_blocks(sc->dev.depth, sc->dev.wide != 0) : 1;
+  if (grid_c <= 0 || grid_a <= 0 || grid_m <= 0)
+    return fail(YC_E_LAUNCH, "trace kernel cannot be resident (stack too deep)");
   int tail_grid = 0, tail_at = 0;
   if (!bdpt && c->tail_paths != 0) {
     const int capacity = yc::tail_capacity(sc->dev, &tail_grid);
@@ -286,27 +291,34 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     yc::RoundCounters* rin = rc + cur;
     yc::RoundCounters* rout = rc + (1 - cur);
     int e1, e2;
-    // the two traces of a round are independent: the any-hit one runs on the side stream
-    // so that each fills the SMs the other's last rays leave idle (sequential when
-    // profiling, so each kernel's events time it alone)
-    const bool overlap = !c->profile;
+    if (mixed) {   // both ray kinds of the round in one launch
+      KTimer kt(c, K_TRACE);
+      if (yc::launch_trace_mixed(sc->dev, in_c, in_a, rin, ps.ro, ps.rd, ps.hit, c->stats.p, grid_m, c->stream))
+        return fail(YC_E_LAUNCH, std::string("trace kernel: ") + cudaGetErrorString(cudaGetLastError()));
+    }
+    // otherwise the two traces of a round are independent: the any-hit one runs on the
+    // side stream so that each fills the SMs the other's last rays leave idle (sequential
+    // when profiling, so each kernel's events time it alone)
+    const bool overlap = !c->profile && !mixed;
     cudaStream_t s_any = overlap ? c->side_stream : c->stream;
     if (overlap) {
       YC_CUDA(cudaEventRecord(c->ev_fork, c->stream));
       YC_CUDA(cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
     }
-    {
-      KTimer kt(c, K_EXTEND);
-      e1 = yc::launch_trace(sc->dev, false, in_c, &rin->n_closest, &rin->work_closest, ps.ro, ps.rd, ps.hit,
-                            c->stats.p, grid_c, c->stream);
+    if (!mixed) {
+      {
+        KTimer kt(c, K_EXTEND);
+        e1 = yc::launch_trace(sc->dev, false, in_c, &rin->n_closest, &rin->work_closest, ps.ro, ps.rd, ps.hit,
+                              c->stats.p, grid_c, c->stream);
+      }
+      if (e1) return fail(YC_E_LAUNCH, std::string("extend kernel: ") + cudaGetErrorString(cudaGetLastError()));
+      {
+        KTimer kt(c, K_OCCL);
+        e2 = yc::launch_trace(sc->dev, true, in_a, &rin->n_any, &rin->work_any, ps.ro, ps.rd, ps.hit, c->stats.p,
+                              grid_a, s_any);
+      }
+      if (e2) return fail(YC_E_LAUNCH, std::string("occlusion kernel: ") + cudaGetErrorString(cudaGetLastError()));
     }
-    if (e1) return fail(YC_E_LAUNCH, std::string("extend kernel: ") + cudaGetErrorString(cudaGetLastError()));
-    {
-      KTimer kt(c, K_OCCL);
-      e2 = yc::launch_trace(sc->dev, true, in_a, &rin->n_any, &rin->work_any, ps.ro, ps.rd, ps.hit, c->stats.p,
-                            grid_a, s_any);
-    }
-    if (e2) return fail(YC_E_LAUNCH, std::string("occlusion kernel: ") + cudaGetErrorString(cudaGetLastError()));
     if (overlap) {
       YC_CUDA(cudaEventRecord(c->ev_join, c->side_stream));
       YC_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
@@ -716,6 +728,10 @@ int yc_set_option(yc_ctx* c, int option, int value) {
       if (value < -1) return fail(YC_E_INVALID, "bad tail threshold");
       c->tail_paths = value;
       return YC_OK;
+    case YC_OPT_MIXED_TRACE:
+      if (value != 0 && value != 1) return fail(YC_E_INVALID, "mixed trace is 0 or 1");
+      c->mixed_trace = value;
+      return YC_OK;
     default:
       return fail(YC_E_INVALID, "unknown option");
   }
@@ -799,7 +815,8 @@ struct yc_batch {
   long long task_total = 0;
   int stack_cap = 0;
   int wide = -1;   // node layout of the batch's scenes (-1: no job yet)
-  int grid_c = 0, grid_a = 0, logic_grid = 0;
+  int grid_c = 0, grid_a = 0, grid_m = 0, logic_grid = 0;
+  bool mixed = true;   // YC_OPT_MIXED_TRACE of the context when the batch was created
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool started = false;
@@ -843,24 +860,30 @@ int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
   yc::RoundCounters* rout = g.rc.p + (1 - cur);
   cudaStream_t sm = serial ? c->stream : g.main;
   cudaStream_t sa = serial ? c->stream : g.side;
-  // the two traces of a round are independent and overlap
-  if (!serial) {
-    YC_CUDA(cudaEventRecord(g.ev_fork, sm));
-    YC_CUDA(cudaStreamWaitEvent(sa, g.ev_fork, 0));
-  }
-  {
-    KTimer kt(c, K_EXTEND, timed);
-    yc::launch_batch_trace(false, b->wide == 1, b->jobs.p, b->job_pass.p, in_c, &rin->n_closest, &rin->work_closest,
-                           ps.ro, ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_c, sm);
-  }
-  {
-    KTimer kt(c, K_OCCL, timed);
-    yc::launch_batch_trace(true, b->wide == 1, b->jobs.p, b->job_pass.p, in_a, &rin->n_any, &rin->work_any, ps.ro,
-                           ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_a, sa);
-  }
-  if (!serial) {
-    YC_CUDA(cudaEventRecord(g.ev_join, sa));
-    YC_CUDA(cudaStreamWaitEvent(sm, g.ev_join, 0));
+  if (b->mixed) {   // both ray kinds of the round in one launch
+    KTimer kt(c, K_TRACE, timed);
+    yc::launch_batch_trace_mixed(b->wide == 1, b->jobs.p, b->job_pass.p, in_c, in_a, rin, ps.ro, ps.rd, ps.hit,
+                                 c->stats.p, b->stack_cap, b->grid_m, sm);
+  } else {
+    // the two traces of a round are independent and overlap
+    if (!serial) {
+      YC_CUDA(cudaEventRecord(g.ev_fork, sm));
+      YC_CUDA(cudaStreamWaitEvent(sa, g.ev_fork, 0));
+    }
+    {
+      KTimer kt(c, K_EXTEND, timed);
+      yc::launch_batch_trace(false, b->wide == 1, b->jobs.p, b->job_pass.p, in_c, &rin->n_closest,
+                             &rin->work_closest, ps.ro, ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_c, sm);
+    }
+    {
+      KTimer kt(c, K_OCCL, timed);
+      yc::launch_batch_trace(true, b->wide == 1, b->jobs.p, b->job_pass.p, in_a, &rin->n_any, &rin->work_any, ps.ro,
+                             ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_a, sa);
+    }
+    if (!serial) {
+      YC_CUDA(cudaEventRecord(g.ev_join, sa));
+      YC_CUDA(cudaStreamWaitEvent(sm, g.ev_join, 0));
+    }
   }
   YC_CUDA(cudaMemsetAsync(rout, 0, sizeof(yc::RoundCounters), sm));
   YC_CUDA(cudaMemsetAsync(g.sctl.p, 0, sizeof(yc::SortCtl), sm));
@@ -935,6 +958,7 @@ int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
   std::unique_ptr<yc_batch> b(new (std::nothrow) yc_batch);
   if (!b) return fail(YC_E_NOMEM, "host allocation failed");
   b->ctx = c;
+  b->mixed = c->mixed_trace != 0;
   if (cfg) b->cfg = *cfg;
   if (b->cfg.pool_paths <= 0) b->cfg.pool_paths = 1 << 21;
   if (b->cfg.rounds_per_launch <= 0) b->cfg.rounds_per_launch = 8;
@@ -1066,7 +1090,9 @@ int yc_batch_run(yc_batch* b, int max_launches, int* unfinished) {
     if (b->stack_cap <= 0) b->stack_cap = b->cfg.stack_cap > 0 ? b->cfg.stack_cap : 32;
     b->grid_c = yc::batch_trace_grid(false, b->stack_cap, b->wide == 1);
     b->grid_a = yc::batch_trace_grid(true, b->stack_cap, b->wide == 1);
-    if (b->grid_c <= 0 || b->grid_a <= 0) return fail(YC_E_LAUNCH, "batch trace kernel cannot be resident");
+    b->grid_m = yc::batch_trace_mixed_grid(b->stack_cap, b->wide == 1);
+    if (b->grid_c <= 0 || b->grid_a <= 0 || b->grid_m <= 0)
+      return fail(YC_E_LAUNCH, "batch trace kernel cannot be resident");
     b->started = true;
   }
   YC_CUDA(cudaEventRecord(c->ev0, c->stream));

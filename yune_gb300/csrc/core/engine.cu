@@ -340,6 +340,43 @@ __global__ void __launch_bounds__(TRACE_TB) k_batch_trace(const BatchJob* jobs, 
   trace_loop<ANY, WIDE>(src, *count, work, stack_cap, st);
 }
 
+// both queues of a round: closest-hit entries first, then any-hit
+struct BatchMixedSrc {
+  const BatchJob* jobs;
+  const int2* job_pass;
+  const int* __restrict__ q_closest;
+  const int* __restrict__ q_any;
+  int nc;
+  const float4* __restrict__ ro;
+  const float4* __restrict__ rd;
+  float4* hit;
+  __device__ __forceinline__ int slot(int e, bool any) const { return any ? q_any[e - nc] : q_closest[e]; }
+  __device__ __forceinline__ const DevScene& begin(int e, bool any, RayIn& r) {
+    const int q = slot(e, any);
+    const float4 o = ro[q];
+    const float4 d = rd[q];
+    r = RayIn{o.x, o.y, o.z, o.w, d.x, d.y, d.z};
+    return jobs[job_pass[q].x].pp.sc;
+  }
+  __device__ __forceinline__ void end(int e, bool any, const HitOut& h) {
+    const int q = slot(e, any);
+    hit[q] = any ? make_float4(h.tri >= 0 ? 1.0f : 0.0f, 0.0f, 0.0f, 0.0f)
+                 : make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+  }
+};
+
+template <bool WIDE>
+__global__ void __launch_bounds__(TRACE_TB) k_batch_trace_mixed(const BatchJob* jobs, const int2* job_pass,
+                                                                const int* __restrict__ q_closest,
+                                                                const int* __restrict__ q_any,
+                                                                RoundCounters* rc, const float4* __restrict__ ro,
+                                                                const float4* __restrict__ rd, float4* hit,
+                                                                int stack_cap, DevStats* st) {
+  const int nc = rc->n_closest;
+  BatchMixedSrc src{jobs, job_pass, q_closest, q_any, nc, ro, rd, hit};
+  trace_loop_mixed<WIDE>(src, nc, nc + rc->n_any, &rc->work_closest, stack_cap, st);
+}
+
 static size_t batch_smem(int cap) { return (size_t)TRACE_TB * 2 * cap * sizeof(int); }
 
 template <class K>
@@ -356,6 +393,24 @@ int batch_trace_grid(bool any_hit, int stack_cap, bool wide) {
   const size_t smem = batch_smem(stack_cap);
   if (wide) return any_hit ? batch_grid_of(k_batch_trace<true, true>, smem) : batch_grid_of(k_batch_trace<false, true>, smem);
   return any_hit ? batch_grid_of(k_batch_trace<true, false>, smem) : batch_grid_of(k_batch_trace<false, false>, smem);
+}
+
+int batch_trace_mixed_grid(int stack_cap, bool wide) {
+  const size_t smem = batch_smem(stack_cap);
+  return wide ? batch_grid_of(k_batch_trace_mixed<true>, smem) : batch_grid_of(k_batch_trace_mixed<false>, smem);
+}
+
+int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, const int2* job_pass, const int* q_closest,
+                             const int* q_any, RoundCounters* rc, const float4* ro, const float4* rd, float4* hit,
+                             DevStats* st, int stack_cap, int grid_blocks, cudaStream_t s) {
+  const size_t smem = batch_smem(stack_cap);
+  if (wide)
+    k_batch_trace_mixed<true><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, q_closest, q_any, rc, ro, rd, hit,
+                                                                  stack_cap, st);
+  else
+    k_batch_trace_mixed<false><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, q_closest, q_any, rc, ro, rd, hit,
+                                                                   stack_cap, st);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launch_batch_trace(bool any_hit, bool wide, const BatchJob* jobs, const int2* job_pass, const int* queue,

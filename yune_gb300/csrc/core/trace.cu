@@ -48,6 +48,41 @@ __global__ void __launch_bounds__(TRACE_TB) k_trace_paths(DevScene sc, const int
   trace_loop<ANY, WIDE>(src, *count, work, stack_cap, st);
 }
 
+// both queues of a round in one launch: closest-hit entries first, then any-hit
+struct PathMixedSrc {
+  const DevScene* sc;
+  const int* __restrict__ q_closest;
+  const int* __restrict__ q_any;
+  int nc;
+  const float4* __restrict__ ro;
+  const float4* __restrict__ rd;
+  float4* hit;
+  __device__ __forceinline__ int slot(int e, bool any) const { return any ? q_any[e - nc] : q_closest[e]; }
+  __device__ __forceinline__ const DevScene& begin(int e, bool any, RayIn& r) {
+    const int q = slot(e, any);
+    const float4 o = ro[q];
+    const float4 d = rd[q];
+    r = RayIn{o.x, o.y, o.z, o.w, d.x, d.y, d.z};
+    return *sc;
+  }
+  __device__ __forceinline__ void end(int e, bool any, const HitOut& h) {
+    const int q = slot(e, any);
+    hit[q] = any ? make_float4(h.tri >= 0 ? 1.0f : 0.0f, 0.0f, 0.0f, 0.0f)
+                 : make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+  }
+};
+
+template <bool WIDE>
+__global__ void __launch_bounds__(TRACE_TB) k_trace_paths_mixed(DevScene sc, const int* __restrict__ q_closest,
+                                                                const int* __restrict__ q_any, RoundCounters* rc,
+                                                                const float4* __restrict__ ro,
+                                                                const float4* __restrict__ rd, float4* hit,
+                                                                int stack_cap, DevStats* st) {
+  const int nc = rc->n_closest;
+  PathMixedSrc src{&sc, q_closest, q_any, nc, ro, rd, hit};
+  trace_loop_mixed<WIDE>(src, nc, nc + rc->n_any, &rc->work_closest, stack_cap, st);
+}
+
 // traceRay (udpt.cl:240-286) on explicit rays of 9 floats: light loop, then the BVH.
 template <bool ANY>
 struct RaySrc {
@@ -127,6 +162,23 @@ int launch_trace(const DevScene& sc, bool any_hit, const int* queue, const int* 
     k_trace_paths<false, true><<<grid_blocks, TRACE_TB, smem, s>>>(sc, queue, count, work, ro, rd, hit, cap, st);
   else
     k_trace_paths<false, false><<<grid_blocks, TRACE_TB, smem, s>>>(sc, queue, count, work, ro, rd, hit, cap, st);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+int trace_mixed_grid_blocks(int depth, bool wide) {
+  const size_t smem = smem_for(stack_cap_for(depth));
+  return wide ? resident_grid(k_trace_paths_mixed<true>, smem) : resident_grid(k_trace_paths_mixed<false>, smem);
+}
+
+int launch_trace_mixed(const DevScene& sc, const int* q_closest, const int* q_any, RoundCounters* rc,
+                       const float4* ro, const float4* rd, float4* hit, DevStats* st, int grid_blocks,
+                       cudaStream_t s) {
+  const int cap = stack_cap_for(sc.depth);
+  const size_t smem = smem_for(cap);
+  if (sc.wide)
+    k_trace_paths_mixed<true><<<grid_blocks, TRACE_TB, smem, s>>>(sc, q_closest, q_any, rc, ro, rd, hit, cap, st);
+  else
+    k_trace_paths_mixed<false><<<grid_blocks, TRACE_TB, smem, s>>>(sc, q_closest, q_any, rc, ro, rd, hit, cap, st);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

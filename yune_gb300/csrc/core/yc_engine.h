@@ -62,5 +62,11 @@ int launch_batch_trace(bool any_hit, bool wide, const BatchJob* jobs, const int2
                        const int* count, int* work, const float4* ro, const float4* rd, float4* hit, DevStats* st,
                        int stack_cap, int grid_blocks, cudaStream_t s);
 int batch_trace_grid(bool any_hit, int stack_cap, bool wide);
+// one launch over both queues of a round (closest-hit entries, then any-hit); the work
+// cursor is rc->work_closest
+int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, const int2* job_pass, const int* q_closest,
+                             const int* q_any, RoundCounters* rc, const float4* ro, const float4* rd, float4* hit,
+                             DevStats* st, int stack_cap, int grid_blocks, cudaStream_t s);
+int batch_trace_mixed_grid(int stack_cap, bool wide);
 
 }  // namespace yc

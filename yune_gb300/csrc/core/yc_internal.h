@@ -81,6 +81,12 @@ int launch_tail(const PassParams& pp, const PathState& ps, const int* in_closest
 int launch_trace_rays(const DevScene& sc, bool any_hit, const float* rays9, int n, int* tri_out, float* t_out,
                       int* work, DevStats* st, cudaStream_t s);
 int trace_grid_blocks(bool any_hit, int depth, bool wide);
+// one launch over both queues of a round (closest-hit entries, then any-hit); the work
+// cursor is rc->work_closest
+int launch_trace_mixed(const DevScene& sc, const int* q_closest, const int* q_any, RoundCounters* rc,
+                       const float4* ro, const float4* rd, float4* hit, DevStats* st, int grid_blocks,
+                       cudaStream_t s);
+int trace_mixed_grid_blocks(int depth, bool wide);
 int l2_read_gbs(size_t bytes, int iters, cudaStream_t s, double* gbs);
 
 }  // namespace yc

@@ -88,4 +88,64 @@ __device__ __forceinline__ void trace_loop(Src& src, int n, int* work, int stack
   flush_counts<ANY>(st, rays, wc, overflow);
 }
 
+// The same loop over both queues of a round in one launch: entries [0, nc) are the
+// closest-hit rays, [nc, n) the any-hit rays (Src::begin and Src::end take the entry and
+// its kind). One launch over all of a round's rays keeps its warps refilling for longer
+// than two launches over half of them each: the lanes a warp leaves idle once the work
+// list runs dry are a smaller share of the launch. Each lane counts its walk's work
+// under its ray's kind.
+template <bool WIDE, class Src>
+__device__ __forceinline__ void trace_loop_mixed(Src& src, int nc, int n, int* work, int stack_cap, DevStats* st) {
+  extern __shared__ int smem[];
+  int* stack = smem + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  unsigned long long overflow = 0;
+  WalkCount wc, wc_ext, wc_any;   // the current ray's walk, and the totals per kind
+  unsigned rays_ext = 0, rays_any = 0;
+  Walk w;
+  int e_cur = -1;
+  bool any = false;
+  bool more = true;
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xffffffffu, e_cur < 0);
+    if (more && (__popc(idle) >= REFILL_AT || idle == 0xffffffffu)) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(work, __popc(idle));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + __popc(idle) >= n) more = false;
+      if (e_cur < 0) {
+        const int e = base + __popc(idle & ((1u << lane) - 1));
+        if (e < n) {
+          e_cur = e;
+          any = e >= nc;
+          RayIn r;
+          const DevScene& sc = src.begin(e, any, r);
+          walk_begin(sc, r, w);
+          if (any) ++rays_any; else ++rays_ext;
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, e_cur >= 0) == 0) {
+      if (!more) break;
+      continue;
+    }
+    if (e_cur >= 0) {
+      bool of = false;
+      bool done = (w.link == LINK_NONE) || walk_step_k<WIDE>(w, any, stack, TRACE_TB, stack_cap, wc, of);
+      if (of) ++overflow;
+      if (done) {
+        HitOut h;
+        h.t = w.best; h.u = w.bu; h.v = w.bv; h.tri = w.best_tri;
+        src.end(e_cur, any, h);
+        if (any) { wc_any.nodes += wc.nodes; wc_any.tris += wc.tris; }
+        else { wc_ext.nodes += wc.nodes; wc_ext.tris += wc.tris; }
+        wc.nodes = 0; wc.tris = 0;
+        e_cur = -1;
+      }
+    }
+  }
+  flush_counts<false>(st, rays_ext, wc_ext, overflow);
+  flush_counts<true>(st, rays_any, wc_any, 0ull);
+}
+
 }  // namespace yc

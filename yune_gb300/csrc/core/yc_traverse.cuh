@@ -154,9 +154,8 @@ __device__ __forceinline__ void walk_begin(const DevScene& sc, const RayIn& r, W
 }
 
 // Triangles of one leaf (the reference's vert_list run, yc_scene.h); returns true when
-// an any-hit walk has found its hit.
-template <bool ANY>
-__device__ __forceinline__ bool walk_leaf(Walk& w, int link, WalkCount& wc) {
+// an any-hit walk (any = true) has found its hit.
+__device__ __forceinline__ bool walk_leaf(Walk& w, int link, WalkCount& wc, bool any) {
   const int enc = ~link;
   const int count = enc & 15;
   const float4* tp = w.tris + 3 * (size_t)(enc >> 4);
@@ -172,7 +171,7 @@ __device__ __forceinline__ bool walk_leaf(Walk& w, int link, WalkCount& wc) {
       w.bv = th.v;
       w.best_tri = __float_as_int(a.w);
       w.best_rank = __float_as_int(b.w);
-      if (ANY) return true;
+      if (any) return true;
     }
   }
   return false;
@@ -300,11 +299,13 @@ __device__ __forceinline__ int visit4(Walk& w, int link, int* stack, int stride,
 // stack bound was reached (the walk then ends early). Leaves are kept aside before the
 // hits inside them lower the culling distance, so the walk may open a few more boxes
 // than a leaf-first order would; it never skips one that can hold a closer hit.
-template <bool ANY, bool WIDE>
-__device__ __forceinline__ bool walk_step(Walk& w, int* stack, int stride, int stack_cap, WalkCount& wc,
-                                          bool& overflow) {
+// `any` selects the any-hit walk (it stops at the first hit); callers that know the kind
+// at compile time use walk_step<ANY, WIDE>, the mixed trace loop passes it per lane.
+template <bool WIDE>
+__device__ __forceinline__ bool walk_step_k(Walk& w, bool any, int* stack, int stride, int stack_cap, WalkCount& wc,
+                                            bool& overflow) {
   // (an any-hit walk keeps its segment length until it stops: nothing to check again)
-  int link = ANY ? w.link : walk_recheck(w, w.link, stack, stride);
+  int link = any ? w.link : walk_recheck(w, w.link, stack, stride);
   int leaf = LINK_NONE;
   while (link >= 0 && link != LINK_NONE) {
     link = WIDE ? visit4(w, link, stack, stride, stack_cap, wc, overflow)
@@ -320,9 +321,9 @@ __device__ __forceinline__ bool walk_step(Walk& w, int* stack, int stride, int s
     link = walk_pop(w, stack, stride);
   }
   while (leaf != LINK_NONE) {
-    if (walk_leaf<ANY>(w, leaf, wc)) { w.sp = 0; w.link = LINK_NONE; return true; }
+    if (walk_leaf(w, leaf, wc, any)) { w.sp = 0; w.link = LINK_NONE; return true; }
     leaf = LINK_NONE;
-    if (!ANY) link = walk_recheck(w, link, stack, stride);
+    if (!any) link = walk_recheck(w, link, stack, stride);
     if (link < 0 && link != LINK_NONE) {   // a second leaf met by the speculative walk
       leaf = link;
       link = walk_pop(w, stack, stride);
@@ -330,6 +331,12 @@ __device__ __forceinline__ bool walk_step(Walk& w, int* stack, int stride, int s
   }
   w.link = link;
   return link == LINK_NONE;
+}
+
+template <bool ANY, bool WIDE>
+__device__ __forceinline__ bool walk_step(Walk& w, int* stack, int stride, int stack_cap, WalkCount& wc,
+                                          bool& overflow) {
+  return walk_step_k<WIDE>(w, ANY, stack, stride, stack_cap, wc, overflow);
 }
 
 }  // namespace yc
