@@ -159,45 +159,67 @@ def scene_for(name):
     return scenes.CONFIGS[name]()
 
 
-def cpu_reference(scene, seeds, seconds, want_rays=True):
+def cpu_reference(scene, seeds, seconds, want_rays=True, band=0):
     """Times the reference kernel source (compiled as C++) on bands of rows of the frame
     with all host threads; rays counted by the oracle on the same band (same algorithm,
     bit-identical results). Falls back to the oracle port when the compiled reference is
-    not available."""
+    not available. band = 0: H/64 rows per band from the top of the frame; band > 0:
+    bands of that many rows spread over the frame (a stride coprime to its height)."""
     from oracle import oracle_py as O
     W, H = scene.width, scene.height
     cfg = dict(scene.cfg)
+    bdpt = cfg.get("integrator", 0) == 1
     threads = os.cpu_count() or 1
     use_ref = O.ref() is not None
     kind = "reference" if use_ref else "port"
     note = ""
-    if use_ref and (cfg.get("brdf_model", 0) or cfg.get("mis_lobe_fix", 0)):
+    if bdpt:
+        bounces = int(cfg.get("bdpt_bounces", 20))
+        variant = {(20, 1): "bdpt20", (8, 1): "bdpt8", (8, 4): "bdpt8_l4"}.get((bounces, len(scene.lights)))
+        if use_ref and variant is None:
+            use_ref, kind = False, "port"
+        note = "; bdpt.cl, %d vertices per subpath, %d lights" % (bounces, len(scene.lights))
+    elif use_ref and (cfg.get("brdf_model", 0) or cfg.get("mis_lobe_fix", 0)):
         # udpt.cl has neither the Oren-Nayar term nor the lobe fix: it runs its nearest
         # variant (Lambert, reference MIS), and the oracle counts the rays of that variant
         cfg["brdf_model"] = 0
         cfg["mis_lobe_fix"] = 0
         note = "; udpt.cl with -DMIS (Lambert diffuse, no lobe fix)"
     acc = np.zeros((H, W, 4), np.float32)
-    band = max(1, H // 64)
+    if band <= 0:
+        band = max(1, H // 64)
+        starts = list(range(0, H, band))
+    else:
+        nb = (H + band - 1) // band
+        step = next(q for q in range(nb // 3 + 1, nb + 1) if np.gcd(q, nb) == 1) if nb > 2 else 1
+        starts = [((i * step) % nb) * band for i in range(nb)]
+
+    def one(k, r, a):
+        if bdpt:
+            if use_ref:
+                O.ref_render(scene, a, seeds[k % len(seeds)], 1, variant, 0, 0, threads=threads, rows=r)
+                return None
+            return O.render_bdpt(scene, a, seeds[k % len(seeds)], 1, bounces, threads=threads, rows=r)
+        if use_ref:
+            O.ref_render(scene, a, seeds[k % len(seeds)], 1, "udpt_mis" if cfg["mis"] else "udpt_a",
+                         cfg["rr_threshold"], cfg["max_depth"], threads=threads, rows=r)
+            return None
+        return O.render(scene, a, seeds[k % len(seeds)], 1, cfg, threads=threads, rows=r)
+
     rows_done, t_total, rays = 0, 0.0, 0
-    y = 0
-    k = 0
-    while t_total < seconds and y < H:
+    for k, y in enumerate(starts):
+        if t_total >= seconds:
+            break
         r = (y, min(H, y + band))
         t0 = time.perf_counter()
-        if use_ref:
-            O.ref_render(scene, acc, seeds[k % len(seeds)], 1, "udpt_mis" if cfg["mis"] else "udpt_a",
-                         cfg["rr_threshold"], cfg["max_depth"], threads=threads, rows=r)
-        else:
-            c = O.render(scene, acc, seeds[k % len(seeds)], 1, cfg, threads=threads, rows=r)
-        dt = time.perf_counter() - t0
-        t_total += dt
-        if use_ref and want_rays:
-            acc2 = np.zeros_like(acc)
-            c = O.render(scene, acc2, seeds[k % len(seeds)], 1, cfg, threads=threads, rows=r)
-        rays += c["rays"]
+        c = one(k, r, acc)
+        t_total += time.perf_counter() - t0
+        if c is None and want_rays:   # the oracle counts the rays of the same band
+            use_ref_saved, use_ref = use_ref, False
+            c = one(k, r, np.zeros_like(acc))
+            use_ref = use_ref_saved
+        rays += c["rays"] if c else 0
         rows_done += r[1] - r[0]
-        y = r[1]
     value = rays / t_total / 1e6 if t_total > 0 else 0.0
     return {"value": value, "unit": METRIC, "cores": threads, "kind": kind,
             "sample": "%d of %d rows x %d px, 1 pass, %.1f s%s" % (rows_done, H, W, t_total, note),
@@ -205,12 +227,12 @@ def cpu_reference(scene, seeds, seconds, want_rays=True):
 
 
 def run_reference(args, rank, ws, dist):
+    if rank != 0:
+        return
     scene = scene_for(args.config)
     from yune_gb300 import scenes
     seeds = scenes.pass_seeds(0, args.steps + args.warmup)
-    if rank != 0:
-        return
-    cb = cpu_reference(scene, seeds, args.cpu_seconds)
+    cb = cpu_reference(scene, seeds, args.cpu_seconds, band=1 if args.config == "c4" else 0)
     cfg = {"workload": "%s: %d tris, %dx%d, cfg %s" % (args.config, scene.n_tri, scene.width, scene.height,
                                                       json.dumps(scene.cfg, sort_keys=True)),
            "spp_total": scene.spp}
@@ -423,6 +445,103 @@ def run_ours(args, rank, local, ws, dist):
     print(json.dumps(line))
 
 
+def run_c4(args, rank, local, ws, dist):
+    """The stress configuration: 10M triangles, 3840x2160, naive BDPT with 8 vertices per
+    subpath and four lights, through yc_render_pass (the drop-in call), one pass per
+    step. The node and triangle set (about 0.7 GB) is far larger than L2, so the
+    traversal kernel's roofline is the HBM copy bandwidth."""
+    from yune_gb300 import scenes
+    from yune_gb300.core import Renderer
+    t0 = time.perf_counter()
+    scene = scenes.c4()
+    build_s = time.perf_counter() - t0
+    K, Wm = args.steps, args.warmup
+    seeds = scenes.pass_seeds(0, Wm + K + args.e2e_steps)
+    W, H = scene.width, scene.height
+    r = Renderer(local)
+    r.set_tree_mode(args.tree)
+    r.set_mixed_trace(args.mixed)
+    t0 = time.perf_counter()
+    sid = r.upload(scene)
+    r.synchronize()
+    upload_s = time.perf_counter() - t0
+    scene_bytes = r.scene_bytes(sid)
+    r.set_camera(scene.cam)
+    l2 = r.measure_l2_gbs(48 << 20, 20)
+    pk, pk_kind = peaks()
+    aid = r.alloc_accum(W, H)
+    for k in range(Wm):
+        r.render(sid, aid, seeds[k], reset=1 if k == 0 else 0, cfg=scene.cfg)
+    r.synchronize()
+    r.reset_stats()
+    r.set_profiling(True)
+    if dist:
+        dist.barrier()
+    ms = 0.0
+    with Clocks(local) as clk:
+        for k in range(K):
+            r.flush_l2(256 << 20)
+            r.render(sid, aid, seeds[Wm + k], reset=0, cfg=scene.cfg)
+            ms += r.last_pass_ms()
+    r.synchronize()
+    st = r.stats()
+    kt = r.kernel_times()
+    r.set_profiling(False)
+    # e2e through the C-ABI with host buffers: camera in, tonemapped frame out per step
+    r.reset_stats()
+    t0 = time.perf_counter()
+    for k in range(args.e2e_steps):
+        r.set_camera(scene.cam)
+        r.render(sid, aid, seeds[Wm + K + k], reset=0, cfg=scene.cfg)
+        r.tonemap(aid)
+    e2e_s = time.perf_counter() - t0
+    e2e_rays = r.stats()["rays"]
+    img = r.read_accum(aid)
+    t_s, rays = _reduce(dist, ms / 1e3, st["rays"])
+    e2e_s, e2e_rays = _reduce(dist, e2e_s, e2e_rays)
+    if rank != 0:
+        r.close()
+        return
+    roof = _trace_roofline(st, kt, l2, pk, pk_kind, "k_trace_paths_mixed (closest + any-hit rays)",
+                           "k_trace_paths<closest> (extend)")
+    # bound: the node and triangle set does not fit in L2
+    roof.update({"bound": "hbm", "peak": pk.get("hbm_gbs"), "frac": roof["hbm_frac"], "peak_source": pk_kind,
+                 "l2_peak": l2, "l2_frac": roof["achieved"] / l2 if l2 else None})
+    for k in ("hbm_peak", "hbm_frac", "hbm_peak_source"):
+        roof.pop(k, None)
+    launches = int(kt["raygen_launches"] + kt["extend_launches"] + kt["occlusion_launches"] + kt["trace_launches"]
+                   + kt["logic_launches"] + kt["tail_launches"])
+    line = {
+        "metric": METRIC, "value": rays / t_s / 1e6, "unit": METRIC, "n_gpus": ws, "steps": K, "warmup": Wm,
+        "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": "c4 stress: 40x40 grid of displaced level-4/5 icospheres, %d tris, mixed materials, "
+                               "4 quad lights, %dx%d, naive BDPT with %d vertices per subpath, 1 spp per step"
+                               % (scene.n_tri, W, H, scene.cfg["bdpt_bounces"]),
+                   "spp_total": scene.spp, "tree_mode": args.tree, "scene_device_bytes": scene_bytes,
+                   "host_build_s": build_s, "upload_s": upload_s,
+                   "l2": "L2 flushed before each step; the node and triangle set is larger than L2",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "samples_per_s": st["samples"] * (ws if dist else 1) / t_s,
+        "rays_per_sample": st["rays"] / max(1, st["samples"]),
+        "gpu_launches": launches,
+        "kernel_ms": {"raygen": kt["raygen_ms"], "trace": kt["trace_ms"], "extend": kt["extend_ms"],
+                      "occlusion": kt["occlusion_ms"], "logic": kt["logic_ms"], "rounds": kt["rounds"]},
+        "roofline": roof,
+        "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else 0.0, "unit": METRIC,
+                "h2d_bytes_per_step": 80 + 4, "d2h_bytes_per_step": W * H * 16, "steps": args.e2e_steps,
+                "path": "yc_set_camera + yc_render_pass + yc_tonemap to host"},
+        "clocks": clk.summary(), "stack_overflow": int(st["stack_overflow"]),
+        "image_mean": float(np.nanmean(img[..., :3])),
+        "image_error": "no FP64 reference for this scene (65,536 passes of the CPU oracle over 10M triangles "
+                       "is out of reach); the BDPT integrator's error is measured on c0_bdpt (--quality)",
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_reference(scene, seeds, args.cpu_seconds, band=1)
+    r.close()
+    print(json.dumps(line))
+
+
 def run_c2(args):
     """Mixed batch: every job rendered pass by pass (plain) and all jobs in one batch."""
     from yune_gb300 import autotune, scenes, workloads
@@ -615,6 +734,8 @@ def main():
     rank, local, ws, dist = dist_init(args)
     if args.impl == "reference":
         run_reference(args, rank, ws, dist)
+    elif args.config == "c4":
+        run_c4(args, rank, local, ws, dist)
     else:
         run_ours(args, rank, local, ws, dist)
     if dist:

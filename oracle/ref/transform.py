@@ -14,7 +14,11 @@ own arithmetic runs unchanged:
     wrapped in #ifndef so a variant can set them, and the GI loop bound 100000
     (udpt.cl:463) becomes YREF_MAX_DEPTH;
   * sampleLights gets an explicit `return -1;` where the reference falls off the end
-    of a non-void function.
+    of a non-void function;
+  * traverseBVH's candidate queue gets one spare entry: its loop checks the length only
+    before a node's two children are pushed (udpt.cl:298,315-319, bdpt.cl likewise), so
+    a full queue takes one write past its end, which the loop never reads. On the GPU
+    that write goes unnoticed; compiled as C++ it would overwrite the stack.
 Usage: python transform.py <in.cl> <out.inc>
 """
 import re
@@ -47,6 +51,7 @@ def transform(text: str) -> str:
     # is undefined and the optimiser may assume it never happens, so give it the value
     # the restatement documents: -1, no light.
     s = re.sub(r"(cumulative_weight \+= weight;\s*\}\s*)\}", r"\1    return -1;\n}", s)
+    s = re.sub(r"int\s+candidate_list\[HEAP_SIZE\]", "int candidate_list[HEAP_SIZE + 1]", s)
     return s
 
 

@@ -75,7 +75,7 @@ struct Tracer {
   static constexpr float INV_PI_F = 0.31830988618f;
   static constexpr float EPS_F = 0.0001f;
 
-  Tracer(const Scene<R>& s, const Config& c, Counters& k) : sc(s), cfg(c), cnt(k), queue(c.heap_size > 0 ? c.heap_size : 1) {}
+  Tracer(const Scene<R>& s, const Config& c, Counters& k) : sc(s), cfg(c), cnt(k), queue(c.heap_size > 0 ? c.heap_size + 1 : 2) {}
 
   static R draw(uint32_t& seed) { seed = ym::xor_shift(seed); return O::u01(seed); }
 
@@ -129,7 +129,10 @@ struct Tracer {
     return false;
   }
 
-  // traverseBVH, udpt.cl:288-324: breadth-first queue, no ordering, no distance cull
+  // traverseBVH, udpt.cl:288-324: breadth-first queue, no ordering, no distance cull.
+  // The loop checks the length only before a node's two children are pushed, so when
+  // the last free entry takes both, the second lands one past the end (udpt.cl:298,315-
+  // 319); the loop stops there and never reads it. The queue has that one spare entry.
   bool traverse(Ray<R>& ray, Hit<R>& hit) {
     const yc_bvh_node* bvh = sc.nodes;
     bool intersect = false;

@@ -203,6 +203,35 @@ def test_render_parity_bdpt(renderer, bounces, lights):
     assert st["samples"] == 40 * 32 * 2
 
 
+def test_c4_stress_scene_bdpt_parity(renderer):
+    """The stress scene itself (10,004,490 triangles, 8.5M reference nodes, four lights,
+    BDPT with 8 vertices per subpath) on a 32 x 18 crop of the frame, two passes: every
+    pixel and the ray counts against the oracle. The oracle's breadth-first queue is
+    raised so that no hit is dropped (the core's walk has no such limit)."""
+    s = scenes.c4(32, 18)
+    assert s.n_tri == 10_004_490
+    seeds = scenes.pass_seeds(44, 2)
+    sid = renderer.upload(s)
+    renderer.set_camera(s.cam)
+    aid = renderer.alloc_accum(32, 18)
+    renderer.reset_stats()
+    renderer.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+    gpu = renderer.read_accum(aid)
+    st = renderer.stats()
+    renderer.free_accum(aid)
+    renderer.release(sid)
+    ref = np.zeros((18, 32, 4), np.float32)
+    rays = 0
+    for k, sd in enumerate(seeds):
+        c = O.render_bdpt(s, ref, sd, 1 if k == 0 else 0, 8, heap_size=1 << 22)
+        assert c["heap_overflow"] == 0
+        rays += c["rays"]
+    assert st["stack_overflow"] == 0
+    assert _rel_bad(gpu, ref) == 0
+    assert np.array_equal(gpu[..., 3], ref[..., 3])
+    assert st["rays"] == rays
+
+
 @pytest.mark.parametrize("tree", [0, 2])
 def test_render_identical_across_tree_modes(renderer, tree):
     """Every interior hierarchy gives the reference's hits, so whole renders are the same

@@ -64,6 +64,12 @@ class Renderer:
         N.check(self.L.yc_scene_depth(self.h, sid, C.byref(d)), "yc_scene_depth")
         return d.value
 
+    def scene_bytes(self, sid):
+        """Bytes the scene holds on the device."""
+        b = C.c_uint64()
+        N.check(self.L.yc_scene_bytes(self.h, sid, C.byref(b)), "yc_scene_bytes")
+        return int(b.value)
+
     def release(self, sid):
         N.check(self.L.yc_release_scene(self.h, sid), "yc_release_scene")
 

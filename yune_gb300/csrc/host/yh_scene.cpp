@@ -8,6 +8,7 @@
 // the same seed gives the same scene on every host.
 #include "yune_host.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -16,15 +17,19 @@
 #include <utility>
 #include <vector>
 
+namespace {
+struct D3 { double x, y, z; };
+}  // namespace
+
 struct yh_scene {
   std::vector<yc_triangle> tris;
   std::vector<yc_material> mats;
   std::vector<yc_quad_light> lights;
+  // unit icosphere per subdivision level (vertices, faces), built on first use
+  std::map<int, std::pair<std::vector<D3>, std::vector<int>>> ico;
 };
 
 namespace {
-
-struct D3 { double x, y, z; };
 inline D3 operator+(D3 a, D3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
 inline D3 operator-(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 inline D3 operator*(D3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
@@ -198,9 +203,14 @@ extern "C" int yh_scene_add_icosphere(yh_scene* s, const float c[3], float r, in
                                       uint64_t seed, int mat_id) {
   if (!s || !c || level < 0 || level > 9 || !(r > 0)) return YH_E_INVALID;
   try {
-    std::vector<D3> v;
-    std::vector<int> f;
-    icosphere(level, v, f);
+    auto it = s->ico.find(level);
+    if (it == s->ico.end()) {
+      std::pair<std::vector<D3>, std::vector<int>> vf;
+      icosphere(level, vf.first, vf.second);
+      it = s->ico.emplace(level, std::move(vf)).first;
+    }
+    const std::vector<D3>& v = it->second.first;
+    const std::vector<int>& f = it->second.second;
     std::mt19937_64 g(seed);
     std::vector<D3> p(v.size()), n(v.size(), D3{0, 0, 0});
     const D3 cc{c[0], c[1], c[2]};
@@ -217,7 +227,8 @@ extern "C" int yh_scene_add_icosphere(yh_scene* s, const float c[3], float r, in
     } else {
       n = v;
     }
-    s->tris.reserve(s->tris.size() + f.size() / 3);
+    const size_t need = s->tris.size() + f.size() / 3;   // grow geometrically: many spheres append here
+    if (need > s->tris.capacity()) s->tris.reserve(std::max(need, 2 * s->tris.capacity()));
     for (size_t t = 0; t < f.size(); t += 3)
       push_tri(s, p[f[t]], p[f[t + 1]], p[f[t + 2]], n[f[t]], n[f[t + 1]], n[f[t + 2]], mat_id);
   } catch (const std::bad_alloc&) {

@@ -12,6 +12,9 @@ Configurations (sizes and spp of the benchmark workloads):
       bounce 3; leaf <= 10, 20 bins.
   c1  c0 plus a level-6 icosphere (81,920 tris, radius 0.35) of dielectric IOR 1.5;
       leaf <= 4; 1024x1024, 256 spp, at most 16 bounces, roulette after bounce 3.
+  c4  stress: 40 x 40 grid of displaced level-4/5 icospheres (10,004,480 tris) with mixed
+      materials on the Cornell floor, four quad lights; naive BDPT, 8 vertices per
+      subpath; 3840x2160, 128 spp; leaf <= 4.
 """
 import ctypes as C
 from dataclasses import dataclass, field
@@ -176,7 +179,41 @@ def c0_bdpt(width=512, height=512, spp=64, seed=0, bounces=8, lights=4):
                      default_cfg(integrator=1, mis=0, bdpt_bounces=bounces), "c0_bdpt")
 
 
-CONFIGS = {"c0": c0, "c1": c1, "c0_bdpt": c0_bdpt}
+def c4(width=3840, height=2160, spp=128, seed=0, grid=40, n_level5=118, bounces=8):
+    """The stress configuration: a flattened grid x grid array of displaced icospheres on
+    the floor of the Cornell box (walls only), four quad lights under the ceiling, naive
+    BDPT with `bounces` vertices per subpath.
+
+    Sphere levels: `n_level5` seeded spheres of level 5 (20,480 triangles) and the rest of
+    level 4 (5,120), so the 40 x 40 grid holds 10,004,480 sphere triangles, the stated
+    10M (a grid of 1,600 level-6 spheres would hold 131M). Each sphere: radius 0.4 of the
+    grid pitch, vertices moved radially by U(-5%, 5%) of the radius, one material drawn
+    uniformly from {Oren-Nayar, modified Phong with exponent in [10, 200], dielectric
+    with IOR in [1.3, 1.7]}. All draws come from numpy's PCG64 stream of `seed`."""
+    from .workloads import random_material
+    rng = np.random.default_rng(seed)
+    b = Builder().cornell(seed=seed, boxes=False)
+    pitch = 0.9 / grid
+    r = 0.4 * pitch
+    big = set(rng.choice(grid * grid, size=min(n_level5, grid * grid), replace=False).tolist())
+    for i in range(grid):
+        for j in range(grid):
+            k = i * grid + j
+            mid = b.add_material(random_material(rng))
+            c = (-0.45 + (j + 0.5) * pitch, -0.5 + r * 1.06, -0.45 + (i + 0.5) * pitch)
+            b.icosphere(c, r, 5 if k in big else 4, mid, disp=0.05, seed=seed * 1000003 + k)
+    tris, mats, ls = b.arrays()
+    ls = four_lights(ls)
+    nodes, depth = build_bvh(tris, 20, 4)
+    look = np.array([0.0, -0.45, -1.0])
+    look /= np.linalg.norm(look)
+    up = np.array([0.0, -look[2], look[1]])
+    cam = camera(eye=(0.0, 0.2, 1.3), side=(1.0, 0.0, 0.0), up=tuple(up), look=tuple(look), fov=50.0)
+    return SceneData(tris, mats, ls, nodes, depth, cam, width, height, spp,
+                     default_cfg(integrator=1, mis=0, bdpt_bounces=bounces), "c4")
+
+
+CONFIGS = {"c0": c0, "c1": c1, "c0_bdpt": c0_bdpt, "c4": c4}
 
 
 def pass_seeds(seed, n):
