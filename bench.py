@@ -74,6 +74,9 @@ def parse():
                                                          "(-1 auto, 0 off)")
     ap.add_argument("--mixed", type=int, default=1,
                     help="1: a round's closest-hit and any-hit rays share one traversal launch; 0: one launch each")
+    ap.add_argument("--ray-sort", type=int, default=32,
+                    help="sort key of a round's rays: origin bits * 10 + direction bits per axis (0: queue order)")
+    ap.add_argument("--ray-sort-min", type=int, default=65536, help="rounds with fewer rays are not sorted")
     ap.add_argument("--tree", type=int, default=1,
                     help="interior hierarchy: 0 reference nodes, 1 binary SAH over the reference leaves, 2 four-wide")
     return ap.parse_args()
@@ -306,6 +309,7 @@ def run_ours(args, rank, local, ws, dist):
     r.set_tree_mode(args.tree)
     r.set_tail_paths(args.tail)
     r.set_mixed_trace(args.mixed)
+    r.set_ray_sort(args.ray_sort // 10, args.ray_sort % 10, args.ray_sort_min)
     sid = r.upload(scene)
     r.set_camera(scene.cam)
     l2 = r.measure_l2_gbs(48 << 20, 20)
@@ -399,7 +403,8 @@ def run_ours(args, rank, local, ws, dist):
         r.close()
         return
     launches = int(kt_en["raygen_launches"] + kt_en["extend_launches"] + kt_en["occlusion_launches"]
-                   + kt_en["trace_launches"] + kt_en["logic_launches"] + kt_en["sort_launches"])
+                   + kt_en["trace_launches"] + kt_en["logic_launches"] + 3 * kt_en["sort_launches"]
+                   + 3 * kt_en["raysort_launches"])
     line = {
         "metric": METRIC, "value": rays / t_s / 1e6, "unit": METRIC, "n_gpus": ws, "steps": K,
         "warmup": Wm, "ms_per_step": en_ms / K, "higher_is_better": True, "scaling": "weak",
@@ -415,14 +420,16 @@ def run_ours(args, rank, local, ws, dist):
         "rays_per_sample": st_en["rays"] / max(1, st_en["samples"]),
         "gpu_launches": launches,
         "engine_equal_to_per_pass": same,
-        "kernel_ms": {"fill": kt_en["raygen_ms"], "trace": kt_en["trace_ms"], "extend": kt_en["extend_ms"],
+        "kernel_ms": {"fill": kt_en["raygen_ms"], "raysort": kt_en["raysort_ms"], "trace": kt_en["trace_ms"],
+                      "extend": kt_en["extend_ms"],
                       "occlusion": kt_en["occlusion_ms"], "sort": kt_en["sort_ms"], "logic": kt_en["logic_ms"],
                       "rounds": kt_en["rounds"]},
         "roofline": _trace_roofline(st_enp, kt_en, l2, pk, pk_kind, "k_batch_trace_mixed (closest + any-hit rays)",
                                     "k_batch_trace<closest> (extend)"),
         "per_pass": {"value": pp_rays / pp_s / 1e6, "ms_per_step": pp_ms / K, "unit": METRIC,
                      "note": "yc_render_pass per pass (the drop-in call), L2 flushed before each pass",
-                     "kernel_ms": {"raygen": kt_pp["raygen_ms"], "trace": kt_pp["trace_ms"],
+                     "kernel_ms": {"raygen": kt_pp["raygen_ms"], "raysort": kt_pp["raysort_ms"],
+                                   "trace": kt_pp["trace_ms"],
                                    "extend": kt_pp["extend_ms"], "occlusion": kt_pp["occlusion_ms"],
                                    "logic": kt_pp["logic_ms"], "tail": kt_pp["tail_ms"], "rounds": kt_pp["rounds"]},
                      "roofline": _trace_roofline(st_pp, kt_pp, l2, pk, pk_kind,
@@ -461,6 +468,7 @@ def run_c4(args, rank, local, ws, dist):
     r = Renderer(local)
     r.set_tree_mode(args.tree)
     r.set_mixed_trace(args.mixed)
+    r.set_ray_sort(args.ray_sort // 10, args.ray_sort % 10, args.ray_sort_min)
     t0 = time.perf_counter()
     sid = r.upload(scene)
     r.synchronize()
@@ -510,7 +518,7 @@ def run_c4(args, rank, local, ws, dist):
     for k in ("hbm_peak", "hbm_frac", "hbm_peak_source"):
         roof.pop(k, None)
     launches = int(kt["raygen_launches"] + kt["extend_launches"] + kt["occlusion_launches"] + kt["trace_launches"]
-                   + kt["logic_launches"] + kt["tail_launches"])
+                   + kt["logic_launches"] + kt["tail_launches"] + 3 * kt["raysort_launches"])
     line = {
         "metric": METRIC, "value": rays / t_s / 1e6, "unit": METRIC, "n_gpus": ws, "steps": K, "warmup": Wm,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
@@ -525,7 +533,8 @@ def run_c4(args, rank, local, ws, dist):
         "samples_per_s": st["samples"] * (ws if dist else 1) / t_s,
         "rays_per_sample": st["rays"] / max(1, st["samples"]),
         "gpu_launches": launches,
-        "kernel_ms": {"raygen": kt["raygen_ms"], "trace": kt["trace_ms"], "extend": kt["extend_ms"],
+        "kernel_ms": {"raygen": kt["raygen_ms"], "raysort": kt["raysort_ms"], "trace": kt["trace_ms"],
+                      "extend": kt["extend_ms"],
                       "occlusion": kt["occlusion_ms"], "logic": kt["logic_ms"], "rounds": kt["rounds"]},
         "roofline": roof,
         "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else 0.0, "unit": METRIC,
@@ -551,6 +560,7 @@ def run_c2(args):
     r = Renderer(0)
     r.set_tree_mode(args.tree)
     r.set_mixed_trace(args.mixed)
+    r.set_ray_sort(args.ray_sort // 10, args.ray_sort % 10, args.ray_sort_min)
     sids = [r.upload(s) for s in jobs]
     seeds = [scenes.pass_seeds(1000 + i, s.spp) for i, s in enumerate(jobs)]
     px = sum(s.width * s.height for s in jobs)

@@ -91,6 +91,8 @@ typedef struct yc_kernel_times {
   double trace_ms;             /* one launch over a round's closest-hit and any-hit rays
                                   (YC_OPT_MIXED_TRACE); extend_ms and occlusion_ms then stay 0 */
   uint64_t trace_launches;
+  double raysort_ms;           /* sort of a round's rays before the trace (YC_OPT_RAY_SORT) */
+  uint64_t raysort_launches;
 } yc_kernel_times;
 
 typedef struct yc_ctx yc_ctx;
@@ -227,7 +229,14 @@ enum {
    * any-hit (shadow, MIS) rays of a round share one launch; 0 = one launch each, the two
    * overlapping on two streams. Same results either way. Applies to later
    * yc_render_pass(es) calls and to batches created afterwards. */
-  YC_OPT_MIXED_TRACE = 3
+  YC_OPT_MIXED_TRACE = 3,
+  /* Order of a round's rays in the mixed traversal launch: a counting sort by the cell of
+   * the ray origin in the scene box and the cell of its direction, so that neighbouring
+   * lanes walk the same nodes. value = origin bits per axis * 10 + direction bits per axis
+   * (each 0..3, sum <= 5); 0 = rays in queue order. Default 32. Same results either way. */
+  YC_OPT_RAY_SORT = 4,
+  /* Rounds (and batch slot groups) with fewer rays than this are not sorted. Default 65536. */
+  YC_OPT_RAY_SORT_MIN = 5
 };
 int yc_set_option(yc_ctx* ctx, int option, int value);
 

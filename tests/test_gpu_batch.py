@@ -73,6 +73,32 @@ def test_batch_separate_trace_launches_match(groups):
         b.close()
 
 
+@pytest.mark.parametrize("groups", [1, 3])
+def test_batch_ray_sort_matches(groups):
+    """With every round's rays sorted by origin and direction cell (threshold 1), the
+    batch still gives the per-pass path's accumulators bit for bit."""
+    jobs = _jobs()
+    with Renderer(0) as r:
+        ids = [r.upload(s) for s, _ in jobs]
+        want = []
+        for (s, seeds), sid in zip(jobs, ids):
+            r.set_camera(s.cam)
+            aid = r.alloc_accum(s.width, s.height)
+            r.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+            want.append(r.read_accum(aid))
+        r.set_ray_sort(3, 2, min_rays=1)
+        b = Batch(r, pool_paths=4096, rounds_per_launch=4, use_graph=True, groups=groups)
+        accs = []
+        for (s, seeds), sid in zip(jobs, ids):
+            aid = r.alloc_accum(s.width, s.height)
+            accs.append(aid)
+            b.add_job(sid, aid, s.cam, seeds, s.cfg)
+        assert b.run() == 0
+        for aid, w in zip(accs, want):
+            assert np.array_equal(r.read_accum(aid).view(np.int32), w.view(np.int32))
+        b.close()
+
+
 def test_batch_jobs_added_while_running():
     """Serving: a job admitted after the batch started still renders exactly."""
     jobs = _jobs()

@@ -288,6 +288,37 @@ def test_render_identical_with_and_without_mixed_trace(renderer, tree):
         assert out[0][1][key] == out[1][1][key], key
 
 
+@pytest.mark.parametrize("key", [(3, 2), (1, 0), (0, 3)])
+def test_ray_sort_gives_the_same_pass(renderer, key):
+    """Sorting each round's rays by origin and direction cell before the trace (forced on
+    every round here) changes no bit and no ray count; both equal the oracle."""
+    s = scenes.c1(48, 40, level=5)
+    seeds = scenes.pass_seeds(17, 2)
+    sid = renderer.upload(s)
+    renderer.set_camera(s.cam)
+    out = []
+    for ob, db, min_rays in ((0, 0, 65536), (key[0], key[1], 1)):
+        renderer.set_ray_sort(ob, db, min_rays)
+        renderer.reset_stats()
+        renderer.set_profiling(True)
+        aid = renderer.alloc_accum(48, 40)
+        renderer.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+        out.append((renderer.read_accum(aid), renderer.stats(), renderer.kernel_times()))
+        renderer.set_profiling(False)
+        renderer.free_accum(aid)
+    renderer.set_ray_sort(3, 2, 65536)
+    renderer.release(sid)
+    assert out[0][2]["raysort_launches"] == 0 and out[1][2]["raysort_launches"] > 0
+    ref = np.zeros((40, 48, 4), np.float32)
+    for k, sd in enumerate(seeds):
+        O.render(s, ref, sd, 1 if k == 0 else 0, s.cfg)
+    for img, st, _ in out:
+        assert st["stack_overflow"] == 0
+        assert np.array_equal(img.view(np.int32), ref.view(np.int32))
+    for k in ("rays", "ext_rays", "any_rays", "traversed"):
+        assert out[0][1][k] == out[1][1][k], k
+
+
 @pytest.mark.parametrize("tree", [1, 2])
 def test_tail_kernel_gives_the_same_pass(renderer, tree):
     """Finishing the last paths a thread each (YC_OPT_TAIL) changes no bit of the pass and

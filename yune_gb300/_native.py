@@ -35,7 +35,8 @@ class KernelTimes(C.Structure):
                 ("logic_ms", C.c_double), ("raygen_launches", C.c_uint64), ("extend_launches", C.c_uint64),
                 ("occlusion_launches", C.c_uint64), ("logic_launches", C.c_uint64), ("rounds", C.c_uint64),
                 ("sort_ms", C.c_double), ("sort_launches", C.c_uint64), ("tail_ms", C.c_double),
-                ("tail_launches", C.c_uint64), ("trace_ms", C.c_double), ("trace_launches", C.c_uint64)]
+                ("tail_launches", C.c_uint64), ("trace_ms", C.c_double), ("trace_launches", C.c_uint64),
+                ("raysort_ms", C.c_double), ("raysort_launches", C.c_uint64)]
 
 
 class BatchCfg(C.Structure):

@@ -153,6 +153,13 @@ class Renderer:
         0: one launch each."""
         N.check(self.L.yc_set_option(self.h, 3, int(on)), "yc_set_option")
 
+    def set_ray_sort(self, origin_bits=3, dir_bits=2, min_rays=None):
+        """Sort key of a round's rays before the mixed traversal launch (0, 0: queue
+        order); rounds with fewer than min_rays rays stay unsorted."""
+        N.check(self.L.yc_set_option(self.h, 4, int(origin_bits) * 10 + int(dir_bits)), "yc_set_option")
+        if min_rays is not None:
+            N.check(self.L.yc_set_option(self.h, 5, int(min_rays)), "yc_set_option")
+
     def set_profiling(self, on=True):
         N.check(self.L.yc_set_profiling(self.h, int(on)), "yc_set_profiling")
 

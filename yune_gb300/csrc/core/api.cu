@@ -96,6 +96,13 @@ struct yc_ctx {
   int tree_mode = yc::TREE_SAH_OVER_LEAVES;
   int tail_paths = -1;   // YC_OPT_TAIL: -1 = one resident launch of the tail kernel, 0 = off
   int mixed_trace = 1;   // YC_OPT_MIXED_TRACE: one traversal launch per round for both ray kinds
+  int rs_ob = 3, rs_db = 2;       // YC_OPT_RAY_SORT: origin / direction bits per axis of the sort key
+  int rs_threshold = 65536;       // YC_OPT_RAY_SORT_MIN: rounds with fewer rays are not sorted
+  // ray sort of the per-pass path (raysort.cu)
+  DevBuf<unsigned> rs_keys, rs_hist, rs_cursor, rs_blk;
+  DevBuf<int> rs_sorted;
+  DevBuf<yc::RaySortCtl> rs_ctl;
+  size_t rs_cap = 0;
   // wavefront buffers, sized for the largest image seen
   size_t cap_paths = 0;
   DevBuf<int4> misc;
@@ -135,8 +142,27 @@ int ensure_paths(yc_ctx* c, size_t n) {
   return 0;
 }
 
+// key, histogram and sorted-list buffers of the per-pass ray sort, for n rays
+int ensure_raysort(yc_ctx* c, size_t n) {
+  if (!c->rs_hist.p) {
+    const size_t bins = (size_t)yc::raysort_bins(3, 2);   // the largest key allowed (16 bits)
+    YC_CUDA(c->rs_hist.alloc(bins));
+    YC_CUDA(c->rs_cursor.alloc(bins));
+    YC_CUDA(c->rs_blk.alloc(64));
+    YC_CUDA(c->rs_ctl.alloc(1));
+    YC_CUDA(cudaMemsetAsync(c->rs_hist.p, 0, c->rs_hist.bytes(), c->stream));
+    YC_CUDA(cudaMemsetAsync(c->rs_ctl.p, 0, sizeof(yc::RaySortCtl), c->stream));
+  }
+  if (n > c->rs_cap) {
+    YC_CUDA(c->rs_keys.alloc(n));
+    YC_CUDA(c->rs_sorted.alloc(n));
+    c->rs_cap = n;
+  }
+  return 0;
+}
+
 // event pairs around kernel launches (profiling only)
-enum { K_RAYGEN = 0, K_EXTEND = 1, K_OCCL = 2, K_LOGIC = 3, K_SORT = 4, K_TAIL = 5, K_TRACE = 6 };
+enum { K_RAYGEN = 0, K_EXTEND = 1, K_OCCL = 2, K_LOGIC = 3, K_SORT = 4, K_TAIL = 5, K_TRACE = 6, K_RAYSORT = 7 };
 cudaEvent_t next_event(yc_ctx* c) {
   if (c->ev_used == c->ev_pool.size()) {
     cudaEvent_t e;
@@ -178,6 +204,7 @@ void collect_events(yc_ctx* c) {
       case K_SORT: c->ktimes.sort_ms += ms; c->ktimes.sort_launches++; break;
       case K_TAIL: c->ktimes.tail_ms += ms; c->ktimes.tail_launches++; break;
       case K_TRACE: c->ktimes.trace_ms += ms; c->ktimes.trace_launches++; break;
+      case K_RAYSORT: c->ktimes.raysort_ms += ms; c->ktimes.raysort_launches++; break;
       default: c->ktimes.logic_ms += ms; c->ktimes.logic_launches++; break;
     }
   }
@@ -271,6 +298,13 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
   }
   YC_CUDA(cudaPeekAtLastError());
   const bool mixed = c->mixed_trace != 0;
+  const bool raysort = mixed && (c->rs_ob + c->rs_db) > 0 && c->rs_threshold > 0 && (size_t)W * H >= (size_t)c->rs_threshold;
+  yc::RaySortBufs rsb{};
+  if (raysort) {
+    if (int e = ensure_raysort(c, (size_t)W * H)) return e;
+    rsb = yc::RaySortBufs{c->rs_keys.p, c->rs_hist.p, c->rs_cursor.p, c->rs_blk.p, c->rs_sorted.p, c->rs_ctl.p,
+                          c->rs_ob, c->rs_db, c->rs_threshold};
+  }
   const int grid_c = yc::trace_grid_blocks(false, sc->dev.depth, sc->dev.wide != 0);
   const int grid_a = yc::trace_grid_blocks(true, sc->dev.depth, sc->dev.wide != 0);
   const int grid_m = mixed ? yc::trace_mixed_grid_blocks(sc->dev.depth, sc->dev.wide != 0) : 1;
@@ -292,8 +326,14 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     yc::RoundCounters* rout = rc + (1 - cur);
     int e1, e2;
     if (mixed) {   // both ray kinds of the round in one launch
+      if (raysort) {
+        KTimer kt(c, K_RAYSORT);
+        if (yc::launch_raysort(sc->dev, in_c, in_a, rin, ps.ro, ps.rd, rsb, c->logic_grid, c->stream))
+          return fail(YC_E_LAUNCH, std::string("ray sort: ") + cudaGetErrorString(cudaGetLastError()));
+      }
       KTimer kt(c, K_TRACE);
-      if (yc::launch_trace_mixed(sc->dev, in_c, in_a, rin, ps.ro, ps.rd, ps.hit, c->stats.p, grid_m, c->stream))
+      if (yc::launch_trace_mixed(sc->dev, in_c, in_a, rin, ps.ro, ps.rd, ps.hit, c->stats.p, grid_m, c->stream,
+                                 raysort ? rsb.sorted : nullptr, raysort ? rsb.ctl : nullptr))
         return fail(YC_E_LAUNCH, std::string("trace kernel: ") + cudaGetErrorString(cudaGetLastError()));
     }
     // otherwise the two traces of a round are independent: the any-hit one runs on the
@@ -732,6 +772,17 @@ int yc_set_option(yc_ctx* c, int option, int value) {
       if (value != 0 && value != 1) return fail(YC_E_INVALID, "mixed trace is 0 or 1");
       c->mixed_trace = value;
       return YC_OK;
+    case YC_OPT_RAY_SORT: {
+      const int ob = value / 10, db = value % 10;
+      if (value < 0 || ob > 3 || db > 3 || ob + db > 5) return fail(YC_E_INVALID, "ray sort key: origin bits * 10 + direction bits, sum <= 5");
+      c->rs_ob = ob;
+      c->rs_db = db;
+      return YC_OK;
+    }
+    case YC_OPT_RAY_SORT_MIN:
+      if (value < 0) return fail(YC_E_INVALID, "ray sort threshold must be >= 0");
+      c->rs_threshold = value;
+      return YC_OK;
     default:
       return fail(YC_E_INVALID, "unknown option");
   }
@@ -781,6 +832,9 @@ struct BatchGroup {
   DevBuf<int> free_stack;
   DevBuf<int> q[4];
   DevBuf<int> sort_keys, sorted;
+  DevBuf<unsigned> rs_keys, rs_hist, rs_cursor, rs_blk;   // ray sort before the trace (raysort.cu)
+  DevBuf<int> rs_sorted;
+  DevBuf<yc::RaySortCtl> rs_ctl;
   DevBuf<yc::SortCtl> sctl;
   DevBuf<yc::RoundCounters> rc;
   DevBuf<yc::BatchCtl> ctl;
@@ -817,6 +871,8 @@ struct yc_batch {
   int wide = -1;   // node layout of the batch's scenes (-1: no job yet)
   int grid_c = 0, grid_a = 0, grid_m = 0, logic_grid = 0;
   bool mixed = true;   // YC_OPT_MIXED_TRACE of the context when the batch was created
+  bool raysort = false;   // YC_OPT_RAY_SORT / _MIN of the context when the batch was created
+  int rs_ob = 0, rs_db = 0, rs_threshold = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool started = false;
@@ -861,9 +917,16 @@ int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
   cudaStream_t sm = serial ? c->stream : g.main;
   cudaStream_t sa = serial ? c->stream : g.side;
   if (b->mixed) {   // both ray kinds of the round in one launch
+    yc::RaySortBufs rsb{g.rs_keys.p, g.rs_hist.p, g.rs_cursor.p, g.rs_blk.p, g.rs_sorted.p, g.rs_ctl.p, b->rs_ob,
+                        b->rs_db, b->rs_threshold};
+    if (b->raysort) {
+      KTimer kt(c, K_RAYSORT, timed);
+      yc::launch_raysort_batch(b->jobs.p, b->job_pass.p, in_c, in_a, rin, ps.ro, ps.rd, rsb, b->logic_grid, sm);
+    }
     KTimer kt(c, K_TRACE, timed);
     yc::launch_batch_trace_mixed(b->wide == 1, b->jobs.p, b->job_pass.p, in_c, in_a, rin, ps.ro, ps.rd, ps.hit,
-                                 c->stats.p, b->stack_cap, b->grid_m, sm);
+                                 c->stats.p, b->stack_cap, b->grid_m, sm, b->raysort ? rsb.sorted : nullptr,
+                                 b->raysort ? rsb.ctl : nullptr);
   } else {
     // the two traces of a round are independent and overlap
     if (!serial) {
@@ -959,6 +1022,9 @@ int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
   if (!b) return fail(YC_E_NOMEM, "host allocation failed");
   b->ctx = c;
   b->mixed = c->mixed_trace != 0;
+  b->rs_ob = c->rs_ob;
+  b->rs_db = c->rs_db;
+  b->rs_threshold = c->rs_threshold;
   if (cfg) b->cfg = *cfg;
   if (b->cfg.pool_paths <= 0) b->cfg.pool_paths = 1 << 21;
   if (b->cfg.rounds_per_launch <= 0) b->cfg.rounds_per_launch = 8;
@@ -993,6 +1059,18 @@ int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
     if (b->cfg.sort_threshold > 0) {
       YC_CUDA(g->sort_keys.alloc(m));
       YC_CUDA(g->sorted.alloc(m));
+    }
+    b->raysort = b->mixed && (b->rs_ob + b->rs_db) > 0 && b->rs_threshold > 0 && m >= (size_t)b->rs_threshold;
+    if (b->raysort) {
+      const size_t bins = (size_t)yc::raysort_bins(b->rs_ob, b->rs_db);
+      YC_CUDA(g->rs_keys.alloc(m));
+      YC_CUDA(g->rs_sorted.alloc(m));
+      YC_CUDA(g->rs_hist.alloc(bins));
+      YC_CUDA(g->rs_cursor.alloc(bins));
+      YC_CUDA(g->rs_blk.alloc(64));
+      YC_CUDA(g->rs_ctl.alloc(1));
+      YC_CUDA(cudaMemsetAsync(g->rs_hist.p, 0, g->rs_hist.bytes(), c->stream));
+      YC_CUDA(cudaMemsetAsync(g->rs_ctl.p, 0, sizeof(yc::RaySortCtl), c->stream));
     }
     YC_CUDA(g->rc.alloc(2));
     YC_CUDA(g->ctl.alloc(1));

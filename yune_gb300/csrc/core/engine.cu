@@ -340,17 +340,21 @@ __global__ void __launch_bounds__(TRACE_TB) k_batch_trace(const BatchJob* jobs, 
   trace_loop<ANY, WIDE>(src, *count, work, stack_cap, st);
 }
 
-// both queues of a round: closest-hit entries first, then any-hit
+// both queues of a round: closest-hit entries first, then any-hit (or the sorted list,
+// which keeps that split)
 struct BatchMixedSrc {
   const BatchJob* jobs;
   const int2* job_pass;
   const int* __restrict__ q_closest;
   const int* __restrict__ q_any;
+  const int* __restrict__ sorted;   // non-null: this round's sorted work list
   int nc;
   const float4* __restrict__ ro;
   const float4* __restrict__ rd;
   float4* hit;
-  __device__ __forceinline__ int slot(int e, bool any) const { return any ? q_any[e - nc] : q_closest[e]; }
+  __device__ __forceinline__ int slot(int e, bool any) const {
+    return sorted ? sorted[e] : (any ? q_any[e - nc] : q_closest[e]);
+  }
   __device__ __forceinline__ const DevScene& begin(int e, bool any, RayIn& r) {
     const int q = slot(e, any);
     const float4 o = ro[q];
@@ -371,9 +375,10 @@ __global__ void __launch_bounds__(TRACE_TB) k_batch_trace_mixed(const BatchJob* 
                                                                 const int* __restrict__ q_any,
                                                                 RoundCounters* rc, const float4* __restrict__ ro,
                                                                 const float4* __restrict__ rd, float4* hit,
-                                                                int stack_cap, DevStats* st) {
+                                                                int stack_cap, DevStats* st, const int* sorted,
+                                                                const RaySortCtl* rs) {
   const int nc = rc->n_closest;
-  BatchMixedSrc src{jobs, job_pass, q_closest, q_any, nc, ro, rd, hit};
+  BatchMixedSrc src{jobs, job_pass, q_closest, q_any, (rs && rs->use) ? sorted : nullptr, nc, ro, rd, hit};
   trace_loop_mixed<WIDE>(src, nc, nc + rc->n_any, &rc->work_closest, stack_cap, st);
 }
 
@@ -402,14 +407,15 @@ int batch_trace_mixed_grid(int stack_cap, bool wide) {
 
 int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, const int2* job_pass, const int* q_closest,
                              const int* q_any, RoundCounters* rc, const float4* ro, const float4* rd, float4* hit,
-                             DevStats* st, int stack_cap, int grid_blocks, cudaStream_t s) {
+                             DevStats* st, int stack_cap, int grid_blocks, cudaStream_t s, const int* sorted,
+                             const RaySortCtl* rs) {
   const size_t smem = batch_smem(stack_cap);
   if (wide)
     k_batch_trace_mixed<true><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, q_closest, q_any, rc, ro, rd, hit,
-                                                                  stack_cap, st);
+                                                                  stack_cap, st, sorted, rs);
   else
     k_batch_trace_mixed<false><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, q_closest, q_any, rc, ro, rd, hit,
-                                                                   stack_cap, st);
+                                                                   stack_cap, st, sorted, rs);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -1,0 +1,200 @@
+// raysort.cu -- counting sort of a round's traversal work list by ray origin and direction.
+//
+// Rays traced in a coherent order walk the same nodes in neighbouring lanes: fewer
+// divergent branches per warp and more L1 hits. Before the mixed trace launch the
+// round's rays (closest-hit queue, then any-hit queue) are sorted by a key of
+//   kind (1 bit, closest-hit first, so entries [0, n_closest) stay the closest-hit ones)
+//   | Morton code of the origin's cell in the scene box (ob bits per axis)
+//   | Morton code of the direction's cell in [-1, 1]^3 (db bits per axis)
+// with a counting sort: key and histogram (one atomic per run of equal keys in a warp),
+// an exclusive scan in tiles of 1024 bins (which also clears the histogram for the next
+// round), and a scatter of the path indices. The order is a heuristic only: every ray is traced with
+// the same arithmetic whatever its position, so results do not change.
+#include <cuda_runtime.h>
+
+#include "yc_engine.h"
+#include "yc_internal.h"
+
+namespace yc {
+
+constexpr int RS_TB = 256;
+constexpr int RS_SCAN_TB = 1024;
+constexpr int RS_MAX_TILES = 64;   // 2^16 bins at most
+
+__device__ __forceinline__ unsigned spread3(unsigned x) {   // bit i of x -> bit 3i (x < 8)
+  return (x & 1u) | ((x & 2u) << 2) | ((x & 4u) << 4);
+}
+
+__device__ __forceinline__ unsigned cell_of(float v, float scale, int n) {
+  const float c = fminf(fmaxf(v * scale, 0.0f), (float)(n - 1));   // NaN -> 0
+  return (unsigned)(int)c;
+}
+
+__device__ __forceinline__ unsigned ray_key(const float4& o, const float4& d, const float4& lo, const float4& hi,
+                                            int ob, int db) {
+  const int no = 1 << ob, nd = 1 << db;
+  const float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = hi.z - lo.z;
+  const unsigned ox = cell_of(o.x - lo.x, ex > 0.0f ? (float)no / ex : 0.0f, no);
+  const unsigned oy = cell_of(o.y - lo.y, ey > 0.0f ? (float)no / ey : 0.0f, no);
+  const unsigned oz = cell_of(o.z - lo.z, ez > 0.0f ? (float)no / ez : 0.0f, no);
+  const float hd = 0.5f * (float)nd;
+  const unsigned dx = cell_of(d.x + 1.0f, hd, nd), dy = cell_of(d.y + 1.0f, hd, nd), dz = cell_of(d.z + 1.0f, hd, nd);
+  const unsigned mo = spread3(ox) | (spread3(oy) << 1) | (spread3(oz) << 2);
+  const unsigned md = spread3(dx) | (spread3(dy) << 1) | (spread3(dz) << 2);
+  return (mo << (3 * db)) | md;
+}
+
+// the scene box of the ray in slot p: one scene per pass, or the job's scene in a batch
+struct BoxOne {
+  float4 lo, hi;
+  __device__ __forceinline__ void of(int, float4& l, float4& h) const { l = lo; h = hi; }
+};
+struct BoxBatch {
+  const BatchJob* jobs;
+  const int2* job_pass;
+  __device__ __forceinline__ void of(int p, float4& l, float4& h) const {
+    const DevScene& sc = jobs[job_pass[p].x].pp.sc;
+    l = sc.root_lo;
+    h = sc.root_hi;
+  }
+};
+
+template <class Box>
+__global__ void __launch_bounds__(RS_TB) k_rs_key(Box box, const int* __restrict__ q_closest,
+                                                  const int* __restrict__ q_any, const RoundCounters* rc,
+                                                  const float4* __restrict__ ro, const float4* __restrict__ rd,
+                                                  unsigned* keys, unsigned* hist, int threshold, int ob, int db) {
+  const int nc = rc->n_closest, n = nc + rc->n_any;
+  if (threshold <= 0 || n < threshold) return;   // uniform over the grid
+  const int lane = threadIdx.x & 31;
+  const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int warps_total = (gridDim.x * blockDim.x) >> 5;
+  const unsigned kind_bit = 1u << (3 * (ob + db));
+  for (int wbase = warp_global * 32; wbase < n; wbase += warps_total * 32) {
+    const int e = wbase + lane;
+    unsigned key = 0xffffffffu - lane;   // idle lanes match nobody
+    if (e < n) {
+      const bool any = e >= nc;
+      const int p = any ? q_any[e - nc] : q_closest[e];
+      float4 lo, hi;
+      box.of(p, lo, hi);
+      key = ray_key(ro[p], rd[p], lo, hi, ob, db) | (any ? kind_bit : 0u);
+      keys[e] = key;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (e < n && lane == __ffs(peers) - 1) atomicAdd(&hist[key], (unsigned)__popc(peers));
+  }
+}
+
+// block-wide exclusive prefix of one value per thread (RS_SCAN_TB threads); *total gets
+// the block's sum
+__device__ __forceinline__ unsigned block_exclusive(unsigned v, unsigned* s_warp, unsigned* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned incl = v;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const unsigned u = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += u;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned w = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : 0u;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned u = __shfl_up_sync(0xffffffffu, w, off);
+      if (lane >= off) w += u;
+    }
+    s_warp[lane] = w;   // inclusive over warps
+  }
+  __syncthreads();
+  *total = s_warp[(blockDim.x >> 5) - 1];
+  return incl - v + (warp > 0 ? s_warp[warp - 1] : 0u);
+}
+
+// Exclusive scan of the histogram in tiles of RS_SCAN_TB bins, one block per tile
+// (coalesced): cursor = prefix within the tile, blk_sum = tile totals (the scatter adds
+// the prefix of the tile totals). Clears the histogram for the next round.
+__global__ void __launch_bounds__(RS_SCAN_TB) k_rs_scan(const RoundCounters* rc, unsigned* hist, unsigned* cursor,
+                                                        unsigned* blk_sum, RaySortCtl* ctl, int threshold,
+                                                        int nbins) {
+  __shared__ unsigned s_warp[32];
+  const int n = rc->n_closest + rc->n_any;
+  const int use = (threshold > 0 && n >= threshold) ? 1 : 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->use = use;
+  if (!use) return;   // uniform over the grid
+  const int bin = blockIdx.x * RS_SCAN_TB + threadIdx.x;
+  const unsigned c = bin < nbins ? hist[bin] : 0u;
+  unsigned total;
+  const unsigned ex = block_exclusive(c, s_warp, &total);
+  if (bin < nbins) {
+    cursor[bin] = ex;
+    hist[bin] = 0;
+  }
+  if (threadIdx.x == 0) blk_sum[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(RS_TB) k_rs_scatter(const int* __restrict__ q_closest,
+                                                      const int* __restrict__ q_any, const RoundCounters* rc,
+                                                      const unsigned* __restrict__ keys, unsigned* cursor,
+                                                      const unsigned* __restrict__ blk_sum, int nblk, int* sorted,
+                                                      const RaySortCtl* ctl) {
+  __shared__ unsigned s_base[RS_MAX_TILES];
+  if (!ctl->use) return;
+  if (threadIdx.x < 32) {   // exclusive prefix of the tile totals (nblk <= 64)
+    const int lane = threadIdx.x;
+    unsigned a = lane < nblk ? blk_sum[lane] : 0u, b = lane + 32 < nblk ? blk_sum[lane + 32] : 0u;
+    unsigned ia = a, ib = b;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned u = __shfl_up_sync(0xffffffffu, ia, off), w = __shfl_up_sync(0xffffffffu, ib, off);
+      if (lane >= off) { ia += u; ib += w; }
+    }
+    const unsigned tot_a = __shfl_sync(0xffffffffu, ia, 31);
+    s_base[lane] = ia - a;
+    s_base[lane + 32] = tot_a + ib - b;
+  }
+  __syncthreads();
+  const int nc = rc->n_closest, n = nc + rc->n_any;
+  const int lane = threadIdx.x & 31;
+  const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int warps_total = (gridDim.x * blockDim.x) >> 5;
+  for (int wbase = warp_global * 32; wbase < n; wbase += warps_total * 32) {
+    const int e = wbase + lane;
+    const bool active = e < n;
+    const unsigned key = active ? keys[e] : 0xffffffffu - lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    unsigned base = 0;
+    if (active && lane == leader) base = s_base[key / RS_SCAN_TB] + atomicAdd(&cursor[key], (unsigned)__popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (active) sorted[base + __popc(peers & ((1u << lane) - 1))] = e < nc ? q_closest[e] : q_any[e - nc];
+  }
+}
+
+int raysort_bins(int ob, int db) { return 1 << (3 * (ob + db) + 1); }
+
+template <class Box>
+static int launch_rs(const Box& box, const int* q_closest, const int* q_any, const RoundCounters* rc,
+                     const float4* ro, const float4* rd, const RaySortBufs& b, int grid, cudaStream_t s) {
+  k_rs_key<Box><<<grid, RS_TB, 0, s>>>(box, q_closest, q_any, rc, ro, rd, b.keys, b.hist, b.threshold, b.ob, b.db);
+  const int nbins = raysort_bins(b.ob, b.db);
+  const int nblk = (nbins + RS_SCAN_TB - 1) / RS_SCAN_TB;
+  if (nblk > RS_MAX_TILES) return -1;
+  k_rs_scan<<<nblk, RS_SCAN_TB, 0, s>>>(rc, b.hist, b.cursor, b.blk_sum, b.ctl, b.threshold, nbins);
+  k_rs_scatter<<<grid, RS_TB, 0, s>>>(q_closest, q_any, rc, b.keys, b.cursor, b.blk_sum, nblk, b.sorted, b.ctl);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_raysort(const DevScene& sc, const int* q_closest, const int* q_any, const RoundCounters* rc,
+                   const float4* ro, const float4* rd, const RaySortBufs& b, int grid, cudaStream_t s) {
+  return launch_rs(BoxOne{sc.root_lo, sc.root_hi}, q_closest, q_any, rc, ro, rd, b, grid, s);
+}
+
+int launch_raysort_batch(const BatchJob* jobs, const int2* job_pass, const int* q_closest, const int* q_any,
+                         const RoundCounters* rc, const float4* ro, const float4* rd, const RaySortBufs& b, int grid,
+                         cudaStream_t s) {
+  return launch_rs(BoxBatch{jobs, job_pass}, q_closest, q_any, rc, ro, rd, b, grid, s);
+}
+
+}  // namespace yc

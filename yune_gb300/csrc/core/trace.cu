@@ -48,16 +48,20 @@ __global__ void __launch_bounds__(TRACE_TB) k_trace_paths(DevScene sc, const int
   trace_loop<ANY, WIDE>(src, *count, work, stack_cap, st);
 }
 
-// both queues of a round in one launch: closest-hit entries first, then any-hit
+// both queues of a round in one launch: closest-hit entries first, then any-hit (or the
+// sorted list, which keeps that split)
 struct PathMixedSrc {
   const DevScene* sc;
   const int* __restrict__ q_closest;
   const int* __restrict__ q_any;
+  const int* __restrict__ sorted;   // non-null: this round's sorted work list
   int nc;
   const float4* __restrict__ ro;
   const float4* __restrict__ rd;
   float4* hit;
-  __device__ __forceinline__ int slot(int e, bool any) const { return any ? q_any[e - nc] : q_closest[e]; }
+  __device__ __forceinline__ int slot(int e, bool any) const {
+    return sorted ? sorted[e] : (any ? q_any[e - nc] : q_closest[e]);
+  }
   __device__ __forceinline__ const DevScene& begin(int e, bool any, RayIn& r) {
     const int q = slot(e, any);
     const float4 o = ro[q];
@@ -77,9 +81,10 @@ __global__ void __launch_bounds__(TRACE_TB) k_trace_paths_mixed(DevScene sc, con
                                                                 const int* __restrict__ q_any, RoundCounters* rc,
                                                                 const float4* __restrict__ ro,
                                                                 const float4* __restrict__ rd, float4* hit,
-                                                                int stack_cap, DevStats* st) {
+                                                                int stack_cap, DevStats* st, const int* sorted,
+                                                                const RaySortCtl* rs) {
   const int nc = rc->n_closest;
-  PathMixedSrc src{&sc, q_closest, q_any, nc, ro, rd, hit};
+  PathMixedSrc src{&sc, q_closest, q_any, (rs && rs->use) ? sorted : nullptr, nc, ro, rd, hit};
   trace_loop_mixed<WIDE>(src, nc, nc + rc->n_any, &rc->work_closest, stack_cap, st);
 }
 
@@ -172,13 +177,15 @@ int trace_mixed_grid_blocks(int depth, bool wide) {
 
 int launch_trace_mixed(const DevScene& sc, const int* q_closest, const int* q_any, RoundCounters* rc,
                        const float4* ro, const float4* rd, float4* hit, DevStats* st, int grid_blocks,
-                       cudaStream_t s) {
+                       cudaStream_t s, const int* sorted, const RaySortCtl* rs) {
   const int cap = stack_cap_for(sc.depth);
   const size_t smem = smem_for(cap);
   if (sc.wide)
-    k_trace_paths_mixed<true><<<grid_blocks, TRACE_TB, smem, s>>>(sc, q_closest, q_any, rc, ro, rd, hit, cap, st);
+    k_trace_paths_mixed<true><<<grid_blocks, TRACE_TB, smem, s>>>(sc, q_closest, q_any, rc, ro, rd, hit, cap, st,
+                                                                  sorted, rs);
   else
-    k_trace_paths_mixed<false><<<grid_blocks, TRACE_TB, smem, s>>>(sc, q_closest, q_any, rc, ro, rd, hit, cap, st);
+    k_trace_paths_mixed<false><<<grid_blocks, TRACE_TB, smem, s>>>(sc, q_closest, q_any, rc, ro, rd, hit, cap, st,
+                                                                   sorted, rs);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

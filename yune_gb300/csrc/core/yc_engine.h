@@ -66,7 +66,12 @@ int batch_trace_grid(bool any_hit, int stack_cap, bool wide);
 // cursor is rc->work_closest
 int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, const int2* job_pass, const int* q_closest,
                              const int* q_any, RoundCounters* rc, const float4* ro, const float4* rd, float4* hit,
-                             DevStats* st, int stack_cap, int grid_blocks, cudaStream_t s);
+                             DevStats* st, int stack_cap, int grid_blocks, cudaStream_t s,
+                             const int* sorted = nullptr, const RaySortCtl* rs = nullptr);
+// raysort.cu, with the scene box of each ray's job
+int launch_raysort_batch(const BatchJob* jobs, const int2* job_pass, const int* q_closest, const int* q_any,
+                         const RoundCounters* rc, const float4* ro, const float4* rd, const RaySortBufs& b, int grid,
+                         cudaStream_t s);
 int batch_trace_mixed_grid(int stack_cap, bool wide);
 
 }  // namespace yc

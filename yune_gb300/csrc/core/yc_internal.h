@@ -44,6 +44,23 @@ struct RoundCounters {
   int pad[3];
 };
 
+// Sorting of a round's traversal work list by ray origin and direction (raysort.cu):
+// `use` tells the trace kernel whether this round's list is the sorted one.
+struct RaySortCtl {
+  int use;
+  int pad[3];
+};
+struct RaySortBufs {
+  unsigned* keys;      // one per work-list entry
+  unsigned* hist;      // raysort_bins(ob, db) counters, zero between rounds
+  unsigned* cursor;    // scatter cursors (exclusive prefix of hist within its tile of 1024 bins)
+  unsigned* blk_sum;   // tile totals (64 at most)
+  int* sorted;         // the sorted work list (path indices)
+  RaySortCtl* ctl;
+  int ob, db;          // origin and direction bits per axis (3 * (ob + db) <= 15)
+  int threshold;       // rounds with fewer rays are traced unsorted
+};
+
 // device-wide statistics (yc_stats layout, 64-bit counters)
 struct DevStats {
   unsigned long long rays, primary, extension, shadow, mis, connection, traversed, samples, stack_overflow;
@@ -85,7 +102,12 @@ int trace_grid_blocks(bool any_hit, int depth, bool wide);
 // cursor is rc->work_closest
 int launch_trace_mixed(const DevScene& sc, const int* q_closest, const int* q_any, RoundCounters* rc,
                        const float4* ro, const float4* rd, float4* hit, DevStats* st, int grid_blocks,
-                       cudaStream_t s);
+                       cudaStream_t s, const int* sorted = nullptr, const RaySortCtl* rs = nullptr);
+// raysort.cu: sorts the round's work list (closest-hit queue, then any-hit queue) into
+// b.sorted when the round has at least b.threshold rays, and sets b.ctl->use
+int raysort_bins(int ob, int db);
+int launch_raysort(const DevScene& sc, const int* q_closest, const int* q_any, const RoundCounters* rc,
+                   const float4* ro, const float4* rd, const RaySortBufs& b, int grid, cudaStream_t s);
 int trace_mixed_grid_blocks(int depth, bool wide);
 int l2_read_gbs(size_t bytes, int iters, cudaStream_t s, double* gbs);
 
