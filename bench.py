@@ -43,6 +43,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Mrays/s"
+L2_BYTES = 126 << 20   # GB300 L2 as the CUDA runtime reports it
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
@@ -64,6 +65,8 @@ def parse():
     ap.add_argument("--pool", type=int, default=0, help="batch path slots (0: 2M)")
     ap.add_argument("--requests", type=int, default=40)
     ap.add_argument("--rate", type=float, default=20.0, help="c3: Poisson arrival rate (req/s)")
+    ap.add_argument("--rates", default="", help="c3: comma list of arrival rates to sweep (overrides --rate)")
+    ap.add_argument("--hbm-budget-mb", type=int, default=40 << 10, help="c3: HBM budget of the accumulators in flight")
     ap.add_argument("--res-max", type=int, default=1024)
     ap.add_argument("--spp-max", type=int, default=128)
     ap.add_argument("--max-tris", type=int, default=500_000)
@@ -77,6 +80,7 @@ def parse():
     ap.add_argument("--ray-sort", type=int, default=32,
                     help="sort key of a round's rays: origin bits * 10 + direction bits per axis (0: queue order)")
     ap.add_argument("--ray-sort-min", type=int, default=65536, help="rounds with fewer rays are not sorted")
+    ap.add_argument("--res", default="", help="c4: frame size WxH instead of 3840x2160 (profiling captures)")
     ap.add_argument("--tree", type=int, default=1,
                     help="interior hierarchy: 0 reference nodes, 1 binary SAH over the reference leaves, 2 four-wide")
     return ap.parse_args()
@@ -236,9 +240,8 @@ def run_reference(args, rank, ws, dist):
     from yune_gb300 import scenes
     seeds = scenes.pass_seeds(0, args.steps + args.warmup)
     cb = cpu_reference(scene, seeds, args.cpu_seconds, band=1 if args.config == "c4" else 0)
-    cfg = {"workload": "%s: %d tris, %dx%d, cfg %s" % (args.config, scene.n_tri, scene.width, scene.height,
-                                                      json.dumps(scene.cfg, sort_keys=True)),
-           "spp_total": scene.spp}
+    cfg = {"workload": workload_string(args.config, scene), "spp_total": scene.spp,
+           "reference_cfg": scene.cfg}
     line = {"metric": METRIC, "value": cb["value"], "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32", "data": "synthetic", "config": cfg,
@@ -298,7 +301,7 @@ def run_ours(args, rank, local, ws, dist):
        host -> device, the step's passes render, and the tonemapped frame comes back;
        once through the engine (E passes per step) and once per pass (yc_render_pass).
     """
-    from yune_gb300 import quality, scenes
+    from yune_gb300 import autotune, quality, scenes
     from yune_gb300.batch import Batch
     from yune_gb300.core import Renderer
     scene = scene_for(args.config)
@@ -333,13 +336,18 @@ def run_ours(args, rank, local, ws, dist):
     r.set_profiling(False)
     img_pp = r.read_accum(aid)
 
-    # B. the whole job through the engine
+    # B. the whole job through the engine, in the launch shape the autotuner picks for this
+    #    frame (untimed calibration passes with seeds of their own), unless --pool fixes it
     cap = r.scene_depth(sid) + 2
-    pool = 1 << 16
-    while pool < W * H and pool < (1 << 22):
-        pool <<= 1
-    shape = dict(pool_paths=pool, rounds_per_launch=8, logic_blocks_per_sm=2, sort_threshold=1 << 16,
-                 groups=args.groups)
+    if args.pool:
+        shape = dict(pool_paths=args.pool, rounds_per_launch=8, logic_blocks_per_sm=2, sort_threshold=1 << 16,
+                     groups=args.groups, ray_sort=0)
+        tune_info = None
+    else:
+        tuned, trials, tune_s = autotune.tune_scenes(r, [scene], [sid], stack_cap=cap)
+        shape = tuned.kwargs()
+        tune_info = {"seconds": tune_s, "trials": len(trials)}
+    pool = shape["pool_paths"]
     aid_e = r.alloc_accum(W, H)
     b = Batch(r, stack_cap=cap, **shape)
     b.add_job(sid, aid_e, scene.cam, seeds[:Wm], scene.cfg, reset_first=1)
@@ -409,13 +417,15 @@ def run_ours(args, rank, local, ws, dist):
         "metric": METRIC, "value": rays / t_s / 1e6, "unit": METRIC, "n_gpus": ws, "steps": K,
         "warmup": Wm, "ms_per_step": en_ms / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded procedural scene)",
-        "config": {"workload": "%s: glass icosphere Cornell box, %d tris, %dx%d, 1 spp per step, NEE+MIS, RR after "
-                               "bounce 3, max depth %d; the K steps rendered as one job of K passes through the "
-                               "batch engine" % (args.config, scene.n_tri, W, H, scene.cfg["max_depth"]),
+        "config": {"workload": workload_string(args.config, scene),
+                   "method": "the K steps rendered as one job of K passes through the batch engine",
                    "spp_total": scene.spp, "tree_mode": args.tree,
-                   "l2": "L2 flushed before the timed job; path state of %d slots (%d MB) is larger than L2"
-                         % (pool, pool * 224 >> 20),
-                   "engine_shape": shape, "parallelism": "replicas" if ws > 1 else "single GPU"},
+                   "l2": "L2 flushed before the timed job of K passes; its working set (path state of %d slots, "
+                         "%d MB accumulator, %d MB scene) is %d MB, above the 126 MB L2"
+                         % (pool, W * H * 16 >> 20, r.scene_bytes(sid) >> 20,
+                            (pool * 232 + W * H * 16 + r.scene_bytes(sid)) >> 20),
+                   "engine_shape": shape, "autotune": tune_info,
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
         "samples_per_s": st_en["samples"] * (ws if dist else 1) / t_s,
         "rays_per_sample": st_en["rays"] / max(1, st_en["samples"]),
         "gpu_launches": launches,
@@ -452,15 +462,41 @@ def run_ours(args, rank, local, ws, dist):
     print(json.dumps(line))
 
 
-def run_c4(args, rank, local, ws, dist):
-    """The stress configuration: 10M triangles, 3840x2160, naive BDPT with 8 vertices per
-    subpath and four lights, through yc_render_pass (the drop-in call), one pass per
-    step. The node and triangle set (about 0.7 GB) is far larger than L2, so the
-    traversal kernel's roofline is the HBM copy bandwidth."""
-    from yune_gb300 import scenes
+WORKLOAD_NAMES = {
+    "c0": "Cornell box (5 Oren-Nayar walls, seeded-yaw boxes, one Phong n=50), quad light",
+    "c1": "glass icosphere (level 6, IOR 1.5) in the Cornell box",
+    "c0_bdpt": "Cornell box, four quad lights, naive BDPT with 8 vertices per subpath",
+    "c4": "stress: 40x40 grid of displaced level-4/5 icospheres, mixed materials, 4 quad lights, naive BDPT with "
+          "8 vertices per subpath",
+}
+
+
+def workload_string(name, scene):
+    """The workload a bench line is quoted on (the same string in both arms)."""
+    W, H = scene.width, scene.height
+    if scene.cfg.get("integrator", 0) == 1:
+        return ("%s: %s, %d tris, %dx%d, %d lights, BDPT with %d vertices per subpath, 1 spp per step"
+                % (name, WORKLOAD_NAMES.get(name, name), scene.n_tri, W, H, len(scene.lights),
+                   scene.cfg["bdpt_bounces"]))
+    return ("%s: %s, %d tris, %dx%d, 1 spp per step, NEE+MIS, RR after bounce %d, max depth %d"
+            % (name, WORKLOAD_NAMES.get(name, name), scene.n_tri, W, H, scene.cfg["rr_threshold"],
+               scene.cfg["max_depth"]))
+
+
+def run_perpass_bdpt(args, rank, local, ws, dist):
+    """BDPT configurations (c0_bdpt, and c4: 10M triangles, 3840x2160, naive BDPT with 8
+    vertices per subpath and four lights) through yc_render_pass (the drop-in call), one
+    pass per step. For c4 the node and triangle set (about 0.7 GB) is far larger than L2,
+    so the traversal kernel's roofline is the HBM copy bandwidth."""
+    from yune_gb300 import quality, scenes
     from yune_gb300.core import Renderer
     t0 = time.perf_counter()
-    scene = scenes.c4()
+    make = scenes.CONFIGS[args.config]
+    if args.res:
+        w, h = (int(x) for x in args.res.lower().split("x"))
+        scene = make(width=w, height=h)
+    else:
+        scene = make()
     build_s = time.perf_counter() - t0
     K, Wm = args.steps, args.warmup
     seeds = scenes.pass_seeds(0, Wm + K + args.e2e_steps)
@@ -512,23 +548,22 @@ def run_c4(args, rank, local, ws, dist):
         return
     roof = _trace_roofline(st, kt, l2, pk, pk_kind, "k_trace_paths_mixed (closest + any-hit rays)",
                            "k_trace_paths<closest> (extend)")
-    # bound: the node and triangle set does not fit in L2
-    roof.update({"bound": "hbm", "peak": pk.get("hbm_gbs"), "frac": roof["hbm_frac"], "peak_source": pk_kind,
-                 "l2_peak": l2, "l2_frac": roof["achieved"] / l2 if l2 else None})
-    for k in ("hbm_peak", "hbm_frac", "hbm_peak_source"):
-        roof.pop(k, None)
+    big = scene_bytes > L2_BYTES
+    if big:   # the node and triangle set does not fit in L2: the bound is HBM
+        roof.update({"bound": "hbm", "peak": pk.get("hbm_gbs"), "frac": roof["hbm_frac"], "peak_source": pk_kind,
+                     "l2_peak": l2, "l2_frac": roof["achieved"] / l2 if l2 else None})
+        for k in ("hbm_peak", "hbm_frac", "hbm_peak_source"):
+            roof.pop(k, None)
     launches = int(kt["raygen_launches"] + kt["extend_launches"] + kt["occlusion_launches"] + kt["trace_launches"]
                    + kt["logic_launches"] + kt["tail_launches"] + 3 * kt["raysort_launches"])
     line = {
         "metric": METRIC, "value": rays / t_s / 1e6, "unit": METRIC, "n_gpus": ws, "steps": K, "warmup": Wm,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
         "data": "synthetic (seeded procedural scene)",
-        "config": {"workload": "c4 stress: 40x40 grid of displaced level-4/5 icospheres, %d tris, mixed materials, "
-                               "4 quad lights, %dx%d, naive BDPT with %d vertices per subpath, 1 spp per step"
-                               % (scene.n_tri, W, H, scene.cfg["bdpt_bounces"]),
+        "config": {"workload": workload_string(args.config, scene),
                    "spp_total": scene.spp, "tree_mode": args.tree, "scene_device_bytes": scene_bytes,
                    "host_build_s": build_s, "upload_s": upload_s,
-                   "l2": "L2 flushed before each step; the node and triangle set is larger than L2",
+                   "l2": "L2 flushed before each step" + ("; the node and triangle set is larger than L2" if big else ""),
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "samples_per_s": st["samples"] * (ws if dist else 1) / t_s,
         "rays_per_sample": st["rays"] / max(1, st["samples"]),
@@ -542,11 +577,13 @@ def run_c4(args, rank, local, ws, dist):
                 "path": "yc_set_camera + yc_render_pass + yc_tonemap to host"},
         "clocks": clk.summary(), "stack_overflow": int(st["stack_overflow"]),
         "image_mean": float(np.nanmean(img[..., :3])),
-        "image_error": "no FP64 reference for this scene (65,536 passes of the CPU oracle over 10M triangles "
-                       "is out of reach); the BDPT integrator's error is measured on c0_bdpt (--quality)",
+        "image_error": (quality.report(img, args.config, int(img[0, 0, 3]))
+                        if quality.load_reference(args.config) is not None and not args.res else
+                        "no FP64 reference for this scene (65,536 passes of the CPU oracle over 10M triangles "
+                        "is out of reach); the BDPT integrator's error is measured on c0_bdpt"),
     }
     if not args.no_cpu:
-        line["cpu_baseline"] = cpu_reference(scene, seeds, args.cpu_seconds, band=1)
+        line["cpu_baseline"] = cpu_reference(scene, seeds, args.cpu_seconds, band=1 if big else 0)
     r.close()
     print(json.dumps(line))
 
@@ -626,34 +663,49 @@ def run_c2(args):
 
 
 def run_c3(args):
-    """Served requests (continuous batching) against the plain first-come loop."""
+    """Served requests (continuous batching) against the plain first-come loop, for each
+    arrival rate of --rates (or --rate), over the same resident scenes."""
     from yune_gb300 import serve, workloads
     from yune_gb300.core import Renderer
+    t0 = time.perf_counter()
     resident = workloads.c3_scenes(8, max_tris=args.max_tris)
-    reqs = workloads.c3_requests(args.requests, args.rate, len(resident), res_range=(256, args.res_max),
-                                 spp_range=(16, args.spp_max))
-    mk = lambda: [serve.Request(a, sc, w, h, spp, seed=i) for i, (a, sc, w, h, spp) in enumerate(reqs)]  # noqa: E731
+    build_s = time.perf_counter() - t0
+    rates = [float(x) for x in args.rates.split(",")] if args.rates else [args.rate]
     r = Renderer(0)
-    r.reset_stats()
-    srv = serve.Server(r, resident, hbm_budget=40 << 30, pool_paths=args.pool or (1 << 21))
-    t0 = time.perf_counter()
-    served = srv.run(mk())
-    ts = time.perf_counter() - t0
-    sts = r.stats()
+    r.set_tree_mode(args.tree)
+    r.set_mixed_trace(args.mixed)
+    r.set_ray_sort(args.ray_sort // 10, args.ray_sort % 10, args.ray_sort_min)
+    srv = serve.Server(r, resident, hbm_budget=args.hbm_budget_mb << 20, pool_paths=args.pool or (1 << 21))
+    runs = []
+    for rate in rates:
+        reqs = workloads.c3_requests(args.requests, rate, len(resident), res_range=(256, args.res_max),
+                                     spp_range=(16, args.spp_max))
+        mk = lambda: [serve.Request(a, sc, w, h, spp, seed=i) for i, (a, sc, w, h, spp) in enumerate(reqs)]  # noqa
+        r.reset_stats()
+        t0 = time.perf_counter()
+        served = srv.run(mk())
+        ts = time.perf_counter() - t0
+        sts = r.stats()
+        r.reset_stats()
+        t0 = time.perf_counter()
+        plain = serve.serve_plain(r, resident, mk())
+        tpl = time.perf_counter() - t0
+        stp = r.stats()
+        p50s, p99s = serve.percentiles(served)
+        p50p, p99p = serve.percentiles(plain)
+        runs.append({"rate_per_s": rate, "requests": len(reqs),
+                     "pixel_passes": int(sum(w * h * spp for (_, _, w, h, spp) in reqs)),
+                     "served": {"p50": p50s, "p99": p99s, "Mrays_s": sts["rays"] / ts / 1e6, "seconds": ts,
+                                "max_in_flight": srv.max_in_flight, "max_bytes_in_use": srv.max_in_use},
+                     "plain": {"p50": p50p, "p99": p99p, "Mrays_s": stp["rays"] / tpl / 1e6, "seconds": tpl},
+                     "rays_equal": sts["rays"] == stp["rays"]})
+        srv.max_in_flight = srv.max_in_use = 0
     srv.close()
-    r.reset_stats()
-    t0 = time.perf_counter()
-    plain = serve.serve_plain(r, resident, mk())
-    tpl = time.perf_counter() - t0
-    stp = r.stats()
-    p50s, p99s = serve.percentiles(served)
-    p50p, p99p = serve.percentiles(plain)
-    out = {"metric": "p50/p99 time to target spp (s)", "unit": "s",
-           "config": {"workload": "c3 serving", "requests": len(reqs), "rate_per_s": args.rate,
-                      "resolution": [256, args.res_max], "spp": [16, args.spp_max],
-                      "scene_triangles": [int(s.n_tri) for s in resident]},
-           "served": {"p50": p50s, "p99": p99s, "Mrays_s": sts["rays"] / ts / 1e6, "seconds": ts},
-           "plain": {"p50": p50p, "p99": p99p, "Mrays_s": stp["rays"] / tpl / 1e6, "seconds": tpl}}
+    out = {"metric": "p50/p99 time to target spp (s) and aggregate Mrays/s", "unit": "s",
+           "config": {"workload": "c3 serving", "resolution": [256, args.res_max], "spp": [16, args.spp_max],
+                      "scene_triangles": [int(s.n_tri) for s in resident], "hbm_budget_mb": args.hbm_budget_mb,
+                      "pool_paths": args.pool or (1 << 21), "host_build_s": build_s},
+           "runs": runs}
     r.close()
     print(json.dumps(out))
 
@@ -731,6 +783,10 @@ def run_trace_bench(args):
     print(json.dumps(out))
 
 
+def scenes_is_bdpt(name):
+    return name in ("c0_bdpt", "c4")
+
+
 def main():
     args = parse()
     if args.quality:
@@ -744,8 +800,8 @@ def main():
     rank, local, ws, dist = dist_init(args)
     if args.impl == "reference":
         run_reference(args, rank, ws, dist)
-    elif args.config == "c4":
-        run_c4(args, rank, local, ws, dist)
+    elif scenes_is_bdpt(args.config):
+        run_perpass_bdpt(args, rank, local, ws, dist)
     else:
         run_ours(args, rank, local, ws, dist)
     if dist:

@@ -193,6 +193,8 @@ typedef struct yc_batch_cfg {
   int32_t sort_threshold;      /* shade queues of at least this many paths are sorted by path
                                   phase and material class before the logic kernel; 0 = never */
   int32_t groups;              /* slot groups whose rounds run concurrently (1..8); 0 = 2 */
+  int32_t ray_sort;            /* sort key of each round's rays (as YC_OPT_RAY_SORT); 0 = the
+                                  context's YC_OPT_RAY_SORT, -1 = rays in queue order */
 } yc_batch_cfg;
 int yc_batch_create(yc_ctx* ctx, const yc_batch_cfg* cfg, yc_batch** out);
 /* Adds a job: n_pass passes of scene_id into accum_id seen from *cam, pass k with

@@ -1026,6 +1026,14 @@ int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
   b->rs_db = c->rs_db;
   b->rs_threshold = c->rs_threshold;
   if (cfg) b->cfg = *cfg;
+  if (b->cfg.ray_sort < 0) {
+    b->rs_ob = b->rs_db = 0;
+  } else if (b->cfg.ray_sort > 0) {
+    const int ob = b->cfg.ray_sort / 10, db = b->cfg.ray_sort % 10;
+    if (ob > 3 || db > 3 || ob + db > 5) return fail(YC_E_INVALID, "ray_sort: origin bits * 10 + direction bits, sum <= 5");
+    b->rs_ob = ob;
+    b->rs_db = db;
+  }
   if (b->cfg.pool_paths <= 0) b->cfg.pool_paths = 1 << 21;
   if (b->cfg.rounds_per_launch <= 0) b->cfg.rounds_per_launch = 8;
   if (b->cfg.rounds_per_launch & 1) b->cfg.rounds_per_launch += 1;

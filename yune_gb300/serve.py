@@ -54,6 +54,8 @@ class Server:
         cap = max(renderer.scene_depth(sid) for sid in self.sids) + 2
         self.batch = Batch(renderer, pool_paths=pool_paths, rounds_per_launch=rounds_per_launch, max_jobs=4096,
                            stack_cap=cap, logic_blocks_per_sm=logic_blocks_per_sm, sort_threshold=sort_threshold)
+        self.max_in_flight = 0   # most requests admitted at once, and most accumulator bytes
+        self.max_in_use = 0
 
     def _admit(self, q, now):
         if q.bytes > self.budget:
@@ -65,6 +67,7 @@ class Server:
         q.job = self.batch.add_job(self.sids[q.scene], q.accum, s.cam, scenes.pass_seeds(q.seed, q.spp), self.cfg)
         q.admitted = now
         self.in_use += q.bytes
+        self.max_in_use = max(self.max_in_use, self.in_use)
         return True
 
     def run(self, requests, clock=time.perf_counter):
@@ -79,6 +82,7 @@ class Server:
             while i < len(pending) and pending[i].arrival <= now and self._admit(pending[i], now):
                 live.append(pending[i])
                 i += 1
+            self.max_in_flight = max(self.max_in_flight, len(live))
             if not live:
                 if i < len(pending):
                     time.sleep(max(0.0, pending[i].arrival - (clock() - t0)))
