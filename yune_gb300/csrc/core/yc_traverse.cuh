@@ -66,18 +66,31 @@ __device__ __forceinline__ bool box_ref(float ox, float oy, float oz, float ix, 
   return t_max > ocl_fmax(t_min, 0.0f);
 }
 
+// minimum and maximum of three (the three-operand PTX forms of sm_100 measured no
+// faster here)
+__device__ __forceinline__ float max3f(float a, float b, float c) { return fmaxf(fmaxf(a, b), c); }
+__device__ __forceinline__ float min3f(float a, float b, float c) { return fminf(fminf(a, b), c); }
+
 // The same test when every 1/d is finite: no operand can be NaN, so min/max are the
-// hardware FMNMX and the result (hit or not) equals the reference's.
+// hardware FMNMX, and the reference's result is t_max > max(t_min, 0). The distance
+// cull is folded in: `cull_up` is the smallest float above the cull bound (+inf when
+// there is none), so min(t_max, cull_up) > max(t_min, 0) holds exactly when the box is
+// hit and its entry distance is within the bound (a negative t_min, an origin inside
+// the box, is never culled). tentry, which orders the children, is max(t_min, 0) when
+// `clamp` (closest-hit walks: children around the origin tie and keep their order, which
+// measured fewer triangle tests) and t_min otherwise (any-hit walks: the child reaching
+// furthest behind the origin first, which measured fewer box tests).
 __device__ __forceinline__ bool box_fast(float ox, float oy, float oz, float ix, float iy, float iz,
                                          float lx, float hx, float ly, float hy, float lz, float hz,
-                                         float& tentry) {
+                                         float cull_up, bool clamp, float& tentry) {
   const float ax = __fmul_rn(__fsub_rn(lx, ox), ix), bx = __fmul_rn(__fsub_rn(hx, ox), ix);
   const float ay = __fmul_rn(__fsub_rn(ly, oy), iy), by = __fmul_rn(__fsub_rn(hy, oy), iy);
   const float az = __fmul_rn(__fsub_rn(lz, oz), iz), bz = __fmul_rn(__fsub_rn(hz, oz), iz);
-  const float t0 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fminf(az, bz));
-  const float t1 = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz));
-  tentry = t0;
-  return t1 > fmaxf(t0, 0.0f);
+  const float t0 = max3f(fminf(ax, bx), fminf(ay, by), fminf(az, bz));
+  const float t1 = min3f(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), cull_up));
+  const float t0c = fmaxf(t0, 0.0f);
+  tentry = clamp ? t0c : t0;
+  return t1 > t0c;
 }
 
 struct TriHit {
@@ -115,6 +128,11 @@ __device__ __forceinline__ bool tri_test(float ox, float oy, float oz, float dx,
 // Cull factor for the distance test: a child is skipped when its entry distance exceeds
 // the best t by more than 2^-10 relative.
 __device__ __forceinline__ float cull_bound(float best) { return best * 1.0009765625f; }
+// the smallest float above cull_bound(best) (best > 0), +inf when the bound is +inf
+__device__ __forceinline__ float cull_up(float best) {
+  const float cb = cull_bound(best);
+  return isinf(cb) ? cb : __int_as_float(__float_as_int(cb) + 1);
+}
 
 // ---- resumable walk for the persistent kernels ----
 // The state of one ray's walk, so a warp can run its lanes' walks step by step and hand
@@ -125,6 +143,7 @@ struct Walk {
   const float4* tris;
   float ox, oy, oz, dx, dy, dz, ix, iy, iz;
   float best, bu, bv;
+  float best_up;         // cull_up(best)
   int best_tri, best_rank;
   int link, sp;
   float link_t;          // entry distance of the subtree `link` (checked again before it is opened)
@@ -139,6 +158,7 @@ __device__ __forceinline__ void walk_begin(const DevScene& sc, const RayIn& r, W
   w.ix = __frcp_rn(r.dx); w.iy = __frcp_rn(r.dy); w.iz = __frcp_rn(r.dz);
   w.exact = isinf(w.ix) || isinf(w.iy) || isinf(w.iz);
   w.best = r.tmax; w.bu = 0.0f; w.bv = 0.0f;
+  w.best_up = cull_up(r.tmax);
   w.best_tri = -1; w.best_rank = -1;
   w.sp = 0;
   w.link = sc.root_link;
@@ -148,7 +168,7 @@ __device__ __forceinline__ void walk_begin(const DevScene& sc, const RayIn& r, W
     const bool h = w.exact ? box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, sc.root_lo.x, sc.root_hi.x, sc.root_lo.y,
                                      sc.root_hi.y, sc.root_lo.z, sc.root_hi.z, te)
                            : box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, sc.root_lo.x, sc.root_hi.x, sc.root_lo.y,
-                                      sc.root_hi.y, sc.root_lo.z, sc.root_hi.z, te);
+                                      sc.root_hi.y, sc.root_lo.z, sc.root_hi.z, __int_as_float(0x7f800000), false, te);
     if (!h) w.link = LINK_NONE;
   }
 }
@@ -167,6 +187,7 @@ __device__ __forceinline__ bool walk_leaf(Walk& w, int link, WalkCount& wc, bool
     TriHit th;
     if (tri_test(w.ox, w.oy, w.oz, w.dx, w.dy, w.dz, a, b, c, w.best, w.best_rank, th)) {
       w.best = th.t;
+      w.best_up = cull_up(th.t);
       w.bu = th.u;
       w.bv = th.v;
       w.best_tri = __float_as_int(a.w);
@@ -199,8 +220,8 @@ __device__ __forceinline__ int walk_recheck(Walk& w, int link, const int* stack,
 // One interior node of the two-child layout: returns the next node (the nearer child
 // hit, the other one pushed), or the next subtree popped from the stack when neither
 // child is hit. LINK_NONE: the walk is over (or the stack bound was reached).
-__device__ __forceinline__ int visit2(Walk& w, int link, int* stack, int stride, int stack_cap, WalkCount& wc,
-                                      bool& overflow) {
+__device__ __forceinline__ int visit2(Walk& w, bool any, int link, int* stack, int stride, int stack_cap,
+                                      WalkCount& wc, bool& overflow) {
   const float4* nd = w.nodes + 4 * (size_t)link;
   const float4 n0 = __ldg(nd + 0);
   const float4 n1 = __ldg(nd + 1);
@@ -209,16 +230,18 @@ __device__ __forceinline__ int visit2(Walk& w, int link, int* stack, int stride,
   wc.nodes += 2;
   float t0, t1;
   bool h0, h1;
-  if (!w.exact) {
-    h0 = box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, t0);
-    h1 = box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, t1);
+  if (!w.exact) {   // hit and within the cull bound
+    h0 = box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, w.best_up, !any, t0);
+    h1 = box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, w.best_up, !any, t1);
   } else {
     h0 = box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, t0);
     h1 = box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, t1);
+    const float cb = cull_bound(w.best);
+    h0 = h0 && !(t0 > cb);
+    h1 = h1 && !(t1 > cb);
   }
-  const float cb = cull_bound(w.best);
-  h0 = h0 && n3.x != LINK_NONE && !(t0 > cb);
-  h1 = h1 && n3.y != LINK_NONE && !(t1 > cb);
+  h0 = h0 && n3.x != LINK_NONE;
+  h1 = h1 && n3.y != LINK_NONE;
   if (h0 && h1) {
     const bool swap = t1 < t0;
     if (w.sp >= stack_cap) { overflow = true; w.sp = 0; return LINK_NONE; }
@@ -244,8 +267,8 @@ __device__ __forceinline__ void cx(float& ta, int& la, float& tb, int& lb) {
 // One interior node of the four-child layout (yc_scene.h, wide nodes): the four child
 // boxes are tested with the reference's slab arithmetic, the hits sorted by entry
 // distance, the nearest returned and the others pushed farthest first.
-__device__ __forceinline__ int visit4(Walk& w, int link, int* stack, int stride, int stack_cap, WalkCount& wc,
-                                      bool& overflow) {
+__device__ __forceinline__ int visit4(Walk& w, bool any, int link, int* stack, int stride, int stack_cap,
+                                      WalkCount& wc, bool& overflow) {
   const float INF = __int_as_float(0x7f800000);
   const float4* nd = w.nodes + 8 * (size_t)link;
   const float4 lx = __ldg(nd + 0), hx = __ldg(nd + 1);
@@ -263,7 +286,8 @@ __device__ __forceinline__ int visit4(Walk& w, int link, int* stack, int stride,
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     float te;
-    bool h = !w.exact ? box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, clx[c], chx[c], cly[c], chy[c], clz[c], chz[c], te)
+    bool h = !w.exact ? box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, clx[c], chx[c], cly[c], chy[c], clz[c], chz[c],
+                                 w.best_up, !any, te)
                       : box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, clx[c], chx[c], cly[c], chy[c], clz[c], chz[c], te);
     h = h && cl[c] != LINK_NONE && !(te > cb);
     t[c] = h ? te : INF;
@@ -308,8 +332,8 @@ __device__ __forceinline__ bool walk_step_k(Walk& w, bool any, int* stack, int s
   int link = any ? w.link : walk_recheck(w, w.link, stack, stride);
   int leaf = LINK_NONE;
   while (link >= 0 && link != LINK_NONE) {
-    link = WIDE ? visit4(w, link, stack, stride, stack_cap, wc, overflow)
-                : visit2(w, link, stack, stride, stack_cap, wc, overflow);
+    link = WIDE ? visit4(w, any, link, stack, stride, stack_cap, wc, overflow)
+                : visit2(w, any, link, stack, stride, stack_cap, wc, overflow);
     if (link < 0 && link != LINK_NONE && leaf == LINK_NONE) {
       leaf = link;
       link = walk_pop(w, stack, stride);
