@@ -147,7 +147,7 @@ int yc_render_passes(yc_ctx* ctx, int scene_id, int accum_id, const uint32_t* ra
  * stall the frame, or a host whose device memory belongs to its own allocator and that
  * forbids driver allocations after start-up. yc_render_pass sizes its wavefront state
  * to the image on first use; this call keeps that state in a static device array of the
- * library (about 3.7 MB, held by every GPU that loads the library until exit) and so
+ * library (about 3.9 MB, held by every GPU that loads the library until exit) and so
  * renders one tile of at most 16384 pixels (cfg->block / block_x / block_y select it,
  * as for yc_render_pass) with no allocation. The scene and accumulator come from
  * yc_upload_scene / yc_alloc_accum, made beforehand. A larger tile is rejected with
@@ -237,7 +237,9 @@ enum {
    * lanes walk the same nodes. value = origin bits per axis * 10 + direction bits per axis
    * (each 0..3, sum <= 5); 0 = rays in queue order. Default 32. Same results either way. */
   YC_OPT_RAY_SORT = 4,
-  /* Rounds (and batch slot groups) with fewer rays than this are not sorted. Default 65536. */
+  /* Rounds (and batch slot groups) with fewer rays than this are not sorted. Default 65536.
+   * yc_render_pass also leaves scenes of fewer than 4096 triangles unsorted (their walks are
+   * too short for the sort to pay). */
   YC_OPT_RAY_SORT_MIN = 5
 };
 int yc_set_option(yc_ctx* ctx, int option, int value);

@@ -105,8 +105,7 @@ struct yc_ctx {
   size_t rs_cap = 0;
   // wavefront buffers, sized for the largest image seen
   size_t cap_paths = 0;
-  DevBuf<int4> misc;
-  DevBuf<float4> f4bufs[12];
+  DevBuf<float4> rec;                // path records, PS_STRIDE float4 per slot
   DevBuf<int> q[4];                  // closest/any for two rounds
   DevBuf<yc::RoundCounters> rc;      // two round-counter blocks
   DevBuf<yc::DevStats> stats;
@@ -135,12 +134,14 @@ namespace {
 
 int ensure_paths(yc_ctx* c, size_t n) {
   if (n <= c->cap_paths) return 0;
-  YC_CUDA(c->misc.alloc(n));
-  for (auto& b : c->f4bufs) YC_CUDA(b.alloc(n));
+  YC_CUDA(c->rec.alloc(n * yc::PS_STRIDE));
   for (auto& b : c->q) YC_CUDA(b.alloc(n));
   c->cap_paths = n;
   return 0;
 }
+
+// scenes with fewer triangles are traced in queue order by yc_render_pass
+constexpr int kRaySortMinTris = 4096;
 
 // key, histogram and sorted-list buffers of the per-pass ray sort, for n rays
 int ensure_raysort(yc_ctx* c, size_t n) {
@@ -212,23 +213,7 @@ void collect_events(yc_ctx* c) {
   c->ev_used = 0;
 }
 
-yc::PathState path_state(yc_ctx* c) {
-  yc::PathState ps;
-  ps.misc = c->misc.p;
-  ps.thr = c->f4bufs[0].p;
-  ps.thr_next = c->f4bufs[1].p;
-  ps.direct = c->f4bufs[2].p;
-  ps.indirect = c->f4bufs[3].p;
-  ps.ls = c->f4bufs[4].p;
-  ps.hp = c->f4bufs[5].p;
-  ps.nrm = c->f4bufs[6].p;
-  ps.wo = c->f4bufs[7].p;
-  ps.wi = c->f4bufs[8].p;
-  ps.ro = c->f4bufs[9].p;
-  ps.rd = c->f4bufs[10].p;
-  ps.hit = c->f4bufs[11].p;
-  return ps;
-}
+yc::PathState path_state(yc_ctx* c) { return yc::path_state_at(c->rec.p); }
 
 Scene* find_scene(yc_ctx* c, int id) {
   auto it = c->scenes.find(id);
@@ -298,7 +283,10 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
   }
   YC_CUDA(cudaPeekAtLastError());
   const bool mixed = c->mixed_trace != 0;
-  const bool raysort = mixed && (c->rs_ob + c->rs_db) > 0 && c->rs_threshold > 0 && (size_t)W * H >= (size_t)c->rs_threshold;
+  // (a walk through a scene of a few thousand triangles is a handful of boxes: sorting
+  // its rays costs more than it saves)
+  const bool raysort = mixed && (c->rs_ob + c->rs_db) > 0 && c->rs_threshold > 0 &&
+                       (size_t)W * H >= (size_t)c->rs_threshold && sc->dev.n_tri >= kRaySortMinTris;
   yc::RaySortBufs rsb{};
   if (raysort) {
     if (int e = ensure_raysort(c, (size_t)W * H)) return e;
@@ -856,8 +844,7 @@ struct BatchGroup {
 struct yc_batch {
   yc_ctx* ctx = nullptr;
   yc_batch_cfg cfg{};
-  DevBuf<int4> misc;
-  DevBuf<float4> f4bufs[12];
+  DevBuf<float4> rec;        // path records, PS_STRIDE float4 per slot
   DevBuf<int2> job_pass;
   DevBuf<yc::BatchTasks> tasks;
   DevBuf<yc::BatchJob> jobs;
@@ -895,14 +882,8 @@ void free_batch(yc_batch* b) {
 }
 
 yc::PathState batch_state(yc_batch* b) {
-  yc::PathState ps;
-  ps.misc = b->misc.p;
-  float4** f[12] = {&ps.thr, &ps.thr_next, &ps.direct, &ps.indirect, &ps.ls, &ps.hp,
-                    &ps.nrm, &ps.wo, &ps.wi, &ps.ro, &ps.rd, &ps.hit};
-  for (int i = 0; i < 12; ++i) *f[i] = b->f4bufs[i].p;
-  return ps;
+  return yc::path_state_at(b->rec.p);
 }
-
 // one round of group g: trace both queues, step every path (A -> B). `serial`: every
 // launch on the context stream (per-kernel timing), else on the group's streams.
 int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
@@ -1043,8 +1024,7 @@ int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
   if (b->cfg.groups > 8 || b->cfg.groups > b->cfg.pool_paths) return fail(YC_E_INVALID, "groups must be 1..8");
   const size_t n = (size_t)b->cfg.pool_paths;
   YC_CUDA(cudaSetDevice(c->device));
-  YC_CUDA(b->misc.alloc(n));
-  for (auto& f : b->f4bufs) YC_CUDA(f.alloc(n));
+  YC_CUDA(b->rec.alloc(n * yc::PS_STRIDE));
   YC_CUDA(b->job_pass.alloc(n));
   YC_CUDA(b->tasks.alloc(1));
   YC_CUDA(b->jobs.alloc(b->cfg.max_jobs));

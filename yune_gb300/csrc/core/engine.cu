@@ -313,13 +313,13 @@ struct BatchSrc {
   const BatchJob* jobs;
   const int2* job_pass;
   const int* __restrict__ queue;
-  const float4* __restrict__ ro;
-  const float4* __restrict__ rd;
-  float4* hit;
+  SF<float4> ro;
+  SF<float4> rd;
+  SF<float4> hit;
   __device__ __forceinline__ const DevScene& begin(int e, RayIn& r) {
     const int q = queue[e];
-    const float4 o = ro[q];
-    const float4 d = rd[q];
+    const float4 o = __ldg(&ro[q]);
+    const float4 d = __ldg(&rd[q]);
     r = RayIn{o.x, o.y, o.z, o.w, d.x, d.y, d.z};
     return jobs[job_pass[q].x].pp.sc;
   }
@@ -333,8 +333,8 @@ struct BatchSrc {
 template <bool ANY, bool WIDE>
 __global__ void __launch_bounds__(TRACE_TB) k_batch_trace(const BatchJob* jobs, const int2* job_pass,
                                                           const int* __restrict__ queue, const int* __restrict__ count,
-                                                          int* work, const float4* __restrict__ ro,
-                                                          const float4* __restrict__ rd, float4* hit, int stack_cap,
+                                                          int* work, SF<float4> ro,
+                                                          SF<float4> rd, SF<float4> hit, int stack_cap,
                                                           DevStats* st) {
   BatchSrc<ANY> src{jobs, job_pass, queue, ro, rd, hit};
   trace_loop<ANY, WIDE>(src, *count, work, stack_cap, st);
@@ -349,16 +349,16 @@ struct BatchMixedSrc {
   const int* __restrict__ q_any;
   const int* __restrict__ sorted;   // non-null: this round's sorted work list
   int nc;
-  const float4* __restrict__ ro;
-  const float4* __restrict__ rd;
-  float4* hit;
+  SF<float4> ro;
+  SF<float4> rd;
+  SF<float4> hit;
   __device__ __forceinline__ int slot(int e, bool any) const {
     return sorted ? sorted[e] : (any ? q_any[e - nc] : q_closest[e]);
   }
   __device__ __forceinline__ const DevScene& begin(int e, bool any, RayIn& r) {
     const int q = slot(e, any);
-    const float4 o = ro[q];
-    const float4 d = rd[q];
+    const float4 o = __ldg(&ro[q]);
+    const float4 d = __ldg(&rd[q]);
     r = RayIn{o.x, o.y, o.z, o.w, d.x, d.y, d.z};
     return jobs[job_pass[q].x].pp.sc;
   }
@@ -373,8 +373,8 @@ template <bool WIDE>
 __global__ void __launch_bounds__(TRACE_TB) k_batch_trace_mixed(const BatchJob* jobs, const int2* job_pass,
                                                                 const int* __restrict__ q_closest,
                                                                 const int* __restrict__ q_any,
-                                                                RoundCounters* rc, const float4* __restrict__ ro,
-                                                                const float4* __restrict__ rd, float4* hit,
+                                                                RoundCounters* rc, SF<float4> ro,
+                                                                SF<float4> rd, SF<float4> hit,
                                                                 int stack_cap, DevStats* st, const int* sorted,
                                                                 const RaySortCtl* rs) {
   const int nc = rc->n_closest;
@@ -406,7 +406,7 @@ int batch_trace_mixed_grid(int stack_cap, bool wide) {
 }
 
 int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, const int2* job_pass, const int* q_closest,
-                             const int* q_any, RoundCounters* rc, const float4* ro, const float4* rd, float4* hit,
+                             const int* q_any, RoundCounters* rc, SF<float4> ro, SF<float4> rd, SF<float4> hit,
                              DevStats* st, int stack_cap, int grid_blocks, cudaStream_t s, const int* sorted,
                              const RaySortCtl* rs) {
   const size_t smem = batch_smem(stack_cap);
@@ -420,7 +420,7 @@ int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, const int2* job_pa
 }
 
 int launch_batch_trace(bool any_hit, bool wide, const BatchJob* jobs, const int2* job_pass, const int* queue,
-                       const int* count, int* work, const float4* ro, const float4* rd, float4* hit, DevStats* st,
+                       const int* count, int* work, SF<float4> ro, SF<float4> rd, SF<float4> hit, DevStats* st,
                        int stack_cap, int grid_blocks, cudaStream_t s) {
   const size_t smem = batch_smem(stack_cap);
   if (any_hit && wide)

@@ -24,8 +24,8 @@
 
 namespace yc {
 
-// per-path bytes: misc (16) + 12 float4 records (192) + 4 queue slots (16)
-constexpr size_t NOALLOC_PATH_BYTES = 16 + 12 * 16 + 4 * 4;
+// per-path bytes: the path record (PS_STRIDE float4, 224) + 4 queue slots (16)
+constexpr size_t NOALLOC_PATH_BYTES = PS_STRIDE * 16 + 4 * 4;
 constexpr size_t NOALLOC_BYTES = (size_t)NOALLOC_MAX_PATHS * NOALLOC_PATH_BYTES + 2 * sizeof(RoundCounters);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
@@ -122,15 +122,11 @@ int noalloc_render(const NoallocPass& a, std::string& err) {
     err = "cudaGetSymbolAddress failed for the render scratch";
     return YC_E_LAUNCH;
   }
-  // carve the scratch: misc, 12 float4 records, 4 queues, 2 round-counter blocks
+  // carve the scratch: the path records, 4 queues, 2 round-counter blocks
   const size_t N = NOALLOC_MAX_PATHS;
-  PathState ps;
-  ps.misc = reinterpret_cast<int4*>(base);
-  float4* f = reinterpret_cast<float4*>(base + N * sizeof(int4));
-  float4** rec[12] = {&ps.thr, &ps.thr_next, &ps.direct, &ps.indirect, &ps.ls, &ps.hp,
-                      &ps.nrm,  &ps.wo,       &ps.wi,     &ps.ro,       &ps.rd, &ps.hit};
-  for (int i = 0; i < 12; ++i) *rec[i] = f + (size_t)i * N;
-  int* q = reinterpret_cast<int*>(f + 12 * N);
+  float4* f = reinterpret_cast<float4*>(base);
+  const PathState ps = path_state_at(f);
+  int* q = reinterpret_cast<int*>(f + PS_STRIDE * N);
   int* qs[4] = {q, q + N, q + 2 * N, q + 3 * N};
   RoundCounters* rc = reinterpret_cast<RoundCounters*>(q + 4 * N);
   cudaStream_t s = a.stream;

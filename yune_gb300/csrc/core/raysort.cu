@@ -62,7 +62,7 @@ struct BoxBatch {
 template <class Box>
 __global__ void __launch_bounds__(RS_TB) k_rs_key(Box box, const int* __restrict__ q_closest,
                                                   const int* __restrict__ q_any, const RoundCounters* rc,
-                                                  const float4* __restrict__ ro, const float4* __restrict__ rd,
+                                                  SF<float4> ro, SF<float4> rd,
                                                   unsigned* keys, unsigned* hist, int threshold, int ob, int db) {
   const int nc = rc->n_closest, n = nc + rc->n_any;
   if (threshold <= 0 || n < threshold) return;   // uniform over the grid
@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(RS_TB) k_rs_key(Box box, const int* __restrict
       const int p = any ? q_any[e - nc] : q_closest[e];
       float4 lo, hi;
       box.of(p, lo, hi);
-      key = ray_key(ro[p], rd[p], lo, hi, ob, db) | (any ? kind_bit : 0u);
+      key = ray_key(__ldg(&ro[p]), __ldg(&rd[p]), lo, hi, ob, db) | (any ? kind_bit : 0u);
       keys[e] = key;
     }
     const unsigned peers = __match_any_sync(0xffffffffu, key);
@@ -176,7 +176,7 @@ int raysort_bins(int ob, int db) { return 1 << (3 * (ob + db) + 1); }
 
 template <class Box>
 static int launch_rs(const Box& box, const int* q_closest, const int* q_any, const RoundCounters* rc,
-                     const float4* ro, const float4* rd, const RaySortBufs& b, int grid, cudaStream_t s) {
+                     SF<float4> ro, SF<float4> rd, const RaySortBufs& b, int grid, cudaStream_t s) {
   k_rs_key<Box><<<grid, RS_TB, 0, s>>>(box, q_closest, q_any, rc, ro, rd, b.keys, b.hist, b.threshold, b.ob, b.db);
   const int nbins = raysort_bins(b.ob, b.db);
   const int nblk = (nbins + RS_SCAN_TB - 1) / RS_SCAN_TB;
@@ -187,12 +187,12 @@ static int launch_rs(const Box& box, const int* q_closest, const int* q_any, con
 }
 
 int launch_raysort(const DevScene& sc, const int* q_closest, const int* q_any, const RoundCounters* rc,
-                   const float4* ro, const float4* rd, const RaySortBufs& b, int grid, cudaStream_t s) {
+                   SF<float4> ro, SF<float4> rd, const RaySortBufs& b, int grid, cudaStream_t s) {
   return launch_rs(BoxOne{sc.root_lo, sc.root_hi}, q_closest, q_any, rc, ro, rd, b, grid, s);
 }
 
 int launch_raysort_batch(const BatchJob* jobs, const int2* job_pass, const int* q_closest, const int* q_any,
-                         const RoundCounters* rc, const float4* ro, const float4* rd, const RaySortBufs& b, int grid,
+                         const RoundCounters* rc, SF<float4> ro, SF<float4> rd, const RaySortBufs& b, int grid,
                          cudaStream_t s) {
   return launch_rs(BoxBatch{jobs, job_pass}, q_closest, q_any, rc, ro, rd, b, grid, s);
 }

@@ -21,13 +21,13 @@ template <bool ANY>
 struct PathSrc {
   const DevScene* sc;
   const int* __restrict__ queue;
-  const float4* __restrict__ ro;
-  const float4* __restrict__ rd;
-  float4* hit;
+  SF<float4> ro;
+  SF<float4> rd;
+  SF<float4> hit;
   __device__ __forceinline__ const DevScene& begin(int e, RayIn& r) {
     const int q = queue[e];
-    const float4 o = ro[q];
-    const float4 d = rd[q];
+    const float4 o = __ldg(&ro[q]);
+    const float4 d = __ldg(&rd[q]);
     r = RayIn{o.x, o.y, o.z, o.w, d.x, d.y, d.z};
     return *sc;
   }
@@ -41,8 +41,8 @@ struct PathSrc {
 template <bool ANY, bool WIDE>
 __global__ void __launch_bounds__(TRACE_TB) k_trace_paths(DevScene sc, const int* __restrict__ queue,
                                                           const int* __restrict__ count, int* work,
-                                                          const float4* __restrict__ ro,
-                                                          const float4* __restrict__ rd, float4* hit, int stack_cap,
+                                                          SF<float4> ro,
+                                                          SF<float4> rd, SF<float4> hit, int stack_cap,
                                                           DevStats* st) {
   PathSrc<ANY> src{&sc, queue, ro, rd, hit};
   trace_loop<ANY, WIDE>(src, *count, work, stack_cap, st);
@@ -56,16 +56,16 @@ struct PathMixedSrc {
   const int* __restrict__ q_any;
   const int* __restrict__ sorted;   // non-null: this round's sorted work list
   int nc;
-  const float4* __restrict__ ro;
-  const float4* __restrict__ rd;
-  float4* hit;
+  SF<float4> ro;
+  SF<float4> rd;
+  SF<float4> hit;
   __device__ __forceinline__ int slot(int e, bool any) const {
     return sorted ? sorted[e] : (any ? q_any[e - nc] : q_closest[e]);
   }
   __device__ __forceinline__ const DevScene& begin(int e, bool any, RayIn& r) {
     const int q = slot(e, any);
-    const float4 o = ro[q];
-    const float4 d = rd[q];
+    const float4 o = __ldg(&ro[q]);
+    const float4 d = __ldg(&rd[q]);
     r = RayIn{o.x, o.y, o.z, o.w, d.x, d.y, d.z};
     return *sc;
   }
@@ -79,8 +79,8 @@ struct PathMixedSrc {
 template <bool WIDE>
 __global__ void __launch_bounds__(TRACE_TB) k_trace_paths_mixed(DevScene sc, const int* __restrict__ q_closest,
                                                                 const int* __restrict__ q_any, RoundCounters* rc,
-                                                                const float4* __restrict__ ro,
-                                                                const float4* __restrict__ rd, float4* hit,
+                                                                SF<float4> ro,
+                                                                SF<float4> rd, SF<float4> hit,
                                                                 int stack_cap, DevStats* st, const int* sorted,
                                                                 const RaySortCtl* rs) {
   const int nc = rc->n_closest;
@@ -154,8 +154,8 @@ int trace_grid_blocks(bool any_hit, int depth, bool wide) {
   return any_hit ? resident_grid(k_trace_paths<true, false>, smem) : resident_grid(k_trace_paths<false, false>, smem);
 }
 
-int launch_trace(const DevScene& sc, bool any_hit, const int* queue, const int* count, int* work, const float4* ro,
-                 const float4* rd, float4* hit, DevStats* st, int grid_blocks, cudaStream_t s) {
+int launch_trace(const DevScene& sc, bool any_hit, const int* queue, const int* count, int* work, SF<float4> ro,
+                 SF<float4> rd, SF<float4> hit, DevStats* st, int grid_blocks, cudaStream_t s) {
   const int cap = stack_cap_for(sc.depth);
   const size_t smem = smem_for(cap);
   const bool wide = sc.wide != 0;
@@ -176,7 +176,7 @@ int trace_mixed_grid_blocks(int depth, bool wide) {
 }
 
 int launch_trace_mixed(const DevScene& sc, const int* q_closest, const int* q_any, RoundCounters* rc,
-                       const float4* ro, const float4* rd, float4* hit, DevStats* st, int grid_blocks,
+                       SF<float4> ro, SF<float4> rd, SF<float4> hit, DevStats* st, int grid_blocks,
                        cudaStream_t s, const int* sorted, const RaySortCtl* rs) {
   const int cap = stack_cap_for(sc.depth);
   const size_t smem = smem_for(cap);

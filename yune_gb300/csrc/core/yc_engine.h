@@ -59,18 +59,18 @@ void launch_batch_logic(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, 
                         unsigned long long* job_done, const int* sorted, const SortCtl* sctl, int grid,
                         cudaStream_t s);
 int launch_batch_trace(bool any_hit, bool wide, const BatchJob* jobs, const int2* job_pass, const int* queue,
-                       const int* count, int* work, const float4* ro, const float4* rd, float4* hit, DevStats* st,
+                       const int* count, int* work, SF<float4> ro, SF<float4> rd, SF<float4> hit, DevStats* st,
                        int stack_cap, int grid_blocks, cudaStream_t s);
 int batch_trace_grid(bool any_hit, int stack_cap, bool wide);
 // one launch over both queues of a round (closest-hit entries, then any-hit); the work
 // cursor is rc->work_closest
 int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, const int2* job_pass, const int* q_closest,
-                             const int* q_any, RoundCounters* rc, const float4* ro, const float4* rd, float4* hit,
+                             const int* q_any, RoundCounters* rc, SF<float4> ro, SF<float4> rd, SF<float4> hit,
                              DevStats* st, int stack_cap, int grid_blocks, cudaStream_t s,
                              const int* sorted = nullptr, const RaySortCtl* rs = nullptr);
 // raysort.cu, with the scene box of each ray's job
 int launch_raysort_batch(const BatchJob* jobs, const int2* job_pass, const int* q_closest, const int* q_any,
-                         const RoundCounters* rc, const float4* ro, const float4* rd, const RaySortBufs& b, int grid,
+                         const RoundCounters* rc, SF<float4> ro, SF<float4> rd, const RaySortBufs& b, int grid,
                          cudaStream_t s);
 int batch_trace_mixed_grid(int stack_cap, bool wide);
 

@@ -9,24 +9,59 @@
 
 namespace yc {
 
-// ---- wavefront path state: one slot per path, structure of arrays ----
+// ---- wavefront path state: one record of PS_STRIDE float4 (224 B, seven 32-byte
+// sectors) per path slot ----
+// The logic kernel reads and writes a path's whole record, and after the shade-queue
+// sort neighbouring threads hold unrelated slots; one contiguous record per path keeps
+// every sector it fetches fully used (a field per array would use half of each). The
+// ray and its hit come first, so the traversal kernels touch the first two sectors only.
 // misc.x seed, misc.y pixel index, misc.z packed (state | flags << 4 | (j+1) << 12 |
 // (k+1) << 20), misc.w bounce index.
-struct PathState {
-  int4* misc;
-  float4* thr;        // throughput
-  float4* thr_next;   // throughput after the pending bounce (udpt.cl:504-507)
-  float4* direct;     // direct_color (udpt.cl:455)
-  float4* indirect;   // indirect_color
-  float4* ls;         // light_sample of the pending NEE (udpt.cl:562-563)
-  float4* hp;         // xyz hit point, w light_pdf
-  float4* nrm;        // xyz shading normal, w brdf_prob of the NEE lobe
-  float4* wo;         // xyz w_o, w brdf_pdf of the MIS sample
-  float4* wi;         // xyz NEE direction, w material index (int bits)
-  float4* ro;         // emitted ray: origin xyz, length
-  float4* rd;         // emitted ray: direction xyz
-  float4* hit;        // trace result: (t, u, v, tri) or (occluded, -, -, -)
+constexpr int PS_STRIDE = 14;
+enum { PSF_RO = 0, PSF_RD, PSF_HIT, PSF_MISC, PSF_THR, PSF_THR_NEXT, PSF_DIRECT, PSF_INDIRECT, PSF_LS, PSF_HP,
+       PSF_NRM, PSF_WO, PSF_WI };
+
+// one field of every record: slot i at p[i * PS_STRIDE]
+template <class T>
+struct SF {
+  T* p;
+  __host__ __device__ __forceinline__ T& operator[](size_t i) const { return p[i * PS_STRIDE]; }
 };
+
+struct PathState {
+  SF<int4> misc;
+  SF<float4> thr;        // throughput
+  SF<float4> thr_next;   // throughput after the pending bounce (udpt.cl:504-507)
+  SF<float4> direct;     // direct_color (udpt.cl:455)
+  SF<float4> indirect;   // indirect_color
+  SF<float4> ls;         // light_sample of the pending NEE (udpt.cl:562-563)
+  SF<float4> hp;         // xyz hit point, w light_pdf
+  SF<float4> nrm;        // xyz shading normal, w brdf_prob of the NEE lobe
+  SF<float4> wo;         // xyz w_o, w brdf_pdf of the MIS sample
+  SF<float4> wi;         // xyz NEE direction, w material index (int bits)
+  SF<float4> ro;         // emitted ray: origin xyz, length
+  SF<float4> rd;         // emitted ray: direction xyz
+  SF<float4> hit;        // trace result: (t, u, v, tri) or (occluded, -, -, -)
+};
+
+// the path state of the records starting at rec (PS_STRIDE float4 per slot)
+inline PathState path_state_at(float4* rec) {
+  PathState ps;
+  ps.misc = SF<int4>{reinterpret_cast<int4*>(rec + PSF_MISC)};
+  ps.thr = SF<float4>{rec + PSF_THR};
+  ps.thr_next = SF<float4>{rec + PSF_THR_NEXT};
+  ps.direct = SF<float4>{rec + PSF_DIRECT};
+  ps.indirect = SF<float4>{rec + PSF_INDIRECT};
+  ps.ls = SF<float4>{rec + PSF_LS};
+  ps.hp = SF<float4>{rec + PSF_HP};
+  ps.nrm = SF<float4>{rec + PSF_NRM};
+  ps.wo = SF<float4>{rec + PSF_WO};
+  ps.wi = SF<float4>{rec + PSF_WI};
+  ps.ro = SF<float4>{rec + PSF_RO};
+  ps.rd = SF<float4>{rec + PSF_RD};
+  ps.hit = SF<float4>{rec + PSF_HIT};
+  return ps;
+}
 
 // queues of one round: path indices for the closest-hit and the any-hit kernels
 struct Queues {
@@ -87,7 +122,7 @@ void launch_logic(const PassParams& pp, const PathState& ps, const int* in_close
                   const RoundCounters* rc_in, int* out_closest, int* out_any, RoundCounters* rc_out,
                   DevStats* st, int grid, cudaStream_t s);
 int launch_trace(const DevScene& sc, bool any_hit, const int* queue, const int* count, int* work,
-                 const float4* ro, const float4* rd, float4* hit, DevStats* st, int grid_blocks,
+                 SF<float4> ro, SF<float4> rd, SF<float4> hit, DevStats* st, int grid_blocks,
                  cudaStream_t s);
 void launch_tonemap(const float4* in, float4* out, int n, cudaStream_t s);
 // tail.cu: finish a pass's paths one thread each once at most `threshold` are left
@@ -101,13 +136,13 @@ int trace_grid_blocks(bool any_hit, int depth, bool wide);
 // one launch over both queues of a round (closest-hit entries, then any-hit); the work
 // cursor is rc->work_closest
 int launch_trace_mixed(const DevScene& sc, const int* q_closest, const int* q_any, RoundCounters* rc,
-                       const float4* ro, const float4* rd, float4* hit, DevStats* st, int grid_blocks,
+                       SF<float4> ro, SF<float4> rd, SF<float4> hit, DevStats* st, int grid_blocks,
                        cudaStream_t s, const int* sorted = nullptr, const RaySortCtl* rs = nullptr);
 // raysort.cu: sorts the round's work list (closest-hit queue, then any-hit queue) into
 // b.sorted when the round has at least b.threshold rays, and sets b.ctl->use
 int raysort_bins(int ob, int db);
 int launch_raysort(const DevScene& sc, const int* q_closest, const int* q_any, const RoundCounters* rc,
-                   const float4* ro, const float4* rd, const RaySortBufs& b, int grid, cudaStream_t s);
+                   SF<float4> ro, SF<float4> rd, const RaySortBufs& b, int grid, cudaStream_t s);
 int trace_mixed_grid_blocks(int depth, bool wide);
 int l2_read_gbs(size_t bytes, int iters, cudaStream_t s, double* gbs);
 

@@ -9,7 +9,7 @@
 
 namespace yc {
 
-// Largest tile (pixels) the static render scratch holds: 16384 paths, about 3.7 MB.
+// Largest tile (pixels) the static render scratch holds: 16384 paths, about 3.9 MB.
 constexpr int NOALLOC_MAX_PATHS = 16384;
 
 struct NoallocPass {
