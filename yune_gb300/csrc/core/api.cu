@@ -845,7 +845,6 @@ struct yc_batch {
   yc_ctx* ctx = nullptr;
   yc_batch_cfg cfg{};
   DevBuf<float4> rec;        // path records, PS_STRIDE float4 per slot
-  DevBuf<int2> job_pass;
   DevBuf<yc::BatchTasks> tasks;
   DevBuf<yc::BatchJob> jobs;
   DevBuf<unsigned long long> job_done;
@@ -902,10 +901,10 @@ int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
                         b->rs_db, b->rs_threshold};
     if (b->raysort) {
       KTimer kt(c, K_RAYSORT, timed);
-      yc::launch_raysort_batch(b->jobs.p, b->job_pass.p, in_c, in_a, rin, ps.ro, ps.rd, rsb, b->logic_grid, sm);
+      yc::launch_raysort_batch(b->jobs.p, batch_state(b).job, in_c, in_a, rin, ps.ro, ps.rd, rsb, b->logic_grid, sm);
     }
     KTimer kt(c, K_TRACE, timed);
-    yc::launch_batch_trace_mixed(b->wide == 1, b->jobs.p, b->job_pass.p, in_c, in_a, rin, ps.ro, ps.rd, ps.hit,
+    yc::launch_batch_trace_mixed(b->wide == 1, b->jobs.p, batch_state(b).job, in_c, in_a, rin, ps.ro, ps.rd, ps.hit,
                                  c->stats.p, b->stack_cap, b->grid_m, sm, b->raysort ? rsb.sorted : nullptr,
                                  b->raysort ? rsb.ctl : nullptr);
   } else {
@@ -916,12 +915,12 @@ int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
     }
     {
       KTimer kt(c, K_EXTEND, timed);
-      yc::launch_batch_trace(false, b->wide == 1, b->jobs.p, b->job_pass.p, in_c, &rin->n_closest,
+      yc::launch_batch_trace(false, b->wide == 1, b->jobs.p, batch_state(b).job, in_c, &rin->n_closest,
                              &rin->work_closest, ps.ro, ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_c, sm);
     }
     {
       KTimer kt(c, K_OCCL, timed);
-      yc::launch_batch_trace(true, b->wide == 1, b->jobs.p, b->job_pass.p, in_a, &rin->n_any, &rin->work_any, ps.ro,
+      yc::launch_batch_trace(true, b->wide == 1, b->jobs.p, batch_state(b).job, in_a, &rin->n_any, &rin->work_any, ps.ro,
                              ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_a, sa);
     }
     if (!serial) {
@@ -933,12 +932,12 @@ int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
   YC_CUDA(cudaMemsetAsync(g.sctl.p, 0, sizeof(yc::SortCtl), sm));
   if (b->cfg.sort_threshold > 0) {
     KTimer kt(c, K_SORT, timed);
-    yc::launch_batch_sort(b->jobs.p, b->job_pass.p, ps, in_c, in_a, rin, g.sort_keys.p, g.sorted.p, g.sctl.p,
+    yc::launch_batch_sort(b->jobs.p, batch_state(b).job, ps, in_c, in_a, rin, g.sort_keys.p, g.sorted.p, g.sctl.p,
                           b->cfg.sort_threshold, b->logic_grid, sm);
   }
   {
     KTimer kt(c, K_LOGIC, timed);
-    yc::launch_batch_logic(b->jobs.p, b->tasks.p, g.ctl.p, ps, b->job_pass.p, g.free_stack.p, in_c, in_a, rin, out_c,
+    yc::launch_batch_logic(b->jobs.p, b->tasks.p, g.ctl.p, ps, batch_state(b).job, g.free_stack.p, in_c, in_a, rin, out_c,
                            out_a, rout, c->stats.p, b->job_done.p, g.sorted.p, g.sctl.p, b->logic_grid, sm);
   }
   c->ktimes.rounds++;
@@ -960,7 +959,7 @@ int batch_body(yc_batch* b, bool timed) {
     if (!serial) YC_CUDA(cudaStreamWaitEvent(sm, b->ev_start, 0));
     {
       KTimer kt(c, K_RAYGEN, timed);
-      yc::launch_batch_fill(b->jobs.p, b->tasks.p, g.ctl.p, batch_state(b), b->job_pass.p, g.free_stack.p, g.q[0].p,
+      yc::launch_batch_fill(b->jobs.p, b->tasks.p, g.ctl.p, batch_state(b), batch_state(b).job, g.free_stack.p, g.q[0].p,
                             g.rc.p, c->stats.p, b->logic_grid, sm);
     }
     for (int k = 0; k < b->cfg.rounds_per_launch; ++k)
@@ -1025,7 +1024,6 @@ int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
   const size_t n = (size_t)b->cfg.pool_paths;
   YC_CUDA(cudaSetDevice(c->device));
   YC_CUDA(b->rec.alloc(n * yc::PS_STRIDE));
-  YC_CUDA(b->job_pass.alloc(n));
   YC_CUDA(b->tasks.alloc(1));
   YC_CUDA(b->jobs.alloc(b->cfg.max_jobs));
   YC_CUDA(b->job_done.alloc(b->cfg.max_jobs));

@@ -35,7 +35,7 @@ __device__ __forceinline__ int job_of_task(const BatchJob* jobs, int n_jobs, uns
 
 // first pass (or the next pass) of pixel `pix` of job `job` in slot p
 __device__ __forceinline__ void start_pass(const BatchJob& J, int job, int pix, int pass, int p, const PathState& ps,
-                                           int2* job_pass) {
+                                           SF<int4> job_pass) {
   const int W = J.pp.width;
   uint32_t seed;
   f4 o, d;
@@ -45,7 +45,7 @@ __device__ __forceinline__ void start_pass(const BatchJob& J, int job, int pix, 
   ps.misc[p] = make_int4((int)seed, pix, pack_misc(S_PRIMARY, 0, -1, k), 0);
   ps.ro[p] = make_float4(o.x, o.y, o.z, len);
   ps.rd[p] = make_float4(d.x, d.y, d.z, d.w);
-  job_pass[p] = make_int2(job, pass);
+  job_pass[p] = make_int4(job, pass, 0, 0);
 }
 
 // Claims up to `want` consecutive tasks below task_total; returns the first and sets got.
@@ -76,7 +76,7 @@ __global__ void k_batch_plan(BatchTasks* tasks, BatchCtl* ctl) {
 
 __global__ void __launch_bounds__(ENGINE_TB) k_batch_fill(const BatchJob* __restrict__ jobs,
                                                           const BatchTasks* tasks, const BatchCtl* ctl,
-                                                          PathState ps, int2* job_pass, const int* free_stack,
+                                                          PathState ps, SF<int4> job_pass, const int* free_stack,
                                                           int* q_closest, RoundCounters* rc, DevStats* st) {
   const int n = ctl->fill_n;
   const int top = ctl->fill_top;
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_fill(const BatchJob* __rest
   }
 }
 
-void launch_batch_fill(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, int2* job_pass,
+void launch_batch_fill(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, SF<int4> job_pass,
                        int* free_stack, int* q_closest, RoundCounters* rc, DevStats* st, int grid, cudaStream_t s) {
   k_batch_plan<<<1, 32, 0, s>>>(tasks, ctl);
   k_batch_fill<<<grid, ENGINE_TB, 0, s>>>(jobs, tasks, ctl, ps, job_pass, free_stack, q_closest, rc, st);
@@ -119,7 +119,7 @@ void launch_batch_fill(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, c
 // ---- logic with regeneration ----
 __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __restrict__ jobs, BatchTasks* tasks,
                                                            BatchCtl* ctl,
-                                                           PathState ps, int2* job_pass, int* free_stack,
+                                                           PathState ps, SF<int4> job_pass, int* free_stack,
                                                            const int* __restrict__ in_closest,
                                                            const int* __restrict__ in_any, const RoundCounters* rc_in,
                                                            int* out_closest, int* out_any, RoundCounters* rc_out,
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __res
     LogicCounts lc;
     if (e < n) {
       p = use_sorted ? sorted[e] : (e < nc ? in_closest[e] : in_any[e - nc]);
-      const int2 jp = job_pass[p];
+      const int4 jp = job_pass[p];
       const BatchJob& J = jobs[jp.x];
       const int reset = (jp.y == 0) ? J.reset_first : 0;
       emit = logic_path(J.pp, reset, ps, p, lc);
@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __res
   }
 }
 
-void launch_batch_logic(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, int2* job_pass,
+void launch_batch_logic(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, SF<int4> job_pass,
                         int* free_stack,
                         const int* in_closest, const int* in_any, const RoundCounters* rc_in, int* out_closest,
                         int* out_any, RoundCounters* rc_out, DevStats* st, unsigned long long* job_done,
@@ -227,7 +227,7 @@ __device__ __forceinline__ int material_class(const yc_material& m) {
   return (m.ks.x > 0.0f || m.ks.y > 0.0f || m.ks.z > 0.0f) ? 1 : 0;   // a glossy lobe can be drawn
 }
 
-__device__ __forceinline__ int logic_key(const BatchJob* jobs, const int2* job_pass, const PathState& ps, int p) {
+__device__ __forceinline__ int logic_key(const BatchJob* jobs, SF<int4> job_pass, const PathState& ps, int p) {
   const DevScene& sc = jobs[job_pass[p].x].pp.sc;
   const int st = ps.misc[p].z & 15;   // the phase a path waits in: S_PRIMARY..S_EXT
   int mat;
@@ -242,7 +242,7 @@ __device__ __forceinline__ int logic_key(const BatchJob* jobs, const int2* job_p
 }
 
 __global__ void __launch_bounds__(ENGINE_TB) k_sort_hist(const BatchJob* __restrict__ jobs,
-                                                         const int2* __restrict__ job_pass, PathState ps,
+                                                         SF<int4> job_pass, PathState ps,
                                                          const int* __restrict__ in_closest,
                                                          const int* __restrict__ in_any, const RoundCounters* rc_in,
                                                          int* keys, SortCtl* sctl, int threshold) {
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(ENGINE_TB) k_sort_scatter(const int* __restric
   }
 }
 
-void launch_batch_sort(const BatchJob* jobs, const int2* job_pass, const PathState& ps, const int* in_closest,
+void launch_batch_sort(const BatchJob* jobs, SF<int4> job_pass, const PathState& ps, const int* in_closest,
                        const int* in_any, const RoundCounters* rc_in, int* keys, int* sorted, SortCtl* sctl,
                        int threshold, int grid, cudaStream_t s) {
   k_sort_hist<<<grid, ENGINE_TB, 0, s>>>(jobs, job_pass, ps, in_closest, in_any, rc_in, keys, sctl, threshold);
@@ -311,7 +311,7 @@ void launch_batch_sort(const BatchJob* jobs, const int2* job_pass, const PathSta
 template <bool ANY>
 struct BatchSrc {
   const BatchJob* jobs;
-  const int2* job_pass;
+  SF<int4> job_pass;
   const int* __restrict__ queue;
   SF<float4> ro;
   SF<float4> rd;
@@ -331,7 +331,7 @@ struct BatchSrc {
 };
 
 template <bool ANY, bool WIDE>
-__global__ void __launch_bounds__(TRACE_TB) k_batch_trace(const BatchJob* jobs, const int2* job_pass,
+__global__ void __launch_bounds__(TRACE_TB) k_batch_trace(const BatchJob* jobs, SF<int4> job_pass,
                                                           const int* __restrict__ queue, const int* __restrict__ count,
                                                           int* work, SF<float4> ro,
                                                           SF<float4> rd, SF<float4> hit, int stack_cap,
@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(TRACE_TB) k_batch_trace(const BatchJob* jobs, 
 // which keeps that split)
 struct BatchMixedSrc {
   const BatchJob* jobs;
-  const int2* job_pass;
+  SF<int4> job_pass;
   const int* __restrict__ q_closest;
   const int* __restrict__ q_any;
   const int* __restrict__ sorted;   // non-null: this round's sorted work list
@@ -370,7 +370,7 @@ struct BatchMixedSrc {
 };
 
 template <bool WIDE>
-__global__ void __launch_bounds__(TRACE_TB) k_batch_trace_mixed(const BatchJob* jobs, const int2* job_pass,
+__global__ void __launch_bounds__(TRACE_TB) k_batch_trace_mixed(const BatchJob* jobs, SF<int4> job_pass,
                                                                 const int* __restrict__ q_closest,
                                                                 const int* __restrict__ q_any,
                                                                 RoundCounters* rc, SF<float4> ro,
@@ -405,7 +405,7 @@ int batch_trace_mixed_grid(int stack_cap, bool wide) {
   return wide ? batch_grid_of(k_batch_trace_mixed<true>, smem) : batch_grid_of(k_batch_trace_mixed<false>, smem);
 }
 
-int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, const int2* job_pass, const int* q_closest,
+int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, SF<int4> job_pass, const int* q_closest,
                              const int* q_any, RoundCounters* rc, SF<float4> ro, SF<float4> rd, SF<float4> hit,
                              DevStats* st, int stack_cap, int grid_blocks, cudaStream_t s, const int* sorted,
                              const RaySortCtl* rs) {
@@ -419,7 +419,7 @@ int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, const int2* job_pa
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_batch_trace(bool any_hit, bool wide, const BatchJob* jobs, const int2* job_pass, const int* queue,
+int launch_batch_trace(bool any_hit, bool wide, const BatchJob* jobs, SF<int4> job_pass, const int* queue,
                        const int* count, int* work, SF<float4> ro, SF<float4> rd, SF<float4> hit, DevStats* st,
                        int stack_cap, int grid_blocks, cudaStream_t s) {
   const size_t smem = batch_smem(stack_cap);

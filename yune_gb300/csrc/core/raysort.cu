@@ -51,7 +51,7 @@ struct BoxOne {
 };
 struct BoxBatch {
   const BatchJob* jobs;
-  const int2* job_pass;
+  SF<int4> job_pass;
   __device__ __forceinline__ void of(int p, float4& l, float4& h) const {
     const DevScene& sc = jobs[job_pass[p].x].pp.sc;
     l = sc.root_lo;
@@ -191,7 +191,7 @@ int launch_raysort(const DevScene& sc, const int* q_closest, const int* q_any, c
   return launch_rs(BoxOne{sc.root_lo, sc.root_hi}, q_closest, q_any, rc, ro, rd, b, grid, s);
 }
 
-int launch_raysort_batch(const BatchJob* jobs, const int2* job_pass, const int* q_closest, const int* q_any,
+int launch_raysort_batch(const BatchJob* jobs, SF<int4> job_pass, const int* q_closest, const int* q_any,
                          const RoundCounters* rc, SF<float4> ro, SF<float4> rd, const RaySortBufs& b, int grid,
                          cudaStream_t s) {
   return launch_rs(BoxBatch{jobs, job_pass}, q_closest, q_any, rc, ro, rd, b, grid, s);

@@ -47,29 +47,29 @@ struct SortCtl {
   int cursor[SORT_KEYS];    // scatter cursors (exclusive prefix of count)
 };
 
-void launch_batch_sort(const BatchJob* jobs, const int2* job_pass, const PathState& ps, const int* in_closest,
+void launch_batch_sort(const BatchJob* jobs, SF<int4> job_pass, const PathState& ps, const int* in_closest,
                        const int* in_any, const RoundCounters* rc_in, int* keys, int* sorted, SortCtl* sctl,
                        int threshold, int grid, cudaStream_t s);
 
-void launch_batch_fill(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, int2* job_pass,
+void launch_batch_fill(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, SF<int4> job_pass,
                        int* free_stack, int* q_closest, RoundCounters* rc, DevStats* st, int grid, cudaStream_t s);
-void launch_batch_logic(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, int2* job_pass,
+void launch_batch_logic(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, SF<int4> job_pass,
                         int* free_stack, const int* in_closest, const int* in_any, const RoundCounters* rc_in,
                         int* out_closest, int* out_any, RoundCounters* rc_out, DevStats* st,
                         unsigned long long* job_done, const int* sorted, const SortCtl* sctl, int grid,
                         cudaStream_t s);
-int launch_batch_trace(bool any_hit, bool wide, const BatchJob* jobs, const int2* job_pass, const int* queue,
+int launch_batch_trace(bool any_hit, bool wide, const BatchJob* jobs, SF<int4> job_pass, const int* queue,
                        const int* count, int* work, SF<float4> ro, SF<float4> rd, SF<float4> hit, DevStats* st,
                        int stack_cap, int grid_blocks, cudaStream_t s);
 int batch_trace_grid(bool any_hit, int stack_cap, bool wide);
 // one launch over both queues of a round (closest-hit entries, then any-hit); the work
 // cursor is rc->work_closest
-int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, const int2* job_pass, const int* q_closest,
+int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, SF<int4> job_pass, const int* q_closest,
                              const int* q_any, RoundCounters* rc, SF<float4> ro, SF<float4> rd, SF<float4> hit,
                              DevStats* st, int stack_cap, int grid_blocks, cudaStream_t s,
                              const int* sorted = nullptr, const RaySortCtl* rs = nullptr);
 // raysort.cu, with the scene box of each ray's job
-int launch_raysort_batch(const BatchJob* jobs, const int2* job_pass, const int* q_closest, const int* q_any,
+int launch_raysort_batch(const BatchJob* jobs, SF<int4> job_pass, const int* q_closest, const int* q_any,
                          const RoundCounters* rc, SF<float4> ro, SF<float4> rd, const RaySortBufs& b, int grid,
                          cudaStream_t s);
 int batch_trace_mixed_grid(int stack_cap, bool wide);

@@ -14,12 +14,13 @@ namespace yc {
 // The logic kernel reads and writes a path's whole record, and after the shade-queue
 // sort neighbouring threads hold unrelated slots; one contiguous record per path keeps
 // every sector it fetches fully used (a field per array would use half of each). The
-// ray and its hit come first, so the traversal kernels touch the first two sectors only.
+// ray, the batch engine's (job, pass) pair and the hit come first, so the traversal
+// kernels touch the first two sectors only.
 // misc.x seed, misc.y pixel index, misc.z packed (state | flags << 4 | (j+1) << 12 |
 // (k+1) << 20), misc.w bounce index.
 constexpr int PS_STRIDE = 14;
-enum { PSF_RO = 0, PSF_RD, PSF_HIT, PSF_MISC, PSF_THR, PSF_THR_NEXT, PSF_DIRECT, PSF_INDIRECT, PSF_LS, PSF_HP,
-       PSF_NRM, PSF_WO, PSF_WI };
+enum { PSF_RO = 0, PSF_RD, PSF_JOB, PSF_HIT, PSF_MISC, PSF_THR, PSF_THR_NEXT, PSF_DIRECT, PSF_INDIRECT, PSF_LS,
+       PSF_HP, PSF_NRM, PSF_WO, PSF_WI };
 
 // one field of every record: slot i at p[i * PS_STRIDE]
 template <class T>
@@ -42,6 +43,7 @@ struct PathState {
   SF<float4> ro;         // emitted ray: origin xyz, length
   SF<float4> rd;         // emitted ray: direction xyz
   SF<float4> hit;        // trace result: (t, u, v, tri) or (occluded, -, -, -)
+  SF<int4> job;          // batch engine: (job, pass) of the slot's pixel task
 };
 
 // the path state of the records starting at rec (PS_STRIDE float4 per slot)
@@ -60,6 +62,7 @@ inline PathState path_state_at(float4* rec) {
   ps.ro = SF<float4>{rec + PSF_RO};
   ps.rd = SF<float4>{rec + PSF_RD};
   ps.hit = SF<float4>{rec + PSF_HIT};
+  ps.job = SF<int4>{reinterpret_cast<int4*>(rec + PSF_JOB)};
   return ps;
 }
 
