@@ -80,6 +80,8 @@ def parse():
     ap.add_argument("--ray-sort", type=int, default=32,
                     help="sort key of a round's rays: origin bits * 10 + direction bits per axis (0: queue order)")
     ap.add_argument("--ray-sort-min", type=int, default=65536, help="rounds with fewer rays are not sorted")
+    ap.add_argument("--shade-sort-min", type=int, default=65536,
+                    help="per-pass path: shade queues of at least this many paths are sorted (0: never)")
     ap.add_argument("--res", default="", help="c4: frame size WxH instead of 3840x2160 (profiling captures)")
     ap.add_argument("--tree", type=int, default=1,
                     help="interior hierarchy: 0 reference nodes, 1 binary SAH over the reference leaves, 2 four-wide")
@@ -313,6 +315,7 @@ def run_ours(args, rank, local, ws, dist):
     r.set_tail_paths(args.tail)
     r.set_mixed_trace(args.mixed)
     r.set_ray_sort(args.ray_sort // 10, args.ray_sort % 10, args.ray_sort_min)
+    r.set_shade_sort(args.shade_sort_min)
     sid = r.upload(scene)
     r.set_camera(scene.cam)
     l2 = r.measure_l2_gbs(48 << 20, 20)
@@ -439,7 +442,7 @@ def run_ours(args, rank, local, ws, dist):
         "per_pass": {"value": pp_rays / pp_s / 1e6, "ms_per_step": pp_ms / K, "unit": METRIC,
                      "note": "yc_render_pass per pass (the drop-in call), L2 flushed before each pass",
                      "kernel_ms": {"raygen": kt_pp["raygen_ms"], "raysort": kt_pp["raysort_ms"],
-                                   "trace": kt_pp["trace_ms"],
+                                   "sort": kt_pp["sort_ms"], "trace": kt_pp["trace_ms"],
                                    "extend": kt_pp["extend_ms"], "occlusion": kt_pp["occlusion_ms"],
                                    "logic": kt_pp["logic_ms"], "tail": kt_pp["tail_ms"], "rounds": kt_pp["rounds"]},
                      "roofline": _trace_roofline(st_pp, kt_pp, l2, pk, pk_kind,
@@ -505,6 +508,7 @@ def run_perpass_bdpt(args, rank, local, ws, dist):
     r.set_tree_mode(args.tree)
     r.set_mixed_trace(args.mixed)
     r.set_ray_sort(args.ray_sort // 10, args.ray_sort % 10, args.ray_sort_min)
+    r.set_shade_sort(args.shade_sort_min)
     t0 = time.perf_counter()
     sid = r.upload(scene)
     r.synchronize()
@@ -598,6 +602,7 @@ def run_c2(args):
     r.set_tree_mode(args.tree)
     r.set_mixed_trace(args.mixed)
     r.set_ray_sort(args.ray_sort // 10, args.ray_sort % 10, args.ray_sort_min)
+    r.set_shade_sort(args.shade_sort_min)
     sids = [r.upload(s) for s in jobs]
     seeds = [scenes.pass_seeds(1000 + i, s.spp) for i, s in enumerate(jobs)]
     px = sum(s.width * s.height for s in jobs)
@@ -675,6 +680,7 @@ def run_c3(args):
     r.set_tree_mode(args.tree)
     r.set_mixed_trace(args.mixed)
     r.set_ray_sort(args.ray_sort // 10, args.ray_sort % 10, args.ray_sort_min)
+    r.set_shade_sort(args.shade_sort_min)
     srv = serve.Server(r, resident, hbm_budget=args.hbm_budget_mb << 20, pool_paths=args.pool or (1 << 21))
     runs = []
     for rate in rates:

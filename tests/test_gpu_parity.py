@@ -319,6 +319,35 @@ def test_ray_sort_gives_the_same_pass(renderer, key):
         assert out[0][1][k] == out[1][1][k], k
 
 
+def test_shade_sort_gives_the_same_pass(renderer):
+    """Sorting every round's shade queue by path phase and material class (forced with a
+    threshold of one path) changes no bit and no ray count of yc_render_pass."""
+    s = scenes.c1(48, 40, level=5)
+    seeds = scenes.pass_seeds(19, 2)
+    sid = renderer.upload(s)
+    renderer.set_camera(s.cam)
+    out = []
+    for min_paths in (0, 1):
+        renderer.set_shade_sort(min_paths)
+        renderer.reset_stats()
+        renderer.set_profiling(True)
+        aid = renderer.alloc_accum(48, 40)
+        renderer.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+        out.append((renderer.read_accum(aid), renderer.stats(), renderer.kernel_times()))
+        renderer.set_profiling(False)
+        renderer.free_accum(aid)
+    renderer.set_shade_sort(65536)
+    renderer.release(sid)
+    assert out[0][2]["sort_launches"] == 0 and out[1][2]["sort_launches"] > 0
+    ref = np.zeros((40, 48, 4), np.float32)
+    for k, sd in enumerate(seeds):
+        O.render(s, ref, sd, 1 if k == 0 else 0, s.cfg)
+    for img, st, _ in out:
+        assert np.array_equal(img.view(np.int32), ref.view(np.int32))
+    for k in ("rays", "ext_rays", "any_rays", "traversed", "samples"):
+        assert out[0][1][k] == out[1][1][k], k
+
+
 @pytest.mark.parametrize("tree", [1, 2])
 def test_tail_kernel_gives_the_same_pass(renderer, tree):
     """Finishing the last paths a thread each (YC_OPT_TAIL) changes no bit of the pass and

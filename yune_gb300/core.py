@@ -160,6 +160,11 @@ class Renderer:
         if min_rays is not None:
             N.check(self.L.yc_set_option(self.h, 5, int(min_rays)), "yc_set_option")
 
+    def set_shade_sort(self, min_paths):
+        """Per-pass shade queues of at least min_paths paths are sorted by phase and
+        material class before shading (0: never)."""
+        N.check(self.L.yc_set_option(self.h, 6, int(min_paths)), "yc_set_option")
+
     def set_profiling(self, on=True):
         N.check(self.L.yc_set_profiling(self.h, int(on)), "yc_set_profiling")
 

@@ -65,6 +65,7 @@ struct Scene {
   DevBuf<yc_quad_light> lights;
   yc::DevScene dev{};
   uint64_t bytes = 0;
+  bool has_specular = false;   // a mirror or dielectric material: shading paths diverge most
 };
 
 struct Accum {
@@ -98,6 +99,10 @@ struct yc_ctx {
   int mixed_trace = 1;   // YC_OPT_MIXED_TRACE: one traversal launch per round for both ray kinds
   int rs_ob = 3, rs_db = 2;       // YC_OPT_RAY_SORT: origin / direction bits per axis of the sort key
   int rs_threshold = 65536;       // YC_OPT_RAY_SORT_MIN: rounds with fewer rays are not sorted
+  int ss_threshold = 65536;       // YC_OPT_SHADE_SORT_MIN: per-pass shade queues this long are sorted
+  DevBuf<int> ss_keys, ss_sorted;
+  DevBuf<yc::SortCtl> ss_ctl;
+  size_t ss_cap = 0;
   // ray sort of the per-pass path (raysort.cu)
   DevBuf<unsigned> rs_keys, rs_hist, rs_cursor, rs_blk;
   DevBuf<int> rs_sorted;
@@ -158,6 +163,17 @@ int ensure_raysort(yc_ctx* c, size_t n) {
     YC_CUDA(c->rs_keys.alloc(n));
     YC_CUDA(c->rs_sorted.alloc(n));
     c->rs_cap = n;
+  }
+  return 0;
+}
+
+// key and sorted-list buffers of the per-pass shade-queue sort, for n paths
+int ensure_shadesort(yc_ctx* c, size_t n) {
+  if (!c->ss_ctl.p) YC_CUDA(c->ss_ctl.alloc(1));
+  if (n > c->ss_cap) {
+    YC_CUDA(c->ss_keys.alloc(n));
+    YC_CUDA(c->ss_sorted.alloc(n));
+    c->ss_cap = n;
   }
   return 0;
 }
@@ -293,6 +309,14 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     rsb = yc::RaySortBufs{c->rs_keys.p, c->rs_hist.p, c->rs_cursor.p, c->rs_blk.p, c->rs_sorted.p, c->rs_ctl.p,
                           c->rs_ob, c->rs_db, c->rs_threshold};
   }
+  // shade-queue sort by phase and material class before the logic kernel (unidirectional
+  // passes whose frame can fill a sorted queue, in scenes with a mirror or dielectric:
+  // with diffuse and glossy materials alone the paths' shading code differs too little
+  // for the sort to pay, measured)
+  const bool shadesort = !bdpt && sc->has_specular && c->ss_threshold > 0 &&
+                         (size_t)W * H >= (size_t)c->ss_threshold;
+  if (shadesort)
+    if (int e = ensure_shadesort(c, (size_t)W * H)) return e;
   const int grid_c = yc::trace_grid_blocks(false, sc->dev.depth, sc->dev.wide != 0);
   const int grid_a = yc::trace_grid_blocks(true, sc->dev.depth, sc->dev.wide != 0);
   const int grid_m = mixed ? yc::trace_mixed_grid_blocks(sc->dev.depth, sc->dev.wide != 0) : 1;
@@ -352,11 +376,18 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
       YC_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     }
     YC_CUDA(cudaMemsetAsync(rout, 0, sizeof(yc::RoundCounters), c->stream));
+    if (shadesort) {
+      KTimer kt(c, K_SORT);
+      YC_CUDA(cudaMemsetAsync(c->ss_ctl.p, 0, sizeof(yc::SortCtl), c->stream));
+      yc::launch_pass_sort(sc->dev, ps, in_c, in_a, rin, c->ss_keys.p, c->ss_sorted.p, c->ss_ctl.p, c->ss_threshold,
+                           c->logic_grid, c->stream);
+    }
     {
       KTimer kt(c, K_LOGIC);
       if (bdpt) yc::launch_logic_bdpt(pp, ps, bb, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid,
                                       c->stream);
-      else yc::launch_logic(pp, ps, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid, c->stream);
+      else yc::launch_logic(pp, ps, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid, c->stream,
+                            shadesort ? c->ss_sorted.p : nullptr, shadesort ? c->ss_ctl.p : nullptr);
     }
     if (tail_at > 0) {
       KTimer kt(c, K_TAIL);
@@ -456,6 +487,8 @@ int yc_upload_scene(yc_ctx* c, const yc_triangle* tris, int n_tri, const yc_mate
   std::string err;
   if (yc::repack_scene(tris, n_tri, nodes, n_node, c->tree_mode, rp, err)) return fail(YC_E_INVALID, err);
   std::unique_ptr<Scene> s(new (std::nothrow) Scene);
+  if (s)
+    for (int i = 0; i < n_mat; ++i) s->has_specular = s->has_specular || mats[i].is_specular != 0;
   if (!s) return fail(YC_E_NOMEM, "host allocation failed");
   YC_CUDA(cudaSetDevice(c->device));
   YC_CUDA(s->nodes.alloc(std::max<size_t>(rp.nodes.size(), 4)));
@@ -770,6 +803,10 @@ int yc_set_option(yc_ctx* c, int option, int value) {
     case YC_OPT_RAY_SORT_MIN:
       if (value < 0) return fail(YC_E_INVALID, "ray sort threshold must be >= 0");
       c->rs_threshold = value;
+      return YC_OK;
+    case YC_OPT_SHADE_SORT_MIN:
+      if (value < 0) return fail(YC_E_INVALID, "shade sort threshold must be >= 0");
+      c->ss_threshold = value;
       return YC_OK;
     default:
       return fail(YC_E_INVALID, "unknown option");

@@ -227,8 +227,20 @@ __device__ __forceinline__ int material_class(const yc_material& m) {
   return (m.ks.x > 0.0f || m.ks.y > 0.0f || m.ks.z > 0.0f) ? 1 : 0;   // a glossy lobe can be drawn
 }
 
-__device__ __forceinline__ int logic_key(const BatchJob* jobs, SF<int4> job_pass, const PathState& ps, int p) {
-  const DevScene& sc = jobs[job_pass[p].x].pp.sc;
+// the scene of the path in slot p: its job's scene in a batch, or the pass's one scene
+struct SceneOfBatch {
+  const BatchJob* jobs;
+  SF<int4> job_pass;
+  __device__ __forceinline__ const DevScene& of(int p) const { return jobs[job_pass[p].x].pp.sc; }
+};
+struct SceneOfOne {
+  DevScene sc;
+  __device__ __forceinline__ const DevScene& of(int) const { return sc; }
+};
+
+template <class SceneOf>
+__device__ __forceinline__ int logic_key(const SceneOf& so, const PathState& ps, int p) {
+  const DevScene& sc = so.of(p);
   const int st = ps.misc[p].z & 15;   // the phase a path waits in: S_PRIMARY..S_EXT
   int mat;
   if (st == S_PRIMARY || st == S_EXT) {
@@ -241,8 +253,8 @@ __device__ __forceinline__ int logic_key(const BatchJob* jobs, SF<int4> job_pass
   return st * 5 + material_class(sc.mats[mat]);
 }
 
-__global__ void __launch_bounds__(ENGINE_TB) k_sort_hist(const BatchJob* __restrict__ jobs,
-                                                         SF<int4> job_pass, PathState ps,
+template <class SceneOf>
+__global__ void __launch_bounds__(ENGINE_TB) k_sort_hist(SceneOf so, PathState ps,
                                                          const int* __restrict__ in_closest,
                                                          const int* __restrict__ in_any, const RoundCounters* rc_in,
                                                          int* keys, SortCtl* sctl, int threshold) {
@@ -253,7 +265,7 @@ __global__ void __launch_bounds__(ENGINE_TB) k_sort_hist(const BatchJob* __restr
   if (n < threshold) return;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
     const int p = e < nc ? in_closest[e] : in_any[e - nc];
-    const int key = logic_key(jobs, job_pass, ps, p);
+    const int key = logic_key(so, ps, p);
     keys[e] = key;
     atomicAdd(&h[key], 1);
   }
@@ -302,7 +314,17 @@ __global__ void __launch_bounds__(ENGINE_TB) k_sort_scatter(const int* __restric
 void launch_batch_sort(const BatchJob* jobs, SF<int4> job_pass, const PathState& ps, const int* in_closest,
                        const int* in_any, const RoundCounters* rc_in, int* keys, int* sorted, SortCtl* sctl,
                        int threshold, int grid, cudaStream_t s) {
-  k_sort_hist<<<grid, ENGINE_TB, 0, s>>>(jobs, job_pass, ps, in_closest, in_any, rc_in, keys, sctl, threshold);
+  k_sort_hist<SceneOfBatch><<<grid, ENGINE_TB, 0, s>>>(SceneOfBatch{jobs, job_pass}, ps, in_closest, in_any, rc_in,
+                                                        keys, sctl, threshold);
+  k_sort_scan<<<1, 32, 0, s>>>(rc_in, sctl, threshold);
+  k_sort_scatter<<<grid, ENGINE_TB, 0, s>>>(in_closest, in_any, rc_in, keys, sorted, sctl);
+}
+
+void launch_pass_sort(const DevScene& sc, const PathState& ps, const int* in_closest, const int* in_any,
+                      const RoundCounters* rc_in, int* keys, int* sorted, SortCtl* sctl, int threshold, int grid,
+                      cudaStream_t s) {
+  k_sort_hist<SceneOfOne><<<grid, ENGINE_TB, 0, s>>>(SceneOfOne{sc}, ps, in_closest, in_any, rc_in, keys, sctl,
+                                                      threshold);
   k_sort_scan<<<1, 32, 0, s>>>(rc_in, sctl, threshold);
   k_sort_scatter<<<grid, ENGINE_TB, 0, s>>>(in_closest, in_any, rc_in, keys, sorted, sctl);
 }

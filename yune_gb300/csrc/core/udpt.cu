@@ -69,7 +69,8 @@ void launch_raygen(const PassParams& pp, const PathState& ps, int* q_closest, Ro
 __global__ void __launch_bounds__(LOGIC_TB) k_logic(PassParams pp, PathState ps, const int* __restrict__ in_closest,
                                                     const int* __restrict__ in_any, const RoundCounters* rc_in,
                                                     int* out_closest, int* out_any, RoundCounters* rc_out,
-                                                    DevStats* st) {
+                                                    DevStats* st, const int* __restrict__ sorted,
+                                                    const SortCtl* sctl) {
   __shared__ unsigned long long s_cnt[8];   // rays, extension, shadow, mis, traversed, samples
   if (threadIdx.x < 8) s_cnt[threadIdx.x] = 0;
   __syncthreads();
@@ -78,13 +79,14 @@ __global__ void __launch_bounds__(LOGIC_TB) k_logic(PassParams pp, PathState ps,
   const int lane = threadIdx.x & 31;
   const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int warps_total = (gridDim.x * blockDim.x) >> 5;
+  const bool use_sorted = sctl && sctl->use;
   for (int wbase = warp_global * 32; wbase < n; wbase += warps_total * 32) {
     const int e = wbase + lane;
     int emit = 0;
     int p = -1;
     LogicCounts lc;
     if (e < n) {
-      p = e < nc ? in_closest[e] : in_any[e - nc];
+      p = use_sorted ? sorted[e] : (e < nc ? in_closest[e] : in_any[e - nc]);
       emit = logic_path(pp, pp.reset, ps, p, lc);
     }
     // compaction: ballot + popc prefix per queue, one atomic per warp and queue
@@ -123,8 +125,9 @@ __global__ void __launch_bounds__(LOGIC_TB) k_logic(PassParams pp, PathState ps,
 
 void launch_logic(const PassParams& pp, const PathState& ps, const int* in_closest, const int* in_any,
                   const RoundCounters* rc_in, int* out_closest, int* out_any, RoundCounters* rc_out, DevStats* st,
-                  int grid, cudaStream_t s) {
-  k_logic<<<grid, LOGIC_TB, 0, s>>>(pp, ps, in_closest, in_any, rc_in, out_closest, out_any, rc_out, st);
+                  int grid, cudaStream_t s, const int* sorted, const SortCtl* sctl) {
+  k_logic<<<grid, LOGIC_TB, 0, s>>>(pp, ps, in_closest, in_any, rc_in, out_closest, out_any, rc_out, st, sorted,
+                                    sctl);
 }
 
 // ---- tonemap (kernels/post-proc/tonemap.cl:14-47) ----

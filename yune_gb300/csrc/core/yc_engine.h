@@ -37,16 +37,6 @@ struct BatchCtl {
   unsigned long long fill_t0;      //   and the first of them
 };
 
-// Sorting of the shade queue by path phase (S_PRIMARY..S_EXT) and material class
-// (diffuse, glossy, mirror, dielectric, no surface): key = phase * 5 + class.
-constexpr int SORT_KEYS = 20;
-struct SortCtl {
-  int use;                  // 1: this round's shade queue is the sorted one
-  int pad_;
-  int count[SORT_KEYS];     // paths per key
-  int cursor[SORT_KEYS];    // scatter cursors (exclusive prefix of count)
-};
-
 void launch_batch_sort(const BatchJob* jobs, SF<int4> job_pass, const PathState& ps, const int* in_closest,
                        const int* in_any, const RoundCounters* rc_in, int* keys, int* sorted, SortCtl* sctl,
                        int threshold, int grid, cudaStream_t s);
@@ -68,6 +58,10 @@ int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, SF<int4> job_pass,
                              const int* q_any, RoundCounters* rc, SF<float4> ro, SF<float4> rd, SF<float4> hit,
                              DevStats* st, int stack_cap, int grid_blocks, cudaStream_t s,
                              const int* sorted = nullptr, const RaySortCtl* rs = nullptr);
+// the same shade-queue sort for the per-pass path (one scene)
+void launch_pass_sort(const DevScene& sc, const PathState& ps, const int* in_closest, const int* in_any,
+                      const RoundCounters* rc_in, int* keys, int* sorted, SortCtl* sctl, int threshold, int grid,
+                      cudaStream_t s);
 // raysort.cu, with the scene box of each ray's job
 int launch_raysort_batch(const BatchJob* jobs, SF<int4> job_pass, const int* q_closest, const int* q_any,
                          const RoundCounters* rc, SF<float4> ro, SF<float4> rd, const RaySortBufs& b, int grid,

@@ -99,6 +99,16 @@ struct RaySortBufs {
   int threshold;       // rounds with fewer rays are traced unsorted
 };
 
+// Sorting of the shade queue by path phase (S_PRIMARY..S_EXT) and material class
+// (diffuse, glossy, mirror, dielectric, no surface): key = phase * 5 + class (engine.cu).
+constexpr int SORT_KEYS = 20;
+struct SortCtl {
+  int use;                  // 1: this round's shade queue is the sorted one
+  int pad_;
+  int count[SORT_KEYS];     // paths per key
+  int cursor[SORT_KEYS];    // scatter cursors (exclusive prefix of count)
+};
+
 // device-wide statistics (yc_stats layout, 64-bit counters)
 struct DevStats {
   unsigned long long rays, primary, extension, shadow, mis, connection, traversed, samples, stack_overflow;
@@ -121,9 +131,12 @@ struct PassParams {
 // launchers (udpt.cu / trace.cu)
 void launch_raygen(const PassParams& pp, const PathState& ps, int* q_closest, RoundCounters* rc, DevStats* st,
                    cudaStream_t s);
+// sorted/sctl: the round's shade queue sorted by phase and material class, used when
+// sctl->use is set (null: the queues in order)
 void launch_logic(const PassParams& pp, const PathState& ps, const int* in_closest, const int* in_any,
                   const RoundCounters* rc_in, int* out_closest, int* out_any, RoundCounters* rc_out,
-                  DevStats* st, int grid, cudaStream_t s);
+                  DevStats* st, int grid, cudaStream_t s, const int* sorted = nullptr,
+                  const SortCtl* sctl = nullptr);
 int launch_trace(const DevScene& sc, bool any_hit, const int* queue, const int* count, int* work,
                  SF<float4> ro, SF<float4> rd, SF<float4> hit, DevStats* st, int grid_blocks,
                  cudaStream_t s);
