@@ -6,8 +6,10 @@
 // emission and next-event estimate and connects it to every light vertex j >= 1 with a
 // shadow ray (shading, bdpt.cl:562-640). Here each path is a state machine like the
 // unidirectional one (udpt.cu): the logic kernel advances it to its next ray, the extend
-// and occlusion kernels trace the queues, and the subpath vertices live in HBM in
-// structure-of-arrays form, vertex k of path p at [(k * 4 + field) * N + p]:
+// and occlusion kernels trace the queues, and the subpath vertices live in HBM as one
+// 64-byte record per vertex (two full 32-byte sectors: a connection reads two vertices of
+// a path whose neighbours in the queue are unrelated), vertex k of path p at
+// [(p * bounces + k) * 4 + field]:
 //   field 0: hit point xyz, material index (int bits)
 //   field 1: shading normal xyz
 //   field 2: direction of the ray that reached the vertex xyz
@@ -52,10 +54,8 @@ __device__ __forceinline__ int pack_st(int state, int flags, int lj, int k) {
 }
 
 struct VertexRef {
-  float4* base;
-  size_t N;
-  int p;
-  __device__ __forceinline__ float4& at(int k, int f) const { return base[((size_t)k * 4 + f) * N + p]; }
+  float4* base;     // the path's first vertex
+  __device__ __forceinline__ float4& at(int k, int f) const { return base[(size_t)k * 4 + f]; }
   __device__ __forceinline__ void store(int k, const Vtx& v, f4 dir, f4 contrib) const {
     at(k, 0) = make_float4(v.hp.x, v.hp.y, v.hp.z, __int_as_float(v.mat));
     at(k, 1) = make_float4(v.n.x, v.n.y, v.n.z, 0.0f);
@@ -111,8 +111,8 @@ __global__ void __launch_bounds__(256) k_raygen_bdpt(PassParams pp, PathState ps
     d.z = ym::dot(ld4(pp.cam.r3), dir);
     d.w = ym::dot(ld4(pp.cam.r4), dir);
     d = ym::normalize(d);
-    VertexRef ev{bb.ev, bb.N, slot};
-    VertexRef lv{bb.lv, bb.N, slot};
+    VertexRef ev{bb.ev + (size_t)slot * bb.bounces * 4};
+    VertexRef lv{bb.lv + (size_t)slot * bb.bounces * 4};
     ev.at(0, 2) = make_float4(d.x, d.y, d.z, d.w);   // the camera ray, traced after the light subpath
     // light vertex 0 on light 0 (createLightPath, bdpt.cl:435-456)
     const yc_quad_light& L = sc.lights[0];
@@ -201,8 +201,8 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(PassParams pp, PathState ps,
     unsigned c[7] = {0, 0, 0, 0, 0, 0, 0};
     if (e < n) {
       p = e < nc ? in_closest[e] : in_any[e - nc];
-      const VertexRef lv{bb.lv, bb.N, p};
-      const VertexRef ev{bb.ev, bb.N, p};
+      const VertexRef lv{bb.lv + (size_t)p * bb.bounces * 4};
+      const VertexRef ev{bb.ev + (size_t)p * bb.bounces * 4};
       const int4 misc = ps.misc[p];
       uint32_t seed = (uint32_t)misc.x;
       const int pix = misc.y;

@@ -7,8 +7,8 @@
 
 namespace yc {
 
-// subpath vertices, structure of arrays: vertex k of path p, field f at
-// [(k * 4 + f) * N + p]; `bounces` vertices per subpath (BDPT_BOUNCES)
+// subpath vertices, one 64-byte record (4 float4 fields) per vertex: vertex k of path p,
+// field f at [(p * bounces + k) * 4 + f]; `bounces` vertices per subpath (BDPT_BOUNCES)
 struct BdptBuffers {
   float4* lv;
   float4* ev;
