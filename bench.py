@@ -559,7 +559,7 @@ def run_perpass_bdpt(args, rank, local, ws, dist):
         for k in ("hbm_peak", "hbm_frac", "hbm_peak_source"):
             roof.pop(k, None)
     launches = int(kt["raygen_launches"] + kt["extend_launches"] + kt["occlusion_launches"] + kt["trace_launches"]
-                   + kt["logic_launches"] + kt["tail_launches"] + 3 * kt["raysort_launches"])
+                   + kt["logic_launches"] + kt["tail_launches"] + 3 * kt["raysort_launches"] + 3 * kt["sort_launches"])
     line = {
         "metric": METRIC, "value": rays / t_s / 1e6, "unit": METRIC, "n_gpus": ws, "steps": K, "warmup": Wm,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
@@ -572,8 +572,8 @@ def run_perpass_bdpt(args, rank, local, ws, dist):
         "samples_per_s": st["samples"] * (ws if dist else 1) / t_s,
         "rays_per_sample": st["rays"] / max(1, st["samples"]),
         "gpu_launches": launches,
-        "kernel_ms": {"raygen": kt["raygen_ms"], "raysort": kt["raysort_ms"], "trace": kt["trace_ms"],
-                      "extend": kt["extend_ms"],
+        "kernel_ms": {"raygen": kt["raygen_ms"], "raysort": kt["raysort_ms"], "sort": kt["sort_ms"],
+                      "trace": kt["trace_ms"], "extend": kt["extend_ms"],
                       "occlusion": kt["occlusion_ms"], "logic": kt["logic_ms"], "rounds": kt["rounds"]},
         "roofline": roof,
         "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else 0.0, "unit": METRIC,

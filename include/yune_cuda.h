@@ -241,10 +241,11 @@ enum {
    * yc_render_pass also leaves scenes of fewer than 4096 triangles unsorted (their walks are
    * too short for the sort to pay). */
   YC_OPT_RAY_SORT_MIN = 5,
-  /* yc_render_pass (unidirectional passes in scenes with a mirror or dielectric material):
-   * shade queues of at least this many paths are sorted by path phase and material class
-   * before the shading kernel, as the batch engine's sort_threshold does; 0 = never.
-   * Default 65536. Same results either way. */
+  /* yc_render_pass (BDPT passes, and unidirectional passes in scenes with a mirror or
+   * dielectric material, in frames of at least 524288 pixels): shade queues of at least
+   * this many paths are sorted by path phase and material class before the shading
+   * kernel, as the batch engine's sort_threshold does; 0 = never. Default 65536. Same
+   * results either way. */
   YC_OPT_SHADE_SORT_MIN = 6
 };
 int yc_set_option(yc_ctx* ctx, int option, int value);

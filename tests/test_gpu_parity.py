@@ -203,6 +203,36 @@ def test_render_parity_bdpt(renderer, bounces, lights):
     assert st["samples"] == 40 * 32 * 2
 
 
+@pytest.mark.parametrize("lights", [1, 4])
+def test_bdpt_shade_sort_gives_the_same_pass(renderer, lights):
+    """BDPT with every round's shade queue sorted by path state and material class
+    (threshold of one path): every pixel against the oracle, the ray count unchanged."""
+    s = scenes.c0_bdpt(1024, 512, bounces=8, lights=lights)   # large enough a frame to be sorted
+    seeds = scenes.pass_seeds(13, 1)
+    sid = renderer.upload(s)
+    renderer.set_camera(s.cam)
+    renderer.set_shade_sort(1)
+    renderer.reset_stats()
+    renderer.set_profiling(True)
+    aid = renderer.alloc_accum(1024, 512)
+    renderer.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+    gpu = renderer.read_accum(aid)
+    st = renderer.stats()
+    kt = renderer.kernel_times()
+    renderer.set_profiling(False)
+    renderer.set_shade_sort(65536)
+    renderer.free_accum(aid)
+    renderer.release(sid)
+    assert kt["sort_launches"] > 0
+    ref = np.zeros((512, 1024, 4), np.float32)
+    rays = 0
+    for k, sd in enumerate(seeds):
+        rays += O.render_bdpt(s, ref, sd, 1 if k == 0 else 0, 8, threads=0)["rays"]
+    assert _rel_bad(gpu, ref) == 0
+    assert np.array_equal(gpu[..., 3], ref[..., 3])
+    assert st["rays"] == rays
+
+
 def test_c4_stress_scene_bdpt_parity(renderer):
     """The stress scene itself (10,004,490 triangles, 8.5M reference nodes, four lights,
     BDPT with 8 vertices per subpath) on a 32 x 18 crop of the frame, two passes: every
@@ -322,8 +352,8 @@ def test_ray_sort_gives_the_same_pass(renderer, key):
 def test_shade_sort_gives_the_same_pass(renderer):
     """Sorting every round's shade queue by path phase and material class (forced with a
     threshold of one path) changes no bit and no ray count of yc_render_pass."""
-    s = scenes.c1(48, 40, level=5)
-    seeds = scenes.pass_seeds(19, 2)
+    s = scenes.c1(1024, 512, level=5)   # large enough a frame to be sorted
+    seeds = scenes.pass_seeds(19, 1)
     sid = renderer.upload(s)
     renderer.set_camera(s.cam)
     out = []
@@ -331,7 +361,7 @@ def test_shade_sort_gives_the_same_pass(renderer):
         renderer.set_shade_sort(min_paths)
         renderer.reset_stats()
         renderer.set_profiling(True)
-        aid = renderer.alloc_accum(48, 40)
+        aid = renderer.alloc_accum(1024, 512)
         renderer.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
         out.append((renderer.read_accum(aid), renderer.stats(), renderer.kernel_times()))
         renderer.set_profiling(False)
@@ -339,7 +369,7 @@ def test_shade_sort_gives_the_same_pass(renderer):
     renderer.set_shade_sort(65536)
     renderer.release(sid)
     assert out[0][2]["sort_launches"] == 0 and out[1][2]["sort_launches"] > 0
-    ref = np.zeros((40, 48, 4), np.float32)
+    ref = np.zeros((512, 1024, 4), np.float32)
     for k, sd in enumerate(seeds):
         O.render(s, ref, sd, 1 if k == 0 else 0, s.cfg)
     for img, st, _ in out:

@@ -25,21 +25,6 @@
 
 namespace yc {
 
-enum : int {
-  // states that wait for a trace result
-  B_LIGHT = 0,   // closest hit of the light-subpath ray that makes light vertex i
-  B_EYE0 = 1,    // closest hit of the camera ray
-  B_EYE = 2,     // closest hit of the eye-subpath ray that makes eye vertex i
-  B_NEE = 3,     // shadow ray of the next-event estimate at eye vertex i
-  B_CONN = 4,    // connection ray between eye vertex i and light vertex j
-  // transient phases
-  Q_LIGHT_SAMPLE = 8,
-  Q_EYE_START = 9,
-  Q_EYE_SAMPLE = 10,
-  Q_VERTEX = 11,
-  Q_CONNECT = 12,
-  Q_FINISH = 13
-};
 enum : int { BF_GLOSSY = 1, BF_OCCLUDED = 2 };
 
 struct BCount {
@@ -180,7 +165,8 @@ void launch_raygen_bdpt(const PassParams& pp, const PathState& ps, const BdptBuf
 __global__ void __launch_bounds__(256) k_logic_bdpt(PassParams pp, PathState ps, BdptBuffers bb,
                                                     const int* __restrict__ in_closest, const int* __restrict__ in_any,
                                                     const RoundCounters* rc_in, int* out_closest, int* out_any,
-                                                    RoundCounters* rc_out, DevStats* st) {
+                                                    RoundCounters* rc_out, DevStats* st, const int* __restrict__ sorted,
+                                                    const SortCtl* sctl) {
   __shared__ unsigned long long s_cnt[8];   // rays, primary, extension, shadow, connection, traversed, samples
   if (threadIdx.x < 8) s_cnt[threadIdx.x] = 0;
   __syncthreads();
@@ -193,6 +179,7 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(PassParams pp, PathState ps,
   const float INF = __int_as_float(0x7f800000);
   const int BOUNCES = bb.bounces;
   const int RR = 4;   // RR_THRESHOLD of bdpt.cl:4
+  const bool use_sorted = sctl && sctl->use;
 
   for (int wbase = warp_global * 32; wbase < n; wbase += warps_total * 32) {
     const int e = wbase + lane;
@@ -200,7 +187,7 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(PassParams pp, PathState ps,
     int p = -1;
     unsigned c[7] = {0, 0, 0, 0, 0, 0, 0};
     if (e < n) {
-      p = e < nc ? in_closest[e] : in_any[e - nc];
+      p = use_sorted ? sorted[e] : (e < nc ? in_closest[e] : in_any[e - nc]);
       const VertexRef lv{bb.lv + (size_t)p * bb.bounces * 4};
       const VertexRef ev{bb.ev + (size_t)p * bb.bounces * 4};
       const int4 misc = ps.misc[p];
@@ -540,8 +527,10 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(PassParams pp, PathState ps,
 
 void launch_logic_bdpt(const PassParams& pp, const PathState& ps, const BdptBuffers& bb, const int* in_closest,
                        const int* in_any, const RoundCounters* rc_in, int* out_closest, int* out_any,
-                       RoundCounters* rc_out, DevStats* st, int grid, cudaStream_t s) {
-  k_logic_bdpt<<<grid, 256, 0, s>>>(pp, ps, bb, in_closest, in_any, rc_in, out_closest, out_any, rc_out, st);
+                       RoundCounters* rc_out, DevStats* st, int grid, cudaStream_t s, const int* sorted,
+                       const SortCtl* sctl) {
+  k_logic_bdpt<<<grid, 256, 0, s>>>(pp, ps, bb, in_closest, in_any, rc_in, out_closest, out_any, rc_out, st, sorted,
+                                    sctl);
 }
 
 }  // namespace yc

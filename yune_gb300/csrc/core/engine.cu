@@ -15,6 +15,7 @@
 // round waits on its last rays, the other groups' kernels use the idle SMs.
 #include <cuda_runtime.h>
 
+#include "yc_bdpt.h"
 #include "yc_engine.h"
 #include "yc_trace_loop.cuh"
 #include "yc_udpt.cuh"
@@ -238,23 +239,38 @@ struct SceneOfOne {
   __device__ __forceinline__ const DevScene& of(int) const { return sc; }
 };
 
-template <class SceneOf>
-__device__ __forceinline__ int logic_key(const SceneOf& so, const PathState& ps, int p) {
-  const DevScene& sc = so.of(p);
-  const int st = ps.misc[p].z & 15;   // the phase a path waits in: S_PRIMARY..S_EXT
-  int mat;
-  if (st == S_PRIMARY || st == S_EXT) {
+// unidirectional paths: the phase, and the material of the surface the step shades
+struct KeyUdpt {
+  template <class SceneOf>
+  __device__ __forceinline__ int operator()(const SceneOf& so, const PathState& ps, int p) const {
+    const DevScene& sc = so.of(p);
+    const int st = ps.misc[p].z & 15;   // the phase a path waits in: S_PRIMARY..S_EXT
+    int mat;
+    if (st == S_PRIMARY || st == S_EXT) {
+      const int tri = __float_as_int(ps.hit[p].w);
+      if (tri < 0) return st * 5 + 4;
+      mat = __float_as_int(__ldg(sc.shade + 4 * (size_t)tri + 3).x);
+    } else {
+      mat = __float_as_int(ps.wi[p].w);
+    }
+    return st * 5 + material_class(sc.mats[mat]);
+  }
+};
+// BDPT paths: the state, and for a closest-hit result the material of the surface hit
+struct KeyBdpt {
+  template <class SceneOf>
+  __device__ __forceinline__ int operator()(const SceneOf& so, const PathState& ps, int p) const {
+    const int st = ps.misc[p].z & 15;   // B_LIGHT..B_CONN
+    if (st == B_NEE || st == B_CONN) return st * 5;
     const int tri = __float_as_int(ps.hit[p].w);
     if (tri < 0) return st * 5 + 4;
-    mat = __float_as_int(__ldg(sc.shade + 4 * (size_t)tri + 3).x);
-  } else {
-    mat = __float_as_int(ps.wi[p].w);
+    const DevScene& sc = so.of(p);
+    return st * 5 + material_class(sc.mats[__float_as_int(__ldg(sc.shade + 4 * (size_t)tri + 3).x)]);
   }
-  return st * 5 + material_class(sc.mats[mat]);
-}
+};
 
-template <class SceneOf>
-__global__ void __launch_bounds__(ENGINE_TB) k_sort_hist(SceneOf so, PathState ps,
+template <class SceneOf, class Key>
+__global__ void __launch_bounds__(ENGINE_TB) k_sort_hist(SceneOf so, Key key_of, PathState ps,
                                                          const int* __restrict__ in_closest,
                                                          const int* __restrict__ in_any, const RoundCounters* rc_in,
                                                          int* keys, SortCtl* sctl, int threshold) {
@@ -265,7 +281,7 @@ __global__ void __launch_bounds__(ENGINE_TB) k_sort_hist(SceneOf so, PathState p
   if (n < threshold) return;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
     const int p = e < nc ? in_closest[e] : in_any[e - nc];
-    const int key = logic_key(so, ps, p);
+    const int key = key_of(so, ps, p);
     keys[e] = key;
     atomicAdd(&h[key], 1);
   }
@@ -314,17 +330,21 @@ __global__ void __launch_bounds__(ENGINE_TB) k_sort_scatter(const int* __restric
 void launch_batch_sort(const BatchJob* jobs, SF<int4> job_pass, const PathState& ps, const int* in_closest,
                        const int* in_any, const RoundCounters* rc_in, int* keys, int* sorted, SortCtl* sctl,
                        int threshold, int grid, cudaStream_t s) {
-  k_sort_hist<SceneOfBatch><<<grid, ENGINE_TB, 0, s>>>(SceneOfBatch{jobs, job_pass}, ps, in_closest, in_any, rc_in,
-                                                        keys, sctl, threshold);
+  k_sort_hist<<<grid, ENGINE_TB, 0, s>>>(SceneOfBatch{jobs, job_pass}, KeyUdpt{}, ps, in_closest, in_any, rc_in, keys,
+                                         sctl, threshold);
   k_sort_scan<<<1, 32, 0, s>>>(rc_in, sctl, threshold);
   k_sort_scatter<<<grid, ENGINE_TB, 0, s>>>(in_closest, in_any, rc_in, keys, sorted, sctl);
 }
 
-void launch_pass_sort(const DevScene& sc, const PathState& ps, const int* in_closest, const int* in_any,
+void launch_pass_sort(const DevScene& sc, bool bdpt, const PathState& ps, const int* in_closest, const int* in_any,
                       const RoundCounters* rc_in, int* keys, int* sorted, SortCtl* sctl, int threshold, int grid,
                       cudaStream_t s) {
-  k_sort_hist<SceneOfOne><<<grid, ENGINE_TB, 0, s>>>(SceneOfOne{sc}, ps, in_closest, in_any, rc_in, keys, sctl,
-                                                      threshold);
+  if (bdpt)
+    k_sort_hist<<<grid, ENGINE_TB, 0, s>>>(SceneOfOne{sc}, KeyBdpt{}, ps, in_closest, in_any, rc_in, keys, sctl,
+                                           threshold);
+  else
+    k_sort_hist<<<grid, ENGINE_TB, 0, s>>>(SceneOfOne{sc}, KeyUdpt{}, ps, in_closest, in_any, rc_in, keys, sctl,
+                                           threshold);
   k_sort_scan<<<1, 32, 0, s>>>(rc_in, sctl, threshold);
   k_sort_scatter<<<grid, ENGINE_TB, 0, s>>>(in_closest, in_any, rc_in, keys, sorted, sctl);
 }

@@ -59,7 +59,7 @@ int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, SF<int4> job_pass,
                              DevStats* st, int stack_cap, int grid_blocks, cudaStream_t s,
                              const int* sorted = nullptr, const RaySortCtl* rs = nullptr);
 // the same shade-queue sort for the per-pass path (one scene)
-void launch_pass_sort(const DevScene& sc, const PathState& ps, const int* in_closest, const int* in_any,
+void launch_pass_sort(const DevScene& sc, bool bdpt, const PathState& ps, const int* in_closest, const int* in_any,
                       const RoundCounters* rc_in, int* keys, int* sorted, SortCtl* sctl, int threshold, int grid,
                       cudaStream_t s);
 // raysort.cu, with the scene box of each ray's job

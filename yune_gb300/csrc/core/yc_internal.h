@@ -99,9 +99,10 @@ struct RaySortBufs {
   int threshold;       // rounds with fewer rays are traced unsorted
 };
 
-// Sorting of the shade queue by path phase (S_PRIMARY..S_EXT) and material class
-// (diffuse, glossy, mirror, dielectric, no surface): key = phase * 5 + class (engine.cu).
-constexpr int SORT_KEYS = 20;
+// Sorting of the shade queue by the phase a path waits in (S_PRIMARY..S_EXT of the
+// unidirectional path, B_LIGHT..B_CONN of BDPT) and material class (diffuse, glossy,
+// mirror, dielectric, no surface): key = phase * 5 + class (engine.cu).
+constexpr int SORT_KEYS = 25;
 struct SortCtl {
   int use;                  // 1: this round's shade queue is the sorted one
   int pad_;
