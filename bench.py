@@ -216,9 +216,9 @@ def cpu_reference(scene, seeds, seconds, want_rays=True, band=0):
         return O.render(scene, a, seeds[k % len(seeds)], 1, cfg, threads=threads, rows=r)
 
     rows_done, t_total, rays = 0, 0.0, 0
-    for k, y in enumerate(starts):
-        if t_total >= seconds:
-            break
+    k = 0
+    while t_total < seconds:   # bands in order, frame after frame (pass k + 1 wraps around)
+        y = starts[k % len(starts)]
         r = (y, min(H, y + band))
         t0 = time.perf_counter()
         c = one(k, r, acc)
@@ -229,9 +229,11 @@ def cpu_reference(scene, seeds, seconds, want_rays=True, band=0):
             use_ref = use_ref_saved
         rays += c["rays"] if c else 0
         rows_done += r[1] - r[0]
+        k += 1
     value = rays / t_total / 1e6 if t_total > 0 else 0.0
     return {"value": value, "unit": METRIC, "cores": threads, "kind": kind,
-            "sample": "%d of %d rows x %d px, 1 pass, %.1f s%s" % (rows_done, H, W, t_total, note),
+            "sample": "%d rows of %d x %d px (%.2f passes' worth), %.1f s%s" % (rows_done, H, W, rows_done / H,
+                                                                            t_total, note),
             "samples_per_s": rows_done * W / t_total if t_total > 0 else 0.0}
 
 
