@@ -10,7 +10,8 @@
  *   yh_camera_look    <- Camera::setViewMatrix + Camera::setBuffer
  *                        src/Camera.cpp:66-82,105-117
  *   yh_scene_*        procedural scenes (Cornell box, seeded boxes, subdivided and
- *                     displaced icospheres, sphere grids) in place of OBJ files.
+ *                     displaced icospheres, sphere grids), and OBJ/MTL files
+ *                     (yh_scene_load_obj <- Scene::loadModel src/Scene.cpp:133-383)
  * Every function returns 0 on success and a negative YH_E* code on failure.
  */
 #ifndef YUNE_HOST_H
@@ -71,6 +72,17 @@ int yh_scene_add_cornell(yh_scene* s, uint64_t seed, float on_sigma2, float phon
 int yh_scene_add_icosphere(yh_scene* s, const float c[3], float r, int level,
                            float disp, uint64_t seed, int mat_id);
 int yh_scene_add_light(yh_scene* s, const yc_quad_light* l);
+/* Loads an OBJ file and its material file (named by the OBJ's first `mtllib` line, read
+ * from the OBJ's directory) the way Scene::loadModel does (src/Scene.cpp:133-383,
+ * :385-410): its triangles are appended with material indices offset by the materials
+ * already in the scene, so loading into an empty scene gives Scene::vert_data and
+ * Scene::mat_data. Quirks kept: `px` sets the py field and `py` the px field; a face
+ * reads its first three vertices; an unknown `usemtl` name is material 0; without an
+ * `mtllib` line the scene gets the default material (nothing is written to disk). A
+ * face without normal indices gets zero normals. *n_tri_loaded (may be NULL) receives the
+ * triangles added. YH_E_INVALID: a file cannot be read or has no material; YH_E_RANGE: a
+ * face index outside the vertices read so far. */
+int yh_scene_load_obj(yh_scene* s, const char* obj_path, int* n_tri_loaded);
 int yh_scene_counts(const yh_scene* s, int* n_tri, int* n_mat, int* n_light);
 int yh_scene_copy(const yh_scene* s, yc_triangle* tris, yc_material* mats, yc_quad_light* lights);
 

@@ -103,7 +103,7 @@ def build_ref(force=False):
                               os.path.join(HERE, "ref", "ref_harness.cpp")]
     if have_tree:
         cmd += ["-I" + os.path.join(HERE, "ref", "stub_include"), "-I" + os.path.join(REF_SRC, "include")]
-        cmd += [os.path.join(REF_SRC, "src", f) for f in ("BVH.cpp", "TriangleCPU.cpp", "BVHNodeCPU.cpp")]
+        cmd += [os.path.join(REF_SRC, "src", f) for f in ("BVH.cpp", "TriangleCPU.cpp", "BVHNodeCPU.cpp", "Scene.cpp")]
     else:
         cmd += ["-DYREF_NO_HOST"]
     cmd += ["-o", out]

@@ -77,6 +77,9 @@ def ref():
             L.ref_oren_nayar.argtypes = [vp, vp, vp, vp, vp, vp]
             if hasattr(L, "ref_bvh_build"):
                 L.ref_bvh_build.argtypes = [vp, i32, i32, i32, vp, i32, C.POINTER(i32)]
+            if hasattr(L, "ref_load_obj"):
+                L.ref_load_obj.argtypes = [C.c_char_p, C.c_char_p, vp, i32, C.POINTER(i32), vp, i32, C.POINTER(i32), vp,
+                                           i32, C.POINTER(i32)]
             _ref = L
     return _ref
 
@@ -194,6 +197,25 @@ def ref_trace(scene, rays9, any_hit=False):
     if rc != 0:
         raise RuntimeError("ref_trace failed: %d" % rc)
     return tri, light, t
+
+
+def ref_load_obj(path, cap_tris=1 << 20, cap_nodes=1 << 21, cap_mats=1024):
+    """Scene::loadModel of the compiled reference on an OBJ file: (triangles, materials,
+    BVH nodes) as the reference leaves them in Scene::vert_data, mat_data and
+    bvh.gpu_node_list (20 bins, leaf <= 10)."""
+    from yune_gb300.layouts import BVH_NODE, MATERIAL, TRIANGLE
+    L = ref()
+    if L is None or not hasattr(L, "ref_load_obj"):
+        raise RuntimeError("compiled reference loader not available")
+    tris = np.zeros(cap_tris, TRIANGLE)
+    mats = np.zeros(cap_mats, MATERIAL)
+    nodes = np.zeros(cap_nodes, BVH_NODE)
+    nt, nm, nn = i32(), i32(), i32()
+    rc = L.ref_load_obj(os.fsencode(path), os.fsencode(os.path.basename(path)), _p(tris), cap_tris, C.byref(nt),
+                        _p(mats), cap_mats, C.byref(nm), _p(nodes), cap_nodes, C.byref(nn))
+    if rc != 0:
+        raise RuntimeError("ref_load_obj failed: %d" % rc)
+    return tris[:nt.value].copy(), mats[:nm.value].copy(), nodes[:nn.value].copy()
 
 
 def ref_tonemap(accum):

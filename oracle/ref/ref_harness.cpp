@@ -303,4 +303,34 @@ extern "C" int ref_bvh_build(const yc_triangle* t, int nt, int bins, int leaf, y
   std::memcpy(out, bvh.gpu_node_list.data(), bvh.gpu_node_list.size() * sizeof(yc_bvh_node));
   return 0;
 }
+
+// The reference OBJ/MTL loader (Scene::loadModel, src/Scene.cpp:133-383, compiled
+// unchanged against glm stand-ins). Its Camera member is never used by the loader; the
+// two Camera members the Scene object needs are defined here as no-ops (the camera code
+// needs the full glm).
+#define private public
+#include "Scene.h"
+#undef private
+namespace yune {
+Camera::Camera() {}
+Camera::~Camera() {}
+}  // namespace yune
+
+extern "C" int ref_load_obj(const char* path, const char* filename, yc_triangle* tris, int cap_t, int* nt,
+                            yc_material* mats, int cap_m, int* nm, yc_bvh_node* nodes, int cap_n, int* nn) {
+  yune::Scene s;
+  try {
+    s.loadModel(path, filename);
+  } catch (...) {
+    return -1;
+  }
+  *nt = (int)s.vert_data.size();
+  *nm = (int)s.mat_data.size();
+  *nn = (int)s.bvh.gpu_node_list.size();
+  if (*nt > cap_t || *nm > cap_m || *nn > cap_n) return -3;
+  for (int i = 0; i < *nt; ++i) std::memcpy(&tris[i], &s.vert_data[i], sizeof(yc_triangle));
+  for (int i = 0; i < *nm; ++i) std::memcpy(&mats[i], &s.mat_data[i], sizeof(yc_material));
+  if (*nn) std::memcpy(nodes, s.bvh.gpu_node_list.data(), (size_t)*nn * sizeof(yc_bvh_node));
+  return 0;
+}
 #endif

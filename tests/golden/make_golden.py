@@ -15,6 +15,10 @@ reference tree:
   oren_nayar.npz       OrenNayarBRDF (kernels/legacy/udpt-primitives.cl:696-725)
   render_bdpt.npz      2 passes of the BDPT `pathtracer` (kernels/legacy/bdpt.cl with
                        BDPT_BOUNCES 8) on a 32x24 Cornell box with 1 and with 4 lights
+  obj_test_scene.npz   Scene::loadModel (src/Scene.cpp:133-383) on the loader test files
+                       of obj_files.py: triangles, materials and the BVH node array
+  obj_cornellbox.npz   the same on the reference's geometry/cornellbox.obj (the test
+                       that uses it needs that file and skips without it)
 Each file records a SHA-256 of the scene arrays it was made from.
 """
 import hashlib
@@ -50,9 +54,33 @@ def node_fields(nodes):
                                    nodes["vert_list"], -1).astype(np.int32))
 
 
+TRI_FIELDS = ("v1", "v2", "v3", "vn1", "vn2", "vn3", "matID")
+
+
+def obj_fields(tris, mats, nodes, no_normals=()):
+    """The loader's output as comparable arrays (padding bytes and vert_list entries past
+    a leaf's count, which the reference leaves unset, are dropped; so are the normals of
+    the triangles in no_normals, faces without normal indices, written as zeros)."""
+    out = {"tri_" + k: np.ascontiguousarray(tris[k]) for k in TRI_FIELDS}
+    for k in ("vn1", "vn2", "vn3"):
+        out["tri_" + k][list(no_normals)] = 0.0
+    out["mats"] = np.ascontiguousarray(mats).view(np.uint8).reshape(len(mats), -1)
+    out.update({"node_" + k: v for k, v in node_fields(nodes).items()})
+    return out
+
+
 def main():
     if O.ref() is None:
         raise SystemExit("the compiled reference is not available here")
+    import tempfile
+    sys.path.insert(0, HERE)
+    import obj_files
+    from oracle import build_oracle
+    with tempfile.TemporaryDirectory() as d:
+        np.savez_compressed(os.path.join(HERE, "obj_test_scene.npz"),
+                            **obj_fields(*O.ref_load_obj(obj_files.write(d)), no_normals=obj_files.NO_NORMALS))
+    np.savez_compressed(os.path.join(HERE, "obj_cornellbox.npz"),
+                        **obj_fields(*O.ref_load_obj(os.path.join(build_oracle.REF_SRC, "geometry", "cornellbox.obj"))))
     for name, s in golden_scenes().items():
         leaf = 10 if name == "c0" else 4
         nodes = O.ref_bvh(s.tris, 20, leaf)

@@ -110,9 +110,12 @@ def test_oracle_bdpt_matches_reference(lights):
 
 # ---- live comparisons against the compiled reference (where the reference tree is) ----
 needs_ref = pytest.mark.skipif(O.ref() is None, reason="compiled reference not available")
+# the reference's host code (BVH builder, loader) is compiled only where its sources are
+needs_ref_host = pytest.mark.skipif(O.ref() is None or not hasattr(O.ref(), "ref_bvh_build"),
+                                    reason="compiled reference host code not available")
 
 
-@needs_ref
+@needs_ref_host
 @pytest.mark.parametrize("level,leaf", [(4, 4), (5, 4), (4, 10)])
 def test_bvh_builder_live(level, leaf):
     s = scenes.c1(16, 16, level=level)
@@ -123,7 +126,7 @@ def test_bvh_builder_live(level, leaf):
         assert np.array_equal(np.asarray(a[k]).view(np.int32), np.asarray(b[k]).view(np.int32)), k
 
 
-@needs_ref
+@needs_ref_host
 def test_bvh_builder_median_and_displaced_live():
     b = scenes.Builder().cornell(seed=3)
     mid = b.add_material(scenes.material(kd=(0.5, 0.5, 0.5)))

@@ -97,6 +97,7 @@ SIGNATURES = {
     "yh_scene_add_icosphere": (i32, [vp, vp, f32, i32, f32, C.c_uint64, i32]),
     "yh_scene_add_light": (i32, [vp, vp]),
     "yh_scene_counts": (i32, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
+    "yh_scene_load_obj": (i32, [vp, C.c_char_p, C.POINTER(i32)]),
     "yh_scene_copy": (i32, [vp, vp, vp, vp]),
 }
 

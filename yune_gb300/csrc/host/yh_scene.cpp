@@ -11,6 +11,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <cstdlib>
 #include <map>
 #include <new>
 #include <random>
@@ -250,5 +254,188 @@ extern "C" int yh_scene_copy(const yh_scene* s, yc_triangle* tris, yc_material* 
   if (tris && !s->tris.empty()) std::memcpy(tris, s->tris.data(), s->tris.size() * sizeof(yc_triangle));
   if (mats && !s->mats.empty()) std::memcpy(mats, s->mats.data(), s->mats.size() * sizeof(yc_material));
   if (lights && !s->lights.empty()) std::memcpy(lights, s->lights.data(), s->lights.size() * sizeof(yc_quad_light));
+  return YH_OK;
+}
+
+// ---- OBJ/MTL ingestion: Scene::loadModel (src/Scene.cpp:133-383) restated ----
+//
+// Rules kept from the reference, so that the triangle, material and BVH arrays equal its
+// own for the same files:
+//   * the material file is named by an `mtllib` line that must be the first line of the
+//     OBJ that is neither empty nor a comment (Scene::getMatFileName, :385-410), and is
+//     read from the OBJ's directory; without one the scene gets the default material
+//     (newMaterial, include/CL_headers.h:109-124) as material 0 "default" (the reference
+//     also writes that default material file to disk; this loader writes nothing);
+//   * material keys ke/kd/ks (w = 1), n, k, alpha_x, alpha_y, is_specular,
+//     is_transmissive; `px` sets the py field and `py` the px field (:215-218);
+//     numbers that fail to parse keep the previous line's value, as the reference's
+//     shared x, y, z do;
+//   * OBJ: `v` (w = 1) and `vn` (w = 0) append to lists that `o` does not reset; `o`
+//     forgets the current material name; `usemtl` selects a material by name (an unknown
+//     name: material 0); a face before any `usemtl` takes material 0; a face reads its
+//     first three vertices `v`, `v//vn` or `v/vt/vn` (texture indices are skipped,
+//     further vertices ignored);
+//   * lines whose first character is '#' and empty lines are skipped.
+// Departures: a face without normal indices gets zero normals (the reference leaves them
+// undefined); an index outside the lists read so far is an error (the reference reads out
+// of bounds).
+namespace {
+
+bool read_float(std::istringstream& ss, float& v) {
+  std::string tok;
+  if (!(ss >> tok)) return false;
+  char* end = nullptr;
+  const float f = std::strtof(tok.c_str(), &end);
+  if (end == tok.c_str()) return false;
+  v = f;
+  return true;
+}
+
+bool read_int(std::istringstream& ss, int& v) {
+  std::string tok;
+  if (!(ss >> tok)) return false;
+  char* end = nullptr;
+  const long x = std::strtol(tok.c_str(), &end, 10);
+  if (end == tok.c_str()) return false;
+  v = (int)x;
+  return true;
+}
+
+yc_material default_material() {
+  yc_material m;
+  std::memset(&m, 0, sizeof(m));
+  m.ke = yc_float4{0, 0, 0, 1};
+  m.kd = yc_float4{0.3f, 0.3f, 0.3f, 1};
+  m.ks = yc_float4{0, 0, 0, 1};
+  m.n = 1; m.k = 1; m.px = 1; m.py = 1; m.alpha_x = 100; m.alpha_y = 100;
+  return m;
+}
+
+// first line of the OBJ that is neither empty nor a comment, if it is `mtllib <name>`
+std::string mtllib_of(const std::string& obj_path) {
+  std::ifstream f(obj_path);
+  std::string line;
+  while (std::getline(f, line)) {
+    if (line.empty() || line[0] == '#') continue;
+    std::istringstream ss(line);
+    std::string key, name;
+    ss >> key;
+    if (key != "mtllib") return "";
+    ss >> name;
+    return name;
+  }
+  return "";
+}
+
+int load_materials(const std::string& path, std::vector<yc_material>& mats, std::map<std::string, int>& index) {
+  std::ifstream f(path);
+  if (!f.is_open()) return YH_E_INVALID;
+  std::string line;
+  float x = 0, y = 0, z = 0;
+  const size_t first = mats.size();
+  while (std::getline(f, line)) {
+    if (line.empty() || line[0] == '#') continue;
+    std::istringstream ss(line);
+    std::string key;
+    ss >> key;
+    if (key == "newmtl") {
+      std::string id;
+      ss >> id;
+      index[id] = (int)(mats.size() - first);
+      mats.push_back(default_material());
+      continue;
+    }
+    if (mats.size() == first) continue;   // keys before the first newmtl
+    yc_material& m = mats.back();
+    if (key == "ke" || key == "kd" || key == "ks") {
+      read_float(ss, x) && read_float(ss, y) && read_float(ss, z);
+      yc_float4& c = key == "ke" ? m.ke : (key == "kd" ? m.kd : m.ks);
+      c = yc_float4{x, y, z, 1.0f};
+    } else if (key == "n") read_float(ss, m.n);
+    else if (key == "k") read_float(ss, m.k);
+    else if (key == "px") read_float(ss, m.py);   // swapped as in the reference
+    else if (key == "py") read_float(ss, m.px);
+    else if (key == "alpha_x") read_float(ss, m.alpha_x);
+    else if (key == "alpha_y") read_float(ss, m.alpha_y);
+    else if (key == "is_specular") read_int(ss, m.is_specular);
+    else if (key == "is_transmissive") read_int(ss, m.is_transmissive);
+  }
+  return mats.size() > first ? YH_OK : YH_E_INVALID;   // "Bad Material file."
+}
+
+}  // namespace
+
+extern "C" int yh_scene_load_obj(yh_scene* s, const char* obj_path, int* n_tri_loaded) {
+  if (!s || !obj_path) return YH_E_INVALID;
+  try {
+    const std::string path(obj_path);
+    const size_t slash = path.find_last_of('/');
+    const std::string dir = slash == std::string::npos ? std::string() : path.substr(0, slash + 1);
+    const int mat_base = (int)s->mats.size();
+    std::map<std::string, int> index;
+    const std::string mtl = mtllib_of(path);
+    if (mtl.empty()) {
+      index["default"] = 0;
+      s->mats.push_back(default_material());
+    } else if (int r = load_materials(dir + mtl, s->mats, index)) {
+      s->mats.resize(mat_base);
+      return r;
+    }
+    std::ifstream f(path);
+    if (!f.is_open()) { s->mats.resize(mat_base); return YH_E_INVALID; }
+    std::vector<D3> v, vn;
+    std::string line, mat_name;
+    int idx = -1;
+    const size_t tri_base = s->tris.size();
+    while (std::getline(f, line)) {
+      if (line.empty() || line[0] == '#') continue;
+      std::istringstream ss(line);
+      std::string key;
+      ss >> key;
+      if (key == "o") {
+        mat_name.clear();
+      } else if (key == "v" || key == "vn") {
+        float c[3] = {0, 0, 0};
+        for (int k = 0; k < 3 && read_float(ss, c[k]); ++k) {}
+        (key == "v" ? v : vn).push_back(D3{c[0], c[1], c[2]});
+      } else if (key == "usemtl") {
+        ss >> mat_name;
+        const auto it = index.find(mat_name);
+        idx = it != index.end() ? it->second : 0;
+      } else if (key == "f") {
+        if (idx < 0) {
+          const auto it = index.find(mat_name);
+          idx = it != index.end() ? it->second : 0;
+        }
+        D3 p[3] = {}, n[3] = {};
+        for (int i = 0; i < 3; ++i) {
+          std::string tok;
+          if (!(ss >> tok)) { s->tris.resize(tri_base); s->mats.resize(mat_base); return YH_E_INVALID; }
+          std::istringstream ts(tok);
+          std::string part;
+          for (int j = 0; std::getline(ts, part, '/'); ++j) {
+            if (j == 1 || part.empty() || j > 2) continue;
+            const long k = std::strtol(part.c_str(), nullptr, 10) - 1;
+            const std::vector<D3>& list = j == 0 ? v : vn;
+            if (k < 0 || k >= (long)list.size()) { s->tris.resize(tri_base); s->mats.resize(mat_base); return YH_E_RANGE; }
+            (j == 0 ? p[i] : n[i]) = list[k];
+          }
+        }
+        yc_triangle t;
+        std::memset(&t, 0, sizeof(t));
+        t.v1 = yc_float4{(float)p[0].x, (float)p[0].y, (float)p[0].z, 1.0f};
+        t.v2 = yc_float4{(float)p[1].x, (float)p[1].y, (float)p[1].z, 1.0f};
+        t.v3 = yc_float4{(float)p[2].x, (float)p[2].y, (float)p[2].z, 1.0f};
+        t.vn1 = yc_float4{(float)n[0].x, (float)n[0].y, (float)n[0].z, 0.0f};
+        t.vn2 = yc_float4{(float)n[1].x, (float)n[1].y, (float)n[1].z, 0.0f};
+        t.vn3 = yc_float4{(float)n[2].x, (float)n[2].y, (float)n[2].z, 0.0f};
+        t.matID = mat_base + idx;
+        s->tris.push_back(t);
+      }
+    }
+    if (n_tri_loaded) *n_tri_loaded = (int)(s->tris.size() - tri_base);
+  } catch (const std::bad_alloc&) {
+    return YH_E_NOMEM;
+  }
   return YH_OK;
 }

@@ -17,6 +17,7 @@ Configurations (sizes and spp of the benchmark workloads):
       subpath; 3840x2160, 128 spp; leaf <= 4.
 """
 import ctypes as C
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -96,6 +97,13 @@ class Builder:
         N.check(N.lib().yh_scene_add_icosphere(self.h, ptr(c), radius, level, disp, seed, mat_id), "icosphere")
         return self
 
+    def load_obj(self, path):
+        """Appends an OBJ file and its material file (yh_scene_load_obj, the rules of
+        Scene::loadModel); returns the number of triangles read."""
+        n = C.c_int()
+        N.check(N.lib().yh_scene_load_obj(self.h, os.fsencode(path), C.byref(n)), "yh_scene_load_obj " + str(path))
+        return n.value
+
     def add_light(self, l):
         N.check(N.lib().yh_scene_add_light(self.h, ptr(l)), "light")
         return self
@@ -135,6 +143,33 @@ def camera(eye=(0.0, 0.0, 1.4), side=(1.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), look=(
 
 def dielectric(ior=1.5, r0=0.04):
     return material(kd=(0, 0, 0), ks=(r0, r0, r0), n=ior, specular=1, transmissive=1, alpha=0.0)
+
+
+def reference_light():
+    """The one quad light compiled into Yune's kernels (kernels/legacy/udpt.cl:97-106),
+    placed for the reference's Cornell-box OBJ: corner (-0.1979, 0.92, -3.1972), facing -y,
+    edges 0.4 along x and z, emission 16."""
+    l = np.zeros(1, QUAD_LIGHT)
+    l["pos"] = (-0.1979, 0.92, -3.1972, 1.0)
+    l["normal"] = (0.0, -1.0, 0.0, 0.0)
+    l["ke"] = (16.0, 16.0, 16.0, 0.0)
+    l["edge_l"] = (0.4, 0.0, 0.0, 0.0)
+    l["edge_w"] = (0.0, 0.0, 0.4, 0.0)
+    return l
+
+
+def from_obj(path, width=512, height=512, spp=64, lights=None, cam=None, bins=20, leaf=10, cfg=None):
+    """A scene loaded from an OBJ/MTL pair as Yune loads it (Scene::loadModel; BVH with the
+    reference's 20 bins and leaves of up to 10 triangles by default). Lights default to
+    the reference kernel's quad light, the camera to Yune's default camera (eye at the
+    origin looking down -z, 60 degree vertical field of view)."""
+    b = Builder()
+    b.load_obj(path)
+    tris, mats, _ = b.arrays()
+    nodes, depth = build_bvh(tris, bins, leaf)
+    return SceneData(tris, mats, reference_light() if lights is None else lights, nodes, depth,
+                     camera(eye=(0.0, 0.0, 0.0)) if cam is None else cam, width, height, spp,
+                     cfg or default_cfg(mis=0, rr_threshold=6, brdf_model=0, mis_lobe_fix=0), "obj")
 
 
 def c0(width=512, height=512, spp=64, seed=0):
