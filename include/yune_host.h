@@ -86,6 +86,15 @@ int yh_scene_load_obj(yh_scene* s, const char* obj_path, int* n_tri_loaded);
 int yh_scene_counts(const yh_scene* s, int* n_tri, int* n_mat, int* n_light);
 int yh_scene_copy(const yh_scene* s, yc_triangle* tris, yc_material* mats, yc_quad_light* lights);
 
+/* ---- image output (RendererCore::saveImage, src/RendererCore.cpp:608-646) ----
+ * rgba: width*height float4 pixels, row y at rgba + y*width*4 (the layout of yc_tonemap
+ * and yc_read_accum). As the reference writes them, the file's first row is the frame's
+ * last row. yh_write_png: 8-bit RGB of the tonemapped frame, each channel
+ * round(clamp(c, 0, 1) * 255) as GL converts it for glReadPixels (uncompressed deflate).
+ * yh_write_hdr: Radiance RGBE of linear radiance (flat scanlines). JPEG is not written. */
+int yh_write_png(const char* path, int width, int height, const float* rgba);
+int yh_write_hdr(const char* path, int width, int height, const float* rgba);
+
 #ifdef __cplusplus
 }
 #endif

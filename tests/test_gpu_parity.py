@@ -262,6 +262,33 @@ def test_render_obj_scene(renderer, tmp_path):
     assert np.isfinite(gpu).all() and gpu[..., :3].max() > 0.0
 
 
+def test_save_image_round_trip(renderer, tmp_path):
+    """Renderer.save_image (RendererCore::saveImage without GL): the PNG holds the 8-bit
+    conversion of the tonemapped frame, rows flipped; the HDR the accumulator's radiance."""
+    import zlib
+    s = scenes.c0(40, 24)
+    sid = renderer.upload(s)
+    renderer.set_camera(s.cam)
+    aid = renderer.alloc_accum(40, 24)
+    renderer.render_passes(sid, aid, scenes.pass_seeds(5, 2), reset_first=1, cfg=s.cfg)
+    renderer.save_image(aid, tmp_path / "f.png")
+    renderer.save_image(aid, tmp_path / "f.hdr")
+    ldr = renderer.tonemap(aid)
+    acc = renderer.read_accum(aid)
+    renderer.free_accum(aid)
+    renderer.release(sid)
+    data = open(tmp_path / "f.png", "rb").read()
+    idat = data[data.index(b"IDAT") + 4:data.index(b"IEND") - 8]
+    raw = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(24, 40 * 3 + 1)[:, 1:].reshape(24, 40, 3)
+    want = np.floor(np.clip(np.nan_to_num(ldr[::-1, :, :3]), 0, 1) * np.float32(255) + np.float32(0.5))
+    assert np.array_equal(raw, want.astype(np.uint8))
+    px = open(tmp_path / "f.hdr", "rb").read().split(b"\n\n", 1)[1].split(b"\n", 1)[1]
+    rgbe = np.frombuffer(px, np.uint8).reshape(24, 40, 4).astype(np.float64)
+    dec = np.where(rgbe[..., 3:] > 0, rgbe[..., :3] * np.ldexp(1.0, (rgbe[..., 3:] - 136).astype(int)), 0.0)
+    ref = acc[::-1, :, :3].astype(np.float64)
+    assert (np.abs(dec - ref) <= ref.max(axis=-1, keepdims=True) * 2.0 ** -7 + 1e-30).all()
+
+
 def test_c4_stress_scene_bdpt_parity(renderer):
     """The stress scene itself (10,004,490 triangles, 8.5M reference nodes, four lights,
     BDPT with 8 vertices per subpath) on a 32 x 18 crop of the frame, two passes: every

@@ -98,6 +98,8 @@ SIGNATURES = {
     "yh_scene_add_light": (i32, [vp, vp]),
     "yh_scene_counts": (i32, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
     "yh_scene_load_obj": (i32, [vp, C.c_char_p, C.POINTER(i32)]),
+    "yh_write_png": (i32, [C.c_char_p, i32, i32, vp]),
+    "yh_write_hdr": (i32, [C.c_char_p, i32, i32, vp]),
     "yh_scene_copy": (i32, [vp, vp, vp, vp]),
 }
 

@@ -8,12 +8,25 @@
     img = r.tonemap(aid)                 # the `tonemap` pass
 """
 import ctypes as C
+import os
 import weakref
 
 import numpy as np
 
 from . import _native as N
 from .layouts import ptr
+
+
+def write_png(path, rgba):
+    """8-bit RGB PNG of an (H, W, 4) float frame (yh_write_png), first file row = last frame row."""
+    a = np.ascontiguousarray(rgba, np.float32)
+    N.check(N.lib().yh_write_png(os.fsencode(str(path)), a.shape[1], a.shape[0], ptr(a)), "yh_write_png")
+
+
+def write_hdr(path, rgba):
+    """Radiance RGBE file of an (H, W, 4) float frame (yh_write_hdr)."""
+    a = np.ascontiguousarray(rgba, np.float32)
+    N.check(N.lib().yh_write_hdr(os.fsencode(str(path)), a.shape[1], a.shape[0], ptr(a)), "yh_write_hdr")
 
 
 def cfg_struct(cfg):
@@ -147,6 +160,17 @@ class Renderer:
     def set_tail_paths(self, n):
         """Paths left at which a pass finishes in the tail kernel (-1 auto, 0 off)."""
         N.check(self.L.yc_set_option(self.h, 2, int(n)), "yc_set_option")
+
+    def save_image(self, aid, path):
+        """RendererCore::saveImage without GL: `.png` writes the tonemapped frame as 8-bit
+        RGB, `.hdr` the accumulator's linear radiance as Radiance RGBE."""
+        ext = os.path.splitext(str(path))[1].lower()
+        if ext == ".png":
+            write_png(path, self.tonemap(aid))
+        elif ext == ".hdr":
+            write_hdr(path, self.read_accum(aid))
+        else:
+            raise ValueError("image output is .png or .hdr")
 
     def set_mixed_trace(self, on):
         """1: a round's closest-hit and any-hit rays share one traversal launch (default);
