@@ -516,6 +516,19 @@ def run_perpass_bdpt(args, rank, local, ws, dist):
     r.synchronize()
     upload_s = time.perf_counter() - t0
     scene_bytes = r.scene_bytes(sid)
+    # the reference BVH of this scene built on the host (yh_bvh_build) and on the GPU
+    # (yc_bvh_build), compared node for node
+    leaf = 4 if args.config == "c4" else 10
+    t0 = time.perf_counter()
+    h_nodes, _ = scenes.build_bvh(scene.tris, 20, leaf)
+    host_bvh_s = time.perf_counter() - t0
+    r.build_bvh(scene.tris, 20, leaf)   # warm-up (allocation, module load)
+    t0 = time.perf_counter()
+    g_nodes, _ = r.build_bvh(scene.tris, 20, leaf)
+    gpu_bvh_s = time.perf_counter() - t0
+    bvh_equal = bool(len(g_nodes) == len(h_nodes) and all(np.array_equal(g_nodes[k], h_nodes[k]) for k in
+                                                          ("p_min", "p_max", "child_idx", "vert_len")))
+    del h_nodes, g_nodes
     r.set_camera(scene.cam)
     l2 = r.measure_l2_gbs(48 << 20, 20)
     pk, pk_kind = peaks()
@@ -569,6 +582,10 @@ def run_perpass_bdpt(args, rank, local, ws, dist):
         "config": {"workload": workload_string(args.config, scene),
                    "spp_total": scene.spp, "tree_mode": args.tree, "scene_device_bytes": scene_bytes,
                    "host_build_s": build_s, "upload_s": upload_s,
+                   "bvh_build": {"host_s": host_bvh_s, "gpu_s": gpu_bvh_s, "equal": bvh_equal,
+                                 "what": "BVH::createBVH node array, 20 bins, leaf <= %d: yh_bvh_build on the host "
+                                         "core against yc_bvh_build on the GPU (host copy of the nodes included)"
+                                         % leaf},
                    "l2": "L2 flushed before each step" + ("; the node and triangle set is larger than L2" if big else ""),
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "samples_per_s": st["samples"] * (ws if dist else 1) / t_s,

@@ -113,6 +113,19 @@ int yc_upload_scene(yc_ctx* ctx, const yc_triangle* tris_host, int n_tri, const 
                     int n_mat, const yc_bvh_node* nodes_host, int n_node, const yc_quad_light* lights_host,
                     int n_light, int* scene_id);
 int yc_set_lights(yc_ctx* ctx, int scene_id, const yc_quad_light* lights_host, int n_light);
+
+/* ---- BVH build on the device: BVH::createBVH (src/BVH.cpp:56-247) ----
+ * Builds, on the context's GPU, the node array the reference builder makes for these
+ * triangles (bins: BVH::bins, 20 in the reference; leaf_max: BVH::leaf_primitives, 1..10;
+ * the root box is the union of the padded triangle boxes, as Scene::loadModel computes
+ * it): breadth-first order, the same splits and the same refit; a bound that is zero is
+ * stored as +0. *n_node and *depth receive the node count and the tree depth; the array
+ * stays with the context until the next build and is read with yc_bvh_copy_nodes
+ * (capacity >= *n_node), ready for yc_upload_scene. Synchronous. YC_E_INVALID when more
+ * than leaf_max triangles share one centroid (the reference builder does not terminate). */
+int yc_bvh_build(yc_ctx* ctx, const yc_triangle* tris_host, int n_tri, int bins, int leaf_max, int* n_node,
+                 int* depth);
+int yc_bvh_copy_nodes(yc_ctx* ctx, yc_bvh_node* nodes_host, int capacity);
 int yc_release_scene(yc_ctx* ctx, int scene_id);
 /* bytes the scene holds on the device */
 int yc_scene_bytes(yc_ctx* ctx, int scene_id, uint64_t* bytes);

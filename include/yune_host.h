@@ -33,6 +33,8 @@ enum {
 /* ---- BVH (src/BVH.cpp) ---- */
 typedef struct yh_bvh yh_bvh;
 /* Builds the breadth-first binned BVH of BVH::createBVH over tris[0..n_tri).
+ * YH_E_RANGE: the tree would pass 1024 levels, which happens when more than leaf_max
+ * triangles share one centroid (the reference builder does not terminate there).
  * bins: BVH::bins (20 by default; <= 2 selects median splits only).
  * leaf_max: BVH::leaf_primitives (10 in the reference; 1..10).
  * The root box is the union of the padded triangle boxes, as Scene::loadModel

@@ -77,6 +77,18 @@ class Renderer:
         N.check(self.L.yc_scene_depth(self.h, sid, C.byref(d)), "yc_scene_depth")
         return d.value
 
+    def build_bvh(self, tris, bins=20, leaf=10):
+        """BVH::createBVH on this renderer's GPU (yc_bvh_build): the node array of
+        scenes.build_bvh, and the tree depth."""
+        from .layouts import BVH_NODE
+        t = np.ascontiguousarray(tris)
+        n, d = C.c_int(), C.c_int()
+        N.check(self.L.yc_bvh_build(self.h, ptr(t), len(t), int(bins), int(leaf), C.byref(n), C.byref(d)),
+                "yc_bvh_build")
+        nodes = np.zeros(n.value, BVH_NODE)
+        N.check(self.L.yc_bvh_copy_nodes(self.h, ptr(nodes), n.value), "yc_bvh_copy_nodes")
+        return nodes, d.value
+
     def scene_bytes(self, sid):
         """Bytes the scene holds on the device."""
         b = C.c_uint64()

@@ -97,6 +97,8 @@ struct yc_ctx {
   int tree_mode = yc::TREE_SAH_OVER_LEAVES;
   int tail_paths = -1;   // YC_OPT_TAIL: -1 = one resident launch of the tail kernel, 0 = off
   int mixed_trace = 1;   // YC_OPT_MIXED_TRACE: one traversal launch per round for both ray kinds
+  std::vector<yc_bvh_node> built_nodes;   // the last yc_bvh_build
+  int built_depth = 0;
   int rs_ob = 3, rs_db = 2;       // YC_OPT_RAY_SORT: origin / direction bits per axis of the sort key
   int rs_threshold = 65536;       // YC_OPT_RAY_SORT_MIN: rounds with fewer rays are not sorted
   int ss_threshold = 65536;       // YC_OPT_SHADE_SORT_MIN: per-pass shade queues this long are sorted
@@ -533,6 +535,37 @@ int yc_upload_scene(yc_ctx* c, const yc_triangle* tris, int n_tri, const yc_mate
   const int id = c->next_scene++;
   c->scenes[id] = std::move(s);
   *scene_id = id;
+  return YC_OK;
+}
+
+int yc_bvh_build(yc_ctx* c, const yc_triangle* tris, int n_tri, int bins, int leaf_max, int* n_node, int* depth) {
+  if (!c || n_tri < 0 || (n_tri > 0 && !tris) || leaf_max < 1 || leaf_max > 10 || bins < 0 || bins > 256)
+    return fail(YC_E_INVALID, "yc_bvh_build: bad argument");
+  YC_CUDA(cudaSetDevice(c->device));
+  DevBuf<yc_triangle> dt;
+  YC_CUDA(dt.alloc(std::max(n_tri, 1)));
+  if (n_tri) YC_CUDA(cudaMemcpyAsync(dt.p, tris, n_tri * sizeof(yc_triangle), cudaMemcpyHostToDevice, c->stream));
+  int d = 0;
+  bool too_deep = false;
+  try {
+    YC_CUDA(yc::bvh_build_device(dt.p, n_tri, bins, leaf_max, c->stream, c->built_nodes, d, too_deep));
+  } catch (const std::bad_alloc&) {
+    return fail(YC_E_NOMEM, "yc_bvh_build: host allocation failed");
+  }
+  if (too_deep) {
+    c->built_nodes.clear();
+    return fail(YC_E_INVALID, "yc_bvh_build: more than leaf_max triangles share one centroid (the tree would not end)");
+  }
+  c->built_depth = d;
+  if (n_node) *n_node = (int)c->built_nodes.size();
+  if (depth) *depth = d;
+  return YC_OK;
+}
+
+int yc_bvh_copy_nodes(yc_ctx* c, yc_bvh_node* out, int capacity) {
+  if (!c || !out) return fail(YC_E_INVALID, "NULL argument");
+  if (capacity < (int)c->built_nodes.size()) return fail(YC_E_INVALID, "yc_bvh_copy_nodes: capacity below the node count");
+  std::memcpy(out, c->built_nodes.data(), c->built_nodes.size() * sizeof(yc_bvh_node));
   return YC_OK;
 }
 

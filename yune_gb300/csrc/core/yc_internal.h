@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "yc_scene.h"
 #include "yune_cuda.h"
 
@@ -162,5 +164,9 @@ int launch_raysort(const DevScene& sc, const int* q_closest, const int* q_any, c
                    SF<float4> ro, SF<float4> rd, const RaySortBufs& b, int grid, cudaStream_t s);
 int trace_mixed_grid_blocks(int depth, bool wide);
 int l2_read_gbs(size_t bytes, int iters, cudaStream_t s, double* gbs);
+// bvh_build.cu: BVH::createBVH on the device (the node array of the host builder)
+// too_deep: the tree would pass 1024 levels (more than leaf_max triangles with one centroid)
+cudaError_t bvh_build_device(const yc_triangle* tris_dev, int n, int bins, int leaf_max, cudaStream_t s,
+                             std::vector<yc_bvh_node>& out, int& depth, bool& too_deep);
 
 }  // namespace yc

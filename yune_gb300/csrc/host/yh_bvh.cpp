@@ -27,6 +27,11 @@
 
 namespace {
 
+// More than leaf_max triangles with one centroid can never be separated: every split
+// sends them all to the same child and the reference builder does not terminate. Trees
+// deeper than this are taken for that case and refused.
+constexpr int kMaxLevels = 1024;
+
 struct V3 { float s[4]; };
 
 struct TriInfo {
@@ -227,6 +232,10 @@ extern "C" int yh_bvh_build(const yc_triangle* tris, int n_tri, int bins, int le
       const int cidx = (int)nodes.size();
       nodes[ni].g.child_idx = cidx;
       const int d = node_depth[ni] + 1;
+      if (d > kMaxLevels) {   // a split that moves nothing, forever (see yh_bvh_build)
+        delete bvh;
+        return YH_E_RANGE;
+      }
       nodes.push_back(Node{fresh_node(best1), std::move(p1)});
       nodes.push_back(Node{fresh_node(best2), std::move(p2)});
       node_depth.push_back(d);
