@@ -20,7 +20,7 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
                    "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
-CXX_FLAGS = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math",
+CXX_FLAGS = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math,-pthread",
              "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 
 CU_SOURCES = ["core/api.cu", "core/trace.cu", "core/udpt.cu", "core/bench_kernels.cu", "core/noalloc.cu", "core/bdpt.cu",
@@ -72,7 +72,7 @@ def build(force=False, jobs=None):
         list(ex.map(lambda a: _compile(*a), todo))
     objs = [_obj(s) for s in CU_SOURCES + CXX_SOURCES]
     if force or todo or _stale(LIB, objs):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"]
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stdout[-6000:])

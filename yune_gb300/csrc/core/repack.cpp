@@ -19,9 +19,11 @@
 // order (udpt.cl:280-284); that case becomes a chain of nodes with unbounded boxes whose
 // leaves hold the triangles in index order.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../ym_math.h"
@@ -60,7 +62,44 @@ struct Builder {
     }
     return ~((first << 4) | count);
   }
+  // the same records as emit_leaf, written at stream slot `first` of a pre-sized stream
+  int fill_leaf(const int* list, int count, int order_base, int first) {
+    for (int k = 0; k < count; ++k) {
+      const yc_triangle& t = tris[list[k]];
+      float4 a, b, c;
+      a.x = t.v1.x; a.y = t.v1.y; a.z = t.v1.z;
+      int id = list[k];
+      std::memcpy(&a.w, &id, 4);
+      const int key = order_base + k;
+      b.x = t.v2.x - t.v1.x; b.y = t.v2.y - t.v1.y; b.z = t.v2.z - t.v1.z;
+      std::memcpy(&b.w, &key, 4);
+      c.x = t.v3.x - t.v1.x; c.y = t.v3.y - t.v1.y; c.z = t.v3.z - t.v1.z; c.w = 0.0f;
+      float4* o = &out_tris[3 * ((size_t)first + k)];
+      o[0] = a;
+      o[1] = b;
+      o[2] = c;
+    }
+    return ~((first << 4) | count);
+  }
 };
+
+// f(i) for i in [0, n) on the host's cores, in contiguous chunks (f must write only
+// its own outputs)
+template <class F>
+void parallel_for(size_t n, F f) {
+  const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t t = std::min(hw, std::max<size_t>(1, n / 4096));
+  if (t <= 1) {
+    for (size_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (size_t k = 0; k < t; ++k)
+    pool.emplace_back([&, k] {
+      for (size_t i = n * k / t; i < n * (k + 1) / t; ++i) f(i);
+    });
+  for (auto& th : pool) th.join();
+}
 
 bool is_leaf(const yc_bvh_node& n) { return (float)n.child_idx == -1.0f && n.vert_len > 0; }
 bool is_queued(const yc_bvh_node& n) { return n.vert_len > 0 || n.child_idx > 0; }
@@ -88,10 +127,21 @@ struct BinNode {
   BinRef c[2];
 };
 
+// Subtrees of more than kParallelItems leaves are built on their own thread while threads
+// are free: a subtree's splits depend only on its own items, and the emitted layout only
+// on the tree's shape, so the result is the sequential build's. Interior nodes take their
+// slots in `bins` (exactly items - 1 of them) from an atomic counter.
+constexpr int kParallelItems = 1 << 15;
+
 struct SahBuilder {
   std::vector<LeafItem>& items;
   std::vector<BinNode> bins;
-  int max_depth = 0;
+  std::atomic<int> max_depth{0};
+  std::atomic<int> next_node{0};
+  std::atomic<int> threads{1};
+  int max_threads = (int)std::max(1u, std::thread::hardware_concurrency());
+
+  SahBuilder(std::vector<LeafItem>& it) : items(it), bins(it.size() > 1 ? it.size() - 1 : 0) {}
 
   static float area(const float lo[3], const float hi[3]) {
     const float d0 = hi[0] - lo[0], d1 = hi[1] - lo[1], d2 = hi[2] - lo[2];
@@ -110,7 +160,7 @@ struct SahBuilder {
         clo[k] = std::min(clo[k], items[i].c[k]);
         chi[k] = std::max(chi[k], items[i].c[k]);
       }
-    max_depth = std::max(max_depth, depth);
+    for (int m = max_depth.load(); depth > m && !max_depth.compare_exchange_weak(m, depth);) {}
     if (e - b == 1) {
       r.node = -1;
       r.link = items[b].link;
@@ -172,10 +222,18 @@ struct SahBuilder {
       mid = (int)(std::partition(items.begin() + b, items.begin() + e, left) - items.begin());
       if (mid == b || mid == e) mid = (b + e) / 2;
     }
-    const int node = (int)bins.size();
-    bins.emplace_back();
-    const BinRef c0 = build(b, mid, depth + 1);
-    const BinRef c1 = build(mid, e, depth + 1);
+    const int node = next_node.fetch_add(1);
+    BinRef c0, c1;
+    if (e - b > kParallelItems && threads.load() < max_threads) {
+      threads.fetch_add(1);
+      std::thread left([&] { c0 = build(b, mid, depth + 1); });
+      c1 = build(mid, e, depth + 1);
+      left.join();
+      threads.fetch_sub(1);
+    } else {
+      c0 = build(b, mid, depth + 1);
+      c1 = build(mid, e, depth + 1);
+    }
     bins[node].c[0] = c0;
     bins[node].c[1] = c1;
     r.node = node;
@@ -261,7 +319,7 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
   const float INF = INFINITY;
   // shading records: normalize(vn1..vn3) and the material index
   out.shade.resize((size_t)n_tri * 4);
-  for (int i = 0; i < n_tri; ++i) {
+  parallel_for((size_t)n_tri, [&](size_t i) {
     const yc_triangle& t = tris[i];
     const yc_float4* vn[3] = {&t.vn1, &t.vn2, &t.vn3};
     for (int k = 0; k < 3; ++k) {
@@ -272,7 +330,7 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
     int m = t.matID;
     std::memcpy(&mid, &m, 4);
     out.shade[4 * (size_t)i + 3] = float4{mid, 0.0f, 0.0f, 0.0f};
-  }
+  });
 
   if (n_tri == 0) {
     out.root_link = LINK_NONE;
@@ -346,31 +404,43 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
     return 0;
   }
   if (tree_mode == TREE_SAH_OVER_LEAVES || tree_mode == TREE_WIDE4) {
-    // the leaves the reference traversal can reach, in node-index order
-    std::vector<LeafItem> items;
+    // the leaves the reference traversal can reach, in node-index order, and the first
+    // stream slot of each (then the stream and the leaf items are filled in parallel,
+    // exactly as emit_leaf would append them one after another)
+    std::vector<int> leaf_node, leaf_first;
     std::vector<char> reach(n_node, 0);
     reach[0] = 1;
+    size_t slots = b.out_tris.size() / 3;
     for (int i = 0; i < n_node; ++i) {
       if (!reach[i]) continue;
       const yc_bvh_node& n = nodes[i];
       if (is_leaf(n)) {
-        LeafItem it;
-        const float* plo = &n.aabb.p_min.x;
-        const float* phi = &n.aabb.p_max.x;
-        for (int k = 0; k < 3; ++k) {
-          it.lo[k] = plo[k];
-          it.hi[k] = phi[k];
-          it.c[k] = 0.5f * (plo[k] + phi[k]);
-        }
-        it.link = b.emit_leaf(n.vert_list, n.vert_len, i * 16);
-        items.push_back(it);
+        leaf_node.push_back(i);
+        leaf_first.push_back((int)slots);
+        slots += (size_t)n.vert_len;
       } else if (is_queued(n) || i == 0) {
         for (int c = 0; c < 2; ++c)
           if (is_queued(nodes[n.child_idx + c])) reach[n.child_idx + c] = 1;
       }
     }
-    if (items.empty()) { out.root_link = LINK_NONE; out.depth = 0; return 0; }
-    SahBuilder sb{items, {}};
+    if (leaf_node.empty()) { out.root_link = LINK_NONE; out.depth = 0; return 0; }
+    if (slots >= (size_t)(1 << 27)) { err = "scene too large for the 27-bit stream index"; return -1; }
+    std::vector<LeafItem> items(leaf_node.size());
+    b.out_tris.resize(slots * 3);
+    parallel_for(leaf_node.size(), [&](size_t j) {
+      const int i = leaf_node[j];
+      const yc_bvh_node& n = nodes[i];
+      LeafItem& it = items[j];
+      const float* plo = &n.aabb.p_min.x;
+      const float* phi = &n.aabb.p_max.x;
+      for (int k = 0; k < 3; ++k) {
+        it.lo[k] = plo[k];
+        it.hi[k] = phi[k];
+        it.c[k] = 0.5f * (plo[k] + phi[k]);
+      }
+      it.link = b.fill_leaf(n.vert_list, n.vert_len, i * 16, leaf_first[j]);
+    });
+    SahBuilder sb{items};
     const BinRef root_ref = sb.build(0, (int)items.size(), 0);
     if (tree_mode == TREE_WIDE4) {
       int d = 0;
