@@ -178,11 +178,16 @@ def cpu_reference(scene, seeds, seconds, want_rays=True, band=0):
     W, H = scene.width, scene.height
     cfg = dict(scene.cfg)
     bdpt = cfg.get("integrator", 0) == 1
+    bdpt_mis = cfg.get("integrator", 0) == 2
     threads = os.cpu_count() or 1
-    use_ref = O.ref() is not None
+    use_ref = O.ref() is not None and not bdpt_mis
     kind = "reference" if use_ref else "port"
     note = ""
-    if bdpt:
+    if bdpt_mis:   # no reference implementation exists: the CPU statement is the baseline
+        kmax = int(cfg.get("bdpt_bounces", 20))
+        note = "; bidirectional tracer with MIS (the CPU statement), paths <= %d segments, %d lights" % (
+            kmax, len(scene.lights))
+    elif bdpt:
         bounces = int(cfg.get("bdpt_bounces", 20))
         variant = {(20, 1): "bdpt20", (8, 1): "bdpt8", (8, 4): "bdpt8_l4"}.get((bounces, len(scene.lights)))
         if use_ref and variant is None:
@@ -204,6 +209,8 @@ def cpu_reference(scene, seeds, seconds, want_rays=True, band=0):
         starts = [((i * step) % nb) * band for i in range(nb)]
 
     def one(k, r, a):
+        if bdpt_mis:
+            return O.render_bdpt_mis(scene, a, seeds[k % len(seeds)], 1, kmax, cfg, threads=threads, rows=r)
         if bdpt:
             if use_ref:
                 O.ref_render(scene, a, seeds[k % len(seeds)], 1, variant, 0, 0, threads=threads, rows=r)
@@ -243,7 +250,7 @@ def run_reference(args, rank, ws, dist):
     scene = scene_for(args.config)
     from yune_gb300 import scenes
     seeds = scenes.pass_seeds(0, args.steps + args.warmup)
-    cb = cpu_reference(scene, seeds, args.cpu_seconds, band=1 if args.config == "c4" else 0)
+    cb = cpu_reference(scene, seeds, args.cpu_seconds, band=1 if args.config in ("c4", "c4_mis") else 0)
     cfg = {"workload": workload_string(args.config, scene), "spp_total": scene.spp,
            "reference_cfg": scene.cfg}
     line = {"metric": METRIC, "value": cb["value"], "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
@@ -473,12 +480,20 @@ WORKLOAD_NAMES = {
     "c0_bdpt": "Cornell box, four quad lights, naive BDPT with 8 vertices per subpath",
     "c4": "stress: 40x40 grid of displaced level-4/5 icospheres, mixed materials, 4 quad lights, naive BDPT with "
           "8 vertices per subpath",
+    "c0_mis": "Cornell box (5 Oren-Nayar walls, seeded-yaw boxes, one Phong n=50), quad light",
+    "c0_bdpt_mis": "Cornell box, four quad lights",
+    "c4_mis": "stress: 40x40 grid of displaced level-4/5 icospheres, mixed materials, 4 quad lights",
 }
 
 
 def workload_string(name, scene):
     """The workload a bench line is quoted on (the same string in both arms)."""
     W, H = scene.width, scene.height
+    if scene.cfg.get("integrator", 0) == 2:
+        return ("%s: %s, %d tris, %dx%d, %d lights, bidirectional path tracing with MIS (power heuristic), paths "
+                "of at most %d segments, 1 spp per step"
+                % (name, WORKLOAD_NAMES.get(name, name), scene.n_tri, W, H, len(scene.lights),
+                   scene.cfg["bdpt_bounces"]))
     if scene.cfg.get("integrator", 0) == 1:
         return ("%s: %s, %d tris, %dx%d, %d lights, BDPT with %d vertices per subpath, 1 spp per step"
                 % (name, WORKLOAD_NAMES.get(name, name), scene.n_tri, W, H, len(scene.lights),
@@ -518,7 +533,7 @@ def run_perpass_bdpt(args, rank, local, ws, dist):
     scene_bytes = r.scene_bytes(sid)
     # the reference BVH of this scene built on the host (yh_bvh_build) and on the GPU
     # (yc_bvh_build), compared node for node
-    leaf = 4 if args.config == "c4" else 10
+    leaf = 4 if args.config in ("c4", "c4_mis") else 10
     t0 = time.perf_counter()
     h_nodes, _ = scenes.build_bvh(scene.tris, 20, leaf)
     host_bvh_s = time.perf_counter() - t0
@@ -809,7 +824,7 @@ def run_trace_bench(args):
 
 
 def scenes_is_bdpt(name):
-    return name in ("c0_bdpt", "c4")
+    return name in ("c0_bdpt", "c4", "c0_mis", "c0_bdpt_mis", "c4_mis")
 
 
 def main():

@@ -40,8 +40,11 @@ enum {
   YC_E_NOTFOUND = -8        /* unknown scene / accumulator / job id */
 };
 
-/* integrators */
-enum { YC_UDPT = 0, YC_BDPT = 1 };
+/* integrators: the unidirectional tracer (udpt.cl), the naive bidirectional tracer
+ * (bdpt.cl) and the bidirectional tracer with multiple importance sampling (power
+ * heuristic over every strategy with at least two eye vertices; converges to the image of
+ * YC_UDPT, which bdpt.cl's heuristic weights do not) */
+enum { YC_UDPT = 0, YC_BDPT = 1, YC_BDPT_MIS = 2 };
 /* diffuse BRDF: Lambert (udpt.cl:621-622) or the Oren-Nayar rule of
  * kernels/legacy/udpt-primitives.cl:673-686 */
 enum { YC_BRDF_LAMBERT = 0, YC_BRDF_OREN_NAYAR = 1 };
@@ -49,14 +52,16 @@ enum { YC_BRDF_LAMBERT = 0, YC_BRDF_OREN_NAYAR = 1 };
 /* Per-pass options. The reference fixes these with #defines in the kernel text
  * (udpt.cl:3-9, bdpt.cl:1-8) or with kernel arguments (udpt.cl:158-160). */
 typedef struct yc_pass_cfg {
-  int32_t integrator;      /* YC_UDPT or YC_BDPT */
+  int32_t integrator;      /* YC_UDPT, YC_BDPT or YC_BDPT_MIS */
   int32_t mis;             /* 1 = the MIS branch of evaluateDirectLighting (udpt.cl:570-608) */
-  int32_t rr_threshold;    /* RR_THRESHOLD: roulette when bounce index > this (6 in udpt.cl) */
+  int32_t rr_threshold;    /* RR_THRESHOLD: roulette when bounce index > this (6 in udpt.cl;
+                              YC_BDPT_MIS: subpath vertex index > this) */
   int32_t max_depth;       /* bound of the GI loop (100000 in udpt.cl:463) */
   int32_t brdf_model;      /* YC_BRDF_* */
   int32_t mis_lobe_fix;    /* 0 = reference behaviour; 1 = draw the lobe when the shadow
                               ray is blocked, so a MIS BRDF hit never divides by zero */
-  int32_t bdpt_bounces;    /* BDPT_BOUNCES (20 in bdpt.cl:7) */
+  int32_t bdpt_bounces;    /* BDPT_BOUNCES (20 in bdpt.cl:7); YC_BDPT_MIS: the longest path
+                              in segments, camera to light (3..32) */
   int32_t block, block_x, block_y;   /* image tile of this launch (udpt.cl:166-167);
                                         block_x = block_y = 1 renders the whole frame */
 } yc_pass_cfg;

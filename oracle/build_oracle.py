@@ -3,7 +3,8 @@
 
 TEST INFRASTRUCTURE: the outputs are checkers and the CPU baseline, never the product.
 
-* liboracle.so   -- the restatement in oracle/udpt_oracle.hpp (+ bdpt_oracle.hpp).
+* liboracle.so   -- the restatement in oracle/udpt_oracle.hpp (+ bdpt_oracle.hpp), and
+                    the bidirectional tracer with MIS (bdpt_mis_oracle.hpp).
 * _ref/          -- Yune's own kernel files compiled as C++: the syntax-only transform
                     of oracle/ref/transform.py turns kernels/legacy/udpt.cl, bdpt.cl,
                     udpt-primitives.cl and kernels/post-proc/tonemap.cl into .inc files
@@ -67,7 +68,7 @@ def _elf_matches_host(path):
 def build_oracle(force=False):
     out = os.path.join(HERE, "liboracle.so")
     srcs = [os.path.join(HERE, f) for f in ("oracle_capi.cpp", "udpt_oracle.hpp", "oracle_math.hpp",
-                                              "bdpt_oracle.hpp")]
+                                              "bdpt_oracle.hpp", "bdpt_mis_oracle.hpp")]
     srcs.append(os.path.join(ROOT, "yune_gb300", "csrc", "ym_math.h"))
     if not force and _newer(out, srcs) and _elf_matches_host(out):
         return out

@@ -10,6 +10,7 @@
 #include <thread>
 #include <vector>
 
+#include "bdpt_mis_oracle.hpp"
 #include "bdpt_oracle.hpp"
 #include "udpt_oracle.hpp"
 
@@ -58,7 +59,8 @@ void add(or_counters* o, const orc::Counters& c) {
 template <class R, class Acc>
 int render(const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_bvh_node* b, int nb,
            const yc_quad_light* l, int nl, const yc_cam* cam, int W, int H, Acc* accum, uint32_t rand_,
-           int reset, const or_cfg* cfg, int threads, int row0, int row1, or_counters* out, int bdpt_bounces = 0) {
+           int reset, const or_cfg* cfg, int threads, int row0, int row1, or_counters* out, int bdpt_bounces = 0,
+           int bdpt_mis = 0) {
   if (!cam || !accum || W <= 0 || H <= 0 || nl < 0 || nl > 16) return -1;
   if (row1 <= row0) { row0 = 0; row1 = H; }
   const orc::Scene<R> sc = mk_scene<R>(t, nt, m, nm, b, nb, l, nl);
@@ -67,13 +69,15 @@ int render(const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_
   std::atomic<int> next(row0);
   std::vector<orc::Counters> cnts(threads);
   auto work = [&](int tid) {
-    orc::BdptTracer<R> tr(sc, k, cnts[tid], bdpt_bounces > 0 ? bdpt_bounces : 20);
+    orc::BdptMisTracer<R> tr(sc, k, cnts[tid], bdpt_bounces > 0 ? bdpt_bounces : 20);
+    tr.bounces = bdpt_bounces > 0 ? bdpt_bounces : 20;
     for (;;) {
       const int y = next.fetch_add(1);
       if (y >= row1) break;
       for (int x = 0; x < W; ++x) {
-        const orc::V4<R> c = bdpt_bounces > 0 ? orc::pixel_sample_bdpt<R>(tr, *cam, x, y, W, H, rand_)
-                                              : orc::pixel_sample<R>(tr, *cam, x, y, W, H, rand_);
+        const orc::V4<R> c = bdpt_mis ? orc::pixel_sample_bdpt_mis<R>(tr, *cam, x, y, W, H, rand_)
+                             : bdpt_bounces > 0 ? orc::pixel_sample_bdpt<R>(tr, *cam, x, y, W, H, rand_)
+                                                : orc::pixel_sample<R>(tr, *cam, x, y, W, H, rand_);
         Acc* p = accum + 4 * ((size_t)y * W + x);
         const orc::V4<R> prev{(R)p[0], (R)p[1], (R)p[2], (R)p[3]};
         const orc::V4<R> o = orc::accumulate<R>(c, prev, reset);
@@ -147,6 +151,25 @@ int or_render_bdpt_f64(const yc_triangle* t, int nt, const yc_material* m, int n
                                 row1, out, bounces);
 }
 
+// One pass of the bidirectional tracer with multiple importance sampling
+// (bdpt_mis_oracle.hpp), paths of at most kmax segments (3 <= kmax <= 32).
+int or_render_bdpt_mis(const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_bvh_node* b, int nb,
+                       const yc_quad_light* l, int nl, const yc_cam* cam, int W, int H, float* accum, uint32_t rand_,
+                       int reset, const or_cfg* cfg, int kmax, int threads, int row0, int row1, or_counters* out) {
+  if (kmax < 3 || kmax > 32) return -1;
+  return render<float, float>(t, nt, m, nm, b, nb, l, nl, cam, W, H, accum, rand_, reset, cfg, threads, row0, row1,
+                              out, kmax, 1);
+}
+
+int or_render_bdpt_mis_f64(const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_bvh_node* b, int nb,
+                           const yc_quad_light* l, int nl, const yc_cam* cam, int W, int H, double* accum,
+                           uint32_t rand_, int reset, const or_cfg* cfg, int kmax, int threads, int row0, int row1,
+                           or_counters* out) {
+  if (kmax < 3 || kmax > 32) return -1;
+  return render<double, double>(t, nt, m, nm, b, nb, l, nl, cam, W, H, accum, rand_, reset, cfg, threads, row0,
+                                row1, out, kmax, 1);
+}
+
 // The same pass evaluated in double precision into a double accumulator.
 int or_render_f64(const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_bvh_node* b, int nb,
                   const yc_quad_light* l, int nl, const yc_cam* cam, int W, int H, double* accum,
@@ -162,7 +185,7 @@ int or_render_f64(const yc_triangle* t, int nt, const yc_material* m, int nm, co
 int or_render_pixels_f64(const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_bvh_node* b, int nb,
                          const yc_quad_light* l, int nl, const yc_cam* cam, int W, int H, const int* xs,
                          const int* ys, int n, const uint32_t* seeds, int n_pass, const or_cfg* cfg, int bdpt_bounces,
-                         int threads, double* out) {
+                         int threads, double* out, int bdpt_mis) {
   if (!cam || !xs || !ys || !seeds || !out || n < 0 || n_pass <= 0) return -1;
   const orc::Scene<double> sc = mk_scene<double>(t, nt, m, nm, b, nb, l, nl);
   const orc::Config k = to_cfg(cfg);
@@ -170,13 +193,15 @@ int or_render_pixels_f64(const yc_triangle* t, int nt, const yc_material* m, int
   std::atomic<int> next(0);
   auto work = [&]() {
     orc::Counters cnt;
-    orc::BdptTracer<double> tr(sc, k, cnt, bdpt_bounces > 0 ? bdpt_bounces : 20);
+    orc::BdptMisTracer<double> tr(sc, k, cnt, bdpt_bounces > 0 ? bdpt_bounces : 20);
+    tr.bounces = bdpt_bounces > 0 ? bdpt_bounces : 20;
     for (;;) {
       const int i = next.fetch_add(1);
       if (i >= n) break;
       orc::V4<double> acc{0, 0, 0, 0};
       for (int p = 0; p < n_pass; ++p) {
-        const orc::V4<double> c = bdpt_bounces > 0 ? orc::pixel_sample_bdpt<double>(tr, *cam, xs[i], ys[i], W, H, seeds[p])
+        const orc::V4<double> c = bdpt_mis ? orc::pixel_sample_bdpt_mis<double>(tr, *cam, xs[i], ys[i], W, H, seeds[p])
+                                  : bdpt_bounces > 0 ? orc::pixel_sample_bdpt<double>(tr, *cam, xs[i], ys[i], W, H, seeds[p])
                                                    : orc::pixel_sample<double>(tr, *cam, xs[i], ys[i], W, H, seeds[p]);
         acc = orc::accumulate<double>(c, acc, p == 0 ? 1 : 0);
       }

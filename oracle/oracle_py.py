@@ -46,6 +46,8 @@ def orc():
         L.or_render_bdpt.argtypes = [vp, i32, vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, u32, i32,
                                      C.POINTER(OrCfg), i32, i32, i32, i32, C.POINTER(OrCounters)]
         L.or_render_bdpt_f64.argtypes = L.or_render_bdpt.argtypes
+        L.or_render_bdpt_mis.argtypes = L.or_render_bdpt.argtypes
+        L.or_render_bdpt_mis_f64.argtypes = L.or_render_bdpt.argtypes
         L.or_tonemap.argtypes = [vp, i32, i32, vp]
         L.or_ym_eval.argtypes = [i32, vp, vp, vp, i32]
         L.or_wang_hash.argtypes = [u32]
@@ -53,7 +55,7 @@ def orc():
         L.or_xor_shift.argtypes = [u32]
         L.or_xor_shift.restype = u32
         L.or_render_pixels_f64.argtypes = [vp, i32, vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, vp, i32, vp, i32,
-                                           C.POINTER(OrCfg), i32, i32, vp]
+                                           C.POINTER(OrCfg), i32, i32, vp, i32]
         L.or_brdf.argtypes = [vp, i32, vp, i32, i32, vp, vp, vp, vp, i32, C.c_float, i32, vp]
         _orc = L
     return _orc
@@ -128,8 +130,27 @@ def render_bdpt(scene, accum, rand_seed, reset, bounces, threads=0, rows=None, f
     return {k: getattr(cnt, k) for k, _ in OrCounters._fields_}
 
 
-def reference_pixels_f64(scene, xs, ys, seeds, cfg, bdpt_bounces=0, threads=0):
-    """FP64 running mean over len(seeds) passes at the given pixels (n x 4 doubles)."""
+def render_bdpt_mis(scene, accum, rand_seed, reset, kmax, cfg, threads=0, rows=None, f64=False, heap_size=1500):
+    """One pass of the bidirectional tracer with multiple importance sampling
+    (bdpt_mis_oracle.hpp) into accum; cfg supplies rr_threshold and brdf_model."""
+    L = orc()
+    H, W = accum.shape[:2]
+    cnt = OrCounters()
+    c = cfg_of(cfg, heap_size)
+    r0, r1 = rows if rows else (0, 0)
+    fn = L.or_render_bdpt_mis_f64 if f64 else L.or_render_bdpt_mis
+    rc = fn(_p(scene.tris), len(scene.tris), _p(scene.mats), len(scene.mats), _p(scene.nodes), len(scene.nodes),
+            _p(scene.lights), len(scene.lights), _p(scene.cam), W, H, _p(accum), int(rand_seed) & 0xFFFFFFFF, reset,
+            C.byref(c), kmax, threads, r0, r1, C.byref(cnt))
+    if rc != 0:
+        raise RuntimeError("or_render_bdpt_mis failed: %d" % rc)
+    return {k: getattr(cnt, k) for k, _ in OrCounters._fields_}
+
+
+def reference_pixels_f64(scene, xs, ys, seeds, cfg, bdpt_bounces=0, threads=0, bdpt_mis=False):
+    """FP64 running mean over len(seeds) passes at the given pixels (n x 4 doubles);
+    bdpt_mis selects the bidirectional tracer with multiple importance sampling, with
+    paths of at most bdpt_bounces segments."""
     L = orc()
     xs = np.ascontiguousarray(xs, np.int32)
     ys = np.ascontiguousarray(ys, np.int32)
@@ -139,7 +160,7 @@ def reference_pixels_f64(scene, xs, ys, seeds, cfg, bdpt_bounces=0, threads=0):
     rc = L.or_render_pixels_f64(_p(scene.tris), len(scene.tris), _p(scene.mats), len(scene.mats), _p(scene.nodes),
                                 len(scene.nodes), _p(scene.lights), len(scene.lights), _p(scene.cam), scene.width,
                                 scene.height, _p(xs), _p(ys), len(xs), _p(sd), len(sd), C.byref(c), bdpt_bounces,
-                                threads, _p(out))
+                                threads, _p(out), int(bool(bdpt_mis)))
     if rc != 0:
         raise RuntimeError("or_render_pixels_f64 failed")
     return out

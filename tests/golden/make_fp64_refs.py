@@ -23,6 +23,13 @@ from yune_gb300 import scenes  # noqa: E402
 N_PASS = 65536
 GRID = 32
 
+# The configurations of the bidirectional tracer with MIS are checked against another
+# estimator of the same image: the unidirectional tracer with next-event estimation only
+# (udpt.cl with MIS off), its loop bounded so that its paths have the same longest length
+# (max_depth = segments - 2).
+INDEPENDENT = {"c0_mis": dict(integrator=0, mis=0, max_depth=18),
+               "c0_bdpt_mis": dict(integrator=0, mis=0, max_depth=6)}
+
 
 def grid(s):
     xs = (np.arange(GRID) * s.width) // GRID + s.width // (2 * GRID)
@@ -33,6 +40,8 @@ def grid(s):
 
 def make(name):
     s = scenes.CONFIGS[name]()
+    if name in INDEPENDENT:
+        s.cfg = dict(s.cfg, **INDEPENDENT[name])
     X, Y = grid(s)
     seeds = scenes.mt19937(7777, N_PASS)
     bounces = s.cfg["bdpt_bounces"] if s.cfg.get("integrator", 0) == 1 else 0
@@ -44,5 +53,5 @@ def make(name):
 
 
 if __name__ == "__main__":
-    for name in (sys.argv[1:] or ["c0", "c1", "c0_bdpt"]):
+    for name in (sys.argv[1:] or ["c0", "c1", "c0_bdpt", "c0_mis", "c0_bdpt_mis"]):
         make(name)

@@ -291,8 +291,9 @@ def test_save_image_round_trip(renderer, tmp_path):
 
 def test_c4_stress_scene_bdpt_parity(renderer):
     """The stress scene itself (10,004,490 triangles, 8.5M reference nodes, four lights,
-    BDPT with 8 vertices per subpath) on a 32 x 18 crop of the frame, two passes: every
-    pixel and the ray counts against the oracle. The oracle's breadth-first queue is
+    BDPT with 8 vertices per subpath, then the bidirectional tracer with MIS, paths of at
+    most 8 segments) on a 32 x 18 crop of the frame, two passes: every pixel and the ray
+    counts against the oracle. The oracle's breadth-first queue is
     raised so that no hit is dropped (the core's walk has no such limit)."""
     s = scenes.c4(32, 18)
     assert s.n_tri == 10_004_490
@@ -300,22 +301,28 @@ def test_c4_stress_scene_bdpt_parity(renderer):
     sid = renderer.upload(s)
     renderer.set_camera(s.cam)
     aid = renderer.alloc_accum(32, 18)
-    renderer.reset_stats()
-    renderer.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
-    gpu = renderer.read_accum(aid)
-    st = renderer.stats()
+    out = []
+    # the naive BDPT of the configuration, then the bidirectional tracer with MIS
+    for cfg in (s.cfg, dict(s.cfg, integrator=2)):
+        renderer.reset_stats()
+        renderer.render_passes(sid, aid, seeds, reset_first=1, cfg=cfg)
+        out.append((renderer.read_accum(aid), renderer.stats()))
     renderer.free_accum(aid)
     renderer.release(sid)
-    ref = np.zeros((18, 32, 4), np.float32)
-    rays = 0
-    for k, sd in enumerate(seeds):
-        c = O.render_bdpt(s, ref, sd, 1 if k == 0 else 0, 8, heap_size=1 << 22)
-        assert c["heap_overflow"] == 0
-        rays += c["rays"]
-    assert st["stack_overflow"] == 0
-    assert _rel_bad(gpu, ref) == 0
-    assert np.array_equal(gpu[..., 3], ref[..., 3])
-    assert st["rays"] == rays
+    for (gpu, st), mis in zip(out, (False, True)):
+        ref = np.zeros((18, 32, 4), np.float32)
+        rays = 0
+        for k, sd in enumerate(seeds):
+            if mis:
+                c = O.render_bdpt_mis(s, ref, sd, 1 if k == 0 else 0, 8, s.cfg, heap_size=1 << 22)
+            else:
+                c = O.render_bdpt(s, ref, sd, 1 if k == 0 else 0, 8, heap_size=1 << 22)
+            assert c["heap_overflow"] == 0
+            rays += c["rays"]
+        assert st["stack_overflow"] == 0
+        assert _rel_bad(gpu, ref) == 0
+        assert np.array_equal(gpu[..., 3], ref[..., 3])
+        assert st["rays"] == rays
 
 
 @pytest.mark.parametrize("tree", [0, 2])

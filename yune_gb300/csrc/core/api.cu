@@ -246,7 +246,8 @@ Accum* find_accum(yc_ctx* c, int id) {
 
 int validate_cfg(const yc_pass_cfg* cfg) {
   if (!cfg) return fail(YC_E_INVALID, "cfg is NULL");
-  if (cfg->integrator != YC_UDPT && cfg->integrator != YC_BDPT) return fail(YC_E_INVALID, "unknown integrator");
+  if (cfg->integrator != YC_UDPT && cfg->integrator != YC_BDPT && cfg->integrator != YC_BDPT_MIS)
+    return fail(YC_E_INVALID, "unknown integrator");
   if (cfg->max_depth < 0) return fail(YC_E_INVALID, "max_depth < 0");
   if (cfg->block_x < 1 || cfg->block_y < 1 || cfg->block < 0 || cfg->block >= cfg->block_x * cfg->block_y)
     return fail(YC_E_INVALID, "bad block tiling");
@@ -256,8 +257,10 @@ int validate_cfg(const yc_pass_cfg* cfg) {
 // Runs one pass (all rounds) on the context stream; the host polls the queue sizes
 // every few rounds.
 int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int gi_check, const yc_pass_cfg* cfg) {
-  const bool bdpt = cfg->integrator == YC_BDPT;
+  const bool bdpt = cfg->integrator != YC_UDPT;
+  const bool bdpt_mis = cfg->integrator == YC_BDPT_MIS;
   if (bdpt && (cfg->bdpt_bounces < 2 || cfg->bdpt_bounces > 32)) return fail(YC_E_INVALID, "bdpt_bounces must be 2..32");
+  if (bdpt_mis && cfg->bdpt_bounces < 3) return fail(YC_E_INVALID, "bdpt_bounces must be 3..32 with YC_BDPT_MIS");
   const int W = ac->w, H = ac->h;
   int rc_ = ensure_paths(c, (size_t)W * H);
   if (rc_) return rc_;
@@ -298,7 +301,8 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
   YC_CUDA(cudaMemsetAsync(rc, 0, 2 * sizeof(yc::RoundCounters), c->stream));
   {
     KTimer kt(c, K_RAYGEN);
-    if (bdpt) yc::launch_raygen_bdpt(pp, ps, bb, c->q[0].p, rc + 0, c->stats.p, c->stream);
+    if (bdpt_mis) yc::launch_raygen_bdpt_mis(pp, ps, bb, c->q[0].p, rc + 0, c->stats.p, c->stream);
+    else if (bdpt) yc::launch_raygen_bdpt(pp, ps, bb, c->q[0].p, rc + 0, c->stats.p, c->stream);
     else yc::launch_raygen(pp, ps, c->q[0].p, rc + 0, c->stats.p, c->stream);
   }
   YC_CUDA(cudaPeekAtLastError());
@@ -394,8 +398,12 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
       KTimer kt(c, K_LOGIC);
       const int* sorted = shadesort ? c->ss_sorted.p : nullptr;
       const yc::SortCtl* sctl = shadesort ? c->ss_ctl.p : nullptr;
-      if (bdpt) yc::launch_logic_bdpt(pp, ps, bb, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid,
-                                      c->stream, sorted, sctl);
+      if (bdpt_mis)
+        yc::launch_logic_bdpt_mis(pp, ps, bb, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid,
+                                  c->stream, sorted, sctl);
+      else if (bdpt)
+        yc::launch_logic_bdpt(pp, ps, bb, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid, c->stream,
+                              sorted, sctl);
       else yc::launch_logic(pp, ps, in_c, in_a, rin, out_c, out_a, rout, c->stats.p, c->logic_grid, c->stream,
                             sorted, sctl);
     }

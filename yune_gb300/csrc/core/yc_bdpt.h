@@ -39,5 +39,13 @@ void launch_logic_bdpt(const PassParams& pp, const PathState& ps, const BdptBuff
                        const int* in_any, const RoundCounters* rc_in, int* out_closest, int* out_any,
                        RoundCounters* rc_out, DevStats* st, int grid, cudaStream_t s, const int* sorted = nullptr,
                        const SortCtl* sctl = nullptr);
+// the bidirectional tracer with multiple importance sampling (bdpt_mis.cu): same buffers,
+// same trace-state numbering (B_LIGHT .. B_CONN), light vertices only
+void launch_raygen_bdpt_mis(const PassParams& pp, const PathState& ps, const BdptBuffers& bb, int* q_closest,
+                            RoundCounters* rc, DevStats* st, cudaStream_t s);
+void launch_logic_bdpt_mis(const PassParams& pp, const PathState& ps, const BdptBuffers& bb, const int* in_closest,
+                           const int* in_any, const RoundCounters* rc_in, int* out_closest, int* out_any,
+                           RoundCounters* rc_out, DevStats* st, int grid, cudaStream_t s, const int* sorted = nullptr,
+                           const SortCtl* sctl = nullptr);
 
 }  // namespace yc

@@ -15,6 +15,9 @@ Configurations (sizes and spp of the benchmark workloads):
   c4  stress: 40 x 40 grid of displaced level-4/5 icospheres (10,004,480 tris) with mixed
       materials on the Cornell floor, four quad lights; naive BDPT, 8 vertices per
       subpath; 3840x2160, 128 spp; leaf <= 4.
+  c0_mis, c0_bdpt_mis, c4_mis
+      the scenes of c0, c0_bdpt and c4 with the bidirectional tracer with multiple
+      importance sampling (YC_BDPT_MIS): paths of at most 20, 8 and 8 segments.
 """
 import ctypes as C
 import os
@@ -248,7 +251,33 @@ def c4(width=3840, height=2160, spp=128, seed=0, grid=40, n_level5=118, bounces=
                      default_cfg(integrator=1, mis=0, bdpt_bounces=bounces), "c4")
 
 
-CONFIGS = {"c0": c0, "c1": c1, "c0_bdpt": c0_bdpt, "c4": c4}
+def _with_mis(s, name, kmax):
+    s.cfg = dict(s.cfg, integrator=2, bdpt_bounces=kmax)
+    s.name = name
+    return s
+
+
+def c0_mis(width=512, height=512, spp=64, seed=0, kmax=20):
+    """c0's scene and options rendered by the bidirectional tracer with MIS, paths of at
+    most kmax segments (the unidirectional c0 is unbounded; 20 segments leave out a
+    fraction of about 1e-5 of the radiance)."""
+    return _with_mis(c0(width, height, spp, seed), "c0_mis", kmax)
+
+
+def c0_bdpt_mis(width=512, height=512, spp=64, seed=0, bounces=8, lights=4):
+    """c0_bdpt's scene (four lights) with the bidirectional tracer with MIS, paths of at
+    most `bounces` segments."""
+    return _with_mis(c0_bdpt(width, height, spp, seed, bounces, lights), "c0_bdpt_mis", bounces)
+
+
+def c4_mis(width=3840, height=2160, spp=128, seed=0, bounces=8):
+    """The stress scene with the bidirectional tracer with MIS, paths of at most `bounces`
+    segments."""
+    return _with_mis(c4(width, height, spp, seed, bounces=bounces), "c4_mis", bounces)
+
+
+CONFIGS = {"c0": c0, "c1": c1, "c0_bdpt": c0_bdpt, "c4": c4, "c0_mis": c0_mis, "c0_bdpt_mis": c0_bdpt_mis,
+           "c4_mis": c4_mis}
 
 
 def pass_seeds(seed, n):
