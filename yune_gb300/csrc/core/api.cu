@@ -325,8 +325,12 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
   // connection steps run different code). The sort's three launches per round pay back
   // from frames of about half a million paths (measured: 1024x1024 and 3840x2160 gain,
   // 512x512 loses).
+  // The MIS tracer's states differ more (light subpath, next event, connections with four
+  // densities each, continuation): its sort pays from the option's threshold on (measured:
+  // 1024x1024 at 662 against 448 Mrays/s unsorted).
   const bool shadesort = (bdpt || sc->has_specular) && c->ss_threshold > 0 &&
-                         (size_t)W * H >= std::max((size_t)c->ss_threshold, kShadeSortMinPixels);
+                         (size_t)W * H >= (bdpt_mis ? (size_t)c->ss_threshold
+                                                    : std::max((size_t)c->ss_threshold, kShadeSortMinPixels));
   if (shadesort)
     if (int e = ensure_shadesort(c, (size_t)W * H)) return e;
   const int grid_c = yc::trace_grid_blocks(false, sc->dev.depth, sc->dev.wide != 0);
