@@ -225,6 +225,12 @@ int yc_batch_add_job(yc_batch* b, int scene_id, int accum_id, const yc_cam* cam,
 int yc_batch_run(yc_batch* b, int max_launches, int* unfinished_jobs);
 /* pixels whose passes are all done, and the job's pixel count */
 int yc_batch_job_progress(yc_batch* b, int job_id, int64_t* pixels_done, int64_t* pixels_total);
+/* Cancels a job between runs: each of its pixels in flight stops after its current pass,
+ * pixels not yet started are counted done without work (those handed to idle slots at
+ * the start of the next launch run one pass), the other jobs are untouched.
+ * The job reports done (pixels_done == pixels_total) once its work in flight drains; its
+ * accumulator must stay allocated until then. */
+int yc_batch_cancel_job(yc_batch* b, int job_id);
 /* A batch belongs to its context: yc_destroy releases the context's remaining batches,
  * after which their handles must not be used. */
 int yc_batch_destroy(yc_batch* b);

@@ -142,3 +142,39 @@ def test_autotuned_shape_gives_identical_results():
             r.render_passes(sid, ref, seeds, reset_first=1, cfg=s.cfg)
             assert np.array_equal(r.read_accum(aid).view(np.int32), r.read_accum(ref).view(np.int32))
         b.close()
+
+
+@pytest.mark.parametrize("groups", [1, 2])
+def test_cancelled_job_drains_and_others_are_unchanged(groups):
+    """yc_batch_cancel_job between runs: the cancelled job's pixels stop after their
+    current pass (fewer passes than asked, none more) and the job drains to done; the
+    other job, and a job added after the cancellation, give exactly their per-pass
+    accumulators."""
+    a = scenes.c0(48, 40)
+    b = scenes.c1(24, 36, level=4)
+    with Renderer(0) as r:
+        sa, sb = r.upload(a), r.upload(b)
+        want = []
+        for s, sid, seeds in ((b, sb, scenes.pass_seeds(2, 6)), (a, sa, scenes.pass_seeds(3, 2))):
+            r.set_camera(s.cam)
+            aid = r.alloc_accum(s.width, s.height)
+            r.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+            want.append(r.read_accum(aid))
+        bt = Batch(r, pool_paths=600, rounds_per_launch=2, groups=groups)
+        acc_a = r.alloc_accum(a.width, a.height)
+        acc_b = r.alloc_accum(b.width, b.height)
+        ja = bt.add_job(sa, acc_a, a.cam, scenes.pass_seeds(1, 64), a.cfg)
+        jb = bt.add_job(sb, acc_b, b.cam, scenes.pass_seeds(2, 6), b.cfg)
+        bt.run(max_launches=1)
+        bt.cancel(ja)
+        acc_c = r.alloc_accum(a.width, a.height)
+        jc = bt.add_job(sa, acc_c, a.cam, scenes.pass_seeds(3, 2), a.cfg)
+        assert bt.run() == 0
+        n = a.width * a.height
+        assert bt.progress(ja) == (n, n)
+        passes = r.read_accum(acc_a)[..., 3]
+        assert passes.max() < 64 and passes.min() >= 0
+        assert np.array_equal(r.read_accum(acc_b).view(np.int32), want[0].view(np.int32))
+        assert np.array_equal(r.read_accum(acc_c).view(np.int32), want[1].view(np.int32))
+        assert bt.progress(jc) == (n, n) and bt.progress(jb) == (b.width * b.height,) * 2
+        bt.close()

@@ -83,6 +83,7 @@ SIGNATURES = {
     "yc_batch_add_job": (i32, [vp, i32, i32, vp, vp, i32, i32, C.POINTER(PassCfg), C.POINTER(i32)]),
     "yc_batch_run": (i32, [vp, i32, C.POINTER(i32)]),
     "yc_batch_job_progress": (i32, [vp, i32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "yc_batch_cancel_job": (i32, [vp, i32]),
     "yc_batch_destroy": (i32, [vp]),
     # host producers
     "yh_bvh_build": (i32, [vp, i32, i32, i32, C.POINTER(vp)]),

@@ -46,6 +46,12 @@ class Batch:
         N.check(self.L.yc_batch_job_progress(self.h, job_id, C.byref(d), C.byref(t)), "yc_batch_job_progress")
         return d.value, t.value
 
+    def cancel(self, job_id):
+        """Stops a job between runs (yc_batch_cancel_job): its pixels in flight finish their
+        current pass, the rest are counted done; progress reaches the total once its work
+        in flight drains, and its accumulator must stay allocated until then."""
+        N.check(self.L.yc_batch_cancel_job(self.h, job_id), "yc_batch_cancel_job")
+
     def close(self):
         if getattr(self, "h", None) and getattr(self.r, "h", None):
             self.L.yc_batch_destroy(self.h)

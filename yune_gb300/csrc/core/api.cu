@@ -1280,6 +1280,17 @@ int yc_batch_run(yc_batch* b, int max_launches, int* unfinished) {
   return YC_OK;
 }
 
+int yc_batch_cancel_job(yc_batch* b, int job_id) {
+  if (!b || job_id < 0 || job_id >= (int)b->host_jobs.size()) return fail(YC_E_NOTFOUND, "unknown job");
+  yc_ctx* c = b->ctx;
+  YC_CUDA(cudaSetDevice(c->device));
+  const int one = 1;
+  b->host_jobs[job_id].cancelled = 1;
+  YC_CUDA(cudaMemcpyAsync(&b->jobs.p[job_id].cancelled, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  return YC_OK;
+}
+
 int yc_batch_job_progress(yc_batch* b, int job_id, int64_t* done, int64_t* total) {
   if (!b || job_id < 0 || job_id >= (int)b->host_jobs.size()) return fail(YC_E_NOTFOUND, "unknown job");
   unsigned long long d = 0;

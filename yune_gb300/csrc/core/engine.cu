@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __res
       const int reset = (jp.y == 0) ? J.reset_first : 0;
       emit = logic_path(J.pp, reset, ps, p, lc);
       if (emit == 0) {
-        if (jp.y + 1 < J.n_pass) {   // next pass of the same pixel
+        if (jp.y + 1 < J.n_pass && !J.cancelled) {   // next pass of the same pixel
           start_pass(J, jp.x, ps.misc[p].y, jp.y + 1, p, ps, job_pass);
           emit = 1;
           lc.rays++; lc.trav++; lc.prim++;
@@ -159,9 +159,12 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __res
         }
       }
     }
-    // slots whose pixel is done take the next tasks, one claim per warp
-    const unsigned mt = __ballot_sync(0xffffffffu, need_task);
-    if (mt) {
+    // slots whose pixel is done take the next tasks, one claim per warp; a task of a
+    // cancelled job is counted done without work and the slot claims again (a few times
+    // at most: then it waits on the free stack for the next launch's fill)
+    for (int attempt = 0; attempt < 4; ++attempt) {
+      const unsigned mt = __ballot_sync(0xffffffffu, need_task);
+      if (!mt) break;
       unsigned long long t0 = 0;
       int got = 0;
       if (lane == 0) t0 = claim_tasks(tasks, __popc(mt), got);
@@ -172,14 +175,21 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __res
         if (rank < got) {
           const unsigned long long t = t0 + (unsigned long long)rank;
           const int job = job_of_task(jobs, n_jobs, t);
-          start_pass(jobs[job], job, (int)(t - (unsigned long long)jobs[job].task_base), 0, p, ps, job_pass);
-          emit = 1;
-          lc.rays++; lc.trav++; lc.prim++;
+          if (jobs[job].cancelled) {
+            atomicAdd(&job_done[job], 1ull);
+          } else {
+            start_pass(jobs[job], job, (int)(t - (unsigned long long)jobs[job].task_base), 0, p, ps, job_pass);
+            emit = 1;
+            lc.rays++; lc.trav++; lc.prim++;
+            need_task = false;
+          }
         } else {
           free_stack[atomicAdd(&ctl->free_top, 1)] = p;
+          need_task = false;
         }
       }
     }
+    if (need_task) free_stack[atomicAdd(&ctl->free_top, 1)] = p;
     const unsigned mc = __ballot_sync(0xffffffffu, emit == 1);
     const unsigned ma = __ballot_sync(0xffffffffu, emit == 2);
     int bc = 0, ba = 0;

@@ -17,7 +17,8 @@ struct BatchJob {
   int reset_first;
   long long task_base;     // first global pixel-task index of this job
   int n_pix;
-  int pad_;
+  int cancelled;           // set between launches: pixels stop after their current pass,
+                           // tasks taken in the logic kernel are counted done without work
 };
 
 // The task cursor and job count, shared by every slot group of a batch.
