@@ -465,3 +465,59 @@ def test_tail_kernel_gives_the_same_pass(renderer, tree):
         assert np.array_equal(img.view(np.int32), out[0][0].view(np.int32))
         for k in ("rays", "extension", "shadow", "mis", "samples", "ext_rays", "any_rays", "stack_overflow"):
             assert st[k] == out[0][1][k], k
+
+
+def test_checkpoint_resume_is_exact(renderer, tmp_path):
+    """A snapshot of the accumulator after three passes, loaded into a fresh accumulator of
+    a new context, continues to the same bits as the uninterrupted render."""
+    s = scenes.c1(40, 32, level=4)
+    seeds = scenes.pass_seeds(61, 5)
+    sid = renderer.upload(s)
+    renderer.set_camera(s.cam)
+    aid = renderer.alloc_accum(40, 32)
+    renderer.render_passes(sid, aid, seeds[:3], reset_first=1, cfg=s.cfg)
+    renderer.save_checkpoint(aid, tmp_path / "ck.npz", next_pass=3)
+    renderer.render_passes(sid, aid, seeds[3:], reset_first=0, cfg=s.cfg)
+    whole = renderer.read_accum(aid)
+    renderer.free_accum(aid)
+    renderer.release(sid)
+    with Renderer(0) as r2:
+        sid2 = r2.upload(s)
+        r2.set_camera(s.cam)
+        aid2, meta = r2.load_checkpoint(tmp_path / "ck.npz")
+        assert int(meta["next_pass"]) == 3
+        r2.render_passes(sid2, aid2, seeds[int(meta["next_pass"]):], reset_first=0, cfg=s.cfg)
+        resumed = r2.read_accum(aid2)
+    assert np.array_equal(resumed.view(np.int32), whole.view(np.int32))
+    assert np.all(whole[..., 3] == 5)
+
+
+@pytest.mark.parametrize("integrator", [0, 1, 2])
+def test_nan_material_is_flagged_pink(renderer, integrator):
+    """A material with a NaN emission: the samples through it are NaN and the pixels
+    take the reference's PINK sentinel (udpt.cl:193-194), on the GPU as in the oracle."""
+    s = scenes.c0(40, 32)
+    s.mats = s.mats.copy()
+    s.mats[3]["ke"][:3] = np.nan   # the Phong box
+    if integrator == 1:
+        s.cfg = dict(s.cfg, integrator=1, mis=0, bdpt_bounces=8)
+    elif integrator == 2:
+        s.cfg = dict(s.cfg, integrator=2, bdpt_bounces=8)
+    seeds = scenes.pass_seeds(17, 1)
+    sid = renderer.upload(s)
+    renderer.set_camera(s.cam)
+    aid = renderer.alloc_accum(40, 32)
+    renderer.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+    gpu = renderer.read_accum(aid)
+    renderer.free_accum(aid)
+    renderer.release(sid)
+    ref = np.zeros((32, 40, 4), np.float32)
+    if integrator == 0:
+        O.render(s, ref, seeds[0], 1, s.cfg)
+    elif integrator == 1:
+        O.render_bdpt(s, ref, seeds[0], 1, 8)
+    else:
+        O.render_bdpt_mis(s, ref, seeds[0], 1, 8, s.cfg)
+    pink = np.all(np.abs(gpu[..., :3] - np.array([0.988, 0.0588, 0.7529], np.float32)) < 1e-6, axis=-1)
+    assert pink.sum() > 0 and not np.isnan(gpu).any()
+    assert np.array_equal(gpu.view(np.int32), ref.view(np.int32))

@@ -184,6 +184,25 @@ class Renderer:
         else:
             raise ValueError("image output is .png or .hdr")
 
+    def save_checkpoint(self, aid, path, **meta):
+        """Snapshot of an accumulator: its float4 running means with the pass count in w
+        (udpt.cl:203-208), so rendering can resume from it in another context or process.
+        `meta` (scene name, next pass index, seeds, ...) is stored beside it."""
+        np.savez(path, accum=self.read_accum(aid), **{k: np.asarray(v) for k, v in meta.items()})
+
+    def load_checkpoint(self, path):
+        """Allocates an accumulator holding a snapshot made by save_checkpoint; returns its
+        id and the stored metadata. Passes rendered into it with reset 0 continue the
+        running mean exactly where the snapshot left it."""
+        with np.load(path) as d:
+            acc = d["accum"]
+            meta = {k: d[k] for k in d.files if k != "accum"}
+        if acc.ndim != 3 or acc.shape[2] != 4:
+            raise ValueError("not an accumulator snapshot")
+        aid = self.alloc_accum(acc.shape[1], acc.shape[0])
+        self.write_accum(aid, acc)
+        return aid, meta
+
     def set_mixed_trace(self, on):
         """1: a round's closest-hit and any-hit rays share one traversal launch (default);
         0: one launch each."""

@@ -27,6 +27,15 @@ namespace yc {
 
 enum : int { BF_GLOSSY = 1, BF_OCCLUDED = 2 };
 
+// The BRDF and Phong-lobe helpers of the logic kernel, inlined or called (BDPT_HELPER).
+#define BDPT_HELPER __forceinline__
+__device__ BDPT_HELPER f4 brdf_bk(f4 w_i, f4 w_o, f4 n, const yc_material& m, bool glossy, float rr_prob) {
+  return brdf_b(w_i, w_o, n, m, glossy, rr_prob);
+}
+__device__ BDPT_HELPER f4 sample_phong_bk(const Vtx& v, const yc_material& m, f4 w_i, uint32_t& seed, float& pdf) {
+  return sample_phong_b(v, m, w_i, seed, pdf);
+}
+
 struct BCount {
   int i, j, lp, ep;
 };
@@ -198,17 +207,34 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(PassParams pp, PathState ps,
       int lj = ((misc.z >> 8) & 31) - 1;
       int k = ((misc.z >> 13) & 31) - 1;
       BCount cnt = unpack_cnt(misc.w);
-      f4 color = f4of(ps.thr[p]);
-      f4 sub = f4of(ps.thr_next[p]);
+      // While the subpaths are built (B_LIGHT, B_EYE0, B_EYE) the connection stage's
+      // fields (colour, sub-sum, NEE direction) are dead: Q_CONNECT initialises them.
+      // They are loaded in the connection states only and stored once the stage has
+      // started; the ray origin is read only where a hit point is built from it.
+      const bool building = phase == B_LIGHT || phase == B_EYE0 || phase == B_EYE;
+      bool conn_live = !building;
+      f4 color = ym::splat(0.0f), sub = ym::splat(0.0f), w_i = ym::splat(0.0f);
+      float light_pdf = 0.0f;
+      if (!building) {
+        color = f4of(ps.thr[p]);
+        sub = f4of(ps.thr_next[p]);
+        const float4 nee = ps.indirect[p];
+        w_i = ym::mk(nee.x, nee.y, nee.z, 0.0f);
+        light_pdf = nee.w;
+      }
       float4 dv = ps.direct[p];
       float weight = dv.x, ks = dv.y, pend_pdf = dv.z, pend_prob = dv.w;
-      const float4 nee = ps.indirect[p];
-      f4 w_i = ym::mk(nee.x, nee.y, nee.z, 0.0f);
-      float light_pdf = nee.w;
-      const float4 ro4 = ps.ro[p], rd4 = ps.rd[p];
-      f4 ro = ym::mk(ro4.x, ro4.y, ro4.z, 1.0f);
-      f4 rd = ym::mk(rd4.x, rd4.y, rd4.z, rd4.w);
-      float tmax = ro4.w;
+      f4 ro = ym::splat(0.0f), rd = ym::splat(0.0f);
+      float tmax = 0.0f;
+      if (building) {
+        const float4 ro4 = ps.ro[p];
+        ro = ym::mk(ro4.x, ro4.y, ro4.z, 1.0f);
+        tmax = ro4.w;
+      }
+      if (building || phase == B_CONN) {
+        const float4 rd4 = ps.rd[p];
+        rd = ym::mk(rd4.x, rd4.y, rd4.z, rd4.w);
+      }
       const float4 hit = ps.hit[p];
       bool done = false;
 
@@ -224,7 +250,7 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(PassParams pp, PathState ps,
               contrib = ym::splat(c1) * lv.contrib(0);
             } else {
               const Vtx pv = lv.vtx(cnt.i - 1);
-              contrib = brdf_b(-lv.dir(cnt.i - 1), rd, pv.n, sc.mats[pv.mat], (flags & BF_GLOSSY) != 0, pend_prob) *
+              contrib = brdf_bk(-lv.dir(cnt.i - 1), rd, pv.n, sc.mats[pv.mat], (flags & BF_GLOSSY) != 0, pend_prob) *
                         ym::fmax(0.0f, ym::dot(rd, pv.n));
               contrib = contrib / pend_pdf;
               contrib = contrib * lv.contrib(cnt.i - 1);
@@ -250,7 +276,7 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(PassParams pp, PathState ps,
             const bool g = sample_glossy_b(m, seed, prob);
             if (prob == 0.0f) { phase = Q_EYE_START; break; }
             float pdf = 1.0f;
-            const f4 nd = g ? sample_phong_b(pv, m, -lv.dir(cnt.i - 1), seed, pdf) : sample_cosine(pv, seed, pdf);
+            const f4 nd = g ? sample_phong_bk(pv, m, -lv.dir(cnt.i - 1), seed, pdf) : sample_cosine(pv, seed, pdf);
             flags = g ? (flags | BF_GLOSSY) : (flags & ~BF_GLOSSY);
             pend_pdf = pdf;
             pend_prob = prob;
@@ -307,7 +333,7 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(PassParams pp, PathState ps,
             const bool g = sample_glossy_b(m, seed, prob);
             if (prob == 0.0f) { phase = Q_CONNECT; cnt.i = 0; cnt.j = 0; flags = 0; break; }
             float pdf = 1.0f;
-            const f4 nd = g ? sample_phong_b(pv, m, -ev.dir(cnt.i - 1), seed, pdf) : sample_cosine(pv, seed, pdf);
+            const f4 nd = g ? sample_phong_bk(pv, m, -ev.dir(cnt.i - 1), seed, pdf) : sample_cosine(pv, seed, pdf);
             if (pdf <= 0.0f) { phase = Q_CONNECT; cnt.i = 0; cnt.j = 0; flags = 0; break; }
             flags = g ? (flags | BF_GLOSSY) : (flags & ~BF_GLOSSY);
             pend_pdf = pdf;
@@ -328,7 +354,7 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(PassParams pp, PathState ps,
             if (tri < 0) { phase = Q_CONNECT; cnt.i = 0; cnt.j = 0; flags = 0; break; }
             const Vtx v = tri_vertex(sc, ro, rd, hit.x, hit.y, hit.z, tri);
             const Vtx pv = ev.vtx(cnt.i - 1);
-            f4 contrib = brdf_b(rd, -ev.dir(cnt.i - 1), pv.n, sc.mats[pv.mat], (flags & BF_GLOSSY) != 0, pend_prob) *
+            f4 contrib = brdf_bk(rd, -ev.dir(cnt.i - 1), pv.n, sc.mats[pv.mat], (flags & BF_GLOSSY) != 0, pend_prob) *
                          ym::max(0.0f, ym::dot(rd, pv.n));
             contrib = contrib / pend_pdf;
             contrib = contrib * ev.contrib(cnt.i - 1);
@@ -351,6 +377,7 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(PassParams pp, PathState ps,
               color = ym::mk(0.0f, 0.0f, 0.0f, 1.0f);
               weight = 1.0f;
               ks = 0.0f;
+              conn_live = true;
               flags = 8;   // connection stage started
             }
             if (cnt.i >= cnt.ep || weight == 0.0f) { phase = Q_FINISH; break; }
@@ -401,7 +428,7 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(PassParams pp, PathState ps,
               if (prob == 0.0f) {
                 dl = em;
               } else {
-                f4 ls = (brdf_b(w_i, -ev.dir(cnt.i), v.n, m, g, prob) * ld4(sc.lights[lj].ke)) *
+                f4 ls = (brdf_bk(w_i, -ev.dir(cnt.i), v.n, m, g, prob) * ld4(sc.lights[lj].ke)) *
                         ym::fmax(ym::dot(w_i, v.n), 0.0f);
                 ls = ls * ym::div(1.0f, light_pdf);
                 dl = ls + em;
@@ -451,9 +478,9 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(PassParams pp, PathState ps,
               const float gf = ym::div(ym::mul(ym::max(ym::dot(wi, e_v.n), 0.0f), ym::max(ym::dot(-wi, l_v.n), 0.0f)), dist);
               float prob = 0.0f;
               bool g = sample_glossy_b(sc.mats[e_v.mat], seed, prob);
-              const f4 e2l = brdf_b(wi, wo, e_v.n, sc.mats[e_v.mat], g, prob);
+              const f4 e2l = brdf_bk(wi, wo, e_v.n, sc.mats[e_v.mat], g, prob);
               g = sample_glossy_b(sc.mats[l_v.mat], seed, prob);
-              const f4 l2e = brdf_b(-lv.dir(cnt.j), -wi, l_v.n, sc.mats[l_v.mat], g, prob);
+              const f4 l2e = brdf_bk(-lv.dir(cnt.j), -wi, l_v.n, sc.mats[l_v.mat], g, prob);
               f4 tlp = lv.contrib(cnt.j);
               tlp = tlp * ((gf * e2l) * l2e);
               tlp = tlp * ev.contrib(cnt.i);
@@ -485,10 +512,12 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(PassParams pp, PathState ps,
       }
       if (emit) {
         ps.misc[p] = make_int4((int)seed, pix, pack_st(phase, flags & 15, lj, k), pack_cnt(cnt));
-        ps.thr[p] = make_float4(color.x, color.y, color.z, color.w);
-        ps.thr_next[p] = make_float4(sub.x, sub.y, sub.z, sub.w);
+        if (conn_live) {
+          ps.thr[p] = make_float4(color.x, color.y, color.z, color.w);
+          ps.thr_next[p] = make_float4(sub.x, sub.y, sub.z, sub.w);
+          ps.indirect[p] = make_float4(w_i.x, w_i.y, w_i.z, light_pdf);
+        }
         ps.direct[p] = make_float4(weight, ks, pend_pdf, pend_prob);
-        ps.indirect[p] = make_float4(w_i.x, w_i.y, w_i.z, light_pdf);
         ps.ro[p] = make_float4(ro.x, ro.y, ro.z, tmax);
         ps.rd[p] = make_float4(rd.x, rd.y, rd.z, rd.w);
       }
