@@ -129,7 +129,7 @@ struct yc_ctx {
   DevBuf<char> flush_buf;
   // BDPT subpath vertices
   DevBuf<float4> bd_lv, bd_ev;
-  size_t bd_cap = 0;
+  size_t bd_cap = 0, bd_ev_cap = 0;   // light / eye vertex records (the MIS tracer has no eye records)
   // direct queries
   DevBuf<float> q_rays;
   DevBuf<int> q_tri;
@@ -289,8 +289,11 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     const size_t need = (size_t)W * H * 4 * cfg->bdpt_bounces;
     if (c->bd_cap < need) {
       YC_CUDA(c->bd_lv.alloc(need));
-      YC_CUDA(c->bd_ev.alloc(need));
       c->bd_cap = need;
+    }
+    if (!bdpt_mis && c->bd_ev_cap < need) {
+      YC_CUDA(c->bd_ev.alloc(need));
+      c->bd_ev_cap = need;
     }
     bb.lv = c->bd_lv.p;
     bb.ev = c->bd_ev.p;
