@@ -521,3 +521,32 @@ def test_nan_material_is_flagged_pink(renderer, integrator):
     pink = np.all(np.abs(gpu[..., :3] - np.array([0.988, 0.0588, 0.7529], np.float32)) < 1e-6, axis=-1)
     assert pink.sum() > 0 and not np.isnan(gpu).any()
     assert np.array_equal(gpu.view(np.int32), ref.view(np.int32))
+
+
+@pytest.mark.parametrize("case", ["brute_force", "no_triangles", "one_pixel", "one_row"])
+def test_render_edge_cases(renderer, case):
+    """Inputs at the edges of the contract, every pixel against the oracle: no BVH
+    (bvh_size = 0: the reference tests every triangle, udpt.cl:277-283), a scene without
+    triangles (only the quad light), a 1 x 1 frame and a 33 x 1 frame."""
+    w, h = {"one_pixel": (1, 1), "one_row": (33, 1)}.get(case, (24, 20))
+    s = scenes.c0(w, h)
+    if case == "brute_force":
+        s.nodes = s.nodes[:0]
+    elif case == "no_triangles":
+        s.tris, s.nodes = s.tris[:0], s.nodes[:0]
+    seeds = scenes.pass_seeds(29, 2)
+    sid = renderer.upload(s)
+    renderer.set_camera(s.cam)
+    aid = renderer.alloc_accum(w, h)
+    renderer.reset_stats()
+    renderer.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+    gpu = renderer.read_accum(aid)
+    st = renderer.stats()
+    renderer.free_accum(aid)
+    renderer.release(sid)
+    ref = np.zeros((h, w, 4), np.float32)
+    rays = 0
+    for k, sd in enumerate(seeds):
+        rays += O.render(s, ref, sd, 1 if k == 0 else 0, s.cfg)["rays"]
+    assert np.array_equal(gpu.view(np.int32), ref.view(np.int32))
+    assert st["rays"] == rays and st["samples"] == w * h * 2
