@@ -17,6 +17,7 @@
 // then a refit over the levels in reverse. The only liberty taken: a box bound that is
 // zero is stored as +0 (atomics cannot keep "the first of -0 and +0 met", which the
 // sequential builder does); the traversal's arithmetic is the same for either zero.
+#include <climits>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -59,21 +60,35 @@ __device__ __forceinline__ void fresh(yc_bvh_node& g, const yc_aabb& box) {
 // TriangleCPU::computeCentroid / computeAABB (src/TriangleCPU.cpp:41-71)
 __global__ void k_tri_info(const yc_triangle* __restrict__ t, int n, float4* cen, float4* lo, float4* hi, int* root) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const yc_triangle tr = t[i];
-  const float a[3] = {tr.v1.x, tr.v1.y, tr.v1.z}, b[3] = {tr.v2.x, tr.v2.y, tr.v2.z}, c[3] = {tr.v3.x, tr.v3.y, tr.v3.z};
-  float ce[3], l[3], h[3];
-  for (int k = 0; k < 3; ++k) {
-    ce[k] = ((a[k] + b[k]) + c[k]) / 3.0f;
-    l[k] = fminf(a[k], fminf(b[k], c[k]));
-    h[k] = fmaxf(a[k], fmaxf(b[k], c[k]));
-    if (h[k] - l[k] == 0.0f) h[k] += 0.2f;
-    atomicMin(&root[k], ord(l[k]));
-    atomicMax(&root[3 + k], ord(h[k]));
+  const bool act = i < n;
+  int rl[3] = {INT_MAX, INT_MAX, INT_MAX}, rh[3] = {INT_MIN, INT_MIN, INT_MIN};
+  if (act) {
+    const yc_triangle tr = t[i];
+    const float a[3] = {tr.v1.x, tr.v1.y, tr.v1.z}, b[3] = {tr.v2.x, tr.v2.y, tr.v2.z}, c[3] = {tr.v3.x, tr.v3.y, tr.v3.z};
+    float ce[3], l[3], h[3];
+    for (int k = 0; k < 3; ++k) {
+      ce[k] = ((a[k] + b[k]) + c[k]) / 3.0f;
+      l[k] = fminf(a[k], fminf(b[k], c[k]));
+      h[k] = fmaxf(a[k], fmaxf(b[k], c[k]));
+      if (h[k] - l[k] == 0.0f) h[k] += 0.2f;
+      rl[k] = ord(l[k]);
+      rh[k] = ord(h[k]);
+    }
+    cen[i] = make_float4(ce[0], ce[1], ce[2], 0.0f);
+    lo[i] = make_float4(l[0], l[1], l[2], 0.0f);
+    hi[i] = make_float4(h[0], h[1], h[2], 0.0f);
   }
-  cen[i] = make_float4(ce[0], ce[1], ce[2], 0.0f);
-  lo[i] = make_float4(l[0], l[1], l[2], 0.0f);
-  hi[i] = make_float4(h[0], h[1], h[2], 0.0f);
+  // the scene box: one update per warp (lanes past n carry the neutral values)
+  for (int k = 0; k < 3; ++k) {
+    rl[k] = __reduce_min_sync(0xffffffffu, rl[k]);
+    rh[k] = __reduce_max_sync(0xffffffffu, rh[k]);
+  }
+  if ((threadIdx.x & 31) == 0 && rl[0] != INT_MAX) {
+    for (int k = 0; k < 3; ++k) {
+      atomicMin(&root[k], rl[k]);
+      atomicMax(&root[3 + k], rh[k]);
+    }
+  }
 }
 
 // per-node working state of the level being split
@@ -105,18 +120,33 @@ __global__ void k_level_clear(NodeWork* work, int* hist, int a, int b, int bins)
   for (int k = 0; k < bins; ++k) hist[(size_t)(i - a) * bins + k] = 0;
 }
 
-// primitives of the level's nodes that can split: their node's box union
+// primitives of the level's nodes that can split: their node's box union. A node's
+// primitives are contiguous in perm, so the lanes of a warp mostly share one node: they
+// combine their boxes first and one lane per run of equal nodes updates the node (six
+// atomics per run instead of per primitive; min and max of the ord() images are exact
+// in any order). Every lane reaches the match, lanes without work with a key of their own.
 __global__ void k_bounds(const int* __restrict__ perm, const int* __restrict__ pnode, const float4* __restrict__ lo,
                          const float4* __restrict__ hi, NodeWork* work, int n, int a, int b, int leaf_max) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int nd = pnode[i];
-  if (nd < a || nd >= b) return;
-  NodeWork& w = work[nd];
-  if (w.e - w.s <= leaf_max) return;
+  const int lane = threadIdx.x & 31;
+  int nd = -1;
+  bool act = false;
+  if (i < n) {
+    nd = pnode[i];
+    act = nd >= a && nd < b && work[nd].e - work[nd].s > leaf_max;
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, act ? nd : -1 - lane);
+  if (!act) return;
   const float4 l = lo[perm[i]], h = hi[perm[i]];
-  atomicMin(&w.box[0], ord(l.x)); atomicMin(&w.box[1], ord(l.y)); atomicMin(&w.box[2], ord(l.z));
-  atomicMax(&w.box[3], ord(h.x)); atomicMax(&w.box[4], ord(h.y)); atomicMax(&w.box[5], ord(h.z));
+  const int x0 = __reduce_min_sync(peers, ord(l.x)), y0 = __reduce_min_sync(peers, ord(l.y));
+  const int z0 = __reduce_min_sync(peers, ord(l.z));
+  const int x1 = __reduce_max_sync(peers, ord(h.x)), y1 = __reduce_max_sync(peers, ord(h.y));
+  const int z1 = __reduce_max_sync(peers, ord(h.z));
+  if (lane == __ffs(peers) - 1) {
+    NodeWork& w = work[nd];
+    atomicMin(&w.box[0], x0); atomicMin(&w.box[1], y0); atomicMin(&w.box[2], z0);
+    atomicMax(&w.box[3], x1); atomicMax(&w.box[4], y1); atomicMax(&w.box[5], z1);
+  }
 }
 
 // split axis: the longest extent of the union (BVH.cpp:280-314)
@@ -130,17 +160,11 @@ __device__ __forceinline__ int split_axis(const NodeWork& w) {
   return axis;
 }
 
-// the bin of each primitive (BVH.cpp:93-126): the first plane not below its centroid
-__global__ void k_hist(const int* __restrict__ perm, const int* __restrict__ pnode, const float4* __restrict__ cen,
-                       const yc_bvh_node* nodes, NodeWork* work, int* hist, int n, int a, int b, int bins,
-                       int leaf_max) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int nd = pnode[i];
-  if (nd < a || nd >= b) return;
+// the bin of primitive perm[i] of node nd (BVH.cpp:93-126): the first plane not below its
+// centroid, by binary search
+__device__ __forceinline__ int bin_of(const int* __restrict__ perm, const float4* __restrict__ cen,
+                                      const yc_bvh_node* nodes, const NodeWork* work, int i, int nd, int bins) {
   const NodeWork& w = work[nd];
-  const int np = w.e - w.s;
-  if (np <= leaf_max || !(bins > 2 && np > 20)) return;
   const int axis = split_axis(w);
   const yc_aabb pbox = nodes[nd].aabb;
   const float4 c4 = cen[perm[i]];
@@ -165,7 +189,29 @@ __global__ void k_hist(const int* __restrict__ perm, const int* __restrict__ pno
     }
     first = lo_;
   }
-  atomicAdd(&hist[(size_t)(nd - a) * bins + first], 1);
+  return first;
+}
+
+// bin counts of the level's nodes that split by SAH
+__global__ void k_hist(const int* __restrict__ perm, const int* __restrict__ pnode, const float4* __restrict__ cen,
+                       const yc_bvh_node* nodes, NodeWork* work, int* hist, int n, int a, int b, int bins,
+                       int leaf_max) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  int nd = -1;
+  bool act = false;
+  if (i < n) {
+    nd = pnode[i];
+    if (nd >= a && nd < b) {
+      const int np = work[nd].e - work[nd].s;
+      act = np > leaf_max && bins > 2 && np > 20;
+    }
+  }
+  int key = -1 - lane;   // lanes without work: a key no other lane has
+  if (act) key = (nd - a) * bins + bin_of(perm, cen, nodes, work, i, nd, bins);
+  // lanes that fall in the same bin of the same node add once (counts are exact in any order)
+  const unsigned peers = __match_any_sync(0xffffffffu, key);
+  if (act && lane == __ffs(peers) - 1) atomicAdd(&hist[key], __popc(peers));
 }
 
 // one thread per node: leaf, empty, binned SAH split or spatial median (BVH.cpp:69-160)
