@@ -91,6 +91,11 @@ __global__ void k_tri_info(const yc_triangle* __restrict__ t, int n, float4* cen
   }
 }
 
+__global__ void k_iota(int* a, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = i;
+}
+
 // per-node working state of the level being split
 struct NodeWork {
   int s, e;          // segment of perm
@@ -275,41 +280,6 @@ __global__ void k_decide(const int* __restrict__ perm, yc_bvh_node* nodes, NodeW
   child_box[2 * (size_t)(nd - a) + 1] = best2;
 }
 
-// child slots in node order: an exclusive scan of the split flags (one block)
-__global__ void k_child_slots(NodeWork* work, int* child_of, int a, int b, int* total) {
-  __shared__ int s_sum[32];
-  const int count = b - a;
-  const int per = (count + blockDim.x - 1) / blockDim.x;
-  const int i0 = threadIdx.x * per;
-  int sum = 0;
-  for (int k = 0; k < per; ++k)
-    if (i0 + k < count) sum += work[a + i0 + k].split;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int incl = sum;
-  for (int off = 1; off < 32; off <<= 1) {
-    const int v = __shfl_up_sync(0xffffffffu, incl, off);
-    if (lane >= off) incl += v;
-  }
-  if (lane == 31) s_sum[warp] = incl;
-  __syncthreads();
-  if (warp == 0) {
-    int v = lane < (int)(blockDim.x >> 5) ? s_sum[lane] : 0;
-    for (int off = 1; off < 32; off <<= 1) {
-      const int u = __shfl_up_sync(0xffffffffu, v, off);
-      if (lane >= off) v += u;
-    }
-    s_sum[lane] = v;
-  }
-  __syncthreads();
-  int run = incl - sum + (warp > 0 ? s_sum[warp - 1] : 0);
-  for (int k = 0; k < per; ++k)
-    if (i0 + k < count) {
-      child_of[i0 + k] = work[a + i0 + k].split ? run : -1;
-      run += work[a + i0 + k].split;
-    }
-  if (threadIdx.x == blockDim.x - 1) *total = run;
-}
-
 // membership of each primitive in its node's first child (BVH.cpp:175-216)
 __global__ void k_flags(const int* __restrict__ perm, const int* __restrict__ pnode, const float4* __restrict__ cen,
                         const NodeWork* work, const yc_aabb* child_box, int* flag, int n, int a, int b) {
@@ -392,6 +362,20 @@ __global__ void k_scan_sums(int* tile_sum, int tiles) {   // one block: exclusiv
 __global__ void k_scan_add(int* out, const int* tile_sum, int n) {
   const int i = blockIdx.x * 1024 + threadIdx.x;
   if (i < n) out[i] += tile_sum[blockIdx.x];
+}
+
+// child slots of a level by the tiled scan: the split flags of its nodes, then (after
+// k_scan_tiles / k_scan_sums) each splitting node's slot and the level's split count
+__global__ void k_split_flags(const NodeWork* work, int* flag, int a, int b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a + i < b) flag[i] = work[a + i].split;
+}
+__global__ void k_slots_finish(const int* flag, const int* tile_sum, int* child_of, int count, int* total) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const int slot = child_of[i] + tile_sum[i >> 10];
+  child_of[i] = flag[i] ? slot : -1;
+  if (i == count - 1) *total = slot + flag[i];
 }
 
 // per splitting node: the first child's count, the children's nodes and segments
@@ -495,7 +479,7 @@ cudaError_t bvh_build_device(const yc_triangle* tris_dev, int n, int bins, int l
   too_deep = false;
   if (n <= 0) return cudaSuccess;
   Buf<float4> cen, lo, hi;
-  Buf<int> perm, perm2, pnode, pnode2, flag, pos, tiles, root, child_of, hist, total;
+  Buf<int> perm, perm2, pnode, pnode2, flag, pos, tiles, root, child_of, hist, total, nflag, ntile;
   Buf<yc_bvh_node> nodes;
   Buf<NodeWork> work;
   Buf<yc_aabb> child_box;
@@ -508,13 +492,9 @@ cudaError_t bvh_build_device(const yc_triangle* tris_dev, int n, int bins, int l
   BB_CHECK(cudaMemcpyAsync(root.p, init_root, sizeof(init_root), cudaMemcpyHostToDevice, s));
   const int gp = (n + BB_TB - 1) / BB_TB;
   k_tri_info<<<gp, BB_TB, 0, s>>>(tris_dev, n, cen.p, lo.p, hi.p, root.p);
-  {   // perm = identity, every primitive in the root
-    std::vector<int> id(n);
-    for (int i = 0; i < n; ++i) id[i] = i;
-    BB_CHECK(cudaMemcpyAsync(perm.p, id.data(), n * sizeof(int), cudaMemcpyHostToDevice, s));
-    BB_CHECK(cudaMemsetAsync(pnode.p, 0, n * sizeof(int), s));
-    BB_CHECK(cudaStreamSynchronize(s));
-  }
+  // perm = identity, every primitive in the root
+  k_iota<<<gp, BB_TB, 0, s>>>(perm.p, n);
+  BB_CHECK(cudaMemsetAsync(pnode.p, 0, n * sizeof(int), s));
   BB_CHECK(nodes.need(1024, s)); BB_CHECK(work.need(1024, s));
   k_root<<<1, 1, 0, s>>>(nodes.p, work.p, root.p, n);
   std::vector<int> level_start = {0};
@@ -527,7 +507,14 @@ cudaError_t bvh_build_device(const yc_triangle* tris_dev, int n, int bins, int l
     k_bounds<<<gp, BB_TB, 0, s>>>(perm.p, pnode.p, lo.p, hi.p, work.p, n, a, b, leaf_max);
     k_hist<<<gp, BB_TB, 0, s>>>(perm.p, pnode.p, cen.p, nodes.p, work.p, hist.p, n, a, b, bins, leaf_max);
     k_decide<<<gn, BB_TB, 0, s>>>(perm.p, nodes.p, work.p, hist.p, child_box.p, a, b, bins, leaf_max);
-    k_child_slots<<<1, 1024, 0, s>>>(work.p, child_of.p, a, b, total.p);
+    {   // child slots in node order: an exclusive scan of the split flags
+      const int ct = (cnt + 1023) / 1024;
+      BB_CHECK(nflag.need(cnt, s)); BB_CHECK(ntile.need(ct, s));
+      k_split_flags<<<gn, BB_TB, 0, s>>>(work.p, nflag.p, a, b);
+      k_scan_tiles<<<ct, 1024, 0, s>>>(nflag.p, child_of.p, ntile.p, cnt);
+      k_scan_sums<<<1, 1024, 0, s>>>(ntile.p, ct);
+      k_slots_finish<<<gn, BB_TB, 0, s>>>(nflag.p, ntile.p, child_of.p, cnt, total.p);
+    }
     int splits = 0;
     BB_CHECK(cudaMemcpyAsync(&splits, total.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     BB_CHECK(cudaStreamSynchronize(s));
