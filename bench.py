@@ -291,6 +291,10 @@ def _trace_roofline(st, kt, l2, pk, pk_kind, kernel_mixed, kernel_extend):
            "peak_source": "measured L2 read bandwidth (yc_measure_l2_gbs, 48 MB x 20 sweeps)",
            "hbm_peak": pk.get("hbm_gbs"), "hbm_frac": achieved / pk.get("hbm_gbs", 1.0), "hbm_peak_source": pk_kind,
            "rays": int(rays), "bytes_per_ray": nbytes / max(1, rays),
+           # the same tests in the reference's layouts (80 B BVHNodeGPU per box, 112 B
+           # TriangleGPU per triangle, include/CL_headers.h:57-107)
+           "ref_layout_bytes_per_ray": (80.0 * boxes + 112.0 * tris + 84.0 * rays) / max(1, rays),
+           "ref_layout_achieved": ((80.0 * boxes + 112.0 * tris + 84.0 * rays) / (ms / 1e3) / 1e9 if ms > 0 else 0.0),
            "box_tests_per_ray": boxes / max(1, rays), "tri_tests_per_ray": tris / max(1, rays),
            "grays_per_s": rays / (ms / 1e3) / 1e9 if ms > 0 else 0.0}
     if mixed:
