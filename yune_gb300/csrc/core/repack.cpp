@@ -38,8 +38,8 @@ struct Builder {
   int n_tri;
   const yc_bvh_node* nodes;
   int n_node;
-  std::vector<float4> out_nodes;
-  std::vector<float4> out_tris;
+  F4Vec out_nodes;
+  F4Vec out_tris;
   int depth = 0;
 
   // order_base: visiting rank of the leaf in the reference traversal; the triangle's
@@ -121,6 +121,7 @@ struct LeafItem {
 struct BinRef {
   int node;
   int link;
+  int count;   // leaves below (1 for a leaf)
   float lo[3], hi[3];
 };
 struct BinNode {
@@ -148,45 +149,119 @@ struct SahBuilder {
     return 2.0f * (d0 * d1 + d0 * d2 + d1 * d2);
   }
 
+  static constexpr int NB = 32;   // SAH bins per axis
+
+  // box and centroid box of items [b, e), and the per-axis bins of their centroids:
+  // min, max and counts, which are exact in any order, so the chunks of a large range
+  // are reduced on their own threads and merged
+  struct RangeStats {
+    float lo[3], hi[3], clo[3], chi[3];
+    int cnt[3][NB];
+    float blo[3][NB][3], bhi[3][NB][3];
+  };
+  static void init_box(float lo[3], float hi[3]) {
+    for (int k = 0; k < 3; ++k) { lo[k] = INFINITY; hi[k] = -INFINITY; }
+  }
+  void bounds(int b, int e, RangeStats& st) const {
+    init_box(st.lo, st.hi);
+    init_box(st.clo, st.chi);
+    for (int i = b; i < e; ++i)
+      for (int k = 0; k < 3; ++k) {
+        st.lo[k] = std::min(st.lo[k], items[i].lo[k]);
+        st.hi[k] = std::max(st.hi[k], items[i].hi[k]);
+        st.clo[k] = std::min(st.clo[k], items[i].c[k]);
+        st.chi[k] = std::max(st.chi[k], items[i].c[k]);
+      }
+  }
+  // bins of [b, e) on the axes with a positive centroid extent, against the node's
+  // centroid box (clo, ext)
+  void binning(int b, int e, const float clo[3], const float ext[3], RangeStats& st) const {
+    for (int k = 0; k < 3; ++k)
+      for (int q = 0; q < NB; ++q) {
+        st.cnt[k][q] = 0;
+        init_box(st.blo[k][q], st.bhi[k][q]);
+      }
+    float scale[3];
+    for (int k = 0; k < 3; ++k) scale[k] = ext[k] > 0.0f ? NB / ext[k] : 0.0f;
+    for (int i = b; i < e; ++i)
+      for (int k = 0; k < 3; ++k) {
+        if (!(ext[k] > 0.0f)) continue;
+        int q = (int)((items[i].c[k] - clo[k]) * scale[k]);
+        q = std::min(NB - 1, std::max(0, q));
+        st.cnt[k][q]++;
+        for (int a = 0; a < 3; ++a) {
+          st.blo[k][q][a] = std::min(st.blo[k][q][a], items[i].lo[a]);
+          st.bhi[k][q][a] = std::max(st.bhi[k][q][a], items[i].hi[a]);
+        }
+      }
+  }
+  // f(chunk b, chunk e, stats) over [b, e) in chunks on threads, merged into st
+  template <class F>
+  void chunked(int b, int e, RangeStats& st, bool boxes, F f) {
+    const int n = e - b;
+    int t = (int)std::min<long>(max_threads, n / (1 << 16));
+    if (t > 1 && threads.load() < max_threads) {
+      std::vector<RangeStats> part(t);
+      std::vector<std::thread> pool;
+      for (int k = 1; k < t; ++k)
+        pool.emplace_back([&, k] { f(b + (int)((long)n * k / t), b + (int)((long)n * (k + 1) / t), part[k]); });
+      f(b, b + n / t, part[0]);
+      for (auto& th : pool) th.join();
+      st = part[0];
+      for (int c = 1; c < t; ++c) {
+        const RangeStats& o = part[c];
+        if (boxes) {
+          for (int k = 0; k < 3; ++k) {
+            st.lo[k] = std::min(st.lo[k], o.lo[k]); st.hi[k] = std::max(st.hi[k], o.hi[k]);
+            st.clo[k] = std::min(st.clo[k], o.clo[k]); st.chi[k] = std::max(st.chi[k], o.chi[k]);
+          }
+        } else {
+          for (int k = 0; k < 3; ++k)
+            for (int q = 0; q < NB; ++q) {
+              st.cnt[k][q] += o.cnt[k][q];
+              for (int a = 0; a < 3; ++a) {
+                st.blo[k][q][a] = std::min(st.blo[k][q][a], o.blo[k][q][a]);
+                st.bhi[k][q][a] = std::max(st.bhi[k][q][a], o.bhi[k][q][a]);
+              }
+            }
+        }
+      }
+    } else {
+      f(b, e, st);
+    }
+  }
+
   // the subtree over items [b, e)
   BinRef build(int b, int e, int depth) {
     BinRef r;
-    float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int k = 0; k < 3; ++k) { r.lo[k] = INFINITY; r.hi[k] = -INFINITY; }
-    for (int i = b; i < e; ++i)
-      for (int k = 0; k < 3; ++k) {
-        r.lo[k] = std::min(r.lo[k], items[i].lo[k]);
-        r.hi[k] = std::max(r.hi[k], items[i].hi[k]);
-        clo[k] = std::min(clo[k], items[i].c[k]);
-        chi[k] = std::max(chi[k], items[i].c[k]);
-      }
+    RangeStats st;
+    chunked(b, e, st, true, [&](int cb, int ce, RangeStats& o) { bounds(cb, ce, o); });
+    float clo[3], chi[3];
+    for (int k = 0; k < 3; ++k) {
+      r.lo[k] = st.lo[k];
+      r.hi[k] = st.hi[k];
+      clo[k] = st.clo[k];
+      chi[k] = st.chi[k];
+    }
     for (int m = max_depth.load(); depth > m && !max_depth.compare_exchange_weak(m, depth);) {}
     if (e - b == 1) {
       r.node = -1;
       r.link = items[b].link;
+      r.count = 1;
       return r;
     }
     // binned SAH
-    constexpr int NB = 32;
+    float ext3[3];
+    for (int k = 0; k < 3; ++k) ext3[k] = chi[k] - clo[k];
+    chunked(b, e, st, false, [&](int cb, int ce, RangeStats& o) { binning(cb, ce, clo, ext3, o); });
     int best_axis = -1, best_split = -1;
     float best_cost = INFINITY;
     for (int k = 0; k < 3; ++k) {
-      const float ext = chi[k] - clo[k];
+      const float ext = ext3[k];
       if (!(ext > 0.0f)) continue;
-      int cnt[NB] = {0};
-      float blo[NB][3], bhi[NB][3];
-      for (int q = 0; q < NB; ++q)
-        for (int a = 0; a < 3; ++a) { blo[q][a] = INFINITY; bhi[q][a] = -INFINITY; }
-      const float scale = NB / ext;
-      for (int i = b; i < e; ++i) {
-        int q = (int)((items[i].c[k] - clo[k]) * scale);
-        q = std::min(NB - 1, std::max(0, q));
-        cnt[q]++;
-        for (int a = 0; a < 3; ++a) {
-          blo[q][a] = std::min(blo[q][a], items[i].lo[a]);
-          bhi[q][a] = std::max(bhi[q][a], items[i].hi[a]);
-        }
-      }
+      const int* cnt = st.cnt[k];
+      const float (*blo)[3] = st.blo[k];
+      const float (*bhi)[3] = st.bhi[k];
       float rlo[NB][3], rhi[NB][3];
       int rcnt[NB];
       float alo[3] = {INFINITY, INFINITY, INFINITY}, ahi[3] = {-INFINITY, -INFINITY, -INFINITY};
@@ -237,20 +312,37 @@ struct SahBuilder {
     bins[node].c[0] = c0;
     bins[node].c[1] = c1;
     r.node = node;
+    r.count = e - b;
     r.link = 0;
     return r;
   }
 
-  // two-child layout of yc_scene.h, nodes in pre-order; returns the link of r
-  int emit_binary(const BinRef& r, std::vector<float4>& out) const {
+  // two-child layout of yc_scene.h, nodes in pre-order; returns the link of r. A
+  // subtree of n leaves holds n - 1 nodes, so each child's first node is known and large
+  // subtrees are written on threads of their own (the same layout as a sequential walk).
+  int emit_binary(const BinRef& r, F4Vec& out) {
     if (r.node < 0) return r.link;
-    const int node = (int)(out.size() / 4);
-    out.resize(out.size() + 4);
+    const size_t base = out.size() / 4;
+    out.resize(out.size() + 4 * (size_t)(r.count - 1));
+    return emit_binary_at(r, out.data(), (int)base);
+  }
+  int emit_binary_at(const BinRef& r, float4* out, int node) {
+    if (r.node < 0) return r.link;
     const BinNode& bn = bins[r.node];
-    const int c0 = emit_binary(bn.c[0], out);
-    const int c1 = emit_binary(bn.c[1], out);
     const BinRef& a = bn.c[0];
     const BinRef& b = bn.c[1];
+    const int left_nodes = a.node < 0 ? 0 : a.count - 1;
+    int c0, c1;
+    if (r.count > kParallelItems && threads.load() < max_threads) {
+      threads.fetch_add(1);
+      std::thread left([&] { c0 = emit_binary_at(a, out, node + 1); });
+      c1 = emit_binary_at(b, out, node + 1 + left_nodes);
+      left.join();
+      threads.fetch_sub(1);
+    } else {
+      c0 = emit_binary_at(a, out, node + 1);
+      c1 = emit_binary_at(b, out, node + 1 + left_nodes);
+    }
     float4* o = &out[4 * (size_t)node];
     o[0] = float4{a.lo[0], a.hi[0], a.lo[1], a.hi[1]};
     o[1] = float4{b.lo[0], b.hi[0], b.lo[1], b.hi[1]};
@@ -266,7 +358,7 @@ struct SahBuilder {
   // four-child layout (yc_scene.h, wide nodes): the children of a binary node are
   // replaced, largest surface area first, by their own children until four remain.
   // depth_out: wide levels below r.
-  int emit_wide(const BinRef& r, std::vector<float4>& out, int& depth_out) const {
+  int emit_wide(const BinRef& r, F4Vec& out, int& depth_out) const {
     depth_out = 0;
     if (r.node < 0) return r.link;
     BinRef kids[4];

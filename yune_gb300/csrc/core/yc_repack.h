@@ -4,16 +4,31 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <memory>
+#include <utility>
 #include <vector>
 
 #include "yc_scene.h"
 
 namespace yc {
 
+// An allocator whose resize() leaves new elements uninitialised (float4 records are
+// written in parallel right after, so their pages are first touched by the filling threads
+// instead of by a sequential zero fill).
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+  template <class U> struct rebind { using other = NoInitAlloc<U>; };
+  NoInitAlloc() = default;
+  template <class U> NoInitAlloc(const NoInitAlloc<U>&) noexcept {}
+  template <class U> void construct(U* p) noexcept { ::new (static_cast<void*>(p)) U; }
+  template <class U, class... A> void construct(U* p, A&&... a) { ::new (static_cast<void*>(p)) U(std::forward<A>(a)...); }
+};
+using F4Vec = std::vector<float4, NoInitAlloc<float4>>;
+
 struct Repacked {
-  std::vector<float4> nodes;   // 4 per two-child node, 8 per four-child node
-  std::vector<float4> tris;    // 3 per stream slot
-  std::vector<float4> shade;   // 4 per original triangle
+  F4Vec nodes;   // 4 per two-child node, 8 per four-child node
+  F4Vec tris;    // 3 per stream slot
+  F4Vec shade;   // 4 per original triangle
   int root_link = LINK_NONE;
   int root_test = 0;
   int depth = 0;               // stack entries a walk can need
