@@ -467,22 +467,35 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
     return 0;
   }
 
-  // validate the reference node array
-  for (int i = 0; i < n_node; ++i) {
+  // validate the reference node array (in parallel; the message names the first bad node)
+  auto node_error = [&](int i, std::string* msg) {
     const yc_bvh_node& n = nodes[i];
-    if (n.vert_len > 10) { err = "BVH node " + std::to_string(i) + " has vert_len > 10"; return -1; }
+    if (n.vert_len > 10) {
+      if (msg) *msg = "BVH node " + std::to_string(i) + " has vert_len > 10";
+      return true;
+    }
     if (is_leaf(n)) {
       for (int k = 0; k < n.vert_len; ++k)
         if (n.vert_list[k] < 0 || n.vert_list[k] >= n_tri) {
-          err = "BVH leaf " + std::to_string(i) + " references triangle " + std::to_string(n.vert_list[k]);
-          return -1;
+          if (msg) *msg = "BVH leaf " + std::to_string(i) + " references triangle " + std::to_string(n.vert_list[k]);
+          return true;
         }
     } else if (is_queued(n) || i == 0) {
       if (n.child_idx <= 0 || n.child_idx + 1 >= n_node) {
-        err = "BVH node " + std::to_string(i) + " has child_idx " + std::to_string(n.child_idx) + " out of range";
-        return -1;
+        if (msg) *msg = "BVH node " + std::to_string(i) + " has child_idx " + std::to_string(n.child_idx) + " out of range";
+        return true;
       }
     }
+    return false;
+  };
+  std::atomic<int> first_bad{n_node};
+  parallel_for((size_t)n_node, [&](size_t i) {
+    if (node_error((int)i, nullptr))
+      for (int m = first_bad.load(); (int)i < m && !first_bad.compare_exchange_weak(m, (int)i);) {}
+  });
+  if (first_bad.load() < n_node) {
+    node_error(first_bad.load(), &err);
+    return -1;
   }
   const yc_bvh_node& root = nodes[0];
   out.root_test = 1;
