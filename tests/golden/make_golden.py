@@ -19,6 +19,11 @@ reference tree:
                        of obj_files.py: triangles, materials and the BVH node array
   obj_cornellbox.npz   the same on the reference's geometry/cornellbox.obj (the test
                        that uses it needs that file and skips without it)
+  bvh_large.npz        SHA-256 digests of BVH::createBVH node arrays for a 327,714-
+                       triangle scene (c1 with a level-7 icosphere) at leaf sizes 4 and
+                       10: large enough for the host builder to split single nodes
+                       over threads (python tests/golden/make_golden.py large writes
+                       this file alone)
 Each file records a SHA-256 of the scene arrays it was made from.
 """
 import hashlib
@@ -52,6 +57,32 @@ def node_fields(nodes):
                 child_idx=nodes["child_idx"].copy(), vert_len=nodes["vert_len"].copy(),
                 vert_list=np.where(np.arange(10)[None, :] < np.maximum(nodes["vert_len"], 0)[:, None],
                                    nodes["vert_list"], -1).astype(np.int32))
+
+
+def node_digest(nodes):
+    """SHA-256 of node_fields(nodes), the fields in a fixed order."""
+    h = hashlib.sha256()
+    f = node_fields(nodes)
+    for k in ("p_min", "p_max", "child_idx", "vert_len", "vert_list"):
+        h.update(np.ascontiguousarray(f[k]).tobytes())
+    return h.hexdigest()
+
+
+LARGE_LEAVES = (4, 10)
+
+
+def large_scene():
+    return scenes.c1(16, 16, level=7)
+
+
+def make_large():
+    s = large_scene()
+    out = {"scene_sha256": scene_hash(s), "bins": 20, "leaves": np.array(LARGE_LEAVES, np.int32)}
+    for leaf in LARGE_LEAVES:
+        nodes = O.ref_bvh(s.tris, 20, leaf)
+        out["nodes_leaf%d" % leaf] = np.int64(len(nodes))
+        out["digest_leaf%d" % leaf] = node_digest(nodes)
+    np.savez_compressed(os.path.join(HERE, "bvh_large.npz"), **out)
 
 
 TRI_FIELDS = ("v1", "v2", "v3", "vn1", "vn2", "vn3", "matID")
@@ -137,8 +168,14 @@ def main():
         out["lights%d" % lights] = acc
         out["sha_lights%d" % lights] = scene_hash(sb)
     np.savez_compressed(os.path.join(HERE, "render_bdpt.npz"), seeds=seeds, **out)
+    make_large()
     print("golden fixtures written to", HERE)
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "large":
+        if O.ref() is None:
+            raise SystemExit("the compiled reference is not available here")
+        make_large()
+    else:
+        main()

@@ -47,6 +47,18 @@ def test_bvh_builder_matches_reference(name):
         assert np.array_equal(np.asarray(f[k]).view(np.int32), np.asarray(g[k]).view(np.int32)), k
 
 
+@pytest.mark.parametrize("leaf", [4, 10])
+def test_bvh_builder_large_matches_reference(leaf):
+    """A scene large enough that the host builder splits single nodes over threads: the
+    node array still equals BVH::createBVH's (digest of the compiled reference's)."""
+    g = _load("bvh_large.npz")
+    s = MG.large_scene()
+    assert MG.scene_hash(s) == str(g["scene_sha256"]), "procedural scene drifted from the fixture"
+    nodes, _ = scenes.build_bvh(s.tris, int(g["bins"]), leaf)
+    assert len(nodes) == int(g["nodes_leaf%d" % leaf])
+    assert MG.node_digest(nodes) == str(g["digest_leaf%d" % leaf])
+
+
 @pytest.mark.parametrize("name", sorted(SCENES))
 def test_oracle_trace_matches_reference(name):
     g = _load("trace_%s.npz" % name)
