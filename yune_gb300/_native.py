@@ -39,6 +39,12 @@ class KernelTimes(C.Structure):
                 ("raysort_ms", C.c_double), ("raysort_launches", C.c_uint64)]
 
 
+class CacheInfo(C.Structure):
+    """yh_cache_info"""
+    _fields_ = [("key", C.c_uint64), ("n_tri", i32), ("n_mat", i32), ("n_light", i32), ("n_node", i32),
+                ("depth", i32), ("has_cam", i32), ("meta_bytes", i32)]
+
+
 class BatchCfg(C.Structure):
     """yc_batch_cfg"""
     _fields_ = [("pool_paths", i32), ("rounds_per_launch", i32), ("logic_blocks_per_sm", i32), ("use_graph", i32),
@@ -104,6 +110,9 @@ SIGNATURES = {
     "yh_write_png": (i32, [C.c_char_p, i32, i32, vp]),
     "yh_write_hdr": (i32, [C.c_char_p, i32, i32, vp]),
     "yh_scene_copy": (i32, [vp, vp, vp, vp]),
+    "yh_cache_save": (i32, [C.c_char_p, C.c_uint64, vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, vp, i32]),
+    "yh_cache_query": (i32, [C.c_char_p, vp]),
+    "yh_cache_load": (i32, [C.c_char_p, C.c_uint64, vp, i32, vp, i32, vp, i32, vp, i32, vp, vp, i32]),
 }
 
 _lib = None
@@ -130,6 +139,21 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+# status codes of the host producers (include/yune_host.h)
+YH_E_INVALID, YH_E_NOMEM, YH_E_RANGE, YH_E_IO, YH_E_FORMAT, YH_E_STALE = -1, -2, -3, -4, -5, -6
+HOST_ERRORS = {YH_E_INVALID: "invalid argument", YH_E_NOMEM: "host allocation failed",
+               YH_E_RANGE: "index or size out of range", YH_E_IO: "file cannot be opened, read or written",
+               YH_E_FORMAT: "not a scene cache of this format, truncated or corrupt",
+               YH_E_STALE: "scene cache made for another key"}
+
+
+def check_host(rc, what=""):
+    """check() for the yh_* host functions, which report by status code alone."""
+    if rc != 0:
+        raise YuneError(rc, (what + ": " if what else "") + HOST_ERRORS.get(rc, "error"))
+    return rc
 
 
 def check(rc, what=""):

@@ -20,6 +20,8 @@ Configurations (sizes and spp of the benchmark workloads):
       importance sampling (YC_BDPT_MIS): paths of at most 20, 8 and 8 segments.
 """
 import ctypes as C
+import hashlib
+import json
 import os
 from dataclasses import dataclass, field
 
@@ -278,6 +280,72 @@ def c4_mis(width=3840, height=2160, spp=128, seed=0, bounces=8):
 
 CONFIGS = {"c0": c0, "c1": c1, "c0_bdpt": c0_bdpt, "c4": c4, "c0_mis": c0_mis, "c0_bdpt_mis": c0_bdpt_mis,
            "c4_mis": c4_mis}
+
+
+# ---- binary scene cache (yh_cache_*) ----
+# Part of every cache key: raise it when a generator's output changes, so that files
+# written by the old generator read as stale instead of standing in for the new scene.
+CACHE_GENERATION = 1
+
+
+def cache_key(name, **params):
+    """64-bit key of configuration `name` built with `params` (and CACHE_GENERATION)."""
+    text = json.dumps([CACHE_GENERATION, name, sorted(params.items())], sort_keys=True)
+    return int.from_bytes(hashlib.sha256(text.encode()).digest()[:8], "little")
+
+
+def save_cache(s, path, key):
+    """Writes scene `s` to the binary scene cache file `path` under `key` (yh_cache_save):
+    its arrays, BVH and camera, and its frame size, spp, options and name as the file's
+    caller bytes."""
+    meta = json.dumps(dict(width=s.width, height=s.height, spp=s.spp, cfg=s.cfg, name=s.name)).encode()
+    arrs = [np.ascontiguousarray(a) for a in (s.tris, s.mats, s.lights, s.nodes, s.cam)]
+    tris, mats, lights, nodes, cam = arrs
+    if cam.nbytes != CAM.itemsize:
+        raise ValueError("the scene's camera must be one Cam record")
+    N.check_host(N.lib().yh_cache_save(os.fsencode(path), key, ptr(tris), len(tris), ptr(mats), len(mats),
+                                       ptr(lights), len(lights), ptr(nodes), len(nodes), int(s.depth), ptr(cam),
+                                       meta, len(meta)), "yh_cache_save " + str(path))
+
+
+def load_cache(path, key):
+    """The SceneData written by save_cache to `path` (yh_cache_load). Raises YuneError with
+    code YH_E_STALE when the file was made for another key, YH_E_FORMAT when it is not an
+    intact cache file, YH_E_IO when it cannot be read."""
+    L = N.lib()
+    info = N.CacheInfo()
+    N.check_host(L.yh_cache_query(os.fsencode(path), C.byref(info)), "yh_cache_query " + str(path))
+    if info.key != key:
+        raise N.YuneError(N.YH_E_STALE, "yh_cache_load %s: %s" % (path, N.HOST_ERRORS[N.YH_E_STALE]))
+    tris = np.empty(info.n_tri, TRIANGLE)
+    mats = np.empty(info.n_mat, MATERIAL)
+    lights = np.empty(info.n_light, QUAD_LIGHT)
+    nodes = np.empty(info.n_node, BVH_NODE)
+    cam = np.empty(1, CAM)
+    meta = C.create_string_buffer(max(1, info.meta_bytes))
+    N.check_host(L.yh_cache_load(os.fsencode(path), key, ptr(tris), len(tris), ptr(mats), len(mats), ptr(lights),
+                                 len(lights), ptr(nodes), len(nodes), ptr(cam) if info.has_cam else None,
+                                 meta, info.meta_bytes), "yh_cache_load " + str(path))
+    m = json.loads(meta.raw[:info.meta_bytes].decode()) if info.meta_bytes else {}
+    if not info.has_cam:
+        cam = camera()
+    return SceneData(tris, mats, lights, nodes, info.depth, cam, int(m.get("width", 512)), int(m.get("height", 512)),
+                     int(m.get("spp", 64)), dict(m.get("cfg", default_cfg())), str(m.get("name", "")))
+
+
+def cached(name, path, **params):
+    """CONFIGS[name](**params) through the cache file `path`: read back when the file holds
+    that configuration with those parameters, otherwise built and written there (a missing,
+    stale or damaged file is replaced)."""
+    key = cache_key(name, **params)
+    try:
+        return load_cache(path, key)
+    except N.YuneError as e:
+        if e.code not in (N.YH_E_IO, N.YH_E_FORMAT, N.YH_E_STALE):
+            raise
+    s = CONFIGS[name](**params)
+    save_cache(s, path, key)
+    return s
 
 
 def pass_seeds(seed, n):
