@@ -35,6 +35,15 @@ enum {
   YH_E_STALE = -6         /* a scene cache made for another key */
 };
 
+/* ---- host threads ----
+ * The host producers (yh_bvh_build, yh_cache_*) and the scene repack inside
+ * yc_upload_scene run on every core the host reports unless a limit is set here
+ * (process-wide; n = 0 lifts it). Their outputs do not depend on the thread count. No
+ * reference counterpart: Yune builds its BVH on one thread.
+ * yh_get_host_threads: the count in effect. */
+int yh_set_host_threads(int n);
+int yh_get_host_threads(void);
+
 /* ---- BVH (src/BVH.cpp) ---- */
 typedef struct yh_bvh yh_bvh;
 /* Builds the breadth-first binned BVH of BVH::createBVH over tris[0..n_tri).

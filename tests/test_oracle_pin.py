@@ -47,14 +47,27 @@ def test_bvh_builder_matches_reference(name):
         assert np.array_equal(np.asarray(f[k]).view(np.int32), np.asarray(g[k]).view(np.int32)), k
 
 
+@pytest.fixture(scope="module")
+def large_scene():
+    return MG.large_scene()
+
+
+@pytest.mark.parametrize("threads", [0, 1, 3, 16])
 @pytest.mark.parametrize("leaf", [4, 10])
-def test_bvh_builder_large_matches_reference(leaf):
+def test_bvh_builder_large_matches_reference(large_scene, leaf, threads):
     """A scene large enough that the host builder splits single nodes over threads: the
-    node array still equals BVH::createBVH's (digest of the compiled reference's)."""
+    node array equals BVH::createBVH's (digest of the compiled reference's) whatever the
+    number of host threads (0: all cores)."""
+    from yune_gb300 import _native as N
     g = _load("bvh_large.npz")
-    s = MG.large_scene()
-    assert MG.scene_hash(s) == str(g["scene_sha256"]), "procedural scene drifted from the fixture"
-    nodes, _ = scenes.build_bvh(s.tris, int(g["bins"]), leaf)
+    assert MG.scene_hash(large_scene) == str(g["scene_sha256"]), "procedural scene drifted from the fixture"
+    L = N.lib()
+    assert L.yh_set_host_threads(threads) == 0
+    try:
+        assert L.yh_get_host_threads() == threads if threads else L.yh_get_host_threads() >= 1
+        nodes, _ = scenes.build_bvh(large_scene.tris, int(g["bins"]), leaf)
+    finally:
+        L.yh_set_host_threads(0)
     assert len(nodes) == int(g["nodes_leaf%d" % leaf])
     assert MG.node_digest(nodes) == str(g["digest_leaf%d" % leaf])
 

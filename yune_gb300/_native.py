@@ -110,6 +110,8 @@ SIGNATURES = {
     "yh_write_png": (i32, [C.c_char_p, i32, i32, vp]),
     "yh_write_hdr": (i32, [C.c_char_p, i32, i32, vp]),
     "yh_scene_copy": (i32, [vp, vp, vp, vp]),
+    "yh_set_host_threads": (i32, [i32]),
+    "yh_get_host_threads": (i32, []),
     "yh_cache_save": (i32, [C.c_char_p, C.c_uint64, vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, vp, i32]),
     "yh_cache_query": (i32, [C.c_char_p, vp]),
     "yh_cache_load": (i32, [C.c_char_p, C.c_uint64, vp, i32, vp, i32, vp, i32, vp, i32, vp, vp, i32]),

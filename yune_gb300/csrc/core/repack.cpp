@@ -28,6 +28,7 @@
 
 #include "../ym_math.h"
 #include "yc_repack.h"
+#include "host/yh_threads.h"
 
 namespace yc {
 
@@ -87,7 +88,7 @@ struct Builder {
 // its own outputs)
 template <class F>
 void parallel_for(size_t n, F f) {
-  const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t hw = (size_t)yh::host_threads();
   const size_t t = std::min(hw, std::max<size_t>(1, n / 4096));
   if (t <= 1) {
     for (size_t i = 0; i < n; ++i) f(i);
@@ -140,7 +141,7 @@ struct SahBuilder {
   std::atomic<int> max_depth{0};
   std::atomic<int> next_node{0};
   std::atomic<int> threads{1};
-  int max_threads = (int)std::max(1u, std::thread::hardware_concurrency());
+  int max_threads = yh::host_threads();
 
   SahBuilder(std::vector<LeafItem>& it) : items(it), bins(it.size() > 1 ? it.size() - 1 : 0) {}
 

@@ -22,6 +22,7 @@
 // then their children are numbered by a prefix count in node order, so the node array
 // is the sequential builder's, bit for bit.
 #include "yune_host.h"
+#include "host/yh_threads.h"
 
 #include <algorithm>
 #include <array>
@@ -346,7 +347,7 @@ extern "C" int yh_bvh_build(const yc_triangle* tris, int n_tri, int bins, int le
   *out = nullptr;
   yh_bvh* bvh = new (std::nothrow) yh_bvh;
   if (!bvh) return YH_E_NOMEM;
-  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int hw = yh::host_threads();
   try {
     std::vector<TriInfo> info(n_tri);
     const float fmax_ = FLT_MAX;

@@ -20,6 +20,7 @@
 // A file is written under a temporary name in the same directory and renamed into
 // place, so a reader sees either the old file or the complete new one.
 #include "yune_host.h"
+#include "host/yh_threads.h"
 
 #include <fcntl.h>
 #include <sys/stat.h>
@@ -78,7 +79,7 @@ uint64_t hash_words(const unsigned char* p, size_t n) {
   return h;
 }
 
-int host_threads() { return (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency())); }
+int host_threads() { return std::max(1, std::min(16, yh::host_threads())); }
 
 // f(k) for k in [0, n) on up to host_threads() threads, one index at a time
 template <class F>
