@@ -313,27 +313,55 @@ __global__ void k_sort_scan(const RoundCounters* rc_in, SortCtl* sctl, int thres
   sctl->use = use;
 }
 
+// Scatter in tiles of SORT_U x 256 entries per block: the tile's entries take their
+// offsets within the tile from shared counters (one shared atomic per run of equal keys
+// in a warp), then one global atomic per key and tile reserves the tile's range. The
+// 25 keys would otherwise put every warp's atomics on the same few addresses.
+constexpr int SORT_U = 8;
+
 __global__ void __launch_bounds__(ENGINE_TB) k_sort_scatter(const int* __restrict__ in_closest,
                                                             const int* __restrict__ in_any, const RoundCounters* rc_in,
                                                             const int* __restrict__ keys, int* sorted, SortCtl* sctl) {
+  __shared__ int s_cnt[SORT_KEYS];
+  __shared__ int s_base[SORT_KEYS];
   if (!sctl->use) return;
   const int nc = rc_in->n_closest, n = nc + rc_in->n_any;
   const int lane = threadIdx.x & 31;
-  const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int warps_total = (gridDim.x * blockDim.x) >> 5;
-  for (int wbase = warp_global * 32; wbase < n; wbase += warps_total * 32) {
-    const int e = wbase + lane;
-    const bool active = e < n;
-    const int key = active ? keys[e] : -1 - lane;   // idle lanes match nobody
-    const unsigned peers = __match_any_sync(0xffffffffu, key);
-    const int leader = __ffs(peers) - 1;
-    int base = 0;
-    if (active && lane == leader) base = atomicAdd(&sctl->cursor[key], __popc(peers));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (active) {
-      const int p = e < nc ? in_closest[e] : in_any[e - nc];
-      sorted[base + __popc(peers & ((1u << lane) - 1))] = p;
+  const int tile = ENGINE_TB * SORT_U;
+  // t0 is the same for every thread of the block, so the barriers below are uniform
+  for (int t0 = blockIdx.x * tile; t0 < n; t0 += gridDim.x * tile) {
+    if (threadIdx.x < SORT_KEYS) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int wbase = t0 + (threadIdx.x >> 5) * 32 * SORT_U;
+    int key[SORT_U], off[SORT_U], val[SORT_U];
+#pragma unroll
+    for (int u = 0; u < SORT_U; ++u) {
+      const int e = wbase + u * 32 + lane;
+      const bool active = e < n;
+      key[u] = active ? keys[e] : -1 - lane;   // idle lanes match nobody
+      val[u] = active ? (e < nc ? in_closest[e] : in_any[e - nc]) : 0;
     }
+#pragma unroll
+    for (int u = 0; u < SORT_U; ++u) {
+      const int e = wbase + u * 32 + lane;
+      const unsigned peers = __match_any_sync(0xffffffffu, key[u]);
+      const int leader = __ffs(peers) - 1;
+      int b = 0;
+      if (e < n && lane == leader) b = atomicAdd(&s_cnt[key[u]], __popc(peers));
+      off[u] = __shfl_sync(0xffffffffu, b, leader) + __popc(peers & ((1u << lane) - 1));
+    }
+    __syncthreads();
+    if (threadIdx.x < SORT_KEYS) {
+      const int c = s_cnt[threadIdx.x];
+      s_base[threadIdx.x] = c ? atomicAdd(&sctl->cursor[threadIdx.x], c) : 0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < SORT_U; ++u) {
+      const int e = wbase + u * 32 + lane;
+      if (e < n) sorted[s_base[key[u]] + off[u]] = val[u];
+    }
+    __syncthreads();   // s_cnt and s_base are reset by the next tile
   }
 }
 

@@ -8,7 +8,9 @@
 //   | Morton code of the direction's cell in [-1, 1]^3 (db bits per axis)
 // with a counting sort: key and histogram (one atomic per run of equal keys in a warp),
 // an exclusive scan in tiles of 1024 bins (which also clears the histogram for the next
-// round), and a scatter of the path indices. The order is a heuristic only: every ray is traced with
+// round), and a scatter of the path indices. The key and scatter kernels are bound by
+// the latency of dependent loads and of the cursor atomics, so each warp keeps four runs
+// of 32 entries in flight. The order is a heuristic only: every ray is traced with
 // the same arithmetic whatever its position, so results do not change.
 #include <cuda_runtime.h>
 
@@ -20,6 +22,7 @@ namespace yc {
 constexpr int RS_TB = 256;
 constexpr int RS_SCAN_TB = 1024;
 constexpr int RS_MAX_TILES = 64;   // 2^16 bins at most
+constexpr int RS_U = 4;            // runs of 32 work-list entries a warp handles per step
 
 __device__ __forceinline__ unsigned spread3(unsigned x) {   // bit i of x -> bit 3i (x < 8)
   return (x & 1u) | ((x & 2u) << 2) | ((x & 4u) << 4);
@@ -70,19 +73,35 @@ __global__ void __launch_bounds__(RS_TB) k_rs_key(Box box, const int* __restrict
   const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int warps_total = (gridDim.x * blockDim.x) >> 5;
   const unsigned kind_bit = 1u << (3 * (ob + db));
-  for (int wbase = warp_global * 32; wbase < n; wbase += warps_total * 32) {
-    const int e = wbase + lane;
-    unsigned key = 0xffffffffu - lane;   // idle lanes match nobody
-    if (e < n) {
-      const bool any = e >= nc;
-      const int p = any ? q_any[e - nc] : q_closest[e];
-      float4 lo, hi;
-      box.of(p, lo, hi);
-      key = ray_key(__ldg(&ro[p]), __ldg(&rd[p]), lo, hi, ob, db) | (any ? kind_bit : 0u);
-      keys[e] = key;
+  // RS_U runs of 32 entries per warp and step: their queue, origin and direction loads
+  // are all issued before the first key is formed
+  for (int wbase = warp_global * 32 * RS_U; wbase < n; wbase += warps_total * 32 * RS_U) {
+    int p[RS_U];
+#pragma unroll
+    for (int u = 0; u < RS_U; ++u) {
+      const int e = wbase + u * 32 + lane;
+      p[u] = e < n ? (e < nc ? q_closest[e] : q_any[e - nc]) : -1;
     }
-    const unsigned peers = __match_any_sync(0xffffffffu, key);
-    if (e < n && lane == __ffs(peers) - 1) atomicAdd(&hist[key], (unsigned)__popc(peers));
+    float4 o[RS_U], d[RS_U];
+#pragma unroll
+    for (int u = 0; u < RS_U; ++u) {
+      const int pc = p[u] >= 0 ? p[u] : 0;   // idle lanes read slot 0 (n > 0 here) and discard it
+      o[u] = __ldg(&ro[pc]);
+      d[u] = __ldg(&rd[pc]);
+    }
+#pragma unroll
+    for (int u = 0; u < RS_U; ++u) {
+      const int e = wbase + u * 32 + lane;
+      unsigned key = 0xffffffffu - lane;   // idle lanes match nobody
+      if (e < n) {
+        float4 lo, hi;
+        box.of(p[u], lo, hi);
+        key = ray_key(o[u], d[u], lo, hi, ob, db) | (e >= nc ? kind_bit : 0u);
+        keys[e] = key;
+      }
+      const unsigned peers = __match_any_sync(0xffffffffu, key);
+      if (e < n && lane == __ffs(peers) - 1) atomicAdd(&hist[key], (unsigned)__popc(peers));
+    }
   }
 }
 
@@ -159,16 +178,33 @@ __global__ void __launch_bounds__(RS_TB) k_rs_scatter(const int* __restrict__ q_
   const int lane = threadIdx.x & 31;
   const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int warps_total = (gridDim.x * blockDim.x) >> 5;
-  for (int wbase = warp_global * 32; wbase < n; wbase += warps_total * 32) {
-    const int e = wbase + lane;
-    const bool active = e < n;
-    const unsigned key = active ? keys[e] : 0xffffffffu - lane;
-    const unsigned peers = __match_any_sync(0xffffffffu, key);
-    const int leader = __ffs(peers) - 1;
-    unsigned base = 0;
-    if (active && lane == leader) base = s_base[key / RS_SCAN_TB] + atomicAdd(&cursor[key], (unsigned)__popc(peers));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (active) sorted[base + __popc(peers & ((1u << lane) - 1))] = e < nc ? q_closest[e] : q_any[e - nc];
+  // RS_U runs of 32 entries per warp and step: the runs' cursor atomics are in flight
+  // together instead of one after another
+  for (int wbase = warp_global * 32 * RS_U; wbase < n; wbase += warps_total * 32 * RS_U) {
+    unsigned key[RS_U], peers[RS_U], base[RS_U];
+    int val[RS_U];
+#pragma unroll
+    for (int u = 0; u < RS_U; ++u) {
+      const int e = wbase + u * 32 + lane;
+      const bool active = e < n;
+      key[u] = active ? keys[e] : 0xffffffffu - lane;
+      val[u] = active ? (e < nc ? q_closest[e] : q_any[e - nc]) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < RS_U; ++u) {
+      const int e = wbase + u * 32 + lane;
+      peers[u] = __match_any_sync(0xffffffffu, key[u]);
+      unsigned b = 0;
+      if (e < n && lane == __ffs(peers[u]) - 1)
+        b = s_base[key[u] / RS_SCAN_TB] + atomicAdd(&cursor[key[u]], (unsigned)__popc(peers[u]));
+      base[u] = b;
+    }
+#pragma unroll
+    for (int u = 0; u < RS_U; ++u) {
+      const int e = wbase + u * 32 + lane;
+      const unsigned b = __shfl_sync(0xffffffffu, base[u], __ffs(peers[u]) - 1);
+      if (e < n) sorted[b + __popc(peers[u] & ((1u << lane) - 1))] = val[u];
+    }
   }
 }
 
