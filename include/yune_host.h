@@ -60,6 +60,19 @@ int yh_bvh_copy_nodes(const yh_bvh* b, yc_bvh_node* out, int capacity);
 int yh_bvh_depth(const yh_bvh* b);
 void yh_bvh_free(yh_bvh* b);
 
+/* Refits nodes[0..n_node) in place after the triangles moved (same count, same
+ * indices): the bottom-up pass BVH::createBVH ends with (BVH::resizeBvh,
+ * src/BVH.cpp:218-247) run on the new positions. A leaf's box becomes the union of its
+ * triangles' padded boxes (TriangleCPU::computeAABB), an interior node's the union of its
+ * two children, an empty node keeps its box. Which triangles share a leaf does not
+ * change: traversal stays exact, and slows down as the geometry departs from the one the
+ * tree was built for (rebuild then). On unmoved triangles the array is unchanged, bit
+ * for bit. Upload the refitted array with yc_upload_scene as any other. YH_E_RANGE: a
+ * leaf entry outside [0, n_tri), a vert_len above 10, or a child index that does not
+ * come after its parent (the reference's breadth-first order). No reference counterpart
+ * as an entry point: Yune rebuilds the whole tree when a scene changes. */
+int yh_bvh_refit(const yc_triangle* tris, int n_tri, yc_bvh_node* nodes, int n_node);
+
 /* TriangleCPU::computeCentroid / computeAABB for one triangle. */
 int yh_triangle_aabb(const yc_triangle* t, yc_aabb* aabb, yc_float4* centroid);
 

@@ -97,6 +97,7 @@ SIGNATURES = {
     "yh_bvh_copy_nodes": (i32, [vp, vp, i32]),
     "yh_bvh_depth": (i32, [vp]),
     "yh_bvh_free": (None, [vp]),
+    "yh_bvh_refit": (i32, [vp, i32, vp, i32]),
     "yh_triangle_aabb": (i32, [vp, vp, vp]),
     "yh_camera_look": (i32, [vp, vp, vp, vp, f32, vp]),
     "yh_scene_new": (i32, [C.POINTER(vp)]),

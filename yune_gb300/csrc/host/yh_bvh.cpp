@@ -1,7 +1,7 @@
 // yh_bvh.cpp -- the breadth-first binned BVH of Yune's BVH::createBVH, restated.
 //
 // The node array this produces is the one src/BVH.cpp:56-173 produces for the same
-// triangles, bins and leaf size (tests/test_host_bvh.py compares the two node by
+// triangles, bins and leaf size (tests/test_oracle_pin.py compares the two node by
 // node). The arithmetic that decides splits is kept in the reference's order, in
 // float, so every comparison takes the same branch:
 //   split axis    longest extent of the union of triangle boxes (BVH.cpp:280-314)
@@ -489,3 +489,52 @@ extern "C" int yh_bvh_copy_nodes(const yh_bvh* b, yc_bvh_node* out, int capacity
   return YH_OK;
 }
 extern "C" void yh_bvh_free(yh_bvh* b) { delete b; }
+
+// The bottom-up pass of BVH::createBVH (BVH::resizeBvh, src/BVH.cpp:218-247) on an
+// existing node array with new triangle positions: leaf boxes are computed in parallel
+// (each from its own triangles), then every interior box, in reverse node order, from
+// its two children, which come after it in the array.
+extern "C" int yh_bvh_refit(const yc_triangle* tris, int n_tri, yc_bvh_node* nodes, int n_node) {
+  if (n_tri < 0 || n_node < 0 || (n_tri > 0 && !tris) || (n_node > 0 && !nodes)) return YH_E_INVALID;
+  for (int j = 0; j < n_node; ++j) {
+    const yc_bvh_node& g = nodes[j];
+    if (g.vert_len > 0) {
+      if (g.vert_len > 10) return YH_E_RANGE;
+      for (int k = 0; k < g.vert_len; ++k)
+        if (g.vert_list[k] < 0 || g.vert_list[k] >= n_tri) return YH_E_RANGE;
+    } else if (g.child_idx > 0) {
+      if (g.child_idx <= j || g.child_idx >= n_node - 1) return YH_E_RANGE;
+    }
+  }
+  const float fmax_ = FLT_MAX;
+  pfor((size_t)n_node, 4096, yh::host_threads(), [&](size_t j) {
+    yc_bvh_node& g = nodes[j];
+    if (g.vert_len <= 0) return;
+    float lo[3] = {fmax_, fmax_, fmax_}, hi[3] = {-fmax_, -fmax_, -fmax_};
+    for (int k = 0; k < g.vert_len; ++k) {
+      TriInfo ti;
+      tri_info(tris[g.vert_list[k]], ti);
+      for (int a = 0; a < 3; ++a) {
+        lo[a] = std::min(ti.lo[a], lo[a]);
+        hi[a] = std::max(ti.hi[a], hi[a]);
+      }
+    }
+    g.aabb.p_min = yc_float4{lo[0], lo[1], lo[2], 1.0f};
+    g.aabb.p_max = yc_float4{hi[0], hi[1], hi[2], 1.0f};
+  });
+  for (int j = n_node - 1; j >= 0; --j) {
+    yc_bvh_node& g = nodes[j];
+    if (g.vert_len > 0 || g.child_idx <= 0) continue;
+    const yc_aabb& ca = nodes[g.child_idx].aabb;
+    const yc_aabb& cb = nodes[g.child_idx + 1].aabb;
+    yc_aabb u = ca;
+    u.p_min.x = std::min(cb.p_min.x, ca.p_min.x);
+    u.p_min.y = std::min(cb.p_min.y, ca.p_min.y);
+    u.p_min.z = std::min(cb.p_min.z, ca.p_min.z);
+    u.p_max.x = std::max(cb.p_max.x, ca.p_max.x);
+    u.p_max.y = std::max(cb.p_max.y, ca.p_max.y);
+    u.p_max.z = std::max(cb.p_max.z, ca.p_max.z);
+    g.aabb = u;
+  }
+  return YH_OK;
+}

@@ -139,6 +139,15 @@ def build_bvh(tris, bins=20, leaf=10):
     return nodes, depth
 
 
+def refit_bvh(tris, nodes):
+    """A copy of `nodes` refitted to the (moved) triangles `tris` (yh_bvh_refit): the tree
+    of the original build with every box recomputed bottom-up from the new positions."""
+    out = np.ascontiguousarray(nodes).copy()
+    tris = np.ascontiguousarray(tris)
+    N.check_host(N.lib().yh_bvh_refit(ptr(tris), len(tris), ptr(out), len(out)), "yh_bvh_refit")
+    return out
+
+
 def camera(eye=(0.0, 0.0, 1.4), side=(1.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), look=(0.0, 0.0, -1.0), fov=60.0):
     cam = np.zeros(1, CAM)
     a = [np.asarray(v, np.float32) for v in (eye, side, up, look)]
