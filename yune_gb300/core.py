@@ -20,13 +20,13 @@ from .layouts import ptr
 def write_png(path, rgba):
     """8-bit RGB PNG of an (H, W, 4) float frame (yh_write_png), first file row = last frame row."""
     a = np.ascontiguousarray(rgba, np.float32)
-    N.check(N.lib().yh_write_png(os.fsencode(str(path)), a.shape[1], a.shape[0], ptr(a)), "yh_write_png")
+    N.check_host(N.lib().yh_write_png(os.fsencode(str(path)), a.shape[1], a.shape[0], ptr(a)), "yh_write_png")
 
 
 def write_hdr(path, rgba):
     """Radiance RGBE file of an (H, W, 4) float frame (yh_write_hdr)."""
     a = np.ascontiguousarray(rgba, np.float32)
-    N.check(N.lib().yh_write_hdr(os.fsencode(str(path)), a.shape[1], a.shape[0], ptr(a)), "yh_write_hdr")
+    N.check_host(N.lib().yh_write_hdr(os.fsencode(str(path)), a.shape[1], a.shape[0], ptr(a)), "yh_write_hdr")
 
 
 def cfg_struct(cfg):

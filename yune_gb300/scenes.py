@@ -80,7 +80,7 @@ class Builder:
     def __init__(self):
         L = N.lib()
         h = C.c_void_p()
-        N.check(L.yh_scene_new(C.byref(h)), "yh_scene_new")
+        N.check_host(L.yh_scene_new(C.byref(h)), "yh_scene_new")
         self.h = h
 
     def __del__(self):
@@ -89,38 +89,38 @@ class Builder:
             self.h = None
 
     def cornell(self, seed=0, sigma2=0.09, phong_exp=50.0, emission=15.0, boxes=True):
-        N.check(N.lib().yh_scene_add_cornell(self.h, seed, sigma2, phong_exp, emission, int(boxes)), "cornell")
+        N.check_host(N.lib().yh_scene_add_cornell(self.h, seed, sigma2, phong_exp, emission, int(boxes)), "cornell")
         return self
 
     def add_material(self, m):
         mid = C.c_int()
-        N.check(N.lib().yh_scene_add_material(self.h, ptr(m), C.byref(mid)), "material")
+        N.check_host(N.lib().yh_scene_add_material(self.h, ptr(m), C.byref(mid)), "material")
         return mid.value
 
     def icosphere(self, center, radius, level, mat_id, disp=0.0, seed=0):
         c = np.asarray(center, np.float32)
-        N.check(N.lib().yh_scene_add_icosphere(self.h, ptr(c), radius, level, disp, seed, mat_id), "icosphere")
+        N.check_host(N.lib().yh_scene_add_icosphere(self.h, ptr(c), radius, level, disp, seed, mat_id), "icosphere")
         return self
 
     def load_obj(self, path):
         """Appends an OBJ file and its material file (yh_scene_load_obj, the rules of
         Scene::loadModel); returns the number of triangles read."""
         n = C.c_int()
-        N.check(N.lib().yh_scene_load_obj(self.h, os.fsencode(path), C.byref(n)), "yh_scene_load_obj " + str(path))
+        N.check_host(N.lib().yh_scene_load_obj(self.h, os.fsencode(path), C.byref(n)), "yh_scene_load_obj " + str(path))
         return n.value
 
     def add_light(self, l):
-        N.check(N.lib().yh_scene_add_light(self.h, ptr(l)), "light")
+        N.check_host(N.lib().yh_scene_add_light(self.h, ptr(l)), "light")
         return self
 
     def arrays(self):
         nt, nm, nl = C.c_int(), C.c_int(), C.c_int()
         L = N.lib()
-        N.check(L.yh_scene_counts(self.h, C.byref(nt), C.byref(nm), C.byref(nl)), "counts")
+        N.check_host(L.yh_scene_counts(self.h, C.byref(nt), C.byref(nm), C.byref(nl)), "counts")
         tris = np.zeros(nt.value, TRIANGLE)
         mats = np.zeros(nm.value, MATERIAL)
         lights = np.zeros(nl.value, QUAD_LIGHT)
-        N.check(L.yh_scene_copy(self.h, ptr(tris), ptr(mats), ptr(lights)), "copy")
+        N.check_host(L.yh_scene_copy(self.h, ptr(tris), ptr(mats), ptr(lights)), "copy")
         return tris, mats, lights
 
 
@@ -128,11 +128,11 @@ def build_bvh(tris, bins=20, leaf=10):
     """Node array of BVH::createBVH for these triangles, and the tree depth."""
     L = N.lib()
     h = C.c_void_p()
-    N.check(L.yh_bvh_build(ptr(tris), len(tris), bins, leaf, C.byref(h)), "yh_bvh_build")
+    N.check_host(L.yh_bvh_build(ptr(tris), len(tris), bins, leaf, C.byref(h)), "yh_bvh_build")
     try:
         n = L.yh_bvh_node_count(h)
         nodes = np.zeros(n, BVH_NODE)
-        N.check(L.yh_bvh_copy_nodes(h, ptr(nodes), n), "copy nodes")
+        N.check_host(L.yh_bvh_copy_nodes(h, ptr(nodes), n), "copy nodes")
         depth = L.yh_bvh_depth(h)
     finally:
         L.yh_bvh_free(h)
@@ -151,7 +151,7 @@ def refit_bvh(tris, nodes):
 def camera(eye=(0.0, 0.0, 1.4), side=(1.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), look=(0.0, 0.0, -1.0), fov=60.0):
     cam = np.zeros(1, CAM)
     a = [np.asarray(v, np.float32) for v in (eye, side, up, look)]
-    N.check(N.lib().yh_camera_look(ptr(a[0]), ptr(a[1]), ptr(a[2]), ptr(a[3]), fov, ptr(cam)), "camera")
+    N.check_host(N.lib().yh_camera_look(ptr(a[0]), ptr(a[1]), ptr(a[2]), ptr(a[3]), fov, ptr(cam)), "camera")
     return cam
 
 
