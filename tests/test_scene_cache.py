@@ -175,3 +175,20 @@ def test_cached_builds_once_then_reads(tmp_path, monkeypatch):
     assert calls == [dict(width=32, height=24, seed=4)]
     assert c.tris.tobytes() != a.tris.tobytes()
     _same(c, scenes.load_cache(p, scenes.cache_key("c0", width=32, height=24, seed=4)))
+
+
+def test_concurrent_writers_leave_one_whole_file(tmp_path):
+    """Writers of one path in parallel: each writes its own temporary file and renames it
+    into place, so the file read afterwards is one writer's scene, whole."""
+    import threading
+    p = str(tmp_path / "shared.ysc")
+    made = {k: scenes.c0(16, 16, seed=k) for k in range(1, 5)}
+    threads = [threading.Thread(target=scenes.save_cache, args=(s, p, k)) for k, s in made.items()]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    info = N.CacheInfo()
+    assert N.lib().yh_cache_query(os.fsencode(p), C.byref(info)) == 0
+    _same(made[info.key], scenes.load_cache(p, info.key))
+    assert sorted(os.listdir(tmp_path)) == ["shared.ysc"]   # no temporary file left behind

@@ -27,6 +27,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cstdint>
 #include <cstdio>
@@ -221,7 +222,10 @@ int yh_cache_save(const char* path, uint64_t key, const yc_triangle* tris, int n
   hd.payload_hash = combine(sect_hash);
   hd.header_hash = header_hash(hd);
 
-  const std::string tmp = std::string(path) + ".tmp." + std::to_string((long long)getpid());
+  // unique per process and call, so concurrent writers of one path never share a file
+  static std::atomic<unsigned> serial{0};
+  const std::string tmp = std::string(path) + ".tmp." + std::to_string((long long)getpid()) + "." +
+                          std::to_string(serial.fetch_add(1));
   int rc = YH_OK;
   {
     Fd f;
