@@ -137,6 +137,24 @@ int yc_scene_bytes(yc_ctx* ctx, int scene_id, uint64_t* bytes);
 /* interior levels of the uploaded hierarchy (a traversal stack needs depth + 2 slots) */
 int yc_scene_depth(yc_ctx* ctx, int scene_id, int* depth);
 
+/* The device layout yc_upload_scene would build for these arrays, computed on the host
+ * without a device or a context: the bytes the scene would hold (what yc_scene_bytes
+ * reports after the upload, so a caller can admit a scene against an HBM budget first),
+ * the traversal stack depth, and a digest of the repacked node, triangle-stream and
+ * shading arrays (FNV-1a over their 64-bit words), equal for equal inputs whatever the
+ * host thread count. tree_mode: the YC_OPT_TREE values. The same checks as the upload:
+ * YC_E_INVALID with yc_last_error() naming the first bad triangle or node. No reference
+ * counterpart (Yune learns its buffer sizes from clCreateBuffer). */
+typedef struct yc_scene_layout_info {
+  uint64_t device_bytes;
+  uint64_t node_bytes, stream_bytes, shade_bytes;
+  uint64_t digest;
+  int32_t depth;            /* interior levels, as yc_scene_depth */
+  int32_t wide;             /* 1: four-child nodes */
+} yc_scene_layout_info;
+int yc_scene_layout(const yc_triangle* tris_host, int n_tri, int n_mat, const yc_bvh_node* nodes_host, int n_node,
+                    int tree_mode, yc_scene_layout_info* out);
+
 /* ---- camera (CLManager::setupCameraBuffer + the map/unmap of
  *      RendererCore::updateRenderKernelArgs, src/RendererCore.cpp:532-555) ---- */
 int yc_set_camera(yc_ctx* ctx, const yc_cam* cam_host);

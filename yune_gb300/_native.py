@@ -39,6 +39,12 @@ class KernelTimes(C.Structure):
                 ("raysort_ms", C.c_double), ("raysort_launches", C.c_uint64)]
 
 
+class SceneLayout(C.Structure):
+    """yc_scene_layout_info"""
+    _fields_ = [("device_bytes", C.c_uint64), ("node_bytes", C.c_uint64), ("stream_bytes", C.c_uint64),
+                ("shade_bytes", C.c_uint64), ("digest", C.c_uint64), ("depth", i32), ("wide", i32)]
+
+
 class CacheInfo(C.Structure):
     """yh_cache_info"""
     _fields_ = [("key", C.c_uint64), ("n_tri", i32), ("n_mat", i32), ("n_light", i32), ("n_node", i32),
@@ -65,6 +71,7 @@ SIGNATURES = {
     "yc_release_scene": (i32, [vp, i32]),
     "yc_scene_bytes": (i32, [vp, i32, C.POINTER(C.c_uint64)]),
     "yc_scene_depth": (i32, [vp, i32, C.POINTER(i32)]),
+    "yc_scene_layout": (i32, [vp, i32, i32, vp, i32, i32, vp]),
     "yc_set_camera": (i32, [vp, vp]),
     "yc_alloc_accum": (i32, [vp, i32, i32, C.POINTER(i32)]),
     "yc_free_accum": (i32, [vp, i32]),

@@ -553,6 +553,44 @@ int yc_upload_scene(yc_ctx* c, const yc_triangle* tris, int n_tri, const yc_mate
   return YC_OK;
 }
 
+int yc_scene_layout(const yc_triangle* tris, int n_tri, int n_mat, const yc_bvh_node* nodes, int n_node,
+                    int tree_mode, yc_scene_layout_info* out) {
+  if (!out) return fail(YC_E_INVALID, "out is NULL");
+  if (n_tri < 0 || n_mat < 0 || n_node < 0) return fail(YC_E_INVALID, "negative count");
+  if ((n_tri > 0 && !tris) || (n_node > 0 && !nodes)) return fail(YC_E_INVALID, "NULL array with non-zero count");
+  if (tree_mode != yc::TREE_REFERENCE && tree_mode != yc::TREE_SAH_OVER_LEAVES && tree_mode != yc::TREE_WIDE4)
+    return fail(YC_E_INVALID, "bad tree mode");
+  for (int i = 0; i < n_tri; ++i)
+    if (tris[i].matID < 0 || tris[i].matID >= n_mat)
+      return fail(YC_E_INVALID, "triangle " + std::to_string(i) + " has matID out of range");
+  yc::Repacked rp;
+  std::string err;
+  if (yc::repack_scene(tris, n_tri, nodes, n_node, tree_mode, rp, err)) return fail(YC_E_INVALID, err);
+  // the allocations of yc_upload_scene
+  out->node_bytes = std::max<size_t>(rp.nodes.size(), 4) * sizeof(float4);
+  out->stream_bytes = std::max<size_t>(rp.tris.size(), 3) * sizeof(float4);
+  out->shade_bytes = std::max<size_t>(rp.shade.size(), 4) * sizeof(float4);
+  out->device_bytes = out->node_bytes + out->stream_bytes + out->shade_bytes +
+                      (uint64_t)std::max(n_mat, 1) * sizeof(yc_material) + yc::MAX_LIGHTS * sizeof(yc_quad_light);
+  uint64_t h = 0xcbf29ce484222325ull;
+  auto words = [&h](const float4* p, size_t n) {
+    const uint64_t* w = reinterpret_cast<const uint64_t*>(p);
+    h = (h ^ (uint64_t)n) * 0x100000001b3ull;
+    for (size_t i = 0; i < 2 * n; ++i) h = (h ^ w[i]) * 0x100000001b3ull;
+  };
+  words(rp.nodes.data(), rp.nodes.size());
+  words(rp.tris.data(), rp.tris.size());
+  words(rp.shade.data(), rp.shade.size());
+  const float4 root[2] = {rp.root_lo, rp.root_hi};
+  words(root, 2);
+  h = (h ^ (uint64_t)(uint32_t)rp.root_link) * 0x100000001b3ull;
+  h = (h ^ (uint64_t)(uint32_t)rp.root_test) * 0x100000001b3ull;
+  out->digest = h;
+  out->depth = rp.depth;
+  out->wide = rp.wide;
+  return YC_OK;
+}
+
 int yc_bvh_build(yc_ctx* c, const yc_triangle* tris, int n_tri, int bins, int leaf_max, int* n_node, int* depth) {
   if (!c || n_tri < 0 || (n_tri > 0 && !tris) || leaf_max < 1 || leaf_max > 10 || bins < 0 || bins > 256)
     return fail(YC_E_INVALID, "yc_bvh_build: bad argument");
