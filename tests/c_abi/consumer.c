@@ -2,9 +2,9 @@
  *
  * Checks that the headers and libyune_gb300.so form a C ABI a non-C++ host can bind
  * (plain structs, pointers and sizes; no C++ or torch types): it builds a scene with the
- * host producers, its BVH (BVH::createBVH) and a camera, refits the BVH on the unmoved
- * triangles (must not change a byte), writes and reads back a scene cache file, writes a
- * PNG, and opens a core context. Without a CUDA device yc_create must fail cleanly with
+ * host producers, its BVH (BVH::createBVH), its device layout and a camera, refits the
+ * BVH on the unmoved triangles (must not change a byte), writes and reads back a scene
+ * cache file, writes a PNG, and opens a core context. Without a CUDA device yc_create must fail cleanly with
  * a negative code and a message; with one the context is created and destroyed.
  * Usage: consumer <scratch directory>. Prints "ok" and exits 0 when every check holds.
  */
@@ -72,6 +72,15 @@ int main(int argc, char** argv) {
   memcpy(refit, nodes, sizeof(yc_bvh_node) * (size_t)n_node);
   CHECK(yh_bvh_refit(tris, n_tri, refit, n_node) == YH_OK, "yh_bvh_refit");
   CHECK(memcmp(refit, nodes, sizeof(yc_bvh_node) * (size_t)n_node) == 0, "refit of unmoved triangles");
+
+  /* the device layout of the upload, computed on the host */
+  yc_scene_layout_info lay;
+  CHECK(yc_scene_layout(tris, n_tri, n_mat, nodes, n_node, 1, &lay) == YC_OK, "yc_scene_layout");
+  CHECK(lay.stream_bytes == 48u * (uint64_t)n_tri && lay.shade_bytes == 64u * (uint64_t)n_tri &&
+        lay.device_bytes > lay.node_bytes + lay.stream_bytes + lay.shade_bytes && lay.depth > 0,
+        "layout sizes");
+  CHECK(yc_scene_layout(tris, n_tri, 0, nodes, n_node, 1, &lay) == YC_E_INVALID && yc_last_error()[0],
+        "layout refuses triangles without materials");
 
   /* Camera::setBuffer */
   const float eye[3] = {0, 0, 1.4f}, side[3] = {1, 0, 0}, up[3] = {0, 1, 0}, look[3] = {0, 0, -1};
