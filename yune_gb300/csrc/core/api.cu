@@ -746,7 +746,7 @@ int yc_render_pass_noalloc(yc_ctx* c, int scene_id, int accum_id, uint32_t rand_
                            const yc_pass_cfg* cfg) {
   if (!c) return fail(YC_E_INVALID, "ctx is NULL");
   if (int r = validate_cfg(cfg)) return r;
-  if (cfg->integrator != YC_UDPT) return fail(YC_E_INVALID, "integrator not available in this build");
+  if (cfg->integrator != YC_UDPT) return fail(YC_E_INVALID, "yc_render_pass_noalloc renders with YC_UDPT only");
   Scene* sc = find_scene(c, scene_id);
   if (!sc) return fail(YC_E_NOTFOUND, "unknown scene");
   Accum* ac = find_accum(c, accum_id);
