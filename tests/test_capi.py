@@ -59,4 +59,9 @@ def test_host_producer_errors():
     t = np.zeros(1, TRIANGLE)
     assert L.yh_bvh_build(t.ctypes.data, 1, 20, 11, C.byref(h)) == -1   # leaf > 10
     assert L.yh_set_host_threads(-1) == -1 and L.yh_get_host_threads() >= 1
+    from yune_gb300 import scenes
+    try:
+        assert scenes.set_host_threads(3) == 3
+    finally:
+        assert scenes.set_host_threads(0) >= 1
     assert L.yh_scene_add_icosphere(None, None, 1.0, 2, 0.0, 0, 0) == -1

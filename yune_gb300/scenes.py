@@ -139,6 +139,14 @@ def build_bvh(tris, bins=20, leaf=10):
     return nodes, depth
 
 
+def set_host_threads(n):
+    """Limits the host threads of the BVH builder, the scene cache and the upload's repack
+    (yh_set_host_threads; 0 = every core). Their outputs do not depend on it. Returns the
+    count now in effect."""
+    N.check_host(N.lib().yh_set_host_threads(int(n)), "yh_set_host_threads")
+    return N.lib().yh_get_host_threads()
+
+
 def refit_bvh(tris, nodes):
     """A copy of `nodes` refitted to the (moved) triangles `tris` (yh_bvh_refit): the tree
     of the original build with every box recomputed bottom-up from the new positions."""
