@@ -113,3 +113,18 @@ def test_cancel_waiting_and_admitted(server):
     assert b.job == -1 and b.accum == -1
     assert a.accum in r.freed and c.accum in r.freed and srv.in_use == 0
     assert a.done < c.done
+
+
+def test_resident_scenes_checked_against_a_scene_budget(monkeypatch):
+    """The resident scenes' device bytes (yc_scene_layout, computed on the host) are
+    checked before any upload; over budget, the server refuses to start."""
+    monkeypatch.setattr(serve, "Batch", lambda renderer, **kw: FakeBatch(renderer, **kw))
+    resident = [scenes.c0(16, 16), scenes.c1(16, 16, level=3)]
+    need = sum(scenes.device_bytes(s) for s in resident)
+    assert need > 0
+    r = FakeRenderer()
+    with pytest.raises(ValueError, match="scene budget"):
+        serve.Server(r, resident, hbm_budget=1 << 20, scene_budget=need - 1)
+    assert next(r.ids) == 0                               # nothing was uploaded
+    srv = serve.Server(FakeRenderer(), resident, hbm_budget=1 << 20, scene_budget=need)
+    assert srv.scene_bytes == need

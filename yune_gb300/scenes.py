@@ -139,6 +139,16 @@ def build_bvh(tris, bins=20, leaf=10):
     return nodes, depth
 
 
+def device_bytes(s, tree_mode=1):
+    """Bytes scene `s` will hold on the device once uploaded in tree mode `tree_mode`
+    (yc_scene_layout: the upload's repack, run on the host without a device)."""
+    out = N.SceneLayout()
+    tris, nodes = np.ascontiguousarray(s.tris), np.ascontiguousarray(s.nodes)
+    N.check(N.lib().yc_scene_layout(ptr(tris), len(tris), len(s.mats), ptr(nodes), len(nodes), tree_mode,
+                                    C.byref(out)), "yc_scene_layout")
+    return int(out.device_bytes)
+
+
 def set_host_threads(n):
     """Limits the host threads of the BVH builder, the scene cache and the upload's repack
     (yh_set_host_threads; 0 = every core). Their outputs do not depend on it. Returns the

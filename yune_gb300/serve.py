@@ -55,9 +55,19 @@ class Request:
 
 class Server:
     def __init__(self, renderer, resident, hbm_budget, pool_paths=1 << 21, rounds_per_launch=8, keep_results=False,
-                 cfg=None, logic_blocks_per_sm=2, sort_threshold=1 << 16, max_queue=None):
+                 cfg=None, logic_blocks_per_sm=2, sort_threshold=1 << 16, max_queue=None, scene_budget=None):
+        """scene_budget: device bytes the resident scenes may take together (None: no
+        limit); checked on the host before anything is uploaded, as CLManager checks each
+        buffer against the device's global memory before creating it
+        (src/CLManager.cpp:428-429, 452-453)."""
         self.r = renderer
         self.scenes = resident
+        self.scene_bytes = None
+        if scene_budget is not None:
+            self.scene_bytes = sum(scenes.device_bytes(s) for s in resident)
+            if self.scene_bytes > scene_budget:
+                raise ValueError("resident scenes need %d device bytes, above the scene budget of %d"
+                                 % (self.scene_bytes, scene_budget))
         self.sids = [renderer.upload(s) for s in resident]
         self.budget = int(hbm_budget)
         self.in_use = 0
