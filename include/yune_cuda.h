@@ -33,9 +33,10 @@ enum {
   YC_E_INVALID = -1,        /* bad argument (CL_INVALID_VALUE and friends) */
   YC_E_NOMEM = -2,          /* device or host allocation failed (CL_OUT_OF_*_MEMORY) */
   YC_E_LAUNCH = -3,         /* kernel launch or CUDA runtime failure */
-  YC_E_TIMEOUT = -4,        /* a bounded device wait gave up */
+  YC_E_TIMEOUT = -4,        /* a pass still had live paths after YC_OPT_MAX_ROUNDS rounds */
   YC_E_NODEVICE = -5,       /* no CUDA device */
-  YC_E_OVERFLOW = -6,       /* a device bound (traversal stack, queue) was exceeded */
+  YC_E_OVERFLOW = -6,       /* a traversal reached its stack bound (YC_OPT_STACK_LIMIT, the
+                               batch's stack_cap): its hit is wrong, so the call fails */
   YC_E_BUDGET = -7,         /* admission refused: the request exceeds the HBM budget */
   YC_E_NOTFOUND = -8        /* unknown scene / accumulator / job id */
 };
@@ -187,10 +188,13 @@ int yc_render_passes(yc_ctx* ctx, int scene_id, int accum_id, const uint32_t* ra
  * renders one tile of at most 16384 pixels (cfg->block / block_x / block_y select it,
  * as for yc_render_pass) with no allocation. The scene and accumulator come from
  * yc_upload_scene / yc_alloc_accum, made beforehand. A larger tile is rejected with
- * YC_E_INVALID. The first call on a device looks up the array's device address; make
- * that first call before any stream capture. All calls share the array: calls whose
- * work overlaps on the GPU (two contexts on one device) race and must be serialised.
- * Results equal yc_render_pass with the same arguments. */
+ * YC_E_INVALID. Every call looks up the array's device address with
+ * cudaGetSymbolAddress on the current device before it launches anything (so a module
+ * reloaded after cudaDeviceReset is found again), and synchronises the context stream
+ * before it returns. All calls share the array, which keeps the last call's contents
+ * (the call clears what must start at zero): calls whose work overlaps on the GPU (two
+ * contexts on one device) race and must be serialised. Results equal yc_render_pass with
+ * the same arguments, with the same YC_E_TIMEOUT and YC_E_OVERFLOW rules. */
 int yc_render_pass_noalloc(yc_ctx* ctx, int scene_id, int accum_id, uint32_t rand_seed, int reset, int gi_check,
                            const yc_pass_cfg* cfg);
 
@@ -288,13 +292,26 @@ enum {
    * this many paths are sorted by path phase and material class before the shading
    * kernel, as the batch engine's sort_threshold does; 0 = never. Default 65536. Same
    * results either way. */
-  YC_OPT_SHADE_SORT_MIN = 6
+  YC_OPT_SHADE_SORT_MIN = 6,
+  /* Rounds (trace + shade) one pass may take before yc_render_pass(es) and
+   * yc_render_pass_noalloc give up with YC_E_TIMEOUT. Default 1,000,000 (the reference's
+   * GI loop bound is 100000 bounces, udpt.cl:463, at most three rays each). */
+  YC_OPT_MAX_ROUNDS = 7,
+  /* Traversal stack entries a walk may use in yc_render_pass(es) and
+   * yc_render_pass_noalloc; 0 (default) = as many as the scene's hierarchy needs (its
+   * depth + 2). A smaller bound shrinks the kernels' shared memory; a walk that reaches it
+   * fails the call with YC_E_OVERFLOW. Otherwise >= 3. */
+  YC_OPT_STACK_LIMIT = 8
 };
 int yc_set_option(yc_ctx* ctx, int option, int value);
 
 /* ---- statistics and tuning ---- */
 int yc_get_stats(yc_ctx* ctx, yc_stats* out);
 int yc_reset_stats(yc_ctx* ctx);
+/* Device allocations (cudaMalloc) the library's contexts and batches have made in this
+ * process so far. A caller that must not allocate while it renders can check that this
+ * count does not change across its calls (yc_render_pass_noalloc never allocates). */
+int yc_device_allocations(uint64_t* count);
 /* Wall time of the device work of the last yc_render_pass(es) call, in ms (CUDA
  * events on the context stream). */
 int yc_last_pass_ms(yc_ctx* ctx, float* ms);

@@ -87,6 +87,7 @@ SIGNATURES = {
     "yc_get_stats": (i32, [vp, C.POINTER(Stats)]),
     "yc_reset_stats": (i32, [vp]),
     "yc_last_pass_ms": (i32, [vp, C.POINTER(f32)]),
+    "yc_device_allocations": (i32, [C.POINTER(C.c_uint64)]),
     "yc_set_profiling": (i32, [vp, i32]),
     "yc_set_option": (i32, [vp, i32, i32]),
     "yc_get_kernel_times": (i32, [vp, C.POINTER(KernelTimes)]),
@@ -149,6 +150,19 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+# status codes of the core (include/yune_cuda.h)
+YC_E_INVALID, YC_E_NOMEM, YC_E_LAUNCH, YC_E_TIMEOUT, YC_E_NODEVICE, YC_E_OVERFLOW, YC_E_BUDGET, YC_E_NOTFOUND = \
+    -1, -2, -3, -4, -5, -6, -7, -8
+
+
+def device_allocations():
+    """Device allocations the library's contexts and batches have made in this process
+    (yc_device_allocations)."""
+    n = C.c_uint64()
+    check(lib().yc_device_allocations(C.byref(n)), "yc_device_allocations")
+    return int(n.value)
 
 
 # status codes of the host producers (include/yune_host.h)

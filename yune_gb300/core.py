@@ -48,6 +48,7 @@ class Renderer:
         self.h = h
         self._accum_shape = {}
         self._children = weakref.WeakSet()   # batches: the context releases them
+        self.tree_mode = 1                   # YC_OPT_TREE of later uploads
 
     def close(self):
         if getattr(self, "h", None):
@@ -166,8 +167,19 @@ class Renderer:
         return ms.value
 
     def set_tree_mode(self, mode):
-        """0: reference node tree; 1: SAH hierarchy over the reference leaves (default)."""
+        """0: reference node tree; 1: SAH hierarchy over the reference leaves (default);
+        2: the same hierarchy with four-child nodes. Applies to later uploads."""
         N.check(self.L.yc_set_option(self.h, 1, int(mode)), "yc_set_option")
+        self.tree_mode = int(mode)
+
+    def set_max_rounds(self, n):
+        """Rounds one pass may take before the call fails with YC_E_TIMEOUT (default 1,000,000)."""
+        N.check(self.L.yc_set_option(self.h, 7, int(n)), "yc_set_option")
+
+    def set_stack_limit(self, n):
+        """Traversal stack entries a walk may use (0: what the scene needs); a walk that
+        reaches the limit fails the call with YC_E_OVERFLOW."""
+        N.check(self.L.yc_set_option(self.h, 8, int(n)), "yc_set_option")
 
     def set_tail_paths(self, n):
         """Paths left at which a pass finishes in the tail kernel (-1 auto, 0 off)."""

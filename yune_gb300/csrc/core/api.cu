@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -21,6 +22,9 @@
 namespace {
 
 thread_local std::string g_last_error;
+
+// device allocations (cudaMalloc) made by the context and batch buffers of this process
+std::atomic<unsigned long long> g_device_allocs{0};
 
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -52,6 +56,7 @@ struct DevBuf {
     release();
     if (count == 0) return cudaSuccess;
     cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    g_device_allocs.fetch_add(1, std::memory_order_relaxed);
     if (e == cudaSuccess) n = count;
     else p = nullptr;
     return e;
@@ -117,6 +122,9 @@ struct yc_ctx {
   DevBuf<yc::RoundCounters> rc;      // two round-counter blocks
   DevBuf<yc::DevStats> stats;
   yc::RoundCounters* rc_host = nullptr;   // pinned
+  unsigned long long* overflow_host = nullptr;   // pinned: DevStats::call_overflow read back
+  int max_rounds = 1000000;   // YC_OPT_MAX_ROUNDS: rounds one pass may take
+  int stack_limit = 0;        // YC_OPT_STACK_LIMIT: traversal stack entries allowed (0 = any)
   int logic_grid = 0;
   int sm_count = 0;
   float last_ms = 0.0f;
@@ -254,27 +262,24 @@ int validate_cfg(const yc_pass_cfg* cfg) {
   return 0;
 }
 
-// Runs one pass (all rounds) on the context stream; the host polls the queue sizes
-// every few rounds.
-int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int gi_check, const yc_pass_cfg* cfg) {
-  const bool bdpt = cfg->integrator != YC_UDPT;
-  const bool bdpt_mis = cfg->integrator == YC_BDPT_MIS;
-  if (bdpt && (cfg->bdpt_bounces < 2 || cfg->bdpt_bounces > 32)) return fail(YC_E_INVALID, "bdpt_bounces must be 2..32");
-  if (bdpt_mis && cfg->bdpt_bounces < 3) return fail(YC_E_INVALID, "bdpt_bounces must be 3..32 with YC_BDPT_MIS");
-  const int W = ac->w, H = ac->h;
-  int rc_ = ensure_paths(c, (size_t)W * H);
-  if (rc_) return rc_;
+// The kernel arguments of one pass (`pathtracer`, udpt.cl:158-160): scene, camera,
+// accumulator, the tile of cfg->block (udpt.cl:166-167, src/RendererCore.cpp:146-150) and
+// the options the reference bakes into its kernel text. yc_render_pass and
+// yc_render_pass_noalloc both build their passes here. The scene's traversal depth is
+// capped by YC_OPT_STACK_LIMIT (a deeper walk then overflows and the call fails).
+yc::PassParams pass_params(const yc_ctx* c, const Scene* sc, const Accum* ac, uint32_t rand_seed, int reset,
+                           int gi_check, const yc_pass_cfg* cfg) {
   yc::PassParams pp{};
   pp.sc = sc->dev;
+  if (c->stack_limit > 0) pp.sc.depth = std::min(pp.sc.depth, c->stack_limit - 2);
   pp.cam = c->cam;
   pp.accum = ac->buf.p;
-  pp.width = W;
-  pp.height = H;
-  // tile of this launch (udpt.cl:166-167, src/RendererCore.cpp:146-150)
-  pp.tile_w = (int)std::ceil((float)W / cfg->block_x);
-  pp.tile_h = (int)std::ceil((float)H / cfg->block_y);
-  pp.off_x = (int)(std::ceil((float)W / cfg->block_x) * (float)(cfg->block % cfg->block_x));
-  pp.off_y = (int)(std::ceil((float)H / cfg->block_y) * (float)(cfg->block / cfg->block_x));
+  pp.width = ac->w;
+  pp.height = ac->h;
+  pp.tile_w = (int)std::ceil((float)ac->w / cfg->block_x);
+  pp.tile_h = (int)std::ceil((float)ac->h / cfg->block_y);
+  pp.off_x = (int)(std::ceil((float)ac->w / cfg->block_x) * (float)(cfg->block % cfg->block_x));
+  pp.off_y = (int)(std::ceil((float)ac->h / cfg->block_y) * (float)(cfg->block / cfg->block_x));
   pp.rand_seed = rand_seed;
   pp.reset = reset;
   pp.gi_check = gi_check;
@@ -283,6 +288,42 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
   pp.max_depth = cfg->max_depth;
   pp.brdf_model = cfg->brdf_model;
   pp.mis_lobe_fix = cfg->mis_lobe_fix;
+  return pp;
+}
+
+// Per-call error state: the call's stack-overflow count is cleared when a render call
+// starts and read back when it ends (the reference surfaces every failure of a pass as an
+// error, src/CLManager.cpp:755-855; a walk that overflowed its stack gave a wrong hit).
+int begin_call_checks(yc_ctx* c) {
+  YC_CUDA(cudaMemsetAsync(&c->stats.p->call_overflow, 0, sizeof(unsigned long long), c->stream));
+  return 0;
+}
+int queue_call_checks(yc_ctx* c) {
+  YC_CUDA(cudaMemcpyAsync(c->overflow_host, &c->stats.p->call_overflow, sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost, c->stream));
+  return 0;
+}
+// after the stream has been synchronised
+int end_call_checks(yc_ctx* c) {
+  if (*c->overflow_host)
+    return fail(YC_E_OVERFLOW, std::to_string(*c->overflow_host) +
+                                   " traversals reached the stack bound (their hits are wrong); the scene's hierarchy "
+                                   "is deeper than YC_OPT_STACK_LIMIT or the batch's stack_cap allows");
+  return 0;
+}
+
+// Runs one pass (all rounds) on the context stream; the host polls the queue sizes
+// every few rounds. YC_E_TIMEOUT when paths are still live after YC_OPT_MAX_ROUNDS rounds.
+int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int gi_check, const yc_pass_cfg* cfg) {
+  const bool bdpt = cfg->integrator != YC_UDPT;
+  const bool bdpt_mis = cfg->integrator == YC_BDPT_MIS;
+  if (bdpt && (cfg->bdpt_bounces < 2 || cfg->bdpt_bounces > 32)) return fail(YC_E_INVALID, "bdpt_bounces must be 2..32");
+  if (bdpt_mis && cfg->bdpt_bounces < 3) return fail(YC_E_INVALID, "bdpt_bounces must be 3..32 with YC_BDPT_MIS");
+  const int W = ac->w, H = ac->h;
+  int rc_ = ensure_paths(c, (size_t)W * H);
+  if (rc_) return rc_;
+  const yc::PassParams pp = pass_params(c, sc, ac, rand_seed, reset, gi_check, cfg);
+  const yc::DevScene& dsc = pp.sc;   // the scene as the kernels walk it (stack limit applied)
   const yc::PathState ps = path_state(c);
   yc::BdptBuffers bb{};
   if (bdpt) {
@@ -313,7 +354,7 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
   // (a walk through a scene of a few thousand triangles is a handful of boxes: sorting
   // its rays costs more than it saves)
   const bool raysort = mixed && (c->rs_ob + c->rs_db) > 0 && c->rs_threshold > 0 &&
-                       (size_t)W * H >= (size_t)c->rs_threshold && sc->dev.n_tri >= kRaySortMinTris;
+                       (size_t)W * H >= (size_t)c->rs_threshold && dsc.n_tri >= kRaySortMinTris;
   yc::RaySortBufs rsb{};
   if (raysort) {
     if (int e = ensure_raysort(c, (size_t)W * H)) return e;
@@ -336,19 +377,20 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
                                                     : std::max((size_t)c->ss_threshold, kShadeSortMinPixels));
   if (shadesort)
     if (int e = ensure_shadesort(c, (size_t)W * H)) return e;
-  const int grid_c = yc::trace_grid_blocks(false, sc->dev.depth, sc->dev.wide != 0);
-  const int grid_a = yc::trace_grid_blocks(true, sc->dev.depth, sc->dev.wide != 0);
-  const int grid_m = mixed ? yc::trace_mixed_grid_blocks(sc->dev.depth, sc->dev.wide != 0) : 1;
+  const int grid_c = yc::trace_grid_blocks(false, dsc.depth, dsc.wide != 0);
+  const int grid_a = yc::trace_grid_blocks(true, dsc.depth, dsc.wide != 0);
+  const int grid_m = mixed ? yc::trace_mixed_grid_blocks(dsc.depth, dsc.wide != 0) : 1;
   if (grid_c <= 0 || grid_a <= 0 || grid_m <= 0)
     return fail(YC_E_LAUNCH, "trace kernel cannot be resident (stack too deep)");
   int tail_grid = 0, tail_at = 0;
   if (!bdpt && c->tail_paths != 0) {
-    const int capacity = yc::tail_capacity(sc->dev, &tail_grid);
+    const int capacity = yc::tail_capacity(dsc, &tail_grid);
     tail_at = c->tail_paths < 0 ? capacity : std::min(c->tail_paths, capacity);
   }
   int cur = 0;
   const int check_every = 6;
-  for (int round = 0; round < 1000000; ++round) {
+  bool finished = false;
+  for (int round = 0; round < c->max_rounds; ++round) {
     int* in_c = c->q[2 * cur].p;
     int* in_a = c->q[2 * cur + 1].p;
     int* out_c = c->q[2 * (1 - cur)].p;
@@ -359,11 +401,11 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     if (mixed) {   // both ray kinds of the round in one launch
       if (raysort) {
         KTimer kt(c, K_RAYSORT);
-        if (yc::launch_raysort(sc->dev, in_c, in_a, rin, ps.ro, ps.rd, rsb, c->logic_grid, c->stream))
+        if (yc::launch_raysort(dsc, in_c, in_a, rin, ps.ro, ps.rd, rsb, c->logic_grid, c->stream))
           return fail(YC_E_LAUNCH, std::string("ray sort: ") + cudaGetErrorString(cudaGetLastError()));
       }
       KTimer kt(c, K_TRACE);
-      if (yc::launch_trace_mixed(sc->dev, in_c, in_a, rin, ps.ro, ps.rd, ps.hit, c->stats.p, grid_m, c->stream,
+      if (yc::launch_trace_mixed(dsc, in_c, in_a, rin, ps.ro, ps.rd, ps.hit, c->stats.p, grid_m, c->stream,
                                  raysort ? rsb.sorted : nullptr, raysort ? rsb.ctl : nullptr))
         return fail(YC_E_LAUNCH, std::string("trace kernel: ") + cudaGetErrorString(cudaGetLastError()));
     }
@@ -379,13 +421,13 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     if (!mixed) {
       {
         KTimer kt(c, K_EXTEND);
-        e1 = yc::launch_trace(sc->dev, false, in_c, &rin->n_closest, &rin->work_closest, ps.ro, ps.rd, ps.hit,
+        e1 = yc::launch_trace(dsc, false, in_c, &rin->n_closest, &rin->work_closest, ps.ro, ps.rd, ps.hit,
                               c->stats.p, grid_c, c->stream);
       }
       if (e1) return fail(YC_E_LAUNCH, std::string("extend kernel: ") + cudaGetErrorString(cudaGetLastError()));
       {
         KTimer kt(c, K_OCCL);
-        e2 = yc::launch_trace(sc->dev, true, in_a, &rin->n_any, &rin->work_any, ps.ro, ps.rd, ps.hit, c->stats.p,
+        e2 = yc::launch_trace(dsc, true, in_a, &rin->n_any, &rin->work_any, ps.ro, ps.rd, ps.hit, c->stats.p,
                               grid_a, s_any);
       }
       if (e2) return fail(YC_E_LAUNCH, std::string("occlusion kernel: ") + cudaGetErrorString(cudaGetLastError()));
@@ -398,7 +440,7 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     if (shadesort) {
       KTimer kt(c, K_SORT);
       YC_CUDA(cudaMemsetAsync(c->ss_ctl.p, 0, sizeof(yc::SortCtl), c->stream));
-      yc::launch_pass_sort(sc->dev, bdpt, ps, in_c, in_a, rin, c->ss_keys.p, c->ss_sorted.p, c->ss_ctl.p,
+      yc::launch_pass_sort(dsc, bdpt, ps, in_c, in_a, rin, c->ss_keys.p, c->ss_sorted.p, c->ss_ctl.p,
                            c->ss_threshold, c->logic_grid, c->stream);
     }
     {
@@ -422,12 +464,16 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     YC_CUDA(cudaPeekAtLastError());
     c->ktimes.rounds++;
     cur = 1 - cur;
-    if ((round + 1) % check_every == 0) {
+    if ((round + 1) % check_every == 0 || round + 1 == c->max_rounds) {
       YC_CUDA(cudaMemcpyAsync(c->rc_host, rc + cur, sizeof(yc::RoundCounters), cudaMemcpyDeviceToHost, c->stream));
       YC_CUDA(cudaStreamSynchronize(c->stream));
-      if (c->rc_host->n_closest == 0 && c->rc_host->n_any == 0) break;
+      if (c->rc_host->n_closest == 0 && c->rc_host->n_any == 0) { finished = true; break; }
     }
   }
+  if (!finished)
+    return fail(YC_E_TIMEOUT, "pass not finished after " + std::to_string(c->max_rounds) + " rounds (" +
+                                  std::to_string(c->rc_host->n_closest + c->rc_host->n_any) +
+                                  " rays still queued; YC_OPT_MAX_ROUNDS)");
   return 0;
 }
 
@@ -456,6 +502,7 @@ int yc_create(int device, yc_ctx** out) {
   if (e == cudaSuccess) e = c->rc.alloc(2);
   if (e == cudaSuccess) e = c->stats.alloc(1);
   if (e == cudaSuccess) e = cudaMallocHost(&c->rc_host, sizeof(yc::RoundCounters));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->overflow_host, sizeof(unsigned long long));
   if (e == cudaSuccess) e = c->q_work.alloc(1);
   if (e == cudaSuccess) e = cudaMemset(c->stats.p, 0, sizeof(yc::DevStats));
   if (e != cudaSuccess) {
@@ -479,6 +526,7 @@ int yc_destroy(yc_ctx* c) {
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   c->ev_pool.clear();
   if (c->rc_host) cudaFreeHost(c->rc_host);
+  if (c->overflow_host) cudaFreeHost(c->overflow_host);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
@@ -725,16 +773,18 @@ int yc_render_passes(yc_ctx* c, int scene_id, int accum_id, const uint32_t* rand
   if (!a) return fail(YC_E_NOTFOUND, "unknown accumulator");
   if (!c->have_cam) return fail(YC_E_INVALID, "no camera set");
   YC_CUDA(cudaSetDevice(c->device));
+  if (int r = begin_call_checks(c)) return r;
   YC_CUDA(cudaEventRecord(c->ev0, c->stream));
   for (int k = 0; k < n_pass; ++k) {
     const int r = run_pass(c, s, a, rands[k], (k == 0) ? reset_first : 0, gi_check, cfg);
     if (r) return r;
   }
+  if (int r = queue_call_checks(c)) return r;
   YC_CUDA(cudaEventRecord(c->ev1, c->stream));
   YC_CUDA(cudaEventSynchronize(c->ev1));
   YC_CUDA(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
   collect_events(c);
-  return YC_OK;
+  return end_call_checks(c);
 }
 
 int yc_render_pass(yc_ctx* c, int scene_id, int accum_id, uint32_t rand_seed, int reset, int gi_check,
@@ -754,35 +804,22 @@ int yc_render_pass_noalloc(yc_ctx* c, int scene_id, int accum_id, uint32_t rand_
   if (!c->have_cam) return fail(YC_E_INVALID, "no camera set");
   YC_CUDA(cudaSetDevice(c->device));
   yc::NoallocPass a{};
-  yc::PassParams& pp = a.pp;
-  const int W = ac->w, H = ac->h;
-  pp.sc = sc->dev;
-  pp.cam = c->cam;
-  pp.accum = ac->buf.p;
-  pp.width = W;
-  pp.height = H;
-  pp.tile_w = (int)std::ceil((float)W / cfg->block_x);
-  pp.tile_h = (int)std::ceil((float)H / cfg->block_y);
-  pp.off_x = (int)(std::ceil((float)W / cfg->block_x) * (float)(cfg->block % cfg->block_x));
-  pp.off_y = (int)(std::ceil((float)H / cfg->block_y) * (float)(cfg->block / cfg->block_x));
-  pp.rand_seed = rand_seed;
-  pp.reset = reset;
-  pp.gi_check = gi_check;
-  pp.mis = cfg->mis;
-  pp.rr_threshold = cfg->rr_threshold;
-  pp.max_depth = cfg->max_depth;
-  pp.brdf_model = cfg->brdf_model;
-  pp.mis_lobe_fix = cfg->mis_lobe_fix;
-  a.device = c->device;
+  a.pp = pass_params(c, sc, ac, rand_seed, reset, gi_check, cfg);
   a.stream = c->stream;
   a.stats = c->stats.p;
   a.rc_host = c->rc_host;
   a.logic_grid = c->logic_grid;
+  a.max_rounds = c->max_rounds;
+  if (int r = begin_call_checks(c)) return r;
   std::string err;
   const int r = yc::noalloc_render(a, err);
-  if (r) return fail(r, err);
+  if (r) {
+    cudaStreamSynchronize(c->stream);
+    return fail(r, err);
+  }
+  if (int q = queue_call_checks(c)) return q;
   YC_CUDA(cudaStreamSynchronize(c->stream));
-  return YC_OK;
+  return end_call_checks(c);
 }
 
 int yc_tonemap(yc_ctx* c, int accum_id, float* out) {
@@ -902,6 +939,14 @@ int yc_set_option(yc_ctx* c, int option, int value) {
       if (value < 0) return fail(YC_E_INVALID, "shade sort threshold must be >= 0");
       c->ss_threshold = value;
       return YC_OK;
+    case YC_OPT_MAX_ROUNDS:
+      if (value < 1) return fail(YC_E_INVALID, "max rounds must be >= 1");
+      c->max_rounds = value;
+      return YC_OK;
+    case YC_OPT_STACK_LIMIT:
+      if (value != 0 && value < 3) return fail(YC_E_INVALID, "stack limit is 0 (none) or >= 3 entries");
+      c->stack_limit = value;
+      return YC_OK;
     default:
       return fail(YC_E_INVALID, "unknown option");
   }
@@ -931,6 +976,12 @@ int yc_flush_l2(yc_ctx* c, size_t bytes) {
 int yc_measure_l2_gbs(yc_ctx* c, size_t bytes, int iters, double* gbs) {
   if (!c || !gbs || bytes < 4096 || iters < 1) return fail(YC_E_INVALID, "bad argument");
   if (yc::l2_read_gbs(bytes, iters, c->stream, gbs)) return fail(YC_E_LAUNCH, "L2 probe failed");
+  return YC_OK;
+}
+
+int yc_device_allocations(uint64_t* count) {
+  if (!count) return fail(YC_E_INVALID, "NULL argument");
+  *count = g_device_allocs.load(std::memory_order_relaxed);
   return YC_OK;
 }
 
@@ -1290,6 +1341,7 @@ int yc_batch_run(yc_batch* b, int max_launches, int* unfinished) {
       return fail(YC_E_LAUNCH, "batch trace kernel cannot be resident");
     b->started = true;
   }
+  if (int r = begin_call_checks(c)) return r;
   YC_CUDA(cudaEventRecord(c->ev0, c->stream));
   int launches = 0;
   for (;;) {
@@ -1303,7 +1355,9 @@ int yc_batch_run(yc_batch* b, int max_launches, int* unfinished) {
     }
     YC_CUDA(cudaMemcpyAsync(b->done_host, b->job_done.p, b->host_jobs.size() * sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, c->stream));
+    if (int r = queue_call_checks(c)) return r;
     YC_CUDA(cudaStreamSynchronize(c->stream));
+    if (int r = end_call_checks(c)) return r;
     collect_events(c);
     int left = 0;
     for (size_t i = 0; i < b->host_jobs.size(); ++i)

@@ -16,8 +16,6 @@
 // streams) race on the array and must be serialised by the caller.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "yc_internal.h"
 #include "yc_noalloc.h"
 #include "yc_shade.cuh"
@@ -32,22 +30,15 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
 namespace {
 
-constexpr int MAX_DEVICES = 64;
-std::mutex g_addr_mu;
-unsigned char* g_addr[MAX_DEVICES] = {};
-
 // Device address of the scratch array on the current device. In host code the array's
-// name is only a host-side stand-in, so the address comes from cudaGetSymbolAddress,
-// once per device (with that device current).
-int scratch_address(int device, unsigned char** out) {
-  if (device < 0 || device >= MAX_DEVICES) return -1;
-  std::lock_guard<std::mutex> lock(g_addr_mu);
-  if (!g_addr[device]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return -1;
-    g_addr[device] = static_cast<unsigned char*>(p);
-  }
-  *out = g_addr[device];
+// name is only a host-side stand-in, so the address comes from cudaGetSymbolAddress. It
+// is looked up on every call (a call already synchronises its stream, and the lookup is
+// a table read): after a cudaDeviceReset or a new primary context the module is loaded
+// again and the array may have moved, so no address is kept from an earlier call.
+int scratch_address(unsigned char** out) {
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return -1;
+  *out = static_cast<unsigned char*>(p);
   return 0;
 }
 
@@ -118,7 +109,7 @@ int noalloc_render(const NoallocPass& a, std::string& err) {
     return YC_E_INVALID;
   }
   unsigned char* base = nullptr;
-  if (scratch_address(a.device, &base)) {
+  if (scratch_address(&base)) {
     err = "cudaGetSymbolAddress failed for the render scratch";
     return YC_E_LAUNCH;
   }
@@ -130,11 +121,19 @@ int noalloc_render(const NoallocPass& a, std::string& err) {
   int* qs[4] = {q, q + N, q + 2 * N, q + 3 * N};
   RoundCounters* rc = reinterpret_cast<RoundCounters*>(q + 4 * N);
   cudaStream_t s = a.stream;
+  auto launch_failed = [&](const char* what) {
+    const cudaError_t e = cudaPeekAtLastError();
+    if (e == cudaSuccess) return false;
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return true;
+  };
+  // the counters keep the previous call's values: clear both blocks first
   if (cudaMemsetAsync(rc, 0, 2 * sizeof(RoundCounters), s) != cudaSuccess) {
     err = "clearing the round counters failed";
     return YC_E_LAUNCH;
   }
   k_raygen_tile<<<(n_paths + 255) / 256, 256, 0, s>>>(a.pp, ps, qs[0], rc, a.stats);
+  if (launch_failed("ray generation")) return YC_E_LAUNCH;
   const int grid_c = trace_grid_blocks(false, a.pp.sc.depth, a.pp.sc.wide != 0);
   const int grid_a = trace_grid_blocks(true, a.pp.sc.depth, a.pp.sc.wide != 0);
   if (grid_c <= 0 || grid_a <= 0) {
@@ -142,22 +141,39 @@ int noalloc_render(const NoallocPass& a, std::string& err) {
     return YC_E_LAUNCH;
   }
   int cur = 0;
-  for (int round = 0; round < 1000000; ++round) {
+  bool finished = false;
+  for (int round = 0; round < a.max_rounds; ++round) {
     RoundCounters* rin = rc + cur;
     RoundCounters* rout = rc + (1 - cur);
-    launch_trace(a.pp.sc, false, qs[2 * cur], &rin->n_closest, &rin->work_closest, ps.ro, ps.rd, ps.hit, a.stats,
-                 grid_c, s);
-    launch_trace(a.pp.sc, true, qs[2 * cur + 1], &rin->n_any, &rin->work_any, ps.ro, ps.rd, ps.hit, a.stats, grid_a,
-                 s);
-    cudaMemsetAsync(rout, 0, sizeof(RoundCounters), s);
+    if (launch_trace(a.pp.sc, false, qs[2 * cur], &rin->n_closest, &rin->work_closest, ps.ro, ps.rd, ps.hit, a.stats,
+                     grid_c, s) ||
+        launch_trace(a.pp.sc, true, qs[2 * cur + 1], &rin->n_any, &rin->work_any, ps.ro, ps.rd, ps.hit, a.stats,
+                     grid_a, s)) {
+      launch_failed("trace kernel");
+      if (err.empty()) err = "trace kernel launch failed";
+      return YC_E_LAUNCH;
+    }
+    if (cudaMemsetAsync(rout, 0, sizeof(RoundCounters), s) != cudaSuccess) {
+      err = "clearing the round counters failed";
+      return YC_E_LAUNCH;
+    }
     launch_logic(a.pp, ps, qs[2 * cur], qs[2 * cur + 1], rin, qs[2 * (1 - cur)], qs[2 * (1 - cur) + 1], rout,
                  a.stats, a.logic_grid, s);
+    if (launch_failed("shading kernel")) return YC_E_LAUNCH;
     cur = 1 - cur;
-    if ((round + 1) % 6 == 0) {
-      cudaMemcpyAsync(a.rc_host, rc + cur, sizeof(RoundCounters), cudaMemcpyDeviceToHost, s);
-      if (cudaStreamSynchronize(s) != cudaSuccess) break;
-      if (a.rc_host->n_closest == 0 && a.rc_host->n_any == 0) break;
+    if ((round + 1) % 6 == 0 || round + 1 == a.max_rounds) {
+      if (cudaMemcpyAsync(a.rc_host, rc + cur, sizeof(RoundCounters), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaStreamSynchronize(s) != cudaSuccess) {
+        launch_failed("render pass");
+        if (err.empty()) err = "render pass failed";
+        return YC_E_LAUNCH;
+      }
+      if (a.rc_host->n_closest == 0 && a.rc_host->n_any == 0) { finished = true; break; }
     }
+  }
+  if (!finished) {
+    err = "pass not finished after " + std::to_string(a.max_rounds) + " rounds (YC_OPT_MAX_ROUNDS)";
+    return YC_E_TIMEOUT;
   }
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {

@@ -89,6 +89,7 @@ __global__ void __launch_bounds__(TAIL_TB) k_tail(PassParams pp, PathState ps, c
                                    &st->any_tris, &st->stack_overflow};
     for (int q = 0; q < 13; ++q)
       if (s_cnt[q]) atomicAdd(dst[q], s_cnt[q]);
+    if (s_cnt[12]) atomicAdd(&st->call_overflow, s_cnt[12]);
     // the last block to finish empties the queues (every block has read the counts)
     __threadfence();
     s_last = atomicAdd(&rc_in->pad[0], 1) == (int)gridDim.x - 1;

@@ -112,10 +112,13 @@ struct SortCtl {
   int cursor[SORT_KEYS];    // scatter cursors (exclusive prefix of count)
 };
 
-// device-wide statistics (yc_stats layout, 64-bit counters)
+// device-wide statistics (yc_stats layout, 64-bit counters); call_overflow counts the
+// stack overflows of the current API call only (cleared when a call starts, read when it
+// ends, so the call can return YC_E_OVERFLOW)
 struct DevStats {
   unsigned long long rays, primary, extension, shadow, mis, connection, traversed, samples, stack_overflow;
   unsigned long long ext_rays, ext_boxes, ext_tris, any_rays, any_boxes, any_tris;
+  unsigned long long call_overflow;
 };
 
 struct PassParams {

@@ -31,7 +31,10 @@ __device__ __forceinline__ void flush_counts(DevStats* st, unsigned rays, const 
       if (nn) atomicAdd(&st->ext_boxes, nn);
       if (tt) atomicAdd(&st->ext_tris, tt);
     }
-    if (overflow) atomicAdd(&st->stack_overflow, overflow);
+    if (overflow) {
+      atomicAdd(&st->stack_overflow, overflow);
+      atomicAdd(&st->call_overflow, overflow);
+    }
   }
 }
 

@@ -64,7 +64,8 @@ class Server:
         self.scenes = resident
         self.scene_bytes = None
         if scene_budget is not None:
-            self.scene_bytes = sum(scenes.device_bytes(s) for s in resident)
+            mode = getattr(renderer, "tree_mode", 1)   # the layout the uploads below will build
+            self.scene_bytes = sum(scenes.device_bytes(s, tree_mode=mode) for s in resident)
             if self.scene_bytes > scene_budget:
                 raise ValueError("resident scenes need %d device bytes, above the scene budget of %d"
                                  % (self.scene_bytes, scene_budget))
