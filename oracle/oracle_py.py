@@ -86,6 +86,55 @@ def ref():
     return _ref
 
 
+_scene_lib = None
+
+
+def scene_lib():
+    """The oracle library's copy of the procedural scene producers (yh_scene_* and
+    yh_camera_look, the same sources as the product's), with argtypes set: the CPU
+    baseline generates its inputs with it, so it never loads the product library."""
+    global _scene_lib
+    if _scene_lib is None:
+        L = orc()
+        f = C.c_float
+        sig = {"yh_scene_new": (i32, [C.POINTER(vp)]), "yh_scene_free": (None, [vp]),
+               "yh_scene_add_material": (i32, [vp, vp, C.POINTER(i32)]),
+               "yh_scene_add_cornell": (i32, [vp, C.c_uint64, f, f, f, i32]),
+               "yh_scene_add_icosphere": (i32, [vp, vp, f, i32, f, C.c_uint64, i32]),
+               "yh_scene_add_light": (i32, [vp, vp]),
+               "yh_scene_counts": (i32, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
+               "yh_scene_copy": (i32, [vp, vp, vp, vp]),
+               "yh_scene_load_obj": (i32, [vp, C.c_char_p, C.POINTER(i32)]),
+               "yh_camera_look": (i32, [vp, vp, vp, vp, f, vp])}
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _scene_lib = L
+    return _scene_lib
+
+
+def node_depth(nodes):
+    """Longest root-to-leaf path (edges) of a reference node array (children of an
+    interior node at child_idx and child_idx + 1)."""
+    n = len(nodes)
+    if n == 0:
+        return 0
+    child = nodes["child_idx"].astype(np.int64)
+    depth = np.zeros(n, np.int64)
+    for i in range(n):   # breadth-first order: a parent precedes its children
+        c = child[i]
+        if c > 0 and c + 1 < n:
+            depth[c] = depth[c + 1] = depth[i] + 1
+    return int(depth.max())
+
+
+def ref_bvh_with_depth(tris, bins=20, leaf=10):
+    """BVH::createBVH of the compiled reference (src/BVH.cpp), and the tree depth."""
+    nodes = ref_bvh(tris, bins, leaf)
+    return nodes, node_depth(nodes)
+
+
 def cfg_of(cfg, heap_size=1500):
     c = OrCfg()
     c.mis = int(cfg.get("mis", 0))
@@ -191,7 +240,7 @@ def tonemap(accum):
 
 
 # ---- the compiled reference ----
-VARIANT = {"udpt_a": 0, "udpt_mis": 1, "udpt_mis4": 2, "bdpt20": 10, "bdpt8": 11, "bdpt8_l4": 12}
+VARIANT = {"udpt_a": 0, "udpt_mis": 1, "udpt_mis4": 2, "udpt_mis_on": 3, "bdpt20": 10, "bdpt8": 11, "bdpt8_l4": 12}
 
 
 def ref_render(scene, accum, rand_seed, reset, variant, rr_threshold, max_depth, gi_check=1, threads=0, rows=None):

@@ -8,6 +8,8 @@
 //   udpt_a      udpt.cl as shipped (no MIS, RR_THRESHOLD 6, LIGHT_SIZE 1)
 //   udpt_mis    udpt.cl with -DMIS
 //   udpt_mis4   udpt.cl with -DMIS and LIGHT_SIZE 4
+//   udpt_mis_on udpt.cl with -DMIS and the Oren-Nayar diffuse rule of udpt-primitives.cl
+//               (udpt_on.inc, transform.graft_oren_nayar): the configurations' variant B
 //   bdpt8/20    bdpt.cl with BDPT_BOUNCES 8 / 20 (shipped: 20), LIGHT_SIZE 1
 //   bdpt8_l4    bdpt.cl with BDPT_BOUNCES 8 and LIGHT_SIZE 4
 // RR_THRESHOLD (udpt.cl) and the GI-loop bound are read at run time.
@@ -60,6 +62,18 @@ constexpr int kLights = LIGHT_SIZE;
 #undef INV_PI
 #undef EPSILON
 }  // namespace udpt_mis4
+
+namespace udpt_mis_on {
+#define MIS
+#define RR_THRESHOLD (yref_rr_threshold)
+#include "udpt_on.inc"
+constexpr int kLights = LIGHT_SIZE;
+#undef RR_THRESHOLD
+#undef MIS
+#undef PI
+#undef INV_PI
+#undef EPSILON
+}  // namespace udpt_mis_on
 
 namespace bdpt20 {
 #include "bdpt.inc"
@@ -182,7 +196,7 @@ static_assert(sizeof(yref::udpt_a::Camera) == sizeof(yc_cam), "Camera");
 extern "C" {
 
 // One pass of the reference `pathtracer` kernel over rows [row0, row1) of a W x H
-// RGBA32F accumulator, updated in place (row1 <= row0: the whole image). variant: 0 udpt_a, 1 udpt_mis, 2 udpt_mis4, 10 bdpt20, 11 bdpt8,
+// RGBA32F accumulator, updated in place (row1 <= row0: the whole image). variant: 0 udpt_a, 1 udpt_mis, 2 udpt_mis4, 3 udpt_mis_on, 10 bdpt20, 11 bdpt8,
 // 12 bdpt8_l4.
 int ref_render(int variant, const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_bvh_node* b,
                int nb, const yc_quad_light* l, int nl, const yc_cam* cam, int W, int H, float* accum,
@@ -207,6 +221,7 @@ int ref_render(int variant, const yc_triangle* t, int nt, const yc_material* m, 
     case 0: YREF_RENDER(udpt_a, set_normal_udpt); break;
     case 1: YREF_RENDER(udpt_mis, set_normal_udpt); break;
     case 2: YREF_RENDER(udpt_mis4, set_normal_udpt); break;
+    case 3: YREF_RENDER(udpt_mis_on, set_normal_udpt); break;
     case 10: YREF_RENDER(bdpt20, set_normal_bdpt); break;
     case 11: YREF_RENDER(bdpt8, set_normal_bdpt); break;
     case 12: YREF_RENDER(bdpt8_l4, set_normal_bdpt); break;

@@ -19,6 +19,12 @@ reference tree:
                        of obj_files.py: triangles, materials and the BVH node array
   obj_cornellbox.npz   the same on the reference's geometry/cornellbox.obj (the test
                        that uses it needs that file and skips without it)
+  render_variant_b.npz passes of udpt.cl -DMIS with the Oren-Nayar diffuse rule of
+                       udpt-primitives.cl (the configurations' composite; oracle/_ref variant
+                       udpt_mis_on) on the 32x24 Cornell box (3 passes, roulette after
+                       bounce 3) and on the level-3 glass scene (2 passes, at most 16
+                       bounces); python tests/golden/make_golden.py variant_b writes this
+                       file alone
   bvh_large.npz        SHA-256 digests of BVH::createBVH node arrays for a 327,714-
                        triangle scene (c1 with a level-7 icosphere) at leaf sizes 4 and
                        10: large enough for the host builder to split single nodes
@@ -100,6 +106,24 @@ def obj_fields(tris, mats, nodes, no_normals=()):
     return out
 
 
+VARIANT_B = {"c0": dict(rr=3, max_depth=100000, passes=3, seed=2025),
+             "c1l3": dict(rr=3, max_depth=16, passes=2, seed=2026)}
+
+
+def make_variant_b():
+    out = {}
+    for name, s in golden_scenes().items():
+        v = VARIANT_B[name]
+        seeds = scenes.pass_seeds(v["seed"], v["passes"])
+        acc = np.zeros((24, 32, 4), np.float32)
+        for k, sd in enumerate(seeds):
+            O.ref_render(s, acc, sd, 1 if k == 0 else 0, "udpt_mis_on", v["rr"], v["max_depth"])
+        out[name] = acc
+        out[name + "_seeds"] = seeds
+        out[name + "_sha256"] = scene_hash(s)
+    np.savez_compressed(os.path.join(HERE, "render_variant_b.npz"), **out)
+
+
 def main():
     if O.ref() is None:
         raise SystemExit("the compiled reference is not available here")
@@ -111,7 +135,7 @@ def main():
         np.savez_compressed(os.path.join(HERE, "obj_test_scene.npz"),
                             **obj_fields(*O.ref_load_obj(obj_files.write(d)), no_normals=obj_files.NO_NORMALS))
     np.savez_compressed(os.path.join(HERE, "obj_cornellbox.npz"),
-                        **obj_fields(*O.ref_load_obj(os.path.join(build_oracle.REF_SRC, "geometry", "cornellbox.obj"))))
+                        **obj_fields(*O.ref_load_obj(os.path.join(build_oracle.reference_tree(), "geometry", "cornellbox.obj"))))
     for name, s in golden_scenes().items():
         leaf = 10 if name == "c0" else 4
         nodes = O.ref_bvh(s.tris, 20, leaf)
@@ -169,6 +193,7 @@ def main():
         out["sha_lights%d" % lights] = scene_hash(sb)
     np.savez_compressed(os.path.join(HERE, "render_bdpt.npz"), seeds=seeds, **out)
     make_large()
+    make_variant_b()
     print("golden fixtures written to", HERE)
 
 
@@ -177,5 +202,9 @@ if __name__ == "__main__":
         if O.ref() is None:
             raise SystemExit("the compiled reference is not available here")
         make_large()
+    elif len(sys.argv) > 1 and sys.argv[1] == "variant_b":
+        if O.ref() is None:
+            raise SystemExit("the compiled reference is not available here")
+        make_variant_b()
     else:
         main()

@@ -25,7 +25,8 @@ def _module(name):
 
 MG = _module("make_golden")
 OBJ = _module("obj_files")
-CORNELL = os.path.join(build_oracle.REF_SRC, "geometry", "cornellbox.obj")
+_TREE = build_oracle.reference_tree()
+CORNELL = os.path.join(_TREE, "geometry", "cornellbox.obj") if _TREE else None
 
 
 def _ours(path):
@@ -62,7 +63,7 @@ def test_test_scene_matches_reference_loader(tmp_path):
 
 
 def test_cornellbox_matches_reference_loader():
-    if not os.path.exists(CORNELL):
+    if not CORNELL or not os.path.exists(CORNELL):
         pytest.skip("the reference's Cornell-box OBJ is not on this machine")
     got = MG.obj_fields(*_ours(CORNELL))
     _check(got, np.load(os.path.join(GOLD, "obj_cornellbox.npz")))
@@ -75,7 +76,7 @@ def test_live_against_the_compiled_reference(tmp_path):
     path = OBJ.write(str(tmp_path))
     want = MG.obj_fields(*O.ref_load_obj(path), no_normals=OBJ.NO_NORMALS)
     _check(MG.obj_fields(*_ours(path)), want)
-    if os.path.exists(CORNELL):
+    if CORNELL and os.path.exists(CORNELL):
         _check(MG.obj_fields(*_ours(CORNELL)), MG.obj_fields(*O.ref_load_obj(CORNELL)))
 
 

@@ -122,6 +122,21 @@ def test_oracle_oren_nayar_matches_reference():
     assert np.array_equal(out.view(np.int32), g["value"].view(np.int32))
 
 
+@pytest.mark.parametrize("name", sorted(MG.VARIANT_B))
+def test_oracle_variant_b_matches_reference(name):
+    """The restatement with brdf_model 1 (Oren-Nayar) and no lobe fix equals the
+    compiled composite udpt.cl -DMIS + udpt-primitives.cl's Oren-Nayar rule."""
+    g = _load("render_variant_b.npz")
+    s = SCENES[name]
+    assert MG.scene_hash(s) == str(g[name + "_sha256"])
+    v = MG.VARIANT_B[name]
+    cfg = dict(mis=1, rr_threshold=v["rr"], max_depth=v["max_depth"], brdf_model=1, mis_lobe_fix=0)
+    acc = np.zeros((24, 32, 4), np.float32)
+    for k, sd in enumerate(g[name + "_seeds"]):
+        O.render(s, acc, sd, 1 if k == 0 else 0, cfg, threads=2)
+    assert np.array_equal(acc.view(np.int32), g[name].view(np.int32))
+
+
 @pytest.mark.parametrize("lights", [1, 4])
 def test_oracle_bdpt_matches_reference(lights):
     g = _load("render_bdpt.npz")
@@ -179,6 +194,10 @@ def test_oracle_trace_live_large():
     ("udpt_a", dict(mis=0, rr_threshold=6, max_depth=100000)),
     ("udpt_mis", dict(mis=1, rr_threshold=3, max_depth=16)),
     ("udpt_mis", dict(mis=1, rr_threshold=0, max_depth=4)),
+    # variant B, the configurations' composite: udpt.cl -DMIS with udpt-primitives.cl's
+    # Oren-Nayar diffuse rule (the restatement's brdf_model 1, without the lobe fix)
+    ("udpt_mis_on", dict(mis=1, rr_threshold=3, max_depth=16, brdf_model=1, mis_lobe_fix=0)),
+    ("udpt_mis_on", dict(mis=1, rr_threshold=0, max_depth=100000, brdf_model=1, mis_lobe_fix=0)),
 ])
 def test_oracle_render_live_glass(variant, cfg):
     s = scenes.c1(24, 20, level=4)
@@ -188,6 +207,21 @@ def test_oracle_render_live_glass(variant, cfg):
     for k, sd in enumerate(seeds):
         O.render(s, a, sd, 1 if k == 0 else 0, cfg, threads=4)
         O.ref_render(s, b, sd, 1 if k == 0 else 0, variant, cfg["rr_threshold"], cfg["max_depth"], threads=4)
+    assert np.array_equal(a.view(np.int32), b.view(np.int32))
+
+
+@needs_ref
+def test_oracle_render_live_variant_b_cornell():
+    """Variant B on the Cornell box, whose walls are Oren-Nayar (sigma^2 0.09) and one box
+    modified Phong: every pixel of the restatement equals the compiled composite."""
+    s = scenes.c0(32, 24)
+    seeds = scenes.pass_seeds(41, 3)
+    cfg = dict(mis=1, rr_threshold=3, max_depth=100000, brdf_model=1, mis_lobe_fix=0)
+    a = np.zeros((24, 32, 4), np.float32)
+    b = np.zeros((24, 32, 4), np.float32)
+    for k, sd in enumerate(seeds):
+        O.render(s, a, sd, 1 if k == 0 else 0, cfg, threads=4)
+        O.ref_render(s, b, sd, 1 if k == 0 else 0, "udpt_mis_on", 3, 100000, threads=4)
     assert np.array_equal(a.view(np.int32), b.view(np.int32))
 
 

@@ -19,6 +19,7 @@ Configurations (sizes and spp of the benchmark workloads):
       the scenes of c0, c0_bdpt and c4 with the bidirectional tracer with multiple
       importance sampling (YC_BDPT_MIS): paths of at most 20, 8 and 8 segments.
 """
+import contextlib
 import ctypes as C
 import hashlib
 import json
@@ -29,6 +30,32 @@ import numpy as np
 
 from . import _native as N
 from .layouts import BVH_NODE, CAM, MATERIAL, QUAD_LIGHT, TRIANGLE, ptr
+
+
+# Where the scene arrays come from: the library whose yh_scene_* and yh_camera_look entry
+# points Builder and camera() call, and the BVH builder of build_bvh. By default both are
+# libyune_gb300.so's. A process that must not load the product library -- the CPU
+# baseline, which runs the reference's own code -- swaps in another library with the same
+# producer entry points and the reference's BVH::createBVH (producers() below); the
+# arrays are the same bytes either way.
+_producers = {"lib": None, "bvh": None}
+
+
+def _host():
+    return _producers["lib"] if _producers["lib"] is not None else N.lib()
+
+
+@contextlib.contextmanager
+def producers(lib, bvh):
+    """Within the block, scenes are generated by `lib` (a ctypes library exporting the
+    yh_scene_* and yh_camera_look functions of include/yune_host.h with their argtypes
+    set) and BVHs built by `bvh(tris, bins, leaf) -> (nodes, depth)`."""
+    old = dict(_producers)
+    _producers.update(lib=lib, bvh=bvh)
+    try:
+        yield
+    finally:
+        _producers.update(old)
 
 
 @dataclass
@@ -78,44 +105,44 @@ class Builder:
     """Thin owner of a yh_scene handle."""
 
     def __init__(self):
-        L = N.lib()
+        self.L = L = _host()
         h = C.c_void_p()
         N.check_host(L.yh_scene_new(C.byref(h)), "yh_scene_new")
         self.h = h
 
     def __del__(self):
         if getattr(self, "h", None):
-            N.lib().yh_scene_free(self.h)
+            self.L.yh_scene_free(self.h)
             self.h = None
 
     def cornell(self, seed=0, sigma2=0.09, phong_exp=50.0, emission=15.0, boxes=True):
-        N.check_host(N.lib().yh_scene_add_cornell(self.h, seed, sigma2, phong_exp, emission, int(boxes)), "cornell")
+        N.check_host(self.L.yh_scene_add_cornell(self.h, seed, sigma2, phong_exp, emission, int(boxes)), "cornell")
         return self
 
     def add_material(self, m):
         mid = C.c_int()
-        N.check_host(N.lib().yh_scene_add_material(self.h, ptr(m), C.byref(mid)), "material")
+        N.check_host(self.L.yh_scene_add_material(self.h, ptr(m), C.byref(mid)), "material")
         return mid.value
 
     def icosphere(self, center, radius, level, mat_id, disp=0.0, seed=0):
         c = np.asarray(center, np.float32)
-        N.check_host(N.lib().yh_scene_add_icosphere(self.h, ptr(c), radius, level, disp, seed, mat_id), "icosphere")
+        N.check_host(self.L.yh_scene_add_icosphere(self.h, ptr(c), radius, level, disp, seed, mat_id), "icosphere")
         return self
 
     def load_obj(self, path):
         """Appends an OBJ file and its material file (yh_scene_load_obj, the rules of
         Scene::loadModel); returns the number of triangles read."""
         n = C.c_int()
-        N.check_host(N.lib().yh_scene_load_obj(self.h, os.fsencode(path), C.byref(n)), "yh_scene_load_obj " + str(path))
+        N.check_host(self.L.yh_scene_load_obj(self.h, os.fsencode(path), C.byref(n)), "yh_scene_load_obj " + str(path))
         return n.value
 
     def add_light(self, l):
-        N.check_host(N.lib().yh_scene_add_light(self.h, ptr(l)), "light")
+        N.check_host(self.L.yh_scene_add_light(self.h, ptr(l)), "light")
         return self
 
     def arrays(self):
         nt, nm, nl = C.c_int(), C.c_int(), C.c_int()
-        L = N.lib()
+        L = self.L
         N.check_host(L.yh_scene_counts(self.h, C.byref(nt), C.byref(nm), C.byref(nl)), "counts")
         tris = np.zeros(nt.value, TRIANGLE)
         mats = np.zeros(nm.value, MATERIAL)
@@ -126,6 +153,8 @@ class Builder:
 
 def build_bvh(tris, bins=20, leaf=10):
     """Node array of BVH::createBVH for these triangles, and the tree depth."""
+    if _producers["bvh"] is not None:
+        return _producers["bvh"](tris, bins, leaf)
     L = N.lib()
     h = C.c_void_p()
     N.check_host(L.yh_bvh_build(ptr(tris), len(tris), bins, leaf, C.byref(h)), "yh_bvh_build")
@@ -169,7 +198,7 @@ def refit_bvh(tris, nodes):
 def camera(eye=(0.0, 0.0, 1.4), side=(1.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), look=(0.0, 0.0, -1.0), fov=60.0):
     cam = np.zeros(1, CAM)
     a = [np.asarray(v, np.float32) for v in (eye, side, up, look)]
-    N.check_host(N.lib().yh_camera_look(ptr(a[0]), ptr(a[1]), ptr(a[2]), ptr(a[3]), fov, ptr(cam)), "camera")
+    N.check_host(_host().yh_camera_look(ptr(a[0]), ptr(a[1]), ptr(a[2]), ptr(a[3]), fov, ptr(cam)), "camera")
     return cam
 
 
