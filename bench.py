@@ -1,33 +1,45 @@
 """Benchmark of the path-tracing core.
 
-Workload (one step = one render pass = one sample per pixel over the frame, the
-per-pass contract of src/RendererCore.cpp:248-469): the glass-icosphere Cornell box
-(81,954 triangles, SAH BVH with leaf <= 4), 1024x1024, NEE + MIS, roulette after bounce
-3, at most 16 bounces; synthetic seeded scene, per-pass seeds from mt19937(0).
+Default workload (--config c2, the mixed workload the batched/served target is stated on):
+64 seeded scenes, each a Cornell box plus displaced icospheres (triangle totals
+log-uniform in [1k, 500k], 6.44M in all), materials drawn from {Oren-Nayar, modified
+Phong, dielectric}, resolutions drawn from {256^2, 512^2, 1280x720, 1920x1080} (59.6M
+pixels per pass), NEE + MIS with udpt-primitives.cl's Oren-Nayar rule, roulette after
+bounce 3, at most 16 bounces, no lobe fix (the reference's own MIS arithmetic, so the
+CPU reference runs the same configuration). One step = one pass (one sample per pixel)
+of every job of the mix; the configuration's 64 spp are 64 steps.
 
 Printed (one JSON line on rank 0):
-  value        Mrays/s of the whole job: the K timed passes rendered as one job of the
-               batch engine (every pixel's passes in order in one path slot, so the image
-               is bit-identical to K yc_render_pass calls, checked in the line): every
-               traceRay-equivalent query (primary, extension, NEE shadow, MIS) / device
-               time (CUDA events on the context stream), inputs resident in HBM
-  per_pass     the same passes through yc_render_pass, one call per pass, L2 flushed
-               before each (the drop-in call of RendererCore)
-  e2e          the metric through the C-ABI with host buffers: per step the camera and
-               the pass seeds go host -> device and the tonemapped frame comes back
-               (engine, E passes per step); e2e_per_pass does it one pass per step
-  roofline     the extend (closest-hit) kernel: algorithmic bytes (32 B per box test,
-               48 B per triangle test, 84 B of ray/hit records per ray) / its event time,
-               against the measured L2 read bandwidth (the node + triangle set stays in
-               L2); hbm_frac against MEASURED_PEAKS.json's HBM copy bandwidth
-  cpu_baseline the reference kernel source compiled as C++ (oracle/_ref), all host
-               threads, on a band of rows of the same frame
-`--impl reference` times that CPU reference alone on the same workload.
+  value        Mrays/s of the batched form: the K timed passes of all 64 jobs rendered
+               in one persistent wavefront (yc_batch_*); every traceRay-equivalent query
+               (primary, extension, NEE shadow, MIS) over the CUDA-event time of the
+               run, inputs resident in HBM; the median of --reps repetitions
+  plain        the same passes through the plain one-frame-at-a-time path
+               (yc_render_passes, job after job), timed the same way; its median, and
+               batched_over_plain = the median of the per-repetition ratios
+  equal_results every accumulator of the batched form equal bit for bit to the plain one
+  walked_grays_per_s, samples_per_s  rays that walked a BVH, and pixel paths, per second
+  roofline     the traversal kernel of the batched form (profiled copy): algorithmic
+               bytes (32 B per box test, 48 B per triangle test, 84 B of ray and hit
+               records per ray) over its event time, against the measured L2 read
+               bandwidth; hbm_frac against MEASURED_PEAKS.json's HBM copy bandwidth
+  e2e          the metric through the C-ABI with host buffers: per step every job's
+               camera and pass seeds go host -> device (yc_batch_add_job), the batch runs
+               and every job's tonemapped frame comes back (yc_tonemap); e2e_plain does
+               the same with yc_set_camera + yc_render_passes
+  cpu_baseline the reference kernel source (udpt.cl -DMIS with udpt-primitives.cl's
+               Oren-Nayar rule) compiled as C++ (oracle/_ref), all host threads, on bands
+               of rows of 8 of the 64 scenes (every eighth), each given time in proportion
+               to its pixels
+`--impl reference` times that CPU reference alone on the same workload; it generates
+the scenes with the oracle library's copy of the scene producers and builds their BVHs
+with the reference's own BVH::createBVH, so it loads no product library.
 With torchrun (N > 1) every rank renders its own replica (the work does not exchange
 data; multi-GPU is replicas only) and the value is the sum of the ranks' rays over the
 slowest rank's time.
-Other modes: --config c2 (mixed batch vs the plain loop), --config c3 (serving),
---quality (RMSE against the FP64 references), --trace-bench N (traversal alone).
+Other modes: --config c1 / c0 (one frame, batch engine against yc_render_pass), c4,
+c0_bdpt, c4_mis, c0_bdpt_mis (per-pass BDPT), --config c3 (serving), --quality (RMSE
+against the FP64 references), --trace-bench N (traversal alone).
 """
 import argparse
 import json
@@ -50,18 +62,20 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=64)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c1")
-    ap.add_argument("--e2e-steps", type=int, default=8)
-    ap.add_argument("--e2e-passes", type=int, default=8, help="passes per e2e step through the engine")
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--reps", type=int, default=3, help="c2: timed repetitions (median reported)")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="e2e steps (0: 8 for one frame, 2 for the mix)")
+    ap.add_argument("--e2e-passes", type=int, default=0, help="passes per e2e step (0: 8 for one frame, 4 for "
+                                                                 "the mix)")
     ap.add_argument("--groups", type=int, default=2, help="slot groups of the engine (c1 whole-job run)")
-    ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    ap.add_argument("--cpu-seconds", type=float, default=0.0, help="CPU baseline budget (0: 8 s, 16 s for the mix)")
     ap.add_argument("--no-cpu", action="store_true")
     # batched (c2) and served (c3) comparisons against the plain per-pass loop
     ap.add_argument("--jobs", type=int, default=64)
-    ap.add_argument("--spp", type=int, default=4, help="c2: passes per job")
+    ap.add_argument("--sample-every", type=int, default=8, help="c2 CPU baseline: every n-th job of the mix")
     ap.add_argument("--pool", type=int, default=0, help="batch path slots (0: 2M)")
     ap.add_argument("--requests", type=int, default=40)
     ap.add_argument("--rate", type=float, default=20.0, help="c3: Poisson arrival rate (req/s)")
@@ -85,7 +99,12 @@ def parse():
     ap.add_argument("--res", default="", help="c4: frame size WxH instead of 3840x2160 (profiling captures)")
     ap.add_argument("--tree", type=int, default=1,
                     help="interior hierarchy: 0 reference nodes, 1 binary SAH over the reference leaves, 2 four-wide")
-    return ap.parse_args()
+    a = ap.parse_args()
+    mix = a.config == "c2"
+    a.e2e_steps = a.e2e_steps or (2 if mix else 8)
+    a.e2e_passes = a.e2e_passes or (4 if mix else 8)
+    a.cpu_seconds = a.cpu_seconds or (16.0 if mix else 8.0)
+    return a
 
 
 def dist_init(args):
@@ -168,12 +187,26 @@ def scene_for(name):
     return scenes.CONFIGS[name]()
 
 
-def cpu_reference(scene, seeds, seconds, want_rays=True, band=0):
+def reference_variant(cfg):
+    """The compiled reference variant (oracle/_ref) that runs configuration `cfg`, and a
+    note; None when no variant of the reference has the configuration."""
+    if cfg.get("integrator", 0) != 0:
+        return None, ""
+    if not cfg.get("mis", 0):
+        return ("udpt_a", "; udpt.cl as shipped") if not cfg.get("brdf_model", 0) else (None, "")
+    v = "udpt_mis_on" if cfg.get("brdf_model", 0) == 1 else "udpt_mis"
+    note = ("; udpt.cl -DMIS with udpt-primitives.cl's Oren-Nayar rule" if v == "udpt_mis_on"
+            else "; udpt.cl -DMIS")
+    return v, note
+
+
+def _cpu_measure(scene, seeds, seconds, want_rays=True, band=0):
     """Times the reference kernel source (compiled as C++) on bands of rows of the frame
     with all host threads; rays counted by the oracle on the same band (same algorithm,
-    bit-identical results). Falls back to the oracle port when the compiled reference is
-    not available. band = 0: H/64 rows per band from the top of the frame; band > 0:
-    bands of that many rows spread over the frame (a stride coprime to its height)."""
+    bit-identical results). Falls back to the oracle port when the compiled reference has
+    no variant for the configuration. band = 0: H/64 rows per band from the top of the
+    frame; band > 0: bands of that many rows spread over the frame (a stride coprime to
+    its height). Returns rays, seconds, rows, kind and a note."""
     from oracle import oracle_py as O
     W, H = scene.width, scene.height
     cfg = dict(scene.cfg)
@@ -181,7 +214,6 @@ def cpu_reference(scene, seeds, seconds, want_rays=True, band=0):
     bdpt_mis = cfg.get("integrator", 0) == 2
     threads = os.cpu_count() or 1
     use_ref = O.ref() is not None and not bdpt_mis
-    kind = "reference" if use_ref else "port"
     note = ""
     if bdpt_mis:   # no reference implementation exists: the CPU statement is the baseline
         kmax = int(cfg.get("bdpt_bounces", 20))
@@ -191,14 +223,19 @@ def cpu_reference(scene, seeds, seconds, want_rays=True, band=0):
         bounces = int(cfg.get("bdpt_bounces", 20))
         variant = {(20, 1): "bdpt20", (8, 1): "bdpt8", (8, 4): "bdpt8_l4"}.get((bounces, len(scene.lights)))
         if use_ref and variant is None:
-            use_ref, kind = False, "port"
+            use_ref = False
         note = "; bdpt.cl, %d vertices per subpath, %d lights" % (bounces, len(scene.lights))
-    elif use_ref and (cfg.get("brdf_model", 0) or cfg.get("mis_lobe_fix", 0)):
-        # udpt.cl has neither the Oren-Nayar term nor the lobe fix: it runs its nearest
-        # variant (Lambert, reference MIS), and the oracle counts the rays of that variant
-        cfg["brdf_model"] = 0
-        cfg["mis_lobe_fix"] = 0
-        note = "; udpt.cl with -DMIS (Lambert diffuse, no lobe fix)"
+    elif use_ref:
+        if cfg.get("mis_lobe_fix", 0):
+            # the reference has no lobe fix: it runs its own MIS arithmetic, and the oracle
+            # counts the rays of that arithmetic
+            cfg["mis_lobe_fix"] = 0
+            note = "; without the lobe fix (reference MIS)"
+        variant, vnote = reference_variant(cfg)
+        if variant is None or len(scene.lights) != 1:
+            use_ref = False
+        note = vnote + note
+    kind = "reference" if use_ref else "port"
     acc = np.zeros((H, W, 4), np.float32)
     if band <= 0:
         band = max(1, H // 64)
@@ -208,17 +245,17 @@ def cpu_reference(scene, seeds, seconds, want_rays=True, band=0):
         step = next(q for q in range(nb // 3 + 1, nb + 1) if np.gcd(q, nb) == 1) if nb > 2 else 1
         starts = [((i * step) % nb) * band for i in range(nb)]
 
-    def one(k, r, a):
+    def one(k, r, a, ref):
         if bdpt_mis:
             return O.render_bdpt_mis(scene, a, seeds[k % len(seeds)], 1, kmax, cfg, threads=threads, rows=r)
         if bdpt:
-            if use_ref:
+            if ref:
                 O.ref_render(scene, a, seeds[k % len(seeds)], 1, variant, 0, 0, threads=threads, rows=r)
                 return None
             return O.render_bdpt(scene, a, seeds[k % len(seeds)], 1, bounces, threads=threads, rows=r)
-        if use_ref:
-            O.ref_render(scene, a, seeds[k % len(seeds)], 1, "udpt_mis" if cfg["mis"] else "udpt_a",
-                         cfg["rr_threshold"], cfg["max_depth"], threads=threads, rows=r)
+        if ref:
+            O.ref_render(scene, a, seeds[k % len(seeds)], 1, variant, cfg["rr_threshold"], cfg["max_depth"],
+                         threads=threads, rows=r)
             return None
         return O.render(scene, a, seeds[k % len(seeds)], 1, cfg, threads=threads, rows=r)
 
@@ -228,20 +265,47 @@ def cpu_reference(scene, seeds, seconds, want_rays=True, band=0):
         y = starts[k % len(starts)]
         r = (y, min(H, y + band))
         t0 = time.perf_counter()
-        c = one(k, r, acc)
+        c = one(k, r, acc, use_ref)
         t_total += time.perf_counter() - t0
         if c is None and want_rays:   # the oracle counts the rays of the same band
-            use_ref_saved, use_ref = use_ref, False
-            c = one(k, r, np.zeros_like(acc))
-            use_ref = use_ref_saved
+            c = one(k, r, np.zeros_like(acc), False)
         rays += c["rays"] if c else 0
         rows_done += r[1] - r[0]
         k += 1
-    value = rays / t_total / 1e6 if t_total > 0 else 0.0
-    return {"value": value, "unit": METRIC, "cores": threads, "kind": kind,
-            "sample": "%d rows of %d x %d px (%.2f passes' worth), %.1f s%s" % (rows_done, H, W, rows_done / H,
-                                                                            t_total, note),
-            "samples_per_s": rows_done * W / t_total if t_total > 0 else 0.0}
+    return {"rays": rays, "seconds": t_total, "rows": rows_done, "pixels": rows_done * W, "kind": kind,
+            "note": note, "threads": threads}
+
+
+def cpu_reference(scene, seeds, seconds, want_rays=True, band=0):
+    """The CPU baseline on one frame (see _cpu_measure)."""
+    m = _cpu_measure(scene, seeds, seconds, want_rays, band)
+    W, H, t = scene.width, scene.height, m["seconds"]
+    return {"value": m["rays"] / t / 1e6 if t > 0 else 0.0, "unit": METRIC, "cores": m["threads"], "kind": m["kind"],
+            "sample": "%d rows of %d x %d px (%.2f passes' worth), %.1f s%s" % (m["rows"], H, W, m["rows"] / H, t,
+                                                                            m["note"]),
+            "samples_per_s": m["pixels"] / t if t > 0 else 0.0}
+
+
+def cpu_reference_mix(jobs, idx, seeds, seconds):
+    """The CPU baseline on the mix: the sampled jobs `idx`, each timed for a share of
+    `seconds` in proportion to its pixels; Mrays/s = all rays over all time."""
+    px = np.array([jobs[i].width * jobs[i].height for i in range(len(jobs))], np.float64)
+    rays = t = pix = 0.0
+    kinds, notes = set(), set()
+    for i in range(len(jobs)):
+        m = _cpu_measure(jobs[i], seeds[i], seconds * px[i] / px.sum())
+        rays += m["rays"]
+        t += m["seconds"]
+        pix += m["pixels"]
+        kinds.add(m["kind"])
+        notes.add(m["note"])
+        threads = m["threads"]
+    return {"value": rays / t / 1e6 if t > 0 else 0.0, "unit": METRIC, "cores": threads,
+            "kind": "reference" if kinds == {"reference"} else "port",
+            "sample": "jobs %s of the mix (every %d-th), bands of rows in proportion to their pixels: %d pixel "
+                      "paths, %.1f s%s" % (list(idx), idx[1] - idx[0] if len(idx) > 1 else 1, pix, t,
+                                           "".join(sorted(notes))),
+            "samples_per_s": pix / t if t > 0 else 0.0}
 
 
 def run_reference(args, rank, ws, dist):
@@ -630,79 +694,250 @@ def run_perpass_bdpt(args, rank, local, ws, dist):
     print(json.dumps(line))
 
 
-def run_c2(args):
-    """Mixed batch: every job rendered pass by pass (plain) and all jobs in one batch."""
+# ---- the mixed workload (c2): batched against plain ----
+def mix_cfg():
+    """Render options of every job of the mix: NEE + MIS, Oren-Nayar diffuse, roulette
+    after bounce 3, at most 16 bounces, the reference's MIS arithmetic (no lobe fix)."""
+    from yune_gb300 import scenes
+    return scenes.default_cfg(max_depth=16, mis_lobe_fix=0)
+
+
+def mix_config(args, jobs_meta):
+    """The `config` of both arms' lines (same workload, same options)."""
+    tris, px = jobs_meta
+    return {"workload": "c2: %d seeded scenes (Cornell box + displaced icospheres, %d triangles in all, 1k-500k "
+                        "each), resolutions from {256^2, 512^2, 1280x720, 1920x1080} (%d pixels per pass), "
+                        "materials from {Oren-Nayar, Phong exp 10-200, dielectric IOR 1.3-1.7}; NEE + MIS, "
+                        "roulette after bounce 3, max depth 16; one step = one pass of every job"
+                        % (args.jobs, tris, px),
+            "jobs": args.jobs, "triangles": tris, "pixels_per_pass": px, "spp_config": 64,
+            "reference_cfg": mix_cfg()}
+
+
+def mix_totals(specs):
+    """(triangles, pixels per pass) of the mix, from its job specifications."""
+    from yune_gb300 import workloads
+    return (int(sum(workloads.mixed_scene_tris(sp[0]) for sp in specs)), int(sum(sp[2] * sp[3] for sp in specs)))
+
+
+def mix_sample(n_jobs, every):
+    return list(range(0, n_jobs, max(1, every)))
+
+
+def run_mix(args, rank, local, ws, dist):
+    """The mixed workload on one GPU (a replica per rank under torchrun).
+
+    Per repetition (--reps, median reported): the K passes of every job through the plain
+    path (yc_render_passes, job after job) and through one batch (yc_batch_*), each timed
+    with CUDA events on the context stream, both continuing the same accumulators from
+    the same W warm-up passes; afterwards every accumulator of the batch equals the plain
+    one bit for bit. Then a profiled copy of the batched form (no graph; per-kernel
+    events: split and roofline), one profiled plain pass, e2e with host buffers, and the
+    CPU baseline on a sample of the jobs."""
     from yune_gb300 import autotune, scenes, workloads
     from yune_gb300.batch import Batch
     from yune_gb300.core import Renderer
-    jobs = workloads.c2_jobs(n_jobs=args.jobs, spp=args.spp, max_tris=args.max_tris)
-    r = Renderer(0)
+    K, Wm, R, E, S = args.steps, args.warmup, args.reps, args.e2e_passes, args.e2e_steps
+    t0 = time.perf_counter()
+    jobs = workloads.c2_jobs(n_jobs=args.jobs, spp=64, max_tris=args.max_tris, cfg=mix_cfg())
+    build_s = time.perf_counter() - t0
+    tris = int(sum(s.n_tri for s in jobs))
+    px = int(sum(s.width * s.height for s in jobs))
+    assert (tris, px) == mix_totals(workloads.c2_specs(args.jobs, max_tris=args.max_tris))
+    n_seeds = Wm + R * K + 2 + S * E
+    seeds = [scenes.pass_seeds(1000 + i, n_seeds) for i in range(len(jobs))]
+    r = Renderer(local)
     r.set_tree_mode(args.tree)
     r.set_mixed_trace(args.mixed)
     r.set_ray_sort(args.ray_sort // 10, args.ray_sort % 10, args.ray_sort_min)
     r.set_shade_sort(args.shade_sort_min)
-    sids = [r.upload(s) for s in jobs]
-    seeds = [scenes.pass_seeds(1000 + i, s.spp) for i, s in enumerate(jobs)]
-    px = sum(s.width * s.height for s in jobs)
-    out = {}
-    # plain
-    accs = [r.alloc_accum(s.width, s.height) for s in jobs]
-    r.reset_stats()
-    r.synchronize()
+    r.set_tail_paths(args.tail)
     t0 = time.perf_counter()
-    for s, sid, a, sd in zip(jobs, sids, accs, seeds):
-        r.set_camera(s.cam)
-        r.render_passes(sid, a, sd, reset_first=1, cfg=s.cfg)
-    r.synchronize()
-    tp = time.perf_counter() - t0
-    stp = r.stats()
-    plain_imgs = [r.read_accum(a) for a in accs[:4]]
-    for a in accs:
-        r.free_accum(a)
-    # batched: launch shape from the autotuner (untimed), unless --pool fixes the pool
+    sids = [r.upload(s) for s in jobs]
+    upload_s = time.perf_counter() - t0
+    scene_bytes = sum(r.scene_bytes(sid) for sid in sids)
     cap = max(r.scene_depth(sid) for sid in sids) + 2
+    l2 = r.measure_l2_gbs(48 << 20, 20)
+    pk, pk_kind = peaks()
     if args.pool:
         shape, trials, tune_s = autotune.BatchShape(pool_paths=args.pool), [], 0.0
-    else:
+    else:   # launch shape from the autotuner (untimed calibration, seeds of its own)
         shape, trials, tune_s = autotune.tune_scenes(r, jobs, sids, stack_cap=cap)
-    if args.profile:   # per-kernel split of the batched run (graph off, CUDA events per launch)
-        accs = [r.alloc_accum(s.width, s.height) for s in jobs]
-        b = Batch(r, use_graph=False, stack_cap=cap, **shape.kwargs())
-        for s, sid, a, sd in zip(jobs, sids, accs, seeds):
-            b.add_job(sid, a, s.cam, sd, s.cfg)
-        r.set_profiling(True)
-        b.run()
-        kt_batch = r.kernel_times()
-        r.set_profiling(False)
-        b.close()
-        for a in accs:
-            r.free_accum(a)
-    accs = [r.alloc_accum(s.width, s.height) for s in jobs]
-    b = Batch(r, stack_cap=cap, **shape.kwargs())
-    for s, sid, a, sd in zip(jobs, sids, accs, seeds):
-        b.add_job(sid, a, s.cam, sd, s.cfg)
+    cfg = mix_cfg()
+    acc_p = [r.alloc_accum(s.width, s.height) for s in jobs]
+    acc_b = [r.alloc_accum(s.width, s.height) for s in jobs]
+    # warm-up: W passes of every job in each form
+    for s, sid, a, sd in zip(jobs, sids, acc_p, seeds):
+        r.set_camera(s.cam)
+        r.render_passes(sid, a, sd[:Wm], reset_first=1, cfg=cfg)
+    b = Batch(r, stack_cap=cap, max_jobs=len(jobs) * (R + S + 2), **shape.kwargs())
+    for s, sid, a, sd in zip(jobs, sids, acc_b, seeds):
+        b.add_job(sid, a, s.cam, sd[:Wm], cfg, reset_first=1)
+    b.run()
+    r.synchronize()
+    reps = []
+    if dist:
+        dist.barrier()
+    with Clocks(local) as clk:
+        for k in range(R):
+            sl = slice(Wm + k * K, Wm + (k + 1) * K)
+            r.reset_stats()
+            r.event(0)
+            for s, sid, a, sd in zip(jobs, sids, acc_p, seeds):
+                r.set_camera(s.cam)
+                r.render_passes(sid, a, sd[sl], reset_first=0, cfg=cfg)
+            r.event(1)
+            ms_p = r.elapsed_ms(0, 1)
+            st_p = r.stats()
+            for s, sid, a, sd in zip(jobs, sids, acc_b, seeds):
+                b.add_job(sid, a, s.cam, sd[sl], cfg, reset_first=0)
+            r.synchronize()
+            r.reset_stats()
+            r.event(2)
+            left = b.run()
+            r.event(3)
+            ms_b = r.elapsed_ms(2, 3)
+            st_b = r.stats()
+            reps.append({"plain_ms": ms_p, "batched_ms": ms_b, "plain_rays": int(st_p["rays"]),
+                         "batched_rays": int(st_b["rays"]), "batched_traversed": int(st_b["traversed"]),
+                         "batched_samples": int(st_b["samples"]), "plain_samples": int(st_p["samples"]),
+                         "unfinished": left, "overflow": int(st_p["stack_overflow"] + st_b["stack_overflow"])})
+    same = True
+    for a, c in zip(acc_p, acc_b):
+        same = same and bool(np.array_equal(r.read_accum(a).view(np.int32), r.read_accum(c).view(np.int32)))
+    # profiled copies (per-kernel events; no graph): two passes of every job batched, one plain
+    prof = slice(Wm + R * K, Wm + R * K + 2)
+    scratch = [r.alloc_accum(s.width, s.height) for s in jobs]
+    bp = Batch(r, stack_cap=cap, use_graph=False, max_jobs=len(jobs), **shape.kwargs())
+    for s, sid, a, sd in zip(jobs, sids, scratch, seeds):
+        bp.add_job(sid, a, s.cam, sd[prof], cfg, reset_first=1)
+    r.synchronize()
     r.reset_stats()
-    r.synchronize()
+    r.set_profiling(True)
+    bp.run()
+    kt_b = r.kernel_times()
+    st_bp = r.stats()
+    r.set_profiling(False)
+    bp.close()
+    r.reset_stats()
+    r.set_profiling(True)
+    for s, sid, a, sd in zip(jobs, sids, scratch, seeds):
+        r.set_camera(s.cam)
+        r.render_passes(sid, a, sd[prof][:1], reset_first=1, cfg=cfg)
+    kt_p = r.kernel_times()
+    st_pp = r.stats()
+    r.set_profiling(False)
+    for a in scratch:
+        r.free_accum(a)
+    # e2e through the C-ABI with host buffers: S steps of E passes of every job
+    base = Wm + R * K + 2
+    r.reset_stats()
     t0 = time.perf_counter()
-    left = b.run()
-    r.synchronize()
-    tb = time.perf_counter() - t0
-    stb = r.stats()
-    same = all(np.array_equal(r.read_accum(a).view(np.int32), w.view(np.int32)) for a, w in zip(accs[:4], plain_imgs))
+    for k in range(S):
+        for s, sid, a, sd in zip(jobs, sids, acc_b, seeds):
+            b.add_job(sid, a, s.cam, sd[base + k * E:base + (k + 1) * E], cfg, reset_first=0)
+        b.run()
+        for a in acc_b:
+            r.tonemap(a)
+    e2e_s = time.perf_counter() - t0
+    e2e_rays = r.stats()["rays"]
+    r.reset_stats()
+    t0 = time.perf_counter()
+    for k in range(S):
+        for s, sid, a, sd in zip(jobs, sids, acc_p, seeds):
+            r.set_camera(s.cam)
+            r.render_passes(sid, a, sd[base + k * E:base + (k + 1) * E], reset_first=0, cfg=cfg)
+            r.tonemap(a)
+    e2e_p_s = time.perf_counter() - t0
+    e2e_p_rays = r.stats()["rays"]
     b.close()
-    out = {"metric": METRIC, "unit": METRIC, "config": {"workload": "c2 mixed batch", "jobs": len(jobs), "spp": args.spp,
-                                                         "pixels_per_pass": px,
-                                                         "triangles": int(sum(s.n_tri for s in jobs))},
-           "plain": {"value": stp["rays"] / tp / 1e6, "seconds": tp, "samples_per_s": stp["samples"] / tp},
-           "batched": {"value": stb["rays"] / tb / 1e6, "seconds": tb, "samples_per_s": stb["samples"] / tb,
-                       "unfinished": left},
-           "speedup": tp / tb, "equal_results": bool(same), "rays_equal": stp["rays"] == stb["rays"],
-           "autotune": {"shape": shape.kwargs(), "seconds": tune_s,
-                        "trials": [[t.kwargs(), ms] for t, ms in trials]}}
-    if args.profile:
-        out["batched"]["kernel_ms"] = kt_batch
+    med = lambda v: float(np.median(v))  # noqa: E731
+    vb = [x["batched_rays"] / (x["batched_ms"] / 1e3) / 1e6 for x in reps]
+    vp = [x["plain_rays"] / (x["plain_ms"] / 1e3) / 1e6 for x in reps]
+    mid = int(np.argsort(vb)[len(vb) // 2])
+    t_s, rays = _reduce(dist, reps[mid]["batched_ms"] / 1e3, reps[mid]["batched_rays"])
+    e2e_s, e2e_rays = _reduce(dist, e2e_s, e2e_rays)
+    e2e_p_s, e2e_p_rays = _reduce(dist, e2e_p_s, e2e_p_rays)
+    if rank != 0:
+        r.close()
+        return
+    launches = int(kt_b["raygen_launches"] + kt_b["extend_launches"] + kt_b["occlusion_launches"]
+                   + kt_b["trace_launches"] + kt_b["logic_launches"] + 3 * kt_b["sort_launches"]
+                   + 3 * kt_b["raysort_launches"]) * K // 2   # the profiled run's launches per pass, times K
+    acc_bytes = 16 * px
+    line = {
+        "metric": METRIC, "value": rays / t_s / 1e6, "unit": METRIC, "n_gpus": ws, "steps": K, "warmup": Wm,
+        "ms_per_step": reps[mid]["batched_ms"] / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded procedural scenes)",
+        "config": dict(mix_config(args, (tris, px)),
+                       method="the K steps of every job rendered as one batch of K passes per job (value), and job "
+                              "after job through yc_render_passes (plain); median of %d repetitions" % R,
+                       l2="inputs larger than L2: %d MB of scenes and %d MB of accumulators per form"
+                          % (scene_bytes >> 20, acc_bytes >> 20),
+                       engine_shape=shape.kwargs(), tree_mode=args.tree,
+                       parallelism="replicas" if ws > 1 else "single GPU"),
+        "batched_over_plain": med([a / b for a, b in zip(vb, vp)]),
+        "plain": {"value": med(vp), "ms_per_step": med([x["plain_ms"] for x in reps]) / K, "unit": METRIC,
+                  "samples_per_s": med([x["plain_samples"] / (x["plain_ms"] / 1e3) for x in reps]),
+                  "path": "yc_set_camera + yc_render_passes, one call of K passes per job, job after job"},
+        "reps": [dict(x, batched_mrays=a, plain_mrays=p) for x, a, p in zip(reps, vb, vp)],
+        "equal_results": same,
+        "samples_per_s": reps[mid]["batched_samples"] / (reps[mid]["batched_ms"] / 1e3),
+        "walked_grays_per_s": reps[mid]["batched_traversed"] / (reps[mid]["batched_ms"] / 1e3) / 1e9,
+        "rays_per_sample": reps[mid]["batched_rays"] / max(1, reps[mid]["batched_samples"]),
+        "walked_share": reps[mid]["batched_traversed"] / max(1, reps[mid]["batched_rays"]),
+        "gpu_launches": launches,
+        "kernel_ms_2_passes": {"fill": kt_b["raygen_ms"], "raysort": kt_b["raysort_ms"], "trace": kt_b["trace_ms"],
+                               "sort": kt_b["sort_ms"], "logic": kt_b["logic_ms"], "rounds": kt_b["rounds"]},
+        "plain_kernel_ms_1_pass": {"raygen": kt_p["raygen_ms"], "raysort": kt_p["raysort_ms"],
+                                   "trace": kt_p["trace_ms"], "sort": kt_p["sort_ms"], "logic": kt_p["logic_ms"],
+                                   "tail": kt_p["tail_ms"], "rounds": kt_p["rounds"]},
+        "roofline": _trace_roofline(st_bp, kt_b, l2, pk, pk_kind, "k_batch_trace_mixed (closest + any-hit rays)",
+                                    "k_batch_trace<closest> (extend)"),
+        "plain_roofline": _trace_roofline(st_pp, kt_p, l2, pk, pk_kind, "k_trace_paths_mixed (closest + any-hit rays)",
+                                          "k_trace_paths<closest> (extend)"),
+        "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else 0.0, "unit": METRIC, "passes_per_step": E,
+                "steps": S, "h2d_bytes_per_step": len(jobs) * (80 + 4 * E), "d2h_bytes_per_step": acc_bytes,
+                "path": "per step: yc_batch_add_job (camera, seeds) for every job + yc_batch_run + yc_tonemap of "
+                        "every job to host"},
+        "e2e_plain": {"value": e2e_p_rays / e2e_p_s / 1e6 if e2e_p_s > 0 else 0.0, "unit": METRIC,
+                      "passes_per_step": E, "steps": S, "h2d_bytes_per_step": len(jobs) * (80 + 4 * E),
+                      "d2h_bytes_per_step": acc_bytes,
+                      "path": "per step and job: yc_set_camera + yc_render_passes + yc_tonemap to host"},
+        "clocks": clk.summary(),
+        "host": {"scene_build_s": build_s, "upload_s": upload_s, "autotune_s": tune_s, "autotune_trials": len(trials)},
+        "stack_overflow": int(sum(x["overflow"] for x in reps)),
+    }
+    if not args.no_cpu:
+        idx = mix_sample(len(jobs), args.sample_every)
+        line["cpu_baseline"] = cpu_reference_mix([jobs[i] for i in idx], idx, [seeds[i] for i in idx],
+                                                 args.cpu_seconds)
     r.close()
-    print(json.dumps(out))
+    print(json.dumps(line))
+
+
+def run_reference_mix(args, rank, ws, dist):
+    """The reference arm on the mix: the compiled reference on the sampled jobs, whose
+    scenes come from the oracle library's producers and whose BVHs come from the
+    reference's BVH::createBVH -- no product library is loaded."""
+    if rank != 0:
+        return
+    from oracle import oracle_py as O
+    from yune_gb300 import scenes, workloads
+    idx = mix_sample(args.jobs, args.sample_every)
+    specs = workloads.c2_specs(args.jobs, max_tris=args.max_tris)
+    with scenes.producers(O.scene_lib(), O.ref_bvh_with_depth):
+        jobs = workloads.c2_jobs(n_jobs=args.jobs, spp=64, max_tris=args.max_tris, cfg=mix_cfg(), only=idx)
+    n_seeds = args.warmup + args.reps * args.steps
+    seeds = [scenes.pass_seeds(1000 + i, n_seeds) for i in idx]
+    cb = cpu_reference_mix(jobs, idx, seeds, args.cpu_seconds)
+    cfg = mix_config(args, mix_totals(specs))
+    line = {"metric": METRIC, "value": cb["value"], "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded procedural scenes)", "config": cfg,
+            "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": METRIC, "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
 
 
 def run_c3(args):
@@ -837,13 +1072,16 @@ def main():
         return run_quality(args)
     if args.trace_bench:
         return run_trace_bench(args)
-    if args.impl == "ours" and args.config == "c2":
-        return run_c2(args)
     if args.impl == "ours" and args.config == "c3":
         return run_c3(args)
     rank, local, ws, dist = dist_init(args)
     if args.impl == "reference":
-        run_reference(args, rank, ws, dist)
+        if args.config == "c2":
+            run_reference_mix(args, rank, ws, dist)
+        else:
+            run_reference(args, rank, ws, dist)
+    elif args.config == "c2":
+        run_mix(args, rank, local, ws, dist)
     elif scenes_is_bdpt(args.config):
         run_perpass_bdpt(args, rank, local, ws, dist)
     else:

@@ -257,6 +257,92 @@ int yc_batch_cancel_job(yc_batch* b, int job_id);
  * after which their handles must not be used. */
 int yc_batch_destroy(yc_batch* b);
 
+/* ---- serving: continuous batching of render requests ----
+ * No counterpart in the reference, which renders one frame at a time from its GUI loop
+ * (src/RendererCore.cpp:248-469); a host that serves many clients submits their frames
+ * here. Requests (scene, frame size, passes, seeds, camera, options) are admitted while
+ * their accumulators fit a device-memory budget and become jobs of one long-lived batch,
+ * so requests that arrive while others run share its wavefront as slots and memory free
+ * up. Each request's accumulator is bit-identical to rendering it alone with
+ * yc_render_passes and the same seeds.
+ *
+ * The admission rules are a host-only object (yc_admission), usable without a device by
+ * callers with their own scheduler: a request costs its accumulator (width * height * 16
+ * bytes) plus its seeds (4 bytes per pass); one larger than the whole budget is rejected
+ * at once, and so is one that arrives while max_queue requests already wait; waiting
+ * requests are admitted in arrival order (the oldest first; a younger one never overtakes
+ * it) whenever the bytes in use plus theirs fit the budget. A waiting request that is
+ * cancelled is dropped; a running one is marked cancelling and finishes (cancelled) when
+ * its work in flight drains, releasing its bytes. */
+enum {
+  YC_REQ_WAITING = 0,          /* queued for memory */
+  YC_REQ_RUNNING = 1,          /* admitted: its job is in the batch */
+  YC_REQ_CANCELLING = 2,       /* cancelled while running; its pixels in flight drain */
+  YC_REQ_DONE = 3,             /* every pass of every pixel rendered */
+  YC_REQ_CANCELLED = 4,
+  YC_REQ_REJECTED_BUDGET = 5,  /* larger than the whole budget */
+  YC_REQ_REJECTED_QUEUE = 6    /* max_queue requests were already waiting */
+};
+typedef struct yc_admission yc_admission;
+/* max_queue < 0: no limit on waiting requests */
+int yc_admission_create(uint64_t budget_bytes, int32_t max_queue, yc_admission** out);
+/* A new request of `bytes`: *ticket identifies it, *state is YC_REQ_RUNNING (admitted at
+ * once: nothing waits and it fits), YC_REQ_WAITING or a YC_REQ_REJECTED_* state. */
+int yc_admission_submit(yc_admission* a, uint64_t bytes, int64_t* ticket, int32_t* state);
+/* Admits the oldest waiting request if it fits now: *ticket = its ticket, or -1. */
+int yc_admission_next(yc_admission* a, int64_t* ticket);
+/* Cancels: waiting -> YC_REQ_CANCELLED (dropped), running -> YC_REQ_CANCELLING; other
+ * states are left as they are. *state receives the new state. */
+int yc_admission_cancel(yc_admission* a, int64_t ticket, int32_t* state);
+/* The request's work is over (running -> DONE, cancelling -> CANCELLED); its bytes are
+ * released. */
+int yc_admission_finish(yc_admission* a, int64_t ticket, int32_t* state);
+int yc_admission_state(const yc_admission* a, int64_t ticket, int32_t* state);
+int yc_admission_usage(const yc_admission* a, uint64_t* bytes_in_use, int32_t* waiting, int32_t* running);
+int yc_admission_destroy(yc_admission* a);
+
+typedef struct yc_server yc_server;
+typedef struct yc_serve_cfg {
+  uint64_t budget_bytes;       /* device bytes of the requests in flight (accumulators, seeds) */
+  int32_t max_queue;           /* waiting requests beyond this are rejected; < 0: no limit */
+  int32_t keep_results;        /* 1: a finished request keeps its accumulator (and its bytes
+                                  in the budget) until yc_serve_release; 0: freed at once */
+  yc_batch_cfg batch;          /* the engine's launch shape (stack_cap 0: from the first
+                                  requests' scenes; give the deepest resident scene's) */
+} yc_serve_cfg;
+typedef struct yc_request_desc {
+  int32_t scene_id;            /* a scene uploaded to the server's context */
+  int32_t width, height;
+  int32_t n_pass;
+  const uint32_t* seeds_host;  /* n_pass pass seeds (copied by yc_serve_submit) */
+  yc_cam cam;
+  yc_pass_cfg cfg;             /* integrator YC_UDPT */
+} yc_request_desc;
+typedef struct yc_request_info {
+  int32_t state;               /* YC_REQ_* */
+  int32_t accum_id;            /* while running and, with keep_results, once done; else -1 */
+  int64_t pixels_done, pixels_total;
+  double submit_s, admit_s, finish_s;   /* seconds on the server's steady clock (-1: not yet) */
+} yc_request_info;
+int yc_serve_create(yc_ctx* ctx, const yc_serve_cfg* cfg, yc_server** out);
+/* Submits a request (seeds are copied); admitted at once when it fits. */
+int yc_serve_submit(yc_server* s, const yc_request_desc* req, int64_t* request_id, int32_t* state);
+int yc_serve_cancel(yc_server* s, int64_t request_id);
+/* One scheduling step: admits waiting requests that fit, runs up to max_launches launches
+ * of the batch (0: none, only admission and completion), then finishes every request whose
+ * pixels are all done (freeing its accumulator unless keep_results). *running receives the
+ * requests still running or cancelling, *waiting those queued. */
+int yc_serve_step(yc_server* s, int max_launches, int32_t* running, int32_t* waiting);
+int yc_serve_info(yc_server* s, int64_t request_id, yc_request_info* out);
+/* The accumulator of a finished request (keep_results = 1): width * height float4. */
+int yc_serve_read(yc_server* s, int64_t request_id, float* rgba_host);
+/* Frees a finished request's accumulator (keep_results = 1) and its budget bytes. */
+int yc_serve_release(yc_server* s, int64_t request_id);
+/* Seconds on the server's clock (the clock of yc_request_info). */
+double yc_serve_clock(const yc_server* s);
+/* Frees every accumulator still held and the batch. */
+int yc_serve_destroy(yc_server* s);
+
 /* ---- options ---- */
 enum {
   /* Interior hierarchy of uploaded scenes (applies to later yc_upload_scene calls):
@@ -308,6 +394,12 @@ int yc_set_option(yc_ctx* ctx, int option, int value);
 /* ---- statistics and tuning ---- */
 int yc_get_stats(yc_ctx* ctx, yc_stats* out);
 int yc_reset_stats(yc_ctx* ctx);
+/* Span timing on the context stream (the OpenCL event profiling RendererCore reads for
+ * its ms/frame and ms/kernel figures, src/RendererCore.cpp:483-505): yc_event_record
+ * records event `slot` (0..7) after the work queued so far; yc_event_elapsed_ms waits for
+ * event `to` and gives the milliseconds between the two recorded events. */
+int yc_event_record(yc_ctx* ctx, int slot);
+int yc_event_elapsed_ms(yc_ctx* ctx, int from, int to, float* ms);
 /* Device allocations (cudaMalloc) the library's contexts and batches have made in this
  * process so far. A caller that must not allocate while it renders can check that this
  * count does not change across its calls (yc_render_pass_noalloc never allocates). */

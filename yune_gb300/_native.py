@@ -57,6 +57,32 @@ class BatchCfg(C.Structure):
                 ("max_jobs", i32), ("stack_cap", i32), ("sort_threshold", i32), ("groups", i32), ("ray_sort", i32)]
 
 
+class ServeCfg(C.Structure):
+    """yc_serve_cfg"""
+    _fields_ = [("budget_bytes", C.c_uint64), ("max_queue", i32), ("keep_results", i32), ("batch", BatchCfg)]
+
+
+class Cam(C.Structure):
+    """yc_cam (80 bytes: rows r1..r4 as float4, view_plane_dist, padding)"""
+    _fields_ = [("f", f32 * 20)]
+
+
+class RequestDesc(C.Structure):
+    """yc_request_desc"""
+    _fields_ = [("scene_id", i32), ("width", i32), ("height", i32), ("n_pass", i32), ("seeds_host", vp),
+                ("cam", Cam), ("cfg", PassCfg)]
+
+
+class RequestInfo(C.Structure):
+    """yc_request_info"""
+    _fields_ = [("state", i32), ("accum_id", i32), ("pixels_done", C.c_int64), ("pixels_total", C.c_int64),
+                ("submit_s", C.c_double), ("admit_s", C.c_double), ("finish_s", C.c_double)]
+
+
+# request states (YC_REQ_*)
+REQ_WAITING, REQ_RUNNING, REQ_CANCELLING, REQ_DONE, REQ_CANCELLED, REQ_REJECTED_BUDGET, REQ_REJECTED_QUEUE = range(7)
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     # core
@@ -88,6 +114,8 @@ SIGNATURES = {
     "yc_reset_stats": (i32, [vp]),
     "yc_last_pass_ms": (i32, [vp, C.POINTER(f32)]),
     "yc_device_allocations": (i32, [C.POINTER(C.c_uint64)]),
+    "yc_event_record": (i32, [vp, i32]),
+    "yc_event_elapsed_ms": (i32, [vp, i32, i32, C.POINTER(f32)]),
     "yc_set_profiling": (i32, [vp, i32]),
     "yc_set_option": (i32, [vp, i32, i32]),
     "yc_get_kernel_times": (i32, [vp, C.POINTER(KernelTimes)]),
@@ -99,6 +127,24 @@ SIGNATURES = {
     "yc_batch_job_progress": (i32, [vp, i32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "yc_batch_cancel_job": (i32, [vp, i32]),
     "yc_batch_destroy": (i32, [vp]),
+    # serving and admission
+    "yc_admission_create": (i32, [C.c_uint64, i32, C.POINTER(vp)]),
+    "yc_admission_submit": (i32, [vp, C.c_uint64, C.POINTER(C.c_int64), C.POINTER(i32)]),
+    "yc_admission_next": (i32, [vp, C.POINTER(C.c_int64)]),
+    "yc_admission_cancel": (i32, [vp, C.c_int64, C.POINTER(i32)]),
+    "yc_admission_finish": (i32, [vp, C.c_int64, C.POINTER(i32)]),
+    "yc_admission_state": (i32, [vp, C.c_int64, C.POINTER(i32)]),
+    "yc_admission_usage": (i32, [vp, C.POINTER(C.c_uint64), C.POINTER(i32), C.POINTER(i32)]),
+    "yc_admission_destroy": (i32, [vp]),
+    "yc_serve_create": (i32, [vp, C.POINTER(ServeCfg), C.POINTER(vp)]),
+    "yc_serve_submit": (i32, [vp, C.POINTER(RequestDesc), C.POINTER(C.c_int64), C.POINTER(i32)]),
+    "yc_serve_cancel": (i32, [vp, C.c_int64]),
+    "yc_serve_step": (i32, [vp, i32, C.POINTER(i32), C.POINTER(i32)]),
+    "yc_serve_info": (i32, [vp, C.c_int64, C.POINTER(RequestInfo)]),
+    "yc_serve_read": (i32, [vp, C.c_int64, vp]),
+    "yc_serve_release": (i32, [vp, C.c_int64]),
+    "yc_serve_clock": (C.c_double, [vp]),
+    "yc_serve_destroy": (i32, [vp]),
     # host producers
     "yh_bvh_build": (i32, [vp, i32, i32, i32, C.POINTER(vp)]),
     "yh_bvh_node_count": (i32, [vp]),

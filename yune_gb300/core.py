@@ -172,6 +172,16 @@ class Renderer:
         N.check(self.L.yc_set_option(self.h, 1, int(mode)), "yc_set_option")
         self.tree_mode = int(mode)
 
+    def event(self, slot):
+        """Records event `slot` (0..7) on the context stream after the work queued so far."""
+        N.check(self.L.yc_event_record(self.h, int(slot)), "yc_event_record")
+
+    def elapsed_ms(self, a, b):
+        """Device milliseconds between recorded events a and b (waits for b)."""
+        ms = C.c_float()
+        N.check(self.L.yc_event_elapsed_ms(self.h, int(a), int(b), C.byref(ms)), "yc_event_elapsed_ms")
+        return ms.value
+
     def set_max_rounds(self, n):
         """Rounds one pass may take before the call fails with YC_E_TIMEOUT (default 1,000,000)."""
         N.check(self.L.yc_set_option(self.h, 7, int(n)), "yc_set_option")

@@ -31,6 +31,15 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
+}  // namespace
+
+namespace yc {
+// the message of yc_last_error() for failures reported by the other host units (serve.cpp)
+int set_error(int code, const char* msg) { return fail(code, msg); }
+}  // namespace yc
+
+namespace {
+
 #define YC_CUDA(call)                                                                        \
   do {                                                                                       \
     cudaError_t e_ = (call);                                                                 \
@@ -91,6 +100,7 @@ struct yc_ctx {
   std::vector<yc_batch*> batches;   // owned: destroyed with the context
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t marks[8] = {};   // yc_event_record slots
   // the any-hit trace of a round runs on side_stream beside the closest-hit trace
   cudaStream_t side_stream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -529,6 +539,8 @@ int yc_destroy(yc_ctx* c) {
   if (c->overflow_host) cudaFreeHost(c->overflow_host);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  for (cudaEvent_t& e : c->marks)
+    if (e) cudaEventDestroy(e);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->side_stream) {
@@ -976,6 +988,21 @@ int yc_flush_l2(yc_ctx* c, size_t bytes) {
 int yc_measure_l2_gbs(yc_ctx* c, size_t bytes, int iters, double* gbs) {
   if (!c || !gbs || bytes < 4096 || iters < 1) return fail(YC_E_INVALID, "bad argument");
   if (yc::l2_read_gbs(bytes, iters, c->stream, gbs)) return fail(YC_E_LAUNCH, "L2 probe failed");
+  return YC_OK;
+}
+
+int yc_event_record(yc_ctx* c, int slot) {
+  if (!c || slot < 0 || slot >= 8) return fail(YC_E_INVALID, "slot must be 0..7");
+  if (!c->marks[slot]) YC_CUDA(cudaEventCreate(&c->marks[slot]));
+  YC_CUDA(cudaEventRecord(c->marks[slot], c->stream));
+  return YC_OK;
+}
+
+int yc_event_elapsed_ms(yc_ctx* c, int from, int to, float* ms) {
+  if (!c || !ms || from < 0 || from >= 8 || to < 0 || to >= 8) return fail(YC_E_INVALID, "bad argument");
+  if (!c->marks[from] || !c->marks[to]) return fail(YC_E_INVALID, "slot not recorded");
+  YC_CUDA(cudaEventSynchronize(c->marks[to]));
+  YC_CUDA(cudaEventElapsedTime(ms, c->marks[from], c->marks[to]));
   return YC_OK;
 }
 

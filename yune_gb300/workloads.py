@@ -45,7 +45,7 @@ def random_material(rng):
     return scenes.dielectric(float(rng.uniform(1.3, 1.7)))
 
 
-def mixed_scene(total_tris, seed, width, height, spp):
+def mixed_scene(total_tris, seed, width, height, spp, cfg=None):
     rng = np.random.default_rng(seed)
     b = scenes.Builder().cornell(seed=seed)
     for i, lv in enumerate(_sphere_levels(total_tris, rng)):
@@ -56,17 +56,33 @@ def mixed_scene(total_tris, seed, width, height, spp):
     tris, mats, lights = b.arrays()
     nodes, depth = scenes.build_bvh(tris, 20, 4)
     return scenes.SceneData(tris, mats, lights, nodes, depth, scenes.camera(), width, height, spp,
-                            scenes.default_cfg(max_depth=16), "mixed")
+                            dict(cfg) if cfg else scenes.default_cfg(max_depth=16), "mixed")
 
 
-def c2_jobs(n_jobs=64, spp=64, seed=0, max_tris=500_000):
+CORNELL_TRIS = 34   # five walls (10 triangles) and two boxes (24)
+
+
+def mixed_scene_tris(total_tris):
+    """The triangle count of mixed_scene(total_tris, ...), without building it."""
+    return CORNELL_TRIS + sum(20 * 4 ** lv for lv in _sphere_levels(total_tris, None))
+
+
+def c2_specs(n_jobs=64, seed=0, max_tris=500_000):
+    """(triangle target, scene seed, width, height) of each job of the mix."""
     rng = np.random.default_rng(seed)
     out = []
     for j in range(n_jobs):
         total = int(math.exp(rng.uniform(math.log(1000), math.log(max_tris))))
         w, h = RESOLUTIONS[int(rng.integers(0, len(RESOLUTIONS)))]
-        out.append(mixed_scene(total, seed * 100003 + j, w, h, spp))
+        out.append((total, seed * 100003 + j, w, h))
     return out
+
+
+def c2_jobs(n_jobs=64, spp=64, seed=0, max_tris=500_000, cfg=None, only=None):
+    """The mix's scenes; `only`: the indices of the jobs to build (all when None)."""
+    specs = c2_specs(n_jobs, seed, max_tris)
+    idx = range(n_jobs) if only is None else only
+    return [mixed_scene(specs[j][0], specs[j][1], specs[j][2], specs[j][3], spp, cfg) for j in idx]
 
 
 def c3_scenes(n_scenes=8, seed=1, min_tris=10_000, max_tris=2_000_000):
