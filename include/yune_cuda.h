@@ -311,13 +311,13 @@ typedef struct yc_serve_cfg {
                                   requests' scenes; give the deepest resident scene's) */
 } yc_serve_cfg;
 typedef struct yc_request_desc {
+  yc_cam cam;
+  yc_pass_cfg cfg;             /* integrator YC_UDPT */
   int32_t scene_id;            /* a scene uploaded to the server's context */
   int32_t width, height;
   int32_t n_pass;
   const uint32_t* seeds_host;  /* n_pass pass seeds (copied by yc_serve_submit) */
-  yc_cam cam;
-  yc_pass_cfg cfg;             /* integrator YC_UDPT */
-} yc_request_desc;
+} yc_request_desc;             /* 144 bytes, no padding */
 typedef struct yc_request_info {
   int32_t state;               /* YC_REQ_* */
   int32_t accum_id;            /* while running and, with keep_results, once done; else -1 */

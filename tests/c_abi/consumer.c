@@ -4,7 +4,8 @@
  * (plain structs, pointers and sizes; no C++ or torch types): it builds a scene with the
  * host producers, its BVH (BVH::createBVH), its device layout and a camera, refits the
  * BVH on the unmoved triangles (must not change a byte), writes and reads back a scene
- * cache file, writes a PNG, and opens a core context. Without a CUDA device yc_create must fail cleanly with
+ * cache file, writes a PNG, checks the request server's admission rules (host only) and
+ * opens a core context. Without a CUDA device yc_create must fail cleanly with
  * a negative code and a message; with one the context is created and destroyed.
  * Usage: consumer <scratch directory>. Prints "ok" and exits 0 when every check holds.
  */
@@ -142,6 +143,34 @@ int main(int argc, char** argv) {
   }
   CHECK(yc_upload_scene(NULL, tris, n_tri, mats, n_mat, nodes, n_node, lights, n_light, NULL) == YC_E_INVALID,
         "yc_upload_scene without a context");
+
+  /* the server's admission rules, host only: a budget for two 16 x 16 requests of two
+   * passes, one waiting place */
+  {
+    const uint64_t req = 16u * 16u * 16u + 8u;
+    yc_admission* adm = NULL;
+    CHECK(yc_admission_create(2 * req, 1, &adm) == YC_OK && adm, "yc_admission_create");
+    int64_t t[5];
+    int32_t st[5];
+    for (int i = 0; i < 4; ++i) CHECK(yc_admission_submit(adm, req, &t[i], &st[i]) == YC_OK, "submit");
+    CHECK(yc_admission_submit(adm, 64u * 64u * 16u + 8u, &t[4], &st[4]) == YC_OK, "submit large");
+    CHECK(st[0] == YC_REQ_RUNNING && st[1] == YC_REQ_RUNNING && st[2] == YC_REQ_WAITING &&
+              st[3] == YC_REQ_REJECTED_QUEUE && st[4] == YC_REQ_REJECTED_BUDGET,
+          "admission states");
+    int64_t next = 0;
+    CHECK(yc_admission_next(adm, &next) == YC_OK && next == -1, "nothing fits yet");
+    int32_t s = -1;
+    CHECK(yc_admission_cancel(adm, t[0], &s) == YC_OK && s == YC_REQ_CANCELLING, "cancel a running request");
+    CHECK(yc_admission_finish(adm, t[0], &s) == YC_OK && s == YC_REQ_CANCELLED, "its work drained");
+    CHECK(yc_admission_next(adm, &next) == YC_OK && next == t[2], "the waiting request is admitted");
+    uint64_t bytes = 0;
+    int32_t waiting = -1, running = -1;
+    CHECK(yc_admission_usage(adm, &bytes, &waiting, &running) == YC_OK && bytes == 2 * req && waiting == 0 &&
+              running == 2,
+          "bytes in use");
+    CHECK(yc_admission_finish(adm, t[3], &s) == YC_E_INVALID, "a rejected request holds nothing");
+    CHECK(yc_admission_destroy(adm) == YC_OK, "yc_admission_destroy");
+  }
 
   free(tris); free(mats); free(lights); free(nodes); free(refit);
   free(t2); free(m2); free(l2); free(nd2);

@@ -48,7 +48,7 @@ def test_cancelled_and_rejected_requests():
         srv.close()
         st = [q.status for q in done]
         assert st == ["cancelled", "cancelled", "done", "rejected: larger than the whole HBM budget"]
-        assert done[1].job == -1 and srv.in_use == 0
+        assert done[1].accum == -1 and srv.in_use == 0     # the waiting one never held an accumulator
         q = done[2]
         sid = r.upload(resident[0])
         r.set_camera(resident[0].cam)
@@ -56,3 +56,62 @@ def test_cancelled_and_rejected_requests():
         r.render_passes(sid, aid, scenes.pass_seeds(q.seed, q.spp), reset_first=1,
                         cfg=scenes.default_cfg(max_depth=16))
         assert np.array_equal(q.result.view(np.int32), r.read_accum(aid).view(np.int32))
+
+
+def test_server_starts_within_its_scene_budget():
+    resident = [scenes.c0(8, 8), scenes.c1(8, 8, level=3)]
+    need = sum(scenes.device_bytes(s) for s in resident)
+    with Renderer(0) as r:
+        srv = serve.Server(r, resident, hbm_budget=1 << 20, scene_budget=need, pool_paths=1024)
+        assert srv.scene_bytes == need == sum(r.scene_bytes(sid) for sid in srv.sids)
+        srv.close()
+
+
+def test_serve_c_abi_directly():
+    """yc_serve_* driven as a C host would: submit, step until done, read, release; the
+    result equals the lone render, and a finished request's bytes return to the budget."""
+    import ctypes as C
+    from yune_gb300 import _native as N
+    from yune_gb300.core import cfg_struct
+    s = scenes.c1(8, 8, level=3)
+    with Renderer(0) as r:
+        sid = r.upload(s)
+        L = r.L
+        bc = N.BatchCfg(2048, 2, 2, 1, 64, r.scene_depth(sid) + 2, 0, 1, 0)
+        sc = N.ServeCfg(24 * 20 * 16 + 64, -1, 1, bc)
+        h = C.c_void_p()
+        N.check(L.yc_serve_create(r.h, C.byref(sc), C.byref(h)), "create")
+        seeds = scenes.pass_seeds(9, 3)
+        d = N.RequestDesc()
+        C.memmove(C.byref(d.cam), s.cam.ctypes.data, C.sizeof(N.Cam))
+        d.cfg = cfg_struct(s.cfg)
+        d.scene_id, d.width, d.height, d.n_pass, d.seeds_host = sid, 24, 20, 3, seeds.ctypes.data
+        ids = []
+        for _ in range(2):
+            rid, st = C.c_int64(), C.c_int32()
+            N.check(L.yc_serve_submit(h, C.byref(d), C.byref(rid), C.byref(st)), "submit")
+            ids.append((rid.value, st.value))
+        assert [st for _, st in ids] == [N.REQ_RUNNING, N.REQ_WAITING]   # one fits the budget at a time
+        run, wait = C.c_int32(), C.c_int32()
+        info = N.RequestInfo()
+        for _ in range(10000):
+            N.check(L.yc_serve_step(h, 1, C.byref(run), C.byref(wait)), "step")
+            N.check(L.yc_serve_info(h, ids[0][0], C.byref(info)), "info")
+            if info.state == N.REQ_DONE:
+                break
+        assert info.state == N.REQ_DONE and info.pixels_done == info.pixels_total == 24 * 20
+        assert 0 <= info.submit_s <= info.admit_s <= info.finish_s
+        out = np.zeros((20, 24, 4), np.float32)
+        N.check(L.yc_serve_read(h, ids[0][0], out.ctypes.data), "read")
+        N.check(L.yc_serve_step(h, 0, C.byref(run), C.byref(wait)), "step")
+        N.check(L.yc_serve_info(h, ids[1][0], C.byref(info)), "info")
+        assert info.state == N.REQ_WAITING            # the first still holds its bytes (kept result)
+        N.check(L.yc_serve_release(h, ids[0][0]), "release")
+        N.check(L.yc_serve_step(h, 0, C.byref(run), C.byref(wait)), "step")
+        N.check(L.yc_serve_info(h, ids[1][0], C.byref(info)), "info")
+        assert info.state == N.REQ_RUNNING and wait.value == 0
+        N.check(L.yc_serve_destroy(h), "destroy")
+        r.set_camera(s.cam)
+        aid = r.alloc_accum(24, 20)
+        r.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+        assert np.array_equal(out.view(np.int32), r.read_accum(aid).view(np.int32))

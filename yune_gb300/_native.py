@@ -69,8 +69,8 @@ class Cam(C.Structure):
 
 class RequestDesc(C.Structure):
     """yc_request_desc"""
-    _fields_ = [("scene_id", i32), ("width", i32), ("height", i32), ("n_pass", i32), ("seeds_host", vp),
-                ("cam", Cam), ("cfg", PassCfg)]
+    _fields_ = [("cam", Cam), ("cfg", PassCfg), ("scene_id", i32), ("width", i32), ("height", i32), ("n_pass", i32),
+                ("seeds_host", vp)]
 
 
 class RequestInfo(C.Structure):

@@ -1,27 +1,31 @@
 """Render server: continuous batching of render requests over resident scenes.
 
-Requests (scene, resolution, target spp) arrive over time. A request is admitted when
-its accumulator fits the HBM budget left by the requests in flight; it then becomes a
-job of one long-lived batch (yune_gb300.batch), whose slots interleave the wavefronts of
-every admitted request and take new work as pixels finish, so requests that arrive
-while others run start as soon as memory frees up. Scenes stay resident; accumulators
-are freed when their request completes. Latency is arrival to completion of the target
-spp (the spp is the RMSE target: the estimate is the same at equal spp in any mix).
+A Python driver of the server in the C-ABI (yc_serve_*, core/serve.cpp): requests (scene,
+resolution, target spp) arrive over time; a request is admitted when its accumulator fits
+the HBM budget left by the requests in flight; it then becomes a job of one long-lived
+batch, whose slots interleave the wavefronts of every admitted request and take new work
+as pixels finish, so requests that arrive while others run start as soon as memory frees
+up. Scenes stay resident; accumulators are freed when their request completes. Latency
+is arrival to completion of the target spp (the spp is the RMSE target: the estimate is
+the same at equal spp in any mix).
 
-Failure handling, all on the host: a request whose accumulator exceeds the whole budget
-is rejected, as is one that arrives while `max_queue` requests already wait for memory;
-a request may carry a cancellation time (seconds after its arrival): still waiting, it is
-dropped; admitted, its job is cancelled in the engine (yc_batch_cancel_job: its pixels
-stop after their current pass) and its accumulator is freed once that work drains. Each
-request ends with status "done", "rejected: ..." or "cancelled".
+Failure handling, all on the host (the admission rules of yc_admission): a request whose
+accumulator exceeds the whole budget is rejected, as is one that arrives while
+`max_queue` requests already wait for memory; a request may carry a cancellation time
+(seconds after its arrival): still waiting, it is dropped; admitted, its job is cancelled
+in the engine (its pixels stop after their current pass) and its accumulator is freed
+once that work drains. Each request ends with status "done", "rejected: ..." or
+"cancelled".
 """
+import ctypes as C
 import time
 from dataclasses import dataclass, field
 
 import numpy as np
 
+from . import _native as N
 from . import scenes
-from .batch import Batch
+from .core import cfg_struct
 
 
 @dataclass
@@ -36,8 +40,8 @@ class Request:
     # filled in by the server
     admitted: float = -1.0
     done: float = -1.0
-    job: int = -1
-    accum: int = -1
+    job: int = -1                # the server's request id once submitted
+    accum: int = -1              # the accumulator while admitted (-1 once freed or never)
     status: str = "pending"
     result: np.ndarray = field(default=None, repr=False)
 
@@ -51,6 +55,11 @@ class Request:
 
     def cancelled_by(self, now):
         return self.cancel_after is not None and now >= self.arrival + self.cancel_after
+
+
+STATUS = {N.REQ_DONE: "done", N.REQ_CANCELLED: "cancelled",
+          N.REQ_REJECTED_BUDGET: "rejected: larger than the whole HBM budget",
+          N.REQ_REJECTED_QUEUE: "rejected: queue full"}
 
 
 class Server:
@@ -71,90 +80,148 @@ class Server:
                                  % (self.scene_bytes, scene_budget))
         self.sids = [renderer.upload(s) for s in resident]
         self.budget = int(hbm_budget)
-        self.in_use = 0
         self.keep = keep_results
         self.cfg = cfg or scenes.default_cfg(max_depth=16)
         cap = max(renderer.scene_depth(sid) for sid in self.sids) + 2
-        self.batch = Batch(renderer, pool_paths=pool_paths, rounds_per_launch=rounds_per_launch, max_jobs=4096,
-                           stack_cap=cap, logic_blocks_per_sm=logic_blocks_per_sm, sort_threshold=sort_threshold)
-        self.max_queue = max_queue   # requests waiting for memory beyond this are rejected
+        bc = N.BatchCfg(pool_paths, rounds_per_launch, logic_blocks_per_sm, 1, 1 << 16, cap, sort_threshold, 0, 0)
+        sc = N.ServeCfg(self.budget, -1 if max_queue is None else int(max_queue), int(bool(keep_results)), bc)
+        h = C.c_void_p()
+        self.L = renderer.L
+        N.check(self.L.yc_serve_create(renderer.h, C.byref(sc), C.byref(h)), "yc_serve_create")
+        self.h = h
+        self.max_queue = max_queue
+        self.in_use = 0          # accumulator bytes of the requests in flight
         self.max_in_flight = 0   # most requests admitted at once, and most accumulator bytes
         self.max_in_use = 0
 
-    def _admit(self, q, now):
-        if self.in_use + q.bytes > self.budget:
-            return False
-        s = self.scenes[q.scene]
-        q.accum = self.r.alloc_accum(q.width, q.height)
-        q.job = self.batch.add_job(self.sids[q.scene], q.accum, s.cam, scenes.pass_seeds(q.seed, q.spp), self.cfg)
-        q.admitted = now
-        self.in_use += q.bytes
-        self.max_in_use = max(self.max_in_use, self.in_use)
-        return True
+    def info(self, q):
+        i = N.RequestInfo()
+        N.check(self.L.yc_serve_info(self.h, q.job, C.byref(i)), "yc_serve_info")
+        return i
 
-    def _arrive(self, q, waiting, live, now):
-        if q.bytes > self.budget:
-            q.status, q.done = "rejected: larger than the whole HBM budget", now
-        elif not waiting and self._admit(q, now):
-            q.status = "running"
-            live.append(q)
-        elif self.max_queue is not None and len(waiting) >= self.max_queue:
-            q.status, q.done = "rejected: queue full", now
-        else:
-            waiting.append(q)
+    def _submit(self, q):
+        s = self.scenes[q.scene]
+        seeds = scenes.pass_seeds(q.seed, q.spp)
+        d = N.RequestDesc()
+        d.scene_id = self.sids[q.scene]
+        d.width, d.height, d.n_pass = q.width, q.height, q.spp
+        d.seeds_host = seeds.ctypes.data
+        C.memmove(C.byref(d.cam), s.cam.ctypes.data, C.sizeof(N.Cam))
+        d.cfg = cfg_struct(self.cfg)
+        rid, st = C.c_int64(), C.c_int32()
+        N.check(self.L.yc_serve_submit(self.h, C.byref(d), C.byref(rid), C.byref(st)), "yc_serve_submit")
+        q.job = rid.value
+        return st.value
 
     def run(self, requests, clock=time.perf_counter):
         """Serves the requests in real time; returns them (sorted by arrival) with their
         status and completion time."""
         pending = sorted(requests, key=lambda q: q.arrival)
-        waiting, live = [], []
+        open_ = []   # submitted, not finished
         t0 = clock()
         i = 0
-        while i < len(pending) or waiting or live:
+        running, waiting = C.c_int32(), C.c_int32()
+        while i < len(pending) or open_:
             now = clock() - t0
             while i < len(pending) and pending[i].arrival <= now:
-                self._arrive(pending[i], waiting, live, now)
-                i += 1
-            # cancellations: waiting requests are dropped, admitted ones stop in the engine
-            for q in [q for q in waiting if q.cancelled_by(now)]:
-                waiting.remove(q)
-                q.status, q.done = "cancelled", now
-            for q in live:
-                if q.status == "running" and q.cancelled_by(now):
-                    self.batch.cancel(q.job)
-                    q.status = "cancelling"
-            # admission in arrival order while memory allows
-            while waiting and self._admit(waiting[0], now):
-                q = waiting.pop(0)
-                q.status = "running"
-                live.append(q)
-            self.max_in_flight = max(self.max_in_flight, len(live))
-            if not live:   # (a waiting request always fits an empty budget)
-                if i < len(pending):
-                    time.sleep(max(0.0, pending[i].arrival - (clock() - t0)))
-                continue
-            self.batch.run(max_launches=1)
-            now = clock() - t0
-            still = []
-            for q in live:
-                d, tot = self.batch.progress(q.job)
-                if d >= tot:
-                    q.done = now
-                    if q.status == "cancelling":
-                        q.status = "cancelled"
-                    else:
-                        q.status = "done"
-                        if self.keep:
-                            q.result = self.r.read_accum(q.accum)
-                    self.r.free_accum(q.accum)
-                    self.in_use -= q.bytes
+                q = pending[i]
+                st = self._submit(q)
+                if st in (N.REQ_REJECTED_BUDGET, N.REQ_REJECTED_QUEUE):
+                    q.status, q.done = STATUS[st], now
                 else:
+                    q.status = "waiting" if st == N.REQ_WAITING else "running"
+                    open_.append(q)
+                i += 1
+            for q in open_:
+                if q.status in ("waiting", "running") and q.cancelled_by(now):
+                    N.check(self.L.yc_serve_cancel(self.h, q.job), "yc_serve_cancel")
+                    q.status = "cancelling"
+            has_work = any(q.status in ("running", "cancelling", "waiting") for q in open_)
+            N.check(self.L.yc_serve_step(self.h, 1 if has_work else 0, C.byref(running), C.byref(waiting)),
+                    "yc_serve_step")
+            now = clock() - t0
+            still, in_use = [], 0
+            for q in open_:
+                inf = self.info(q)
+                if inf.admit_s >= 0 and q.admitted < 0:
+                    q.admitted = now
+                if inf.state in (N.REQ_RUNNING, N.REQ_CANCELLING):
+                    q.accum = inf.accum_id
+                    in_use += q.bytes
+                if inf.state in (N.REQ_DONE, N.REQ_CANCELLED):
+                    q.done, q.status = now, STATUS[inf.state]
+                    if inf.state == N.REQ_DONE and self.keep:
+                        q.result = np.zeros((q.height, q.width, 4), np.float32)
+                        N.check(self.L.yc_serve_read(self.h, q.job, q.result.ctypes.data), "yc_serve_read")
+                        N.check(self.L.yc_serve_release(self.h, q.job), "yc_serve_release")
+                else:
+                    if inf.state == N.REQ_RUNNING and q.status == "waiting":
+                        q.status = "running"
                     still.append(q)
-            live = still
+            open_ = still
+            self.in_use = in_use
+            self.max_in_use = max(self.max_in_use, in_use)
+            self.max_in_flight = max(self.max_in_flight, running.value)
+            if not open_ and i < len(pending):
+                time.sleep(max(0.0, pending[i].arrival - (clock() - t0)))
         return pending
 
     def close(self):
-        self.batch.close()
+        if getattr(self, "h", None):
+            self.L.yc_serve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Admission:
+    """The admission rules alone (yc_admission_*), on the host: no device needed."""
+
+    def __init__(self, budget, max_queue=None):
+        h = C.c_void_p()
+        L = N.lib()
+        N.check(L.yc_admission_create(int(budget), -1 if max_queue is None else int(max_queue), C.byref(h)),
+                "yc_admission_create")
+        self.L, self.h = L, h
+
+    def submit(self, nbytes):
+        t, st = C.c_int64(), C.c_int32()
+        N.check(self.L.yc_admission_submit(self.h, int(nbytes), C.byref(t), C.byref(st)), "yc_admission_submit")
+        return t.value, st.value
+
+    def next(self):
+        t = C.c_int64()
+        N.check(self.L.yc_admission_next(self.h, C.byref(t)), "yc_admission_next")
+        return t.value
+
+    def cancel(self, t):
+        st = C.c_int32()
+        N.check(self.L.yc_admission_cancel(self.h, int(t), C.byref(st)), "yc_admission_cancel")
+        return st.value
+
+    def finish(self, t):
+        st = C.c_int32()
+        N.check(self.L.yc_admission_finish(self.h, int(t), C.byref(st)), "yc_admission_finish")
+        return st.value
+
+    def state(self, t):
+        st = C.c_int32()
+        N.check(self.L.yc_admission_state(self.h, int(t), C.byref(st)), "yc_admission_state")
+        return st.value
+
+    def usage(self):
+        b, w, r = C.c_uint64(), C.c_int32(), C.c_int32()
+        N.check(self.L.yc_admission_usage(self.h, C.byref(b), C.byref(w), C.byref(r)), "yc_admission_usage")
+        return b.value, w.value, r.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.yc_admission_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 def serve_plain(renderer, resident, requests, cfg=None, clock=time.perf_counter, keep_results=False):
