@@ -103,6 +103,19 @@ void parallel_for(size_t n, F f) {
 }
 
 bool is_leaf(const yc_bvh_node& n) { return (float)n.child_idx == -1.0f && n.vert_len > 0; }
+
+// One two-child node of yc_scene.h: per axis the pair (child 0, child 1) of lower bounds,
+// then the pair of upper bounds, so that each 64-bit half of a float4 is the pair one
+// packed f32x2 operation takes; then the two links.
+void write_node2(float4* o, const float lo0[3], const float hi0[3], const float lo1[3], const float hi1[3], int l0,
+                 int l1) {
+  for (int k = 0; k < 3; ++k) o[k] = float4{lo0[k], lo1[k], hi0[k], hi1[k]};
+  float4 l;
+  std::memcpy(&l.x, &l0, 4);
+  std::memcpy(&l.y, &l1, 4);
+  l.z = l.w = 0.0f;
+  o[3] = l;
+}
 bool is_queued(const yc_bvh_node& n) { return n.vert_len > 0 || n.child_idx > 0; }
 
 // ---- SAH hierarchy over the reference leaves ----
@@ -344,15 +357,7 @@ struct SahBuilder {
       c0 = emit_binary_at(a, out, node + 1);
       c1 = emit_binary_at(b, out, node + 1 + left_nodes);
     }
-    float4* o = &out[4 * (size_t)node];
-    o[0] = float4{a.lo[0], a.hi[0], a.lo[1], a.hi[1]};
-    o[1] = float4{b.lo[0], b.hi[0], b.lo[1], b.hi[1]};
-    o[2] = float4{a.lo[2], a.hi[2], b.lo[2], b.hi[2]};
-    float4 l;
-    std::memcpy(&l.x, &c0, 4);
-    std::memcpy(&l.y, &c1, 4);
-    l.z = l.w = 0.0f;
-    o[3] = l;
+    write_node2(&out[4 * (size_t)node], a.lo, a.hi, b.lo, b.hi, c0, c1);
     return node;
   }
 
@@ -449,15 +454,10 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
         } else {
           next = (int)(b.out_nodes.size() / 4) + 1;
         }
-        int l0 = leaf, l1 = next;
-        float4 n0{-INF, INF, -INF, INF}, n1{-INF, INF, -INF, INF}, n2{-INF, INF, -INF, INF}, n3;
-        std::memcpy(&n3.x, &l0, 4);
-        std::memcpy(&n3.y, &l1, 4);
-        n3.z = n3.w = 0.0f;
-        b.out_nodes.push_back(n0);
-        b.out_nodes.push_back(n1);
-        b.out_nodes.push_back(n2);
-        b.out_nodes.push_back(n3);
+        const float lo[3] = {-INF, -INF, -INF}, hi[3] = {INF, INF, INF};
+        const size_t at = b.out_nodes.size();
+        b.out_nodes.resize(at + 4);
+        write_node2(&b.out_nodes[at], lo, hi, lo, hi, leaf, next);
       }
       out.root_link = 0;
     }
@@ -598,15 +598,8 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
       else if (is_leaf(ch)) link[c] = b.emit_leaf(ch.vert_list, ch.vert_len, ci * 16);
       else link[c] = packed_of[ci];
     }
-    float4* o = &b.out_nodes[4 * q];
-    o[0] = float4{box[0]->p_min.x, box[0]->p_max.x, box[0]->p_min.y, box[0]->p_max.y};
-    o[1] = float4{box[1]->p_min.x, box[1]->p_max.x, box[1]->p_min.y, box[1]->p_max.y};
-    o[2] = float4{box[0]->p_min.z, box[0]->p_max.z, box[1]->p_min.z, box[1]->p_max.z};
-    float4 l;
-    std::memcpy(&l.x, &link[0], 4);
-    std::memcpy(&l.y, &link[1], 4);
-    l.z = l.w = 0.0f;
-    o[3] = l;
+    write_node2(&b.out_nodes[4 * q], &box[0]->p_min.x, &box[0]->p_max.x, &box[1]->p_min.x, &box[1]->p_max.x, link[0],
+                link[1]);
     if ((b.out_tris.size() / 3) >= (size_t)(1 << 27)) { err = "scene too large for the 27-bit stream index"; return -1; }
   }
   out.root_link = 0;

@@ -4,10 +4,12 @@
 // 128-bit loads:
 //   nodes   two-child layout: 4 x float4 (64 B) per interior node, holding the boxes
 //           of its two children (the 32 B a box test reads) and their links:
-//             n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
-//             n1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
-//             n2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//             n0 = (c0.lo.x, c1.lo.x, c0.hi.x, c1.hi.x)
+//             n1 = (c0.lo.y, c1.lo.y, c0.hi.y, c1.hi.y)
+//             n2 = (c0.lo.z, c1.lo.z, c0.hi.z, c1.hi.z)
 //             n3 = (link0, link1, 0, 0) as int bits
+//           (each 64-bit half is the (child 0, child 1) pair one packed f32x2 operation
+//           of the box test takes)
 //           link >= 0: interior node index; link < 0: leaf, ~link = (first stream slot
 //           << 4) | triangle count (a reference leaf holds at most 10); LINK_NONE: a
 //           child the reference never queues (vert_len <= 0 and child_idx <= 0,

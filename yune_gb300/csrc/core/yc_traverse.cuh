@@ -39,6 +39,33 @@ struct WalkCount {
   unsigned nodes = 0, tris = 0;
 };
 
+// ---- packed pairs: the f32x2 operations of sm_100 and later apply the IEEE
+// round-to-nearest operation to each 32-bit half of a 64-bit register, so one packed
+// operation gives exactly the bits of the two scalar operations it replaces, at one
+// instruction issue. The two-child node stores its bounds as (child 0, child 1) pairs.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void up2(f32x2 v, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v)); }
+__device__ __forceinline__ float lo2(f32x2 v) {
+  float a, b;
+  up2(v, a, b);
+  return a;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+
 // OpenCL `min` (y if y < x, otherwise x); NaN-sensitive like the reference.
 __device__ __forceinline__ float ocl_min(float x, float y) { return (y < x) ? y : x; }
 // OpenCL `fmax` (NaN operand ignored; ties keep x).
@@ -66,6 +93,20 @@ __device__ __forceinline__ bool box_ref(float ox, float oy, float oz, float ix, 
   return t_max > ocl_fmax(t_min, 0.0f);
 }
 
+// rayAabbIntersection on the slab values a = (lo - o) * inv and b = (hi - o) * inv of each
+// axis (computed by the caller, possibly two boxes at a time with packed operations):
+// box_ref's NaN-skipping arithmetic
+__device__ __forceinline__ bool box_ref_ab(float ax, float bx, float ay, float by, float az, float bz,
+                                           float& tentry) {
+  float t_max = __int_as_float(0x7f800000), t_min = -__int_as_float(0x7f800000);
+  if (!(ax != ax)) { t_min = ocl_fmax(ocl_min(ax, bx), t_min); t_max = ocl_min(ocl_fmax(ax, bx), t_max); }
+  if (!(ay != ay)) { t_min = ocl_fmax(ocl_min(ay, by), t_min); t_max = ocl_min(ocl_fmax(ay, by), t_max); }
+  if (t_max < t_min) { tentry = t_min; return false; }
+  if (!(az != az)) { t_min = ocl_fmax(ocl_min(az, bz), t_min); t_max = ocl_min(ocl_fmax(az, bz), t_max); }
+  tentry = t_min;
+  return t_max > ocl_fmax(t_min, 0.0f);
+}
+
 // minimum and maximum of three (the three-operand PTX forms of sm_100 measured no
 // faster here)
 __device__ __forceinline__ float max3f(float a, float b, float c) { return fmaxf(fmaxf(a, b), c); }
@@ -86,6 +127,16 @@ __device__ __forceinline__ bool box_fast(float ox, float oy, float oz, float ix,
   const float ax = __fmul_rn(__fsub_rn(lx, ox), ix), bx = __fmul_rn(__fsub_rn(hx, ox), ix);
   const float ay = __fmul_rn(__fsub_rn(ly, oy), iy), by = __fmul_rn(__fsub_rn(hy, oy), iy);
   const float az = __fmul_rn(__fsub_rn(lz, oz), iz), bz = __fmul_rn(__fsub_rn(hz, oz), iz);
+  const float t0 = max3f(fminf(ax, bx), fminf(ay, by), fminf(az, bz));
+  const float t1 = min3f(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), cull_up));
+  const float t0c = fmaxf(t0, 0.0f);
+  tentry = clamp ? t0c : t0;
+  return t1 > t0c;
+}
+
+// box_fast on slab values (see box_ref_ab)
+__device__ __forceinline__ bool box_fast_ab(float ax, float bx, float ay, float by, float az, float bz,
+                                            float cull_up, bool clamp, float& tentry) {
   const float t0 = max3f(fminf(ax, bx), fminf(ay, by), fminf(az, bz));
   const float t1 = min3f(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), cull_up));
   const float t0c = fmaxf(t0, 0.0f);
@@ -141,7 +192,14 @@ __device__ __forceinline__ float cull_up(float best) {
 struct Walk {
   const float4* nodes;   // the scene of this ray (lanes of one warp may walk different scenes)
   const float4* tris;
-  float ox, oy, oz, dx, dy, dz, ix, iy, iz;
+  float dx, dy, dz;
+  f32x2 ox2, oy2, oz2, ix2, iy2, iz2;   // origin and 1/direction, each component twice (packed box tests)
+  __device__ __forceinline__ float ox() const { return lo2(ox2); }
+  __device__ __forceinline__ float oy() const { return lo2(oy2); }
+  __device__ __forceinline__ float oz() const { return lo2(oz2); }
+  __device__ __forceinline__ float ix() const { return lo2(ix2); }
+  __device__ __forceinline__ float iy() const { return lo2(iy2); }
+  __device__ __forceinline__ float iz() const { return lo2(iz2); }
   float best, bu, bv;
   float best_up;         // cull_up(best)
   int best_tri, best_rank;
@@ -153,10 +211,12 @@ struct Walk {
 __device__ __forceinline__ void walk_begin(const DevScene& sc, const RayIn& r, Walk& w) {
   w.nodes = sc.nodes;
   w.tris = sc.tris;
-  w.ox = r.ox; w.oy = r.oy; w.oz = r.oz;
+
   w.dx = r.dx; w.dy = r.dy; w.dz = r.dz;
-  w.ix = __frcp_rn(r.dx); w.iy = __frcp_rn(r.dy); w.iz = __frcp_rn(r.dz);
-  w.exact = isinf(w.ix) || isinf(w.iy) || isinf(w.iz);
+  const float ix = __frcp_rn(r.dx), iy = __frcp_rn(r.dy), iz = __frcp_rn(r.dz);
+  w.exact = isinf(ix) || isinf(iy) || isinf(iz);
+  w.ox2 = pk2(r.ox, r.ox); w.oy2 = pk2(r.oy, r.oy); w.oz2 = pk2(r.oz, r.oz);
+  w.ix2 = pk2(ix, ix); w.iy2 = pk2(iy, iy); w.iz2 = pk2(iz, iz);
   w.best = r.tmax; w.bu = 0.0f; w.bv = 0.0f;
   w.best_up = cull_up(r.tmax);
   w.best_tri = -1; w.best_rank = -1;
@@ -165,9 +225,9 @@ __device__ __forceinline__ void walk_begin(const DevScene& sc, const RayIn& r, W
   w.link_t = -__int_as_float(0x7f800000);
   if (w.link != LINK_NONE && sc.root_test) {
     float te;
-    const bool h = w.exact ? box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, sc.root_lo.x, sc.root_hi.x, sc.root_lo.y,
+    const bool h = w.exact ? box_ref(w.ox(), w.oy(), w.oz(), w.ix(), w.iy(), w.iz(), sc.root_lo.x, sc.root_hi.x, sc.root_lo.y,
                                      sc.root_hi.y, sc.root_lo.z, sc.root_hi.z, te)
-                           : box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, sc.root_lo.x, sc.root_hi.x, sc.root_lo.y,
+                           : box_fast(w.ox(), w.oy(), w.oz(), w.ix(), w.iy(), w.iz(), sc.root_lo.x, sc.root_hi.x, sc.root_lo.y,
                                       sc.root_hi.y, sc.root_lo.z, sc.root_hi.z, __int_as_float(0x7f800000), false, te);
     if (!h) w.link = LINK_NONE;
   }
@@ -185,7 +245,7 @@ __device__ __forceinline__ bool walk_leaf(Walk& w, int link, WalkCount& wc, bool
     const float4 b = __ldg(tp + 3 * k + 1);
     const float4 c = __ldg(tp + 3 * k + 2);
     TriHit th;
-    if (tri_test(w.ox, w.oy, w.oz, w.dx, w.dy, w.dz, a, b, c, w.best, w.best_rank, th)) {
+    if (tri_test(w.ox(), w.oy(), w.oz(), w.dx, w.dy, w.dz, a, b, c, w.best, w.best_rank, th)) {
       w.best = th.t;
       w.best_up = cull_up(th.t);
       w.bu = th.u;
@@ -223,19 +283,27 @@ __device__ __forceinline__ int walk_recheck(Walk& w, int link, const int* stack,
 __device__ __forceinline__ int visit2(Walk& w, bool any, int link, int* stack, int stride, int stack_cap,
                                       WalkCount& wc, bool& overflow) {
   const float4* nd = w.nodes + 4 * (size_t)link;
-  const float4 n0 = __ldg(nd + 0);
-  const float4 n1 = __ldg(nd + 1);
-  const float4 n2 = __ldg(nd + 2);
+  const ulonglong2 nx = __ldg(reinterpret_cast<const ulonglong2*>(nd + 0));   // (lo pair, hi pair)
+  const ulonglong2 ny = __ldg(reinterpret_cast<const ulonglong2*>(nd + 1));
+  const ulonglong2 nz = __ldg(reinterpret_cast<const ulonglong2*>(nd + 2));
   const int2 n3 = __ldg(reinterpret_cast<const int2*>(nd + 3));
   wc.nodes += 2;
+  // (lo - o) * inv and (hi - o) * inv of both children, two packed operations per bound
+  float ax0, ax1, bx0, bx1, ay0, ay1, by0, by1, az0, az1, bz0, bz1;
+  up2(mul2(sub2(nx.x, w.ox2), w.ix2), ax0, ax1);
+  up2(mul2(sub2(nx.y, w.ox2), w.ix2), bx0, bx1);
+  up2(mul2(sub2(ny.x, w.oy2), w.iy2), ay0, ay1);
+  up2(mul2(sub2(ny.y, w.oy2), w.iy2), by0, by1);
+  up2(mul2(sub2(nz.x, w.oz2), w.iz2), az0, az1);
+  up2(mul2(sub2(nz.y, w.oz2), w.iz2), bz0, bz1);
   float t0, t1;
   bool h0, h1;
   if (!w.exact) {   // hit and within the cull bound
-    h0 = box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, w.best_up, !any, t0);
-    h1 = box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, w.best_up, !any, t1);
+    h0 = box_fast_ab(ax0, bx0, ay0, by0, az0, bz0, w.best_up, !any, t0);
+    h1 = box_fast_ab(ax1, bx1, ay1, by1, az1, bz1, w.best_up, !any, t1);
   } else {
-    h0 = box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, t0);
-    h1 = box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, t1);
+    h0 = box_ref_ab(ax0, bx0, ay0, by0, az0, bz0, t0);
+    h1 = box_ref_ab(ax1, bx1, ay1, by1, az1, bz1, t1);
     const float cb = cull_bound(w.best);
     h0 = h0 && !(t0 > cb);
     h1 = h1 && !(t1 > cb);
@@ -286,9 +354,9 @@ __device__ __forceinline__ int visit4(Walk& w, bool any, int link, int* stack, i
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     float te;
-    bool h = !w.exact ? box_fast(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, clx[c], chx[c], cly[c], chy[c], clz[c], chz[c],
+    bool h = !w.exact ? box_fast(w.ox(), w.oy(), w.oz(), w.ix(), w.iy(), w.iz(), clx[c], chx[c], cly[c], chy[c], clz[c], chz[c],
                                  w.best_up, !any, te)
-                      : box_ref(w.ox, w.oy, w.oz, w.ix, w.iy, w.iz, clx[c], chx[c], cly[c], chy[c], clz[c], chz[c], te);
+                      : box_ref(w.ox(), w.oy(), w.oz(), w.ix(), w.iy(), w.iz(), clx[c], chx[c], cly[c], chy[c], clz[c], chz[c], te);
     h = h && cl[c] != LINK_NONE && !(te > cb);
     t[c] = h ? te : INF;
     l[c] = h ? cl[c] : LINK_NONE;
