@@ -65,9 +65,19 @@ __device__ __forceinline__ void camera_ray(const PassParams& pp, int px, int py,
   light_test(pp.sc, o, d, len, k);
 }
 
+// Fields of the path record a step rewrote (stored back when the step emits a ray).
+enum : unsigned {
+  D_THR = 1, D_THR_NEXT = 2, D_DIRECT = 4, D_INDIRECT = 8, D_LS = 16, D_HP = 32, D_NRM = 64, D_WO = 128, D_WI = 256
+};
+
 // One step of path p: runs its state machine from the result of its last ray until it
 // needs the next one. Returns 1 (closest-hit ray written to the path state), 2 (any-hit
 // ray) or 0 (the path finished and its colour went into the accumulator).
+// The step loads only the record fields its entry state can read before writing them
+// (a camera-ray result reads the ray and the hit; an extension result does not read the
+// last vertex's shading frame, light sample or densities; a shadow or MIS result does not
+// read the ray it traced) and stores only the fields it changed: the record is the same,
+// with fewer bytes moved (pass starts write the misc word and the ray only).
 __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const PathState& ps, int p, LogicCounts& cnt) {
   const DevScene& sc = pp.sc;
   const f4 BG = ym::mk(0.4f, 0.4f, 0.4f, 1.0f);
@@ -82,10 +92,16 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
   int j = ((misc.z >> 12) & 0xff) - 1;
   int k = ((misc.z >> 20) & 0xff) - 1;
   int bounce = misc.w;
-  f4 thr = f4of(ps.thr[p]), thr_next = f4of(ps.thr_next[p]);
-  f4 direct = f4of(ps.direct[p]), indirect = f4of(ps.indirect[p]);
-  f4 ls = f4of(ps.ls[p]);
-  const float4 hp4 = ps.hp[p], n4 = ps.nrm[p], wo4 = ps.wo[p], wi4 = ps.wi[p];
+  const bool enter_cam = phase == S_PRIMARY, enter_ext = phase == S_EXT;
+  const bool enter_nee = phase == S_NEE_SHADOW || phase == S_NEE_MIS;
+  unsigned dirty = 0;
+  const float4 Z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  f4 thr = f4of(enter_cam ? Z4 : ps.thr[p]);
+  f4 thr_next = f4of(enter_ext ? ps.thr_next[p] : Z4);
+  f4 direct = f4of(enter_cam ? Z4 : ps.direct[p]), indirect = f4of(enter_cam ? Z4 : ps.indirect[p]);
+  f4 ls = f4of(phase == S_NEE_MIS ? ps.ls[p] : Z4);
+  const float4 hp4 = enter_nee ? ps.hp[p] : Z4, n4 = enter_nee ? ps.nrm[p] : Z4;
+  const float4 wo4 = enter_nee ? ps.wo[p] : Z4, wi4 = enter_nee ? ps.wi[p] : Z4;
   Vtx V;
   V.hp = ym::mk(hp4.x, hp4.y, hp4.z, 1.0f);
   V.n = ym::mk(n4.x, n4.y, n4.z, 0.0f);
@@ -93,7 +109,7 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
   float light_pdf = hp4.w, brdf_prob = n4.w, brdf_pdf = wo4.w;
   f4 wo = ym::mk(wo4.x, wo4.y, wo4.z, -0.0f);
   f4 w_i = ym::mk(wi4.x, wi4.y, wi4.z, 0.0f);
-  const float4 ro4 = ps.ro[p], rd4 = ps.rd[p];
+  const float4 ro4 = enter_nee ? Z4 : ps.ro[p], rd4 = enter_nee ? Z4 : ps.rd[p];
   f4 ro = ym::mk(ro4.x, ro4.y, ro4.z, 1.0f);
   f4 rd = ym::mk(rd4.x, rd4.y, rd4.z, rd4.w);
   float tmax = ro4.w;
@@ -114,6 +130,7 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
           bounce = 0;
           wo = -rd;
           flags = 0;
+          dirty |= D_THR | D_DIRECT | D_INDIRECT | D_HP | D_NRM | D_WO | D_WI;
           if (!sc.mats[V.mat].is_specular) phase = P_NEE_BEGIN;
           else phase = pp.gi_check ? P_GI_SAMPLE : P_FINISH;
           if (phase == P_FINISH) color = direct + indirect;
@@ -131,6 +148,7 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
         const yc_material& m = sc.mats[V.mat];
         f4 wi_raw;
         j = sample_lights(sc, V, seed, light_pdf, wi_raw);
+        dirty |= D_HP;   // light_pdf
         if (j == -1 || light_pdf <= 0.0f) {
           dl = ld4(m.ke);
           phase = P_NEE_DELIVER;
@@ -142,8 +160,8 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
         ro = V.hp + w_i * EPS_F;
         rd = w_i;
         tmax = len;
-        ls = ym::splat(0.0f);
         flags &= ~(F_NEE_GLOSSY | F_OCCLUDED);
+        dirty |= D_WI;
         cnt.rays++; cnt.shadow++;
         int lk = -1;
         float tl = len;
@@ -160,6 +178,8 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
         break;
       }
       case S_NEE_SHADOW: {
+        ls = ym::splat(0.0f);   // the light sample of this shadow ray (zero while occluded)
+        dirty |= D_LS | D_NRM | D_WO;   // ls, brdf_prob, brdf_pdf
         if (hit.x != 0.0f) flags |= F_OCCLUDED;
         const yc_material& m = sc.mats[V.mat];
         const f4 em = ld4(m.ke);
@@ -188,6 +208,7 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
         else bdir = sample_cosine(V, seed, brdf_pdf);
         if (brdf_pdf <= 0.0f) { dl = ls + em; phase = P_NEE_DELIVER; break; }
         w_i = bdir;
+        dirty |= D_WI;
         cnt.rays++; cnt.mis++;
         // closest light along the BRDF ray; only light j can satisfy the test
         ro = V.hp + bdir * EPS_F;
@@ -218,8 +239,8 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
         break;
       }
       case P_NEE_DELIVER: {
-        if (flags & F_TARGET_INDIRECT) indirect = indirect + thr * dl;
-        else direct = dl;
+        if (flags & F_TARGET_INDIRECT) { indirect = indirect + thr * dl; dirty |= D_INDIRECT; }
+        else { direct = dl; dirty |= D_DIRECT; }
         if (!pp.gi_check) { color = direct + indirect; phase = P_FINISH; }
         else phase = P_GI_SAMPLE;
         break;
@@ -254,6 +275,7 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
         if (pdf <= 0.0f) { color = direct + indirect; phase = P_FINISH; break; }
         if (spec) thr_next = thr * ior;
         else thr_next = ((thr * brdf(nd, wo, V, m, glossy, prob, pp.brdf_model)) * ym::fmax(ym::dot(nd, V.n), 0.0f)) / pdf;
+        dirty |= D_THR_NEXT;
         flags = spec ? (flags | F_SPEC) : (flags & ~F_SPEC);
         ro = V.hp + nd * EPS_F;
         rd = nd;
@@ -272,7 +294,7 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
         const int tri = __float_as_int(hit.w);
         const bool spec = (flags & F_SPEC) != 0;
         if (tri < 0) {
-          if (spec && k >= 0) indirect = indirect + thr * ld4(sc.lights[k].ke);
+          if (spec && k >= 0) { indirect = indirect + thr * ld4(sc.lights[k].ke); dirty |= D_INDIRECT; }
           color = direct + indirect;
           phase = P_FINISH;
           break;
@@ -280,6 +302,7 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
         const Vtx NV = tri_vertex(sc, ro, rd, hit.x, hit.y, hit.z, tri);
         indirect = indirect + thr * ld4(sc.mats[NV.mat].ke);
         thr = thr_next;
+        dirty |= D_THR | D_INDIRECT | D_HP | D_NRM | D_WO | D_WI;   // new vertex
         if (bounce > pp.rr_threshold) {
           const float pr = ym::min(luminance(thr), 0.95f);
           const float r = draw(seed);
@@ -315,15 +338,15 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
   }
   if (emit) {
     ps.misc[p] = make_int4((int)seed, pix, pack_misc(phase, flags, j, k), bounce);
-    ps.thr[p] = make_float4(thr.x, thr.y, thr.z, thr.w);
-    ps.thr_next[p] = make_float4(thr_next.x, thr_next.y, thr_next.z, thr_next.w);
-    ps.direct[p] = make_float4(direct.x, direct.y, direct.z, direct.w);
-    ps.indirect[p] = make_float4(indirect.x, indirect.y, indirect.z, indirect.w);
-    ps.ls[p] = make_float4(ls.x, ls.y, ls.z, ls.w);
-    ps.hp[p] = make_float4(V.hp.x, V.hp.y, V.hp.z, light_pdf);
-    ps.nrm[p] = make_float4(V.n.x, V.n.y, V.n.z, brdf_prob);
-    ps.wo[p] = make_float4(wo.x, wo.y, wo.z, brdf_pdf);
-    ps.wi[p] = make_float4(w_i.x, w_i.y, w_i.z, __int_as_float(V.mat));
+    if (dirty & D_THR) ps.thr[p] = make_float4(thr.x, thr.y, thr.z, thr.w);
+    if (dirty & D_THR_NEXT) ps.thr_next[p] = make_float4(thr_next.x, thr_next.y, thr_next.z, thr_next.w);
+    if (dirty & D_DIRECT) ps.direct[p] = make_float4(direct.x, direct.y, direct.z, direct.w);
+    if (dirty & D_INDIRECT) ps.indirect[p] = make_float4(indirect.x, indirect.y, indirect.z, indirect.w);
+    if (dirty & D_LS) ps.ls[p] = make_float4(ls.x, ls.y, ls.z, ls.w);
+    if (dirty & D_HP) ps.hp[p] = make_float4(V.hp.x, V.hp.y, V.hp.z, light_pdf);
+    if (dirty & D_NRM) ps.nrm[p] = make_float4(V.n.x, V.n.y, V.n.z, brdf_prob);
+    if (dirty & D_WO) ps.wo[p] = make_float4(wo.x, wo.y, wo.z, brdf_pdf);
+    if (dirty & D_WI) ps.wi[p] = make_float4(w_i.x, w_i.y, w_i.z, __int_as_float(V.mat));
     ps.ro[p] = make_float4(ro.x, ro.y, ro.z, tmax);
     ps.rd[p] = make_float4(rd.x, rd.y, rd.z, rd.w);
   }
