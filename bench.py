@@ -337,25 +337,70 @@ def _reduce(dist, t_s, rays):
     return mx.item(), sm.item()
 
 
-def _trace_roofline(st, kt, l2, pk, pk_kind, kernel_mixed, kernel_extend):
-    """Roofline of the traversal kernel: algorithmic bytes (32 B per child box tested,
-    48 B per triangle tested, 84 B of ray and hit records per ray) over its event time.
-    With the mixed kernel (both ray kinds in one launch) the bytes of both kinds count;
-    otherwise the closest-hit (extend) kernel alone."""
+def replay_sample(jobs, seeds, every=128):
+    """Algorithmic traversal work per walked ray, by kind: the rays an oracle pass walks a
+    BVH with (the same rays the core walks) over every `every`-th row of each job's frame
+    (so each job contributes in proportion to its pixels, as in the mix), replayed one at
+    a time on the host in the device walk's order without the warp's speculation
+    (yc_walk_counts). Returns {"closest"|"any": (rays, boxes, tris)}."""
+    from oracle import oracle_py as O
+    from yune_gb300 import scenes
+    out = {"closest": [0, 0, 0], "any": [0, 0, 0]}
+    for s, sd in zip(jobs, seeds):
+        parts = [O.record_rays(s, int(sd[0]), s.cfg, (y, y + 1)) for y in range(every // 2, s.height, every)]
+        rec = np.concatenate(parts) if parts else np.zeros((0, 8), np.float32)
+        for name, sel in (("closest", rec[:, 7] < 2), ("any", rec[:, 7] >= 2)):
+            r9 = O.rays9_of(rec[sel])
+            if len(r9) == 0:
+                continue
+            b, t, _, _ = scenes.walk_counts(s, r9, any_hit=(name == "any"))
+            out[name][0] += len(r9)
+            out[name][1] += b
+            out[name][2] += t
+    return {k: tuple(v) for k, v in out.items()}
+
+
+def _trace_roofline(st, kt, l2, pk, pk_kind, kernel_mixed, kernel_extend, replay=None):
+    """Roofline of the traversal kernel over its event time. achieved: the algorithmic
+    bytes of the rays it walked -- 32 B per child box and 48 B per triangle a lone walk of
+    the ray needs (replay: per-ray counts from the host replay of a sample of the same
+    rays), plus 64 B of shading record fetched per closest-hit ray -- with the number of
+    rays of each kind from the device counters. executed_*: the same with the boxes and
+    triangles the device tested (its counters, speculation included) and 84 B of ray and
+    hit records per ray. With the mixed kernel (both ray kinds in one launch) both kinds
+    count; otherwise the closest-hit (extend) kernel alone."""
     mixed = kt.get("trace_launches", 0) > 0
     kinds = ("ext", "any") if mixed else ("ext",)
     boxes = sum(st[k + "_boxes"] for k in kinds)
     tris = sum(st[k + "_tris"] for k in kinds)
     rays = sum(st[k + "_rays"] for k in kinds)
     ms = kt["trace_ms"] if mixed else kt["extend_ms"]
-    nbytes = 32.0 * boxes + 48.0 * tris + 84.0 * rays
+    ex_bytes = 32.0 * boxes + 48.0 * tris + 84.0 * rays
+    ex_achieved = ex_bytes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+    if replay:
+        alg = 0.0
+        per_kind = {}
+        for k, name, rec_b in (("ext", "closest", 64.0), ("any", "any", 0.0)):
+            if k not in kinds:
+                continue
+            n, b, t = replay[name]
+            per_ray = (32.0 * b + 48.0 * t) / n + rec_b if n else 0.0
+            per_kind[name] = {"sample_rays": n, "boxes_per_ray": b / n if n else 0.0,
+                              "tris_per_ray": t / n if n else 0.0, "bytes_per_ray": per_ray}
+            alg += per_ray * st[k + "_rays"]
+        nbytes, source = alg, "host replay of sampled rays (yc_walk_counts), no speculation"
+    else:
+        nbytes, source, per_kind = ex_bytes, "device counters (speculation included)", None
     achieved = nbytes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
     out = {"kernel": kernel_mixed if mixed else kernel_extend, "bound": "l2", "achieved": achieved, "peak": l2,
            "unit": "GB/s", "frac": achieved / l2 if l2 else None, "traffic": None,
+           "bytes_source": source, "replay": per_kind,
+           "executed_achieved": ex_achieved, "executed_frac": ex_achieved / l2 if l2 else None,
+           "executed_bytes_per_ray": ex_bytes / max(1, rays), "speculation_ratio": ex_bytes / nbytes if nbytes else None,
            "peak_source": "measured L2 read bandwidth (yc_measure_l2_gbs, 48 MB x 20 sweeps)",
            "hbm_peak": pk.get("hbm_gbs"), "hbm_frac": achieved / pk.get("hbm_gbs", 1.0), "hbm_peak_source": pk_kind,
            "rays": int(rays), "bytes_per_ray": nbytes / max(1, rays),
-           # the same tests in the reference's layouts (80 B BVHNodeGPU per box, 112 B
+           # the device's tests in the reference's layouts (80 B BVHNodeGPU per box, 112 B
            # TriangleGPU per triangle, include/CL_headers.h:57-107)
            "ref_layout_bytes_per_ray": (80.0 * boxes + 112.0 * tris + 84.0 * rays) / max(1, rays),
            "ref_layout_achieved": ((80.0 * boxes + 112.0 * tris + 84.0 * rays) / (ms / 1e3) / 1e9 if ms > 0 else 0.0),
@@ -851,6 +896,10 @@ def run_mix(args, rank, local, ws, dist):
     e2e_p_s = time.perf_counter() - t0
     e2e_p_rays = r.stats()["rays"]
     b.close()
+    idx = mix_sample(len(jobs), args.sample_every)
+    t0 = time.perf_counter()
+    replay = replay_sample([jobs[i] for i in idx], [seeds[i][prof.start:] for i in idx])
+    replay_s = time.perf_counter() - t0
     med = lambda v: float(np.median(v))  # noqa: E731
     vb = [x["batched_rays"] / (x["batched_ms"] / 1e3) / 1e6 for x in reps]
     vp = [x["plain_rays"] / (x["plain_ms"] / 1e3) / 1e6 for x in reps]
@@ -893,9 +942,9 @@ def run_mix(args, rank, local, ws, dist):
                                    "trace": kt_p["trace_ms"], "sort": kt_p["sort_ms"], "logic": kt_p["logic_ms"],
                                    "tail": kt_p["tail_ms"], "rounds": kt_p["rounds"]},
         "roofline": _trace_roofline(st_bp, kt_b, l2, pk, pk_kind, "k_batch_trace_mixed (closest + any-hit rays)",
-                                    "k_batch_trace<closest> (extend)"),
+                                    "k_batch_trace<closest> (extend)", replay),
         "plain_roofline": _trace_roofline(st_pp, kt_p, l2, pk, pk_kind, "k_trace_paths_mixed (closest + any-hit rays)",
-                                          "k_trace_paths<closest> (extend)"),
+                                          "k_trace_paths<closest> (extend)", replay),
         "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else 0.0, "unit": METRIC, "passes_per_step": E,
                 "steps": S, "h2d_bytes_per_step": len(jobs) * (80 + 4 * E), "d2h_bytes_per_step": acc_bytes,
                 "path": "per step: yc_batch_add_job (camera, seeds) for every job + yc_batch_run + yc_tonemap of "
@@ -905,11 +954,11 @@ def run_mix(args, rank, local, ws, dist):
                       "d2h_bytes_per_step": acc_bytes,
                       "path": "per step and job: yc_set_camera + yc_render_passes + yc_tonemap to host"},
         "clocks": clk.summary(),
-        "host": {"scene_build_s": build_s, "upload_s": upload_s, "autotune_s": tune_s, "autotune_trials": len(trials)},
+        "host": {"scene_build_s": build_s, "upload_s": upload_s, "autotune_s": tune_s, "autotune_trials": len(trials),
+                 "replay_s": replay_s},
         "stack_overflow": int(sum(x["overflow"] for x in reps)),
     }
     if not args.no_cpu:
-        idx = mix_sample(len(jobs), args.sample_every)
         line["cpu_baseline"] = cpu_reference_mix([jobs[i] for i in idx], idx, [seeds[i] for i in idx],
                                                  args.cpu_seconds)
     r.close()

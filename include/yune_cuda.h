@@ -156,6 +156,19 @@ typedef struct yc_scene_layout_info {
 int yc_scene_layout(const yc_triangle* tris_host, int n_tri, int n_mat, const yc_bvh_node* nodes_host, int n_node,
                     int tree_mode, yc_scene_layout_info* out);
 
+/* The traversal's algorithmic work on explicit rays, counted on the host without a
+ * device: the upload's repack of these arrays (tree_mode 0 or 1), then each ray walked
+ * alone in the device walk's order (nearer child first, the same distance cull, the
+ * reference's slab and Moller-Trumbore arithmetic) but without the speculation of a warp
+ * whose lanes walk together. *boxes and *tris_tested receive the child boxes (32 B each)
+ * and triangles (48 B each) tested over all rays: the algorithmic bytes of the traversal
+ * roofline. rays_host: 9 floats per ray as for yc_trace; any_hit: stop at the first hit
+ * closer than the length. tri_out (original index, -1 none) and t_out (final length) may
+ * be NULL. No reference counterpart (measurement). */
+int yc_walk_counts(const yc_triangle* tris_host, int n_tri, const yc_bvh_node* nodes_host, int n_node, int tree_mode,
+                   const float* rays_host, int n, int any_hit, uint64_t* boxes, uint64_t* tris_tested, int* tri_out,
+                   float* t_out);
+
 /* ---- camera (CLManager::setupCameraBuffer + the map/unmap of
  *      RendererCore::updateRenderKernelArgs, src/RendererCore.cpp:532-555) ---- */
 int yc_set_camera(yc_ctx* ctx, const yc_cam* cam_host);

@@ -123,6 +123,28 @@ int or_trace(const yc_triangle* t, int nt, const yc_bvh_node* b, int nb, const y
   return 0;
 }
 
+// The rays one pass of pathtracer (udpt.cl:158-211) walks a BVH with over rows
+// [row0, row1), in order (the Tracer::rec format, 8 floats per ray). Writes at most cap
+// rays and their number to *n_out (the full count, which may exceed cap).
+int or_record_rays(const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_bvh_node* b, int nb,
+                   const yc_quad_light* l, int nl, const yc_cam* cam, int W, int H, uint32_t rand_, const or_cfg* cfg,
+                   int row0, int row1, float* out, int64_t cap, int64_t* n_out) {
+  if (!cam || !out || !n_out || W <= 0 || H <= 0 || nl < 0 || nl > 16) return -1;
+  if (row1 <= row0) { row0 = 0; row1 = H; }
+  const orc::Scene<float> sc = mk_scene<float>(t, nt, m, nm, b, nb, l, nl);
+  const orc::Config k = to_cfg(cfg);
+  orc::Counters cnt;
+  orc::Tracer<float> tr(sc, k, cnt);
+  std::vector<float> rec;
+  tr.rec = &rec;
+  for (int y = row0; y < row1; ++y)
+    for (int x = 0; x < W; ++x) orc::pixel_sample<float>(tr, *cam, x, y, W, H, rand_);
+  const int64_t n = (int64_t)(rec.size() / 8);
+  *n_out = n;
+  std::memcpy(out, rec.data(), (size_t)std::min(n, cap) * 8 * sizeof(float));
+  return 0;
+}
+
 // One pass of pathtracer (udpt.cl:158-211) over rows [row0, row1) of a W x H RGBA32F
 // accumulator updated in place (row1 <= row0 means the whole image).
 int or_render(const yc_triangle* t, int nt, const yc_material* m, int nm, const yc_bvh_node* b, int nb,

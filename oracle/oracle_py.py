@@ -57,6 +57,8 @@ def orc():
         L.or_render_pixels_f64.argtypes = [vp, i32, vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, vp, i32, vp, i32,
                                            C.POINTER(OrCfg), i32, i32, vp, i32]
         L.or_brdf.argtypes = [vp, i32, vp, i32, i32, vp, vp, vp, vp, i32, C.c_float, i32, vp]
+        L.or_record_rays.argtypes = [vp, i32, vp, i32, vp, i32, vp, i32, vp, i32, i32, u32, C.POINTER(OrCfg), i32,
+                                     i32, vp, C.c_int64, C.POINTER(C.c_int64)]
         _orc = L
     return _orc
 
@@ -161,6 +163,34 @@ def render(scene, accum, rand_seed, reset, cfg, threads=0, rows=None, f64=False,
     if rc != 0:
         raise RuntimeError("or_render failed: %d" % rc)
     return {k: getattr(cnt, k) for k, _ in OrCounters._fields_}
+
+
+def record_rays(scene, rand_seed, cfg, rows, cap=1 << 22):
+    """The rays one oracle pass over `rows` (y0, y1) walks a BVH with, as the CUDA core
+    walks them (a shadow ray a light closes first and a MIS ray that misses the sampled
+    light settle without a walk): (n, 8) float32, origin xyz, direction xyz, length,
+    kind (0 camera, 1 extension: closest hit; 2 shadow, 3 MIS: any hit)."""
+    L = orc()
+    out = np.zeros((cap, 8), np.float32)
+    n = C.c_int64()
+    c = cfg_of(cfg)
+    rc = L.or_record_rays(_p(scene.tris), len(scene.tris), _p(scene.mats), len(scene.mats), _p(scene.nodes),
+                          len(scene.nodes), _p(scene.lights), len(scene.lights), _p(scene.cam), scene.width,
+                          scene.height, int(rand_seed) & 0xFFFFFFFF, C.byref(c), rows[0], rows[1], _p(out), cap,
+                          C.byref(n))
+    if rc != 0:
+        raise RuntimeError("or_record_rays failed")
+    return out[:min(n.value, cap)].copy()
+
+
+def rays9_of(rec):
+    """Recorded rays in the 9-float ray format (origin xyzw, dir xyzw, length)."""
+    r = np.zeros((len(rec), 9), np.float32)
+    r[:, 0:3] = rec[:, 0:3]
+    r[:, 3] = 1.0
+    r[:, 4:7] = rec[:, 3:6]
+    r[:, 8] = rec[:, 6]
+    return r
 
 
 def render_bdpt(scene, accum, rand_seed, reset, bounces, threads=0, rows=None, f64=False, heap_size=1500):

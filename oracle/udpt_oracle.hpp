@@ -77,6 +77,15 @@ struct Tracer {
 
   Tracer(const Scene<R>& s, const Config& c, Counters& k) : sc(s), cfg(c), cnt(k), queue(c.heap_size > 0 ? c.heap_size + 1 : 2) {}
 
+  // Optional record of the rays that walk a BVH (measurement of the traversal's
+  // algorithmic work, replayed on the host): 8 floats each, origin xyz, direction xyz,
+  // segment length and kind (0 camera ray, 1 extension ray: closest hit; 2 shadow ray,
+  // 3 MIS ray: any hit). A shadow ray that a light closes first, and a MIS ray whose
+  // closest light is not the sampled one, settle without a walk (as the CUDA core settles
+  // them) and are not recorded. rec_kind is set by the caller of trace() and consumed.
+  std::vector<float>* rec = nullptr;
+  int rec_kind = -1, rec_light = -1;
+
   static R draw(uint32_t& seed) { seed = ym::xor_shift(seed); return O::u01(seed); }
 
   // rayAabbIntersection, udpt.cl:392-431
@@ -192,6 +201,15 @@ struct Tracer {
         }
       }
     }
+    if (rec && rec_kind >= 0 && sc.n_node > 0) {
+      const bool walked = rec_kind < 2 || (rec_kind == 2 && !flag) || (rec_kind == 3 && flag && hit.light == rec_light);
+      if (walked) {
+        const float r8[8] = {(float)ray.origin.x, (float)ray.origin.y, (float)ray.origin.z, (float)ray.dir.x,
+                             (float)ray.dir.y, (float)ray.dir.z, (float)ray.length, (float)rec_kind};
+        rec->insert(rec->end(), r8, r8 + 8);
+      }
+    }
+    rec_kind = -1;
     if (sc.n_node > 0) flag |= traverse(ray, hit);
     else
       for (int i = 0; i < sc.n_tri; ++i) flag |= ray_tri(ray, hit, i);
@@ -458,6 +476,7 @@ struct Tracer {
     Ray<R> sray{h.hit_point + w_i * (R)EPS_F, w_i, len, true};
     Hit<R> shit;
     cnt.shadow++;
+    rec_kind = 2;
     const bool occluded = trace(sray, shit);
     const V4<R> lke = ld<R>(sc.lights[j].ke);
     if (!occluded) {
@@ -483,6 +502,8 @@ struct Tracer {
     w_i = bray.dir;
     Hit<R> nh;
     cnt.mis++;
+    rec_kind = 3;
+    rec_light = j;
     if (!trace(bray, nh) || nh.light != j) return light_sample + emission;
     mis_w = brdf_pdf;
     mis_w = O::div(ym_pown(mis_w), O::add(ym_pown(light_pdf), ym_pown(brdf_pdf)));
@@ -500,6 +521,7 @@ struct Tracer {
   V4<R> shade(Ray<R> ray, uint32_t& seed) {
     Hit<R> hit;
     cnt.primary++;
+    rec_kind = 0;
     if (!trace(ray, hit)) return V4<R>{(R)0.4f, (R)0.4f, (R)0.4f, R(1)};
     if (hit.light >= 0) {
       if (dot(ray.dir, ld<R>(sc.lights[hit.light].normal)) < 0) return V4<R>{R(1), R(1), R(1), R(1)};
@@ -525,7 +547,7 @@ struct Tracer {
           else sample_cosine(nray, pdf, hit, seed);
         }
         bool traced_hit = false;
-        if (!(pdf <= 0.0)) { cnt.extension++; traced_hit = trace(nray, nh); }
+        if (!(pdf <= 0.0)) { cnt.extension++; rec_kind = 1; traced_hit = trace(nray, nh); }
         if (pdf <= 0.0 || !traced_hit || nh.light >= 0) {
           if (spec && nh.light >= 0) indirect = indirect + thr * ld<R>(sc.lights[nh.light].ke);
           break;

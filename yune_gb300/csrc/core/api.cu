@@ -651,6 +651,20 @@ int yc_scene_layout(const yc_triangle* tris, int n_tri, int n_mat, const yc_bvh_
   return YC_OK;
 }
 
+int yc_walk_counts(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, int n_node, int tree_mode,
+                   const float* rays9, int n, int any_hit, uint64_t* boxes, uint64_t* tris_tested, int* tri_out,
+                   float* t_out) {
+  if (!boxes || !tris_tested || n < 0 || (n > 0 && !rays9)) return fail(YC_E_INVALID, "bad argument");
+  if (tree_mode != yc::TREE_REFERENCE && tree_mode != yc::TREE_SAH_OVER_LEAVES)
+    return fail(YC_E_INVALID, "the host replay walks tree modes 0 and 1");
+  yc::Repacked rp;
+  std::string err;
+  if (yc::repack_scene(tris, n_tri, nodes, n_node, tree_mode, rp, err)) return fail(YC_E_INVALID, err);
+  if (yc::walk_counts_host(rp, rays9, n, any_hit != 0, boxes, tris_tested, tri_out, t_out, err))
+    return fail(YC_E_INVALID, err);
+  return YC_OK;
+}
+
 int yc_bvh_build(yc_ctx* c, const yc_triangle* tris, int n_tri, int bins, int leaf_max, int* n_node, int* depth) {
   if (!c || n_tri < 0 || (n_tri > 0 && !tris) || leaf_max < 1 || leaf_max > 10 || bins < 0 || bins > 256)
     return fail(YC_E_INVALID, "yc_bvh_build: bad argument");

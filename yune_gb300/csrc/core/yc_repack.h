@@ -44,4 +44,10 @@ enum { TREE_REFERENCE = 0, TREE_SAH_OVER_LEAVES = 1, TREE_WIDE4 = 2 };
 int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, int n_node, int tree_mode,
                  Repacked& out, std::string& err);
 
+// walk_host.cpp: the device walk's work on explicit rays (9 floats each) replayed one ray
+// at a time on the host, without the warp's speculative leaves: child boxes and triangles
+// tested, and each ray's closest (any = false) or first (any = true) triangle and t.
+int walk_counts_host(const Repacked& rp, const float* rays9, int n, bool any, uint64_t* boxes, uint64_t* tris,
+                     int* tri_out, float* t_out, std::string& err);
+
 }  // namespace yc

@@ -178,6 +178,20 @@ def device_bytes(s, tree_mode=1):
     return int(out.device_bytes)
 
 
+def walk_counts(s, rays9, any_hit=False, tree_mode=1):
+    """The traversal's algorithmic work on explicit rays, replayed on the host
+    (yc_walk_counts): (child boxes tested, triangles tested, per-ray triangle, per-ray t)."""
+    tris, nodes = np.ascontiguousarray(s.tris), np.ascontiguousarray(s.nodes)
+    rays9 = np.ascontiguousarray(rays9, np.float32)
+    n = len(rays9)
+    tri = np.zeros(n, np.int32)
+    t = np.zeros(n, np.float32)
+    b, tt = C.c_uint64(), C.c_uint64()
+    N.check(N.lib().yc_walk_counts(ptr(tris), len(tris), ptr(nodes), len(nodes), tree_mode, ptr(rays9), n,
+                                   int(any_hit), C.byref(b), C.byref(tt), ptr(tri), ptr(t)), "yc_walk_counts")
+    return int(b.value), int(tt.value), tri, t
+
+
 def set_host_threads(n):
     """Limits the host threads of the BVH builder, the scene cache and the upload's repack
     (yh_set_host_threads; 0 = every core). Their outputs do not depend on it. Returns the

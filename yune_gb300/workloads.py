@@ -85,13 +85,12 @@ def c2_jobs(n_jobs=64, spp=64, seed=0, max_tris=500_000, cfg=None, only=None):
     return [mixed_scene(specs[j][0], specs[j][1], specs[j][2], specs[j][3], spp, cfg) for j in idx]
 
 
-def c3_scenes(n_scenes=8, seed=1, min_tris=10_000, max_tris=2_000_000):
+def c3_scenes(n_scenes=8, seed=1, min_tris=10_000, max_tris=2_000_000, only=None, cfg=None, width=256, height=256):
+    """The serving pool's scenes; `only`: the indices of the scenes to build (all when None)."""
     rng = np.random.default_rng(seed)
-    out = []
-    for j in range(n_scenes):
-        total = int(math.exp(rng.uniform(math.log(min_tris), math.log(max_tris))))
-        out.append(mixed_scene(total, seed * 7919 + j, 256, 256, 1))
-    return out
+    totals = [int(math.exp(rng.uniform(math.log(min_tris), math.log(max_tris)))) for _ in range(n_scenes)]
+    idx = range(n_scenes) if only is None else only
+    return [mixed_scene(totals[j], seed * 7919 + j, width, height, 1, cfg) for j in idx]
 
 
 def c3_requests(n_requests, rate, n_scenes, seed=2, res_range=(256, 2048), spp_range=(16, 1024)):
