@@ -248,6 +248,10 @@ typedef struct yc_batch_cfg {
   int32_t groups;              /* slot groups whose rounds run concurrently (1..8); 0 = 2 */
   int32_t ray_sort;            /* sort key of each round's rays (as YC_OPT_RAY_SORT); 0 = the
                                   context's YC_OPT_RAY_SORT, -1 = rays in queue order */
+  int32_t trace_block;         /* threads per block of the traversal kernels (a multiple of 32
+                                  up to 256): with the stack columns of its threads it sets the
+                                  shared memory per block and so the blocks and the L1 left
+                                  per SM; 0 = 128 */
 } yc_batch_cfg;
 int yc_batch_create(yc_ctx* ctx, const yc_batch_cfg* cfg, yc_batch** out);
 /* Adds a job: n_pass passes of scene_id into accum_id seen from *cam, pass k with
@@ -269,6 +273,38 @@ int yc_batch_cancel_job(yc_batch* b, int job_id);
 /* A batch belongs to its context: yc_destroy releases the context's remaining batches,
  * after which their handles must not be used. */
 int yc_batch_destroy(yc_batch* b);
+
+/* ---- launch-shape tuner of the batch engine ----
+ * Times candidate shapes on the job mix itself and returns the fastest: every job renders
+ * its calibration passes (seeds_host, n_pass; seeds of their own, not the jobs' real ones)
+ * into scratch accumulators under each candidate, timed with CUDA events. The search runs
+ * one parameter at a time from *start -- pool_paths (512K..4M, at most the mix's pixels
+ * rounded up to a power of two), rounds_per_launch (4/8/16), logic_blocks_per_sm (2/4/8),
+ * sort_threshold (0, 64K, 256K), groups (1/2/4), ray_sort (off, 32) and trace_block
+ * (64/128/256 threads) -- keeping the best value of each, and sweeps again while a sweep
+ * moved the shape (at most `sweeps` sweeps). start->stack_cap must hold the deepest
+ * scene (depth + 2; the stack depth is not searched: a shorter stack fails the walks).
+ * trials (capacity trial_cap) receive every timed shape in order; *n_trials their count.
+ * No reference counterpart (the reference has one fixed launch per frame). */
+typedef struct yc_tune_job {
+  yc_cam cam;
+  yc_pass_cfg cfg;             /* integrator YC_UDPT */
+  int32_t scene_id, width, height, n_pass;
+  const uint32_t* seeds_host;
+} yc_tune_job;                 /* 144 bytes, no padding */
+typedef struct yc_tune_trial {
+  yc_batch_cfg cfg;
+  float ms;
+} yc_tune_trial;
+int yc_batch_tune(yc_ctx* ctx, const yc_tune_job* jobs, int n_jobs, const yc_batch_cfg* start, int sweeps,
+                  yc_batch_cfg* best, yc_tune_trial* trials, int trial_cap, int* n_trials);
+/* The same search over a clock the caller supplies (host only, no device): clock(cfg,
+ * user) returns the time of a candidate shape (any unit, lower is better; negative: an
+ * error that ends the search with YC_E_LAUNCH). total_px bounds pool_paths as above.
+ * yc_batch_tune is this search with the calibration run of the mix as the clock. */
+typedef float (*yc_tune_clock)(const yc_batch_cfg* cfg, void* user);
+int yc_tune_search(const yc_batch_cfg* start, int64_t total_px, int sweeps, yc_tune_clock clock, void* user,
+                   yc_batch_cfg* best, yc_tune_trial* trials, int trial_cap, int* n_trials);
 
 /* ---- serving: continuous batching of render requests ----
  * No counterpart in the reference, which renders one frame at a time from its GUI loop

@@ -1,39 +1,38 @@
-"""The batch autotuner's search on the CPU, with a fake calibration clock."""
+"""The batch tuner's search on the CPU (yc_tune_search, the search of yc_batch_tune with a
+clock supplied by the caller): one parameter at a time, each keeping its best value, a
+second sweep when the first moved, the pool bounded by the mix's pixels."""
 from yune_gb300 import autotune
 
-
-class _FakeRenderer:
-    def __init__(self):
-        self.live = 0
-
-    def alloc_accum(self, w, h):
-        self.live += 1
-        return self.live
-
-    def free_accum(self, a):
-        self.live -= 1
+START = autotune.BatchShape()
 
 
-def test_coordinate_search_finds_the_separable_optimum(monkeypatch):
+def test_coordinate_search_finds_the_separable_optimum():
     seen = []
 
-    def clock(renderer, jobs, shape, cap, accs, passes=1):
+    def clock(shape):
         seen.append(shape.kwargs())
         return (abs(shape.pool_paths - (1 << 20)) / 1e5 + abs(shape.rounds_per_launch - 16)
-                + abs(shape.logic_blocks_per_sm - 2))
+                + abs(shape.logic_blocks_per_sm - 2) + abs(shape.trace_block - 256) / 64.0)
 
-    monkeypatch.setattr(autotune, "_calibrate", clock)
-    r = _FakeRenderer()
-    best, trials = autotune.tune(r, [(0, None, [1], None)] * 3, [(1920, 1080)] * 3)
-    assert best == autotune.BatchShape(1 << 20, 16, 2, 1 << 16, 2)
-    assert len(trials) == len(seen) and r.live == 0   # scratch accumulators released
+    best, trials = autotune.search(START, 3 * 1920 * 1080, clock)
+    assert best == autotune.BatchShape(1 << 20, 16, 2, 1 << 16, 2, 0, 256)
+    assert len(trials) == len(seen)
+    assert len({tuple(sorted(k.items())) for k in seen}) == len(seen)   # no shape timed twice
 
 
-def test_pool_never_exceeds_the_pixels_in_the_mix(monkeypatch):
-    monkeypatch.setattr(autotune, "_calibrate", lambda r, j, shape, c, a, passes=1: 1.0 / shape.pool_paths)
-    best, trials = autotune.tune(_FakeRenderer(), [(0, None, [1], None)], [(256, 256)])
+def test_pool_never_exceeds_the_pixels_in_the_mix():
+    best, trials = autotune.search(START, 256 * 256, lambda shape: 1.0 / shape.pool_paths)
     assert best.pool_paths == 1 << 16
     assert all(t.pool_paths <= 1 << 16 for t, _ in trials)
+
+
+def test_trace_block_is_searched_and_a_second_sweep_follows_a_move():
+    def clock(shape):   # rewards 64-thread trace blocks, then 4 groups once blocks are 64 wide
+        return (shape.trace_block != 64) * 10 + (shape.trace_block == 64 and shape.groups != 4) * 5
+
+    best, trials = autotune.search(START, 8 << 20, clock)
+    assert best.trace_block == 64 and best.groups == 4
+    assert {t.trace_block for t, _ in trials} >= {64, 128, 256}
 
 
 def test_small_mixes_calibrate_over_several_passes():

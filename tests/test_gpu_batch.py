@@ -18,9 +18,10 @@ def _jobs():
     return [(a, scenes.pass_seeds(1, 3)), (b, scenes.pass_seeds(2, 2)), (c, scenes.pass_seeds(3, 5))]
 
 
-@pytest.mark.parametrize("use_graph,pool,sort,groups", [(True, 4096, 0, 1), (False, 1000, 0, 2), (True, 1 << 16, 0, 2),
-                                                       (True, 4096, 1, 3), (False, 1000, 64, 4), (True, 999, 0, 8)])
-def test_batch_matches_per_pass(use_graph, pool, sort, groups):
+@pytest.mark.parametrize("use_graph,pool,sort,groups,tb", [(True, 4096, 0, 1, 0), (False, 1000, 0, 2, 64),
+                                                          (True, 1 << 16, 0, 2, 256), (True, 4096, 1, 3, 32),
+                                                          (False, 1000, 64, 4, 128), (True, 999, 0, 8, 96)])
+def test_batch_matches_per_pass(use_graph, pool, sort, groups, tb):
     jobs = _jobs()
     with Renderer(0) as r:
         ids = []
@@ -33,7 +34,8 @@ def test_batch_matches_per_pass(use_graph, pool, sort, groups):
             aid = r.alloc_accum(s.width, s.height)
             r.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
             want.append(r.read_accum(aid))
-        b = Batch(r, pool_paths=pool, rounds_per_launch=4, use_graph=use_graph, sort_threshold=sort, groups=groups)
+        b = Batch(r, pool_paths=pool, rounds_per_launch=4, use_graph=use_graph, sort_threshold=sort, groups=groups,
+                  trace_block=tb)
         accs = []
         for (s, seeds), sid in zip(jobs, ids):
             aid = r.alloc_accum(s.width, s.height)

@@ -54,7 +54,8 @@ class CacheInfo(C.Structure):
 class BatchCfg(C.Structure):
     """yc_batch_cfg"""
     _fields_ = [("pool_paths", i32), ("rounds_per_launch", i32), ("logic_blocks_per_sm", i32), ("use_graph", i32),
-                ("max_jobs", i32), ("stack_cap", i32), ("sort_threshold", i32), ("groups", i32), ("ray_sort", i32)]
+                ("max_jobs", i32), ("stack_cap", i32), ("sort_threshold", i32), ("groups", i32), ("ray_sort", i32),
+                ("trace_block", i32)]
 
 
 class ServeCfg(C.Structure):
@@ -78,6 +79,19 @@ class RequestInfo(C.Structure):
     _fields_ = [("state", i32), ("accum_id", i32), ("pixels_done", C.c_int64), ("pixels_total", C.c_int64),
                 ("submit_s", C.c_double), ("admit_s", C.c_double), ("finish_s", C.c_double)]
 
+
+class TuneJob(C.Structure):
+    """yc_tune_job"""
+    _fields_ = [("cam", Cam), ("cfg", PassCfg), ("scene_id", i32), ("width", i32), ("height", i32), ("n_pass", i32),
+                ("seeds_host", vp)]
+
+
+class TuneTrial(C.Structure):
+    """yc_tune_trial"""
+    _fields_ = [("cfg", BatchCfg), ("ms", f32)]
+
+
+TUNE_CLOCK = C.CFUNCTYPE(f32, C.POINTER(BatchCfg), vp)   # yc_tune_clock
 
 # request states (YC_REQ_*)
 REQ_WAITING, REQ_RUNNING, REQ_CANCELLING, REQ_DONE, REQ_CANCELLED, REQ_REJECTED_BUDGET, REQ_REJECTED_QUEUE = range(7)
@@ -129,6 +143,9 @@ SIGNATURES = {
     "yc_batch_job_progress": (i32, [vp, i32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "yc_batch_cancel_job": (i32, [vp, i32]),
     "yc_batch_destroy": (i32, [vp]),
+    "yc_batch_tune": (i32, [vp, vp, i32, C.POINTER(BatchCfg), i32, C.POINTER(BatchCfg), vp, i32, C.POINTER(i32)]),
+    "yc_tune_search": (i32, [C.POINTER(BatchCfg), C.c_int64, i32, vp, vp, C.POINTER(BatchCfg), vp, i32,
+                             C.POINTER(i32)]),
     # serving and admission
     "yc_admission_create": (i32, [C.c_uint64, i32, C.POINTER(vp)]),
     "yc_admission_submit": (i32, [vp, C.c_uint64, C.POINTER(C.c_int64), C.POINTER(i32)]),

@@ -1,31 +1,32 @@
-"""Autotuner for the batch engine's launch shape.
+"""Autotuner for the batch engine's launch shape: a Python front end of yc_batch_tune
+(core/tune.cpp, in the C-ABI so that a C or C++ host tunes the same way).
 
-The batch engine (yc_batch_*) has six free parameters that change speed but never
-results: the number of path slots in flight (the wavefront size), the rounds captured
-in one CUDA graph launch, the logic kernel's blocks per SM, the queue size from which
-the shade queue is sorted by path phase and material class (0: never), the number of
-slot groups whose rounds run concurrently, and whether each round's rays are sorted by
-origin and direction cell before the trace. The best values depend
-on the job mix (total pixels, scene sizes, path lengths), so the tuner times candidate
-shapes on a calibration run of the mix itself: every job's first passes, into scratch
-accumulators, with the engine's own CUDA-event clock (yc_last_pass_ms); small mixes
-render several passes per job so that the calibration sees the steady state. It
-searches one parameter at a time (pool size, rounds per launch, logic blocks, sort threshold,
-groups, ray sort) from a measured starting shape, keeping the best value of each before
-moving on, and sweeps once more if the first sweep changed the shape.
+The batch engine (yc_batch_*) has seven free parameters that change speed but never
+results: the number of path slots in flight (the wavefront size), the rounds captured in
+one CUDA graph launch, the logic kernel's blocks per SM, the queue size from which the
+shade queue is sorted by path phase and material class (0: never), the number of slot
+groups whose rounds run concurrently, whether each round's rays are sorted by origin and
+direction cell before the trace, and the traversal kernels' block shape (threads per
+block: with the per-thread stack columns it sets the shared memory per block, hence the
+blocks and the L1 left per SM). The best values depend on the job mix (total pixels,
+scene sizes, path lengths), so the tuner times candidate shapes on a calibration run of
+the mix itself: every job's first passes, into scratch accumulators, with the engine's own
+CUDA-event clock; small mixes render several passes per job so that the calibration sees
+the steady state. It searches one parameter at a time from a measured starting shape,
+keeping the best value of each before moving on, and sweeps once more if the first sweep
+changed the shape. The traversal stack depth is what the deepest scene needs.
 """
+import ctypes as C
 import time
 from dataclasses import dataclass
 
+import numpy as np
+
+from . import _native as N
 from . import scenes
-from .batch import Batch
+from .core import cfg_struct
 
 POOLS = (1 << 19, 1 << 20, 1 << 21, 1 << 22)
-ROUNDS = (4, 8, 16)
-LOGIC_BLOCKS = (2, 4, 8)
-SORT = (0, 1 << 16, 1 << 18)
-GROUPS = (1, 2, 4)
-RAY_SORT = (-1, 32)   # rays in queue order, or sorted by 3 origin and 2 direction bits per axis
 
 
 @dataclass
@@ -38,11 +39,17 @@ class BatchShape:
     sort_threshold: int = 1 << 16
     groups: int = 2
     ray_sort: int = 0
+    trace_block: int = 128
 
     def kwargs(self):
         return dict(pool_paths=self.pool_paths, rounds_per_launch=self.rounds_per_launch,
                     logic_blocks_per_sm=self.logic_blocks_per_sm, sort_threshold=self.sort_threshold,
-                    groups=self.groups, ray_sort=self.ray_sort)
+                    groups=self.groups, ray_sort=self.ray_sort, trace_block=self.trace_block)
+
+    @staticmethod
+    def of(cfg):
+        return BatchShape(cfg.pool_paths, cfg.rounds_per_launch, cfg.logic_blocks_per_sm, cfg.sort_threshold,
+                          cfg.groups, cfg.ray_sort, cfg.trace_block)
 
 
 def calibration_passes(total_px):
@@ -53,61 +60,51 @@ def calibration_passes(total_px):
     return max(1, min(16, -(-4 * POOLS[-1] // max(1, total_px))))
 
 
-def _calibrate(renderer, jobs, shape, stack_cap, accs, passes=1):
-    """Milliseconds of `passes` passes of every job under `shape` (device time of
-    yc_batch_run)."""
-    b = Batch(renderer, stack_cap=stack_cap, **shape.kwargs())
-    try:
-        for (sid, cam, seeds, cfg), a in zip(jobs, accs):
-            b.add_job(sid, a, cam, seeds[:passes], cfg)
-        b.run()
-        return renderer.last_pass_ms()
-    finally:
-        b.close()
-
-
-def tune(renderer, jobs, sizes, stack_cap=0, log=None):
+def tune(renderer, jobs, sizes, stack_cap=0, log=None, sweeps=2):
     """Picks a BatchShape for `jobs`, a list of (scene_id, cam, seeds, cfg) tuples, whose
-    frames have the (width, height) of `sizes`. Returns (shape, trials) where trials lists
-    (shape, ms) in the order they were timed."""
-    accs = [renderer.alloc_accum(w, h) for (w, h) in sizes]
+    frames have the (width, height) of `sizes`, with yc_batch_tune. Returns (shape,
+    trials) where trials lists (shape, ms) in the order they were timed."""
     total_px = sum(w * h for (w, h) in sizes)
     passes = min(calibration_passes(total_px), min(len(j[2]) for j in jobs))
-    trials = []
-    try:
-        best = BatchShape()
-        best.pool_paths = min(best.pool_paths, _round_pool(total_px))
-        best_ms = _calibrate(renderer, jobs, best, stack_cap, accs, passes)
-        trials.append((BatchShape(**best.kwargs()), best_ms))
-        timed = {tuple(sorted(best.kwargs().items())): best_ms}
-        for sweep in range(2):   # a second sweep only when the first one moved
-            start = BatchShape(**best.kwargs())
-            for field, values in (("pool_paths", POOLS), ("rounds_per_launch", ROUNDS),
-                                  ("logic_blocks_per_sm", LOGIC_BLOCKS), ("sort_threshold", SORT),
-                                  ("groups", GROUPS), ("ray_sort", RAY_SORT)):
-                for v in values:
-                    if v == getattr(best, field):
-                        continue
-                    if field == "pool_paths" and v > _round_pool(total_px):
-                        continue   # more slots than pixels stay idle
-                    cand = BatchShape(**best.kwargs())
-                    setattr(cand, field, v)
-                    key = tuple(sorted(cand.kwargs().items()))
-                    if key in timed:
-                        continue
-                    ms = _calibrate(renderer, jobs, cand, stack_cap, accs, passes)
-                    timed[key] = ms
-                    trials.append((cand, ms))
-                    if log:
-                        log("autotune %s -> %.2f ms" % (cand, ms))
-                    if ms < best_ms:
-                        best, best_ms = cand, ms
-            if best == start:
-                break
-    finally:
-        for a in accs:
-            renderer.free_accum(a)
-    return best, trials
+    arr = (N.TuneJob * len(jobs))()
+    keep = []
+    for t, (sid, cam, seeds, cfg), (w, h) in zip(arr, jobs, sizes):
+        sd = np.ascontiguousarray(seeds[:passes], np.uint32)
+        keep.append(sd)
+        C.memmove(C.byref(t.cam), np.ascontiguousarray(cam).ctypes.data, C.sizeof(N.Cam))
+        t.cfg = cfg_struct(cfg)
+        t.scene_id, t.width, t.height, t.n_pass, t.seeds_host = sid, w, h, passes, sd.ctypes.data
+    b = BatchShape()
+    start = N.BatchCfg(b.pool_paths, b.rounds_per_launch, b.logic_blocks_per_sm, 1, 0, stack_cap, b.sort_threshold,
+                       b.groups, b.ray_sort, b.trace_block)
+    cap = 256
+    out = N.BatchCfg()
+    tr = (N.TuneTrial * cap)()
+    n = C.c_int()
+    N.check(renderer.L.yc_batch_tune(renderer.h, arr, len(jobs), C.byref(start), sweeps, C.byref(out), tr, cap,
+                                     C.byref(n)), "yc_batch_tune")
+    trials = [(BatchShape.of(tr[i].cfg), float(tr[i].ms)) for i in range(min(n.value, cap))]
+    if log:
+        for sh, ms in trials:
+            log("autotune %s -> %.2f ms" % (sh, ms))
+    return BatchShape.of(out), trials
+
+
+def search(start, total_px, clock, sweeps=2):
+    """The tuner's search alone (yc_tune_search) over clock(shape) -> time: no device.
+    Returns (best shape, [(shape, time)] in the order timed)."""
+    def cb(cfg, _user):
+        return float(clock(BatchShape.of(cfg.contents)))
+    fn = N.TUNE_CLOCK(cb)
+    st = N.BatchCfg(start.pool_paths, start.rounds_per_launch, start.logic_blocks_per_sm, 1, 0, 0,
+                    start.sort_threshold, start.groups, start.ray_sort, start.trace_block)
+    out = N.BatchCfg()
+    cap = 256
+    tr = (N.TuneTrial * cap)()
+    n = C.c_int()
+    N.check(N.lib().yc_tune_search(C.byref(st), int(total_px), sweeps, C.cast(fn, C.c_void_p), None, C.byref(out), tr,
+                                   cap, C.byref(n)), "yc_tune_search")
+    return BatchShape.of(out), [(BatchShape.of(tr[i].cfg), float(tr[i].ms)) for i in range(min(n.value, cap))]
 
 
 def _round_pool(total_px):

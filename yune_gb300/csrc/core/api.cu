@@ -1128,7 +1128,8 @@ int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
     }
     KTimer kt(c, K_TRACE, timed);
     yc::launch_batch_trace_mixed(b->wide == 1, b->jobs.p, batch_state(b).job, in_c, in_a, rin, ps.ro, ps.rd, ps.hit,
-                                 c->stats.p, b->stack_cap, b->grid_m, sm, b->raysort ? rsb.sorted : nullptr,
+                                 c->stats.p, b->stack_cap, b->grid_m, b->cfg.trace_block, sm,
+                                 b->raysort ? rsb.sorted : nullptr,
                                  b->raysort ? rsb.ctl : nullptr);
   } else {
     // the two traces of a round are independent and overlap
@@ -1139,12 +1140,13 @@ int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
     {
       KTimer kt(c, K_EXTEND, timed);
       yc::launch_batch_trace(false, b->wide == 1, b->jobs.p, batch_state(b).job, in_c, &rin->n_closest,
-                             &rin->work_closest, ps.ro, ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_c, sm);
+                             &rin->work_closest, ps.ro, ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_c,
+                             b->cfg.trace_block, sm);
     }
     {
       KTimer kt(c, K_OCCL, timed);
       yc::launch_batch_trace(true, b->wide == 1, b->jobs.p, batch_state(b).job, in_a, &rin->n_any, &rin->work_any, ps.ro,
-                             ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_a, sa);
+                             ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_a, b->cfg.trace_block, sa);
     }
     if (!serial) {
       YC_CUDA(cudaEventRecord(g.ev_join, sa));
@@ -1243,6 +1245,9 @@ int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
   if (b->cfg.logic_blocks_per_sm <= 0) b->cfg.logic_blocks_per_sm = 4;
   if (b->cfg.max_jobs <= 0) b->cfg.max_jobs = 1024;
   if (b->cfg.groups <= 0) b->cfg.groups = 2;
+  if (b->cfg.trace_block <= 0) b->cfg.trace_block = 128;
+  if (b->cfg.trace_block > 256 || b->cfg.trace_block % 32)
+    return fail(YC_E_INVALID, "trace_block must be a multiple of 32 up to 256");
   if (b->cfg.groups > 8 || b->cfg.groups > b->cfg.pool_paths) return fail(YC_E_INVALID, "groups must be 1..8");
   const size_t n = (size_t)b->cfg.pool_paths;
   YC_CUDA(cudaSetDevice(c->device));
@@ -1375,9 +1380,9 @@ int yc_batch_run(yc_batch* b, int max_launches, int* unfinished) {
   YC_CUDA(cudaSetDevice(c->device));
   if (!b->started) {
     if (b->stack_cap <= 0) b->stack_cap = b->cfg.stack_cap > 0 ? b->cfg.stack_cap : 32;
-    b->grid_c = yc::batch_trace_grid(false, b->stack_cap, b->wide == 1);
-    b->grid_a = yc::batch_trace_grid(true, b->stack_cap, b->wide == 1);
-    b->grid_m = yc::batch_trace_mixed_grid(b->stack_cap, b->wide == 1);
+    b->grid_c = yc::batch_trace_grid(false, b->stack_cap, b->wide == 1, b->cfg.trace_block);
+    b->grid_a = yc::batch_trace_grid(true, b->stack_cap, b->wide == 1, b->cfg.trace_block);
+    b->grid_m = yc::batch_trace_mixed_grid(b->stack_cap, b->wide == 1, b->cfg.trace_block);
     if (b->grid_c <= 0 || b->grid_a <= 0 || b->grid_m <= 0)
       return fail(YC_E_LAUNCH, "batch trace kernel cannot be resident");
     b->started = true;

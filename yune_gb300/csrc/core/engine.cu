@@ -411,7 +411,7 @@ struct BatchSrc {
 };
 
 template <bool ANY, bool WIDE>
-__global__ void __launch_bounds__(TRACE_TB) k_batch_trace(const BatchJob* jobs, SF<int4> job_pass,
+__global__ void __launch_bounds__(TRACE_TB_MAX) k_batch_trace(const BatchJob* jobs, SF<int4> job_pass,
                                                           const int* __restrict__ queue, const int* __restrict__ count,
                                                           int* work, SF<float4> ro,
                                                           SF<float4> rd, SF<float4> hit, int stack_cap,
@@ -450,7 +450,7 @@ struct BatchMixedSrc {
 };
 
 template <bool WIDE>
-__global__ void __launch_bounds__(TRACE_TB) k_batch_trace_mixed(const BatchJob* jobs, SF<int4> job_pass,
+__global__ void __launch_bounds__(TRACE_TB_MAX) k_batch_trace_mixed(const BatchJob* jobs, SF<int4> job_pass,
                                                                 const int* __restrict__ q_closest,
                                                                 const int* __restrict__ q_any,
                                                                 RoundCounters* rc, SF<float4> ro,
@@ -462,59 +462,61 @@ __global__ void __launch_bounds__(TRACE_TB) k_batch_trace_mixed(const BatchJob* 
   trace_loop_mixed<WIDE>(src, nc, nc + rc->n_any, &rc->work_closest, stack_cap, st);
 }
 
-static size_t batch_smem(int cap) { return (size_t)TRACE_TB * 2 * cap * sizeof(int); }
+// the stack columns of a block of tb threads
+static size_t batch_smem(int cap, int tb) { return (size_t)tb * 2 * cap * sizeof(int); }
 
 template <class K>
-static int batch_grid_of(K kernel, size_t smem) {
+static int batch_grid_of(K kernel, size_t smem, int tb) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TRACE_TB, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, tb, smem);
   return per_sm > 0 ? per_sm * sms : -1;
 }
 
-int batch_trace_grid(bool any_hit, int stack_cap, bool wide) {
-  const size_t smem = batch_smem(stack_cap);
-  if (wide) return any_hit ? batch_grid_of(k_batch_trace<true, true>, smem) : batch_grid_of(k_batch_trace<false, true>, smem);
-  return any_hit ? batch_grid_of(k_batch_trace<true, false>, smem) : batch_grid_of(k_batch_trace<false, false>, smem);
+int batch_trace_grid(bool any_hit, int stack_cap, bool wide, int tb) {
+  const size_t smem = batch_smem(stack_cap, tb);
+  if (wide)
+    return any_hit ? batch_grid_of(k_batch_trace<true, true>, smem, tb) : batch_grid_of(k_batch_trace<false, true>, smem, tb);
+  return any_hit ? batch_grid_of(k_batch_trace<true, false>, smem, tb) : batch_grid_of(k_batch_trace<false, false>, smem, tb);
 }
 
-int batch_trace_mixed_grid(int stack_cap, bool wide) {
-  const size_t smem = batch_smem(stack_cap);
-  return wide ? batch_grid_of(k_batch_trace_mixed<true>, smem) : batch_grid_of(k_batch_trace_mixed<false>, smem);
+int batch_trace_mixed_grid(int stack_cap, bool wide, int tb) {
+  const size_t smem = batch_smem(stack_cap, tb);
+  return wide ? batch_grid_of(k_batch_trace_mixed<true>, smem, tb) : batch_grid_of(k_batch_trace_mixed<false>, smem, tb);
 }
 
 int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, SF<int4> job_pass, const int* q_closest,
                              const int* q_any, RoundCounters* rc, SF<float4> ro, SF<float4> rd, SF<float4> hit,
-                             DevStats* st, int stack_cap, int grid_blocks, cudaStream_t s, const int* sorted,
+                             DevStats* st, int stack_cap, int grid_blocks, int tb, cudaStream_t s, const int* sorted,
                              const RaySortCtl* rs) {
-  const size_t smem = batch_smem(stack_cap);
+  const size_t smem = batch_smem(stack_cap, tb);
   if (wide)
-    k_batch_trace_mixed<true><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, q_closest, q_any, rc, ro, rd, hit,
-                                                                  stack_cap, st, sorted, rs);
+    k_batch_trace_mixed<true><<<grid_blocks, tb, smem, s>>>(jobs, job_pass, q_closest, q_any, rc, ro, rd, hit,
+                                                            stack_cap, st, sorted, rs);
   else
-    k_batch_trace_mixed<false><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, q_closest, q_any, rc, ro, rd, hit,
-                                                                   stack_cap, st, sorted, rs);
+    k_batch_trace_mixed<false><<<grid_blocks, tb, smem, s>>>(jobs, job_pass, q_closest, q_any, rc, ro, rd, hit,
+                                                             stack_cap, st, sorted, rs);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launch_batch_trace(bool any_hit, bool wide, const BatchJob* jobs, SF<int4> job_pass, const int* queue,
                        const int* count, int* work, SF<float4> ro, SF<float4> rd, SF<float4> hit, DevStats* st,
-                       int stack_cap, int grid_blocks, cudaStream_t s) {
-  const size_t smem = batch_smem(stack_cap);
+                       int stack_cap, int grid_blocks, int tb, cudaStream_t s) {
+  const size_t smem = batch_smem(stack_cap, tb);
   if (any_hit && wide)
-    k_batch_trace<true, true><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
-                                                                  stack_cap, st);
+    k_batch_trace<true, true><<<grid_blocks, tb, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
+                                                            stack_cap, st);
   else if (any_hit)
-    k_batch_trace<true, false><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
-                                                                   stack_cap, st);
+    k_batch_trace<true, false><<<grid_blocks, tb, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
+                                                             stack_cap, st);
   else if (wide)
-    k_batch_trace<false, true><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
-                                                                   stack_cap, st);
+    k_batch_trace<false, true><<<grid_blocks, tb, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
+                                                             stack_cap, st);
   else
-    k_batch_trace<false, false><<<grid_blocks, TRACE_TB, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
-                                                                    stack_cap, st);
+    k_batch_trace<false, false><<<grid_blocks, tb, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
+                                                              stack_cap, st);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -7,7 +7,8 @@
 
 namespace yc {
 
-constexpr int TRACE_TB = 128;
+constexpr int TRACE_TB = 128;       // block of the per-pass trace kernels
+constexpr int TRACE_TB_MAX = 256;   // largest block of the batch engine's trace kernels
 
 // warp-reduced traversal counters, one atomic per warp and counter
 template <bool ANY>
@@ -42,7 +43,8 @@ __device__ __forceinline__ void flush_counts(DevStats* st, unsigned rays, const 
 constexpr int REFILL_AT = 8;
 
 // The persistent loop shared by the kernels. Src supplies ray e of the work list and the
-// scene it walks (begin) and stores its result (end).
+// scene it walks (begin) and stores its result (end). Each thread's stack is a column of
+// the block's dynamic shared memory with a stride of the block size.
 template <bool ANY, bool WIDE, class Src>
 __device__ __forceinline__ void trace_loop(Src& src, int n, int* work, int stack_cap, DevStats* st) {
   extern __shared__ int smem[];
@@ -78,7 +80,7 @@ __device__ __forceinline__ void trace_loop(Src& src, int n, int* work, int stack
     }
     if (e_cur >= 0) {
       bool of = false;
-      bool done = (w.link == LINK_NONE) || walk_step<ANY, WIDE>(w, stack, TRACE_TB, stack_cap, wc, of);
+      bool done = (w.link == LINK_NONE) || walk_step<ANY, WIDE>(w, stack, (int)blockDim.x, stack_cap, wc, of);
       if (of) ++overflow;
       if (done) {
         HitOut h;
@@ -134,7 +136,7 @@ __device__ __forceinline__ void trace_loop_mixed(Src& src, int nc, int n, int* w
     }
     if (e_cur >= 0) {
       bool of = false;
-      bool done = (w.link == LINK_NONE) || walk_step_k<WIDE>(w, any, stack, TRACE_TB, stack_cap, wc, of);
+      bool done = (w.link == LINK_NONE) || walk_step_k<WIDE>(w, any, stack, (int)blockDim.x, stack_cap, wc, of);
       if (of) ++overflow;
       if (done) {
         HitOut h;
