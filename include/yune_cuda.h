@@ -132,6 +132,17 @@ int yc_set_lights(yc_ctx* ctx, int scene_id, const yc_quad_light* lights_host, i
 int yc_bvh_build(yc_ctx* ctx, const yc_triangle* tris_host, int n_tri, int bins, int leaf_max, int* n_node,
                  int* depth);
 int yc_bvh_copy_nodes(yc_ctx* ctx, yc_bvh_node* nodes_host, int capacity);
+/* Refit of an uploaded scene for moving geometry (BVH::resizeBvh, src/BVH.cpp:218-247,
+ * and the vertex re-upload of CLManager::setupVertexBuffer), on the device: tris_host holds
+ * new positions and normals of the same n_tri triangles (same order, materials in range);
+ * the stream and shading records are rewritten from them and every box of the hierarchy
+ * is recomputed bottom-up from the triangles' padded boxes (TriangleCPU::computeAABB). The
+ * hierarchy's topology, leaves and tie-break ranks are kept, so a render equals the
+ * reference's with its node array refitted by resizeBvh (yh_bvh_refit) -- as long as the
+ * motion leaves the old hierarchy a fair fit; a large motion calls for a new build and
+ * upload. The first refit of a scene groups its nodes by depth (one copy of the node
+ * links to the host). Synchronous. */
+int yc_refit_scene(yc_ctx* ctx, int scene_id, const yc_triangle* tris_host, int n_tri);
 int yc_release_scene(yc_ctx* ctx, int scene_id);
 /* bytes the scene holds on the device */
 int yc_scene_bytes(yc_ctx* ctx, int scene_id, uint64_t* bytes);

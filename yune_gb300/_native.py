@@ -109,6 +109,7 @@ SIGNATURES = {
     "yc_bvh_build": (i32, [vp, vp, i32, i32, i32, C.POINTER(i32), C.POINTER(i32)]),
     "yc_bvh_copy_nodes": (i32, [vp, vp, i32]),
     "yc_release_scene": (i32, [vp, i32]),
+    "yc_refit_scene": (i32, [vp, i32, vp, i32]),
     "yc_scene_bytes": (i32, [vp, i32, C.POINTER(C.c_uint64)]),
     "yc_scene_depth": (i32, [vp, i32, C.POINTER(i32)]),
     "yc_scene_layout": (i32, [vp, i32, i32, vp, i32, i32, vp]),

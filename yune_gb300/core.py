@@ -90,6 +90,12 @@ class Renderer:
         N.check(self.L.yc_bvh_copy_nodes(self.h, ptr(nodes), n.value), "yc_bvh_copy_nodes")
         return nodes, d.value
 
+    def refit(self, sid, tris):
+        """Moves the uploaded scene's triangles to `tris` (same triangles, new positions) and
+        refits its hierarchy on the device (yc_refit_scene)."""
+        t = np.ascontiguousarray(tris)
+        N.check(self.L.yc_refit_scene(self.h, sid, ptr(t), len(t)), "yc_refit_scene")
+
     def scene_bytes(self, sid):
         """Bytes the scene holds on the device."""
         b = C.c_uint64()

@@ -80,6 +80,12 @@ struct Scene {
   yc::DevScene dev{};
   uint64_t bytes = 0;
   bool has_specular = false;   // a mirror or dielectric material: shading paths diverge most
+  // yc_refit_scene: the nodes by depth (made on the first refit) and the new triangles
+  DevBuf<int> refit_order;
+  std::vector<int> refit_levels;
+  bool refit_ready = false;
+  DevBuf<yc_triangle> refit_tris;
+  DevBuf<float4> refit_root;
 };
 
 struct Accum {
@@ -704,6 +710,97 @@ int yc_set_lights(yc_ctx* c, int scene_id, const yc_quad_light* lights, int n_li
   YC_CUDA(cudaMemcpyAsync(s->lights.p, lights, n_light * sizeof(yc_quad_light), cudaMemcpyHostToDevice, c->stream));
   YC_CUDA(cudaStreamSynchronize(c->stream));
   s->dev.n_lights = n_light;
+  return YC_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// the nodes of scene s grouped by depth, deepest first (from the links of its node array)
+int make_refit_plan(yc_ctx* c, Scene* s) {
+  const bool wide = s->dev.wide != 0;
+  const size_t per = wide ? 8 : 4;
+  const size_t n = s->dev.root_link >= 0 && s->dev.root_link != yc::LINK_NONE ? s->nodes.n / per : 0;
+  std::vector<int> links(n * (wide ? 4 : 2));
+  if (n > 0)   // the link words of each node record, gathered with one strided copy
+    YC_CUDA(cudaMemcpy2DAsync(links.data(), (wide ? 4 : 2) * sizeof(int), s->nodes.p + (per - (wide ? 2 : 1)),
+                              per * sizeof(float4), (wide ? 4 : 2) * sizeof(int), n, cudaMemcpyDeviceToHost, c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  const int nc = wide ? 4 : 2;
+  std::vector<int> depth(n, -1);
+  std::vector<int> q;
+  if (n > 0) {
+    depth[s->dev.root_link] = 0;
+    q.push_back(s->dev.root_link);
+  }
+  int max_d = 0;
+  for (size_t i = 0; i < q.size(); ++i) {
+    const int node = q[i];
+    for (int k = 0; k < nc; ++k) {
+      const int l = links[(size_t)node * nc + k];
+      if (l >= 0 && l != yc::LINK_NONE && (size_t)l < n && depth[l] < 0) {
+        depth[l] = depth[node] + 1;
+        max_d = std::max(max_d, depth[l]);
+        q.push_back(l);
+      }
+    }
+  }
+  std::vector<int> order;
+  order.reserve(q.size());
+  s->refit_levels.clear();
+  for (int d = max_d; d >= 0 && !q.empty(); --d) {
+    s->refit_levels.push_back((int)order.size());
+    for (int node : q)
+      if (depth[node] == d) order.push_back(node);
+  }
+  s->refit_levels.push_back((int)order.size());
+  YC_CUDA(s->refit_order.alloc(std::max<size_t>(order.size(), 1)));
+  if (!order.empty())
+    YC_CUDA(cudaMemcpyAsync(s->refit_order.p, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice,
+                            c->stream));
+  YC_CUDA(s->refit_root.alloc(2));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  s->refit_ready = true;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int yc_refit_scene(yc_ctx* c, int scene_id, const yc_triangle* tris, int n_tri) {
+  if (!c || (n_tri > 0 && !tris)) return fail(YC_E_INVALID, "NULL argument");
+  Scene* s = find_scene(c, scene_id);
+  if (!s) return fail(YC_E_NOTFOUND, "unknown scene");
+  if (n_tri != s->dev.n_tri) return fail(YC_E_INVALID, "a refit keeps the scene's triangles: counts differ");
+  for (int i = 0; i < n_tri; ++i)
+    if (tris[i].matID < 0 || tris[i].matID >= s->dev.n_mat)
+      return fail(YC_E_INVALID, "triangle " + std::to_string(i) + " has matID out of range");
+  YC_CUDA(cudaSetDevice(c->device));
+  if (!s->refit_ready)
+    if (int r = make_refit_plan(c, s)) return r;
+  if (s->refit_tris.n < (size_t)n_tri) YC_CUDA(s->refit_tris.alloc(std::max(n_tri, 1)));
+  if (n_tri > 0)
+    YC_CUDA(cudaMemcpyAsync(s->refit_tris.p, tris, (size_t)n_tri * sizeof(yc_triangle), cudaMemcpyHostToDevice,
+                            c->stream));
+  yc::RefitPlan plan;
+  plan.order = s->refit_order.p;
+  plan.level_off = s->refit_levels;
+  // a scene without a BVH walks a chain of unbounded boxes: nothing to refit there
+  const bool refit_nodes = s->dev.root_test != 0;
+  const int n_slots = (int)(s->tris.n / 3);
+  if (yc::launch_refit(plan, s->refit_tris.p, n_tri, s->nodes.p, s->tris.p, n_slots, s->shade.p, s->dev.wide != 0,
+                       s->dev.root_link, refit_nodes, s->refit_root.p, c->stream))
+    return fail(YC_E_LAUNCH, std::string("refit: ") + cudaGetErrorString(cudaGetLastError()));
+  float4 root[2];
+  if (refit_nodes && s->dev.root_link != yc::LINK_NONE)
+    YC_CUDA(cudaMemcpyAsync(root, s->refit_root.p, sizeof root, cudaMemcpyDeviceToHost, c->stream));
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  if (refit_nodes && s->dev.root_link != yc::LINK_NONE) {
+    s->dev.root_lo = root[0];
+    s->dev.root_hi = root[1];
+  }
   return YC_OK;
 }
 

@@ -134,6 +134,18 @@ struct PassParams {
   int mis, rr_threshold, max_depth, brdf_model, mis_lobe_fix;
 };
 
+// refit.cu: the nodes of an uploaded scene grouped by depth, deepest level first: order
+// (device) lists node indices, level_off (host) the start of each level in it
+struct RefitPlan {
+  int* order = nullptr;
+  std::vector<int> level_off;
+};
+// rewrites the stream and shading records from new triangles (device) and, with
+// refit_nodes, every child box level by level and the scene box (root_out: lo, hi)
+int launch_refit(const RefitPlan& plan, const yc_triangle* tris_dev, int n_tri, float4* nodes, float4* stream,
+                 int n_slots, float4* shade, bool wide, int root_link, bool refit_nodes, float4* root_out,
+                 cudaStream_t s);
+
 // launchers (udpt.cu / trace.cu)
 void launch_raygen(const PassParams& pp, const PathState& ps, int* q_closest, RoundCounters* rc, DevStats* st,
                    cudaStream_t s);
