@@ -850,6 +850,14 @@ def run_mix(args, rank, local, ws, dist):
     same = True
     for a, c in zip(acc_p, acc_b):
         same = same and bool(np.array_equal(r.read_accum(a).view(np.int32), r.read_accum(c).view(np.int32)))
+    # image error of the jobs with a converged FP64 reference (tests/golden/fp64_c2_j*.npz)
+    from yune_gb300 import quality
+    image_error = {}
+    for j in (0, 8, 16):
+        if j < len(jobs):
+            rep_j = quality.report(r.read_accum(acc_b[j]), "c2_j%d" % j, Wm + R * K)
+            if rep_j:
+                image_error["c2_j%d" % j] = rep_j
     # profiled copies (per-kernel events; no graph): two passes of every job batched, one plain
     prof = slice(Wm + R * K, Wm + R * K + 2)
     scratch = [r.alloc_accum(s.width, s.height) for s in jobs]
@@ -954,6 +962,7 @@ def run_mix(args, rank, local, ws, dist):
                       "d2h_bytes_per_step": acc_bytes,
                       "path": "per step and job: yc_set_camera + yc_render_passes + yc_tonemap to host"},
         "clocks": clk.summary(),
+        "image_error": image_error,
         "host": {"scene_build_s": build_s, "upload_s": upload_s, "autotune_s": tune_s, "autotune_trials": len(trials),
                  "replay_s": replay_s},
         "stack_overflow": int(sum(x["overflow"] for x in reps)),

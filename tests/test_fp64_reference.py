@@ -79,3 +79,22 @@ def test_reference_mis_branch_converges_above_next_event_only():
     z = err.mean() / (err.std() / np.sqrt(len(err)))
     rel = err.mean() / nee["ref"][:, :3].mean()
     assert z > 5.0 and 0.005 < rel < 0.02
+
+
+@pytest.mark.parametrize("name", ["c2_j0", "c2_j8", "c2_j16", "c3_s2", "c3_s4"])
+def test_mix_and_pool_references_are_unbiased(name):
+    """The references of three jobs of the mixed workload and two scenes of the serving
+    pool (the benchmark's options: NEE + MIS, Oren-Nayar, roulette after bounce 3, at most
+    16 bounces) against 32 independent FP64 passes of the same pixels."""
+    import importlib.util
+    import os
+    spec = importlib.util.spec_from_file_location(
+        "make_fp64_refs", os.path.join(os.path.dirname(__file__), "golden", "make_fp64_refs.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    ref = quality.load_reference(name)
+    assert ref is not None and ref["n_pass"] == 65536
+    s = mk.scene_of(name)
+    short = O.reference_pixels_f64(s, ref["xs"], ref["ys"], scenes.mt19937(101, 32), s.cfg)
+    err = (short[:, :3] - ref["ref"][:, :3]).mean(axis=1)
+    assert abs(err.mean()) < 5.0 * err.std() / np.sqrt(len(err))
