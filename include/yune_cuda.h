@@ -257,7 +257,10 @@ typedef struct yc_batch_cfg {
   int32_t sort_threshold;      /* shade queues of at least this many paths are sorted by path
                                   phase and material class before the logic kernel; 0 = never */
   int32_t groups;              /* slot groups whose rounds run concurrently (1..8); 0 = 2 */
-  int32_t ray_sort;            /* sort key of each round's rays (as YC_OPT_RAY_SORT); 0 = the
+  int32_t ray_sort;            /* sort key of each round's rays: job bits * 100 + origin bits * 10
+                                  + direction bits per axis (as YC_OPT_RAY_SORT, plus the low job
+                                  bits of each ray's job, so that rays of different scenes do not
+                                  share warps; 3 * (origin + direction) + job bits <= 15); 0 = the
                                   context's YC_OPT_RAY_SORT, -1 = rays in queue order */
   int32_t trace_block;         /* threads per block of the traversal kernels (a multiple of 32
                                   up to 256): with the stack columns of its threads it sets the
@@ -291,7 +294,7 @@ int yc_batch_destroy(yc_batch* b);
  * into scratch accumulators under each candidate, timed with CUDA events. The search runs
  * one parameter at a time from *start -- pool_paths (512K..4M, at most the mix's pixels
  * rounded up to a power of two), rounds_per_launch (4/8/16), logic_blocks_per_sm (2/4/8),
- * sort_threshold (0, 64K, 256K), groups (1/2/4), ray_sort (off, 32) and trace_block
+ * sort_threshold (0, 64K, 256K), groups (1/2/4), ray_sort (off, 32, 322) and trace_block
  * (64/128/256 threads) -- keeping the best value of each, and sweeps again while a sweep
  * moved the shape (at most `sweeps` sweeps). start->stack_cap must hold the deepest
  * scene (depth + 2; the stack depth is not searched: a shorter stack fails the walks).

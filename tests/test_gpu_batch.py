@@ -75,10 +75,11 @@ def test_batch_separate_trace_launches_match(groups):
         b.close()
 
 
-@pytest.mark.parametrize("groups", [1, 3])
-def test_batch_ray_sort_matches(groups):
-    """With every round's rays sorted by origin and direction cell (threshold 1), the
-    batch still gives the per-pass path's accumulators bit for bit."""
+@pytest.mark.parametrize("groups,key", [(1, 0), (3, 0), (2, 322), (1, 111)])
+def test_batch_ray_sort_matches(groups, key):
+    """With every round's rays sorted by origin and direction cell (threshold 1), or by
+    job and cell (key = job bits * 100 + origin bits * 10 + direction bits), the batch
+    still gives the per-pass path's accumulators bit for bit."""
     jobs = _jobs()
     with Renderer(0) as r:
         ids = [r.upload(s) for s, _ in jobs]
@@ -89,7 +90,7 @@ def test_batch_ray_sort_matches(groups):
             r.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
             want.append(r.read_accum(aid))
         r.set_ray_sort(3, 2, min_rays=1)
-        b = Batch(r, pool_paths=4096, rounds_per_launch=4, use_graph=True, groups=groups)
+        b = Batch(r, pool_paths=4096, rounds_per_launch=4, use_graph=True, groups=groups, ray_sort=key)
         accs = []
         for (s, seeds), sid in zip(jobs, ids):
             aid = r.alloc_accum(s.width, s.height)

@@ -375,7 +375,7 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
   if (raysort) {
     if (int e = ensure_raysort(c, (size_t)W * H)) return e;
     rsb = yc::RaySortBufs{c->rs_keys.p, c->rs_hist.p, c->rs_cursor.p, c->rs_blk.p, c->rs_sorted.p, c->rs_ctl.p,
-                          c->rs_ob, c->rs_db, c->rs_threshold};
+                          c->rs_ob, c->rs_db, 0, c->rs_threshold};
   }
   // shade-queue sort by phase and material class before the logic kernel (unidirectional
   // passes whose frame can fill a sorted queue, in scenes with a mirror or dielectric:
@@ -1178,7 +1178,7 @@ struct yc_batch {
   int grid_c = 0, grid_a = 0, grid_m = 0, logic_grid = 0;
   bool mixed = true;   // YC_OPT_MIXED_TRACE of the context when the batch was created
   bool raysort = false;   // YC_OPT_RAY_SORT / _MIN of the context when the batch was created
-  int rs_ob = 0, rs_db = 0, rs_threshold = 0;
+  int rs_ob = 0, rs_db = 0, rs_jb = 0, rs_threshold = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool started = false;
@@ -1218,7 +1218,7 @@ int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
   cudaStream_t sa = serial ? c->stream : g.side;
   if (b->mixed) {   // both ray kinds of the round in one launch
     yc::RaySortBufs rsb{g.rs_keys.p, g.rs_hist.p, g.rs_cursor.p, g.rs_blk.p, g.rs_sorted.p, g.rs_ctl.p, b->rs_ob,
-                        b->rs_db, b->rs_threshold};
+                        b->rs_db, b->rs_jb, b->rs_threshold};
     if (b->raysort) {
       KTimer kt(c, K_RAYSORT, timed);
       yc::launch_raysort_batch(b->jobs.p, batch_state(b).job, in_c, in_a, rin, ps.ro, ps.rd, rsb, b->logic_grid, sm);
@@ -1331,10 +1331,13 @@ int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
   if (b->cfg.ray_sort < 0) {
     b->rs_ob = b->rs_db = 0;
   } else if (b->cfg.ray_sort > 0) {
-    const int ob = b->cfg.ray_sort / 10, db = b->cfg.ray_sort % 10;
-    if (ob > 3 || db > 3 || ob + db > 5) return fail(YC_E_INVALID, "ray_sort: origin bits * 10 + direction bits, sum <= 5");
+    const int jb = b->cfg.ray_sort / 100, ob = (b->cfg.ray_sort / 10) % 10, db = b->cfg.ray_sort % 10;
+    if (ob > 3 || db > 3 || ob + db > 5 || 3 * (ob + db) + jb > 15)
+      return fail(YC_E_INVALID, "ray_sort: job bits * 100 + origin bits * 10 + direction bits, "
+                                "3 * (origin + direction) + job bits <= 15");
     b->rs_ob = ob;
     b->rs_db = db;
+    b->rs_jb = jb;
   }
   if (b->cfg.pool_paths <= 0) b->cfg.pool_paths = 1 << 21;
   if (b->cfg.rounds_per_launch <= 0) b->cfg.rounds_per_launch = 8;
@@ -1373,7 +1376,7 @@ int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
     }
     b->raysort = b->mixed && (b->rs_ob + b->rs_db) > 0 && b->rs_threshold > 0 && m >= (size_t)b->rs_threshold;
     if (b->raysort) {
-      const size_t bins = (size_t)yc::raysort_bins(b->rs_ob, b->rs_db);
+      const size_t bins = (size_t)yc::raysort_bins(b->rs_ob, b->rs_db, b->rs_jb);
       YC_CUDA(g->rs_keys.alloc(m));
       YC_CUDA(g->rs_sorted.alloc(m));
       YC_CUDA(g->rs_hist.alloc(bins));

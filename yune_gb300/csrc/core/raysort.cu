@@ -4,6 +4,8 @@
 // divergent branches per warp and more L1 hits. Before the mixed trace launch the
 // round's rays (closest-hit queue, then any-hit queue) are sorted by a key of
 //   kind (1 bit, closest-hit first, so entries [0, n_closest) stay the closest-hit ones)
+//   | in a batch, the low jb bits of the ray's job (rays of different scenes walk
+//     different trees: keyed by job they stop sharing warps)
 //   | Morton code of the origin's cell in the scene box (ob bits per axis)
 //   | Morton code of the direction's cell in [-1, 1]^3 (db bits per axis)
 // with a counting sort: key and histogram (one atomic per run of equal keys in a warp),
@@ -47,16 +49,22 @@ __device__ __forceinline__ unsigned ray_key(const float4& o, const float4& d, co
   return (mo << (3 * db)) | md;
 }
 
-// the scene box of the ray in slot p: one scene per pass, or the job's scene in a batch
+// the scene box and job of the ray in slot p: one scene per pass, or the job's scene in
+// a batch
 struct BoxOne {
   float4 lo, hi;
-  __device__ __forceinline__ void of(int, float4& l, float4& h) const { l = lo; h = hi; }
+  __device__ __forceinline__ void of(int, float4& l, float4& h, unsigned& job) const {
+    l = lo;
+    h = hi;
+    job = 0;
+  }
 };
 struct BoxBatch {
   const BatchJob* jobs;
   SF<int4> job_pass;
-  __device__ __forceinline__ void of(int p, float4& l, float4& h) const {
-    const DevScene& sc = jobs[job_pass[p].x].pp.sc;
+  __device__ __forceinline__ void of(int p, float4& l, float4& h, unsigned& job) const {
+    job = (unsigned)job_pass[p].x;
+    const DevScene& sc = jobs[job].pp.sc;
     l = sc.root_lo;
     h = sc.root_hi;
   }
@@ -66,13 +74,15 @@ template <class Box>
 __global__ void __launch_bounds__(RS_TB) k_rs_key(Box box, const int* __restrict__ q_closest,
                                                   const int* __restrict__ q_any, const RoundCounters* rc,
                                                   SF<float4> ro, SF<float4> rd,
-                                                  unsigned* keys, unsigned* hist, int threshold, int ob, int db) {
+                                                  unsigned* keys, unsigned* hist, int threshold, int ob, int db,
+                                                  int jb) {
   const int nc = rc->n_closest, n = nc + rc->n_any;
   if (threshold <= 0 || n < threshold) return;   // uniform over the grid
   const int lane = threadIdx.x & 31;
   const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int warps_total = (gridDim.x * blockDim.x) >> 5;
-  const unsigned kind_bit = 1u << (3 * (ob + db));
+  const unsigned kind_bit = 1u << (3 * (ob + db) + jb);
+  const unsigned job_mask = (1u << jb) - 1u;
   // RS_U runs of 32 entries per warp and step: their queue, origin and direction loads
   // are all issued before the first key is formed
   for (int wbase = warp_global * 32 * RS_U; wbase < n; wbase += warps_total * 32 * RS_U) {
@@ -95,8 +105,9 @@ __global__ void __launch_bounds__(RS_TB) k_rs_key(Box box, const int* __restrict
       unsigned key = 0xffffffffu - lane;   // idle lanes match nobody
       if (e < n) {
         float4 lo, hi;
-        box.of(p[u], lo, hi);
-        key = ray_key(o[u], d[u], lo, hi, ob, db) | (e >= nc ? kind_bit : 0u);
+        unsigned job;
+        box.of(p[u], lo, hi, job);
+        key = ray_key(o[u], d[u], lo, hi, ob, db) | ((job & job_mask) << (3 * (ob + db))) | (e >= nc ? kind_bit : 0u);
         keys[e] = key;
       }
       const unsigned peers = __match_any_sync(0xffffffffu, key);
@@ -208,13 +219,14 @@ __global__ void __launch_bounds__(RS_TB) k_rs_scatter(const int* __restrict__ q_
   }
 }
 
-int raysort_bins(int ob, int db) { return 1 << (3 * (ob + db) + 1); }
+int raysort_bins(int ob, int db, int jb) { return 1 << (3 * (ob + db) + jb + 1); }
 
 template <class Box>
 static int launch_rs(const Box& box, const int* q_closest, const int* q_any, const RoundCounters* rc,
                      SF<float4> ro, SF<float4> rd, const RaySortBufs& b, int grid, cudaStream_t s) {
-  k_rs_key<Box><<<grid, RS_TB, 0, s>>>(box, q_closest, q_any, rc, ro, rd, b.keys, b.hist, b.threshold, b.ob, b.db);
-  const int nbins = raysort_bins(b.ob, b.db);
+  k_rs_key<Box><<<grid, RS_TB, 0, s>>>(box, q_closest, q_any, rc, ro, rd, b.keys, b.hist, b.threshold, b.ob, b.db,
+                                        b.jb);
+  const int nbins = raysort_bins(b.ob, b.db, b.jb);
   const int nblk = (nbins + RS_SCAN_TB - 1) / RS_SCAN_TB;
   if (nblk > RS_MAX_TILES) return -1;
   k_rs_scan<<<nblk, RS_SCAN_TB, 0, s>>>(rc, b.hist, b.cursor, b.blk_sum, b.ctl, b.threshold, nbins);

@@ -7,7 +7,8 @@
 // run concurrently, the ray sort before the traversal, and the traversal kernels' block
 // (threads per block, which with the per-thread stack columns sets the shared memory per
 // block, hence the blocks and the L1 left per SM). The best values depend on the job mix,
-// so the tuner times candidate shapes on the mix itself: each candidate renders the
+// so the tuner times candidate shapes on the mix itself (the ray sort: off, by origin and
+// direction cell, or by job and cell): each candidate renders the
 // jobs' calibration passes into scratch accumulators, timed with CUDA events on the
 // context stream. It searches one parameter at a time from a starting shape, keeps the
 // best value of each, and repeats the sweep while a sweep changed the shape (up to
@@ -92,7 +93,7 @@ extern "C" int yc_tune_search(const yc_batch_cfg* start, int64_t total_px, int s
       {&yc_batch_cfg::logic_blocks_per_sm, {2, 4, 8}},
       {&yc_batch_cfg::sort_threshold, {0, 1 << 16, 1 << 18}},
       {&yc_batch_cfg::groups, {1, 2, 4}},
-      {&yc_batch_cfg::ray_sort, {-1, 32}},
+      {&yc_batch_cfg::ray_sort, {-1, 32, 322}},
       {&yc_batch_cfg::trace_block, {64, 128, 256}},
   };
   std::vector<std::pair<yc_batch_cfg, float>> timed;

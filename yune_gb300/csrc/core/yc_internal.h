@@ -97,7 +97,8 @@ struct RaySortBufs {
   unsigned* blk_sum;   // tile totals (64 at most)
   int* sorted;         // the sorted work list (path indices)
   RaySortCtl* ctl;
-  int ob, db;          // origin and direction bits per axis (3 * (ob + db) <= 15)
+  int ob, db;          // origin and direction bits per axis
+  int jb;              // job bits of a batch's key (3 * (ob + db) + jb <= 15; 0 for one scene)
   int threshold;       // rounds with fewer rays are traced unsorted
 };
 
@@ -174,7 +175,7 @@ int launch_trace_mixed(const DevScene& sc, const int* q_closest, const int* q_an
                        cudaStream_t s, const int* sorted = nullptr, const RaySortCtl* rs = nullptr);
 // raysort.cu: sorts the round's work list (closest-hit queue, then any-hit queue) into
 // b.sorted when the round has at least b.threshold rays, and sets b.ctl->use
-int raysort_bins(int ob, int db);
+int raysort_bins(int ob, int db, int jb = 0);
 int launch_raysort(const DevScene& sc, const int* q_closest, const int* q_any, const RoundCounters* rc,
                    SF<float4> ro, SF<float4> rd, const RaySortBufs& b, int grid, cudaStream_t s);
 int trace_mixed_grid_blocks(int depth, bool wide);
