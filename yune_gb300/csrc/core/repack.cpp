@@ -121,12 +121,14 @@ bool is_queued(const yc_bvh_node& n) { return n.vert_len > 0 || n.child_idx > 0;
 // ---- SAH hierarchy over the reference leaves ----
 // Each reference leaf keeps its triangles, their order and its tie-break rank; only the
 // interior nodes above the leaves are rebuilt, by a binned surface-area-heuristic split
-// of the leaves' box centroids (32 bins per axis). A node's box is the union of the
+// of the leaves' box centroids (up to 256 bins per axis; each side of a split costs its
+// box area times its triangles). A node's box is the union of the
 // leaf boxes below it, so it contains every box the reference tree places below it and
 // a ray that reaches a leaf in the reference passes every box on the way down here too.
 struct LeafItem {
   float lo[3], hi[3];
   float c[3];
+  int w;   // the leaf's triangles (its cost in the SAH; integer sums are exact in any order)
   int link;
 };
 
@@ -163,7 +165,7 @@ struct SahBuilder {
     return 2.0f * (d0 * d1 + d0 * d2 + d1 * d2);
   }
 
-  static constexpr int NB = 32;   // SAH bins per axis
+  static constexpr int NB = 256;   // SAH bins per axis, at most
 
   // box and centroid box of items [b, e), and the per-axis bins of their centroids:
   // min, max and counts, which are exact in any order, so the chunks of a large range
@@ -171,6 +173,7 @@ struct SahBuilder {
   struct RangeStats {
     float lo[3], hi[3], clo[3], chi[3];
     int cnt[3][NB];
+    int wsum[3][NB];
     float blo[3][NB][3], bhi[3][NB][3];
   };
   static void init_box(float lo[3], float hi[3]) {
@@ -189,20 +192,25 @@ struct SahBuilder {
   }
   // bins of [b, e) on the axes with a positive centroid extent, against the node's
   // centroid box (clo, ext)
-  void binning(int b, int e, const float clo[3], const float ext[3], RangeStats& st) const {
+  // bins for a range of n leaves: 256 for large ranges, fewer (at least 8 per leaf) for
+  // small ones, where the binning of every node would otherwise cost more than its items
+  static int bins_for(int n) { return std::min(NB, std::max(32, 8 * n)); }
+  void binning(int b, int e, const float clo[3], const float ext[3], RangeStats& st, int nb) const {
     for (int k = 0; k < 3; ++k)
-      for (int q = 0; q < NB; ++q) {
+      for (int q = 0; q < nb; ++q) {
         st.cnt[k][q] = 0;
+        st.wsum[k][q] = 0;
         init_box(st.blo[k][q], st.bhi[k][q]);
       }
     float scale[3];
-    for (int k = 0; k < 3; ++k) scale[k] = ext[k] > 0.0f ? NB / ext[k] : 0.0f;
+    for (int k = 0; k < 3; ++k) scale[k] = ext[k] > 0.0f ? nb / ext[k] : 0.0f;
     for (int i = b; i < e; ++i)
       for (int k = 0; k < 3; ++k) {
         if (!(ext[k] > 0.0f)) continue;
         int q = (int)((items[i].c[k] - clo[k]) * scale[k]);
-        q = std::min(NB - 1, std::max(0, q));
+        q = std::min(nb - 1, std::max(0, q));
         st.cnt[k][q]++;
+        st.wsum[k][q] += items[i].w;
         for (int a = 0; a < 3; ++a) {
           st.blo[k][q][a] = std::min(st.blo[k][q][a], items[i].lo[a]);
           st.bhi[k][q][a] = std::max(st.bhi[k][q][a], items[i].hi[a]);
@@ -233,6 +241,7 @@ struct SahBuilder {
           for (int k = 0; k < 3; ++k)
             for (int q = 0; q < NB; ++q) {
               st.cnt[k][q] += o.cnt[k][q];
+              st.wsum[k][q] += o.wsum[k][q];
               for (int a = 0; a < 3; ++a) {
                 st.blo[k][q][a] = std::min(st.blo[k][q][a], o.blo[k][q][a]);
                 st.bhi[k][q][a] = std::max(st.bhi[k][q][a], o.bhi[k][q][a]);
@@ -267,7 +276,8 @@ struct SahBuilder {
     // binned SAH
     float ext3[3];
     for (int k = 0; k < 3; ++k) ext3[k] = chi[k] - clo[k];
-    chunked(b, e, st, false, [&](int cb, int ce, RangeStats& o) { binning(cb, ce, clo, ext3, o); });
+    const int nb = bins_for(e - b);
+    chunked(b, e, st, false, [&](int cb, int ce, RangeStats& o) { binning(cb, ce, clo, ext3, o, nb); });
     int best_axis = -1, best_split = -1;
     float best_cost = INFINITY;
     for (int k = 0; k < 3; ++k) {
@@ -278,22 +288,28 @@ struct SahBuilder {
       const float (*bhi)[3] = st.bhi[k];
       float rlo[NB][3], rhi[NB][3];
       int rcnt[NB];
+      int rw[NB];
       float alo[3] = {INFINITY, INFINITY, INFINITY}, ahi[3] = {-INFINITY, -INFINITY, -INFINITY};
       int ac = 0;
-      for (int q = NB - 1; q >= 0; --q) {
+      int aw = 0;
+      for (int q = nb - 1; q >= 0; --q) {
         for (int a = 0; a < 3; ++a) { alo[a] = std::min(alo[a], blo[q][a]); ahi[a] = std::max(ahi[a], bhi[q][a]); }
         ac += cnt[q];
+        aw += st.wsum[k][q];
         for (int a = 0; a < 3; ++a) { rlo[q][a] = alo[a]; rhi[q][a] = ahi[a]; }
         rcnt[q] = ac;
+        rw[q] = aw;
       }
       float llo[3] = {INFINITY, INFINITY, INFINITY}, lhi[3] = {-INFINITY, -INFINITY, -INFINITY};
       int lc = 0;
-      for (int q = 0; q < NB - 1; ++q) {
+      int lw = 0;
+      for (int q = 0; q < nb - 1; ++q) {
         for (int a = 0; a < 3; ++a) { llo[a] = std::min(llo[a], blo[q][a]); lhi[a] = std::max(lhi[a], bhi[q][a]); }
         lc += cnt[q];
+        lw += st.wsum[k][q];
         const int rc = rcnt[q + 1];
         if (lc == 0 || rc == 0) continue;
-        const float cost = area(llo, lhi) * lc + area(rlo[q + 1], rhi[q + 1]) * rc;
+        const float cost = area(llo, lhi) * (float)lw + area(rlo[q + 1], rhi[q + 1]) * (float)rw[q + 1];
         if (cost < best_cost) { best_cost = cost; best_axis = k; best_split = q; }
       }
     }
@@ -302,10 +318,10 @@ struct SahBuilder {
       mid = (b + e) / 2;   // coincident centroids: split the list in half
     } else {
       const float ext = chi[best_axis] - clo[best_axis];
-      const float scale = NB / ext;
+      const float scale = nb / ext;
       auto left = [&](const LeafItem& it) {
         int q = (int)((it.c[best_axis] - clo[best_axis]) * scale);
-        q = std::min(NB - 1, std::max(0, q));
+        q = std::min(nb - 1, std::max(0, q));
         return q <= best_split;
       };
       mid = (int)(std::partition(items.begin() + b, items.begin() + e, left) - items.begin());
@@ -545,6 +561,7 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
         it.c[k] = 0.5f * (plo[k] + phi[k]);
       }
       it.link = b.fill_leaf(n.vert_list, n.vert_len, i * 16, leaf_first[j]);
+      it.w = n.vert_len;
     });
     SahBuilder sb{items};
     const BinRef root_ref = sb.build(0, (int)items.size(), 0);
