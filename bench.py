@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--sample-every", type=int, default=8, help="c2 CPU baseline: every n-th job of the mix")
     ap.add_argument("--pool", type=int, default=0, help="batch path slots (0: 2M)")
+    ap.add_argument("--shape", default="", help="c2: the batch's launch shape as JSON (BatchShape fields) instead "
+                                                "of the autotuner's, e.g. to profile the tuned shape")
     ap.add_argument("--requests", type=int, default=40)
     ap.add_argument("--rate", type=float, default=20.0, help="c3: Poisson arrival rate (req/s)")
     ap.add_argument("--rates", default="", help="c3: comma list of arrival rates to sweep (overrides --rate)")
@@ -804,7 +806,9 @@ def run_mix(args, rank, local, ws, dist):
     cap = max(r.scene_depth(sid) for sid in sids) + 2
     l2 = r.measure_l2_gbs(48 << 20, 20)
     pk, pk_kind = peaks()
-    if args.pool:
+    if args.shape:
+        shape, trials, tune_s = autotune.BatchShape(**json.loads(args.shape)), [], 0.0
+    elif args.pool:
         shape, trials, tune_s = autotune.BatchShape(pool_paths=args.pool), [], 0.0
     else:   # launch shape from the autotuner (untimed calibration, seeds of its own)
         shape, trials, tune_s = autotune.tune_scenes(r, jobs, sids, stack_cap=cap)

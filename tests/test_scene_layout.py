@@ -49,12 +49,13 @@ def test_layout_sizes(big):
     s, nodes = big
     lay = layout(s.tris, len(s.mats), nodes, 1)
     # 48-byte stream record per triangle, 64-byte shading record per triangle, 64-byte
-    # two-child nodes; materials and the 16-light table as uploaded
+    # two-child nodes; materials as uploaded with their 8-byte Oren-Nayar constants, and
+    # the 16-light table
     assert lay.stream_bytes == 48 * s.n_tri
     assert lay.shade_bytes == 64 * s.n_tri
     assert lay.node_bytes % 64 == 0 and 0 < lay.node_bytes < 64 * len(nodes)
-    assert lay.device_bytes == (lay.node_bytes + lay.stream_bytes + lay.shade_bytes + MATERIAL.itemsize * len(s.mats)
-                                + 16 * QUAD_LIGHT.itemsize)
+    assert lay.device_bytes == (lay.node_bytes + lay.stream_bytes + lay.shade_bytes
+                                + (MATERIAL.itemsize + 8) * len(s.mats) + 16 * QUAD_LIGHT.itemsize)
     assert lay.depth > 0
     # tree modes differ in their nodes, not in the triangle data
     ref = layout(s.tris, len(s.mats), nodes, 0)

@@ -17,6 +17,7 @@
 #include "yc_internal.h"
 #include "yc_noalloc.h"
 #include "yc_repack.h"
+#include "yc_shade.cuh"
 #include "yune_cuda.h"
 
 namespace {
@@ -76,6 +77,7 @@ struct DevBuf {
 struct Scene {
   DevBuf<float4> nodes, tris, shade;
   DevBuf<yc_material> mats;
+  DevBuf<float2> on_ab;
   DevBuf<yc_quad_light> lights;
   yc::DevScene dev{};
   uint64_t bytes = 0;
@@ -292,6 +294,7 @@ yc::PassParams pass_params(const yc_ctx* c, const Scene* sc, const Accum* ac, ui
   pp.accum = ac->buf.p;
   pp.width = ac->w;
   pp.height = ac->h;
+  pp.aspect = yc::frame_aspect(ac->w, ac->h);
   pp.tile_w = (int)std::ceil((float)ac->w / cfg->block_x);
   pp.tile_h = (int)std::ceil((float)ac->h / cfg->block_y);
   pp.off_x = (int)(std::ceil((float)ac->w / cfg->block_x) * (float)(cfg->block % cfg->block_x));
@@ -586,6 +589,7 @@ int yc_upload_scene(yc_ctx* c, const yc_triangle* tris, int n_tri, const yc_mate
   YC_CUDA(s->tris.alloc(std::max<size_t>(rp.tris.size(), 3)));
   YC_CUDA(s->shade.alloc(std::max<size_t>(rp.shade.size(), 4)));
   YC_CUDA(s->mats.alloc(std::max(n_mat, 1)));
+  YC_CUDA(s->on_ab.alloc(std::max(n_mat, 1)));
   YC_CUDA(s->lights.alloc(yc::MAX_LIGHTS));
   if (!rp.nodes.empty())
     YC_CUDA(cudaMemcpyAsync(s->nodes.p, rp.nodes.data(), rp.nodes.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
@@ -593,8 +597,11 @@ int yc_upload_scene(yc_ctx* c, const yc_triangle* tris, int n_tri, const yc_mate
     YC_CUDA(cudaMemcpyAsync(s->tris.p, rp.tris.data(), rp.tris.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
   if (!rp.shade.empty())
     YC_CUDA(cudaMemcpyAsync(s->shade.p, rp.shade.data(), rp.shade.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+  std::vector<float2> on_ab(std::max(n_mat, 1), float2{0.0f, 0.0f});
+  for (int i = 0; i < n_mat; ++i) on_ab[i] = yc::oren_nayar_ab(mats[i].alpha_x);
   if (n_mat > 0)
     YC_CUDA(cudaMemcpyAsync(s->mats.p, mats, n_mat * sizeof(yc_material), cudaMemcpyHostToDevice, c->stream));
+  YC_CUDA(cudaMemcpyAsync(s->on_ab.p, on_ab.data(), on_ab.size() * sizeof(float2), cudaMemcpyHostToDevice, c->stream));
   YC_CUDA(cudaMemcpyAsync(s->lights.p, lights, n_light * sizeof(yc_quad_light), cudaMemcpyHostToDevice, c->stream));
   YC_CUDA(cudaStreamSynchronize(c->stream));
   yc::DevScene& d = s->dev;
@@ -603,6 +610,7 @@ int yc_upload_scene(yc_ctx* c, const yc_triangle* tris, int n_tri, const yc_mate
   d.shade = s->shade.p;
   d.mats = s->mats.p;
   d.lights = s->lights.p;
+  d.on_ab = s->on_ab.p;
   d.n_lights = n_light;
   d.n_tri = n_tri;
   d.n_mat = n_mat;
@@ -612,7 +620,8 @@ int yc_upload_scene(yc_ctx* c, const yc_triangle* tris, int n_tri, const yc_mate
   d.wide = rp.wide;
   d.root_lo = rp.root_lo;
   d.root_hi = rp.root_hi;
-  s->bytes = s->nodes.bytes() + s->tris.bytes() + s->shade.bytes() + s->mats.bytes() + s->lights.bytes();
+  s->bytes = s->nodes.bytes() + s->tris.bytes() + s->shade.bytes() + s->mats.bytes() + s->on_ab.bytes() +
+             s->lights.bytes();
   const int id = c->next_scene++;
   c->scenes[id] = std::move(s);
   *scene_id = id;
@@ -637,7 +646,8 @@ int yc_scene_layout(const yc_triangle* tris, int n_tri, int n_mat, const yc_bvh_
   out->stream_bytes = std::max<size_t>(rp.tris.size(), 3) * sizeof(float4);
   out->shade_bytes = std::max<size_t>(rp.shade.size(), 4) * sizeof(float4);
   out->device_bytes = out->node_bytes + out->stream_bytes + out->shade_bytes +
-                      (uint64_t)std::max(n_mat, 1) * sizeof(yc_material) + yc::MAX_LIGHTS * sizeof(yc_quad_light);
+                      (uint64_t)std::max(n_mat, 1) * (sizeof(yc_material) + sizeof(float2)) +
+                      yc::MAX_LIGHTS * sizeof(yc_quad_light);
   uint64_t h = 0xcbf29ce484222325ull;
   auto words = [&h](const float4* p, size_t n) {
     const uint64_t* w = reinterpret_cast<const uint64_t*>(p);
@@ -1439,6 +1449,7 @@ int yc_batch_add_job(yc_batch* b, int scene_id, int accum_id, const yc_cam* cam,
   j.pp.accum = ac->buf.p;
   j.pp.width = ac->w;
   j.pp.height = ac->h;
+  j.pp.aspect = yc::frame_aspect(ac->w, ac->h);
   j.pp.tile_w = ac->w;
   j.pp.tile_h = ac->h;
   j.pp.gi_check = 1;

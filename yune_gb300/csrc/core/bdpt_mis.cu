@@ -68,10 +68,11 @@ __device__ __forceinline__ f4 mirror(f4 w, f4 n) { return ym::normalize(ym::mul(
 // f_eval and pdf_dir are called, not inlined: the logic kernel's lanes run different
 // states, and one copy of each keeps the code within the instruction cache (measured
 // 1024x1024: 797 against 651 Mrays/s inlined, despite the call's register spills).
-__device__ __noinline__ f4 f_eval(const Vtx& v, const yc_material& m, f4 w_prev, f4 w_next, int brdf_model) {
+__device__ __noinline__ f4 f_eval(const Vtx& v, const yc_material& m, f4 w_prev, f4 w_next, int brdf_model,
+                                  const float2* on_ab) {
   const bool glossy = ym::length3(ld4(m.ks)) != 0.0f;
   f4 f;
-  if (brdf_model == 1 && !glossy) f = oren_nayar(w_next, w_prev, v, m);
+  if (brdf_model == 1 && !glossy) f = oren_nayar(w_next, w_prev, v, m, on_ab[v.mat]);
   else f = ld4(m.kd) * INV_PI_F;
   if (glossy) {
     const float ca = ym::pow(ym::fmax(ym::dot(w_next, mirror(w_prev, v.n)), 0.0f), ym::add(m.px, m.py));
@@ -193,7 +194,7 @@ __global__ void __launch_bounds__(256) k_raygen_bdpt_mis(PassParams pp, PathStat
     const float r1 = draw(seed);
     const float r2 = draw(seed);
     const float fx = ym::add((float)px, r1), fy = ym::add((float)py, r2);
-    const float aspect = (float)(((double)W * 1.0) / (double)H);
+    const float aspect = pp.aspect;
     f4 dir;
     dir.x = (float)((double)aspect * ((2.0 * (double)fx / (double)W) - 1));
     dir.y = (float)((2.0 * (double)fy / (double)H) - 1);
@@ -382,7 +383,7 @@ __global__ void __launch_bounds__(256) k_logic_bdpt_mis(PassParams pp, PathState
             const float w_r = pdf_dir(v, m, wn, lp);
             c_out = ym::dot(wn, v.n);
             acc = ym::add(r, mul0(s, mis(w_r)));
-            bnext = ((cont * f_eval(v, m, lp, wn, pp.brdf_model)) * c_out) / w_f;
+            bnext = ((cont * f_eval(v, m, lp, wn, pp.brdf_model, sc.on_ab)) * c_out) / w_f;
             w_bounce = true;
             ro = v.hp + wn * EPS_F;
             rd = wn;
@@ -462,7 +463,7 @@ __global__ void __launch_bounds__(256) k_logic_bdpt_mis(PassParams pp, PathState
             const float es = mul0(mis(ym::div(ym::mul(ym::mul(cl, INV_PI_F), cy), d2)), ym::add(r_y, mul0(s_y, mis(wr))));
             const float w = ym::div(1.0f, ym::add(ym::add(1.0f, ls), es));
             const float g = ym::div(ym::mul(cy, cl), ym::mul(d2, pk));
-            pend = ((beta * f_eval(y, m, wp, dir, pp.brdf_model)) * rgb(L.ke)) * ym::mul(g, w);
+            pend = ((beta * f_eval(y, m, wp, dir, pp.brdf_model, sc.on_ab)) * rgb(L.ke)) * ym::mul(g, w);
             w_pend = true;
             ro = y.hp + dir * EPS_F;
             rd = dir;
@@ -513,7 +514,7 @@ __global__ void __launch_bounds__(256) k_logic_bdpt_mis(PassParams pp, PathState
             const float w = ym::div(1.0f, ym::add(ym::add(1.0f, ls), es));
             const float g = ym::div(ym::mul(cy, cl), d2);
             const f4 le = rgb(sc.lights[lk].ke) * ym::div(PI_F, p0);
-            pend = ((((beta * f_eval(y, my, wp, dir, pp.brdf_model)) * f_eval(lvx, ml, lp, wl, pp.brdf_model)) *
+            pend = ((((beta * f_eval(y, my, wp, dir, pp.brdf_model, sc.on_ab)) * f_eval(lvx, ml, lp, wl, pp.brdf_model, sc.on_ab)) *
                      ym::mk(f3.x, f3.y, f3.z, 0.0f)) * le) * ym::mul(g, w);
             w_pend = true;
             ro = y.hp + dir * EPS_F;
@@ -553,7 +554,7 @@ __global__ void __launch_bounds__(256) k_logic_bdpt_mis(PassParams pp, PathState
             const float w_r = pdf_dir(y, m, wn, wp);
             c_out = ym::dot(wn, y.n);
             acc = ym::add(r_y, mul0(s_y, mis(w_r)));
-            bnext = ((cont * f_eval(y, m, wp, wn, pp.brdf_model)) * c_out) / w_f;
+            bnext = ((cont * f_eval(y, m, wp, wn, pp.brdf_model, sc.on_ab)) * c_out) / w_f;
             w_bounce = true;
             ro = y.hp + wn * EPS_F;
             rd = wn;

@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(256) k_raygen_tile(PassParams pp, PathState ps
     const float r1 = draw(seed);
     const float r2 = draw(seed);
     const float fx = ym::add((float)px, r1), fy = ym::add((float)py, r2);
-    const float aspect = (float)(((double)W * 1.0) / (double)H);
+    const float aspect = pp.aspect;
     f4 dir;
     dir.x = (float)((double)aspect * ((2.0 * (double)fx / (double)W) - 1));
     dir.y = (float)((2.0 * (double)fy / (double)H) - 1);

@@ -40,8 +40,9 @@ __device__ __forceinline__ HitOut walk_full(const DevScene& sc, const float4& o,
   return h;
 }
 
+// three blocks per SM: up to 170 registers a thread, which the kernel needs without spills
 template <bool WIDE>
-__global__ void __launch_bounds__(TAIL_TB) k_tail(PassParams pp, PathState ps, const int* __restrict__ in_closest,
+__global__ void __launch_bounds__(TAIL_TB, 3) k_tail(PassParams pp, PathState ps, const int* __restrict__ in_closest,
                                                   const int* __restrict__ in_any, RoundCounters* rc_in,
                                                   int threshold, int stack_cap, DevStats* st) {
   extern __shared__ int smem[];

@@ -122,11 +122,16 @@ struct DevStats {
   unsigned long long call_overflow;
 };
 
+// the camera's aspect ratio as createRay computes it (udpt.cl:216-217, in double precision):
+// one value per frame, computed on the host when a pass is set up
+inline float frame_aspect(int width, int height) { return (float)(((double)width * 1.0) / (double)height); }
+
 struct PassParams {
   DevScene sc;
   yc_cam cam;
   float4* accum;
   int width, height;
+  float aspect;            // udpt.cl:216-217 in double precision, set by frame_aspect
   int tile_w, tile_h;      // work-item grid of one block launch
   int off_x, off_y;        // pixel offset of the block (udpt.cl:166-167)
   uint32_t rand_seed;

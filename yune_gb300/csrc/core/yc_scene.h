@@ -44,6 +44,7 @@ struct DevScene {
   const float4* shade;
   const yc_material* mats;
   const yc_quad_light* lights;
+  const float2* on_ab;   // per material: the Oren-Nayar A and B of its sigma^2 (oren_nayar_ab)
   int n_lights;
   int n_tri;
   int n_mat;

@@ -195,8 +195,18 @@ __device__ __forceinline__ float sin_phi(f4 w) {
   if (st <= EPS_F && st >= -EPS_F) return 0.0f;
   return ym::clamp(ym::div(w.y, st), -1.0f, 1.0f);
 }
-// OrenNayarBRDF, udpt-primitives.cl:696-725 (alpha_x holds sigma^2)
-__device__ __forceinline__ f4 oren_nayar(f4 w_i, f4 w_o, const Vtx& v, const yc_material& m) {
+// OrenNayarBRDF, udpt-primitives.cl:696-725 (alpha_x holds sigma^2). A and B depend on
+// the material alone and are computed in double precision; oren_nayar_ab (host and
+// device) is that computation, done once per material at upload (DevScene::on_ab), so a
+// shading step runs no double-precision division.
+__host__ __device__ inline float2 oren_nayar_ab(float alpha_x) {
+  const double s2 = (double)alpha_x;
+  float2 ab;
+  ab.x = (float)(1 - (s2 / (2 * (s2 + 0.33))));
+  ab.y = (float)(0.45 * s2 / (s2 + 0.09));
+  return ab;
+}
+__device__ __forceinline__ f4 oren_nayar(f4 w_i, f4 w_o, const Vtx& v, const yc_material& m, float2 ab) {
   w_i = to_shading(w_i, v);
   w_o = to_shading(w_o, v);
   float costerm = 0.0f;
@@ -205,19 +215,16 @@ __device__ __forceinline__ f4 oren_nayar(f4 w_i, f4 w_o, const Vtx& v, const yc_
   float sa, tb;
   if (ym::fabs(w_i.z) < ym::fabs(w_o.z)) { sa = sin_theta(w_i); tb = ym::div(sin_theta(w_o), ym::fabs(w_o.z)); }
   else { sa = sin_theta(w_o); tb = ym::div(sin_theta(w_i), ym::fabs(w_i.z)); }
-  const double s2 = (double)m.alpha_x;
-  const float A = (float)(1 - (s2 / (2 * (s2 + 0.33))));
-  const float B = (float)(0.45 * s2 / (s2 + 0.09));
-  return (ld4(m.kd) * INV_PI_F) * ym::add(A, ym::mul(B, ym::mul(ym::mul(costerm, sa), tb)));
+  return (ld4(m.kd) * INV_PI_F) * ym::add(ab.x, ym::mul(ab.y, ym::mul(ym::mul(costerm, sa), tb)));
 }
 
 // evaluateBRDF, udpt.cl:611-630 (Oren-Nayar for a probability-1 diffuse lobe when
-// brdf_model = 1, udpt-primitives.cl:673-686)
+// brdf_model = 1, udpt-primitives.cl:673-686; on_ab: the scene's per-material A and B)
 __device__ __forceinline__ f4 brdf(f4 w_i, f4 w_o, const Vtx& v, const yc_material& m, bool glossy, float rr_prob,
-                                   int brdf_model) {
+                                   int brdf_model, const float2* on_ab) {
   const f4 refl = ym::normalize(reflect(w_i, v.n));
   if (!glossy) {
-    if (brdf_model == 1 && rr_prob == 1.0f) return oren_nayar(w_i, w_o, v, m);
+    if (brdf_model == 1 && rr_prob == 1.0f) return oren_nayar(w_i, w_o, v, m, on_ab[v.mat]);
     return (ld4(m.kd) * INV_PI_F) / rr_prob;
   }
   const float ca = ym::pow(ym::fmax(ym::dot(w_o, refl), 0.0f), ym::add(m.px, m.py));

@@ -48,7 +48,7 @@ __device__ __forceinline__ void camera_ray(const PassParams& pp, int px, int py,
   const float r1 = draw(seed);
   const float r2 = draw(seed);
   const float fx = ym::add((float)px, r1), fy = ym::add((float)py, r2);
-  const float aspect = (float)(((double)W * 1.0) / (double)H);
+  const float aspect = pp.aspect;
   f4 dir;
   dir.x = (float)((double)aspect * ((2.0 * (double)fx / (double)W) - 1));
   dir.y = (float)((2.0 * (double)fy / (double)H) - 1);
@@ -190,7 +190,7 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
         if (!occluded) {
           glossy = sample_glossy(m, seed, brdf_prob);
           if (brdf_prob == 0.0f) { dl = em; phase = P_NEE_DELIVER; break; }
-          ls = (brdf(w_i, wo, V, m, glossy, brdf_prob, pp.brdf_model) * lke) * ym::fmax(ym::dot(w_i, V.n), 0.0f);
+          ls = (brdf(w_i, wo, V, m, glossy, brdf_prob, pp.brdf_model, sc.on_ab) * lke) * ym::fmax(ym::dot(w_i, V.n), 0.0f);
           ls = ls * ym::div(1.0f, light_pdf);
         }
         if (!pp.mis) { dl = ls + em; phase = P_NEE_DELIVER; break; }
@@ -231,7 +231,7 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
         const bool glossy = (flags & F_NEE_GLOSSY) != 0;
         float mw = brdf_pdf;
         mw = ym::div(ym::mul(mw, mw), ym::add(ym::mul(light_pdf, light_pdf), ym::mul(brdf_pdf, brdf_pdf)));
-        f4 bs = (brdf(w_i, wo, V, m, glossy, brdf_prob, pp.brdf_model) * ld4(sc.lights[j].ke)) *
+        f4 bs = (brdf(w_i, wo, V, m, glossy, brdf_prob, pp.brdf_model, sc.on_ab) * ld4(sc.lights[j].ke)) *
                 ym::fmax(ym::dot(w_i, V.n), 0.0f);
         bs = bs * ym::div(mw, brdf_pdf);
         dl = (ls + bs) + em;
@@ -274,7 +274,7 @@ __device__ __forceinline__ int logic_path(const PassParams& pp, int reset, const
         }
         if (pdf <= 0.0f) { color = direct + indirect; phase = P_FINISH; break; }
         if (spec) thr_next = thr * ior;
-        else thr_next = ((thr * brdf(nd, wo, V, m, glossy, prob, pp.brdf_model)) * ym::fmax(ym::dot(nd, V.n), 0.0f)) / pdf;
+        else thr_next = ((thr * brdf(nd, wo, V, m, glossy, prob, pp.brdf_model, sc.on_ab)) * ym::fmax(ym::dot(nd, V.n), 0.0f)) / pdf;
         dirty |= D_THR_NEXT;
         flags = spec ? (flags | F_SPEC) : (flags & ~F_SPEC);
         ro = V.hp + nd * EPS_F;
