@@ -266,6 +266,11 @@ typedef struct yc_batch_cfg {
                                   up to 256): with the stack columns of its threads it sets the
                                   shared memory per block and so the blocks and the L1 left
                                   per SM; 0 = 128 */
+  int32_t stack_smem;          /* entries of each walk's stack kept in shared memory; deeper
+                                  entries go to a global spill area of the batch (allocated
+                                  when it first runs). Fewer entries leave more of the SM's L1
+                                  to the node and triangle fetches; a value at or above the
+                                  stack depth keeps the whole stack in shared memory; 0 = 12 */
 } yc_batch_cfg;
 int yc_batch_create(yc_ctx* ctx, const yc_batch_cfg* cfg, yc_batch** out);
 /* Adds a job: n_pass passes of scene_id into accum_id seen from *cam, pass k with
@@ -294,8 +299,9 @@ int yc_batch_destroy(yc_batch* b);
  * into scratch accumulators under each candidate, timed with CUDA events. The search runs
  * one parameter at a time from *start -- pool_paths (512K..4M, at most the mix's pixels
  * rounded up to a power of two), rounds_per_launch (4/8/16), logic_blocks_per_sm (2/4/8),
- * sort_threshold (0, 64K, 256K), groups (1/2/4), ray_sort (off, 32, 322) and trace_block
- * (64/128/256 threads) -- keeping the best value of each, and sweeps again while a sweep
+ * sort_threshold (0, 64K, 256K), groups (1/2/4), ray_sort (off, 32, 322), trace_block
+ * (64/128/256 threads) and stack_smem (8/12/16 entries, or the whole stack) -- keeping the
+ * best value of each, and sweeps again while a sweep
  * moved the shape (at most `sweeps` sweeps). start->stack_cap must hold the deepest
  * scene (depth + 2; the stack depth is not searched: a shorter stack fails the walks).
  * trials (capacity trial_cap) receive every timed shape in order; *n_trials their count.

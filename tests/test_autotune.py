@@ -35,6 +35,14 @@ def test_trace_block_is_searched_and_a_second_sweep_follows_a_move():
     assert {t.trace_block for t, _ in trials} >= {64, 128, 256}
 
 
+def test_stack_split_is_searched():
+    """stack_smem (walk-stack entries kept in shared memory) is a search dimension: 8, 12,
+    16 or the whole stack (64)."""
+    best, trials = autotune.search(START, 8 << 20, lambda shape: abs(shape.stack_smem - 8))
+    assert best.stack_smem == 8
+    assert {t.stack_smem for t, _ in trials} >= {8, 12, 16, 64}
+
+
 def test_small_mixes_calibrate_over_several_passes():
     """A frame smaller than the largest pool is calibrated over enough passes to fill that
     pool four times (at most 16); a large mix needs one pass."""

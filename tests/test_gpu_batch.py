@@ -18,10 +18,12 @@ def _jobs():
     return [(a, scenes.pass_seeds(1, 3)), (b, scenes.pass_seeds(2, 2)), (c, scenes.pass_seeds(3, 5))]
 
 
-@pytest.mark.parametrize("use_graph,pool,sort,groups,tb", [(True, 4096, 0, 1, 0), (False, 1000, 0, 2, 64),
-                                                          (True, 1 << 16, 0, 2, 256), (True, 4096, 1, 3, 32),
-                                                          (False, 1000, 64, 4, 128), (True, 999, 0, 8, 96)])
-def test_batch_matches_per_pass(use_graph, pool, sort, groups, tb):
+# stack_smem: walk-stack entries in shared memory (0: the default 12; 1, 2, 4: most of
+# each walk's stack in the global spill area; 64: all of it in shared memory)
+@pytest.mark.parametrize("use_graph,pool,sort,groups,tb,smem", [(True, 4096, 0, 1, 0, 0), (False, 1000, 0, 2, 64, 4),
+                                                               (True, 1 << 16, 0, 2, 256, 2), (True, 4096, 1, 3, 32, 64),
+                                                               (False, 1000, 64, 4, 128, 1), (True, 999, 0, 8, 96, 12)])
+def test_batch_matches_per_pass(use_graph, pool, sort, groups, tb, smem):
     jobs = _jobs()
     with Renderer(0) as r:
         ids = []
@@ -35,7 +37,7 @@ def test_batch_matches_per_pass(use_graph, pool, sort, groups, tb):
             r.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
             want.append(r.read_accum(aid))
         b = Batch(r, pool_paths=pool, rounds_per_launch=4, use_graph=use_graph, sort_threshold=sort, groups=groups,
-                  trace_block=tb)
+                  trace_block=tb, stack_smem=smem)
         accs = []
         for (s, seeds), sid in zip(jobs, ids):
             aid = r.alloc_accum(s.width, s.height)
@@ -49,8 +51,8 @@ def test_batch_matches_per_pass(use_graph, pool, sort, groups, tb):
         b.close()
 
 
-@pytest.mark.parametrize("groups", [1, 2])
-def test_batch_separate_trace_launches_match(groups):
+@pytest.mark.parametrize("groups,smem", [(1, 0), (2, 2)])
+def test_batch_separate_trace_launches_match(groups, smem):
     """With one traversal launch per ray kind (YC_OPT_MIXED_TRACE = 0) the batch gives the
     same accumulators as the per-pass path, as with the mixed launch."""
     jobs = _jobs()
@@ -63,7 +65,7 @@ def test_batch_separate_trace_launches_match(groups):
             aid = r.alloc_accum(s.width, s.height)
             r.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
             want.append(r.read_accum(aid))
-        b = Batch(r, pool_paths=4096, rounds_per_launch=4, use_graph=True, groups=groups)
+        b = Batch(r, pool_paths=4096, rounds_per_launch=4, use_graph=True, groups=groups, stack_smem=smem)
         accs = []
         for (s, seeds), sid in zip(jobs, ids):
             aid = r.alloc_accum(s.width, s.height)

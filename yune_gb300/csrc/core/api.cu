@@ -1156,6 +1156,7 @@ struct BatchGroup {
   DevBuf<yc::SortCtl> sctl;
   DevBuf<yc::RoundCounters> rc;
   DevBuf<yc::BatchCtl> ctl;
+  DevBuf<int> spill;   // walk stack entries beyond the shared-memory part: two launch slots
   cudaStream_t main = nullptr, side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_done = nullptr;
   yc::BatchCtl* ctl_host = nullptr;         // pinned readback
@@ -1184,6 +1185,8 @@ struct yc_batch {
   std::vector<yc::BatchJob> host_jobs;
   long long task_total = 0;
   int stack_cap = 0;
+  int stack_smem = 0;   // walk stack entries in shared memory (the rest spill to BatchGroup::spill)
+  size_t spill_slot = 0;   // ints of one launch's spill columns
   int wide = -1;   // node layout of the batch's scenes (-1: no job yet)
   int grid_c = 0, grid_a = 0, grid_m = 0, logic_grid = 0;
   bool mixed = true;   // YC_OPT_MIXED_TRACE of the context when the batch was created
@@ -1235,7 +1238,7 @@ int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
     }
     KTimer kt(c, K_TRACE, timed);
     yc::launch_batch_trace_mixed(b->wide == 1, b->jobs.p, batch_state(b).job, in_c, in_a, rin, ps.ro, ps.rd, ps.hit,
-                                 c->stats.p, b->stack_cap, b->grid_m, b->cfg.trace_block, sm,
+                                 c->stats.p, b->stack_cap, b->stack_smem, g.spill.p, b->grid_m, b->cfg.trace_block, sm,
                                  b->raysort ? rsb.sorted : nullptr,
                                  b->raysort ? rsb.ctl : nullptr);
   } else {
@@ -1247,13 +1250,14 @@ int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
     {
       KTimer kt(c, K_EXTEND, timed);
       yc::launch_batch_trace(false, b->wide == 1, b->jobs.p, batch_state(b).job, in_c, &rin->n_closest,
-                             &rin->work_closest, ps.ro, ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_c,
-                             b->cfg.trace_block, sm);
+                             &rin->work_closest, ps.ro, ps.rd, ps.hit, c->stats.p, b->stack_cap, b->stack_smem,
+                             g.spill.p, b->grid_c, b->cfg.trace_block, sm);
     }
     {
       KTimer kt(c, K_OCCL, timed);
       yc::launch_batch_trace(true, b->wide == 1, b->jobs.p, batch_state(b).job, in_a, &rin->n_any, &rin->work_any, ps.ro,
-                             ps.rd, ps.hit, c->stats.p, b->stack_cap, b->grid_a, b->cfg.trace_block, sa);
+                             ps.rd, ps.hit, c->stats.p, b->stack_cap, b->stack_smem,
+                             g.spill.p ? g.spill.p + b->spill_slot : nullptr, b->grid_a, b->cfg.trace_block, sa);
     }
     if (!serial) {
       YC_CUDA(cudaEventRecord(g.ev_join, sa));
@@ -1356,6 +1360,8 @@ int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
   if (b->cfg.max_jobs <= 0) b->cfg.max_jobs = 1024;
   if (b->cfg.groups <= 0) b->cfg.groups = 2;
   if (b->cfg.trace_block <= 0) b->cfg.trace_block = 128;
+  if (b->cfg.stack_smem < 0) return fail(YC_E_INVALID, "stack_smem must not be negative");
+  if (b->cfg.stack_smem == 0) b->cfg.stack_smem = 12;
   if (b->cfg.trace_block > 256 || b->cfg.trace_block % 32)
     return fail(YC_E_INVALID, "trace_block must be a multiple of 32 up to 256");
   if (b->cfg.groups > 8 || b->cfg.groups > b->cfg.pool_paths) return fail(YC_E_INVALID, "groups must be 1..8");
@@ -1491,11 +1497,17 @@ int yc_batch_run(yc_batch* b, int max_launches, int* unfinished) {
   YC_CUDA(cudaSetDevice(c->device));
   if (!b->started) {
     if (b->stack_cap <= 0) b->stack_cap = b->cfg.stack_cap > 0 ? b->cfg.stack_cap : 32;
-    b->grid_c = yc::batch_trace_grid(false, b->stack_cap, b->wide == 1, b->cfg.trace_block);
-    b->grid_a = yc::batch_trace_grid(true, b->stack_cap, b->wide == 1, b->cfg.trace_block);
-    b->grid_m = yc::batch_trace_mixed_grid(b->stack_cap, b->wide == 1, b->cfg.trace_block);
+    b->stack_smem = std::min(b->stack_cap, b->cfg.stack_smem);
+    b->grid_c = yc::batch_trace_grid(false, b->stack_smem, b->wide == 1, b->cfg.trace_block);
+    b->grid_a = yc::batch_trace_grid(true, b->stack_smem, b->wide == 1, b->cfg.trace_block);
+    b->grid_m = yc::batch_trace_mixed_grid(b->stack_smem, b->wide == 1, b->cfg.trace_block);
     if (b->grid_c <= 0 || b->grid_a <= 0 || b->grid_m <= 0)
       return fail(YC_E_LAUNCH, "batch trace kernel cannot be resident");
+    if (b->stack_smem < b->stack_cap) {
+      const size_t threads = (size_t)std::max({b->grid_c, b->grid_a, b->grid_m}) * b->cfg.trace_block;
+      b->spill_slot = threads * 2 * (size_t)(b->stack_cap - b->stack_smem);
+      for (auto& g : b->groups) YC_CUDA(g->spill.alloc(2 * b->spill_slot));
+    }
     b->started = true;
   }
   if (int r = begin_call_checks(c)) return r;

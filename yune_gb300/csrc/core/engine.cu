@@ -415,9 +415,9 @@ __global__ void __launch_bounds__(TRACE_TB_MAX) k_batch_trace(const BatchJob* jo
                                                           const int* __restrict__ queue, const int* __restrict__ count,
                                                           int* work, SF<float4> ro,
                                                           SF<float4> rd, SF<float4> hit, int stack_cap,
-                                                          DevStats* st) {
+                                                          DevStats* st, int n_smem, int* spill) {
   BatchSrc<ANY> src{jobs, job_pass, queue, ro, rd, hit};
-  trace_loop<ANY, WIDE>(src, *count, work, stack_cap, st);
+  trace_loop<ANY, WIDE>(src, *count, work, stack_cap, st, n_smem, spill);
 }
 
 // both queues of a round: closest-hit entries first, then any-hit (or the sorted list,
@@ -449,21 +449,25 @@ struct BatchMixedSrc {
   }
 };
 
+// At most 64 registers a thread (four blocks of 256 or eight of 128 threads per SM): with
+// the walk stack mostly outside shared memory (stack_smem) the traversal is bound by the
+// latency of its node and triangle fetches, and the extra warps hide more of it than the
+// few spilled registers cost (measured on the mixed workload: +4% over 78 registers).
 template <bool WIDE>
-__global__ void __launch_bounds__(TRACE_TB_MAX) k_batch_trace_mixed(const BatchJob* jobs, SF<int4> job_pass,
+__global__ void __launch_bounds__(TRACE_TB_MAX, 4) k_batch_trace_mixed(const BatchJob* jobs, SF<int4> job_pass,
                                                                 const int* __restrict__ q_closest,
                                                                 const int* __restrict__ q_any,
                                                                 RoundCounters* rc, SF<float4> ro,
                                                                 SF<float4> rd, SF<float4> hit,
                                                                 int stack_cap, DevStats* st, const int* sorted,
-                                                                const RaySortCtl* rs) {
+                                                                const RaySortCtl* rs, int n_smem, int* spill) {
   const int nc = rc->n_closest;
   BatchMixedSrc src{jobs, job_pass, q_closest, q_any, (rs && rs->use) ? sorted : nullptr, nc, ro, rd, hit};
-  trace_loop_mixed<WIDE>(src, nc, nc + rc->n_any, &rc->work_closest, stack_cap, st);
+  trace_loop_mixed<WIDE>(src, nc, nc + rc->n_any, &rc->work_closest, stack_cap, st, n_smem, spill);
 }
 
-// the stack columns of a block of tb threads
-static size_t batch_smem(int cap, int tb) { return (size_t)tb * 2 * cap * sizeof(int); }
+// the shared-memory stack columns of a block of tb threads (n_smem entries each)
+static size_t batch_smem(int n_smem, int tb) { return (size_t)tb * 2 * n_smem * sizeof(int); }
 
 template <class K>
 static int batch_grid_of(K kernel, size_t smem, int tb) {
@@ -475,48 +479,48 @@ static int batch_grid_of(K kernel, size_t smem, int tb) {
   return per_sm > 0 ? per_sm * sms : -1;
 }
 
-int batch_trace_grid(bool any_hit, int stack_cap, bool wide, int tb) {
-  const size_t smem = batch_smem(stack_cap, tb);
+int batch_trace_grid(bool any_hit, int n_smem, bool wide, int tb) {
+  const size_t smem = batch_smem(n_smem, tb);
   if (wide)
     return any_hit ? batch_grid_of(k_batch_trace<true, true>, smem, tb) : batch_grid_of(k_batch_trace<false, true>, smem, tb);
   return any_hit ? batch_grid_of(k_batch_trace<true, false>, smem, tb) : batch_grid_of(k_batch_trace<false, false>, smem, tb);
 }
 
-int batch_trace_mixed_grid(int stack_cap, bool wide, int tb) {
-  const size_t smem = batch_smem(stack_cap, tb);
+int batch_trace_mixed_grid(int n_smem, bool wide, int tb) {
+  const size_t smem = batch_smem(n_smem, tb);
   return wide ? batch_grid_of(k_batch_trace_mixed<true>, smem, tb) : batch_grid_of(k_batch_trace_mixed<false>, smem, tb);
 }
 
 int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, SF<int4> job_pass, const int* q_closest,
                              const int* q_any, RoundCounters* rc, SF<float4> ro, SF<float4> rd, SF<float4> hit,
-                             DevStats* st, int stack_cap, int grid_blocks, int tb, cudaStream_t s, const int* sorted,
-                             const RaySortCtl* rs) {
-  const size_t smem = batch_smem(stack_cap, tb);
+                             DevStats* st, int stack_cap, int n_smem, int* spill, int grid_blocks, int tb, cudaStream_t s,
+                             const int* sorted, const RaySortCtl* rs) {
+  const size_t smem = batch_smem(n_smem, tb);
   if (wide)
     k_batch_trace_mixed<true><<<grid_blocks, tb, smem, s>>>(jobs, job_pass, q_closest, q_any, rc, ro, rd, hit,
-                                                            stack_cap, st, sorted, rs);
+                                                            stack_cap, st, sorted, rs, n_smem, spill);
   else
     k_batch_trace_mixed<false><<<grid_blocks, tb, smem, s>>>(jobs, job_pass, q_closest, q_any, rc, ro, rd, hit,
-                                                             stack_cap, st, sorted, rs);
+                                                             stack_cap, st, sorted, rs, n_smem, spill);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launch_batch_trace(bool any_hit, bool wide, const BatchJob* jobs, SF<int4> job_pass, const int* queue,
                        const int* count, int* work, SF<float4> ro, SF<float4> rd, SF<float4> hit, DevStats* st,
-                       int stack_cap, int grid_blocks, int tb, cudaStream_t s) {
-  const size_t smem = batch_smem(stack_cap, tb);
+                       int stack_cap, int n_smem, int* spill, int grid_blocks, int tb, cudaStream_t s) {
+  const size_t smem = batch_smem(n_smem, tb);
   if (any_hit && wide)
     k_batch_trace<true, true><<<grid_blocks, tb, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
-                                                            stack_cap, st);
+                                                            stack_cap, st, n_smem, spill);
   else if (any_hit)
     k_batch_trace<true, false><<<grid_blocks, tb, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
-                                                             stack_cap, st);
+                                                             stack_cap, st, n_smem, spill);
   else if (wide)
     k_batch_trace<false, true><<<grid_blocks, tb, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
-                                                             stack_cap, st);
+                                                             stack_cap, st, n_smem, spill);
   else
     k_batch_trace<false, false><<<grid_blocks, tb, smem, s>>>(jobs, job_pass, queue, count, work, ro, rd, hit,
-                                                              stack_cap, st);
+                                                              stack_cap, st, n_smem, spill);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -33,7 +33,8 @@ __device__ __forceinline__ HitOut walk_full(const DevScene& sc, const float4& o,
   walk_begin(sc, r, w);
   bool of = false;
   bool done = w.link == LINK_NONE;
-  while (!done) done = walk_step<ANY, WIDE>(w, stack, TAIL_TB, stack_cap, wc, of);
+  const WalkStack ws{stack, nullptr, TAIL_TB, 0, stack_cap, stack_cap};
+  while (!done) done = walk_step<ANY, WIDE>(w, ws, wc, of);
   if (of) ++overflow;
   HitOut h;
   h.t = w.best; h.u = w.bu; h.v = w.bv; h.tri = w.best_tri;

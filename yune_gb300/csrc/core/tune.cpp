@@ -26,7 +26,7 @@ int set_error(int code, const char* msg);   // api.cu: sets yc_last_error()
 }
 
 static_assert(sizeof(yc_tune_job) == 144, "yc_tune_job: cam, cfg, four ints, a pointer");
-static_assert(sizeof(yc_tune_trial) == 44, "yc_tune_trial: yc_batch_cfg and a float");
+static_assert(sizeof(yc_tune_trial) == 48, "yc_tune_trial: yc_batch_cfg (11 ints) and a float");
 
 namespace {
 
@@ -36,6 +36,9 @@ struct Param {
 };
 
 bool same(const yc_batch_cfg& a, const yc_batch_cfg& b) { return std::memcmp(&a, &b, sizeof a) == 0; }
+
+// stack_smem of a whole stack in shared memory (above any scene's depth + 2)
+constexpr int32_t kWholeStack = 64;
 
 // device milliseconds of the calibration passes of every job under `cfg`
 int calibrate(yc_ctx* ctx, const yc_tune_job* jobs, int n_jobs, const std::vector<int>& accs,
@@ -95,6 +98,7 @@ extern "C" int yc_tune_search(const yc_batch_cfg* start, int64_t total_px, int s
       {&yc_batch_cfg::groups, {1, 2, 4}},
       {&yc_batch_cfg::ray_sort, {-1, 32, 322}},
       {&yc_batch_cfg::trace_block, {64, 128, 256}},
+      {&yc_batch_cfg::stack_smem, {8, 12, 16, kWholeStack}},
   };
   std::vector<std::pair<yc_batch_cfg, float>> timed;
   auto record = [&](const yc_batch_cfg& c, float ms) {
@@ -104,6 +108,7 @@ extern "C" int yc_tune_search(const yc_batch_cfg* start, int64_t total_px, int s
   yc_batch_cfg best = *start;
   if (best.pool_paths <= 0 || best.pool_paths > pool_cap) best.pool_paths = std::min(1 << 21, pool_cap);
   if (best.trace_block <= 0) best.trace_block = 128;
+  if (best.stack_smem <= 0) best.stack_smem = 12;
   float best_ms = clock(&best, user);
   if (best_ms < 0.0f) return yc::set_error(YC_E_LAUNCH, "yc_tune_search: the clock failed");
   record(best, best_ms);

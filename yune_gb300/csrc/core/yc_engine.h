@@ -50,16 +50,19 @@ void launch_batch_logic(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, 
                         unsigned long long* job_done, const int* sorted, const SortCtl* sctl, int grid,
                         cudaStream_t s);
 // tb: threads per block of the trace kernels (32..256, a multiple of 32)
+// The walk stack holds stack_cap entries: n_smem (<= stack_cap) in shared memory, the rest
+// in `spill`, one column per thread of the launch (grid_blocks * tb columns of
+// 2 * (stack_cap - n_smem) ints; may be null when n_smem == stack_cap).
 int launch_batch_trace(bool any_hit, bool wide, const BatchJob* jobs, SF<int4> job_pass, const int* queue,
                        const int* count, int* work, SF<float4> ro, SF<float4> rd, SF<float4> hit, DevStats* st,
-                       int stack_cap, int grid_blocks, int tb, cudaStream_t s);
-int batch_trace_grid(bool any_hit, int stack_cap, bool wide, int tb);
+                       int stack_cap, int n_smem, int* spill, int grid_blocks, int tb, cudaStream_t s);
+int batch_trace_grid(bool any_hit, int n_smem, bool wide, int tb);
 // one launch over both queues of a round (closest-hit entries, then any-hit); the work
 // cursor is rc->work_closest
 int launch_batch_trace_mixed(bool wide, const BatchJob* jobs, SF<int4> job_pass, const int* q_closest,
                              const int* q_any, RoundCounters* rc, SF<float4> ro, SF<float4> rd, SF<float4> hit,
-                             DevStats* st, int stack_cap, int grid_blocks, int tb, cudaStream_t s,
-                             const int* sorted = nullptr, const RaySortCtl* rs = nullptr);
+                             DevStats* st, int stack_cap, int n_smem, int* spill, int grid_blocks, int tb,
+                             cudaStream_t s, const int* sorted = nullptr, const RaySortCtl* rs = nullptr);
 // the same shade-queue sort for the per-pass path (one scene)
 void launch_pass_sort(const DevScene& sc, bool bdpt, const PathState& ps, const int* in_closest, const int* in_any,
                       const RoundCounters* rc_in, int* keys, int* sorted, SortCtl* sctl, int threshold, int grid,
@@ -68,6 +71,6 @@ void launch_pass_sort(const DevScene& sc, bool bdpt, const PathState& ps, const 
 int launch_raysort_batch(const BatchJob* jobs, SF<int4> job_pass, const int* q_closest, const int* q_any,
                          const RoundCounters* rc, SF<float4> ro, SF<float4> rd, const RaySortBufs& b, int grid,
                          cudaStream_t s);
-int batch_trace_mixed_grid(int stack_cap, bool wide, int tb);
+int batch_trace_mixed_grid(int n_smem, bool wide, int tb);
 
 }  // namespace yc

@@ -195,7 +195,7 @@ __device__ __forceinline__ float sin_phi(f4 w) {
   if (st <= EPS_F && st >= -EPS_F) return 0.0f;
   return ym::clamp(ym::div(w.y, st), -1.0f, 1.0f);
 }
-// OrenNayarBRDF, udpt-primitives.cl:696-725 (alpha_x holds sigma^2). A and B depend on
+// OrenNayarBRDF, udpt-primitives.cl:696-725 (alpha_x holds sigma^2). A and B (:722-723) depend on
 // the material alone and are computed in double precision; oren_nayar_ab (host and
 // device) is that computation, done once per material at upload (DevScene::on_ab), so a
 // shading step runs no double-precision division.

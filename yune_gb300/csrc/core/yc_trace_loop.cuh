@@ -42,13 +42,27 @@ __device__ __forceinline__ void flush_counts(DevStats* st, unsigned rays, const 
 // Lanes refill when at least this many of a warp's 32 lanes are idle.
 constexpr int REFILL_AT = 8;
 
-// The persistent loop shared by the kernels. Src supplies ray e of the work list and the
-// scene it walks (begin) and stores its result (end). Each thread's stack is a column of
-// the block's dynamic shared memory with a stride of the block size.
-template <bool ANY, bool WIDE, class Src>
-__device__ __forceinline__ void trace_loop(Src& src, int n, int* work, int stack_cap, DevStats* st) {
+// The walk stack of this thread: its first n_smem entries in a column of the block's
+// dynamic shared memory (stride: the block size), the rest of stack_cap in a column of
+// `spill` (stride: the grid's threads; unused when n_smem == stack_cap)
+__device__ __forceinline__ WalkStack thread_stack(int stack_cap, int n_smem, int* spill) {
   extern __shared__ int smem[];
-  int* stack = smem + threadIdx.x;
+  WalkStack ws;
+  ws.s = smem + threadIdx.x;
+  ws.stride = (int)blockDim.x;
+  ws.gstride = (int)(gridDim.x * blockDim.x);
+  ws.g = spill ? spill + (blockIdx.x * blockDim.x + threadIdx.x) : nullptr;
+  ws.cap = stack_cap;
+  ws.n_smem = n_smem < stack_cap ? n_smem : stack_cap;
+  return ws;
+}
+
+// The persistent loop shared by the kernels. Src supplies ray e of the work list and the
+// scene it walks (begin) and stores its result (end). Each thread's stack is thread_stack.
+template <bool ANY, bool WIDE, class Src>
+__device__ __forceinline__ void trace_loop(Src& src, int n, int* work, int stack_cap, DevStats* st,
+                                           int n_smem = 1 << 30, int* spill = nullptr) {
+  const WalkStack stack = thread_stack(stack_cap, n_smem, spill);
   const int lane = threadIdx.x & 31;
   unsigned long long overflow = 0;
   WalkCount wc;
@@ -80,7 +94,7 @@ __device__ __forceinline__ void trace_loop(Src& src, int n, int* work, int stack
     }
     if (e_cur >= 0) {
       bool of = false;
-      bool done = (w.link == LINK_NONE) || walk_step<ANY, WIDE>(w, stack, (int)blockDim.x, stack_cap, wc, of);
+      bool done = (w.link == LINK_NONE) || walk_step<ANY, WIDE>(w, stack, wc, of);
       if (of) ++overflow;
       if (done) {
         HitOut h;
@@ -100,9 +114,9 @@ __device__ __forceinline__ void trace_loop(Src& src, int n, int* work, int stack
 // list runs dry are a smaller share of the launch. Each lane counts its walk's work
 // under its ray's kind.
 template <bool WIDE, class Src>
-__device__ __forceinline__ void trace_loop_mixed(Src& src, int nc, int n, int* work, int stack_cap, DevStats* st) {
-  extern __shared__ int smem[];
-  int* stack = smem + threadIdx.x;
+__device__ __forceinline__ void trace_loop_mixed(Src& src, int nc, int n, int* work, int stack_cap, DevStats* st,
+                                                 int n_smem = 1 << 30, int* spill = nullptr) {
+  const WalkStack stack = thread_stack(stack_cap, n_smem, spill);
   const int lane = threadIdx.x & 31;
   unsigned long long overflow = 0;
   WalkCount wc, wc_ext, wc_any;   // the current ray's walk, and the totals per kind
@@ -136,7 +150,7 @@ __device__ __forceinline__ void trace_loop_mixed(Src& src, int nc, int n, int* w
     }
     if (e_cur >= 0) {
       bool of = false;
-      bool done = (w.link == LINK_NONE) || walk_step_k<WIDE>(w, any, stack, (int)blockDim.x, stack_cap, wc, of);
+      bool done = (w.link == LINK_NONE) || walk_step_k<WIDE>(w, any, stack, wc, of);
       if (of) ++overflow;
       if (done) {
         HitOut h;

@@ -258,30 +258,57 @@ __device__ __forceinline__ bool walk_leaf(Walk& w, int link, WalkCount& wc, bool
   return false;
 }
 
+// A walk's stack of (subtree link, entry distance) pairs, at most `cap` deep: entries
+// [0, n_smem) in this thread's column of the block's shared memory (stride: the block
+// size), deeper ones in its column of a global spill area (stride: the grid's threads).
+// A short shared part leaves more of the SM's unified L1 and shared memory to the node
+// and triangle fetches; n_smem == cap (g unused) keeps the whole stack in shared memory.
+struct WalkStack {
+  int* s;
+  int* g;
+  int stride, gstride, n_smem, cap;
+  __device__ __forceinline__ void put(int i, int link, float t) const {
+    if (i < n_smem) {
+      s[(2 * i) * stride] = link;
+      s[(2 * i + 1) * stride] = __float_as_int(t);
+    } else {
+      const size_t j = (size_t)(2 * (i - n_smem)) * gstride;
+      g[j] = link;
+      g[j + gstride] = __float_as_int(t);
+    }
+  }
+  __device__ __forceinline__ float t_at(int i) const {
+    return __int_as_float(i < n_smem ? s[(2 * i + 1) * stride] : g[(size_t)(2 * (i - n_smem) + 1) * gstride]);
+  }
+  __device__ __forceinline__ int link_at(int i) const {
+    return i < n_smem ? s[(2 * i) * stride] : g[(size_t)(2 * (i - n_smem)) * gstride];
+  }
+};
+
 // pops the next subtree whose entry is still within reach (LINK_NONE: the walk ends)
-__device__ __forceinline__ int walk_pop(Walk& w, const int* stack, int stride) {
+__device__ __forceinline__ int walk_pop(Walk& w, const WalkStack& st) {
   while (w.sp > 0) {
     --w.sp;
-    const float te = __int_as_float(stack[(2 * w.sp + 1) * stride]);
+    const float te = st.t_at(w.sp);
     if (!(te > cull_bound(w.best))) {
       w.link_t = te;
-      return stack[(2 * w.sp) * stride];
+      return st.link_at(w.sp);
     }
   }
   return LINK_NONE;
 }
 
 // the pending subtree, unless a hit found since it was chosen puts it out of reach
-__device__ __forceinline__ int walk_recheck(Walk& w, int link, const int* stack, int stride) {
-  if (link != LINK_NONE && w.link_t > cull_bound(w.best)) return walk_pop(w, stack, stride);
+__device__ __forceinline__ int walk_recheck(Walk& w, int link, const WalkStack& st) {
+  if (link != LINK_NONE && w.link_t > cull_bound(w.best)) return walk_pop(w, st);
   return link;
 }
 
 // One interior node of the two-child layout: returns the next node (the nearer child
 // hit, the other one pushed), or the next subtree popped from the stack when neither
 // child is hit. LINK_NONE: the walk is over (or the stack bound was reached).
-__device__ __forceinline__ int visit2(Walk& w, bool any, int link, int* stack, int stride, int stack_cap,
-                                      WalkCount& wc, bool& overflow) {
+__device__ __forceinline__ int visit2(Walk& w, bool any, int link, const WalkStack& st, WalkCount& wc,
+                                      bool& overflow) {
   const float4* nd = w.nodes + 4 * (size_t)link;
   const ulonglong2 nx = __ldg(reinterpret_cast<const ulonglong2*>(nd + 0));   // (lo pair, hi pair)
   const ulonglong2 ny = __ldg(reinterpret_cast<const ulonglong2*>(nd + 1));
@@ -312,16 +339,15 @@ __device__ __forceinline__ int visit2(Walk& w, bool any, int link, int* stack, i
   h1 = h1 && n3.y != LINK_NONE;
   if (h0 && h1) {
     const bool swap = t1 < t0;
-    if (w.sp >= stack_cap) { overflow = true; w.sp = 0; return LINK_NONE; }
-    stack[(2 * w.sp + 0) * stride] = swap ? n3.x : n3.y;
-    stack[(2 * w.sp + 1) * stride] = __float_as_int(swap ? t0 : t1);
+    if (w.sp >= st.cap) { overflow = true; w.sp = 0; return LINK_NONE; }
+    st.put(w.sp, swap ? n3.x : n3.y, swap ? t0 : t1);
     ++w.sp;
     w.link_t = swap ? t1 : t0;
     return swap ? n3.y : n3.x;
   }
   if (h0) { w.link_t = t0; return n3.x; }
   if (h1) { w.link_t = t1; return n3.y; }
-  return walk_pop(w, stack, stride);
+  return walk_pop(w, st);
 }
 
 // (t, link) compare-exchange: the smaller entry distance first
@@ -335,8 +361,8 @@ __device__ __forceinline__ void cx(float& ta, int& la, float& tb, int& lb) {
 // One interior node of the four-child layout (yc_scene.h, wide nodes): the four child
 // boxes are tested with the reference's slab arithmetic, the hits sorted by entry
 // distance, the nearest returned and the others pushed farthest first.
-__device__ __forceinline__ int visit4(Walk& w, bool any, int link, int* stack, int stride, int stack_cap,
-                                      WalkCount& wc, bool& overflow) {
+__device__ __forceinline__ int visit4(Walk& w, bool any, int link, const WalkStack& st, WalkCount& wc,
+                                      bool& overflow) {
   const float INF = __int_as_float(0x7f800000);
   const float4* nd = w.nodes + 8 * (size_t)link;
   const float4 lx = __ldg(nd + 0), hx = __ldg(nd + 1);
@@ -367,14 +393,13 @@ __device__ __forceinline__ int visit4(Walk& w, bool any, int link, int* stack, i
   cx(t[0], l[0], t[2], l[2]);
   cx(t[1], l[1], t[3], l[3]);
   cx(t[1], l[1], t[2], l[2]);
-  if (l[0] == LINK_NONE) return walk_pop(w, stack, stride);
+  if (l[0] == LINK_NONE) return walk_pop(w, st);
   const int extra = (l[1] != LINK_NONE) + (l[2] != LINK_NONE) + (l[3] != LINK_NONE);
-  if (w.sp + extra > stack_cap) { overflow = true; w.sp = 0; return LINK_NONE; }
+  if (w.sp + extra > st.cap) { overflow = true; w.sp = 0; return LINK_NONE; }
 #pragma unroll
   for (int c = 3; c >= 1; --c) {
     if (l[c] != LINK_NONE) {
-      stack[(2 * w.sp + 0) * stride] = l[c];
-      stack[(2 * w.sp + 1) * stride] = __float_as_int(t[c]);
+      st.put(w.sp, l[c], t[c]);
       ++w.sp;
     }
   }
@@ -394,31 +419,29 @@ __device__ __forceinline__ int visit4(Walk& w, bool any, int link, int* stack, i
 // `any` selects the any-hit walk (it stops at the first hit); callers that know the kind
 // at compile time use walk_step<ANY, WIDE>, the mixed trace loop passes it per lane.
 template <bool WIDE>
-__device__ __forceinline__ bool walk_step_k(Walk& w, bool any, int* stack, int stride, int stack_cap, WalkCount& wc,
-                                            bool& overflow) {
+__device__ __forceinline__ bool walk_step_k(Walk& w, bool any, const WalkStack& st, WalkCount& wc, bool& overflow) {
   // (an any-hit walk keeps its segment length until it stops: nothing to check again)
-  int link = any ? w.link : walk_recheck(w, w.link, stack, stride);
+  int link = any ? w.link : walk_recheck(w, w.link, st);
   int leaf = LINK_NONE;
   while (link >= 0 && link != LINK_NONE) {
-    link = WIDE ? visit4(w, any, link, stack, stride, stack_cap, wc, overflow)
-                : visit2(w, any, link, stack, stride, stack_cap, wc, overflow);
+    link = WIDE ? visit4(w, any, link, st, wc, overflow) : visit2(w, any, link, st, wc, overflow);
     if (link < 0 && link != LINK_NONE && leaf == LINK_NONE) {
       leaf = link;
-      link = walk_pop(w, stack, stride);
+      link = walk_pop(w, st);
     }
     if (!__any_sync(__activemask(), leaf == LINK_NONE)) break;
   }
   if (leaf == LINK_NONE && link < 0 && link != LINK_NONE) {
     leaf = link;
-    link = walk_pop(w, stack, stride);
+    link = walk_pop(w, st);
   }
   while (leaf != LINK_NONE) {
     if (walk_leaf(w, leaf, wc, any)) { w.sp = 0; w.link = LINK_NONE; return true; }
     leaf = LINK_NONE;
-    if (!any) link = walk_recheck(w, link, stack, stride);
+    if (!any) link = walk_recheck(w, link, st);
     if (link < 0 && link != LINK_NONE) {   // a second leaf met by the speculative walk
       leaf = link;
-      link = walk_pop(w, stack, stride);
+      link = walk_pop(w, st);
     }
   }
   w.link = link;
@@ -426,9 +449,8 @@ __device__ __forceinline__ bool walk_step_k(Walk& w, bool any, int* stack, int s
 }
 
 template <bool ANY, bool WIDE>
-__device__ __forceinline__ bool walk_step(Walk& w, int* stack, int stride, int stack_cap, WalkCount& wc,
-                                          bool& overflow) {
-  return walk_step_k<WIDE>(w, ANY, stack, stride, stack_cap, wc, overflow);
+__device__ __forceinline__ bool walk_step(Walk& w, const WalkStack& st, WalkCount& wc, bool& overflow) {
+  return walk_step_k<WIDE>(w, ANY, st, wc, overflow);
 }
 
 }  // namespace yc
