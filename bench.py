@@ -79,6 +79,9 @@ def parse():
     ap.add_argument("--pool", type=int, default=0, help="batch path slots (0: 2M)")
     ap.add_argument("--shape", default="", help="c2: the batch's launch shape as JSON (BatchShape fields) instead "
                                                 "of the autotuner's, e.g. to profile the tuned shape")
+    ap.add_argument("--traffic-only", action="store_true",
+                    help="c2: only two passes of every job through the batch engine (no graph), then print the "
+                         "rays its traversal launches walked: the run an ncu capture of their DRAM bytes divides by")
     ap.add_argument("--requests", type=int, default=40)
     ap.add_argument("--rate", type=float, default=20.0, help="c3: Poisson arrival rate (req/s)")
     ap.add_argument("--rates", default="", help="c3: comma list of arrival rates to sweep (overrides --rate)")
@@ -362,7 +365,16 @@ def replay_sample(jobs, seeds, every=128):
     return {k: tuple(v) for k, v in out.items()}
 
 
-def _trace_roofline(st, kt, l2, pk, pk_kind, kernel_mixed, kernel_extend, replay=None):
+# DRAM bytes (read + write) per walked ray of k_batch_trace_mixed on the mixed workload
+# with the default tree (mode 1): one ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum, one pass) of all 320 launches of two passes of the 64 jobs,
+# 87,115,783,168 + 12,610,023,424 bytes over 452,296,636 walked rays; the command and the
+# per-launch spread are in profiles/k_batch_trace_mixed_c2_dram_traffic.md. A launch's
+# traffic is this figure times the rays it walks.
+MIX_TRACE_DRAM_BYTES_PER_RAY = (87115783168 + 12610023424) / 452296636
+
+
+def _trace_roofline(st, kt, l2, pk, pk_kind, kernel_mixed, kernel_extend, replay=None, dram_per_ray=None):
     """Roofline of the traversal kernel over its event time. achieved: the algorithmic
     bytes of the rays it walked -- 32 B per child box and 48 B per triangle a lone walk of
     the ray needs (replay: per-ray counts from the host replay of a sample of the same
@@ -411,6 +423,12 @@ def _trace_roofline(st, kt, l2, pk, pk_kind, kernel_mixed, kernel_extend, replay
     if mixed:
         out["closest_rays"] = int(st["ext_rays"])
         out["any_rays"] = int(st["any_rays"])
+        launches = kt.get("trace_launches", 0)
+        if dram_per_ray and launches:
+            out["traffic"] = dram_per_ray * rays / launches
+            out["traffic_source"] = ("DRAM bytes per walked ray from one ncu capture of this kernel on this "
+                                     "workload, times the rays per launch of this run")
+            out["algorithmic_bytes_per_launch"] = nbytes / launches
     return out
 
 
@@ -813,6 +831,25 @@ def run_mix(args, rank, local, ws, dist):
     else:   # launch shape from the autotuner (untimed calibration, seeds of its own)
         shape, trials, tune_s = autotune.tune_scenes(r, jobs, sids, stack_cap=cap)
     cfg = mix_cfg()
+    if args.traffic_only:
+        acc = [r.alloc_accum(s.width, s.height) for s in jobs]
+        bt = Batch(r, stack_cap=cap, use_graph=False, max_jobs=len(jobs), **shape.kwargs())
+        for s, sid, a, sd in zip(jobs, sids, acc, seeds):
+            bt.add_job(sid, a, s.cam, sd[:2], cfg, reset_first=1)
+        r.synchronize()
+        r.reset_stats()
+        r.set_profiling(True)
+        bt.run()
+        kt_t, st_t = r.kernel_times(), r.stats()
+        r.set_profiling(False)
+        bt.close()
+        if rank == 0:
+            print(json.dumps({"traffic_run": "two passes of every job, batch engine without a graph",
+                              "jobs": len(jobs), "shape": shape.kwargs(),
+                              "walked_rays": int(st_t["ext_rays"] + st_t["any_rays"]),
+                              "trace_launches": int(kt_t["trace_launches"]), "trace_ms": kt_t["trace_ms"]}))
+        r.close()
+        return
     acc_p = [r.alloc_accum(s.width, s.height) for s in jobs]
     acc_b = [r.alloc_accum(s.width, s.height) for s in jobs]
     # warm-up: W passes of every job in each form
@@ -954,7 +991,8 @@ def run_mix(args, rank, local, ws, dist):
                                    "trace": kt_p["trace_ms"], "sort": kt_p["sort_ms"], "logic": kt_p["logic_ms"],
                                    "tail": kt_p["tail_ms"], "rounds": kt_p["rounds"]},
         "roofline": _trace_roofline(st_bp, kt_b, l2, pk, pk_kind, "k_batch_trace_mixed (closest + any-hit rays)",
-                                    "k_batch_trace<closest> (extend)", replay),
+                                    "k_batch_trace<closest> (extend)", replay,
+                                    dram_per_ray=MIX_TRACE_DRAM_BYTES_PER_RAY if args.tree == 1 else None),
         "plain_roofline": _trace_roofline(st_pp, kt_p, l2, pk, pk_kind, "k_trace_paths_mixed (closest + any-hit rays)",
                                           "k_trace_paths<closest> (extend)", replay),
         "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else 0.0, "unit": METRIC, "passes_per_step": E,

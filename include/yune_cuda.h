@@ -168,7 +168,7 @@ int yc_scene_layout(const yc_triangle* tris_host, int n_tri, int n_mat, const yc
                     int tree_mode, yc_scene_layout_info* out);
 
 /* The traversal's algorithmic work on explicit rays, counted on the host without a
- * device: the upload's repack of these arrays (tree_mode 0 or 1), then each ray walked
+ * device: the upload's repack of these arrays (tree_mode 0, 1 or 2), then each ray walked
  * alone in the device walk's order (nearer child first, the same distance cull, the
  * reference's slab and Moller-Trumbore arithmetic) but without the speculation of a warp
  * whose lanes walk together. *boxes and *tris_tested receive the child boxes (32 B each)

@@ -1,7 +1,7 @@
 """The host replay of the traversal (yc_walk_counts), which counts the algorithmic work
 of the traversal roofline: one ray at a time in the device walk's order, without a warp's
 speculation. Its results must be the reference's (closest triangle and t bit for bit, the
-any-hit verdict), in both tree modes it walks; and the oracle's record of the rays a pass
+any-hit verdict), in every tree mode; and the oracle's record of the rays a pass
 walks must hold the rays the core walks (camera rays: one per pixel)."""
 import numpy as np
 import pytest
@@ -11,7 +11,7 @@ from yune_gb300 import _native as N
 from yune_gb300 import scenes, workloads
 
 
-@pytest.mark.parametrize("tree", [0, 1])
+@pytest.mark.parametrize("tree", [0, 1, 2])
 @pytest.mark.parametrize("name", ["c0", "c1"])
 def test_replay_hits_equal_the_reference(name, tree):
     s = scenes.c0(32, 32) if name == "c0" else scenes.c1(32, 32, level=4)
@@ -50,7 +50,7 @@ def test_recorded_rays_of_a_pass():
     assert (tri >= 0).mean() > 0.5
 
 
-def test_replay_refuses_four_child_nodes():
+def test_replay_refuses_an_unknown_tree_mode():
     s = scenes.c0(8, 8)
     with pytest.raises(N.YuneError):
-        scenes.walk_counts(s, O.seeded_rays(s, 10), tree_mode=2)
+        scenes.walk_counts(s, O.seeded_rays(s, 10), tree_mode=7)

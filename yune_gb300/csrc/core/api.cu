@@ -671,8 +671,8 @@ int yc_walk_counts(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes,
                    const float* rays9, int n, int any_hit, uint64_t* boxes, uint64_t* tris_tested, int* tri_out,
                    float* t_out) {
   if (!boxes || !tris_tested || n < 0 || (n > 0 && !rays9)) return fail(YC_E_INVALID, "bad argument");
-  if (tree_mode != yc::TREE_REFERENCE && tree_mode != yc::TREE_SAH_OVER_LEAVES)
-    return fail(YC_E_INVALID, "the host replay walks tree modes 0 and 1");
+  if (tree_mode != yc::TREE_REFERENCE && tree_mode != yc::TREE_SAH_OVER_LEAVES && tree_mode != yc::TREE_WIDE4)
+    return fail(YC_E_INVALID, "bad tree mode");
   yc::Repacked rp;
   std::string err;
   if (yc::repack_scene(tris, n_tri, nodes, n_node, tree_mode, rp, err)) return fail(YC_E_INVALID, err);

@@ -17,6 +17,7 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "yc_repack.h"
@@ -112,8 +113,8 @@ bool tri_test(const HostRay& r, const float4& a, const float4& b, const float4& 
 
 int walk_counts_host(const Repacked& rp, const float* rays9, int n, bool any, uint64_t* boxes_out,
                      uint64_t* tris_out, int* tri_out, float* t_out, std::string& err) {
-  if (rp.wide) {
-    err = "the host replay walks two-child nodes (tree modes 0 and 1)";
+  if (rp.wide > 1) {
+    err = "the host replay walks two-child and four-child float nodes (tree modes 0, 1 and 2)";
     return -1;
   }
   uint64_t boxes = 0, tris = 0;
@@ -170,6 +171,37 @@ int walk_counts_host(const Repacked& rp, const float* rays9, int n, bool any, ui
           }
         }
         link = stop ? (int)LINK_NONE : pop();
+        continue;
+      }
+      if (rp.wide) {   // four-child node (yc_scene.h): lo.x[4], hi.x[4], ..., links; visit4's order
+        const float4* nd = rp.nodes.data() + 8 * (size_t)link;
+        boxes += 4;
+        const float* f = reinterpret_cast<const float*>(nd);
+        int cl[4];
+        std::memcpy(cl, &nd[6], 16);
+        const float cb = cull_bound(best), up = cull_up(best);
+        float t[4];
+        int l[4];
+        for (int c = 0; c < 4; ++c) {
+          const float lo[3] = {f[c], f[8 + c], f[16 + c]}, hi[3] = {f[4 + c], f[12 + c], f[20 + c]};
+          float te;
+          bool h = !r.exact ? box_fast(r, lo, hi, up, !any, te) : (box_ref(r, lo, hi, te) && !(te > cb));
+          h = h && cl[c] != LINK_NONE;
+          t[c] = h ? te : INFINITY;
+          l[c] = h ? cl[c] : (int)LINK_NONE;
+        }
+        auto cx = [&](int a, int b) {
+          if (t[b] < t[a]) { std::swap(t[a], t[b]); std::swap(l[a], l[b]); }
+        };
+        cx(0, 1); cx(2, 3); cx(0, 2); cx(1, 3); cx(1, 2);
+        if (l[0] == LINK_NONE) {
+          link = pop();
+          continue;
+        }
+        for (int c = 3; c >= 1; --c)
+          if (l[c] != LINK_NONE) stack.emplace_back(l[c], t[c]);
+        link_t = t[0];
+        link = l[0];
         continue;
       }
       // two-child node (yc_scene.h): per axis (lo pair, hi pair), then the links
