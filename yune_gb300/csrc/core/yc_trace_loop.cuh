@@ -113,14 +113,19 @@ __device__ __forceinline__ void trace_loop(Src& src, int n, int* work, int stack
 // than two launches over half of them each: the lanes a warp leaves idle once the work
 // list runs dry are a smaller share of the launch. Each lane counts its walk's work
 // under its ray's kind.
+// The per-kind totals (rays, child boxes and triangles of closest-hit and any-hit walks)
+// are kept in shared memory, added once per finished ray, rather than in six registers
+// of every thread for the whole launch.
 template <bool WIDE, class Src>
 __device__ __forceinline__ void trace_loop_mixed(Src& src, int nc, int n, int* work, int stack_cap, DevStats* st,
                                                  int n_smem = 1 << 30, int* spill = nullptr) {
+  __shared__ unsigned s_tot[6];   // closest: rays, boxes, triangles; any-hit: the same
+  if (threadIdx.x < 6) s_tot[threadIdx.x] = 0;
+  __syncthreads();
   const WalkStack stack = thread_stack(stack_cap, n_smem, spill);
   const int lane = threadIdx.x & 31;
-  unsigned long long overflow = 0;
-  WalkCount wc, wc_ext, wc_any;   // the current ray's walk, and the totals per kind
-  unsigned rays_ext = 0, rays_any = 0;
+  unsigned overflow = 0;
+  WalkCount wc;   // the current ray's walk
   Walk w;
   int e_cur = -1;
   bool any = false;
@@ -140,7 +145,6 @@ __device__ __forceinline__ void trace_loop_mixed(Src& src, int nc, int n, int* w
           RayIn r;
           const DevScene& sc = src.begin(e, any, r);
           walk_begin(sc, r, w);
-          if (any) ++rays_any; else ++rays_ext;
         }
       }
     }
@@ -156,15 +160,29 @@ __device__ __forceinline__ void trace_loop_mixed(Src& src, int nc, int n, int* w
         HitOut h;
         h.t = w.best; h.u = w.bu; h.v = w.bv; h.tri = w.best_tri;
         src.end(e_cur, any, h);
-        if (any) { wc_any.nodes += wc.nodes; wc_any.tris += wc.tris; }
-        else { wc_ext.nodes += wc.nodes; wc_ext.tris += wc.tris; }
+        unsigned* t = s_tot + (any ? 3 : 0);
+        atomicAdd(t, 1u);
+        atomicAdd(t + 1, wc.nodes);
+        atomicAdd(t + 2, wc.tris);
         wc.nodes = 0; wc.tris = 0;
         e_cur = -1;
       }
     }
   }
-  flush_counts<false>(st, rays_ext, wc_ext, overflow);
-  flush_counts<true>(st, rays_any, wc_any, 0ull);
+  unsigned long long of = overflow;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) of += __shfl_xor_sync(0xffffffffu, of, off);
+  if (lane == 0 && of) {
+    atomicAdd(&st->stack_overflow, of);
+    atomicAdd(&st->call_overflow, of);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long* dst[6] = {&st->ext_rays, &st->ext_boxes, &st->ext_tris, &st->any_rays, &st->any_boxes,
+                                  &st->any_tris};
+    for (int k = 0; k < 6; ++k)
+      if (s_tot[k]) atomicAdd(dst[k], (unsigned long long)s_tot[k]);
+  }
 }
 
 }  // namespace yc

@@ -193,13 +193,21 @@ struct Walk {
   const float4* nodes;   // the scene of this ray (lanes of one warp may walk different scenes)
   const float4* tris;
   float dx, dy, dz;
-  f32x2 ox2, oy2, oz2, ix2, iy2, iz2;   // origin and 1/direction, each component twice (packed box tests)
-  __device__ __forceinline__ float ox() const { return lo2(ox2); }
-  __device__ __forceinline__ float oy() const { return lo2(oy2); }
-  __device__ __forceinline__ float oz() const { return lo2(oz2); }
-  __device__ __forceinline__ float ix() const { return lo2(ix2); }
-  __device__ __forceinline__ float iy() const { return lo2(iy2); }
-  __device__ __forceinline__ float iz() const { return lo2(iz2); }
+  float ox_, oy_, oz_, ix_, iy_, iz_;   // origin and 1/direction
+  __device__ __forceinline__ float ox() const { return ox_; }
+  __device__ __forceinline__ float oy() const { return oy_; }
+  __device__ __forceinline__ float oz() const { return oz_; }
+  __device__ __forceinline__ float ix() const { return ix_; }
+  __device__ __forceinline__ float iy() const { return iy_; }
+  __device__ __forceinline__ float iz() const { return iz_; }
+  // each component twice, the operand of the packed box tests (built where it is used:
+  // a register pair per component would hold six more registers through the walk)
+  __device__ __forceinline__ f32x2 ox2() const { return pk2(ox_, ox_); }
+  __device__ __forceinline__ f32x2 oy2() const { return pk2(oy_, oy_); }
+  __device__ __forceinline__ f32x2 oz2() const { return pk2(oz_, oz_); }
+  __device__ __forceinline__ f32x2 ix2() const { return pk2(ix_, ix_); }
+  __device__ __forceinline__ f32x2 iy2() const { return pk2(iy_, iy_); }
+  __device__ __forceinline__ f32x2 iz2() const { return pk2(iz_, iz_); }
   float best, bu, bv;
   float best_up;         // cull_up(best)
   int best_tri, best_rank;
@@ -215,8 +223,8 @@ __device__ __forceinline__ void walk_begin(const DevScene& sc, const RayIn& r, W
   w.dx = r.dx; w.dy = r.dy; w.dz = r.dz;
   const float ix = __frcp_rn(r.dx), iy = __frcp_rn(r.dy), iz = __frcp_rn(r.dz);
   w.exact = isinf(ix) || isinf(iy) || isinf(iz);
-  w.ox2 = pk2(r.ox, r.ox); w.oy2 = pk2(r.oy, r.oy); w.oz2 = pk2(r.oz, r.oz);
-  w.ix2 = pk2(ix, ix); w.iy2 = pk2(iy, iy); w.iz2 = pk2(iz, iz);
+  w.ox_ = r.ox; w.oy_ = r.oy; w.oz_ = r.oz;
+  w.ix_ = ix; w.iy_ = iy; w.iz_ = iz;
   w.best = r.tmax; w.bu = 0.0f; w.bv = 0.0f;
   w.best_up = cull_up(r.tmax);
   w.best_tri = -1; w.best_rank = -1;
@@ -317,12 +325,12 @@ __device__ __forceinline__ int visit2(Walk& w, bool any, int link, const WalkSta
   wc.nodes += 2;
   // (lo - o) * inv and (hi - o) * inv of both children, two packed operations per bound
   float ax0, ax1, bx0, bx1, ay0, ay1, by0, by1, az0, az1, bz0, bz1;
-  up2(mul2(sub2(nx.x, w.ox2), w.ix2), ax0, ax1);
-  up2(mul2(sub2(nx.y, w.ox2), w.ix2), bx0, bx1);
-  up2(mul2(sub2(ny.x, w.oy2), w.iy2), ay0, ay1);
-  up2(mul2(sub2(ny.y, w.oy2), w.iy2), by0, by1);
-  up2(mul2(sub2(nz.x, w.oz2), w.iz2), az0, az1);
-  up2(mul2(sub2(nz.y, w.oz2), w.iz2), bz0, bz1);
+  up2(mul2(sub2(nx.x, w.ox2()), w.ix2()), ax0, ax1);
+  up2(mul2(sub2(nx.y, w.ox2()), w.ix2()), bx0, bx1);
+  up2(mul2(sub2(ny.x, w.oy2()), w.iy2()), ay0, ay1);
+  up2(mul2(sub2(ny.y, w.oy2()), w.iy2()), by0, by1);
+  up2(mul2(sub2(nz.x, w.oz2()), w.iz2()), az0, az1);
+  up2(mul2(sub2(nz.y, w.oz2()), w.iz2()), bz0, bz1);
   float t0, t1;
   bool h0, h1;
   if (!w.exact) {   // hit and within the cull bound
