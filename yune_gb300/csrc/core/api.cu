@@ -649,10 +649,17 @@ int yc_scene_layout(const yc_triangle* tris, int n_tri, int n_mat, const yc_bvh_
                       (uint64_t)std::max(n_mat, 1) * (sizeof(yc_material) + sizeof(float2)) +
                       yc::MAX_LIGHTS * sizeof(yc_quad_light);
   uint64_t h = 0xcbf29ce484222325ull;
+  // the 64-bit words are copied out of the float4 bytes (memcpy), not read through a
+  // uint64_t pointer: an aliased read of a float4 object is undefined, and an optimising
+  // compiler may then drop the stores that fill the array (the root box below)
   auto words = [&h](const float4* p, size_t n) {
-    const uint64_t* w = reinterpret_cast<const uint64_t*>(p);
+    const unsigned char* bytes = reinterpret_cast<const unsigned char*>(p);
     h = (h ^ (uint64_t)n) * 0x100000001b3ull;
-    for (size_t i = 0; i < 2 * n; ++i) h = (h ^ w[i]) * 0x100000001b3ull;
+    for (size_t i = 0; i < 2 * n; ++i) {
+      uint64_t w;
+      std::memcpy(&w, bytes + 8 * i, 8);
+      h = (h ^ w) * 0x100000001b3ull;
+    }
   };
   words(rp.nodes.data(), rp.nodes.size());
   words(rp.tris.data(), rp.tris.size());
