@@ -298,7 +298,7 @@ int yc_batch_destroy(yc_batch* b);
  * its calibration passes (seeds_host, n_pass; seeds of their own, not the jobs' real ones)
  * into scratch accumulators under each candidate, timed with CUDA events. The search runs
  * one parameter at a time from *start -- pool_paths (512K..4M, at most the mix's pixels
- * rounded up to a power of two), rounds_per_launch (4/8/16), logic_blocks_per_sm (2/4/8),
+ * rounded up to a power of two), rounds_per_launch (4/8/16/32), logic_blocks_per_sm (2/4/8),
  * sort_threshold (0, 64K, 256K), groups (1/2/4), ray_sort (off, 32, 322), trace_block
  * (64/128/256 threads) and stack_smem (8/12/16 entries, or the whole stack) -- keeping the
  * best value of each, and sweeps again while a sweep

@@ -92,7 +92,7 @@ extern "C" int yc_tune_search(const yc_batch_cfg* start, int64_t total_px, int s
   while (pool_cap < total_px && pool_cap < (1 << 22)) pool_cap <<= 1;
   const std::vector<Param> params = {
       {&yc_batch_cfg::pool_paths, {1 << 19, 1 << 20, 1 << 21, 1 << 22}},
-      {&yc_batch_cfg::rounds_per_launch, {4, 8, 16}},
+      {&yc_batch_cfg::rounds_per_launch, {4, 8, 16, 32}},
       {&yc_batch_cfg::logic_blocks_per_sm, {2, 4, 8}},
       {&yc_batch_cfg::sort_threshold, {0, 1 << 16, 1 << 18}},
       {&yc_batch_cfg::groups, {1, 2, 4}},

@@ -40,7 +40,7 @@ __device__ __forceinline__ void flush_counts(DevStats* st, unsigned rays, const 
 }
 
 // Lanes refill when at least this many of a warp's 32 lanes are idle.
-constexpr int REFILL_AT = 8;
+constexpr int REFILL_AT = 16;
 
 // The walk stack of this thread: its first n_smem entries in a column of the block's
 // dynamic shared memory (stride: the block size), the rest of stack_cap in a column of
