@@ -115,3 +115,14 @@ def test_serve_c_abi_directly():
         aid = r.alloc_accum(24, 20)
         r.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
         assert np.array_equal(out.view(np.int32), r.read_accum(aid).view(np.int32))
+
+
+@pytest.mark.parametrize("tree", [0, 1, 2])
+def test_layout_bytes_are_the_upload_bytes_in_every_tree_mode(tree):
+    """The admission estimate (yc_scene_layout on the host) is what the upload holds on the
+    device (yc_scene_bytes), in each layout a renderer can be set to."""
+    s = scenes.c1(8, 8, level=4)
+    with Renderer(0) as r:
+        r.set_tree_mode(tree)
+        sid = r.upload(s)
+        assert r.scene_bytes(sid) == scenes.device_bytes(s, tree_mode=tree)
