@@ -377,7 +377,7 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
   yc::RaySortBufs rsb{};
   if (raysort) {
     if (int e = ensure_raysort(c, (size_t)W * H)) return e;
-    rsb = yc::RaySortBufs{c->rs_keys.p, c->rs_hist.p, c->rs_cursor.p, c->rs_blk.p, c->rs_sorted.p, c->rs_ctl.p,
+    rsb = yc::RaySortBufs{c->rs_keys.p, nullptr, c->rs_hist.p, c->rs_cursor.p, c->rs_blk.p, c->rs_sorted.p, c->rs_ctl.p,
                           c->rs_ob, c->rs_db, 0, c->rs_threshold};
   }
   // shade-queue sort by phase and material class before the logic kernel (unidirectional
@@ -1223,6 +1223,12 @@ void free_batch(yc_batch* b) {
 yc::PathState batch_state(yc_batch* b) {
   return yc::path_state_at(b->rec.p);
 }
+// where the logic and fill kernels of group g put the ray-sort keys of the rays they
+// queue (raysort.cu sorts every round of a mixed-trace batch by them)
+yc::RsProduce rs_produce(const yc_batch* b, const BatchGroup& g) {
+  if (!b->raysort) return yc::RsProduce{nullptr, nullptr, nullptr, 0, 0, 0};
+  return yc::RsProduce{g.rs_keys.p, g.rs_keys.p + g.count, g.rs_hist.p, b->rs_ob, b->rs_db, b->rs_jb};
+}
 // one round of group g: trace both queues, step every path (A -> B). `serial`: every
 // launch on the context stream (per-kernel timing), else on the group's streams.
 int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
@@ -1237,8 +1243,8 @@ int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
   cudaStream_t sm = serial ? c->stream : g.main;
   cudaStream_t sa = serial ? c->stream : g.side;
   if (b->mixed) {   // both ray kinds of the round in one launch
-    yc::RaySortBufs rsb{g.rs_keys.p, g.rs_hist.p, g.rs_cursor.p, g.rs_blk.p, g.rs_sorted.p, g.rs_ctl.p, b->rs_ob,
-                        b->rs_db, b->rs_jb, b->rs_threshold};
+    yc::RaySortBufs rsb{g.rs_keys.p, g.rs_keys.p + g.count, g.rs_hist.p, g.rs_cursor.p, g.rs_blk.p, g.rs_sorted.p,
+                        g.rs_ctl.p, b->rs_ob, b->rs_db, b->rs_jb, b->rs_threshold};
     if (b->raysort) {
       KTimer kt(c, K_RAYSORT, timed);
       yc::launch_raysort_batch(b->jobs.p, batch_state(b).job, in_c, in_a, rin, ps.ro, ps.rd, rsb, b->logic_grid, sm);
@@ -1281,7 +1287,8 @@ int batch_round(yc_batch* b, BatchGroup& g, int cur, bool timed, bool serial) {
   {
     KTimer kt(c, K_LOGIC, timed);
     yc::launch_batch_logic(b->jobs.p, b->tasks.p, g.ctl.p, ps, batch_state(b).job, g.free_stack.p, in_c, in_a, rin, out_c,
-                           out_a, rout, c->stats.p, b->job_done.p, g.sorted.p, g.sctl.p, b->logic_grid, sm);
+                           out_a, rout, c->stats.p, b->job_done.p, g.sorted.p, g.sctl.p, rs_produce(b, g), b->logic_grid,
+                           sm);
   }
   c->ktimes.rounds++;
   YC_CUDA(cudaPeekAtLastError());
@@ -1303,7 +1310,7 @@ int batch_body(yc_batch* b, bool timed) {
     {
       KTimer kt(c, K_RAYGEN, timed);
       yc::launch_batch_fill(b->jobs.p, b->tasks.p, g.ctl.p, batch_state(b), batch_state(b).job, g.free_stack.p, g.q[0].p,
-                            g.rc.p, c->stats.p, b->logic_grid, sm);
+                            g.rc.p, c->stats.p, rs_produce(b, *gp), b->logic_grid, sm);
     }
     for (int k = 0; k < b->cfg.rounds_per_launch; ++k)
       if (int r = batch_round(b, g, k & 1, timed, serial)) return r;
@@ -1400,7 +1407,7 @@ int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
     b->raysort = b->mixed && (b->rs_ob + b->rs_db) > 0 && b->rs_threshold > 0 && m >= (size_t)b->rs_threshold;
     if (b->raysort) {
       const size_t bins = (size_t)yc::raysort_bins(b->rs_ob, b->rs_db, b->rs_jb);
-      YC_CUDA(g->rs_keys.alloc(m));
+      YC_CUDA(g->rs_keys.alloc(2 * m));   // the closest-hit queue's keys, then the any-hit queue's
       YC_CUDA(g->rs_sorted.alloc(m));
       YC_CUDA(g->rs_hist.alloc(bins));
       YC_CUDA(g->rs_cursor.alloc(bins));

@@ -61,6 +61,27 @@ __device__ __forceinline__ unsigned long long claim_tasks(BatchTasks* tasks, int
   return t;
 }
 
+// ---- ray-sort keys formed by the kernels that queue the rays ----
+// The queued ray of slot p (ps.ro / ps.rd as just written, the scene box of its job) gets
+// the key of k_rs_key (raysort.cu) at its queue position; the warp's equal keys are
+// counted with one histogram atomic. Every lane of the warp calls it (kind 0: no ray).
+__device__ __forceinline__ void produce_key(const RsProduce& rsp, const BatchJob* jobs, const PathState& ps,
+                                            SF<int4> job_pass, int p, int kind, int pos) {
+  const int lane = threadIdx.x & 31;
+  unsigned key = 0xffffffffu - lane;   // lanes without a ray match nobody
+  if (kind) {
+    const float4 o = ps.ro[p], d = ps.rd[p];
+    const unsigned job = (unsigned)job_pass[p].x;
+    const DevScene& sc = jobs[job].pp.sc;
+    key = ray_key(o, d, sc.root_lo, sc.root_hi, rsp.ob, rsp.db) |
+          ((job & ((1u << rsp.jb) - 1u)) << (3 * (rsp.ob + rsp.db))) |
+          (kind == 2 ? 1u << (3 * (rsp.ob + rsp.db) + rsp.jb) : 0u);
+    (kind == 1 ? rsp.keys_c : rsp.keys_a)[pos] = key;
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, key);
+  if (kind && lane == __ffs(peers) - 1) atomicAdd(&rsp.hist[key], (unsigned)__popc(peers));
+}
+
 // ---- fill: idle slots (on the free stack) take new tasks ----
 // k_batch_plan claims, in one thread, as many tasks as there are free slots; k_batch_fill
 // then starts them across the grid.
@@ -78,7 +99,8 @@ __global__ void k_batch_plan(BatchTasks* tasks, BatchCtl* ctl) {
 __global__ void __launch_bounds__(ENGINE_TB) k_batch_fill(const BatchJob* __restrict__ jobs,
                                                           const BatchTasks* tasks, const BatchCtl* ctl,
                                                           PathState ps, SF<int4> job_pass, const int* free_stack,
-                                                          int* q_closest, RoundCounters* rc, DevStats* st) {
+                                                          int* q_closest, RoundCounters* rc, DevStats* st,
+                                                          RsProduce rsp) {
   const int n = ctl->fill_n;
   const int top = ctl->fill_top;
   const unsigned long long t0 = ctl->fill_t0;
@@ -101,7 +123,9 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_fill(const BatchJob* __rest
     int b = 0;
     if (lane == 0) b = atomicAdd(&rc->n_closest, __popc(m));
     b = __shfl_sync(0xffffffffu, b, 0);
-    if (active) q_closest[b + __popc(m & ((1u << lane) - 1))] = p;
+    const int pos = b + __popc(m & ((1u << lane) - 1));
+    if (active) q_closest[pos] = p;
+    if (rsp.keys_c) produce_key(rsp, jobs, ps, job_pass, p, active ? 1 : 0, pos);
     started += __popc(m);
   }
   if (lane == 0 && started) {
@@ -112,9 +136,10 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_fill(const BatchJob* __rest
 }
 
 void launch_batch_fill(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, SF<int4> job_pass,
-                       int* free_stack, int* q_closest, RoundCounters* rc, DevStats* st, int grid, cudaStream_t s) {
+                       int* free_stack, int* q_closest, RoundCounters* rc, DevStats* st, const RsProduce& rsp, int grid,
+                       cudaStream_t s) {
   k_batch_plan<<<1, 32, 0, s>>>(tasks, ctl);
-  k_batch_fill<<<grid, ENGINE_TB, 0, s>>>(jobs, tasks, ctl, ps, job_pass, free_stack, q_closest, rc, st);
+  k_batch_fill<<<grid, ENGINE_TB, 0, s>>>(jobs, tasks, ctl, ps, job_pass, free_stack, q_closest, rc, st, rsp);
 }
 
 // ---- logic with regeneration ----
@@ -125,7 +150,8 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __res
                                                            const int* __restrict__ in_any, const RoundCounters* rc_in,
                                                            int* out_closest, int* out_any, RoundCounters* rc_out,
                                                            DevStats* st, unsigned long long* job_done,
-                                                           const int* __restrict__ sorted, const SortCtl* sctl) {
+                                                           const int* __restrict__ sorted, const SortCtl* sctl,
+                                                           RsProduce rsp) {
   __shared__ unsigned long long s_cnt[8];
   if (threadIdx.x < 8) s_cnt[threadIdx.x] = 0;
   __syncthreads();
@@ -200,8 +226,10 @@ __global__ void __launch_bounds__(ENGINE_TB) k_batch_logic(const BatchJob* __res
     bc = __shfl_sync(0xffffffffu, bc, 0);
     ba = __shfl_sync(0xffffffffu, ba, 0);
     const unsigned below = (1u << lane) - 1;
-    if (emit == 1) out_closest[bc + __popc(mc & below)] = p;
-    if (emit == 2) out_any[ba + __popc(ma & below)] = p;
+    const int pos = emit == 1 ? bc + __popc(mc & below) : ba + __popc(ma & below);
+    if (emit == 1) out_closest[pos] = p;
+    if (emit == 2) out_any[pos] = p;
+    if (rsp.keys_c) produce_key(rsp, jobs, ps, job_pass, p, emit, pos);
     unsigned v[7] = {lc.rays, lc.ext, lc.shadow, lc.mis, lc.trav, lc.samples, lc.prim};
 #pragma unroll
     for (int q = 0; q < 7; ++q) {
@@ -227,9 +255,9 @@ void launch_batch_logic(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, 
                         int* free_stack,
                         const int* in_closest, const int* in_any, const RoundCounters* rc_in, int* out_closest,
                         int* out_any, RoundCounters* rc_out, DevStats* st, unsigned long long* job_done,
-                        const int* sorted, const SortCtl* sctl, int grid, cudaStream_t s) {
+                        const int* sorted, const SortCtl* sctl, const RsProduce& rsp, int grid, cudaStream_t s) {
   k_batch_logic<<<grid, ENGINE_TB, 0, s>>>(jobs, tasks, ctl, ps, job_pass, free_stack, in_closest, in_any, rc_in,
-                                           out_closest, out_any, rc_out, st, job_done, sorted, sctl);
+                                           out_closest, out_any, rc_out, st, job_done, sorted, sctl, rsp);
 }
 
 // ---- shade-queue sort (counting sort over SORT_KEYS keys) ----

@@ -10,7 +10,9 @@
 //   | Morton code of the direction's cell in [-1, 1]^3 (db bits per axis)
 // with a counting sort: key and histogram (one atomic per run of equal keys in a warp),
 // an exclusive scan in tiles of 1024 bins (which also clears the histogram for the next
-// round), and a scatter of the path indices. The key and scatter kernels are bound by
+// round), and a scatter of the path indices. In the batch engine the kernels that queue
+// the rays (logic, fill) form the keys and fill the histogram themselves, from the ray
+// they just wrote (RsProduce, engine.cu), and only the scan and the scatter run here. The key and scatter kernels are bound by
 // the latency of dependent loads and of the cursor atomics, so each warp keeps four runs
 // of 32 entries in flight. The order is a heuristic only: every ray is traced with
 // the same arithmetic whatever its position, so results do not change.
@@ -25,29 +27,6 @@ constexpr int RS_TB = 256;
 constexpr int RS_SCAN_TB = 1024;
 constexpr int RS_MAX_TILES = 64;   // 2^16 bins at most
 constexpr int RS_U = 4;            // runs of 32 work-list entries a warp handles per step
-
-__device__ __forceinline__ unsigned spread3(unsigned x) {   // bit i of x -> bit 3i (x < 8)
-  return (x & 1u) | ((x & 2u) << 2) | ((x & 4u) << 4);
-}
-
-__device__ __forceinline__ unsigned cell_of(float v, float scale, int n) {
-  const float c = fminf(fmaxf(v * scale, 0.0f), (float)(n - 1));   // NaN -> 0
-  return (unsigned)(int)c;
-}
-
-__device__ __forceinline__ unsigned ray_key(const float4& o, const float4& d, const float4& lo, const float4& hi,
-                                            int ob, int db) {
-  const int no = 1 << ob, nd = 1 << db;
-  const float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = hi.z - lo.z;
-  const unsigned ox = cell_of(o.x - lo.x, ex > 0.0f ? (float)no / ex : 0.0f, no);
-  const unsigned oy = cell_of(o.y - lo.y, ey > 0.0f ? (float)no / ey : 0.0f, no);
-  const unsigned oz = cell_of(o.z - lo.z, ez > 0.0f ? (float)no / ez : 0.0f, no);
-  const float hd = 0.5f * (float)nd;
-  const unsigned dx = cell_of(d.x + 1.0f, hd, nd), dy = cell_of(d.y + 1.0f, hd, nd), dz = cell_of(d.z + 1.0f, hd, nd);
-  const unsigned mo = spread3(ox) | (spread3(oy) << 1) | (spread3(oz) << 2);
-  const unsigned md = spread3(dx) | (spread3(dy) << 1) | (spread3(dz) << 2);
-  return (mo << (3 * db)) | md;
-}
 
 // the scene box and job of the ray in slot p: one scene per pass, or the job's scene in
 // a batch
@@ -152,9 +131,12 @@ __global__ void __launch_bounds__(RS_SCAN_TB) k_rs_scan(const RoundCounters* rc,
   const int n = rc->n_closest + rc->n_any;
   const int use = (threshold > 0 && n >= threshold) ? 1 : 0;
   if (blockIdx.x == 0 && threadIdx.x == 0) ctl->use = use;
-  if (!use) return;   // uniform over the grid
   const int bin = blockIdx.x * RS_SCAN_TB + threadIdx.x;
   const unsigned c = bin < nbins ? hist[bin] : 0u;
+  if (!use) {   // uniform over the grid; the keys' producers filled the histogram all the same
+    if (c) hist[bin] = 0;
+    return;
+  }
   unsigned total;
   const unsigned ex = block_exclusive(c, s_warp, &total);
   if (bin < nbins) {
@@ -166,7 +148,8 @@ __global__ void __launch_bounds__(RS_SCAN_TB) k_rs_scan(const RoundCounters* rc,
 
 __global__ void __launch_bounds__(RS_TB) k_rs_scatter(const int* __restrict__ q_closest,
                                                       const int* __restrict__ q_any, const RoundCounters* rc,
-                                                      const unsigned* __restrict__ keys, unsigned* cursor,
+                                                      const unsigned* __restrict__ keys,
+                                                      const unsigned* __restrict__ keys_any, unsigned* cursor,
                                                       const unsigned* __restrict__ blk_sum, int nblk, int* sorted,
                                                       const RaySortCtl* ctl) {
   __shared__ unsigned s_base[RS_MAX_TILES];
@@ -198,7 +181,7 @@ __global__ void __launch_bounds__(RS_TB) k_rs_scatter(const int* __restrict__ q_
     for (int u = 0; u < RS_U; ++u) {
       const int e = wbase + u * 32 + lane;
       const bool active = e < n;
-      key[u] = active ? keys[e] : 0xffffffffu - lane;
+      key[u] = active ? (keys_any && e >= nc ? keys_any[e - nc] : keys[e]) : 0xffffffffu - lane;
       val[u] = active ? (e < nc ? q_closest[e] : q_any[e - nc]) : 0;
     }
 #pragma unroll
@@ -224,13 +207,15 @@ int raysort_bins(int ob, int db, int jb) { return 1 << (3 * (ob + db) + jb + 1);
 template <class Box>
 static int launch_rs(const Box& box, const int* q_closest, const int* q_any, const RoundCounters* rc,
                      SF<float4> ro, SF<float4> rd, const RaySortBufs& b, int grid, cudaStream_t s) {
-  k_rs_key<Box><<<grid, RS_TB, 0, s>>>(box, q_closest, q_any, rc, ro, rd, b.keys, b.hist, b.threshold, b.ob, b.db,
-                                        b.jb);
+  if (!b.keys_any)   // else the keys and the histogram were written as the rays were queued
+    k_rs_key<Box><<<grid, RS_TB, 0, s>>>(box, q_closest, q_any, rc, ro, rd, b.keys, b.hist, b.threshold, b.ob, b.db,
+                                          b.jb);
   const int nbins = raysort_bins(b.ob, b.db, b.jb);
   const int nblk = (nbins + RS_SCAN_TB - 1) / RS_SCAN_TB;
   if (nblk > RS_MAX_TILES) return -1;
   k_rs_scan<<<nblk, RS_SCAN_TB, 0, s>>>(rc, b.hist, b.cursor, b.blk_sum, b.ctl, b.threshold, nbins);
-  k_rs_scatter<<<grid, RS_TB, 0, s>>>(q_closest, q_any, rc, b.keys, b.cursor, b.blk_sum, nblk, b.sorted, b.ctl);
+  k_rs_scatter<<<grid, RS_TB, 0, s>>>(q_closest, q_any, rc, b.keys, b.keys_any, b.cursor, b.blk_sum, nblk, b.sorted,
+                                      b.ctl);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

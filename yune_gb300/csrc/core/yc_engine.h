@@ -42,13 +42,23 @@ void launch_batch_sort(const BatchJob* jobs, SF<int4> job_pass, const PathState&
                        const int* in_any, const RoundCounters* rc_in, int* keys, int* sorted, SortCtl* sctl,
                        int threshold, int grid, cudaStream_t s);
 
+// The ray-sort keys of the rays a kernel queues (RaySortBufs: keys of the closest-hit
+// queue, keys of the any-hit queue, the histogram), formed where the rays are written;
+// keys_c == nullptr: the rounds are not sorted
+struct RsProduce {
+  unsigned* keys_c;
+  unsigned* keys_a;
+  unsigned* hist;
+  int ob, db, jb;
+};
 void launch_batch_fill(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, SF<int4> job_pass,
-                       int* free_stack, int* q_closest, RoundCounters* rc, DevStats* st, int grid, cudaStream_t s);
+                       int* free_stack, int* q_closest, RoundCounters* rc, DevStats* st, const RsProduce& rsp, int grid,
+                       cudaStream_t s);
 void launch_batch_logic(const BatchJob* jobs, BatchTasks* tasks, BatchCtl* ctl, const PathState& ps, SF<int4> job_pass,
                         int* free_stack, const int* in_closest, const int* in_any, const RoundCounters* rc_in,
                         int* out_closest, int* out_any, RoundCounters* rc_out, DevStats* st,
-                        unsigned long long* job_done, const int* sorted, const SortCtl* sctl, int grid,
-                        cudaStream_t s);
+                        unsigned long long* job_done, const int* sorted, const SortCtl* sctl, const RsProduce& rsp,
+                        int grid, cudaStream_t s);
 // tb: threads per block of the trace kernels (32..256, a multiple of 32)
 // The walk stack holds stack_cap entries: n_smem (<= stack_cap) in shared memory, the rest
 // in `spill`, one column per thread of the launch (grid_blocks * tb columns of

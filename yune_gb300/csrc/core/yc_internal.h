@@ -90,8 +90,37 @@ struct RaySortCtl {
   int use;
   int pad[3];
 };
+#ifdef __CUDACC__
+// ---- ray-sort key (raysort.cu, and the batch engine's producers) ----
+__device__ __forceinline__ unsigned rs_spread3(unsigned x) {   // bit i of x -> bit 3i (x < 8)
+  return (x & 1u) | ((x & 2u) << 2) | ((x & 4u) << 4);
+}
+__device__ __forceinline__ unsigned rs_cell_of(float v, float scale, int n) {
+  const float c = fminf(fmaxf(v * scale, 0.0f), (float)(n - 1));   // NaN -> 0
+  return (unsigned)(int)c;
+}
+// Morton code of the origin's cell in the scene box (ob bits per axis), then of the
+// direction's cell in [-1, 1]^3 (db bits per axis)
+__device__ __forceinline__ unsigned ray_key(const float4& o, const float4& d, const float4& lo, const float4& hi,
+                                            int ob, int db) {
+  const int no = 1 << ob, nd = 1 << db;
+  const float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = hi.z - lo.z;
+  const unsigned ox = rs_cell_of(o.x - lo.x, ex > 0.0f ? (float)no / ex : 0.0f, no);
+  const unsigned oy = rs_cell_of(o.y - lo.y, ey > 0.0f ? (float)no / ey : 0.0f, no);
+  const unsigned oz = rs_cell_of(o.z - lo.z, ez > 0.0f ? (float)no / ez : 0.0f, no);
+  const float hd = 0.5f * (float)nd;
+  const unsigned dx = rs_cell_of(d.x + 1.0f, hd, nd), dy = rs_cell_of(d.y + 1.0f, hd, nd),
+                 dz = rs_cell_of(d.z + 1.0f, hd, nd);
+  const unsigned mo = rs_spread3(ox) | (rs_spread3(oy) << 1) | (rs_spread3(oz) << 2);
+  const unsigned md = rs_spread3(dx) | (rs_spread3(dy) << 1) | (rs_spread3(dz) << 2);
+  return (mo << (3 * db)) | md;
+}
+#endif
+
 struct RaySortBufs {
-  unsigned* keys;      // one per work-list entry
+  unsigned* keys;      // one per work-list entry (with keys_any: one per closest-hit queue entry)
+  unsigned* keys_any;  // null, or the any-hit queue's keys (the batch engine's logic and fill
+                       // kernels write both arrays and the histogram as they queue rays)
   unsigned* hist;      // raysort_bins(ob, db) counters, zero between rounds
   unsigned* cursor;    // scatter cursors (exclusive prefix of hist within its tile of 1024 bins)
   unsigned* blk_sum;   // tile totals (64 at most)
