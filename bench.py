@@ -368,10 +368,10 @@ def replay_sample(jobs, seeds, every=128):
 # DRAM bytes (read + write) per walked ray of k_batch_trace_mixed on the mixed workload
 # with the default tree (mode 1): one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum, one pass) of all 320 launches of two passes of the 64 jobs,
-# 87,115,783,168 + 12,610,023,424 bytes over 452,296,636 walked rays; the command and the
+# 85,848,500,224 + 11,191,529,216 bytes over 452,296,636 walked rays; the command and the
 # per-launch spread are in profiles/k_batch_trace_mixed_c2_dram_traffic.md. A launch's
 # traffic is this figure times the rays it walks.
-MIX_TRACE_DRAM_BYTES_PER_RAY = (87115783168 + 12610023424) / 452296636
+MIX_TRACE_DRAM_BYTES_PER_RAY = (85848500224 + 11191529216) / 452296636
 
 
 def _trace_roofline(st, kt, l2, pk, pk_kind, kernel_mixed, kernel_extend, replay=None, dram_per_ray=None):
@@ -555,9 +555,9 @@ def run_ours(args, rank, local, ws, dist):
     if rank != 0:
         r.close()
         return
-    launches = int(kt_en["raygen_launches"] + kt_en["extend_launches"] + kt_en["occlusion_launches"]
+    launches = int(2 * kt_en["raygen_launches"] + kt_en["extend_launches"] + kt_en["occlusion_launches"]
                    + kt_en["trace_launches"] + kt_en["logic_launches"] + 3 * kt_en["sort_launches"]
-                   + 3 * kt_en["raysort_launches"])
+                   + 2 * kt_en["raysort_launches"])   # engine: fill = plan + fill, ray sort = scan + scatter
     line = {
         "metric": METRIC, "value": rays / t_s / 1e6, "unit": METRIC, "n_gpus": ws, "steps": K,
         "warmup": Wm, "ms_per_step": en_ms / K, "higher_is_better": True, "scaling": "weak",
@@ -959,9 +959,11 @@ def run_mix(args, rank, local, ws, dist):
     if rank != 0:
         r.close()
         return
-    launches = int(kt_b["raygen_launches"] + kt_b["extend_launches"] + kt_b["occlusion_launches"]
+    # the profiled run's launches per pass, times K: the engine's fill is two kernels (plan,
+    # fill), its ray sort two (scan, scatter: the keys come from the logic and fill kernels)
+    launches = int(2 * kt_b["raygen_launches"] + kt_b["extend_launches"] + kt_b["occlusion_launches"]
                    + kt_b["trace_launches"] + kt_b["logic_launches"] + 3 * kt_b["sort_launches"]
-                   + 3 * kt_b["raysort_launches"]) * K // 2   # the profiled run's launches per pass, times K
+                   + 2 * kt_b["raysort_launches"]) * K // 2
     acc_bytes = 16 * px
     line = {
         "metric": METRIC, "value": rays / t_s / 1e6, "unit": METRIC, "n_gpus": ws, "steps": K, "warmup": Wm,
