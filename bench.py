@@ -1045,7 +1045,7 @@ def run_reference_mix(args, rank, ws, dist):
 def run_c3(args):
     """Served requests (continuous batching) against the plain first-come loop, for each
     arrival rate of --rates (or --rate), over the same resident scenes."""
-    from yune_gb300 import serve, workloads
+    from yune_gb300 import autotune, scenes, serve, workloads
     from yune_gb300.core import Renderer
     t0 = time.perf_counter()
     resident = workloads.c3_scenes(8, max_tris=args.max_tris)
@@ -1056,7 +1056,18 @@ def run_c3(args):
     r.set_mixed_trace(args.mixed)
     r.set_ray_sort(args.ray_sort // 10, args.ray_sort % 10, args.ray_sort_min)
     r.set_shade_sort(args.shade_sort_min)
-    srv = serve.Server(r, resident, hbm_budget=args.hbm_budget_mb << 20, pool_paths=args.pool or (1 << 21))
+    sids = [r.upload(s) for s in resident]
+    cap = max(r.scene_depth(sid) for sid in sids) + 2
+    if args.pool:
+        shape, tune_s = autotune.BatchShape(pool_paths=args.pool), 0.0
+    else:   # the server's launch shape from the tuner: every resident scene at 1024x1024
+        t0 = time.perf_counter()
+        sizes = [(1024, 1024)] * len(resident)
+        n = autotune.calibration_passes(sum(w * h for w, h in sizes))
+        cal = [(sid, s.cam, scenes.pass_seeds(4242 + i, n), s.cfg) for i, (s, sid) in enumerate(zip(resident, sids))]
+        shape, _ = autotune.tune(r, cal, sizes, stack_cap=cap)
+        tune_s = time.perf_counter() - t0
+    srv = serve.Server(r, resident, hbm_budget=args.hbm_budget_mb << 20, shape=shape, sids=sids)
     runs = []
     for rate in rates:
         reqs = workloads.c3_requests(args.requests, rate, len(resident), res_range=(256, args.res_max),
@@ -1085,7 +1096,7 @@ def run_c3(args):
     out = {"metric": "p50/p99 time to target spp (s) and aggregate Mrays/s", "unit": "s",
            "config": {"workload": "c3 serving", "resolution": [256, args.res_max], "spp": [16, args.spp_max],
                       "scene_triangles": [int(s.n_tri) for s in resident], "hbm_budget_mb": args.hbm_budget_mb,
-                      "pool_paths": args.pool or (1 << 21), "host_build_s": build_s},
+                      "engine_shape": shape.kwargs(), "autotune_s": tune_s, "host_build_s": build_s},
            "runs": runs}
     r.close()
     print(json.dumps(out))

@@ -64,11 +64,15 @@ STATUS = {N.REQ_DONE: "done", N.REQ_CANCELLED: "cancelled",
 
 class Server:
     def __init__(self, renderer, resident, hbm_budget, pool_paths=1 << 21, rounds_per_launch=8, keep_results=False,
-                 cfg=None, logic_blocks_per_sm=2, sort_threshold=1 << 16, max_queue=None, scene_budget=None):
+                 cfg=None, logic_blocks_per_sm=2, sort_threshold=1 << 16, max_queue=None, scene_budget=None,
+                 shape=None, sids=None):
         """scene_budget: device bytes the resident scenes may take together (None: no
         limit); checked on the host before anything is uploaded, as CLManager checks each
         buffer against the device's global memory before creating it
-        (src/CLManager.cpp:428-429, 452-453)."""
+        (src/CLManager.cpp:428-429, 452-453). shape: an autotune.BatchShape for the
+        server's batch (its fields replace pool_paths, rounds_per_launch,
+        logic_blocks_per_sm and sort_threshold). sids: the resident scenes' ids when
+        they are uploaded already (else they are uploaded here)."""
         self.r = renderer
         self.scenes = resident
         self.scene_bytes = None
@@ -78,12 +82,16 @@ class Server:
             if self.scene_bytes > scene_budget:
                 raise ValueError("resident scenes need %d device bytes, above the scene budget of %d"
                                  % (self.scene_bytes, scene_budget))
-        self.sids = [renderer.upload(s) for s in resident]
+        self.sids = list(sids) if sids is not None else [renderer.upload(s) for s in resident]
         self.budget = int(hbm_budget)
         self.keep = keep_results
         self.cfg = cfg or scenes.default_cfg(max_depth=16)
         cap = max(renderer.scene_depth(sid) for sid in self.sids) + 2
-        bc = N.BatchCfg(pool_paths, rounds_per_launch, logic_blocks_per_sm, 1, 1 << 16, cap, sort_threshold, 0, 0)
+        if shape is not None:
+            bc = N.BatchCfg(shape.pool_paths, shape.rounds_per_launch, shape.logic_blocks_per_sm, 1, 1 << 16, cap,
+                            shape.sort_threshold, shape.groups, shape.ray_sort, shape.trace_block, shape.stack_smem)
+        else:
+            bc = N.BatchCfg(pool_paths, rounds_per_launch, logic_blocks_per_sm, 1, 1 << 16, cap, sort_threshold, 0, 0)
         sc = N.ServeCfg(self.budget, -1 if max_queue is None else int(max_queue), int(bool(keep_results)), bc)
         h = C.c_void_p()
         self.L = renderer.L
