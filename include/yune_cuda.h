@@ -456,7 +456,14 @@ enum {
    * yc_render_pass_noalloc; 0 (default) = as many as the scene's hierarchy needs (its
    * depth + 2). A smaller bound shrinks the kernels' shared memory; a walk that reaches it
    * fails the call with YC_E_OVERFLOW. Otherwise >= 3. */
-  YC_OPT_STACK_LIMIT = 8
+  YC_OPT_STACK_LIMIT = 8,
+  /* Walk-stack entries kept in shared memory by yc_render_pass(es)'s traversal (one launch
+   * per round, YC_OPT_MIXED_TRACE); the deeper entries go to a spill area of the context in
+   * global memory. Fewer entries leave more of each SM's L1 to the node and triangle
+   * fetches and more blocks per SM. 0 (default) = the whole stack in shared memory.
+   * yc_render_pass_noalloc keeps the whole stack there (it allocates nothing). The batch
+   * engine has its own setting (yc_batch_cfg.stack_smem). */
+  YC_OPT_STACK_SMEM = 9
 };
 int yc_set_option(yc_ctx* ctx, int option, int value);
 

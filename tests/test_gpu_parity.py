@@ -578,3 +578,33 @@ def test_render_edge_cases(renderer, case):
         rays += O.render(s, ref, sd, 1 if k == 0 else 0, s.cfg)["rays"]
     assert np.array_equal(gpu.view(np.int32), ref.view(np.int32))
     assert st["rays"] == rays and st["samples"] == w * h * 2
+
+
+@pytest.mark.parametrize("tree", [1, 2])
+def test_render_identical_with_a_split_walk_stack(renderer, tree):
+    """YC_OPT_STACK_SMEM: with only 2 or 12 walk-stack entries in shared memory (the rest in
+    the context's spill area) a pass gives the oracle's bits and the same ray counts as
+    with the whole stack in shared memory."""
+    s = scenes.c1(40, 32, level=5)
+    seeds = scenes.pass_seeds(37, 2)
+    renderer.set_tree_mode(tree)
+    sid = renderer.upload(s)
+    renderer.set_tree_mode(1)
+    renderer.set_camera(s.cam)
+    out = []
+    for smem in (0, 2, 12):
+        renderer.set_stack_smem(smem)
+        aid = renderer.alloc_accum(40, 32)
+        renderer.reset_stats()
+        renderer.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
+        out.append((renderer.read_accum(aid), renderer.stats()))
+        renderer.free_accum(aid)
+    renderer.set_stack_smem(0)
+    renderer.release(sid)
+    ref = np.zeros((32, 40, 4), np.float32)
+    for k, sd in enumerate(seeds):
+        O.render(s, ref, sd, 1 if k == 0 else 0, s.cfg)
+    for img, st in out:
+        assert st["stack_overflow"] == 0
+        assert st["rays"] == out[0][1]["rays"]
+        assert np.array_equal(img.view(np.int32), ref.view(np.int32))

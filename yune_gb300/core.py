@@ -197,6 +197,11 @@ class Renderer:
         reaches the limit fails the call with YC_E_OVERFLOW."""
         N.check(self.L.yc_set_option(self.h, 8, int(n)), "yc_set_option")
 
+    def set_stack_smem(self, n):
+        """Walk-stack entries the per-pass traversal keeps in shared memory (YC_OPT_STACK_SMEM;
+        the deeper ones go to a spill area in global memory; 0 = the whole stack)."""
+        N.check(self.L.yc_set_option(self.h, 9, int(n)), "yc_set_option")
+
     def set_tail_paths(self, n):
         """Paths left at which a pass finishes in the tail kernel (-1 auto, 0 off)."""
         N.check(self.L.yc_set_option(self.h, 2, int(n)), "yc_set_option")

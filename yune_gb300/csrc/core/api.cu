@@ -143,6 +143,8 @@ struct yc_ctx {
   unsigned long long* overflow_host = nullptr;   // pinned: DevStats::call_overflow read back
   int max_rounds = 1000000;   // YC_OPT_MAX_ROUNDS: rounds one pass may take
   int stack_limit = 0;        // YC_OPT_STACK_LIMIT: traversal stack entries allowed (0 = any)
+  int stack_smem = 0;         // YC_OPT_STACK_SMEM: per-pass walk-stack entries in shared memory (0 = all)
+  DevBuf<int> pass_spill;     // the deeper entries of the per-pass walks (with stack_smem)
   int logic_grid = 0;
   int sm_count = 0;
   float last_ms = 0.0f;
@@ -177,6 +179,12 @@ int ensure_paths(yc_ctx* c, size_t n) {
 constexpr int kRaySortMinTris = 4096;
 // frames with fewer pixels are shaded in queue order by yc_render_pass
 constexpr size_t kShadeSortMinPixels = 1u << 19;
+
+// the per-pass walks' stack spill area: n ints
+int ensure_pass_spill(yc_ctx* c, size_t n) {
+  if (n > c->pass_spill.n) YC_CUDA(c->pass_spill.alloc(n));
+  return 0;
+}
 
 // key, histogram and sorted-list buffers of the per-pass ray sort, for n rays
 int ensure_raysort(yc_ctx* c, size_t n) {
@@ -398,7 +406,12 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
     if (int e = ensure_shadesort(c, (size_t)W * H)) return e;
   const int grid_c = yc::trace_grid_blocks(false, dsc.depth, dsc.wide != 0);
   const int grid_a = yc::trace_grid_blocks(true, dsc.depth, dsc.wide != 0);
-  const int grid_m = mixed ? yc::trace_mixed_grid_blocks(dsc.depth, dsc.wide != 0) : 1;
+  // the mixed trace's walk stacks: c->stack_smem entries in shared memory, the rest spilled
+  const int cap = yc::trace_stack_cap(dsc.depth);
+  const int n_smem = (mixed && c->stack_smem > 0 && c->stack_smem < cap) ? c->stack_smem : 0;
+  const int grid_m = mixed ? yc::trace_mixed_grid_blocks(dsc.depth, dsc.wide != 0, n_smem) : 1;
+  if (n_smem > 0 && grid_m > 0)
+    if (int e = ensure_pass_spill(c, (size_t)grid_m * yc::TRACE_TB_PASS * 2 * (size_t)(cap - n_smem))) return e;
   if (grid_c <= 0 || grid_a <= 0 || grid_m <= 0)
     return fail(YC_E_LAUNCH, "trace kernel cannot be resident (stack too deep)");
   int tail_grid = 0, tail_at = 0;
@@ -425,7 +438,8 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
       }
       KTimer kt(c, K_TRACE);
       if (yc::launch_trace_mixed(dsc, in_c, in_a, rin, ps.ro, ps.rd, ps.hit, c->stats.p, grid_m, c->stream,
-                                 raysort ? rsb.sorted : nullptr, raysort ? rsb.ctl : nullptr))
+                                 raysort ? rsb.sorted : nullptr, raysort ? rsb.ctl : nullptr, n_smem,
+                                 n_smem > 0 ? c->pass_spill.p : nullptr))
         return fail(YC_E_LAUNCH, std::string("trace kernel: ") + cudaGetErrorString(cudaGetLastError()));
     }
     // otherwise the two traces of a round are independent: the any-hit one runs on the
@@ -1086,6 +1100,10 @@ int yc_set_option(yc_ctx* c, int option, int value) {
     case YC_OPT_STACK_LIMIT:
       if (value != 0 && value < 3) return fail(YC_E_INVALID, "stack limit is 0 (none) or >= 3 entries");
       c->stack_limit = value;
+      return YC_OK;
+    case YC_OPT_STACK_SMEM:
+      if (value < 0) return fail(YC_E_INVALID, "stack_smem must not be negative");
+      c->stack_smem = value;
       return YC_OK;
     default:
       return fail(YC_E_INVALID, "unknown option");

@@ -82,10 +82,10 @@ __global__ void __launch_bounds__(TRACE_TB) k_trace_paths_mixed(DevScene sc, con
                                                                 SF<float4> ro,
                                                                 SF<float4> rd, SF<float4> hit,
                                                                 int stack_cap, DevStats* st, const int* sorted,
-                                                                const RaySortCtl* rs) {
+                                                                const RaySortCtl* rs, int n_smem, int* spill) {
   const int nc = rc->n_closest;
   PathMixedSrc src{&sc, q_closest, q_any, (rs && rs->use) ? sorted : nullptr, nc, ro, rd, hit};
-  trace_loop_mixed<WIDE>(src, nc, nc + rc->n_any, &rc->work_closest, stack_cap, st);
+  trace_loop_mixed<WIDE>(src, nc, nc + rc->n_any, &rc->work_closest, stack_cap, st, n_smem, spill);
 }
 
 // traceRay (udpt.cl:240-286) on explicit rays of 9 floats: light loop, then the BVH.
@@ -170,22 +170,27 @@ int launch_trace(const DevScene& sc, bool any_hit, const int* queue, const int* 
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-int trace_mixed_grid_blocks(int depth, bool wide) {
-  const size_t smem = smem_for(stack_cap_for(depth));
+static_assert(TRACE_TB == TRACE_TB_PASS, "the host sizes the per-pass spill area by TRACE_TB_PASS");
+int trace_stack_cap(int depth) { return stack_cap_for(depth); }
+
+int trace_mixed_grid_blocks(int depth, bool wide, int n_smem) {
+  const int cap = stack_cap_for(depth);
+  const size_t smem = smem_for(n_smem > 0 && n_smem < cap ? n_smem : cap);
   return wide ? resident_grid(k_trace_paths_mixed<true>, smem) : resident_grid(k_trace_paths_mixed<false>, smem);
 }
 
 int launch_trace_mixed(const DevScene& sc, const int* q_closest, const int* q_any, RoundCounters* rc,
                        SF<float4> ro, SF<float4> rd, SF<float4> hit, DevStats* st, int grid_blocks,
-                       cudaStream_t s, const int* sorted, const RaySortCtl* rs) {
+                       cudaStream_t s, const int* sorted, const RaySortCtl* rs, int n_smem, int* spill) {
   const int cap = stack_cap_for(sc.depth);
-  const size_t smem = smem_for(cap);
+  if (!(n_smem > 0 && n_smem < cap && spill)) n_smem = cap;
+  const size_t smem = smem_for(n_smem);
   if (sc.wide)
     k_trace_paths_mixed<true><<<grid_blocks, TRACE_TB, smem, s>>>(sc, q_closest, q_any, rc, ro, rd, hit, cap, st,
-                                                                  sorted, rs);
+                                                                  sorted, rs, n_smem, spill);
   else
     k_trace_paths_mixed<false><<<grid_blocks, TRACE_TB, smem, s>>>(sc, q_closest, q_any, rc, ro, rd, hit, cap, st,
-                                                                   sorted, rs);
+                                                                   sorted, rs, n_smem, spill);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

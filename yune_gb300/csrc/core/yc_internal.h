@@ -203,16 +203,21 @@ int launch_trace_rays(const DevScene& sc, bool any_hit, const float* rays9, int 
                       int* work, DevStats* st, cudaStream_t s);
 int trace_grid_blocks(bool any_hit, int depth, bool wide);
 // one launch over both queues of a round (closest-hit entries, then any-hit); the work
-// cursor is rc->work_closest
+// cursor is rc->work_closest. n_smem (< the stack depth, with spill): walk-stack entries in
+// shared memory, the deeper ones in `spill` (grid_blocks * TRACE_TB columns of
+// 2 * (depth - n_smem) ints); otherwise the whole stack is in shared memory.
 int launch_trace_mixed(const DevScene& sc, const int* q_closest, const int* q_any, RoundCounters* rc,
                        SF<float4> ro, SF<float4> rd, SF<float4> hit, DevStats* st, int grid_blocks,
-                       cudaStream_t s, const int* sorted = nullptr, const RaySortCtl* rs = nullptr);
+                       cudaStream_t s, const int* sorted = nullptr, const RaySortCtl* rs = nullptr, int n_smem = 0,
+                       int* spill = nullptr);
 // raysort.cu: sorts the round's work list (closest-hit queue, then any-hit queue) into
 // b.sorted when the round has at least b.threshold rays, and sets b.ctl->use
 int raysort_bins(int ob, int db, int jb = 0);
 int launch_raysort(const DevScene& sc, const int* q_closest, const int* q_any, const RoundCounters* rc,
                    SF<float4> ro, SF<float4> rd, const RaySortBufs& b, int grid, cudaStream_t s);
-int trace_mixed_grid_blocks(int depth, bool wide);
+int trace_mixed_grid_blocks(int depth, bool wide, int n_smem = 0);
+int trace_stack_cap(int depth);   // walk-stack entries the per-pass kernels give a scene of this depth
+constexpr int TRACE_TB_PASS = 128;   // block of the per-pass trace kernels (TRACE_TB of yc_trace_loop.cuh)
 int l2_read_gbs(size_t bytes, int iters, cudaStream_t s, double* gbs);
 // bvh_build.cu: BVH::createBVH on the device (the node array of the host builder)
 // too_deep: the tree would pass 1024 levels (more than leaf_max triangles with one centroid)
