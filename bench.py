@@ -667,6 +667,23 @@ def run_perpass_bdpt(args, rank, local, ws, dist):
     r.synchronize()
     upload_s = time.perf_counter() - t0
     scene_bytes = r.scene_bytes(sid)
+    # the upload's repack on the host (YC_OPT_REPACK 0) against the device (the default),
+    # each uploading a second copy of the scene: time and equal bytes
+    repack = {}
+    if args.tree == 1:
+        digest = r.scene_digest(sid)
+        for mode, key in ((0, "host_s"), (1, "device_s")):
+            r.set_repack(mode)
+            t0 = time.perf_counter()
+            sid2 = r.upload(scene)
+            r.synchronize()
+            repack[key] = time.perf_counter() - t0
+            repack["equal" if mode == 0 else "repeatable"] = r.scene_digest(sid2) == digest
+            r.release(sid2)
+        r.set_repack(1)
+        repack["what"] = ("yc_upload_scene of the scene (checks, repack, copies) with the repack on the host "
+                          "threads and on the device; equal: the host repack's arrays have the device repack's "
+                          "digest; repeatable: a second device repack too")
     # the reference BVH of this scene built on the host (yh_bvh_build) and on the GPU
     # (yc_bvh_build), compared node for node
     leaf = 4 if args.config in ("c4", "c4_mis") else 10
@@ -732,7 +749,7 @@ def run_perpass_bdpt(args, rank, local, ws, dist):
         "data": "synthetic (seeded procedural scene)",
         "config": {"workload": workload_string(args.config, scene),
                    "spp_total": scene.spp, "tree_mode": args.tree, "scene_device_bytes": scene_bytes,
-                   "host_build_s": build_s, "upload_s": upload_s,
+                   "host_build_s": build_s, "upload_s": upload_s, "repack": repack,
                    "bvh_build": {"host_s": host_bvh_s, "gpu_s": gpu_bvh_s, "equal": bvh_equal,
                                  "what": "BVH::createBVH node array, 20 bins, leaf <= %d: yh_bvh_build on the host "
                                          "core against yc_bvh_build on the GPU (host copy of the nodes included)"

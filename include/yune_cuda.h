@@ -148,6 +148,11 @@ int yc_release_scene(yc_ctx* ctx, int scene_id);
 int yc_scene_bytes(yc_ctx* ctx, int scene_id, uint64_t* bytes);
 /* interior levels of the uploaded hierarchy (a traversal stack needs depth + 2 slots) */
 int yc_scene_depth(yc_ctx* ctx, int scene_id, int* depth);
+/* FNV-1a digest of the uploaded scene's repacked arrays as they lie on the device (node,
+ * triangle-stream and shading records, root box, root link), the digest yc_scene_layout
+ * computes on the host for the same inputs. Synchronous. No reference counterpart (an
+ * integrity check of the upload). */
+int yc_scene_digest(yc_ctx* ctx, int scene_id, uint64_t* digest);
 
 /* The device layout yc_upload_scene would build for these arrays, computed on the host
  * without a device or a context: the bytes the scene would hold (what yc_scene_bytes
@@ -463,7 +468,15 @@ enum {
    * fetches and more blocks per SM. 0 (default) = the whole stack in shared memory.
    * yc_render_pass_noalloc keeps the whole stack there (it allocates nothing). The batch
    * engine has its own setting (yc_batch_cfg.stack_smem). */
-  YC_OPT_STACK_SMEM = 9
+  YC_OPT_STACK_SMEM = 9,
+  /* Where yc_upload_scene repacks a scene for YC_OPT_TREE 1: 1 (default) on the device
+   * (the caller's triangle and node arrays are copied over and the SAH hierarchy above the
+   * reference leaves, the leaves' triangle stream and the shading records are built by
+   * kernels), 0 on the host. Both give the same bytes (yc_scene_digest equals
+   * yc_scene_layout's digest). The node checks and the list of reachable leaves stay on
+   * the host; tree modes 0 and 2, and scenes with fewer than two reachable leaves, are
+   * repacked on the host either way. */
+  YC_OPT_REPACK = 10
 };
 int yc_set_option(yc_ctx* ctx, int option, int value);
 

@@ -8,6 +8,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
+import leafgen
 from yune_gb300 import _native as N
 from yune_gb300 import scenes
 from yune_gb300.layouts import MATERIAL, QUAD_LIGHT, ptr
@@ -94,3 +95,26 @@ def test_layout_refuses_what_the_upload_refuses():
     bad["vert_list"][j, 0] = len(s.tris)                    # a triangle that does not exist
     assert call(s.tris, len(s.mats), bad) == -1
     assert L.yc_scene_layout(None, 0, 0, None, 0, 1, None) == -1
+
+
+@pytest.mark.parametrize("kind,n", [("coincident", 3000), ("grid", 140000), ("random", 140000)])
+def test_sah_over_leaves_independent_of_host_threads(kind, n):
+    """The SAH build over the reference leaves (tree mode 1) chooses the same splits whatever
+    the host threads: leaf boxes that all coincide (every split halves the list), boxes on an
+    integer grid with zeros of both signs (equal costs; -0 and +0 met in one min or max in
+    different orders by different chunkings) and random boxes; ranges above 64K leaves are
+    reduced in chunks on threads."""
+    s = leafgen.leaf_scene(n, kind, seed=3)
+    L = N.lib()
+    got = {}
+    try:
+        for th in (1, 3, 0):
+            assert L.yh_set_host_threads(th) == 0
+            lay = scenes.layout(s, 1)
+            got[th] = (lay["digest"], lay["depth"], lay["node_bytes"])
+    finally:
+        L.yh_set_host_threads(0)
+    assert len(set(got.values())) == 1, got
+    assert got[0][2] == 64 * (n - 1)
+    if kind == "coincident":   # halving: a balanced tree
+        assert got[0][1] == int(np.ceil(np.log2(n))) + 1

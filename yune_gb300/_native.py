@@ -112,6 +112,7 @@ SIGNATURES = {
     "yc_refit_scene": (i32, [vp, i32, vp, i32]),
     "yc_scene_bytes": (i32, [vp, i32, C.POINTER(C.c_uint64)]),
     "yc_scene_depth": (i32, [vp, i32, C.POINTER(i32)]),
+    "yc_scene_digest": (i32, [vp, i32, C.POINTER(C.c_uint64)]),
     "yc_scene_layout": (i32, [vp, i32, i32, vp, i32, i32, vp]),
     "yc_set_camera": (i32, [vp, vp]),
     "yc_walk_counts": (i32, [vp, i32, vp, i32, i32, vp, i32, i32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), vp,

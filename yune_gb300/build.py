@@ -24,12 +24,13 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fa
              "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 
 CU_SOURCES = ["core/api.cu", "core/trace.cu", "core/udpt.cu", "core/bench_kernels.cu", "core/noalloc.cu", "core/bdpt.cu",
-              "core/engine.cu", "core/tail.cu", "core/raysort.cu", "core/bvh_build.cu", "core/bdpt_mis.cu", "core/refit.cu"]
+              "core/engine.cu", "core/tail.cu", "core/raysort.cu", "core/bvh_build.cu", "core/bdpt_mis.cu", "core/refit.cu",
+              "core/repack_dev.cu"]
 CXX_SOURCES = ["core/repack.cpp", "core/serve.cpp", "core/walk_host.cpp", "core/tune.cpp", "host/yh_bvh.cpp", "host/yh_camera.cpp", "host/yh_scene.cpp", "host/yh_image.cpp",
                "host/yh_cache.cpp", "host/yh_threads.cpp"]
 HEADERS = ["ym_math.h", "core/yc_scene.h", "core/yc_internal.h", "core/yc_traverse.cuh", "core/yc_shade.cuh",
            "core/yc_repack.h", "core/yc_noalloc.h", "core/yc_bdpt.h", "core/yc_udpt.cuh",
-           "core/yc_trace_loop.cuh", "core/yc_engine.h", "host/yh_threads.h"]
+           "core/yc_trace_loop.cuh", "core/yc_engine.h", "core/yc_sah.h", "host/yh_threads.h"]
 
 
 def _deps():

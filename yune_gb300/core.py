@@ -78,6 +78,13 @@ class Renderer:
         N.check(self.L.yc_scene_depth(self.h, sid, C.byref(d)), "yc_scene_depth")
         return d.value
 
+    def scene_digest(self, sid):
+        """Digest of the uploaded scene's repacked arrays as they lie on the device (yc_scene_digest);
+        equals `scenes.layout(...).digest` for the same inputs and tree mode."""
+        h = C.c_uint64()
+        N.check(self.L.yc_scene_digest(self.h, sid, C.byref(h)), "yc_scene_digest")
+        return int(h.value)
+
     def build_bvh(self, tris, bins=20, leaf=10):
         """BVH::createBVH on this renderer's GPU (yc_bvh_build): the node array of
         scenes.build_bvh, and the tree depth."""
@@ -201,6 +208,11 @@ class Renderer:
         """Walk-stack entries the per-pass traversal keeps in shared memory (YC_OPT_STACK_SMEM;
         the deeper ones go to a spill area in global memory; 0 = the whole stack)."""
         N.check(self.L.yc_set_option(self.h, 9, int(n)), "yc_set_option")
+
+    def set_repack(self, on_device):
+        """Where later uploads repack a tree-mode-1 scene (YC_OPT_REPACK): 1 on the device
+        (default), 0 on the host; the bytes are the same."""
+        N.check(self.L.yc_set_option(self.h, 10, int(on_device)), "yc_set_option")
 
     def set_tail_paths(self, n):
         """Paths left at which a pass finishes in the tail kernel (-1 auto, 0 off)."""

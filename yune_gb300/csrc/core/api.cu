@@ -88,6 +88,7 @@ struct Scene {
   bool refit_ready = false;
   DevBuf<yc_triangle> refit_tris;
   DevBuf<float4> refit_root;
+  size_t n_node4 = 0, n_tri4 = 0, n_shade4 = 0;   // float4 records of the repacked arrays
 };
 
 struct Accum {
@@ -144,6 +145,7 @@ struct yc_ctx {
   int max_rounds = 1000000;   // YC_OPT_MAX_ROUNDS: rounds one pass may take
   int stack_limit = 0;        // YC_OPT_STACK_LIMIT: traversal stack entries allowed (0 = any)
   int stack_smem = 0;         // YC_OPT_STACK_SMEM: per-pass walk-stack entries in shared memory (0 = all)
+  int repack_device = 1;      // YC_OPT_REPACK: the upload's repack of tree mode 1 on the device
   DevBuf<int> pass_spill;     // the deeper entries of the per-pass walks (with stack_smem)
   int logic_grid = 0;
   int sm_count = 0;
@@ -179,6 +181,33 @@ int ensure_paths(yc_ctx* c, size_t n) {
 constexpr int kRaySortMinTris = 4096;
 // frames with fewer pixels are shaded in queue order by yc_render_pass
 constexpr size_t kShadeSortMinPixels = 1u << 19;
+
+// FNV-1a over the 64-bit words of the repacked node, stream and shading arrays, the root
+// box and the root link and test (yc_scene_layout, yc_scene_digest)
+uint64_t layout_digest(const float4* nodes, size_t n_nodes, const float4* tris, size_t n_tris, const float4* shade,
+                       size_t n_shade, float4 root_lo, float4 root_hi, int root_link, int root_test) {
+  uint64_t h = 0xcbf29ce484222325ull;
+  // the 64-bit words are copied out of the float4 bytes (memcpy), not read through a
+  // uint64_t pointer: an aliased read of a float4 object is undefined, and an optimising
+  // compiler may then drop the stores that fill the array (the root box below)
+  auto words = [&h](const float4* p, size_t n) {
+    const unsigned char* bytes = reinterpret_cast<const unsigned char*>(p);
+    h = (h ^ (uint64_t)n) * 0x100000001b3ull;
+    for (size_t i = 0; i < 2 * n; ++i) {
+      uint64_t w;
+      std::memcpy(&w, bytes + 8 * i, 8);
+      h = (h ^ w) * 0x100000001b3ull;
+    }
+  };
+  words(nodes, n_nodes);
+  words(tris, n_tris);
+  words(shade, n_shade);
+  const float4 root[2] = {root_lo, root_hi};
+  words(root, 2);
+  h = (h ^ (uint64_t)(uint32_t)root_link) * 0x100000001b3ull;
+  h = (h ^ (uint64_t)(uint32_t)root_test) * 0x100000001b3ull;
+  return h;
+}
 
 // the per-pass walks' stack spill area: n ints
 int ensure_pass_spill(yc_ctx* c, size_t n) {
@@ -592,19 +621,45 @@ int yc_upload_scene(yc_ctx* c, const yc_triangle* tris, int n_tri, const yc_mate
     if (tris[i].matID < 0 || tris[i].matID >= n_mat)
       return fail(YC_E_INVALID, "triangle " + std::to_string(i) + " has matID out of range");
   yc::Repacked rp;
+  yc::DevRepackPlan plan;
   std::string err;
-  if (yc::repack_scene(tris, n_tri, nodes, n_node, c->tree_mode, rp, err)) return fail(YC_E_INVALID, err);
+  // the repack: on the device for tree mode 1 (YC_OPT_REPACK), where a scene has two
+  // reachable leaves or more; otherwise (and for the trivial scenes) on the host
+  int on_device = 0;
+  if (c->repack_device && c->tree_mode == yc::TREE_SAH_OVER_LEAVES) {
+    on_device = yc::plan_device_repack(nodes, n_node, n_tri, plan, err);
+    if (on_device < 0) return fail(YC_E_INVALID, err);
+  }
+  if (!on_device && yc::repack_scene(tris, n_tri, nodes, n_node, c->tree_mode, rp, err)) return fail(YC_E_INVALID, err);
+  const size_t n_node4 = on_device ? 4 * (plan.leaf_node.size() - 1) : rp.nodes.size();
+  const size_t n_tri4 = on_device ? 3 * plan.slots : rp.tris.size();
+  const size_t n_shade4 = on_device ? 4 * (size_t)n_tri : rp.shade.size();
   std::unique_ptr<Scene> s(new (std::nothrow) Scene);
   if (s)
     for (int i = 0; i < n_mat; ++i) s->has_specular = s->has_specular || mats[i].is_specular != 0;
   if (!s) return fail(YC_E_NOMEM, "host allocation failed");
   YC_CUDA(cudaSetDevice(c->device));
-  YC_CUDA(s->nodes.alloc(std::max<size_t>(rp.nodes.size(), 4)));
-  YC_CUDA(s->tris.alloc(std::max<size_t>(rp.tris.size(), 3)));
-  YC_CUDA(s->shade.alloc(std::max<size_t>(rp.shade.size(), 4)));
+  YC_CUDA(s->nodes.alloc(std::max<size_t>(n_node4, 4)));
+  YC_CUDA(s->tris.alloc(std::max<size_t>(n_tri4, 3)));
+  YC_CUDA(s->shade.alloc(std::max<size_t>(n_shade4, 4)));
   YC_CUDA(s->mats.alloc(std::max(n_mat, 1)));
   YC_CUDA(s->on_ab.alloc(std::max(n_mat, 1)));
   YC_CUDA(s->lights.alloc(yc::MAX_LIGHTS));
+  s->n_node4 = n_node4;
+  s->n_tri4 = n_tri4;
+  s->n_shade4 = n_shade4;
+  if (on_device) {
+    int depth = 0;
+    const int r = yc::repack_device(tris, n_tri, nodes, n_node, plan, s->nodes.p, s->tris.p, s->shade.p, depth,
+                                    c->stream, err);
+    if (r) return fail(r == -2 ? YC_E_NOMEM : YC_E_LAUNCH, err);
+    rp.root_link = 0;   // the root is the first node (two leaves or more)
+    rp.root_test = 1;
+    rp.depth = depth;
+    rp.wide = 0;
+    rp.root_lo = plan.root_lo;
+    rp.root_hi = plan.root_hi;
+  }
   if (!rp.nodes.empty())
     YC_CUDA(cudaMemcpyAsync(s->nodes.p, rp.nodes.data(), rp.nodes.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
   if (!rp.tris.empty())
@@ -662,27 +717,8 @@ int yc_scene_layout(const yc_triangle* tris, int n_tri, int n_mat, const yc_bvh_
   out->device_bytes = out->node_bytes + out->stream_bytes + out->shade_bytes +
                       (uint64_t)std::max(n_mat, 1) * (sizeof(yc_material) + sizeof(float2)) +
                       yc::MAX_LIGHTS * sizeof(yc_quad_light);
-  uint64_t h = 0xcbf29ce484222325ull;
-  // the 64-bit words are copied out of the float4 bytes (memcpy), not read through a
-  // uint64_t pointer: an aliased read of a float4 object is undefined, and an optimising
-  // compiler may then drop the stores that fill the array (the root box below)
-  auto words = [&h](const float4* p, size_t n) {
-    const unsigned char* bytes = reinterpret_cast<const unsigned char*>(p);
-    h = (h ^ (uint64_t)n) * 0x100000001b3ull;
-    for (size_t i = 0; i < 2 * n; ++i) {
-      uint64_t w;
-      std::memcpy(&w, bytes + 8 * i, 8);
-      h = (h ^ w) * 0x100000001b3ull;
-    }
-  };
-  words(rp.nodes.data(), rp.nodes.size());
-  words(rp.tris.data(), rp.tris.size());
-  words(rp.shade.data(), rp.shade.size());
-  const float4 root[2] = {rp.root_lo, rp.root_hi};
-  words(root, 2);
-  h = (h ^ (uint64_t)(uint32_t)rp.root_link) * 0x100000001b3ull;
-  h = (h ^ (uint64_t)(uint32_t)rp.root_test) * 0x100000001b3ull;
-  out->digest = h;
+  out->digest = layout_digest(rp.nodes.data(), rp.nodes.size(), rp.tris.data(), rp.tris.size(), rp.shade.data(),
+                              rp.shade.size(), rp.root_lo, rp.root_hi, rp.root_link, rp.root_test);
   out->depth = rp.depth;
   out->wide = rp.wide;
   return YC_OK;
@@ -857,6 +893,22 @@ int yc_scene_depth(yc_ctx* c, int scene_id, int* depth) {
   Scene* s = find_scene(c, scene_id);
   if (!s) return fail(YC_E_NOTFOUND, "unknown scene");
   *depth = s->dev.depth;
+  return YC_OK;
+}
+
+int yc_scene_digest(yc_ctx* c, int scene_id, uint64_t* digest) {
+  if (!c || !digest) return fail(YC_E_INVALID, "ctx or digest is NULL");
+  Scene* s = find_scene(c, scene_id);
+  if (!s) return fail(YC_E_NOTFOUND, "unknown scene");
+  YC_CUDA(cudaSetDevice(c->device));
+  std::vector<float4> nodes(s->n_node4), tris(s->n_tri4), shade(s->n_shade4);
+  YC_CUDA(cudaStreamSynchronize(c->stream));
+  if (!nodes.empty()) YC_CUDA(cudaMemcpy(nodes.data(), s->nodes.p, nodes.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+  if (!tris.empty()) YC_CUDA(cudaMemcpy(tris.data(), s->tris.p, tris.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+  if (!shade.empty()) YC_CUDA(cudaMemcpy(shade.data(), s->shade.p, shade.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+  const yc::DevScene& d = s->dev;
+  *digest = layout_digest(nodes.data(), nodes.size(), tris.data(), tris.size(), shade.data(), shade.size(), d.root_lo,
+                          d.root_hi, d.root_link, d.root_test);
   return YC_OK;
 }
 
@@ -1104,6 +1156,10 @@ int yc_set_option(yc_ctx* c, int option, int value) {
     case YC_OPT_STACK_SMEM:
       if (value < 0) return fail(YC_E_INVALID, "stack_smem must not be negative");
       c->stack_smem = value;
+      return YC_OK;
+    case YC_OPT_REPACK:
+      if (value != 0 && value != 1) return fail(YC_E_INVALID, "repack is 0 (host) or 1 (device)");
+      c->repack_device = value;
       return YC_OK;
     default:
       return fail(YC_E_INVALID, "unknown option");

@@ -28,6 +28,7 @@
 
 #include "../ym_math.h"
 #include "yc_repack.h"
+#include "yc_sah.h"
 #include "host/yh_threads.h"
 
 namespace yc {
@@ -125,6 +126,9 @@ bool is_queued(const yc_bvh_node& n) { return n.vert_len > 0 || n.child_idx > 0;
 // box area times its triangles). A node's box is the union of the
 // leaf boxes below it, so it contains every box the reference tree places below it and
 // a ray that reaches a leaf in the reference passes every box on the way down here too.
+// The arithmetic (bins, areas, costs, min / max order) is yc_sah.h's, and a split keeps
+// the leaves' order on each side (a stable partition), so the device repack
+// (repack_dev.cu) builds the same hierarchy bit for bit.
 struct LeafItem {
   float lo[3], hi[3];
   float c[3];
@@ -160,12 +164,24 @@ struct SahBuilder {
 
   SahBuilder(std::vector<LeafItem>& it) : items(it), bins(it.size() > 1 ? it.size() - 1 : 0) {}
 
-  static float area(const float lo[3], const float hi[3]) {
-    const float d0 = hi[0] - lo[0], d1 = hi[1] - lo[1], d2 = hi[2] - lo[2];
-    return 2.0f * (d0 * d1 + d0 * d2 + d1 * d2);
+  static float area(const float lo[3], const float hi[3]) { return sah_area(lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]); }
+
+  // stable partition of items [b, e): the leaves with left(item) first, each side in its
+  // old order; returns the first of the right side (a scratch vector per thread holds them)
+  template <class P>
+  int stable_split(int b, int e, P left) {
+    thread_local std::vector<LeafItem> right;
+    right.clear();
+    int w = b;
+    for (int i = b; i < e; ++i) {
+      if (left(items[i])) items[w++] = items[i];
+      else right.push_back(items[i]);
+    }
+    std::copy(right.begin(), right.end(), items.begin() + w);
+    return w;
   }
 
-  static constexpr int NB = 256;   // SAH bins per axis, at most
+  static constexpr int NB = SAH_NB;
 
   // box and centroid box of items [b, e), and the per-axis bins of their centroids:
   // min, max and counts, which are exact in any order, so the chunks of a large range
@@ -184,17 +200,17 @@ struct SahBuilder {
     init_box(st.clo, st.chi);
     for (int i = b; i < e; ++i)
       for (int k = 0; k < 3; ++k) {
-        st.lo[k] = std::min(st.lo[k], items[i].lo[k]);
-        st.hi[k] = std::max(st.hi[k], items[i].hi[k]);
-        st.clo[k] = std::min(st.clo[k], items[i].c[k]);
-        st.chi[k] = std::max(st.chi[k], items[i].c[k]);
+        st.lo[k] = sah_min(st.lo[k], items[i].lo[k]);
+        st.hi[k] = sah_max(st.hi[k], items[i].hi[k]);
+        st.clo[k] = sah_min(st.clo[k], items[i].c[k]);
+        st.chi[k] = sah_max(st.chi[k], items[i].c[k]);
       }
   }
   // bins of [b, e) on the axes with a positive centroid extent, against the node's
   // centroid box (clo, ext)
   // bins for a range of n leaves: 256 for large ranges, fewer (at least 8 per leaf) for
   // small ones, where the binning of every node would otherwise cost more than its items
-  static int bins_for(int n) { return std::min(NB, std::max(32, 8 * n)); }
+  static int bins_for(int n) { return sah_bins_for(n); }
   void binning(int b, int e, const float clo[3], const float ext[3], RangeStats& st, int nb) const {
     for (int k = 0; k < 3; ++k)
       for (int q = 0; q < nb; ++q) {
@@ -207,13 +223,12 @@ struct SahBuilder {
     for (int i = b; i < e; ++i)
       for (int k = 0; k < 3; ++k) {
         if (!(ext[k] > 0.0f)) continue;
-        int q = (int)((items[i].c[k] - clo[k]) * scale[k]);
-        q = std::min(nb - 1, std::max(0, q));
+        const int q = sah_bin(items[i].c[k], clo[k], scale[k], nb);
         st.cnt[k][q]++;
         st.wsum[k][q] += items[i].w;
         for (int a = 0; a < 3; ++a) {
-          st.blo[k][q][a] = std::min(st.blo[k][q][a], items[i].lo[a]);
-          st.bhi[k][q][a] = std::max(st.bhi[k][q][a], items[i].hi[a]);
+          st.blo[k][q][a] = sah_min(st.blo[k][q][a], items[i].lo[a]);
+          st.bhi[k][q][a] = sah_max(st.bhi[k][q][a], items[i].hi[a]);
         }
       }
   }
@@ -234,8 +249,8 @@ struct SahBuilder {
         const RangeStats& o = part[c];
         if (boxes) {
           for (int k = 0; k < 3; ++k) {
-            st.lo[k] = std::min(st.lo[k], o.lo[k]); st.hi[k] = std::max(st.hi[k], o.hi[k]);
-            st.clo[k] = std::min(st.clo[k], o.clo[k]); st.chi[k] = std::max(st.chi[k], o.chi[k]);
+            st.lo[k] = sah_min(st.lo[k], o.lo[k]); st.hi[k] = sah_max(st.hi[k], o.hi[k]);
+            st.clo[k] = sah_min(st.clo[k], o.clo[k]); st.chi[k] = sah_max(st.chi[k], o.chi[k]);
           }
         } else {
           for (int k = 0; k < 3; ++k)
@@ -243,8 +258,8 @@ struct SahBuilder {
               st.cnt[k][q] += o.cnt[k][q];
               st.wsum[k][q] += o.wsum[k][q];
               for (int a = 0; a < 3; ++a) {
-                st.blo[k][q][a] = std::min(st.blo[k][q][a], o.blo[k][q][a]);
-                st.bhi[k][q][a] = std::max(st.bhi[k][q][a], o.bhi[k][q][a]);
+                st.blo[k][q][a] = sah_min(st.blo[k][q][a], o.blo[k][q][a]);
+                st.bhi[k][q][a] = sah_max(st.bhi[k][q][a], o.bhi[k][q][a]);
               }
             }
         }
@@ -293,7 +308,7 @@ struct SahBuilder {
       int ac = 0;
       int aw = 0;
       for (int q = nb - 1; q >= 0; --q) {
-        for (int a = 0; a < 3; ++a) { alo[a] = std::min(alo[a], blo[q][a]); ahi[a] = std::max(ahi[a], bhi[q][a]); }
+        for (int a = 0; a < 3; ++a) { alo[a] = sah_min(alo[a], blo[q][a]); ahi[a] = sah_max(ahi[a], bhi[q][a]); }
         ac += cnt[q];
         aw += st.wsum[k][q];
         for (int a = 0; a < 3; ++a) { rlo[q][a] = alo[a]; rhi[q][a] = ahi[a]; }
@@ -304,7 +319,7 @@ struct SahBuilder {
       int lc = 0;
       int lw = 0;
       for (int q = 0; q < nb - 1; ++q) {
-        for (int a = 0; a < 3; ++a) { llo[a] = std::min(llo[a], blo[q][a]); lhi[a] = std::max(lhi[a], bhi[q][a]); }
+        for (int a = 0; a < 3; ++a) { llo[a] = sah_min(llo[a], blo[q][a]); lhi[a] = sah_max(lhi[a], bhi[q][a]); }
         lc += cnt[q];
         lw += st.wsum[k][q];
         const int rc = rcnt[q + 1];
@@ -319,12 +334,8 @@ struct SahBuilder {
     } else {
       const float ext = chi[best_axis] - clo[best_axis];
       const float scale = nb / ext;
-      auto left = [&](const LeafItem& it) {
-        int q = (int)((it.c[best_axis] - clo[best_axis]) * scale);
-        q = std::min(nb - 1, std::max(0, q));
-        return q <= best_split;
-      };
-      mid = (int)(std::partition(items.begin() + b, items.begin() + e, left) - items.begin());
+      auto left = [&](const LeafItem& it) { return sah_bin(it.c[best_axis], clo[best_axis], scale, nb) <= best_split; };
+      mid = stable_split(b, e, left);
       if (mid == b || mid == e) mid = (b + e) / 2;
     }
     const int node = next_node.fetch_add(1);
@@ -424,7 +435,77 @@ struct SahBuilder {
   }
 };
 
+// the reference node array's checks (in parallel; the message names the first bad node)
+int check_nodes(const yc_bvh_node* nodes, int n_node, int n_tri, std::string& err) {
+  auto node_error = [&](int i, std::string* msg) {
+    const yc_bvh_node& n = nodes[i];
+    if (n.vert_len > 10) {
+      if (msg) *msg = "BVH node " + std::to_string(i) + " has vert_len > 10";
+      return true;
+    }
+    if (is_leaf(n)) {
+      for (int k = 0; k < n.vert_len; ++k)
+        if (n.vert_list[k] < 0 || n.vert_list[k] >= n_tri) {
+          if (msg) *msg = "BVH leaf " + std::to_string(i) + " references triangle " + std::to_string(n.vert_list[k]);
+          return true;
+        }
+    } else if (is_queued(n) || i == 0) {
+      if (n.child_idx <= 0 || n.child_idx + 1 >= n_node) {
+        if (msg) *msg = "BVH node " + std::to_string(i) + " has child_idx " + std::to_string(n.child_idx) + " out of range";
+        return true;
+      }
+    }
+    return false;
+  };
+  std::atomic<int> first_bad{n_node};
+  parallel_for((size_t)n_node, [&](size_t i) {
+    if (node_error((int)i, nullptr))
+      for (int m = first_bad.load(); (int)i < m && !first_bad.compare_exchange_weak(m, (int)i);) {}
+  });
+  if (first_bad.load() < n_node) {
+    node_error(first_bad.load(), &err);
+    return -1;
+  }
+  return 0;
+}
+
+// the leaves the reference traversal can reach, in node-index order, the first stream
+// slot of each (the slots their triangles take one leaf after another) and the slot total
+void reachable_leaves(const yc_bvh_node* nodes, int n_node, std::vector<int>& leaf_node, std::vector<int>& leaf_first,
+                      size_t& slots) {
+  std::vector<char> reach(n_node, 0);
+  reach[0] = 1;
+  slots = 0;
+  for (int i = 0; i < n_node; ++i) {
+    if (!reach[i]) continue;
+    const yc_bvh_node& n = nodes[i];
+    if (is_leaf(n)) {
+      leaf_node.push_back(i);
+      leaf_first.push_back((int)slots);
+      slots += (size_t)n.vert_len;
+    } else if (is_queued(n) || i == 0) {
+      for (int c = 0; c < 2; ++c)
+        if (is_queued(nodes[n.child_idx + c])) reach[n.child_idx + c] = 1;
+    }
+  }
+}
+
 }  // namespace
+
+int plan_device_repack(const yc_bvh_node* nodes, int n_node, int n_tri, DevRepackPlan& plan, std::string& err) {
+  plan = DevRepackPlan();
+  if (n_tri == 0 || n_node == 0) return 0;
+  if (check_nodes(nodes, n_node, n_tri, err)) return -1;
+  if (n_node >= (1 << 27)) { err = "BVH too large for the 27-bit tie-break rank"; return -1; }
+  const yc_bvh_node& root = nodes[0];
+  if (is_leaf(root)) return 0;
+  reachable_leaves(nodes, n_node, plan.leaf_node, plan.leaf_first, plan.slots);
+  if (plan.leaf_node.size() < 2) return 0;
+  if (plan.slots >= (size_t)(1 << 27)) { err = "scene too large for the 27-bit stream index"; return -1; }
+  plan.root_lo = float4{root.aabb.p_min.x, root.aabb.p_min.y, root.aabb.p_min.z, 0.0f};
+  plan.root_hi = float4{root.aabb.p_max.x, root.aabb.p_max.y, root.aabb.p_max.z, 0.0f};
+  return 1;
+}
 
 int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, int n_node, int tree_mode,
                  Repacked& out, std::string& err) {
@@ -484,36 +565,7 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
     return 0;
   }
 
-  // validate the reference node array (in parallel; the message names the first bad node)
-  auto node_error = [&](int i, std::string* msg) {
-    const yc_bvh_node& n = nodes[i];
-    if (n.vert_len > 10) {
-      if (msg) *msg = "BVH node " + std::to_string(i) + " has vert_len > 10";
-      return true;
-    }
-    if (is_leaf(n)) {
-      for (int k = 0; k < n.vert_len; ++k)
-        if (n.vert_list[k] < 0 || n.vert_list[k] >= n_tri) {
-          if (msg) *msg = "BVH leaf " + std::to_string(i) + " references triangle " + std::to_string(n.vert_list[k]);
-          return true;
-        }
-    } else if (is_queued(n) || i == 0) {
-      if (n.child_idx <= 0 || n.child_idx + 1 >= n_node) {
-        if (msg) *msg = "BVH node " + std::to_string(i) + " has child_idx " + std::to_string(n.child_idx) + " out of range";
-        return true;
-      }
-    }
-    return false;
-  };
-  std::atomic<int> first_bad{n_node};
-  parallel_for((size_t)n_node, [&](size_t i) {
-    if (node_error((int)i, nullptr))
-      for (int m = first_bad.load(); (int)i < m && !first_bad.compare_exchange_weak(m, (int)i);) {}
-  });
-  if (first_bad.load() < n_node) {
-    node_error(first_bad.load(), &err);
-    return -1;
-  }
+  if (check_nodes(nodes, n_node, n_tri, err)) return -1;
   const yc_bvh_node& root = nodes[0];
   out.root_test = 1;
   out.root_lo = float4{root.aabb.p_min.x, root.aabb.p_min.y, root.aabb.p_min.z, 0.0f};
@@ -530,21 +582,8 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
     // stream slot of each (then the stream and the leaf items are filled in parallel,
     // exactly as emit_leaf would append them one after another)
     std::vector<int> leaf_node, leaf_first;
-    std::vector<char> reach(n_node, 0);
-    reach[0] = 1;
-    size_t slots = b.out_tris.size() / 3;
-    for (int i = 0; i < n_node; ++i) {
-      if (!reach[i]) continue;
-      const yc_bvh_node& n = nodes[i];
-      if (is_leaf(n)) {
-        leaf_node.push_back(i);
-        leaf_first.push_back((int)slots);
-        slots += (size_t)n.vert_len;
-      } else if (is_queued(n) || i == 0) {
-        for (int c = 0; c < 2; ++c)
-          if (is_queued(nodes[n.child_idx + c])) reach[n.child_idx + c] = 1;
-      }
-    }
+    size_t slots = 0;
+    reachable_leaves(nodes, n_node, leaf_node, leaf_first, slots);
     if (leaf_node.empty()) { out.root_link = LINK_NONE; out.depth = 0; return 0; }
     if (slots >= (size_t)(1 << 27)) { err = "scene too large for the 27-bit stream index"; return -1; }
     std::vector<LeafItem> items(leaf_node.size());
@@ -558,7 +597,7 @@ int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, i
       for (int k = 0; k < 3; ++k) {
         it.lo[k] = plo[k];
         it.hi[k] = phi[k];
-        it.c[k] = 0.5f * (plo[k] + phi[k]);
+        it.c[k] = sah_centroid(plo[k], phi[k]);
       }
       it.link = b.fill_leaf(n.vert_list, n.vert_len, i * 16, leaf_first[j]);
       it.w = n.vert_len;

@@ -1,0 +1,607 @@
+// repack_dev.cu -- the upload's repack on the device for the default tree mode (an SAH
+// hierarchy over the reference leaves; yc_upload_scene with YC_OPT_REPACK 1).
+//
+// The reference uploads its BVHNodeGPU array as it is and walks it (traverseBVH,
+// kernels/legacy/udpt.cl:298-321); the core repacks it into the layout of yc_scene.h
+// (repack.cpp states what the layout keeps: each reference leaf's triangles, their order
+// and tie-break ranks). This file writes that layout on the GPU, byte for byte what the
+// host repack writes: the leaves' triangle stream, the shading records and the two-child
+// nodes of the binned SAH split of yc_sah.h.
+//
+// The split, top down. A range of leaves is one block's task: its bounds (block
+// reduction), its bins (shared-memory atomics), its split (one warp per axis scans the
+// bins, the first minimum of the cost in (axis, bin) order wins, as the host's sequential
+// sweep), then a stable partition through a second buffer. A node's index is known before
+// its subtree is built (pre-order: the left child follows its parent, the right child
+// comes after the left subtree's leaves - 1 nodes), so every task writes its own box and
+// link into its parent's record and no pass orders anything afterwards. Ranges of more
+// than SMALL_MAX leaves are split one level per launch, a block per range, with the
+// leaves in global memory; a range of at most SMALL_MAX leaves is loaded into one
+// block's shared memory and its whole subtree built there.
+//
+// Compiled with -fmad=false like the rest of the core: the areas and costs round as the
+// host's (-ffp-contract=off) do.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "yc_internal.h"
+#include "yc_repack.h"
+#include "yc_sah.h"
+
+namespace yc {
+
+namespace {
+
+constexpr int LEVEL_TB = 512;    // threads of a block that splits one large range
+constexpr int SMALL_TB = 128;    // threads of a block that builds one small subtree
+constexpr int SMALL_MAX = 512;   // ranges of at most this many leaves are built in shared memory
+constexpr int ITEM_TB = 256;
+
+// a reference leaf: its box, its triangle count (lo.w, integer bits) and its link (hi.w)
+struct __align__(16) SahItem {
+  float4 lo, hi;
+};
+
+// leaves [b, e) under node `node` (pre-order index); up = parent * 2 + side, -1 for the root
+struct SahTask {
+  int b, e, node, up, depth;
+};
+
+struct SahCtl {
+  int n_next;    // ranges queued for the next level
+  int n_small;   // ranges queued for the shared-memory builds
+  int depth;     // deepest task or leaf (the root is 0)
+  int bad;       // a list or a partition would have left its bounds (nothing was written there)
+};
+
+// per axis and bin: leaves, triangles, the union of the leaf boxes
+struct SahBins {
+  int cnt[3][SAH_NB];
+  int w[3][SAH_NB];
+  float lo[3][3][SAH_NB];
+  float hi[3][3][SAH_NB];
+};
+
+struct SahScratch {
+  float red[32][12];   // per-warp partial bounds
+  float box[12];       // the range's lo[3], hi[3], centroid lo[3], centroid hi[3]
+  float cost[3];       // per axis: the first minimal cost, its bin and left leaves
+  int split[3], nleft[3];
+  int axis, at, mid;   // the chosen axis (-1: split in half), bin, first leaf of the right side
+  int wcount[32];
+};
+
+constexpr float kInf = INFINITY;
+
+// a partial union of bins: box, leaves, triangles
+struct Acc {
+  float lo[3], hi[3];
+  int cnt, w;
+};
+__device__ __forceinline__ void acc_empty(Acc& a) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    a.lo[k] = kInf;
+    a.hi[k] = -kInf;
+  }
+  a.cnt = 0;
+  a.w = 0;
+}
+__device__ __forceinline__ void acc_join(Acc& a, const Acc& b) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    a.lo[k] = sah_min(a.lo[k], b.lo[k]);
+    a.hi[k] = sah_max(a.hi[k], b.hi[k]);
+  }
+  a.cnt += b.cnt;
+  a.w += b.w;
+}
+__device__ __forceinline__ void acc_bin(Acc& a, const SahBins& bn, int k, int q) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    a.lo[c] = sah_min(a.lo[c], bn.lo[k][c][q]);
+    a.hi[c] = sah_max(a.hi[c], bn.hi[k][c][q]);
+  }
+  a.cnt += bn.cnt[k][q];
+  a.w += bn.w[k][q];
+}
+__device__ __forceinline__ Acc acc_shfl_up(const Acc& a, int d) {
+  Acc r;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    r.lo[k] = __shfl_up_sync(0xffffffffu, a.lo[k], d);
+    r.hi[k] = __shfl_up_sync(0xffffffffu, a.hi[k], d);
+  }
+  r.cnt = __shfl_up_sync(0xffffffffu, a.cnt, d);
+  r.w = __shfl_up_sync(0xffffffffu, a.w, d);
+  return r;
+}
+__device__ __forceinline__ Acc acc_shfl_down(const Acc& a, int d) {
+  Acc r;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    r.lo[k] = __shfl_down_sync(0xffffffffu, a.lo[k], d);
+    r.hi[k] = __shfl_down_sync(0xffffffffu, a.hi[k], d);
+  }
+  r.cnt = __shfl_down_sync(0xffffffffu, a.cnt, d);
+  r.w = __shfl_down_sync(0xffffffffu, a.w, d);
+  return r;
+}
+
+__device__ __forceinline__ float comp(const float4& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+// the parent's record of a child: its box at the child's side and its link
+__device__ __forceinline__ void put_child(float4* nodes, int up, const float lo[3], const float hi[3], int link) {
+  if (up < 0) return;
+  float* o = reinterpret_cast<float*>(nodes + 4 * (size_t)(up >> 1));
+  const int side = up & 1;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    o[4 * k + side] = lo[k];
+    o[4 * k + 2 + side] = hi[k];
+  }
+  o[12 + side] = __int_as_float(link);
+}
+
+// bounds of items [b, e) into sc.box (all threads)
+__device__ void range_bounds(const SahItem* it, int b, int e, SahScratch& sc) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float v[12];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    v[k] = kInf;
+    v[3 + k] = -kInf;
+    v[6 + k] = kInf;
+    v[9 + k] = -kInf;
+  }
+  for (int i = b + threadIdx.x; i < e; i += blockDim.x) {
+    const float4 lo = it[i].lo, hi = it[i].hi;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float l = comp(lo, k), h = comp(hi, k), c = sah_centroid(l, h);
+      v[k] = sah_min(v[k], l);
+      v[3 + k] = sah_max(v[3 + k], h);
+      v[6 + k] = sah_min(v[6 + k], c);
+      v[9 + k] = sah_max(v[9 + k], c);
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+    for (int j = 0; j < 12; ++j) {
+      const float o = __shfl_xor_sync(0xffffffffu, v[j], off);
+      v[j] = ((j / 3) & 1) ? sah_max(v[j], o) : sah_min(v[j], o);
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int j = 0; j < 12; ++j) sc.red[warp][j] = v[j];
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int j = 0; j < 12; ++j) v[j] = lane < nw ? sc.red[lane][j] : (((j / 3) & 1) ? -kInf : kInf);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+      for (int j = 0; j < 12; ++j) {
+        const float o = __shfl_xor_sync(0xffffffffu, v[j], off);
+        v[j] = ((j / 3) & 1) ? sah_max(v[j], o) : sah_min(v[j], o);
+      }
+    if (lane == 0)
+#pragma unroll
+      for (int j = 0; j < 12; ++j) sc.box[j] = v[j];
+  }
+  __syncthreads();
+}
+
+// the bins of items [b, e) on the axes with a positive centroid extent (all threads)
+__device__ void range_bins(const SahItem* it, int b, int e, int nb, SahBins& bn, const SahScratch& sc) {
+  for (int x = threadIdx.x; x < 3 * nb; x += blockDim.x) {
+    const int k = x / nb, q = x - k * nb;
+    bn.cnt[k][q] = 0;
+    bn.w[k][q] = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      bn.lo[k][c][q] = kInf;
+      bn.hi[k][c][q] = -kInf;
+    }
+  }
+  float clo[3], scale[3];
+  bool on[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    clo[k] = sc.box[6 + k];
+    const float ext = sc.box[9 + k] - clo[k];
+    on[k] = ext > 0.0f;
+    scale[k] = on[k] ? (float)nb / ext : 0.0f;
+  }
+  __syncthreads();
+  for (int i = b + threadIdx.x; i < e; i += blockDim.x) {
+    const float4 lo = it[i].lo, hi = it[i].hi;
+    const int w = __float_as_int(lo.w);
+    const float l[3] = {lo.x, lo.y, lo.z}, h[3] = {hi.x, hi.y, hi.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (!on[k]) continue;
+      const int q = sah_bin(sah_centroid(l[k], h[k]), clo[k], scale[k], nb);
+      atomicAdd(&bn.cnt[k][q], 1);
+      atomicAdd(&bn.w[k][q], w);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        sah_atomic_min(&bn.lo[k][c][q], l[c]);
+        sah_atomic_max(&bn.hi[k][c][q], h[c]);
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// the split of the binned range [b, e): sc.axis, sc.at, sc.mid (all threads). Warp k
+// sweeps axis k: lane j owns bins [j per, (j + 1) per); the unions of the lanes below and
+// above come from warp scans, then each lane walks its bins for the left unions (upward)
+// and the right unions and costs (downward), keeping the smallest bin of its minimal cost.
+constexpr int kMaxPer = SAH_NB / 32;
+
+__device__ void range_split(int b, int e, int nb, const SahBins& bn, SahScratch& sc) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp < 3) {
+    const int k = warp;
+    const float ext = sc.box[9 + k] - sc.box[6 + k];
+    float best = kInf;
+    int bq = -1, bl = 0;
+    if (ext > 0.0f) {
+      const int per = (nb + 31) >> 5;
+      const int s0 = min(nb, lane * per), s1 = min(nb, s0 + per);
+      Acc agg;
+      acc_empty(agg);
+      for (int q = s0; q < s1; ++q) acc_bin(agg, bn, k, q);
+      // inclusive scans of the lane unions, upward and downward
+      Acc up = agg, down = agg;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const Acc u = acc_shfl_up(up, d);
+        if (lane >= d) acc_join(up, u);
+        const Acc v = acc_shfl_down(down, d);
+        if (lane + d < 32) acc_join(down, v);
+      }
+      Acc below = acc_shfl_up(up, 1), above = acc_shfl_down(down, 1);
+      if (lane == 0) acc_empty(below);
+      if (lane == 31) acc_empty(above);
+      // left unions at the lane's bins
+      Acc L[kMaxPer];
+      Acc run = below;
+#pragma unroll
+      for (int j = 0; j < kMaxPer; ++j) {
+        if (s0 + j < s1) acc_bin(run, bn, k, s0 + j);
+        L[j] = run;
+      }
+      Acc R = above;   // the union of the bins above the current one
+#pragma unroll
+      for (int j = kMaxPer - 1; j >= 0; --j) {
+        const int q = s0 + j;
+        if (q >= s1) continue;
+        if (q <= nb - 2 && L[j].cnt > 0 && R.cnt > 0) {
+          const float cost = sah_area(L[j].lo[0], L[j].lo[1], L[j].lo[2], L[j].hi[0], L[j].hi[1], L[j].hi[2]) *
+                                 (float)L[j].w +
+                             sah_area(R.lo[0], R.lo[1], R.lo[2], R.hi[0], R.hi[1], R.hi[2]) * (float)R.w;
+          if (cost < kInf && cost <= best) {   // downward: on equal costs the smaller bin
+            best = cost;
+            bq = q;
+            bl = L[j].cnt;
+          }
+        }
+        acc_bin(R, bn, k, q);
+      }
+    }
+    // the first minimum over the lanes: the smaller cost, then the smaller bin
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const float oc = __shfl_xor_sync(0xffffffffu, best, off);
+      const int oq = __shfl_xor_sync(0xffffffffu, bq, off);
+      const int ol = __shfl_xor_sync(0xffffffffu, bl, off);
+      if (oq >= 0 && (bq < 0 || oc < best || (oc == best && oq < bq))) {
+        best = oc;
+        bq = oq;
+        bl = ol;
+      }
+    }
+    if (lane == 0) {
+      sc.cost[k] = best;
+      sc.split[k] = bq;
+      sc.nleft[k] = bl;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int axis = -1;
+    float best = kInf;
+    for (int k = 0; k < 3; ++k)
+      if (sc.split[k] >= 0 && sc.cost[k] < best) {
+        best = sc.cost[k];
+        axis = k;
+      }
+    sc.axis = axis;
+    sc.at = axis >= 0 ? sc.split[axis] : -1;
+    sc.mid = axis >= 0 ? b + sc.nleft[axis] : (b + e) / 2;   // coincident centroids: split the list in half
+  }
+  __syncthreads();
+}
+
+// stable partition of items [b, e) by the chosen split, through tmp (all threads)
+__device__ void range_partition(SahItem* it, SahItem* tmp, int b, int e, int nb, SahScratch& sc, int* bad) {
+  const int k = sc.axis, split = sc.at, mid = sc.mid;
+  const float clo = sc.box[6 + k];
+  const float scale = (float)nb / (sc.box[9 + k] - clo);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int run_l = 0, run_r = 0;
+  for (int base = b; base < e; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const bool in = i < e;
+    SahItem x;
+    bool left = false;
+    if (in) {
+      x = it[i];
+      left = sah_bin(sah_centroid(comp(x.lo, k), comp(x.hi, k)), clo, scale, nb) <= split;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, left);
+    const int rank = __popc(m & ((1u << lane) - 1u));
+    if (lane == 0) sc.wcount[warp] = __popc(m);
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int w = 0; w < nw; ++w) {
+      const int c = sc.wcount[w];
+      before += w < warp ? c : 0;
+      total += c;
+    }
+    if (in) {
+      const int at = left ? b + run_l + before + rank : mid + run_r + (int)threadIdx.x - before - rank;
+      if (left ? at < mid : (at >= mid && at < e)) tmp[at] = x;
+      else *bad = 1;   // the bins and the partition disagree: the upload fails
+    }
+    run_l += total;
+    run_r += min((int)blockDim.x, e - base) - total;
+    __syncthreads();
+  }
+  for (int i = b + threadIdx.x; i < e; i += blockDim.x) it[i] = tmp[i];
+  __syncthreads();
+}
+
+// one task: its box and link into the parent's record, its depth, its split (all threads)
+__device__ void split_task(SahItem* it, SahItem* tmp, int b, int e, const SahTask& t, SahBins& bn, SahScratch& sc,
+                           float4* nodes, int* depth, int* bad) {
+  range_bounds(it, b, e, sc);
+  if (threadIdx.x == 0) {
+    const float lo[3] = {sc.box[0], sc.box[1], sc.box[2]}, hi[3] = {sc.box[3], sc.box[4], sc.box[5]};
+    put_child(nodes, t.up, lo, hi, t.node);
+    float* o = reinterpret_cast<float*>(nodes + 4 * (size_t)t.node);
+    o[14] = 0.0f;
+    o[15] = 0.0f;
+    atomicMax(depth, t.depth);
+  }
+  const int nb = sah_bins_for(e - b);
+  range_bins(it, b, e, nb, bn, sc);
+  range_split(b, e, nb, bn, sc);
+  if (sc.axis >= 0) range_partition(it, tmp, b, e, nb, sc, bad);
+}
+
+// a child range of one leaf: the parent's record takes the leaf's box and link
+__device__ __forceinline__ void put_leaf(float4* nodes, int up, const SahItem& x) {
+  const float lo[3] = {x.lo.x, x.lo.y, x.lo.z}, hi[3] = {x.hi.x, x.hi.y, x.hi.z};
+  put_child(nodes, up, lo, hi, __float_as_int(x.hi.w));
+}
+
+// one level of the large ranges, a block per range
+__global__ void __launch_bounds__(LEVEL_TB) k_sah_level(SahItem* items, SahItem* tmp, const SahTask* tasks,
+                                                        SahTask* next, int cap_next, SahTask* small, int cap_small,
+                                                        SahCtl* ctl, float4* nodes) {
+  __shared__ SahBins bn;
+  __shared__ SahScratch sc;
+  const SahTask t = tasks[blockIdx.x];
+  split_task(items, tmp, t.b, t.e, t, bn, sc, nodes, &ctl->depth, &ctl->bad);
+  if (threadIdx.x == 0) {
+    const int mid = sc.mid;
+    const SahTask kids[2] = {{t.b, mid, t.node + 1, 2 * t.node, t.depth + 1},
+                             {mid, t.e, t.node + (mid - t.b), 2 * t.node + 1, t.depth + 1}};
+    for (const SahTask& c : kids) {
+      const int n = c.e - c.b;
+      if (n == 1) {
+        put_leaf(nodes, c.up, items[c.b]);
+        atomicMax(&ctl->depth, c.depth);
+      } else if (n > SMALL_MAX) {
+        const int at = atomicAdd(&ctl->n_next, 1);
+        if (at < cap_next) next[at] = c;
+        else ctl->bad = 1;
+      } else {
+        const int at = atomicAdd(&ctl->n_small, 1);
+        if (at < cap_small) small[at] = c;
+        else ctl->bad = 1;
+      }
+    }
+  }
+}
+
+// shared memory of a small-range block: the leaves, the partition buffer, the bins and the
+// stack of pending ranges (disjoint, of two leaves or more: at most SMALL_MAX / 2)
+constexpr size_t kSmallSmem = 2 * SMALL_MAX * sizeof(SahItem) + sizeof(SahBins) + (SMALL_MAX / 2) * sizeof(SahTask);
+
+// the whole subtree of a range of at most SMALL_MAX leaves, a block per range
+__global__ void __launch_bounds__(SMALL_TB) k_sah_small(const SahItem* items, const SahTask* small, SahCtl* ctl,
+                                                        float4* nodes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  SahItem* it = reinterpret_cast<SahItem*>(smem);
+  SahItem* tmp = it + SMALL_MAX;
+  SahBins& bn = *reinterpret_cast<SahBins*>(tmp + SMALL_MAX);
+  SahTask* stack = reinterpret_cast<SahTask*>(&bn + 1);
+  __shared__ SahScratch sc;
+  __shared__ int top, dmax;
+  const SahTask r = small[blockIdx.x];
+  const int n = r.e - r.b;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) it[i] = items[r.b + i];
+  if (threadIdx.x == 0) {
+    stack[0] = SahTask{0, n, r.node, r.up, r.depth};
+    top = 1;
+    dmax = 0;
+  }
+  __syncthreads();
+  while (top > 0) {
+    const SahTask t = stack[top - 1];
+    __syncthreads();
+    if (threadIdx.x == 0) --top;
+    split_task(it, tmp, t.b, t.e, t, bn, sc, nodes, &dmax, &ctl->bad);
+    if (threadIdx.x == 0) {
+      const int mid = sc.mid;
+      const SahTask kids[2] = {{t.b, mid, t.node + 1, 2 * t.node, t.depth + 1},
+                               {mid, t.e, t.node + (mid - t.b), 2 * t.node + 1, t.depth + 1}};
+      for (const SahTask& c : kids) {
+        if (c.e - c.b == 1) {
+          put_leaf(nodes, c.up, it[c.b]);
+          dmax = max(dmax, c.depth);
+        } else if (top < SMALL_MAX / 2) {
+          stack[top++] = c;
+        } else {
+          ctl->bad = 1;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicMax(&ctl->depth, dmax);
+}
+
+// the leaf items and the leaves' triangle stream (as repack.cpp's fill_leaf), a thread per leaf
+__global__ void __launch_bounds__(ITEM_TB) k_leaf_items(const yc_bvh_node* __restrict__ nodes,
+                                                        const int* __restrict__ leaf_node,
+                                                        const int* __restrict__ leaf_first, int n_leaf,
+                                                        const yc_triangle* __restrict__ tris, SahItem* items,
+                                                        float4* stream) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_leaf) return;
+  const int i = leaf_node[j];
+  const yc_bvh_node& n = nodes[i];
+  const int first = leaf_first[j], count = n.vert_len;
+  const int link = ~((first << 4) | count);
+  items[j].lo = make_float4(n.aabb.p_min.x, n.aabb.p_min.y, n.aabb.p_min.z, __int_as_float(count));
+  items[j].hi = make_float4(n.aabb.p_max.x, n.aabb.p_max.y, n.aabb.p_max.z, __int_as_float(link));
+  for (int k = 0; k < count; ++k) {
+    const int id = n.vert_list[k];
+    const yc_triangle& t = tris[id];
+    float4* r = stream + 3 * ((size_t)first + k);
+    r[0] = make_float4(t.v1.x, t.v1.y, t.v1.z, __int_as_float(id));
+    r[1] = make_float4(__fsub_rn(t.v2.x, t.v1.x), __fsub_rn(t.v2.y, t.v1.y), __fsub_rn(t.v2.z, t.v1.z),
+                       __int_as_float(i * 16 + k));
+    r[2] = make_float4(__fsub_rn(t.v3.x, t.v1.x), __fsub_rn(t.v3.y, t.v1.y), __fsub_rn(t.v3.z, t.v1.z), 0.0f);
+  }
+}
+
+// a device temporary, freed on scope exit
+template <class T>
+struct Tmp {
+  T* p = nullptr;
+  ~Tmp() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t alloc(size_t n) { return cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)); }
+};
+
+}  // namespace
+
+int repack_device(const yc_triangle* tris_host, int n_tri, const yc_bvh_node* nodes_host, int n_node,
+                  const DevRepackPlan& plan, float4* nodes, float4* stream, float4* shade, int& depth, cudaStream_t s,
+                  std::string& err) {
+  const int n_leaf = (int)plan.leaf_node.size();
+  if (n_leaf < 2 || n_tri <= 0 || n_node <= 0) {
+    err = "device repack: the plan has fewer than two leaves";
+    return -1;
+  }
+  auto cuda_fail = [&](cudaError_t e, const char* what) {
+    err = std::string("device repack: ") + what + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? -2 : -1;
+  };
+#define YC_REPACK_CUDA(call, what)                  \
+  do {                                              \
+    const cudaError_t e_ = (call);                  \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+  const size_t cap_large = (size_t)n_leaf / (SMALL_MAX + 1) + 1;   // disjoint ranges of more than SMALL_MAX
+  const size_t cap_small = (size_t)n_leaf / 2 + 1;                 // disjoint ranges of two leaves or more
+  Tmp<yc_triangle> d_tris;
+  Tmp<yc_bvh_node> d_nodes;
+  Tmp<int> d_leaf, d_first;
+  Tmp<SahItem> d_items, d_tmp;
+  Tmp<SahTask> d_ta, d_tb, d_small;
+  Tmp<SahCtl> d_ctl;
+  YC_REPACK_CUDA(d_tris.alloc(n_tri), "allocation");
+  YC_REPACK_CUDA(d_nodes.alloc(n_node), "allocation");
+  YC_REPACK_CUDA(d_leaf.alloc(n_leaf), "allocation");
+  YC_REPACK_CUDA(d_first.alloc(n_leaf), "allocation");
+  YC_REPACK_CUDA(d_items.alloc(n_leaf), "allocation");
+  YC_REPACK_CUDA(d_tmp.alloc(n_leaf), "allocation");
+  YC_REPACK_CUDA(d_ta.alloc(cap_large), "allocation");
+  YC_REPACK_CUDA(d_tb.alloc(cap_large), "allocation");
+  YC_REPACK_CUDA(d_small.alloc(cap_small), "allocation");
+  YC_REPACK_CUDA(d_ctl.alloc(1), "allocation");
+  YC_REPACK_CUDA(cudaMemcpyAsync(d_tris.p, tris_host, (size_t)n_tri * sizeof(yc_triangle), cudaMemcpyHostToDevice, s),
+                 "copy");
+  YC_REPACK_CUDA(
+      cudaMemcpyAsync(d_nodes.p, nodes_host, (size_t)n_node * sizeof(yc_bvh_node), cudaMemcpyHostToDevice, s), "copy");
+  YC_REPACK_CUDA(cudaMemcpyAsync(d_leaf.p, plan.leaf_node.data(), (size_t)n_leaf * sizeof(int),
+                                 cudaMemcpyHostToDevice, s),
+                 "copy");
+  YC_REPACK_CUDA(cudaMemcpyAsync(d_first.p, plan.leaf_first.data(), (size_t)n_leaf * sizeof(int),
+                                 cudaMemcpyHostToDevice, s),
+                 "copy");
+  // shading records: the refit's kernel alone (no stream slots, no nodes)
+  if (launch_refit(RefitPlan(), d_tris.p, n_tri, nullptr, nullptr, 0, shade, false, LINK_NONE, false, nullptr, s))
+    return cuda_fail(cudaGetLastError(), "shading records");
+  k_leaf_items<<<(n_leaf + ITEM_TB - 1) / ITEM_TB, ITEM_TB, 0, s>>>(d_nodes.p, d_leaf.p, d_first.p, n_leaf, d_tris.p,
+                                                                   d_items.p, stream);
+  YC_REPACK_CUDA(cudaPeekAtLastError(), "leaf items");
+  const SahTask root{0, n_leaf, 0, -1, 0};
+  SahCtl h_ctl{0, 0, 0, 0};
+  int n_large = 0;
+  if (n_leaf > SMALL_MAX) {
+    YC_REPACK_CUDA(cudaMemcpyAsync(d_ta.p, &root, sizeof(root), cudaMemcpyHostToDevice, s), "copy");
+    n_large = 1;
+  } else {
+    YC_REPACK_CUDA(cudaMemcpyAsync(d_small.p, &root, sizeof(root), cudaMemcpyHostToDevice, s), "copy");
+    h_ctl.n_small = 1;
+  }
+  YC_REPACK_CUDA(cudaMemcpyAsync(d_ctl.p, &h_ctl, sizeof(h_ctl), cudaMemcpyHostToDevice, s), "copy");
+  YC_REPACK_CUDA(cudaStreamSynchronize(s), "upload");   // h_ctl and root are read by the copies above
+  while (n_large > 0) {
+    k_sah_level<<<n_large, LEVEL_TB, 0, s>>>(d_items.p, d_tmp.p, d_ta.p, d_tb.p, (int)cap_large, d_small.p,
+                                             (int)cap_small, d_ctl.p, nodes);
+    YC_REPACK_CUDA(cudaPeekAtLastError(), "split level");
+    YC_REPACK_CUDA(cudaMemcpyAsync(&h_ctl, d_ctl.p, sizeof(h_ctl), cudaMemcpyDeviceToHost, s), "copy");
+    YC_REPACK_CUDA(cudaStreamSynchronize(s), "split level");
+    n_large = h_ctl.n_next;
+    if (h_ctl.bad || (size_t)n_large > cap_large || (size_t)h_ctl.n_small > cap_small) {
+      err = "device repack: a split left its bounds";
+      return -1;
+    }
+    YC_REPACK_CUDA(cudaMemsetAsync(&d_ctl.p->n_next, 0, sizeof(int), s), "reset");
+    std::swap(d_ta.p, d_tb.p);
+  }
+  if (h_ctl.n_small > 0) {
+    YC_REPACK_CUDA(cudaFuncSetAttribute(k_sah_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmem),
+                   "shared memory");
+    k_sah_small<<<h_ctl.n_small, SMALL_TB, kSmallSmem, s>>>(d_items.p, d_small.p, d_ctl.p, nodes);
+    YC_REPACK_CUDA(cudaPeekAtLastError(), "subtrees");
+  }
+  YC_REPACK_CUDA(cudaMemcpyAsync(&h_ctl, d_ctl.p, sizeof(h_ctl), cudaMemcpyDeviceToHost, s), "copy");
+  YC_REPACK_CUDA(cudaStreamSynchronize(s), "subtrees");
+#undef YC_REPACK_CUDA
+  if (h_ctl.bad) {
+    err = "device repack: a split left its bounds";
+    return -1;
+  }
+  depth = h_ctl.depth + 1;
+  return 0;
+}
+
+}  // namespace yc

@@ -168,14 +168,22 @@ def build_bvh(tris, bins=20, leaf=10):
     return nodes, depth
 
 
-def device_bytes(s, tree_mode=1):
-    """Bytes scene `s` will hold on the device once uploaded in tree mode `tree_mode`
-    (yc_scene_layout: the upload's repack, run on the host without a device)."""
+def layout(s, tree_mode=1):
+    """The device layout scene `s` takes once uploaded in tree mode `tree_mode`, computed by
+    the upload's repack on the host without a device (yc_scene_layout): a dict of
+    device_bytes, node_bytes, stream_bytes, shade_bytes, digest, depth, wide."""
     out = N.SceneLayout()
     tris, nodes = np.ascontiguousarray(s.tris), np.ascontiguousarray(s.nodes)
     N.check(N.lib().yc_scene_layout(ptr(tris), len(tris), len(s.mats), ptr(nodes), len(nodes), tree_mode,
                                     C.byref(out)), "yc_scene_layout")
-    return int(out.device_bytes)
+    return {k: int(getattr(out, k)) for k in ("device_bytes", "node_bytes", "stream_bytes", "shade_bytes", "digest",
+                                              "depth", "wide")}
+
+
+def device_bytes(s, tree_mode=1):
+    """Bytes scene `s` will hold on the device once uploaded in tree mode `tree_mode`
+    (yc_scene_layout: the upload's repack, run on the host without a device)."""
+    return layout(s, tree_mode)["device_bytes"]
 
 
 def walk_counts(s, rays9, any_hit=False, tree_mode=1):
