@@ -103,8 +103,10 @@ def build_oracle(force=False):
     return out
 
 
-def build_ref(force=False):
-    """Returns the path of libyune_ref.so, or None when no reference text is at hand."""
+def build_ref(force=False, libm=False):
+    """Returns the path of libyune_ref.so, or None when no reference text is at hand. With
+    libm, libyune_ref_libm.so: the same kernels with the host C library's cosf, sinf and
+    powf as the OpenCL built-ins (cl_shim.hpp, YREF_LIBM)."""
     os.makedirs(REF_OUT, exist_ok=True)
     REF_SRC = reference_tree()
     have_tree = REF_SRC is not None
@@ -139,7 +141,7 @@ def build_ref(force=False):
     if not all(os.path.exists(os.path.join(REF_OUT, inc)) for inc in incs):
         return None
     have_host = all(os.path.exists(os.path.join(HOST_DIR, rel)) for rel in HOST_SOURCES)
-    out = os.path.join(REF_OUT, "libyune_ref.so")
+    out = os.path.join(REF_OUT, "libyune_ref_libm.so" if libm else "libyune_ref.so")
     deps = [os.path.join(REF_OUT, inc) for inc in incs]
     if have_host:
         deps += [os.path.join(HOST_DIR, rel) for rel in HOST_SOURCES]
@@ -154,6 +156,8 @@ def build_ref(force=False):
         cmd += [os.path.join(HOST_DIR, rel) for rel in HOST_SOURCES]
     else:
         cmd += ["-DYREF_NO_HOST"]
+    if libm:
+        cmd += ["-DYREF_LIBM"]
     cmd += ["-o", out]
     _run(cmd)
     return out

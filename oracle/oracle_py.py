@@ -68,24 +68,43 @@ def ref():
     global _ref, _ref_tried
     if not _ref_tried:
         _ref_tried = True
-        try:
-            path = build_oracle.build_ref()
-        except RuntimeError:
-            path = None
-        if path and os.path.exists(path):
-            L = C.CDLL(path)
-            L.ref_render.argtypes = [i32, vp, i32, vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, u32, i32, i32, i32, i32,
-                                     i32, i32, i32]
-            L.ref_trace.argtypes = [vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, vp, vp]
-            L.ref_tonemap.argtypes = [vp, i32, i32, vp]
-            L.ref_oren_nayar.argtypes = [vp, vp, vp, vp, vp, vp]
-            if hasattr(L, "ref_bvh_build"):
-                L.ref_bvh_build.argtypes = [vp, i32, i32, i32, vp, i32, C.POINTER(i32)]
-            if hasattr(L, "ref_load_obj"):
-                L.ref_load_obj.argtypes = [C.c_char_p, C.c_char_p, vp, i32, C.POINTER(i32), vp, i32, C.POINTER(i32), vp,
-                                           i32, C.POINTER(i32)]
-            _ref = L
+        _ref = _load_ref(False)
     return _ref
+
+
+_ref_libm = None
+_ref_libm_tried = False
+
+
+def ref_libm():
+    """The compiled reference with the host C library's cosf, sinf and powf as its built-ins,
+    or None when no reference text is available."""
+    global _ref_libm, _ref_libm_tried
+    if not _ref_libm_tried:
+        _ref_libm_tried = True
+        _ref_libm = _load_ref(True)
+    return _ref_libm
+
+
+def _load_ref(libm):
+    try:
+        path = build_oracle.build_ref(libm=libm)
+    except RuntimeError:
+        path = None
+    if not (path and os.path.exists(path)):
+        return None
+    L = C.CDLL(path)
+    L.ref_render.argtypes = [i32, vp, i32, vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, u32, i32, i32, i32, i32, i32,
+                             i32, i32]
+    L.ref_trace.argtypes = [vp, i32, vp, i32, vp, i32, vp, i32, i32, vp, vp, vp]
+    L.ref_tonemap.argtypes = [vp, i32, i32, vp]
+    L.ref_oren_nayar.argtypes = [vp, vp, vp, vp, vp, vp]
+    if hasattr(L, "ref_bvh_build"):
+        L.ref_bvh_build.argtypes = [vp, i32, i32, i32, vp, i32, C.POINTER(i32)]
+    if hasattr(L, "ref_load_obj"):
+        L.ref_load_obj.argtypes = [C.c_char_p, C.c_char_p, vp, i32, C.POINTER(i32), vp, i32, C.POINTER(i32), vp,
+                                   i32, C.POINTER(i32)]
+    return L
 
 
 _scene_lib = None
@@ -273,8 +292,9 @@ def tonemap(accum):
 VARIANT = {"udpt_a": 0, "udpt_mis": 1, "udpt_mis4": 2, "udpt_mis_on": 3, "bdpt20": 10, "bdpt8": 11, "bdpt8_l4": 12}
 
 
-def ref_render(scene, accum, rand_seed, reset, variant, rr_threshold, max_depth, gi_check=1, threads=0, rows=None):
-    L = ref()
+def ref_render(scene, accum, rand_seed, reset, variant, rr_threshold, max_depth, gi_check=1, threads=0, rows=None,
+               libm=False):
+    L = ref_libm() if libm else ref()
     H, W = accum.shape[:2]
     r0, r1 = rows if rows else (0, 0)
     rc = L.ref_render(VARIANT[variant], _p(scene.tris), len(scene.tris), _p(scene.mats), len(scene.mats),

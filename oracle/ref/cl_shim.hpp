@@ -5,7 +5,8 @@
 // calls resolve to these built-ins and never to <cmath>. The built-ins are the ym::
 // routines, i.e. the same IEEE operation sequence the oracle and the CUDA core use;
 // the OpenCL spec leaves their rounding to the implementation, and this is the
-// implementation the reference is run with here.
+// implementation the reference is run with here. Built with YREF_LIBM, cos, sin and pow
+// come from the host C library instead (oracle/_ref/libyune_ref_libm.so).
 #pragma once
 
 #include <climits>
@@ -80,9 +81,17 @@ inline float4 clamp(float4 x, float4 lo, float4 hi) {
   return float4(clamp(x.x, lo.x, hi.x), clamp(x.y, lo.y, hi.y), clamp(x.z, lo.z, hi.z), clamp(x.w, lo.w, hi.w));
 }
 inline float sqrt(float x) { return ym::sqrt(x); }
+#if defined(YREF_LIBM)
+// the host C library's single-precision routines instead (another implementation the
+// OpenCL spec allows: the measure of how far the image moves with the built-ins)
+inline float cos(float x) { return ::cosf(x); }
+inline float sin(float x) { return ::sinf(x); }
+inline float pow(float x, float y) { return ::powf(x, y); }
+#else
 inline float cos(float x) { return ym::cos(x); }
 inline float sin(float x) { return ym::sin(x); }
 inline float pow(float x, float y) { return ym::pow(x, y); }
+#endif
 inline float4 pow(float4 x, float4 y) { return float4(pow(x.x, y.x), pow(x.y, y.y), pow(x.z, y.z), pow(x.w, y.w)); }
 inline float pown(float x, int n) { return ym::pown(x, n); }
 inline float ceil(float x) { return ym::ceil(x); }
