@@ -276,6 +276,10 @@ typedef struct yc_batch_cfg {
                                   when it first runs). Fewer entries leave more of the SM's L1
                                   to the node and triangle fetches; a value at or above the
                                   stack depth keeps the whole stack in shared memory; 0 = 12 */
+  int32_t trace_share;         /* percent of the traversal blocks that fit on an SM that the
+                                  persistent traversal grid launches (10..100): below 100 each
+                                  SM keeps room for the other slot groups' kernels (ray sort,
+                                  shading) to run beside a group's traversal; 0 = 100 */
 } yc_batch_cfg;
 int yc_batch_create(yc_ctx* ctx, const yc_batch_cfg* cfg, yc_batch** out);
 /* Adds a job: n_pass passes of scene_id into accum_id seen from *cam, pass k with
@@ -304,7 +308,8 @@ int yc_batch_destroy(yc_batch* b);
  * into scratch accumulators under each candidate, timed with CUDA events. The search runs
  * one parameter at a time from *start -- pool_paths (512K..4M, at most the mix's pixels
  * rounded up to a power of two), rounds_per_launch (4/8/16/32), logic_blocks_per_sm (2/4/8),
- * sort_threshold (0, 64K, 256K), groups (1/2/4), ray_sort (off, 32, 322), trace_block
+ * sort_threshold (0, 64K, 256K), groups and trace_share together (1/2/4 groups at 100%,
+ * 2/4/8 groups at 50%, 4/8 groups at 25%), ray_sort (off, 32, 322), trace_block
  * (64/128/256 threads) and stack_smem (8/12/16 entries, or the whole stack) -- keeping the
  * best value of each, and sweeps again while a sweep
  * moved the shape (at most `sweeps` sweeps). start->stack_cap must hold the deepest

@@ -49,3 +49,19 @@ def test_small_mixes_calibrate_over_several_passes():
     assert autotune.calibration_passes(1024 * 1024) == 16
     assert autotune.calibration_passes(8 << 20) == 2
     assert autotune.calibration_passes(60_000_000) == 1
+
+
+def test_groups_and_trace_share_are_searched_together():
+    """More slot groups pay only when each group's traversal leaves room on the SMs for
+    the others (trace_share below 100): the two are one search dimension, so an optimum
+    that neither reaches alone (4 groups at 50%, where 4 groups at 100% and 2 groups at
+    50% are both worse than the start) is found."""
+    def clock(shape):
+        if shape.groups == 4 and shape.trace_share == 50:
+            return 1.0
+        return 2.0 + (shape.groups != 2) + (shape.trace_share != 100)
+
+    best, trials = autotune.search(START, 8 << 20, clock)
+    assert (best.groups, best.trace_share) == (4, 50)
+    assert {(t.groups, t.trace_share) for t, _ in trials} >= {(1, 100), (2, 100), (4, 100), (2, 50), (4, 50),
+                                                                 (8, 50), (4, 25), (8, 25)}

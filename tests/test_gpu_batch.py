@@ -1,6 +1,8 @@
 """The batch engine against the per-pass path: jobs of different scenes, resolutions and
 pass counts rendered together must give, per job, exactly the accumulator the per-pass
 path gives alone (each pixel's passes run in order in one slot)."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -19,11 +21,13 @@ def _jobs():
 
 
 # stack_smem: walk-stack entries in shared memory (0: the default 12; 1, 2, 4: most of
-# each walk's stack in the global spill area; 64: all of it in shared memory)
-@pytest.mark.parametrize("use_graph,pool,sort,groups,tb,smem", [(True, 4096, 0, 1, 0, 0), (False, 1000, 0, 2, 64, 4),
-                                                               (True, 1 << 16, 0, 2, 256, 2), (True, 4096, 1, 3, 32, 64),
-                                                               (False, 1000, 64, 4, 128, 1), (True, 999, 0, 8, 96, 12)])
-def test_batch_matches_per_pass(use_graph, pool, sort, groups, tb, smem):
+# each walk's stack in the global spill area; 64: all of it in shared memory); share: the
+# traversal grid's percent of the resident blocks (0: 100; 10: one block per SM)
+@pytest.mark.parametrize("use_graph,pool,sort,groups,tb,smem,share",
+                         [(True, 4096, 0, 1, 0, 0, 0), (False, 1000, 0, 2, 64, 4, 50),
+                          (True, 1 << 16, 0, 2, 256, 2, 0), (True, 4096, 1, 3, 32, 64, 25),
+                          (False, 1000, 64, 4, 128, 1, 10), (True, 999, 0, 8, 96, 12, 75)])
+def test_batch_matches_per_pass(use_graph, pool, sort, groups, tb, smem, share):
     jobs = _jobs()
     with Renderer(0) as r:
         ids = []
@@ -37,7 +41,7 @@ def test_batch_matches_per_pass(use_graph, pool, sort, groups, tb, smem):
             r.render_passes(sid, aid, seeds, reset_first=1, cfg=s.cfg)
             want.append(r.read_accum(aid))
         b = Batch(r, pool_paths=pool, rounds_per_launch=4, use_graph=use_graph, sort_threshold=sort, groups=groups,
-                  trace_block=tb, stack_smem=smem)
+                  trace_block=tb, stack_smem=smem, trace_share=share)
         accs = []
         for (s, seeds), sid in zip(jobs, ids):
             aid = r.alloc_accum(s.width, s.height)
@@ -183,3 +187,15 @@ def test_cancelled_job_drains_and_others_are_unchanged(groups):
         assert np.array_equal(r.read_accum(acc_c).view(np.int32), want[1].view(np.int32))
         assert bt.progress(jc) == (n, n) and bt.progress(jb) == (b.width * b.height,) * 2
         bt.close()
+
+
+@pytest.mark.parametrize("field,value", [("trace_share", 5), ("trace_share", 101), ("trace_block", 48),
+                                         ("groups", 9), ("stack_smem", -1)])
+def test_batch_refuses_bad_shapes(field, value):
+    """yc_batch_create refuses a launch shape outside its ranges with YC_E_INVALID."""
+    from yune_gb300 import _native as N
+    with Renderer(0) as r:
+        cfg = N.BatchCfg(4096, 4, 2, 1, 0, 0, 0, 0, 0, 0, 0, 0)
+        setattr(cfg, field, value)
+        h = C.c_void_p()
+        assert r.L.yc_batch_create(r.h, C.byref(cfg), C.byref(h)) == N.YC_E_INVALID

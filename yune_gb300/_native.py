@@ -55,7 +55,7 @@ class BatchCfg(C.Structure):
     """yc_batch_cfg"""
     _fields_ = [("pool_paths", i32), ("rounds_per_launch", i32), ("logic_blocks_per_sm", i32), ("use_graph", i32),
                 ("max_jobs", i32), ("stack_cap", i32), ("sort_threshold", i32), ("groups", i32), ("ray_sort", i32),
-                ("trace_block", i32), ("stack_smem", i32)]
+                ("trace_block", i32), ("stack_smem", i32), ("trace_share", i32)]
 
 
 class ServeCfg(C.Structure):

@@ -1,15 +1,17 @@
 """Autotuner for the batch engine's launch shape: a Python front end of yc_batch_tune
 (core/tune.cpp, in the C-ABI so that a C or C++ host tunes the same way).
 
-The batch engine (yc_batch_*) has eight free parameters that change speed but never
+The batch engine (yc_batch_*) has nine free parameters that change speed but never
 results: the number of path slots in flight (the wavefront size), the rounds captured in
 one CUDA graph launch, the logic kernel's blocks per SM, the queue size from which the
 shade queue is sorted by path phase and material class (0: never), the number of slot
 groups whose rounds run concurrently, whether each round's rays are sorted by origin and
 direction cell before the trace, the traversal kernels' block shape (threads per
 block: with the per-thread stack columns it sets the shared memory per block, hence the
-blocks and the L1 left per SM), and how many entries of each walk's stack stay in shared
-memory (the deeper ones spill to global memory; fewer leave more L1). The best values depend on the job mix (total pixels,
+blocks and the L1 left per SM), how many entries of each walk's stack stay in shared
+memory (the deeper ones spill to global memory; fewer leave more L1), and the share of
+each SM the persistent traversal grid takes (below 100% the other slot groups' kernels
+run beside it; searched together with the number of groups). The best values depend on the job mix (total pixels,
 scene sizes, path lengths), so the tuner times candidate shapes on a calibration run of
 the mix itself: every job's first passes, into scratch accumulators, with the engine's own
 CUDA-event clock; small mixes render several passes per job so that the calibration sees
@@ -42,17 +44,24 @@ class BatchShape:
     ray_sort: int = 0
     trace_block: int = 128
     stack_smem: int = 12
+    trace_share: int = 100
 
     def kwargs(self):
         return dict(pool_paths=self.pool_paths, rounds_per_launch=self.rounds_per_launch,
                     logic_blocks_per_sm=self.logic_blocks_per_sm, sort_threshold=self.sort_threshold,
                     groups=self.groups, ray_sort=self.ray_sort, trace_block=self.trace_block,
-                    stack_smem=self.stack_smem)
+                    stack_smem=self.stack_smem, trace_share=self.trace_share)
 
     @staticmethod
     def of(cfg):
         return BatchShape(cfg.pool_paths, cfg.rounds_per_launch, cfg.logic_blocks_per_sm, cfg.sort_threshold,
-                          cfg.groups, cfg.ray_sort, cfg.trace_block, cfg.stack_smem)
+                          cfg.groups, cfg.ray_sort, cfg.trace_block, cfg.stack_smem, cfg.trace_share)
+
+    def cfg(self, stack_cap=0, use_graph=1):
+        """The yc_batch_cfg of this shape."""
+        return N.BatchCfg(self.pool_paths, self.rounds_per_launch, self.logic_blocks_per_sm, use_graph, 0, stack_cap,
+                          self.sort_threshold, self.groups, self.ray_sort, self.trace_block, self.stack_smem,
+                          self.trace_share)
 
 
 def calibration_passes(total_px):
@@ -77,9 +86,7 @@ def tune(renderer, jobs, sizes, stack_cap=0, log=None, sweeps=2):
         C.memmove(C.byref(t.cam), np.ascontiguousarray(cam).ctypes.data, C.sizeof(N.Cam))
         t.cfg = cfg_struct(cfg)
         t.scene_id, t.width, t.height, t.n_pass, t.seeds_host = sid, w, h, passes, sd.ctypes.data
-    b = BatchShape()
-    start = N.BatchCfg(b.pool_paths, b.rounds_per_launch, b.logic_blocks_per_sm, 1, 0, stack_cap, b.sort_threshold,
-                       b.groups, b.ray_sort, b.trace_block, b.stack_smem)
+    start = BatchShape().cfg(stack_cap)
     cap = 256
     out = N.BatchCfg()
     tr = (N.TuneTrial * cap)()
@@ -99,8 +106,7 @@ def search(start, total_px, clock, sweeps=2):
     def cb(cfg, _user):
         return float(clock(BatchShape.of(cfg.contents)))
     fn = N.TUNE_CLOCK(cb)
-    st = N.BatchCfg(start.pool_paths, start.rounds_per_launch, start.logic_blocks_per_sm, 1, 0, 0,
-                    start.sort_threshold, start.groups, start.ray_sort, start.trace_block, start.stack_smem)
+    st = start.cfg()
     out = N.BatchCfg()
     cap = 256
     tr = (N.TuneTrial * cap)()

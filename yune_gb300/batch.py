@@ -15,11 +15,12 @@ from .layouts import ptr
 
 class Batch:
     def __init__(self, renderer, pool_paths=0, rounds_per_launch=0, logic_blocks_per_sm=0, use_graph=True,
-                 max_jobs=0, stack_cap=0, sort_threshold=0, groups=0, ray_sort=0, trace_block=0, stack_smem=0):
+                 max_jobs=0, stack_cap=0, sort_threshold=0, groups=0, ray_sort=0, trace_block=0, stack_smem=0,
+                 trace_share=0):
         self.r = renderer
         self.L = renderer.L
         cfg = N.BatchCfg(pool_paths, rounds_per_launch, logic_blocks_per_sm, int(use_graph), max_jobs, stack_cap,
-                         sort_threshold, groups, ray_sort, trace_block, stack_smem)
+                         sort_threshold, groups, ray_sort, trace_block, stack_smem, trace_share)
         h = C.c_void_p()
         N.check(self.L.yc_batch_create(renderer.h, C.byref(cfg), C.byref(h)), "yc_batch_create")
         self.h = h

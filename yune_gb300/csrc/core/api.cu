@@ -1450,6 +1450,8 @@ int yc_batch_create(yc_ctx* c, const yc_batch_cfg* cfg, yc_batch** out) {
   if (b->cfg.trace_block <= 0) b->cfg.trace_block = 128;
   if (b->cfg.stack_smem < 0) return fail(YC_E_INVALID, "stack_smem must not be negative");
   if (b->cfg.stack_smem == 0) b->cfg.stack_smem = 12;
+  if (b->cfg.trace_share == 0) b->cfg.trace_share = 100;
+  if (b->cfg.trace_share < 10 || b->cfg.trace_share > 100) return fail(YC_E_INVALID, "trace_share must be 10..100");
   if (b->cfg.trace_block > 256 || b->cfg.trace_block % 32)
     return fail(YC_E_INVALID, "trace_block must be a multiple of 32 up to 256");
   if (b->cfg.groups > 8 || b->cfg.groups > b->cfg.pool_paths) return fail(YC_E_INVALID, "groups must be 1..8");
@@ -1589,6 +1591,10 @@ int yc_batch_run(yc_batch* b, int max_launches, int* unfinished) {
     b->grid_c = yc::batch_trace_grid(false, b->stack_smem, b->wide == 1, b->cfg.trace_block);
     b->grid_a = yc::batch_trace_grid(true, b->stack_smem, b->wide == 1, b->cfg.trace_block);
     b->grid_m = yc::batch_trace_mixed_grid(b->stack_smem, b->wide == 1, b->cfg.trace_block);
+    // trace_share: a persistent grid of that share of the resident blocks (at least one per
+    // SM) leaves each SM room for the other groups' kernels
+    if (b->cfg.trace_share < 100 && b->grid_m > 0)
+      b->grid_m = std::max(c->sm_count, (int)((int64_t)b->grid_m * b->cfg.trace_share / 100));
     if (b->grid_c <= 0 || b->grid_a <= 0 || b->grid_m <= 0)
       return fail(YC_E_LAUNCH, "batch trace kernel cannot be resident");
     if (b->stack_smem < b->stack_cap) {

@@ -23,7 +23,7 @@ int set_error(int code, const char* msg);   // api.cu: sets yc_last_error()
 using yc::set_error;
 
 static_assert(sizeof(yc_request_desc) == 144, "yc_request_desc: cam, cfg, four ints, a pointer");
-static_assert(sizeof(yc_serve_cfg) == 64, "yc_serve_cfg: 16 bytes, then yc_batch_cfg (11 ints), padding");
+static_assert(sizeof(yc_serve_cfg) == 64, "yc_serve_cfg: 16 bytes, then yc_batch_cfg (12 ints)");
 static_assert(sizeof(yc_request_info) == 48, "yc_request_info: two ints, two int64, three doubles");
 
 // ---------------------------------------------------------------------------------------

@@ -26,13 +26,14 @@ int set_error(int code, const char* msg);   // api.cu: sets yc_last_error()
 }
 
 static_assert(sizeof(yc_tune_job) == 144, "yc_tune_job: cam, cfg, four ints, a pointer");
-static_assert(sizeof(yc_tune_trial) == 48, "yc_tune_trial: yc_batch_cfg (11 ints) and a float");
+static_assert(sizeof(yc_tune_trial) == 52, "yc_tune_trial: yc_batch_cfg (12 ints) and a float");
 
 namespace {
 
+// one search dimension: one field, or fields searched together (each value a tuple)
 struct Param {
-  int32_t yc_batch_cfg::*field;
-  std::vector<int32_t> values;
+  std::vector<int32_t yc_batch_cfg::*> fields;
+  std::vector<std::vector<int32_t>> values;
 };
 
 bool same(const yc_batch_cfg& a, const yc_batch_cfg& b) { return std::memcmp(&a, &b, sizeof a) == 0; }
@@ -90,15 +91,18 @@ extern "C" int yc_tune_search(const yc_batch_cfg* start, int64_t total_px, int s
   // more slots than the mix has pixels would stay idle
   int32_t pool_cap = 1 << 16;
   while (pool_cap < total_px && pool_cap < (1 << 22)) pool_cap <<= 1;
+  // slot groups and the traversal's share of each SM are searched together: more groups
+  // pay only when a group's traversal leaves room on the SMs for the others' kernels
   const std::vector<Param> params = {
-      {&yc_batch_cfg::pool_paths, {1 << 19, 1 << 20, 1 << 21, 1 << 22}},
-      {&yc_batch_cfg::rounds_per_launch, {4, 8, 16, 32}},
-      {&yc_batch_cfg::logic_blocks_per_sm, {2, 4, 8}},
-      {&yc_batch_cfg::sort_threshold, {0, 1 << 16, 1 << 18}},
-      {&yc_batch_cfg::groups, {1, 2, 4}},
-      {&yc_batch_cfg::ray_sort, {-1, 32, 322}},
-      {&yc_batch_cfg::trace_block, {64, 128, 256}},
-      {&yc_batch_cfg::stack_smem, {8, 12, 16, kWholeStack}},
+      {{&yc_batch_cfg::pool_paths}, {{1 << 19}, {1 << 20}, {1 << 21}, {1 << 22}}},
+      {{&yc_batch_cfg::rounds_per_launch}, {{4}, {8}, {16}, {32}}},
+      {{&yc_batch_cfg::logic_blocks_per_sm}, {{2}, {4}, {8}}},
+      {{&yc_batch_cfg::sort_threshold}, {{0}, {1 << 16}, {1 << 18}}},
+      {{&yc_batch_cfg::groups, &yc_batch_cfg::trace_share},
+       {{1, 100}, {2, 100}, {4, 100}, {2, 50}, {4, 50}, {8, 50}, {4, 25}, {8, 25}}},
+      {{&yc_batch_cfg::ray_sort}, {{-1}, {32}, {322}}},
+      {{&yc_batch_cfg::trace_block}, {{64}, {128}, {256}}},
+      {{&yc_batch_cfg::stack_smem}, {{8}, {12}, {16}, {kWholeStack}}},
   };
   std::vector<std::pair<yc_batch_cfg, float>> timed;
   auto record = [&](const yc_batch_cfg& c, float ms) {
@@ -109,17 +113,19 @@ extern "C" int yc_tune_search(const yc_batch_cfg* start, int64_t total_px, int s
   if (best.pool_paths <= 0 || best.pool_paths > pool_cap) best.pool_paths = std::min(1 << 21, pool_cap);
   if (best.trace_block <= 0) best.trace_block = 128;
   if (best.stack_smem <= 0) best.stack_smem = 12;
+  if (best.trace_share <= 0) best.trace_share = 100;
+  if (best.groups <= 0) best.groups = 2;
   float best_ms = clock(&best, user);
   if (best_ms < 0.0f) return yc::set_error(YC_E_LAUNCH, "yc_tune_search: the clock failed");
   record(best, best_ms);
   for (int sw = 0; sw < sweeps; ++sw) {
     const yc_batch_cfg at_start = best;
     for (const Param& p : params) {
-      for (int32_t v : p.values) {
-        if (best.*p.field == v) continue;
-        if (p.field == &yc_batch_cfg::pool_paths && v > pool_cap) continue;
+      for (const std::vector<int32_t>& v : p.values) {
         yc_batch_cfg cand = best;
-        cand.*p.field = v;
+        for (size_t f = 0; f < p.fields.size(); ++f) cand.*p.fields[f] = v[f];
+        if (same(cand, best)) continue;
+        if (p.fields[0] == &yc_batch_cfg::pool_paths && v[0] > pool_cap) continue;
         bool seen = false;
         for (const auto& t : timed) seen = seen || same(t.first, cand);
         if (seen) continue;

@@ -89,7 +89,8 @@ class Server:
         cap = max(renderer.scene_depth(sid) for sid in self.sids) + 2
         if shape is not None:
             bc = N.BatchCfg(shape.pool_paths, shape.rounds_per_launch, shape.logic_blocks_per_sm, 1, 1 << 16, cap,
-                            shape.sort_threshold, shape.groups, shape.ray_sort, shape.trace_block, shape.stack_smem)
+                            shape.sort_threshold, shape.groups, shape.ray_sort, shape.trace_block, shape.stack_smem,
+                            shape.trace_share)
         else:
             bc = N.BatchCfg(pool_paths, rounds_per_launch, logic_blocks_per_sm, 1, 1 << 16, cap, sort_threshold, 0, 0)
         sc = N.ServeCfg(self.budget, -1 if max_queue is None else int(max_queue), int(bool(keep_results)), bc)
