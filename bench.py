@@ -368,12 +368,13 @@ def replay_sample(jobs, seeds, every=128):
 
 
 # DRAM bytes (read + write) per walked ray of k_batch_trace_mixed on the mixed workload
-# with the default tree (mode 1): one ncu capture (dram__bytes_read.sum +
-# dram__bytes_write.sum, one pass) of all 320 launches of two passes of the 64 jobs,
-# 85,848,500,224 + 11,191,529,216 bytes over 452,296,636 walked rays; the command and the
-# per-launch spread are in profiles/k_batch_trace_mixed_c2_dram_traffic.md. A launch's
-# traffic is this figure times the rays it walks.
-MIX_TRACE_DRAM_BYTES_PER_RAY = (85848500224 + 11191529216) / 452296636
+# with the default tree (mode 1) and the tuned shape (4 slot groups, traversal grid at
+# 50%, 128-thread blocks): one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum,
+# one pass) of all 576 launches of two passes of the 64 jobs, 85,934,615,808 +
+# 7,993,981,696 bytes over 452,296,636 walked rays; the command and the per-launch spread
+# are in profiles/k_batch_trace_mixed_c2_dram_traffic.md. A launch's traffic is this
+# figure times the rays it walks.
+MIX_TRACE_DRAM_BYTES_PER_RAY = (85934615808 + 7993981696) / 452296636
 
 
 def _trace_roofline(st, kt, l2, pk, pk_kind, kernel_mixed, kernel_extend, replay=None, dram_per_ray=None):
@@ -934,6 +935,21 @@ def run_mix(args, rank, local, ws, dist):
     st_bp = r.stats()
     r.set_profiling(False)
     bp.close()
+    # the same two passes with one slot group and the whole of each SM for the traversal:
+    # the kernel's speed when no other group's kernels share its SMs
+    alone = dict(shape.kwargs(), groups=1, trace_share=100)
+    kt_a = st_a = None
+    if (shape.groups, shape.trace_share) != (1, 100):
+        ba = Batch(r, stack_cap=cap, use_graph=False, max_jobs=len(jobs), **alone)
+        for s, sid, a, sd in zip(jobs, sids, scratch, seeds):
+            ba.add_job(sid, a, s.cam, sd[prof], cfg, reset_first=1)
+        r.synchronize()
+        r.reset_stats()
+        r.set_profiling(True)
+        ba.run()
+        kt_a, st_a = r.kernel_times(), r.stats()
+        r.set_profiling(False)
+        ba.close()
     r.reset_stats()
     r.set_profiling(True)
     for s, sid, a, sd in zip(jobs, sids, scratch, seeds):
@@ -1032,6 +1048,20 @@ def run_mix(args, rank, local, ws, dist):
                  "replay_s": replay_s},
         "stack_overflow": int(sum(x["overflow"] for x in reps)),
     }
+    if kt_a is not None:
+        # with several slot groups and a traversal grid below the whole SM, a traversal
+        # launch shares the SMs with the other groups' kernels (and traversals), so its
+        # event time -- the denominator of roofline.achieved -- counts that shared time
+        line["roofline"]["concurrency"] = (
+            "%d slot groups, traversal grid at %d%% of each SM's resident blocks: launches of the groups overlap, "
+            "so the launch times count time shared with other kernels; roofline_alone is the kernel with the SMs "
+            "to itself" % (shape.groups, shape.trace_share))
+        line["roofline_alone"] = _trace_roofline(st_a, kt_a, l2, pk, pk_kind,
+                                                 "k_batch_trace_mixed (closest + any-hit rays), one slot group, "
+                                                 "whole SM", "k_batch_trace<closest> (extend)", replay,
+                                                 dram_per_ray=MIX_TRACE_DRAM_BYTES_PER_RAY if args.tree == 1 else None)
+        line["kernel_ms_2_passes_alone"] = {"trace": kt_a["trace_ms"], "logic": kt_a["logic_ms"],
+                                            "sort": kt_a["sort_ms"], "raysort": kt_a["raysort_ms"]}
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_reference_mix([jobs[i] for i in idx], idx, [seeds[i] for i in idx],
                                                  args.cpu_seconds)
