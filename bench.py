@@ -103,7 +103,8 @@ def parse():
                     help="per-pass path: shade queues of at least this many paths are sorted (0: never)")
     ap.add_argument("--res", default="", help="c4: frame size WxH instead of 3840x2160 (profiling captures)")
     ap.add_argument("--stack-smem", type=int, default=0,
-                    help="walk-stack entries the per-pass traversal keeps in shared memory (0: all)")
+                    help="walk-stack entries the per-pass traversal keeps in shared memory (0: the default 12; "
+                         "64: the whole stack)")
     ap.add_argument("--tree", type=int, default=1,
                     help="interior hierarchy: 0 reference nodes, 1 binary SAH over the reference leaves, 2 four-wide")
     a = ap.parse_args()
@@ -661,6 +662,7 @@ def run_perpass_bdpt(args, rank, local, ws, dist):
     r = Renderer(local)
     r.set_tree_mode(args.tree)
     r.set_mixed_trace(args.mixed)
+    r.set_stack_smem(args.stack_smem)
     r.set_ray_sort(args.ray_sort // 10, args.ray_sort % 10, args.ray_sort_min)
     r.set_shade_sort(args.shade_sort_min)
     t0 = time.perf_counter()

@@ -469,10 +469,11 @@ enum {
   YC_OPT_STACK_LIMIT = 8,
   /* Walk-stack entries kept in shared memory by yc_render_pass(es)'s traversal (one launch
    * per round, YC_OPT_MIXED_TRACE); the deeper entries go to a spill area of the context in
-   * global memory. Fewer entries leave more of each SM's L1 to the node and triangle
-   * fetches and more blocks per SM. 0 (default) = the whole stack in shared memory.
-   * yc_render_pass_noalloc keeps the whole stack there (it allocates nothing). The batch
-   * engine has its own setting (yc_batch_cfg.stack_smem). */
+   * global memory (allocated by the first pass that needs it). Fewer entries leave more of
+   * each SM's L1 to the node and triangle fetches and more blocks per SM. 0 = 12 (the
+   * default); a value at or above the scene's stack depth keeps the whole stack in shared
+   * memory. yc_render_pass_noalloc keeps the whole stack there (it allocates nothing). The
+   * batch engine has its own setting (yc_batch_cfg.stack_smem). */
   YC_OPT_STACK_SMEM = 9,
   /* Where yc_upload_scene repacks a scene for YC_OPT_TREE 1: 1 (default) on the device
    * (the caller's triangle and node arrays are copied over and the SAH hierarchy above the

@@ -582,9 +582,9 @@ def test_render_edge_cases(renderer, case):
 
 @pytest.mark.parametrize("tree", [1, 2])
 def test_render_identical_with_a_split_walk_stack(renderer, tree):
-    """YC_OPT_STACK_SMEM: with only 2 or 12 walk-stack entries in shared memory (the rest in
-    the context's spill area) a pass gives the oracle's bits and the same ray counts as
-    with the whole stack in shared memory."""
+    """YC_OPT_STACK_SMEM: with only 2 or 12 (the default, 0) walk-stack entries in shared
+    memory (the rest in the context's spill area) a pass gives the oracle's bits and the
+    same ray counts as with the whole stack in shared memory (64)."""
     s = scenes.c1(40, 32, level=5)
     seeds = scenes.pass_seeds(37, 2)
     renderer.set_tree_mode(tree)
@@ -592,7 +592,7 @@ def test_render_identical_with_a_split_walk_stack(renderer, tree):
     renderer.set_tree_mode(1)
     renderer.set_camera(s.cam)
     out = []
-    for smem in (0, 2, 12):
+    for smem in (64, 2, 12, 0):
         renderer.set_stack_smem(smem)
         aid = renderer.alloc_accum(40, 32)
         renderer.reset_stats()

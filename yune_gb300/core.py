@@ -206,7 +206,8 @@ class Renderer:
 
     def set_stack_smem(self, n):
         """Walk-stack entries the per-pass traversal keeps in shared memory (YC_OPT_STACK_SMEM;
-        the deeper ones go to a spill area in global memory; 0 = the whole stack)."""
+        the deeper ones go to a spill area in global memory; 0 = 12, the default; 64 or any
+        value at or above the scene's stack depth = the whole stack)."""
         N.check(self.L.yc_set_option(self.h, 9, int(n)), "yc_set_option")
 
     def set_repack(self, on_device):

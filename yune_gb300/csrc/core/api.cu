@@ -144,7 +144,7 @@ struct yc_ctx {
   unsigned long long* overflow_host = nullptr;   // pinned: DevStats::call_overflow read back
   int max_rounds = 1000000;   // YC_OPT_MAX_ROUNDS: rounds one pass may take
   int stack_limit = 0;        // YC_OPT_STACK_LIMIT: traversal stack entries allowed (0 = any)
-  int stack_smem = 0;         // YC_OPT_STACK_SMEM: per-pass walk-stack entries in shared memory (0 = all)
+  int stack_smem = 12;        // YC_OPT_STACK_SMEM: per-pass walk-stack entries in shared memory
   int repack_device = 1;      // YC_OPT_REPACK: the upload's repack of tree mode 1 on the device
   DevBuf<int> pass_spill;     // the deeper entries of the per-pass walks (with stack_smem)
   int logic_grid = 0;
@@ -437,7 +437,7 @@ int run_pass(yc_ctx* c, Scene* sc, Accum* ac, uint32_t rand_seed, int reset, int
   const int grid_a = yc::trace_grid_blocks(true, dsc.depth, dsc.wide != 0);
   // the mixed trace's walk stacks: c->stack_smem entries in shared memory, the rest spilled
   const int cap = yc::trace_stack_cap(dsc.depth);
-  const int n_smem = (mixed && c->stack_smem > 0 && c->stack_smem < cap) ? c->stack_smem : 0;
+  const int n_smem = (mixed && c->stack_smem < cap) ? c->stack_smem : 0;   // 0: the whole stack
   const int grid_m = mixed ? yc::trace_mixed_grid_blocks(dsc.depth, dsc.wide != 0, n_smem) : 1;
   if (n_smem > 0 && grid_m > 0)
     if (int e = ensure_pass_spill(c, (size_t)grid_m * yc::TRACE_TB_PASS * 2 * (size_t)(cap - n_smem))) return e;
@@ -1155,7 +1155,7 @@ int yc_set_option(yc_ctx* c, int option, int value) {
       return YC_OK;
     case YC_OPT_STACK_SMEM:
       if (value < 0) return fail(YC_E_INVALID, "stack_smem must not be negative");
-      c->stack_smem = value;
+      c->stack_smem = value == 0 ? 12 : value;
       return YC_OK;
     case YC_OPT_REPACK:
       if (value != 0 && value != 1) return fail(YC_E_INVALID, "repack is 0 (host) or 1 (device)");

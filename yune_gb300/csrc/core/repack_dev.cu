@@ -425,31 +425,213 @@ __global__ void __launch_bounds__(LEVEL_TB) k_sah_level(SahItem* items, SahItem*
   }
 }
 
-// shared memory of a small-range block: the leaves, the partition buffer, the bins and the
-// stack of pending ranges (disjoint, of two leaves or more: at most SMALL_MAX / 2)
-constexpr size_t kSmallSmem = 2 * SMALL_MAX * sizeof(SahItem) + sizeof(SahBins) + (SMALL_MAX / 2) * sizeof(SahTask);
+// A range of at most 32 leaves, split by one warp with the leaves in its lanes. The split
+// is the binned sweep's without the bins: per axis the lanes are ranked by bin (stable),
+// the unions of the first r + 1 ranked leaves and of the rest come from warp scans, and a
+// cost is evaluated between neighbours of different bins only. Every bin q between two
+// occupied bins has the same two sides, hence the same cost, so the sweep's first minimum
+// in bin order is the first minimum in rank order, at the lower neighbour's bin; bins
+// before the first occupied one or from the last one on have an empty side.
+constexpr int TINY_MAX = 32;
 
-// the whole subtree of a range of at most SMALL_MAX leaves, a block per range
+__device__ __forceinline__ float shfl_f(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+// the tiny range [t.b, t.e) of `it` and its whole subtree, by one warp; stack: 16 entries
+__device__ void tiny_subtree(SahItem* it, const SahTask& root, SahTask* stack, float4* nodes, int* dmax, int* bad) {
+  const int lane = threadIdx.x & 31;
+  int top = 0;
+  SahTask t = root;
+  for (;;) {
+    const int b = t.b, e = t.e, n = e - b;
+    const bool on = lane < n;
+    float lo[3], hi[3], c[3];
+    int w = 0, link = 0;
+    {
+      const SahItem x = on ? it[b + lane] : SahItem{};
+      lo[0] = x.lo.x; lo[1] = x.lo.y; lo[2] = x.lo.z;
+      hi[0] = x.hi.x; hi[1] = x.hi.y; hi[2] = x.hi.z;
+      w = __float_as_int(x.lo.w);
+      link = __float_as_int(x.hi.w);
+    }
+    __syncwarp();
+    // bounds of the range (lanes past n contribute nothing)
+    float box[12];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      c[k] = sah_centroid(lo[k], hi[k]);
+      box[k] = on ? lo[k] : kInf;
+      box[3 + k] = on ? hi[k] : -kInf;
+      box[6 + k] = on ? c[k] : kInf;
+      box[9 + k] = on ? c[k] : -kInf;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+      for (int j = 0; j < 12; ++j) {
+        const float o = __shfl_xor_sync(0xffffffffu, box[j], off);
+        box[j] = ((j / 3) & 1) ? sah_max(box[j], o) : sah_min(box[j], o);
+      }
+    if (lane == 0) {
+      const float blo[3] = {box[0], box[1], box[2]}, bhi[3] = {box[3], box[4], box[5]};
+      put_child(nodes, t.up, blo, bhi, t.node);
+      float* o = reinterpret_cast<float*>(nodes + 4 * (size_t)t.node);
+      o[14] = 0.0f;
+      o[15] = 0.0f;
+      atomicMax(dmax, t.depth);
+    }
+    const int nb = sah_bins_for(n);
+    float best = kInf;
+    int axis = -1, at = -1, nleft = 0;
+    int q_of[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float clo = box[6 + k], ext = box[9 + k] - clo;
+      if (!(ext > 0.0f)) continue;   // uniform across the warp
+      const float scale = (float)nb / ext;
+      const int q = on ? sah_bin(c[k], clo, scale, nb) : 0x7fffffff;
+      q_of[k] = q;
+      // stable rank by bin, then the leaf of each rank
+      int rank = 0;
+      for (int jj = 0; jj < n; ++jj) {
+        const int qj = __shfl_sync(0xffffffffu, q, jj);
+        rank += (qj < q || (qj == q && jj < lane)) ? 1 : 0;
+      }
+      // the lane holding the leaf of rank `lane` (lanes < n hold distinct ranks 0..n-1)
+      int src = lane;
+      for (int r = 0; r < n; ++r) {
+        const unsigned m = __ballot_sync(0xffffffffu, on && rank == r);
+        if (lane == r) src = __ffs(m) - 1;
+      }
+      const int qs = __shfl_sync(0xffffffffu, q, src);
+      float slo[3], shi[3];
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc) {
+        slo[cc] = shfl_f(lo[cc], src);
+        shi[cc] = shfl_f(hi[cc], src);
+      }
+      const int sw = __shfl_sync(0xffffffffu, w, src);
+      Acc a;   // the leaf of rank `lane` (lanes past n: empty)
+      acc_empty(a);
+      if (on) {
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) {
+          a.lo[cc] = slo[cc];
+          a.hi[cc] = shi[cc];
+        }
+        a.cnt = 1;
+        a.w = sw;
+      }
+      Acc L = a, R = a;   // inclusive prefix and suffix unions in rank order
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const Acc u = acc_shfl_up(L, d);
+        if (lane >= d) acc_join(L, u);
+        const Acc v = acc_shfl_down(R, d);
+        if (lane + d < 32) acc_join(R, v);
+      }
+      const Acc R1 = acc_shfl_down(R, 1);          // the leaves ranked after this one
+      const int qn = __shfl_down_sync(0xffffffffu, qs, 1);
+      float cost = kInf;
+      if (lane < n - 1 && qs < qn)
+        cost = sah_area(L.lo[0], L.lo[1], L.lo[2], L.hi[0], L.hi[1], L.hi[2]) * (float)L.w +
+               sah_area(R1.lo[0], R1.lo[1], R1.lo[2], R1.hi[0], R1.hi[1], R1.hi[2]) * (float)R1.w;
+      float bc = cost < kInf ? cost : kInf;
+      int br = cost < kInf ? lane : 32;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const float oc = __shfl_xor_sync(0xffffffffu, bc, off);
+        const int orr = __shfl_xor_sync(0xffffffffu, br, off);
+        if (oc < bc || (oc == bc && orr < br)) {
+          bc = oc;
+          br = orr;
+        }
+      }
+      const int q_at = __shfl_sync(0xffffffffu, qs, br & 31);
+      if (br < 32 && bc < best) {   // the first axis with the smallest cost
+        best = bc;
+        axis = k;
+        at = q_at;
+        nleft = br + 1;
+      }
+    }
+    int mid;
+    if (axis >= 0) {
+      mid = b + nleft;
+      const int qa = axis == 0 ? q_of[0] : (axis == 1 ? q_of[1] : q_of[2]);
+      const bool left = on && qa <= at;
+      const unsigned m = __ballot_sync(0xffffffffu, left);
+      if (__popc(m) != nleft && lane == 0) *bad = 1;
+      const int before = __popc(m & ((1u << lane) - 1u));
+      if (on) {
+        const int to = left ? b + before : mid + (lane - before);
+        if (to >= b && to < e) {
+          it[to].lo = make_float4(lo[0], lo[1], lo[2], __int_as_float(w));
+          it[to].hi = make_float4(hi[0], hi[1], hi[2], __int_as_float(link));
+        }
+      }
+    } else {
+      mid = (b + e) / 2;   // coincident centroids: split the list in half
+    }
+    __syncwarp();
+    if (lane == 0) {
+      const SahTask kids[2] = {{b, mid, t.node + 1, 2 * t.node, t.depth + 1},
+                               {mid, e, t.node + (mid - b), 2 * t.node + 1, t.depth + 1}};
+      for (const SahTask& kd : kids) {
+        if (kd.e - kd.b == 1) {
+          put_leaf(nodes, kd.up, it[kd.b]);
+          atomicMax(dmax, kd.depth);
+        } else if (top < TINY_MAX / 2) {
+          stack[top++] = kd;
+        } else {
+          *bad = 1;
+        }
+      }
+    }
+    top = __shfl_sync(0xffffffffu, top, 0);
+    __syncwarp();
+    if (top == 0) break;
+    --top;
+    t = stack[top];
+    __syncwarp();
+  }
+}
+
+// shared memory of a small-range block: the leaves, the partition buffer, the bins, the
+// pending ranges (a stack from the bottom, the ranges of at most TINY_MAX leaves from the
+// top: disjoint, of two leaves or more, so at most SMALL_MAX / 2 together) and a 16-entry
+// stack per warp for the tiny subtrees
+constexpr int SMALL_WARPS = SMALL_TB / 32;
+constexpr int PEND_MAX = SMALL_MAX / 2;
+constexpr size_t kSmallSmem = 2 * SMALL_MAX * sizeof(SahItem) + sizeof(SahBins) + PEND_MAX * sizeof(SahTask) +
+                              SMALL_WARPS * (TINY_MAX / 2) * sizeof(SahTask);
+
+// the whole subtree of a range of at most SMALL_MAX leaves, a block per range: the ranges
+// above TINY_MAX leaves split by the whole block, then the tiny ones by one warp each
 __global__ void __launch_bounds__(SMALL_TB) k_sah_small(const SahItem* items, const SahTask* small, SahCtl* ctl,
                                                         float4* nodes) {
   extern __shared__ __align__(16) unsigned char smem[];
   SahItem* it = reinterpret_cast<SahItem*>(smem);
   SahItem* tmp = it + SMALL_MAX;
   SahBins& bn = *reinterpret_cast<SahBins*>(tmp + SMALL_MAX);
-  SahTask* stack = reinterpret_cast<SahTask*>(&bn + 1);
+  SahTask* pend = reinterpret_cast<SahTask*>(&bn + 1);
+  SahTask* wstack = pend + PEND_MAX;
   __shared__ SahScratch sc;
-  __shared__ int top, dmax;
+  __shared__ int top, ntiny, tiny_next, dmax;
   const SahTask r = small[blockIdx.x];
   const int n = r.e - r.b;
   for (int i = threadIdx.x; i < n; i += blockDim.x) it[i] = items[r.b + i];
   if (threadIdx.x == 0) {
-    stack[0] = SahTask{0, n, r.node, r.up, r.depth};
-    top = 1;
+    const SahTask t0{0, n, r.node, r.up, r.depth};
+    top = 0;
+    ntiny = 0;
+    tiny_next = 0;
     dmax = 0;
+    if (n <= TINY_MAX) pend[PEND_MAX - 1 - ntiny++] = t0;
+    else pend[top++] = t0;
   }
   __syncthreads();
   while (top > 0) {
-    const SahTask t = stack[top - 1];
+    const SahTask t = pend[top - 1];
     __syncthreads();
     if (threadIdx.x == 0) --top;
     split_task(it, tmp, t.b, t.e, t, bn, sc, nodes, &dmax, &ctl->bad);
@@ -461,15 +643,27 @@ __global__ void __launch_bounds__(SMALL_TB) k_sah_small(const SahItem* items, co
         if (c.e - c.b == 1) {
           put_leaf(nodes, c.up, it[c.b]);
           dmax = max(dmax, c.depth);
-        } else if (top < SMALL_MAX / 2) {
-          stack[top++] = c;
-        } else {
+        } else if (top + ntiny >= PEND_MAX) {
           ctl->bad = 1;
+        } else if (c.e - c.b <= TINY_MAX) {
+          pend[PEND_MAX - 1 - ntiny++] = c;
+        } else {
+          pend[top++] = c;
         }
       }
     }
     __syncthreads();
   }
+  // the tiny ranges, one warp each
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (;;) {
+    int k = 0;
+    if (lane == 0) k = atomicAdd(&tiny_next, 1);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= ntiny) break;
+    tiny_subtree(it, pend[PEND_MAX - 1 - k], wstack + warp * (TINY_MAX / 2), nodes, &dmax, &ctl->bad);
+  }
+  __syncthreads();
   if (threadIdx.x == 0) atomicMax(&ctl->depth, dmax);
 }
 
