@@ -21,7 +21,33 @@ def r():
         yield rr
 
 
+def _no_bvh():
+    s = scenes.c0(16, 16)
+    s.nodes = s.nodes[:0]
+    return s
+
+
+def _no_triangles():
+    s = scenes.c0(16, 16)
+    s.tris, s.nodes = s.tris[:0], s.nodes[:0]
+    return s
+
+
+def _one_reachable_leaf():
+    # an interior root whose second child the reference never queues (vert_len 0, no children)
+    s = leafgen.leaf_scene(2, "random", 8)
+    s.nodes["vert_len"][2] = 0
+    s.nodes["child_idx"][2] = -2
+    return s
+
+
 CASES = {
+    # scenes the upload repacks on the host whatever the option (no BVH, no triangles, a
+    # leaf at the root, fewer than two reachable leaves)
+    "no_bvh": _no_bvh,
+    "no_triangles": _no_triangles,
+    "root_leaf": lambda: leafgen.leaf_scene(1, "random", 9),
+    "one_reachable_leaf": _one_reachable_leaf,
     "c0": lambda: scenes.c0(16, 16),
     "c1_l5": lambda: scenes.c1(16, 16, level=5),
     "c1_l7": lambda: scenes.c1(16, 16, level=7),
