@@ -692,6 +692,199 @@ __global__ void __launch_bounds__(ITEM_TB) k_leaf_items(const yc_bvh_node* __res
   }
 }
 
+// ---- ranges of more than BIG_MIN leaves (the top of the tree): each pass over a range's
+// leaves is spread over blocks of CHUNK leaves; the bounds and bins of the chunks are merged
+// with the order-independent atomics of yc_sah.h, one block per range chooses the split
+// from the merged bins, and the stable partition is a count per chunk, the chunks'
+// offsets (an exclusive scan over the range's chunks in order, on the host) and a scatter
+// per chunk ----
+constexpr int BIG_MIN = 1 << 16;
+constexpr int CHUNK = 8192;
+constexpr int BIG_TB = 512;
+
+struct BigChunk {
+  int task, b, e;
+};
+struct BigSplit {
+  int axis, at, mid, pad;
+};
+// a range's lo[3], hi[3], centroid lo[3], centroid hi[3], merged over its chunks
+struct BigStat {
+  float box[12];
+};
+
+__global__ void __launch_bounds__(256) k_big_init(BigStat* st, SahBins* gb) {
+  const int t = blockIdx.x;
+  if (threadIdx.x < 12) st[t].box[threadIdx.x] = ((threadIdx.x / 3) & 1) ? -kInf : kInf;
+  SahBins& g = gb[t];
+  for (int x = threadIdx.x; x < 3 * SAH_NB; x += blockDim.x) {
+    const int k = x / SAH_NB, q = x - k * SAH_NB;
+    g.cnt[k][q] = 0;
+    g.w[k][q] = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      g.lo[k][c][q] = kInf;
+      g.hi[k][c][q] = -kInf;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(BIG_TB) k_big_bounds(const SahItem* items, const BigChunk* ch, BigStat* st) {
+  __shared__ SahScratch sc;
+  const BigChunk c = ch[blockIdx.x];
+  range_bounds(items, c.b, c.e, sc);
+  if (threadIdx.x < 12) {
+    float* a = &st[c.task].box[threadIdx.x];
+    if ((threadIdx.x / 3) & 1) sah_atomic_max(a, sc.box[threadIdx.x]);
+    else sah_atomic_min(a, sc.box[threadIdx.x]);
+  }
+}
+
+__global__ void __launch_bounds__(BIG_TB) k_big_bins(const SahItem* items, const BigChunk* ch, const SahTask* tasks,
+                                                     const BigStat* st, SahBins* gb) {
+  __shared__ SahBins bn;
+  __shared__ SahScratch sc;
+  const BigChunk c = ch[blockIdx.x];
+  if (threadIdx.x < 12) sc.box[threadIdx.x] = st[c.task].box[threadIdx.x];
+  __syncthreads();
+  const SahTask t = tasks[c.task];
+  const int nb = sah_bins_for(t.e - t.b);
+  range_bins(items, c.b, c.e, nb, bn, sc);
+  SahBins& g = gb[c.task];
+  for (int x = threadIdx.x; x < 3 * nb; x += blockDim.x) {
+    const int k = x / nb, q = x - k * nb;
+    if (bn.cnt[k][q] == 0) continue;
+    atomicAdd(&g.cnt[k][q], bn.cnt[k][q]);
+    atomicAdd(&g.w[k][q], bn.w[k][q]);
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) {
+      sah_atomic_min(&g.lo[k][cc][q], bn.lo[k][cc][q]);
+      sah_atomic_max(&g.hi[k][cc][q], bn.hi[k][cc][q]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(BIG_TB) k_big_split(const SahTask* tasks, const BigStat* st, const SahBins* gb,
+                                                      BigSplit* out, float4* nodes, int* depth) {
+  __shared__ SahBins bn;
+  __shared__ SahScratch sc;
+  const SahTask t = tasks[blockIdx.x];
+  if (threadIdx.x < 12) sc.box[threadIdx.x] = st[blockIdx.x].box[threadIdx.x];
+  const int nb = sah_bins_for(t.e - t.b);
+  const SahBins& g = gb[blockIdx.x];
+  for (int x = threadIdx.x; x < 3 * nb; x += blockDim.x) {
+    const int k = x / nb, q = x - k * nb;
+    bn.cnt[k][q] = g.cnt[k][q];
+    bn.w[k][q] = g.w[k][q];
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) {
+      bn.lo[k][cc][q] = g.lo[k][cc][q];
+      bn.hi[k][cc][q] = g.hi[k][cc][q];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const float lo[3] = {sc.box[0], sc.box[1], sc.box[2]}, hi[3] = {sc.box[3], sc.box[4], sc.box[5]};
+    put_child(nodes, t.up, lo, hi, t.node);
+    float* o = reinterpret_cast<float*>(nodes + 4 * (size_t)t.node);
+    o[14] = 0.0f;
+    o[15] = 0.0f;
+    atomicMax(depth, t.depth);
+  }
+  range_split(t.b, t.e, nb, bn, sc);
+  if (threadIdx.x == 0) out[blockIdx.x] = BigSplit{sc.axis, sc.at, sc.mid, 0};
+}
+
+// the chosen split's bin scale of range t on axis k, as range_bins and range_partition form it
+__device__ __forceinline__ float big_scale(const BigStat& s, int k, int nb) {
+  return (float)nb / (s.box[9 + k] - s.box[6 + k]);
+}
+
+__global__ void __launch_bounds__(BIG_TB) k_big_count(const SahItem* items, const BigChunk* ch, const SahTask* tasks,
+                                                      const BigStat* st, const BigSplit* sp, int* left) {
+  __shared__ int wsum[BIG_TB / 32];
+  const BigChunk c = ch[blockIdx.x];
+  const BigSplit s = sp[c.task];
+  if (s.axis < 0) {
+    if (threadIdx.x == 0) left[blockIdx.x] = 0;
+    return;
+  }
+  const int k = s.axis;
+  const SahTask t = tasks[c.task];
+  const int nb = sah_bins_for(t.e - t.b);
+  const float clo = st[c.task].box[6 + k], scale = big_scale(st[c.task], k, nb);
+  int cnt = 0;
+  for (int i = c.b + threadIdx.x; i < c.e; i += blockDim.x) {
+    const SahItem x = items[i];
+    cnt += sah_bin(sah_centroid(comp(x.lo, k), comp(x.hi, k)), clo, scale, nb) <= s.at ? 1 : 0;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int total = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) total += wsum[w];
+    left[blockIdx.x] = total;
+  }
+}
+
+__global__ void __launch_bounds__(BIG_TB) k_big_scatter(const SahItem* items, SahItem* tmp, const BigChunk* ch,
+                                                        const SahTask* tasks, const BigStat* st, const BigSplit* sp,
+                                                        const int* loff, const int* roff, int* bad) {
+  __shared__ int wcount[BIG_TB / 32];
+  const BigChunk c = ch[blockIdx.x];
+  const BigSplit s = sp[c.task];
+  if (s.axis < 0) return;
+  const int k = s.axis;
+  const SahTask t = tasks[c.task];
+  const int nb = sah_bins_for(t.e - t.b);
+  const float clo = st[c.task].box[6 + k], scale = big_scale(st[c.task], k, nb);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int run_l = t.b + loff[blockIdx.x], run_r = s.mid + roff[blockIdx.x];
+  for (int base = c.b; base < c.e; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const bool in = i < c.e;
+    SahItem x;
+    bool left = false;
+    if (in) {
+      x = items[i];
+      left = sah_bin(sah_centroid(comp(x.lo, k), comp(x.hi, k)), clo, scale, nb) <= s.at;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, left);
+    const int rank = __popc(m & ((1u << lane) - 1u));
+    if (lane == 0) wcount[warp] = __popc(m);
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int w = 0; w < nw; ++w) {
+      const int cw = wcount[w];
+      before += w < warp ? cw : 0;
+      total += cw;
+    }
+    if (in) {
+      const int at = left ? run_l + before + rank : run_r + (int)threadIdx.x - before - rank;
+      if (left ? (at >= t.b && at < s.mid) : (at >= s.mid && at < t.e)) tmp[at] = x;
+      else *bad = 1;
+    }
+    run_l += total;
+    run_r += min((int)blockDim.x, c.e - base) - total;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(BIG_TB) k_big_copy(SahItem* items, const SahItem* tmp, const BigChunk* ch,
+                                                     const BigSplit* sp) {
+  const BigChunk c = ch[blockIdx.x];
+  if (sp[c.task].axis < 0) return;
+  for (int i = c.b + threadIdx.x; i < c.e; i += blockDim.x) items[i] = tmp[i];
+}
+
+// leaf children of the big ranges: (parent * 2 + side, leaf item)
+__global__ void __launch_bounds__(256) k_put_leaves(const SahItem* items, const int2* leaves, int n, float4* nodes) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) put_leaf(nodes, leaves[j].x, items[leaves[j].y]);
+}
+
 // a device temporary, freed on scope exit
 template <class T>
 struct Tmp {
@@ -757,16 +950,135 @@ int repack_device(const yc_triangle* tris_host, int n_tri, const yc_bvh_node* no
   YC_REPACK_CUDA(cudaPeekAtLastError(), "leaf items");
   const SahTask root{0, n_leaf, 0, -1, 0};
   SahCtl h_ctl{0, 0, 0, 0};
-  int n_large = 0;
-  if (n_leaf > SMALL_MAX) {
-    YC_REPACK_CUDA(cudaMemcpyAsync(d_ta.p, &root, sizeof(root), cudaMemcpyHostToDevice, s), "copy");
-    n_large = 1;
-  } else {
-    YC_REPACK_CUDA(cudaMemcpyAsync(d_small.p, &root, sizeof(root), cudaMemcpyHostToDevice, s), "copy");
-    h_ctl.n_small = 1;
-  }
   YC_REPACK_CUDA(cudaMemcpyAsync(d_ctl.p, &h_ctl, sizeof(h_ctl), cudaMemcpyHostToDevice, s), "copy");
-  YC_REPACK_CUDA(cudaStreamSynchronize(s), "upload");   // h_ctl and root are read by the copies above
+  // the ranges above BIG_MIN leaves, level by level, many blocks per range; their children
+  // of more than SMALL_MAX leaves start the block-per-range levels, the smaller ones the
+  // shared-memory subtrees, the single leaves a leaf record each
+  std::vector<SahTask> big, lvl, sml;
+  std::vector<int2> leaves;
+  int host_depth = 0;
+  if (n_leaf > BIG_MIN) big.push_back(root);
+  else if (n_leaf > SMALL_MAX) lvl.push_back(root);
+  else sml.push_back(root);
+  if (!big.empty()) {
+    const size_t cap_big = (size_t)n_leaf / (BIG_MIN + 1) + 1;
+    const size_t cap_chunks = (size_t)n_leaf / CHUNK + 2 * cap_big + 1;
+    Tmp<SahTask> d_big;
+    Tmp<BigStat> d_stat;
+    Tmp<SahBins> d_gbins;
+    Tmp<BigSplit> d_split;
+    Tmp<BigChunk> d_chunks;
+    Tmp<int> d_left, d_loff, d_roff;
+    YC_REPACK_CUDA(d_big.alloc(cap_big), "allocation");
+    YC_REPACK_CUDA(d_stat.alloc(cap_big), "allocation");
+    YC_REPACK_CUDA(d_gbins.alloc(cap_big), "allocation");
+    YC_REPACK_CUDA(d_split.alloc(cap_big), "allocation");
+    YC_REPACK_CUDA(d_chunks.alloc(cap_chunks), "allocation");
+    YC_REPACK_CUDA(d_left.alloc(cap_chunks), "allocation");
+    YC_REPACK_CUDA(d_loff.alloc(cap_chunks), "allocation");
+    YC_REPACK_CUDA(d_roff.alloc(cap_chunks), "allocation");
+    std::vector<BigChunk> chunks;
+    std::vector<BigSplit> splits;
+    std::vector<int> left, loff, roff;
+    while (!big.empty()) {
+      const int nt = (int)big.size();
+      chunks.clear();
+      for (int ti = 0; ti < nt; ++ti)
+        for (int b = big[ti].b; b < big[ti].e; b += CHUNK) chunks.push_back(BigChunk{ti, b, std::min(b + CHUNK, big[ti].e)});
+      const int nc = (int)chunks.size();
+      if ((size_t)nt > cap_big || (size_t)nc > cap_chunks) {
+        err = "device repack: too many top-level ranges";
+        return -1;
+      }
+      YC_REPACK_CUDA(cudaMemcpyAsync(d_big.p, big.data(), nt * sizeof(SahTask), cudaMemcpyHostToDevice, s), "copy");
+      YC_REPACK_CUDA(cudaMemcpyAsync(d_chunks.p, chunks.data(), nc * sizeof(BigChunk), cudaMemcpyHostToDevice, s),
+                     "copy");
+      k_big_init<<<nt, 256, 0, s>>>(d_stat.p, d_gbins.p);
+      k_big_bounds<<<nc, BIG_TB, 0, s>>>(d_items.p, d_chunks.p, d_stat.p);
+      k_big_bins<<<nc, BIG_TB, 0, s>>>(d_items.p, d_chunks.p, d_big.p, d_stat.p, d_gbins.p);
+      k_big_split<<<nt, BIG_TB, 0, s>>>(d_big.p, d_stat.p, d_gbins.p, d_split.p, nodes, &d_ctl.p->depth);
+      k_big_count<<<nc, BIG_TB, 0, s>>>(d_items.p, d_chunks.p, d_big.p, d_stat.p, d_split.p, d_left.p);
+      YC_REPACK_CUDA(cudaPeekAtLastError(), "top-level split");
+      splits.resize(nt);
+      left.resize(nc);
+      YC_REPACK_CUDA(cudaMemcpyAsync(splits.data(), d_split.p, nt * sizeof(BigSplit), cudaMemcpyDeviceToHost, s),
+                     "copy");
+      YC_REPACK_CUDA(cudaMemcpyAsync(left.data(), d_left.p, nc * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+      YC_REPACK_CUDA(cudaStreamSynchronize(s), "top-level split");
+      // each chunk's place on its range's two sides: the chunks before it in order
+      loff.resize(nc);
+      roff.resize(nc);
+      std::vector<int> run_l(nt, 0), run_r(nt, 0);
+      for (int ci = 0; ci < nc; ++ci) {
+        const int ti = chunks[ci].task;
+        loff[ci] = run_l[ti];
+        roff[ci] = run_r[ti];
+        run_l[ti] += left[ci];
+        run_r[ti] += (chunks[ci].e - chunks[ci].b) - left[ci];
+      }
+      for (int ti = 0; ti < nt; ++ti)
+        if (splits[ti].axis >= 0 && big[ti].b + run_l[ti] != splits[ti].mid) {
+          err = "device repack: the bins and the partition of a top-level range disagree";
+          return -1;
+        }
+      YC_REPACK_CUDA(cudaMemcpyAsync(d_loff.p, loff.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s), "copy");
+      YC_REPACK_CUDA(cudaMemcpyAsync(d_roff.p, roff.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s), "copy");
+      k_big_scatter<<<nc, BIG_TB, 0, s>>>(d_items.p, d_tmp.p, d_chunks.p, d_big.p, d_stat.p, d_split.p, d_loff.p,
+                                          d_roff.p, &d_ctl.p->bad);
+      k_big_copy<<<nc, BIG_TB, 0, s>>>(d_items.p, d_tmp.p, d_chunks.p, d_split.p);
+      YC_REPACK_CUDA(cudaPeekAtLastError(), "top-level partition");
+      std::vector<SahTask> next;
+      for (int ti = 0; ti < nt; ++ti) {
+        const SahTask& t = big[ti];
+        const int mid = splits[ti].mid;
+        const SahTask kids[2] = {{t.b, mid, t.node + 1, 2 * t.node, t.depth + 1},
+                                 {mid, t.e, t.node + (mid - t.b), 2 * t.node + 1, t.depth + 1}};
+        for (const SahTask& c : kids) {
+          const int n = c.e - c.b;
+          if (n == 1) {
+            leaves.push_back(make_int2(c.up, c.b));
+            host_depth = std::max(host_depth, c.depth);
+          } else if (n > BIG_MIN) {
+            next.push_back(c);
+          } else if (n > SMALL_MAX) {
+            lvl.push_back(c);
+          } else {
+            sml.push_back(c);
+          }
+        }
+      }
+      big.swap(next);
+      YC_REPACK_CUDA(cudaStreamSynchronize(s), "top-level partition");   // the host vectors above are reused
+    }
+    if (!leaves.empty()) {
+      Tmp<int2> d_leaves;
+      YC_REPACK_CUDA(d_leaves.alloc(leaves.size()), "allocation");
+      YC_REPACK_CUDA(cudaMemcpyAsync(d_leaves.p, leaves.data(), leaves.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                     s),
+                     "copy");
+      k_put_leaves<<<((int)leaves.size() + 255) / 256, 256, 0, s>>>(d_items.p, d_leaves.p, (int)leaves.size(), nodes);
+      YC_REPACK_CUDA(cudaPeekAtLastError(), "leaf records");
+      YC_REPACK_CUDA(cudaStreamSynchronize(s), "leaf records");
+    }
+  }
+  if (lvl.size() > cap_large || sml.size() > cap_small) {
+    err = "device repack: a split left its bounds";
+    return -1;
+  }
+  int n_large = (int)lvl.size();
+  YC_REPACK_CUDA(cudaMemcpyAsync(&h_ctl, d_ctl.p, sizeof(h_ctl), cudaMemcpyDeviceToHost, s), "copy");
+  YC_REPACK_CUDA(cudaStreamSynchronize(s), "upload");
+  h_ctl.n_next = 0;
+  h_ctl.n_small = (int)sml.size();
+  h_ctl.depth = std::max(h_ctl.depth, host_depth);
+  if (n_large)
+    YC_REPACK_CUDA(cudaMemcpyAsync(d_ta.p, lvl.data(), lvl.size() * sizeof(SahTask), cudaMemcpyHostToDevice, s),
+                   "copy");
+  if (!sml.empty())
+    YC_REPACK_CUDA(cudaMemcpyAsync(d_small.p, sml.data(), sml.size() * sizeof(SahTask), cudaMemcpyHostToDevice, s),
+                   "copy");
+  YC_REPACK_CUDA(cudaMemcpyAsync(d_ctl.p, &h_ctl, sizeof(h_ctl), cudaMemcpyHostToDevice, s), "copy");
+  YC_REPACK_CUDA(cudaStreamSynchronize(s), "upload");   // h_ctl and the lists are read by the copies above
   while (n_large > 0) {
     k_sah_level<<<n_large, LEVEL_TB, 0, s>>>(d_items.p, d_tmp.p, d_ta.p, d_tb.p, (int)cap_large, d_small.p,
                                              (int)cap_small, d_ctl.p, nodes);
