@@ -118,3 +118,21 @@ def test_sah_over_leaves_independent_of_host_threads(kind, n):
     assert got[0][2] == 64 * (n - 1)
     if kind == "coincident":   # halving: a balanced tree
         assert got[0][1] == int(np.ceil(np.log2(n))) + 1
+
+
+def test_first_bad_material_is_named(big):
+    """The material check runs on the host's threads and still names the first triangle
+    whose matID is out of range, whatever the thread count."""
+    s, nodes = big
+    t = s.tris.copy()
+    t["matID"][200_000] = len(s.mats)
+    t["matID"][70_001] = -1
+    L = N.lib()
+    try:
+        for th in (1, 3, 0):
+            assert L.yh_set_host_threads(th) == 0
+            out = N.SceneLayout()
+            assert L.yc_scene_layout(ptr(t), len(t), len(s.mats), ptr(nodes), len(nodes), 1, C.byref(out)) == -1
+            assert b"triangle 70001 " in L.yc_last_error()
+    finally:
+        L.yh_set_host_threads(0)

@@ -617,9 +617,10 @@ int yc_upload_scene(yc_ctx* c, const yc_triangle* tris, int n_tri, const yc_mate
   if ((n_tri > 0 && !tris) || (n_mat > 0 && !mats) || (n_node > 0 && !nodes))
     return fail(YC_E_INVALID, "NULL array with non-zero count");
   if (n_light < 1 || n_light > yc::MAX_LIGHTS || !lights) return fail(YC_E_INVALID, "need 1..16 lights");
-  for (int i = 0; i < n_tri; ++i)
-    if (tris[i].matID < 0 || tris[i].matID >= n_mat)
-      return fail(YC_E_INVALID, "triangle " + std::to_string(i) + " has matID out of range");
+  {
+    std::string err;
+    if (yc::check_materials(tris, n_tri, n_mat, err)) return fail(YC_E_INVALID, err);
+  }
   yc::Repacked rp;
   yc::DevRepackPlan plan;
   std::string err;
@@ -704,9 +705,10 @@ int yc_scene_layout(const yc_triangle* tris, int n_tri, int n_mat, const yc_bvh_
   if ((n_tri > 0 && !tris) || (n_node > 0 && !nodes)) return fail(YC_E_INVALID, "NULL array with non-zero count");
   if (tree_mode != yc::TREE_REFERENCE && tree_mode != yc::TREE_SAH_OVER_LEAVES && tree_mode != yc::TREE_WIDE4)
     return fail(YC_E_INVALID, "bad tree mode");
-  for (int i = 0; i < n_tri; ++i)
-    if (tris[i].matID < 0 || tris[i].matID >= n_mat)
-      return fail(YC_E_INVALID, "triangle " + std::to_string(i) + " has matID out of range");
+  {
+    std::string err;
+    if (yc::check_materials(tris, n_tri, n_mat, err)) return fail(YC_E_INVALID, err);
+  }
   yc::Repacked rp;
   std::string err;
   if (yc::repack_scene(tris, n_tri, nodes, n_node, tree_mode, rp, err)) return fail(YC_E_INVALID, err);
@@ -841,9 +843,10 @@ int yc_refit_scene(yc_ctx* c, int scene_id, const yc_triangle* tris, int n_tri) 
   Scene* s = find_scene(c, scene_id);
   if (!s) return fail(YC_E_NOTFOUND, "unknown scene");
   if (n_tri != s->dev.n_tri) return fail(YC_E_INVALID, "a refit keeps the scene's triangles: counts differ");
-  for (int i = 0; i < n_tri; ++i)
-    if (tris[i].matID < 0 || tris[i].matID >= s->dev.n_mat)
-      return fail(YC_E_INVALID, "triangle " + std::to_string(i) + " has matID out of range");
+  {
+    std::string err;
+    if (yc::check_materials(tris, n_tri, s->dev.n_mat, err)) return fail(YC_E_INVALID, err);
+  }
   YC_CUDA(cudaSetDevice(c->device));
   if (!s->refit_ready)
     if (int r = make_refit_plan(c, s)) return r;

@@ -492,6 +492,19 @@ void reachable_leaves(const yc_bvh_node* nodes, int n_node, std::vector<int>& le
 
 }  // namespace
 
+int check_materials(const yc_triangle* tris, int n_tri, int n_mat, std::string& err) {
+  std::atomic<int> first_bad{n_tri};
+  parallel_for((size_t)n_tri, [&](size_t i) {
+    if (tris[i].matID < 0 || tris[i].matID >= n_mat)
+      for (int m = first_bad.load(); (int)i < m && !first_bad.compare_exchange_weak(m, (int)i);) {}
+  });
+  if (first_bad.load() < n_tri) {
+    err = "triangle " + std::to_string(first_bad.load()) + " has matID out of range";
+    return -1;
+  }
+  return 0;
+}
+
 int plan_device_repack(const yc_bvh_node* nodes, int n_node, int n_tri, DevRepackPlan& plan, std::string& err) {
   plan = DevRepackPlan();
   if (n_tri == 0 || n_node == 0) return 0;

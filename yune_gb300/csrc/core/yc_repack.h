@@ -44,6 +44,10 @@ enum { TREE_REFERENCE = 0, TREE_SAH_OVER_LEAVES = 1, TREE_WIDE4 = 2 };
 int repack_scene(const yc_triangle* tris, int n_tri, const yc_bvh_node* nodes, int n_node, int tree_mode,
                  Repacked& out, std::string& err);
 
+// -1 with err naming the first triangle whose matID is outside [0, n_mat) (checked on the
+// host's threads), else 0
+int check_materials(const yc_triangle* tris, int n_tri, int n_mat, std::string& err);
+
 // The host half of the device repack of TREE_SAH_OVER_LEAVES (repack_dev.cu): the node
 // array's checks (those of repack_scene) and the reachable leaves with their first
 // stream slots. Returns 1 when the scene takes the device repack (two reachable leaves or
