@@ -483,10 +483,30 @@ __device__ void tiny_subtree(SahItem* it, const SahTask& root, SahTask* stack, f
     float best = kInf;
     int axis = -1, at = -1, nleft = 0;
     int q_of[3] = {0, 0, 0};
+    if (n == 2) {
+      // two leaves: on every axis where their centroids differ the one split puts the lower
+      // centroid's leaf (bin 0) left and the other (the last bin) right, at the same cost
+      // area(A) wA + area(B) wB (a sum of two terms: the same bits in either order), so the
+      // first such axis wins if that cost is finite
+      const float ai = sah_area(lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]) * (float)w;
+      const float cost = __shfl_sync(0xffffffffu, ai, 0) + __shfl_sync(0xffffffffu, ai, 1);
+      for (int k = 0; k < 3 && axis < 0; ++k)
+        if (box[9 + k] - box[6 + k] > 0.0f && cost < kInf) axis = k;
+      if (axis >= 0) {
+        const float ck = axis == 0 ? c[0] : (axis == 1 ? c[1] : c[2]);
+        const float clo = axis == 0 ? box[6] : (axis == 1 ? box[7] : box[8]);
+        const int qv = ck == clo ? 0 : nb - 1;
+        q_of[0] = axis == 0 ? qv : 0;
+        q_of[1] = axis == 1 ? qv : 0;
+        q_of[2] = axis == 2 ? qv : 0;
+        at = 0;
+        nleft = 1;
+      }
+    }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const float clo = box[6 + k], ext = box[9 + k] - clo;
-      if (!(ext > 0.0f)) continue;   // uniform across the warp
+      if (n == 2 || !(ext > 0.0f)) continue;   // uniform across the warp
       const float scale = (float)nb / ext;
       const int q = on ? sah_bin(c[k], clo, scale, nb) : 0x7fffffff;
       q_of[k] = q;
