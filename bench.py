@@ -371,10 +371,9 @@ def replay_sample(jobs, seeds, every=128):
 # DRAM bytes (read + write) per walked ray of k_batch_trace_mixed on the mixed workload
 # with the default tree (mode 1) and the tuned shape (4 slot groups, traversal grid at
 # 50%, 128-thread blocks): one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum,
-# one pass) of all 576 launches of two passes of the 64 jobs, 85,934,615,808 +
-# 7,993,981,696 bytes over 452,296,636 walked rays; the command and the per-launch spread
-# are in profiles/k_batch_trace_mixed_c2_dram_traffic.md. A launch's traffic is this
-# figure times the rays it walks.
+# one pass) of all 576 launches of two passes of the 64 jobs (`bench.py --traffic-only`
+# with that shape under ncu), 85,934,615,808 + 7,993,981,696 bytes over 452,296,636
+# walked rays. A launch's traffic is this figure times the rays it walks.
 MIX_TRACE_DRAM_BYTES_PER_RAY = (85934615808 + 7993981696) / 452296636
 
 
