@@ -377,6 +377,20 @@ def replay_sample(jobs, seeds, every=128):
 MIX_TRACE_DRAM_BYTES_PER_RAY = (85934615808 + 7993981696) / 452296636
 
 
+def host_frames(sizes):
+    """Page-locked (h, w, 4) float32 host buffers for the tonemapped frames the e2e steps
+    read back, allocated before the timed region and reused step after step (plain numpy
+    arrays where page-locked memory cannot be had)."""
+    out = []
+    for (w, h) in sizes:
+        try:
+            import torch
+            out.append(torch.empty((h, w, 4), dtype=torch.float32, pin_memory=True).numpy())
+        except Exception:
+            out.append(np.empty((h, w, 4), np.float32))
+    return out
+
+
 def _trace_roofline(st, kt, l2, pk, pk_kind, kernel_mixed, kernel_extend, replay=None, dram_per_ray=None):
     """Roofline of the traversal kernel over its event time. achieved: the algorithmic
     bytes of the rays it walked -- 32 B per child box and 48 B per triangle a lone walk of
@@ -531,14 +545,14 @@ def run_ours(args, rank, local, ws, dist):
 
     # D. e2e with host buffers
     base = Wm + 2 * K
-    ldr = None
+    ldr = host_frames([(W, H)])[0]
     be = Batch(r, stack_cap=cap, **shape)
     r.reset_stats()
     t0 = time.perf_counter()
     for k in range(args.e2e_steps):
         be.add_job(sid, aid_e, scene.cam, seeds[base + k * E:base + (k + 1) * E], scene.cfg, reset_first=0)
         be.run()
-        ldr = r.tonemap(aid_e)
+        r.tonemap(aid_e, out=ldr)
     e2e_s = time.perf_counter() - t0
     e2e_rays = r.stats()["rays"]
     be.close()
@@ -548,7 +562,7 @@ def run_ours(args, rank, local, ws, dist):
     for k in range(args.e2e_steps):
         r.set_camera(scene.cam)
         r.render(sid, aid, seeds[base + k], reset=0, cfg=scene.cfg)
-        ldr = r.tonemap(aid)
+        r.tonemap(aid, out=ldr)
     e2e_pp_s = time.perf_counter() - t0
     e2e_pp_rays = r.stats()["rays"]
 
@@ -596,10 +610,10 @@ def run_ours(args, rank, local, ws, dist):
                                                  "k_trace_paths<closest> (extend)")},
         "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else 0.0, "unit": METRIC, "passes_per_step": E,
                 "h2d_bytes_per_step": 80 + 4 * E, "d2h_bytes_per_step": W * H * 16, "steps": args.e2e_steps,
-                "path": "yc_batch_add_job + yc_batch_run + yc_tonemap to host"},
+                "path": "yc_batch_add_job + yc_batch_run + yc_tonemap into a page-locked host buffer"},
         "e2e_per_pass": {"value": e2e_pp_rays / e2e_pp_s / 1e6 if e2e_pp_s > 0 else 0.0, "unit": METRIC,
                          "h2d_bytes_per_step": 80 + 4, "d2h_bytes_per_step": W * H * 16, "steps": args.e2e_steps,
-                         "path": "yc_set_camera + yc_render_pass + yc_tonemap to host"},
+                         "path": "yc_set_camera + yc_render_pass + yc_tonemap into a page-locked host buffer"},
         "clocks": clk.summary(),
         "image_error": quality.report(img_en, args.config, int(img_en[0, 0, 3])),
         "stack_overflow": int(st_en["stack_overflow"] + st_pp["stack_overflow"]),
@@ -721,12 +735,13 @@ def run_perpass_bdpt(args, rank, local, ws, dist):
     kt = r.kernel_times()
     r.set_profiling(False)
     # e2e through the C-ABI with host buffers: camera in, tonemapped frame out per step
+    frame = host_frames([(W, H)])[0]
     r.reset_stats()
     t0 = time.perf_counter()
     for k in range(args.e2e_steps):
         r.set_camera(scene.cam)
         r.render(sid, aid, seeds[Wm + K + k], reset=0, cfg=scene.cfg)
-        r.tonemap(aid)
+        r.tonemap(aid, out=frame)
     e2e_s = time.perf_counter() - t0
     e2e_rays = r.stats()["rays"]
     img = r.read_accum(aid)
@@ -767,7 +782,7 @@ def run_perpass_bdpt(args, rank, local, ws, dist):
         "roofline": roof,
         "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else 0.0, "unit": METRIC,
                 "h2d_bytes_per_step": 80 + 4, "d2h_bytes_per_step": W * H * 16, "steps": args.e2e_steps,
-                "path": "yc_set_camera + yc_render_pass + yc_tonemap to host"},
+                "path": "yc_set_camera + yc_render_pass + yc_tonemap into a page-locked host buffer"},
         "clocks": clk.summary(), "stack_overflow": int(st["stack_overflow"]),
         "image_mean": float(np.nanmean(img[..., :3])),
         "image_error": (quality.report(img, args.config, int(img[0, 0, 3]))
@@ -963,23 +978,24 @@ def run_mix(args, rank, local, ws, dist):
         r.free_accum(a)
     # e2e through the C-ABI with host buffers: S steps of E passes of every job
     base = Wm + R * K + 2
+    frames = host_frames([(s.width, s.height) for s in jobs])
     r.reset_stats()
     t0 = time.perf_counter()
     for k in range(S):
         for s, sid, a, sd in zip(jobs, sids, acc_b, seeds):
             b.add_job(sid, a, s.cam, sd[base + k * E:base + (k + 1) * E], cfg, reset_first=0)
         b.run()
-        for a in acc_b:
-            r.tonemap(a)
+        for a, f in zip(acc_b, frames):
+            r.tonemap(a, out=f)
     e2e_s = time.perf_counter() - t0
     e2e_rays = r.stats()["rays"]
     r.reset_stats()
     t0 = time.perf_counter()
     for k in range(S):
-        for s, sid, a, sd in zip(jobs, sids, acc_p, seeds):
+        for s, sid, a, sd, f in zip(jobs, sids, acc_p, seeds, frames):
             r.set_camera(s.cam)
             r.render_passes(sid, a, sd[base + k * E:base + (k + 1) * E], reset_first=0, cfg=cfg)
-            r.tonemap(a)
+            r.tonemap(a, out=f)
     e2e_p_s = time.perf_counter() - t0
     e2e_p_rays = r.stats()["rays"]
     b.close()
@@ -1038,11 +1054,11 @@ def run_mix(args, rank, local, ws, dist):
         "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else 0.0, "unit": METRIC, "passes_per_step": E,
                 "steps": S, "h2d_bytes_per_step": len(jobs) * (80 + 4 * E), "d2h_bytes_per_step": acc_bytes,
                 "path": "per step: yc_batch_add_job (camera, seeds) for every job + yc_batch_run + yc_tonemap of "
-                        "every job to host"},
+                        "every job into its page-locked host buffer"},
         "e2e_plain": {"value": e2e_p_rays / e2e_p_s / 1e6 if e2e_p_s > 0 else 0.0, "unit": METRIC,
                       "passes_per_step": E, "steps": S, "h2d_bytes_per_step": len(jobs) * (80 + 4 * E),
                       "d2h_bytes_per_step": acc_bytes,
-                      "path": "per step and job: yc_set_camera + yc_render_passes + yc_tonemap to host"},
+                      "path": "per step and job: yc_set_camera + yc_render_passes + yc_tonemap into the job's page-locked host buffer"},
         "clocks": clk.summary(),
         "image_error": image_error,
         "host": {"scene_build_s": build_s, "upload_s": upload_s, "autotune_s": tune_s, "autotune_trials": len(trials),

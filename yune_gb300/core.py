@@ -146,9 +146,15 @@ class Renderer:
         img = np.ascontiguousarray(img, np.float32)
         N.check(self.L.yc_write_accum(self.h, aid, ptr(img)), "yc_write_accum")
 
-    def tonemap(self, aid):
+    def tonemap(self, aid, out=None):
+        """The tonemapped frame (yc_tonemap) as a (h, w, 4) float32 array: a new one, or `out`
+        (C-contiguous float32 of that shape, e.g. a page-locked buffer reused frame after
+        frame)."""
         h, w = self._accum_shape[aid]
-        out = np.zeros((h, w, 4), np.float32)
+        if out is None:
+            out = np.zeros((h, w, 4), np.float32)
+        elif out.shape != (h, w, 4) or out.dtype != np.float32 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("tonemap: out must be a C-contiguous float32 array of shape %s" % ((h, w, 4),))
         N.check(self.L.yc_tonemap(self.h, aid, ptr(out)), "yc_tonemap")
         return out
 
