@@ -192,6 +192,12 @@ def test_tonemap_parity(renderer):
     tm = renderer.tonemap(aid)
     ref = O.tonemap(acc)
     assert np.array_equal(tm.view(np.int32), ref.view(np.int32))
+    # into a caller's buffer (reused frame after frame): the same bits; a wrong shape is refused
+    out = np.full((24, 32, 4), np.nan, np.float32)
+    assert renderer.tonemap(aid, out=out) is out
+    assert np.array_equal(out.view(np.int32), ref.view(np.int32))
+    with pytest.raises(ValueError):
+        renderer.tonemap(aid, out=np.zeros((32, 24, 4), np.float32))
 
 
 def test_block_tiling_covers_frame(renderer):
